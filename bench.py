@@ -1,0 +1,334 @@
+#!/usr/bin/env python3
+"""Widom-insertion throughput on GB300 (one JSON line on rank 0).
+
+Workload (default): plain Widom K_H with Ewald -- rigid 3-site CO2 in a 600-atom triclinic
+cell (13.2 / 18.9 / 9.8 Å, β = 102°, Zn:O:C:H = 32:104:192:96, N(0, 0.4) neutralised
+charges) replicated 2x2x3 (7,200 framework sites), 12.5 Å cutoff, Ewald precision 1e-6
+(α = 0.24713 / Å, 1,424 k-vectors), 1e6 insertions in 5 blocks at 298 K, seeded synthetic
+inputs.  A step is one Widom pass over the 1e6 insertions.
+
+  value : insertions/s of pmgb_widom_device on the resident system (CUDA events on the
+          launching stream, L2 flushed before every timed step)
+  e2e   : insertions/s of pmgb.henry_coefficient(...) -- the reference-facing call: host
+          set-up, host->device copies, S(k), the Widom launch and the device->host read
+  --impl reference : the reference's algorithm on the host cores (the FP64 oracle port:
+          direct e^{ik.r} Ewald sum, OpenMP over insertions), bounded samples.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "porousmaterials.jl_gb300"))
+
+METRIC = "Widom insertions/s (+grad) on 1 GB300, batched vs plain, at ≤1e-6 rel KH error"
+UNIT = "insertions/s"
+T = 298.0
+N_BLOCKS = 5
+N_INS = 1_000_000
+# algorithmic flops per pair / k-term (FMA = 2, MUFU = 1, erfc = 10): LJ 28, Ewald real 40, k-term 17
+F_LJ, F_COUL, F_K = 28, 40, 17
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--insertions", type=int, default=N_INS)
+    p.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline leg (profiling runs)")
+    p.add_argument("--skip-e2e", action="store_true", help="omit the end-to-end leg (profiling runs)")
+    return p.parse_args()
+
+
+def workload():
+    import pmgb
+    from pmgb import synthetic
+
+    cr = synthetic.config1()
+    ff = synthetic.forcefield(12.5)
+    rep = pmgb.replication_factors(cr.box, ff)
+    sc = pmgb.replicate(cr, rep)
+    ep = pmgb.setup_Ewald_sum(sc.box, ff.r_cutoff, eps=1e-6)
+    return cr, sc, ff, ep, synthetic.co2(), rep
+
+
+def flops_per_insertion(sc, mol, ep):
+    n_lj = mol.n_atoms * sc.atoms.n
+    n_q = mol.n_charges * sc.charges.n
+    return F_LJ * n_lj + F_COUL * n_q + F_K * mol.n_charges * ep.n_kvecs
+
+
+# ------------------------------------------------------------------ clocks sampling
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.lines: list[str] = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                rows.append((float(parts[0]), float(parts[1]), parts[4:8]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = sorted(r[0] for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[2]) if v.lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ CPU legs
+def cpu_rate(sc, mol, ep, budget_s: float, seed: int = 99, poses=None):
+    """Insertions/s of the FP64 oracle (direct e^{ik.r} form, all host threads) on a bounded
+    sample of the workload's insertions."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import numpy as np
+
+    import oracle
+    from pmgb.molecule import body_offsets
+
+    species = list(dict.fromkeys(list(sc.atoms.species) + list(mol.atom_species)))
+    sid = {s: i for i, s in enumerate(species)}
+    ff_eps, ff_sig2 = _tables
+    o = oracle.OracleSystem(sc.box.f_to_c, sc.atoms.xf, [sid[s] for s in sc.atoms.species], sc.charges.xf,
+                            sc.charges.q, ff_eps, ff_sig2, 12.5 ** 2, [sid[s] for s in mol.atom_species],
+                            mol.charge_q)
+    o.set_ewald(ep.alpha, ep.sr_cutoff_r, ep.kreps, ep.kvec_abc, ep.kvec_wt)
+    cores = oracle.num_threads()
+    rng = np.random.default_rng(seed)
+    ax, qx = body_offsets(mol, sc.box)
+
+    def run(n):
+        xf = rng.random((n, 3))
+        R = np.stack([_rot(rng) for _ in range(n)])
+        lj = xf[:, None, :] + np.einsum("ij,njk,lk->nli", sc.box.c_to_f, R, ax)
+        q = xf[:, None, :] + np.einsum("ij,njk,lk->nli", sc.box.c_to_f, R, qx)
+        t0 = time.perf_counter()
+        o.energies(lj, q, charged=True, use_sk=False)
+        return time.perf_counter() - t0
+
+    n = max(cores, 8)
+    dt = run(n)
+    per = dt / n
+    n2 = max(cores, int(budget_s / max(per, 1e-9)))
+    dt2 = run(n2)
+    return n2 / dt2, cores, n2, dt2
+
+
+def _rot(rng):
+    import pmgb
+
+    return pmgb.random_rotation_matrix(rng)
+
+
+_tables = None
+
+
+def reference_arm(args, rank, world):
+    global _tables
+    if rank != 0:
+        return
+    cr, sc, ff, ep, mol, rep = workload()
+    species = list(dict.fromkeys(list(sc.atoms.species) + list(mol.atom_species)))
+    _tables = ff.tables(species)
+    for _ in range(args.warmup):
+        cpu_rate(sc, mol, ep, budget_s=1.0)
+    rates, times, ns = [], [], []
+    for s in range(args.steps):
+        r, cores, n, dt = cpu_rate(sc, mol, ep, budget_s=8.0, seed=1000 + s)
+        rates.append(r)
+        times.append(dt)
+        ns.append(n)
+    value = sum(ns) / sum(times)
+    sample = (f"{sum(ns)} insertions of the workload (random poses) over {args.steps} steps; FP64 direct "
+              f"e^(ik.r) Ewald sum + LJ, OpenMP over insertions")
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "widom_co2_ewald_600atom_triclinic_2x2x3_1e6", "insertions_per_step": None,
+                      "cpu_sample": True},
+           "impl": "reference",
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+def ours(args, rank, world, local_rank):
+    global _tables
+    import numpy as np
+    import torch
+
+    import pmgb
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    cr, sc, ff, ep, mol, rep = workload()
+    species = list(dict.fromkeys(list(sc.atoms.species) + list(mol.atom_species)))
+    _tables = ff.tables(species)
+    ctx = pmgb.Context(local_rank)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    system = pmgb.GPUSystem(sc, pmgb.Frac(mol, sc.box), ff, ep, ctx=ctx)
+    n_ins = args.insertions
+    npb = n_ins // N_BLOCKS
+    n_ins = npb * N_BLOCKS
+    block_out = torch.zeros(N_BLOCKS * 4, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
+    lib = ctx._lib
+
+    def step(seed):
+        ctx.check(lib.pmgb_widom_device(system.handle, npb, N_BLOCKS, seed, T, block_out.data_ptr(), None))
+
+    fp32_peak = ctx.fp32_peak_tflops() if rank == 0 else None
+    for w in range(args.warmup):
+        step(10_000 + w)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local_rank) as clk:
+        torch.cuda.synchronize()
+        t_wall0 = time.perf_counter()
+        for s in range(args.steps):
+            flush.zero_()
+            starts[s].record(stream)
+            step(s + 1)
+            ends[s].record(stream)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall0
+    ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    ms_total = sum(ms)
+    assert ctx.device_status() == 0
+    blocks = block_out.cpu().numpy().reshape(N_BLOCKS, 4)
+    assert np.all(np.isfinite(blocks[:, 0])), blocks
+
+    # the slowest rank bounds the job
+    t = torch.tensor([ms_total], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * n_ins * args.steps / (ms_max * 1e-3)
+
+    # end to end through the reference-facing call (host buffers, copies inside)
+    e2e = None
+    if not args.skip_e2e:
+        ipv = n_ins / cr.box.Omega
+        e_times = []
+        ctx_default = pmgb.Context.default(local_rank)
+        ctx_default.set_stream(stream.cuda_stream)
+        holder = []
+        for s in range(2 + args.steps):
+            holder.clear()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = pmgb.henry_coefficient(cr, mol, T, ff, insertions_per_volume=ipv, verbose=False, autosave=False,
+                                         seed=500 + s, system_out=holder)
+            t1 = time.perf_counter()
+            if s >= 2:
+                e_times.append(t1 - t0)
+        n_e2e = res.n_insertions_per_block * N_BLOCKS
+        h2d = holder[0].info()["h2d_bytes"] + 0
+        e2e = {"value": n_e2e * len(e_times) / sum(e_times), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": N_BLOCKS * 4 * 8, "call": "pmgb.henry_coefficient (host set-up + "
+               "pmgb_system_create + pmgb_system_set_ewald + pmgb_widom)"}
+
+    if rank != 0:
+        return
+    fpi = flops_per_insertion(sc, mol, ep)
+    achieved = fpi * n_ins / (ms_total / args.steps * 1e-3) / 1e12
+    cpu = None
+    if not args.skip_cpu:
+        r, cores, n, dt = cpu_rate(sc, mol, ep, budget_s=15.0)
+        cpu = {"value": r, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{n} insertions of the workload (random poses), FP64 direct e^(ik.r) Ewald sum + LJ "
+                         f"(the reference's algorithm), OpenMP over insertions, {dt:.1f} s"}
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "widom_co2_ewald_600atom_triclinic_2x2x3_1e6",
+                      "insertions_per_step": n_ins, "framework_sites": sc.atoms.n, "kvectors": ep.n_kvecs,
+                      "guest": "CO2 (3 LJ sites, 3 charges)", "temperature_K": T, "blocks": N_BLOCKS,
+                      "l2": "flushed (256 MB write) before every timed step",
+                      "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+           "gpu_launches": 2 * args.steps,
+           "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                        "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
+                        "peak_source": "in-run FFMA probe (pmgb_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
+                        "flops_per_insertion": fpi,
+                        "kernel": "pairs_kernel<3,true> + reduce_blocks_kernel per step"},
+           "clocks": clk.summary(),
+           "wall_s_timed_region": t_wall,
+           "e2e": e2e,
+           "cpu_baseline": cpu}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    if world > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    try:
+        ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch
+
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,173 @@
+/*
+ * pmgb.h -- C ABI of libpmgb, the GB300 (sm_103a) implementation of the Widom-insertion
+ * Henry-coefficient and potential-energy-grid path of PorousMaterials.jl.
+ *
+ * The reference (PorousMaterials.jl v0.4.2, pure Julia) has no FFI for this path; its
+ * boundary is the exported Julia functions.  Each entry point below names the reference
+ * function it replaces (file:line inside the PorousMaterials.jl source tree).  A Julia
+ * package binds these with `ccall`; Python binds them with ctypes
+ * (porousmaterials.jl_gb300/pmgb/_lib.py).
+ *
+ * Conventions
+ *   - Every function returns PMGB_OK (0) or a negative PMGB_ERR_* code; the message of the
+ *     last failure is available from pmgb_last_error().  Nothing aborts or throws.
+ *   - 3x3 matrices are column-major (Julia layout): m[i + 3*j] = M[i][j].
+ *   - Coordinate arrays are packed xyz triplets: xf[3*k + d].
+ *   - Host buffers are owned by the caller; the library copies in and writes out.
+ *     Device buffers are owned by the context / system handles.
+ *   - A context is not thread-safe: use one context per host thread.  All work of a
+ *     context runs in order on one CUDA stream.
+ *   - Kernel-side failures (a bounded wait that gave up) are reported through a status
+ *     word read back after each synchronous call (PMGB_ERR_DEVICE_STATUS); no kernel traps.
+ */
+#ifndef PMGB_H
+#define PMGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PMGB_ABI_VERSION 1
+
+#define PMGB_OK 0
+#define PMGB_ERR_INVALID_ARGUMENT (-1)
+#define PMGB_ERR_CUDA (-2)
+#define PMGB_ERR_OUT_OF_MEMORY (-3)
+#define PMGB_ERR_DEVICE_STATUS (-4)
+#define PMGB_ERR_UNSUPPORTED (-5)
+#define PMGB_ERR_NOT_READY (-6)
+
+typedef struct pmgb_ctx pmgb_ctx;
+typedef struct pmgb_system pmgb_system;
+
+/* ---- library / context ---------------------------------------------------------- */
+
+/* ABI version of the loaded library (PMGB_ABI_VERSION). */
+int pmgb_abi_version(void);
+
+/* Create a context on CUDA device `device` with its own stream.  No reference
+ * counterpart: the reference runs in Julia worker processes (src/henry.jl:109). */
+int pmgb_create(int device, pmgb_ctx** out);
+void pmgb_destroy(pmgb_ctx* ctx);
+
+/* Message of the last failure on this context ("" if none); NULL ctx gives the last
+ * failure of pmgb_create. */
+const char* pmgb_last_error(const pmgb_ctx* ctx);
+
+/* Run subsequent work on `stream` (a cudaStream_t); NULL restores the context's own stream. */
+int pmgb_set_stream(pmgb_ctx* ctx, void* stream);
+int pmgb_synchronize(pmgb_ctx* ctx);
+
+/* ---- system: replicated crystal + force field + guest molecule ---------------------
+ *
+ * Replaces the state the reference threads through its hot loop: the replicated
+ * `Crystal` (src/henry.jl:80-89; Xtals.replicate), the `LJForceField` tables
+ * (src/forcefield.jl:12-22, ϵ and σ² indexed by species) and the rigid `Molecule`
+ * (src/molecule.jl:10-15, converted to fractional coordinates at src/henry.jl:89).
+ *
+ *   f_to_c            supercell box (columns = lattice vectors, Å)
+ *   atom_xf/species   crystal.atoms: fractional coordinates of the supercell, species id
+ *   charge_xf/q       crystal.charges: fractional coordinates, charges (e)
+ *   epsilon, sigma2   n_species x n_species tables (K, Å²), species ids index both axes
+ *                     (row-major and symmetric: epsilon[a*n_species + b])
+ *   r2_cutoff         LJ cutoff radius squared (ljff.r²_cutoff)
+ *   guest_atom_x      Cartesian offsets of the guest's LJ sites from its centre of mass
+ *   guest_charge_x/q  Cartesian offsets and charges of the guest's point charges
+ * Guest LJ sites and charges at the same offset are merged into one site; at most 8
+ * sites result.  Electrostatics are on iff n_charges > 0 and n_guest_charges > 0
+ * (src/henry.jl:93) and then need pmgb_system_set_ewald. */
+int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9],
+                       int32_t n_atoms, const double* atom_xf, const int32_t* atom_species,
+                       int32_t n_charges, const double* charge_xf, const double* charge_q,
+                       int32_t n_species, const double* epsilon, const double* sigma2,
+                       double r2_cutoff,
+                       int32_t n_guest_atoms, const double* guest_atom_x,
+                       const int32_t* guest_atom_species,
+                       int32_t n_guest_charges, const double* guest_charge_x,
+                       const double* guest_charge_q,
+                       pmgb_system** out);
+
+/* Ewald parameters: EwaldParams (src/electrostatics.jl:54-63) as produced by
+ * setup_Ewald_sum (src/electrostatics.jl:256-272): α, the short-range cutoff, and the
+ * k-vectors (ka, kb, kc) with weights wt (precompute_kvec_wts, :198-232).  The
+ * structure factor S(k) of the framework charges is built on the device here. */
+int pmgb_system_set_ewald(pmgb_system* sys, double alpha, double sr_cutoff,
+                          int32_t n_kvecs, const int32_t* kvec_abc, const double* kvec_wt);
+void pmgb_system_destroy(pmgb_system* sys);
+
+/* Sizes of the device-resident system: out[0..5] = (framework records incl. padding,
+ * species segments, k-vectors, k-rows, guest sites, bytes copied host->device when the
+ * system and its Ewald state were built).  No reference counterpart (diagnostics). */
+int pmgb_system_info(const pmgb_system* sys, int64_t* out6);
+
+/* Number of guest sites and, for each site, the guest atom / guest charge it carries
+ * (-1 when none).  Explicit-coordinate calls take one position per site. */
+int pmgb_system_n_sites(const pmgb_system* sys);
+int pmgb_system_sites(const pmgb_system* sys, int32_t* site_atom, int32_t* site_charge);
+
+/* S(k) = Σ_c q_c e^{ik·r_c} for each k-vector (re, im interleaved; 2*n_kvecs doubles).
+ * The reference evaluates the same sum per guest charge in _ϕ
+ * (src/electrostatics.jl:361-372); exposed for checking. */
+int pmgb_structure_factor(pmgb_system* sys, double* sk_out);
+
+/* ---- single-configuration energies --------------------------------------------------
+ * For n_conf guest configurations given as fractional site coordinates of the supercell
+ * (n_conf x n_sites x 3), out[3*i..3*i+2] = (U_vdw, U_es short-range, U_es long-range) in K.
+ * Replaces vdw_energy(crystal, molecule, ljff) (src/vdw_energetics.jl:62-64 -> 25-47;
+ * +Inf on overlap) and electrostatic_potential_energy(crystal, molecule, eparams, eikr)
+ * (src/electrostatics.jl:331-342 -> _ϕ :347-388; the EwaldSum sr and lr parts). */
+int pmgb_energies(pmgb_system* sys, int64_t n_conf, const double* site_xf, double* out);
+
+/* ---- Widom insertions ----------------------------------------------------------------
+ * Replaces the pmap over N_BLOCKS blocks of _conduct_Widom_insertions
+ * (src/henry.jl:103-113 -> :185-265).  Insertion i (0 <= i < n_blocks*n_per_block)
+ * belongs to block i / n_per_block; its pose is drawn from Philox4x32-10 keyed by
+ * (seed, i): centre of mass uniform in the supercell, uniform random rotation.
+ * block_out[4*b..4*b+3] = (log Σ e^{-U/T}, Σ U_vdw e^{-U/T} / Σ e^{-U/T},
+ *                          Σ U_es e^{-U/T} / Σ e^{-U/T}, number of insertions with U = +Inf)
+ * (the reference's boltzmann_factor_sum and wtd_energy_sum, henry.jl:205-244, in
+ * log-sum-exp form).  u_out (optional, may be NULL) receives (U_vdw, U_es) per insertion. */
+int pmgb_widom(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
+               double temperature, double* block_out, double* u_out);
+
+/* Same computation on device-resident outputs, enqueued on the context stream without
+ * synchronising (block_out_dev: 4*n_blocks doubles, u_out_dev optional). */
+int pmgb_widom_device(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
+                      double temperature, double* block_out_dev, double* u_out_dev);
+
+/* Poses the Widom kernel uses for insertions start .. start+n-1: xf_out (n x 3, centre of
+ * mass, supercell fractional) and rot_out (n x 9, column-major rotation applied to the
+ * Cartesian site offsets).  Replaces rand(3) + random_rotation! (src/henry.jl:214-220,
+ * src/molecule.jl:233-281). */
+int pmgb_sample_poses(pmgb_ctx* ctx, uint64_t seed, int64_t start, int64_t n,
+                      float* xf_out, float* rot_out);
+
+/* ---- energy grid -----------------------------------------------------------------------
+ * Replaces energy_grid(crystal, molecule, ljff; resolution=(n1,n2,n3)) for single-site
+ * probes (src/grid.jl:291-362): point (i,j,k) sits at (i/(n1-1), j/(n2-1), k/(n3-1)) of
+ * the unit cell, i.e. that divided by repfactors in the supercell this system holds;
+ * out[i + n1*(j + n2*k)] = U_vdw * unit_factor (1 for K, 8.314/1000 for kJ/mol). */
+int pmgb_energy_grid(pmgb_system* sys, const int32_t n_pts[3], const int32_t repfactors[3],
+                     double unit_factor, float* out);
+int pmgb_energy_grid_device(pmgb_system* sys, const int32_t n_pts[3], const int32_t repfactors[3],
+                            double unit_factor, float* out_dev);
+
+/* ---- utilities -------------------------------------------------------------------------- */
+
+/* Philox4x32-10 of n (counter[4], key[2]) pairs, for checking the generator bit for bit. */
+int pmgb_philox4x32_10(pmgb_ctx* ctx, int64_t n, const uint32_t* ctr, const uint32_t* key,
+                       uint32_t* out);
+
+/* FP32 FMA throughput probe: runs n_ctas x 256 threads x iters x 128 FMAs and returns the
+ * measured TFLOP/s (the roofline denominator of the pair kernels). */
+int pmgb_fp32_peak(pmgb_ctx* ctx, int n_ctas, int iters, double* tflops_out);
+
+/* Read and clear the device status word (0 = no kernel-side failure). */
+int pmgb_device_status(pmgb_ctx* ctx, uint32_t* status_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PMGB_H */

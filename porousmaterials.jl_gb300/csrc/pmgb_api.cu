@@ -1,0 +1,835 @@
+// pmgb_api.cu -- the extern "C" boundary of libpmgb (declared in include/pmgb.h).
+//
+// Host-side preparation of a system: wrap and species-sort the replicated framework
+// into padded float4 segments, merge framework charges onto LJ sites that share their
+// coordinates, merge guest LJ sites and charges, build per (segment, site) LJ
+// parameters, group Ewald k-vectors into kc rows; then launches and status checks.
+#include "pmgb.h"
+#include "pmgb_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_create_error;
+
+constexpr double kPi = 3.14159265358979323846;
+
+// 1/(4 pi eps0) with eps0 in e^2/(A K), following src/electrostatics.jl:6-7.
+double coulomb_constant() {
+    const double qe = 1.602176565e-19;
+    const double eps0 = 8.854187817e-12 / (qe * qe) / 1.0e10 * 1.3806488e-23;
+    return 1.0 / (4.0 * kPi * eps0);
+}
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t n = 0;
+};
+
+}  // namespace
+
+struct pmgb_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    unsigned int* d_status = nullptr;
+    std::string err;
+};
+
+struct pmgb_system {
+    pmgb_ctx* ctx = nullptr;
+    SysDev dev{};
+    // device allocations
+    float4* d_rec = nullptr;
+    SegDesc* d_seg = nullptr;
+    SitePar* d_segpar = nullptr;
+    uint32_t* d_qfix = nullptr;
+    double* d_q = nullptr;
+    int n_q = 0;
+    KRow* d_krow = nullptr;
+    float2* d_skw = nullptr;
+    double* d_sk = nullptr;
+    int* d_kabc = nullptr;
+    double* d_wt = nullptr;
+    int n_k = 0;
+    bool ewald_set = false;
+    int n_sites = 0;
+    int64_t h2d_bytes = 0;
+    int site_atom[PMGB_MAX_SITES];
+    int site_charge[PMGB_MAX_SITES];
+    // grow-only scratch used by launches
+    DevBuf partials, block_out, in_buf, out_buf, axes;
+};
+
+namespace {
+
+int fail(pmgb_ctx* ctx, int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (ctx) ctx->err = buf;
+    else g_create_error = buf;
+    return code;
+}
+
+int cuda_fail(pmgb_ctx* ctx, cudaError_t e, const char* what) {
+    const int code = (e == cudaErrorMemoryAllocation) ? PMGB_ERR_OUT_OF_MEMORY : PMGB_ERR_CUDA;
+    return fail(ctx, code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define PMGB_CK(ctx, call)                                        \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call); \
+    } while (0)
+
+int ensure(pmgb_ctx* ctx, DevBuf& b, size_t bytes) {
+    if (bytes <= b.n) return PMGB_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.n = 0;
+    const size_t want = std::max<size_t>(bytes, 256);
+    PMGB_CK(ctx, cudaMalloc(&b.p, want));
+    b.n = want;
+    return PMGB_OK;
+}
+
+template <class T>
+int upload(pmgb_ctx* ctx, T** dst, const std::vector<T>& v, int64_t* counter = nullptr) {
+    *dst = nullptr;
+    if (counter) *counter += static_cast<int64_t>(v.size() * sizeof(T));
+    const size_t bytes = std::max<size_t>(v.size() * sizeof(T), 16);
+    PMGB_CK(ctx, cudaMalloc(reinterpret_cast<void**>(dst), bytes));
+    if (!v.empty())
+        PMGB_CK(ctx, cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    return PMGB_OK;
+}
+
+// Read back and clear the device status word; synchronises the stream.
+int check_status(pmgb_ctx* ctx) {
+    unsigned int st = 0;
+    PMGB_CK(ctx, cudaMemcpyAsync(&st, ctx->d_status, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (st != 0) {
+        PMGB_CK(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(unsigned int), ctx->stream));
+        PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        return fail(ctx, PMGB_ERR_DEVICE_STATUS, "kernel reported status 0x%x (%s)", st,
+                    (st & PMGB_DEVERR_TMA_TIMEOUT) ? "shared-memory staging wait gave up" : "bad arguments");
+    }
+    return PMGB_OK;
+}
+
+bool finite3(const double* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+
+double wrap01(double x) {
+    double y = x - std::floor(x);
+    if (y >= 1.0) y = 0.0;  // x - floor(x) can round up to 1 for tiny negative x
+    return y;
+}
+
+// 3x3 helpers on column-major matrices
+void inv_upper(const double R[9], double out[9]) {
+    // R upper-triangular: R(i,j) = R[i + 3j], zero below the diagonal
+    for (int k = 0; k < 9; ++k) out[k] = 0.0;
+    const double a = R[0], b = R[3], c = R[6], d = R[4], e = R[7], f = R[8];
+    out[0] = 1.0 / a;
+    out[4] = 1.0 / d;
+    out[8] = 1.0 / f;
+    out[3] = -b / (a * d);
+    out[7] = -e / (d * f);
+    out[6] = (b * e - c * d) / (a * d * f);
+}
+
+// Upper-triangular R with R^T R = H^T H (Cholesky of the metric) and Q = H R^-1, so that
+// |H d| = |R d| for every fractional d; Q^T maps Cartesian offsets into R's frame.
+bool upper_factor(const double H[9], double R[9], double Q[9]) {
+    double G[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            G[i + 3 * j] = H[3 * i] * H[3 * j] + H[3 * i + 1] * H[3 * j + 1] + H[3 * i + 2] * H[3 * j + 2];
+    for (int k = 0; k < 9; ++k) R[k] = 0.0;
+    if (G[0] <= 0.0) return false;
+    R[0] = std::sqrt(G[0]);
+    R[3] = G[3] / R[0];
+    R[6] = G[6] / R[0];
+    const double d11 = G[4] - R[3] * R[3];
+    if (d11 <= 0.0) return false;
+    R[4] = std::sqrt(d11);
+    R[7] = (G[7] - R[3] * R[6]) / R[4];
+    const double d22 = G[8] - R[6] * R[6] - R[7] * R[7];
+    if (d22 <= 0.0) return false;
+    R[8] = std::sqrt(d22);
+    double Ri[9];
+    inv_upper(R, Ri);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            Q[i + 3 * j] = H[i] * Ri[3 * j] + H[i + 3] * Ri[3 * j + 1] + H[i + 6] * Ri[3 * j + 2];
+    return true;
+}
+
+using Key3 = std::tuple<double, double, double>;
+
+}  // namespace
+
+// ============================================================================
+// library / context
+// ============================================================================
+extern "C" int pmgb_abi_version(void) { return PMGB_ABI_VERSION; }
+
+extern "C" int pmgb_create(int device, pmgb_ctx** out) {
+    if (!out) return fail(nullptr, PMGB_ERR_INVALID_ARGUMENT, "pmgb_create: out is NULL");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        return fail(nullptr, PMGB_ERR_CUDA, "pmgb_create: no CUDA device (%s)", cudaGetErrorString(e));
+    if (device < 0 || device >= n)
+        return fail(nullptr, PMGB_ERR_INVALID_ARGUMENT, "pmgb_create: device %d out of range [0, %d)", device, n);
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fail(nullptr, PMGB_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, device);
+    if (prop.major < 10)
+        return fail(nullptr, PMGB_ERR_UNSUPPORTED, "pmgb_create: device %d is sm_%d%d; this build targets sm_103a",
+                    device, prop.major, prop.minor);
+    pmgb_ctx* c = new pmgb_ctx();
+    c->device = device;
+    e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(unsigned int));
+    if (e != cudaSuccess) {
+        if (c->d_status) cudaFree(c->d_status);
+        if (c->own_stream) cudaStreamDestroy(c->own_stream);
+        delete c;
+        return fail(nullptr, PMGB_ERR_CUDA, "pmgb_create: %s", cudaGetErrorString(e));
+    }
+    c->stream = c->own_stream;
+    *out = c;
+    return PMGB_OK;
+}
+
+extern "C" void pmgb_destroy(pmgb_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->d_status) cudaFree(ctx->d_status);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+extern "C" const char* pmgb_last_error(const pmgb_ctx* ctx) {
+    return ctx ? ctx->err.c_str() : g_create_error.c_str();
+}
+
+extern "C" int pmgb_set_stream(pmgb_ctx* ctx, void* stream) {
+    if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
+    ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_synchronize(pmgb_ctx* ctx) {
+    if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_device_status(pmgb_ctx* ctx, uint32_t* status_out) {
+    if (!ctx || !status_out) return PMGB_ERR_INVALID_ARGUMENT;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    unsigned int st = 0;
+    PMGB_CK(ctx, cudaMemcpyAsync(&st, ctx->d_status, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream));
+    PMGB_CK(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(unsigned int), ctx->stream));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    *status_out = st;
+    return PMGB_OK;
+}
+
+// ============================================================================
+// system
+// ============================================================================
+static void free_system_device(pmgb_system* s) {
+    void* ptrs[] = {s->d_rec, s->d_seg, s->d_segpar, s->d_qfix, s->d_q, s->d_krow, s->d_skw, s->d_sk,
+                    s->d_kabc, s->d_wt, s->partials.p, s->block_out.p, s->in_buf.p, s->out_buf.p, s->axes.p};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+}
+
+extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t n_atoms, const double* atom_xf,
+                                  const int32_t* atom_species, int32_t n_charges, const double* charge_xf,
+                                  const double* charge_q, int32_t n_species, const double* epsilon,
+                                  const double* sigma2, double r2_cutoff, int32_t n_guest_atoms,
+                                  const double* guest_atom_x, const int32_t* guest_atom_species,
+                                  int32_t n_guest_charges, const double* guest_charge_x,
+                                  const double* guest_charge_q, pmgb_system** out) {
+    if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
+    if (!out) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_system_create: out is NULL");
+    *out = nullptr;
+    if (!f_to_c) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_system_create: f_to_c is NULL");
+    for (int k = 0; k < 9; ++k)
+        if (!std::isfinite(f_to_c[k])) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "f_to_c has a non-finite entry");
+    if (n_atoms < 0 || n_charges < 0 || n_guest_atoms < 0 || n_guest_charges < 0 || n_species < 0)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "negative count");
+    if ((n_atoms > 0 && (!atom_xf || !atom_species)) || (n_charges > 0 && (!charge_xf || !charge_q)) ||
+        (n_guest_atoms > 0 && (!guest_atom_x || !guest_atom_species)) ||
+        (n_guest_charges > 0 && (!guest_charge_x || !guest_charge_q)) ||
+        (n_species > 0 && (!epsilon || !sigma2)))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "NULL array with a nonzero count");
+    if (!(r2_cutoff > 0.0) || !std::isfinite(r2_cutoff))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "r2_cutoff must be positive and finite (got %g)", r2_cutoff);
+    if (n_guest_atoms + n_guest_charges == 0)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "guest has no atoms and no charges");
+    for (int i = 0; i < n_atoms; ++i) {
+        if (atom_species[i] < 0 || atom_species[i] >= n_species)
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "framework atom %d: species id %d not in [0, %d)", i,
+                        atom_species[i], n_species);
+        if (!finite3(atom_xf + 3 * i))
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "framework atom %d has a non-finite coordinate", i);
+    }
+    for (int i = 0; i < n_charges; ++i)
+        if (!finite3(charge_xf + 3 * i) || !std::isfinite(charge_q[i]))
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "framework charge %d is not finite", i);
+    for (int i = 0; i < n_guest_atoms; ++i) {
+        if (guest_atom_species[i] < 0 || guest_atom_species[i] >= n_species)
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "guest atom %d: species id %d not in [0, %d)", i,
+                        guest_atom_species[i], n_species);
+        if (!finite3(guest_atom_x + 3 * i))
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "guest atom %d has a non-finite coordinate", i);
+    }
+    for (int i = 0; i < n_guest_charges; ++i)
+        if (!finite3(guest_charge_x + 3 * i) || !std::isfinite(guest_charge_q[i]))
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "guest charge %d is not finite", i);
+    for (int k = 0; k < n_species * n_species; ++k)
+        if (!std::isfinite(epsilon[k]) || !std::isfinite(sigma2[k]))
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "force-field table entry %d is not finite", k);
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+
+    // ---- box: upper-triangular factor --------------------------------------------
+    double R[9], Q[9], G[9];
+    const double scale = std::max({std::fabs(f_to_c[0]), std::fabs(f_to_c[4]), std::fabs(f_to_c[8])});
+    const bool upper = std::fabs(f_to_c[1]) <= 1e-12 * scale && std::fabs(f_to_c[2]) <= 1e-12 * scale &&
+                       std::fabs(f_to_c[5]) <= 1e-12 * scale && f_to_c[0] > 0 && f_to_c[4] > 0 && f_to_c[8] > 0;
+    if (upper) {
+        for (int k = 0; k < 9; ++k) R[k] = f_to_c[k];
+        R[1] = R[2] = R[5] = 0.0;
+        for (int k = 0; k < 9; ++k) Q[k] = (k % 4 == 0) ? 1.0 : 0.0;
+    } else if (!upper_factor(f_to_c, R, Q)) {
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "f_to_c is singular");
+    }
+    inv_upper(R, G);
+
+    // ---- framework records ---------------------------------------------------------
+    struct Rec {
+        double x, y, z, q;
+        int species;  // -1: charge-only
+    };
+    std::vector<Rec> recs;
+    recs.reserve(n_atoms + n_charges);
+    std::map<Key3, int> at_pos;
+    for (int i = 0; i < n_atoms; ++i) {
+        Rec r{wrap01(atom_xf[3 * i]), wrap01(atom_xf[3 * i + 1]), wrap01(atom_xf[3 * i + 2]), 0.0, atom_species[i]};
+        at_pos.emplace(Key3(r.x, r.y, r.z), static_cast<int>(recs.size()));
+        recs.push_back(r);
+    }
+    std::vector<char> taken(recs.size(), 0);
+    for (int c = 0; c < n_charges; ++c) {
+        const Key3 key(wrap01(charge_xf[3 * c]), wrap01(charge_xf[3 * c + 1]), wrap01(charge_xf[3 * c + 2]));
+        auto it = at_pos.find(key);
+        if (it != at_pos.end() && !taken[it->second]) {
+            recs[it->second].q = charge_q[c];
+            taken[it->second] = 1;
+        } else {
+            recs.push_back(Rec{std::get<0>(key), std::get<1>(key), std::get<2>(key), charge_q[c], -1});
+        }
+    }
+    // species-sorted segments, each padded with NaN records to PMGB_SEG_ALIGN
+    std::vector<int> order(recs.size());
+    for (size_t i = 0; i < recs.size(); ++i) order[i] = static_cast<int>(i);
+    auto sp_key = [&](int i) { return recs[i].species < 0 ? n_species : recs[i].species; };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sp_key(a) < sp_key(b); });
+    std::vector<float4> h_rec;
+    std::vector<SegDesc> h_seg;
+    const float qnan = std::nanf("");
+    for (size_t p = 0; p < order.size();) {
+        const int sp = recs[order[p]].species;
+        size_t e = p;
+        while (e < order.size() && recs[order[e]].species == sp) ++e;
+        SegDesc d{};
+        d.lo = static_cast<int>(h_rec.size());
+        for (size_t k = p; k < e; ++k) {
+            const Rec& r = recs[order[k]];
+            h_rec.push_back(make_float4(static_cast<float>(r.x), static_cast<float>(r.y), static_cast<float>(r.z),
+                                        static_cast<float>(r.q)));
+        }
+        while (h_rec.size() % PMGB_SEG_ALIGN) h_rec.push_back(make_float4(qnan, qnan, qnan, 0.0f));
+        d.hi = static_cast<int>(h_rec.size());
+        d.species = sp;
+        d.has_lj = sp >= 0;
+        h_seg.push_back(d);
+        p = e;
+    }
+    if (h_seg.size() > PMGB_MAX_SEG)
+        return fail(ctx, PMGB_ERR_UNSUPPORTED, "framework has %zu species segments (max %d)", h_seg.size(),
+                    PMGB_MAX_SEG);
+
+    // ---- guest sites: merge LJ atoms and charges sharing an offset -------------------
+    pmgb_system* s = new pmgb_system();
+    s->ctx = ctx;
+    double body[PMGB_MAX_SITES][3];
+    double sq[PMGB_MAX_SITES];
+    int ns = 0;
+    for (int i = 0; i < n_guest_atoms; ++i) {
+        if (ns >= PMGB_MAX_SITES) {
+            delete s;
+            return fail(ctx, PMGB_ERR_UNSUPPORTED, "guest has more than %d sites", PMGB_MAX_SITES);
+        }
+        for (int d = 0; d < 3; ++d) body[ns][d] = guest_atom_x[3 * i + d];
+        s->site_atom[ns] = i;
+        s->site_charge[ns] = -1;
+        sq[ns] = 0.0;
+        ++ns;
+    }
+    for (int c = 0; c < n_guest_charges; ++c) {
+        int hit = -1;
+        for (int k = 0; k < ns; ++k) {
+            if (s->site_charge[k] >= 0) continue;
+            const double dd = std::fabs(body[k][0] - guest_charge_x[3 * c]) +
+                              std::fabs(body[k][1] - guest_charge_x[3 * c + 1]) +
+                              std::fabs(body[k][2] - guest_charge_x[3 * c + 2]);
+            if (dd <= 1e-12) {
+                hit = k;
+                break;
+            }
+        }
+        if (hit < 0) {
+            if (ns >= PMGB_MAX_SITES) {
+                delete s;
+                return fail(ctx, PMGB_ERR_UNSUPPORTED, "guest has more than %d sites", PMGB_MAX_SITES);
+            }
+            hit = ns++;
+            for (int d = 0; d < 3; ++d) body[hit][d] = guest_charge_x[3 * c + d];
+            s->site_atom[hit] = -1;
+        }
+        s->site_charge[hit] = c;
+        sq[hit] = guest_charge_q[c];
+    }
+    s->n_sites = ns;
+
+    // per (segment, site) LJ parameters
+    std::vector<SitePar> h_par(h_seg.size() * PMGB_MAX_SITES, SitePar{1.0f, 0.0f, -1.0f, 0.0f});
+    for (size_t g = 0; g < h_seg.size(); ++g)
+        for (int k = 0; k < ns; ++k) {
+            const int a = s->site_atom[k];
+            const int fs = h_seg[g].species;
+            if (a < 0 || fs < 0) continue;
+            const int gs = guest_atom_species[a];
+            SitePar& p = h_par[g * PMGB_MAX_SITES + k];
+            p.sig2 = static_cast<float>(sigma2[gs * n_species + fs]);
+            p.eps4 = static_cast<float>(4.0 * epsilon[gs * n_species + fs]);
+            p.r2ovl = 0.1f;  // R²_OVERLAP, src/vdw_energetics.jl:2
+        }
+
+    // charge fixed-point coordinates for S(k)
+    std::vector<uint32_t> h_qfix;
+    std::vector<double> h_q;
+    for (int c = 0; c < n_charges; ++c) {
+        for (int d = 0; d < 3; ++d) {
+            const double u = wrap01(charge_xf[3 * c + d]);
+            h_qfix.push_back(static_cast<uint32_t>(static_cast<uint64_t>(std::llround(u * 4294967296.0)) & 0xffffffffull));
+        }
+        h_q.push_back(charge_q[c]);
+    }
+    s->n_q = n_charges;
+
+    int rc = PMGB_OK;
+    int64_t* nb = &s->h2d_bytes;
+    if ((rc = upload(ctx, &s->d_rec, h_rec, nb)) || (rc = upload(ctx, &s->d_seg, h_seg, nb)) ||
+        (rc = upload(ctx, &s->d_segpar, h_par, nb)) || (rc = upload(ctx, &s->d_qfix, h_qfix, nb)) ||
+        (rc = upload(ctx, &s->d_q, h_q, nb))) {
+        free_system_device(s);
+        delete s;
+        return rc;
+    }
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        free_system_device(s);
+        delete s;
+        return cuda_fail(ctx, e, "pmgb_system_create upload");
+    }
+
+    SysDev& D = s->dev;
+    D.rec = s->d_rec;
+    D.n_rec = static_cast<int>(h_rec.size());
+    D.n_tiles = (D.n_rec + PMGB_TILE - 1) / PMGB_TILE;
+    D.n_seg = static_cast<int>(h_seg.size());
+    D.seg = s->d_seg;
+    D.segpar = s->d_segpar;
+    D.h00 = static_cast<float>(R[0]);
+    D.h01 = static_cast<float>(R[3]);
+    D.h02 = static_cast<float>(R[6]);
+    D.h11 = static_cast<float>(R[4]);
+    D.h12 = static_cast<float>(R[7]);
+    D.h22 = static_cast<float>(R[8]);
+    D.g00 = static_cast<float>(G[0]);
+    D.g01 = static_cast<float>(G[3]);
+    D.g02 = static_cast<float>(G[6]);
+    D.g11 = static_cast<float>(G[4]);
+    D.g12 = static_cast<float>(G[7]);
+    D.g22 = static_cast<float>(G[8]);
+    D.rc2 = static_cast<float>(r2_cutoff);
+    D.rc2e = static_cast<float>(r2_cutoff);
+    D.alpha = 0.0f;
+    D.coul = coulomb_constant();
+    D.charged = (n_charges > 0 && n_guest_charges > 0) ? 1 : 0;
+    D.n_sites = ns;
+    for (int k = 0; k < PMGB_MAX_SITES; ++k) {
+        // offsets rotated into the frame of the upper-triangular box (Q^T b)
+        for (int d = 0; d < 3; ++d) {
+            double v = 0.0;
+            if (k < ns)
+                for (int m = 0; m < 3; ++m) v += Q[m + 3 * d] * body[k][m];
+            D.body[k][d] = static_cast<float>(v);
+        }
+        D.q[k] = (k < ns) ? static_cast<float>(sq[k]) : 0.0f;
+    }
+    D.n_krow = 0;
+    D.n_k = 0;
+    D.krow = nullptr;
+    D.skw = nullptr;
+    *out = s;
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cutoff, int32_t n_kvecs,
+                                     const int32_t* kvec_abc, const double* kvec_wt) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (!(alpha > 0.0) || !std::isfinite(alpha) || !(sr_cutoff > 0.0) || !std::isfinite(sr_cutoff))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "Ewald alpha and sr_cutoff must be positive and finite");
+    if (n_kvecs < 0 || (n_kvecs > 0 && (!kvec_abc || !kvec_wt)))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "bad k-vector arrays");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    std::vector<KRow> rows;
+    std::vector<int> kabc(kvec_abc, kvec_abc + 3 * static_cast<size_t>(n_kvecs));
+    std::vector<double> wt(kvec_wt, kvec_wt + n_kvecs);
+    for (int k = 0; k < n_kvecs; ++k) {
+        if (!std::isfinite(wt[k])) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "k-vector %d weight not finite", k);
+        const int ka = kabc[3 * k], kb = kabc[3 * k + 1], kc = kabc[3 * k + 2];
+        if (!rows.empty()) {
+            KRow& r = rows.back();
+            if (r.ka == ka && r.kb == kb && r.kc0 + r.n == kc) {
+                ++r.n;
+                continue;
+            }
+        }
+        rows.push_back(KRow{ka, kb, kc, 1, k, 0, 0, 0});
+    }
+    // drop previous Ewald state
+    void* old[] = {s->d_krow, s->d_skw, s->d_sk, s->d_kabc, s->d_wt};
+    for (void* p : old)
+        if (p) cudaFree(p);
+    s->d_krow = nullptr;
+    s->d_skw = nullptr;
+    s->d_sk = nullptr;
+    s->d_kabc = nullptr;
+    s->d_wt = nullptr;
+    int rc;
+    if ((rc = upload(ctx, &s->d_krow, rows, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_kabc, kabc, &s->h2d_bytes)) ||
+        (rc = upload(ctx, &s->d_wt, wt, &s->h2d_bytes)))
+        return rc;
+    PMGB_CK(ctx, cudaMalloc(&s->d_skw, std::max<size_t>(sizeof(float2) * n_kvecs, 16)));
+    PMGB_CK(ctx, cudaMalloc(&s->d_sk, std::max<size_t>(2 * sizeof(double) * n_kvecs, 16)));
+    PMGB_CK(ctx, pmgb_launch_structure_factor(s->d_qfix, s->d_q, s->n_q, s->d_kabc, s->d_wt, n_kvecs, s->d_sk,
+                                              s->d_skw, ctx->stream));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    s->n_k = n_kvecs;
+    s->ewald_set = true;
+    s->dev.alpha = static_cast<float>(alpha);
+    s->dev.rc2e = static_cast<float>(sr_cutoff * sr_cutoff);
+    s->dev.n_krow = static_cast<int>(rows.size());
+    s->dev.n_k = n_kvecs;
+    s->dev.krow = s->d_krow;
+    s->dev.skw = s->d_skw;
+    return PMGB_OK;
+}
+
+extern "C" void pmgb_system_destroy(pmgb_system* s) {
+    if (!s) return;
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    free_system_device(s);
+    delete s;
+}
+
+extern "C" int pmgb_system_info(const pmgb_system* s, int64_t* out6) {
+    if (!s || !out6) return PMGB_ERR_INVALID_ARGUMENT;
+    out6[0] = s->dev.n_rec;
+    out6[1] = s->dev.n_seg;
+    out6[2] = s->n_k;
+    out6[3] = s->dev.n_krow;
+    out6[4] = s->n_sites;
+    out6[5] = s->h2d_bytes;
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_system_n_sites(const pmgb_system* s) { return s ? s->n_sites : PMGB_ERR_INVALID_ARGUMENT; }
+
+extern "C" int pmgb_system_sites(const pmgb_system* s, int32_t* site_atom, int32_t* site_charge) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    for (int k = 0; k < s->n_sites; ++k) {
+        if (site_atom) site_atom[k] = s->site_atom[k];
+        if (site_charge) site_charge[k] = s->site_charge[k];
+    }
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_structure_factor(pmgb_system* s, double* sk_out) {
+    if (!s || !sk_out) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (!s->ewald_set) return fail(ctx, PMGB_ERR_NOT_READY, "pmgb_structure_factor: Ewald parameters not set");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    if (s->n_k > 0)
+        PMGB_CK(ctx, cudaMemcpyAsync(sk_out, s->d_sk, 2 * sizeof(double) * s->n_k, cudaMemcpyDeviceToHost, ctx->stream));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return PMGB_OK;
+}
+
+// ============================================================================
+// launches
+// ============================================================================
+static int ready_for_charges(pmgb_system* s) {
+    if (s->dev.charged && !s->ewald_set)
+        return fail(s->ctx, PMGB_ERR_NOT_READY,
+                    "framework and guest are charged: call pmgb_system_set_ewald before evaluating energies");
+    return PMGB_OK;
+}
+
+static LaunchArgs base_args(pmgb_system* s) {
+    LaunchArgs a{};
+    a.sys = s->dev;
+    a.status = s->ctx->d_status;
+    return a;
+}
+
+extern "C" int pmgb_energies(pmgb_system* s, int64_t n_conf, const double* site_xf, double* out) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (n_conf < 0 || (n_conf > 0 && (!site_xf || !out)))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energies: bad arguments");
+    if (int rc = ready_for_charges(s)) return rc;
+    if (n_conf == 0) return PMGB_OK;
+    if (n_conf > (int64_t(1) << 31) * PMGB_THREADS / 2)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energies: n_conf too large");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    const size_t in_bytes = sizeof(double) * 3 * s->n_sites * static_cast<size_t>(n_conf);
+    const size_t out_bytes = sizeof(double) * 3 * static_cast<size_t>(n_conf);
+    int rc;
+    if ((rc = ensure(ctx, s->in_buf, in_bytes)) || (rc = ensure(ctx, s->out_buf, out_bytes))) return rc;
+    PMGB_CK(ctx, cudaMemcpyAsync(s->in_buf.p, site_xf, in_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    LaunchArgs a = base_args(s);
+    a.pose_mode = POSE_SITES;
+    a.out_mode = OUT_ENERGY;
+    a.site_xf = static_cast<const double*>(s->in_buf.p);
+    a.n_conf = n_conf;
+    a.e_out = static_cast<double*>(s->out_buf.p);
+    const int n_ctas = static_cast<int>((n_conf + PMGB_THREADS - 1) / PMGB_THREADS);
+    PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
+    PMGB_CK(ctx, cudaMemcpyAsync(out, s->out_buf.p, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_status(ctx);
+}
+
+extern "C" int pmgb_widom_device(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
+                                 double temperature, double* block_out_dev, double* u_out_dev) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (n_per_block < 1 || n_blocks < 1 || !block_out_dev)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom: need n_per_block >= 1, n_blocks >= 1, block_out");
+    if (!(temperature > 0.0) || !std::isfinite(temperature))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom: temperature must be positive (got %g)", temperature);
+    if (int rc = ready_for_charges(s)) return rc;
+    const int64_t cpb = (n_per_block + PMGB_THREADS - 1) / PMGB_THREADS;
+    if (cpb * n_blocks > INT32_MAX)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom: too many insertions for one launch");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    const int n_ctas = static_cast<int>(cpb * n_blocks);
+    if (int rc = ensure(ctx, s->partials, sizeof(LsePartial) * n_ctas)) return rc;
+    LaunchArgs a = base_args(s);
+    a.pose_mode = POSE_PHILOX;
+    a.out_mode = OUT_WIDOM;
+    a.seed = seed;
+    a.n_per_block = n_per_block;
+    a.n_blocks = n_blocks;
+    a.ctas_per_block = static_cast<int>(cpb);
+    a.inv_temperature = 1.0 / temperature;
+    a.partials = static_cast<LsePartial*>(s->partials.p);
+    a.u_out = u_out_dev;
+    PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
+    PMGB_CK(ctx, pmgb_launch_reduce_blocks(a.partials, n_blocks, a.ctas_per_block, block_out_dev, ctx->stream));
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_widom(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uint64_t seed, double temperature,
+                          double* block_out, double* u_out) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (!block_out) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom: block_out is NULL");
+    if (n_per_block < 1 || n_blocks < 1)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom: need n_per_block >= 1 and n_blocks >= 1");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    int rc;
+    if ((rc = ensure(ctx, s->block_out, sizeof(double) * 4 * n_blocks))) return rc;
+    const size_t u_bytes = u_out ? sizeof(double) * 2 * static_cast<size_t>(n_per_block) * n_blocks : 0;
+    if (u_out && (rc = ensure(ctx, s->out_buf, u_bytes))) return rc;
+    rc = pmgb_widom_device(s, n_per_block, n_blocks, seed, temperature, static_cast<double*>(s->block_out.p),
+                           u_out ? static_cast<double*>(s->out_buf.p) : nullptr);
+    if (rc) return rc;
+    PMGB_CK(ctx, cudaMemcpyAsync(block_out, s->block_out.p, sizeof(double) * 4 * n_blocks, cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    if (u_out) PMGB_CK(ctx, cudaMemcpyAsync(u_out, s->out_buf.p, u_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_status(ctx);
+}
+
+extern "C" int pmgb_sample_poses(pmgb_ctx* ctx, uint64_t seed, int64_t start, int64_t n, float* xf_out,
+                                 float* rot_out) {
+    if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
+    if (n < 0 || start < 0 || (n > 0 && (!xf_out || !rot_out)))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_sample_poses: bad arguments");
+    if (n == 0) return PMGB_OK;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    float *dx = nullptr, *dr = nullptr;
+    PMGB_CK(ctx, cudaMalloc(&dx, sizeof(float) * 3 * n));
+    cudaError_t e = cudaMalloc(&dr, sizeof(float) * 9 * n);
+    if (e == cudaSuccess) e = pmgb_launch_sample_poses(seed, start, n, dx, dr, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(xf_out, dx, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rot_out, dr, sizeof(float) * 9 * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(dx);
+    if (dr) cudaFree(dr);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "pmgb_sample_poses");
+    return PMGB_OK;
+}
+
+static int grid_axes(pmgb_system* s, const int32_t n_pts[3], const int32_t rep[3]) {
+    pmgb_ctx* ctx = s->ctx;
+    std::vector<float> ax;
+    for (int d = 0; d < 3; ++d)
+        for (int i = 0; i < n_pts[d]; ++i) {
+            double f = (n_pts[d] > 1) ? static_cast<double>(i) / static_cast<double>(n_pts[d] - 1) : 0.0;
+            // the end plane (f = 1) is the periodic image of the first one: evaluate the
+            // identical position so both planes hold bit-identical energies
+            if (f >= 1.0) f -= 1.0;
+            ax.push_back(static_cast<float>(f / rep[d]));
+        }
+    if (int rc = ensure(ctx, s->axes, sizeof(float) * ax.size())) return rc;
+    PMGB_CK(ctx, cudaMemcpyAsync(s->axes.p, ax.data(), sizeof(float) * ax.size(), cudaMemcpyHostToDevice, ctx->stream));
+    // the staging vector is released on return: make the copy complete first
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_energy_grid_device(pmgb_system* s, const int32_t n_pts[3], const int32_t repfactors[3],
+                                       double unit_factor, float* out_dev) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (!n_pts || !repfactors || !out_dev)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid: NULL argument");
+    for (int d = 0; d < 3; ++d)
+        if (n_pts[d] < 1 || repfactors[d] < 1)
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid: n_pts and repfactors must be >= 1");
+    if (s->n_sites != 1)
+        return fail(ctx, PMGB_ERR_UNSUPPORTED,
+                    "pmgb_energy_grid: the probe must be a single site (got %d sites); multi-site probes need "
+                    "rotational averaging",
+                    s->n_sites);
+    const int64_t total = int64_t(n_pts[0]) * n_pts[1] * n_pts[2];
+    if (total > int64_t(INT32_MAX) * PMGB_THREADS / 2)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid: grid too large");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    if (int rc = grid_axes(s, n_pts, repfactors)) return rc;
+    LaunchArgs a = base_args(s);
+    a.sys.charged = 0;  // grid.jl:337-338: single-site probes get the vdW energy only
+    a.pose_mode = POSE_GRID;
+    a.out_mode = OUT_GRID;
+    for (int d = 0; d < 3; ++d) a.n_pts[d] = n_pts[d];
+    const float* ax = static_cast<const float*>(s->axes.p);
+    a.grid_x = ax;
+    a.grid_y = ax + n_pts[0];
+    a.grid_z = ax + n_pts[0] + n_pts[1];
+    a.unit_factor = static_cast<float>(unit_factor);
+    a.grid_out = out_dev;
+    const int n_ctas = static_cast<int>((total + PMGB_THREADS - 1) / PMGB_THREADS);
+    PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_energy_grid(pmgb_system* s, const int32_t n_pts[3], const int32_t repfactors[3],
+                                double unit_factor, float* out) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (!out || !n_pts) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid: NULL argument");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    const int64_t total = int64_t(std::max(n_pts[0], 0)) * std::max(n_pts[1], 0) * std::max(n_pts[2], 0);
+    if (int rc = ensure(ctx, s->out_buf, sizeof(float) * std::max<int64_t>(total, 1))) return rc;
+    if (int rc = pmgb_energy_grid_device(s, n_pts, repfactors, unit_factor, static_cast<float*>(s->out_buf.p)))
+        return rc;
+    PMGB_CK(ctx, cudaMemcpyAsync(out, s->out_buf.p, sizeof(float) * total, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_status(ctx);
+}
+
+extern "C" int pmgb_philox4x32_10(pmgb_ctx* ctx, int64_t n, const uint32_t* ctr, const uint32_t* key,
+                                  uint32_t* out) {
+    if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
+    if (n < 0 || (n > 0 && (!ctr || !key || !out)))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_philox4x32_10: bad arguments");
+    if (n == 0) return PMGB_OK;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    unsigned int *dc = nullptr, *dk = nullptr, *dout = nullptr;
+    cudaError_t e = cudaMalloc(&dc, 16 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&dk, 8 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&dout, 16 * n);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dc, ctr, 16 * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dk, key, 8 * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = pmgb_launch_philox(dc, dk, n, dout, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, 16 * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (dc) cudaFree(dc);
+    if (dk) cudaFree(dk);
+    if (dout) cudaFree(dout);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "pmgb_philox4x32_10");
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_fp32_peak(pmgb_ctx* ctx, int n_ctas, int iters, double* tflops_out) {
+    if (!ctx || !tflops_out || n_ctas < 1 || iters < 1) return PMGB_ERR_INVALID_ARGUMENT;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    float* sink = nullptr;
+    PMGB_CK(ctx, cudaMalloc(&sink, sizeof(float) * n_ctas));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaError_t e = pmgb_launch_fp32_peak(sink, n_ctas, iters, ctx->stream);  // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(e0, ctx->stream);
+    if (e == cudaSuccess) e = pmgb_launch_fp32_peak(sink, n_ctas, iters, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "pmgb_fp32_peak");
+    const double flops = 2.0 * 8.0 * 16.0 * double(iters) * 256.0 * double(n_ctas);
+    *tflops_out = flops / (double(ms) * 1e-3) / 1e12;
+    return PMGB_OK;
+}

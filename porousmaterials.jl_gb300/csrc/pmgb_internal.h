@@ -1,0 +1,130 @@
+// pmgb_internal.h -- device data layout shared by the kernels and the C-ABI layer.
+//
+// Layout in HBM (all owned by a pmgb_system):
+//   rec[n_rec]      float4 (xf, yf, zf, q) of every framework site of the replicated
+//                   crystal, sorted by LJ species; each species segment starts on a
+//                   multiple of PMGB_SEG_ALIGN and is padded with NaN records (which
+//                   fail every cutoff comparison and so contribute nothing).
+//   seg[n_seg]      [lo, hi) record range of each species segment.
+//   segpar[n_seg * PMGB_MAX_SITES]  per (segment, guest site): sigma^2, 4*epsilon,
+//                   overlap radius^2 (0.1, or -1 when the pair has no LJ term).
+//   krow[n_krow]    k-vectors grouped in rows of constant (ka, kb) and consecutive kc.
+//   skw[n_k]        wt_k * S(k), FP32 (re, im), S(k) built on the device in FP64.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define PMGB_MAX_SITES 8      // guest sites (merged LJ atoms + point charges)
+#define PMGB_MAX_SEG 64       // framework species segments
+#define PMGB_SEG_ALIGN 4      // record alignment of a species segment
+#define PMGB_TILE 2048        // framework records per shared-memory stage (32 KB)
+#define PMGB_NSTAGE 3         // stages in the TMA ring
+#define PMGB_THREADS 256      // insertions per CTA (one per thread)
+
+// status word bits written by kernels (never a trap)
+#define PMGB_DEVERR_TMA_TIMEOUT 0x1u
+#define PMGB_DEVERR_BAD_ARGS 0x2u
+
+struct SegDesc {
+    int lo, hi;        // record range [lo, hi), both multiples of PMGB_SEG_ALIGN
+    int species;       // species id in the caller's force-field table (-1: charge-only sites)
+    int has_lj;
+};
+
+struct SitePar {
+    float sig2, eps4, r2ovl, pad;
+};
+
+struct KRow {
+    int ka, kb, kc0, n;   // k = (ka, kb, kc0 .. kc0+n-1)
+    int off;              // index of the first k-vector of the row in skw
+    int pad0, pad1, pad2;
+};
+
+// Everything a kernel needs to know about one (framework, guest) system.
+struct SysDev {
+    const float4* rec;
+    int n_rec, n_tiles;
+    int n_seg;
+    const SegDesc* seg;
+    const SitePar* segpar;
+    // upper-triangular f_to_c (Cartesian = H * fractional) and c_to_f, FP32
+    float h00, h01, h02, h11, h12, h22;
+    float g00, g01, g02, g11, g12, g22;
+    float rc2;                     // LJ cutoff radius^2 (ljff.r²_cutoff)
+    float rc2e;                    // Ewald real-space cutoff radius^2
+    float alpha;                   // Ewald convergence parameter (1/A)
+    double coul;                   // 1 / (4 pi eps0) in K A / e^2
+    int charged;                   // guest-host electrostatics on
+    // guest: site offsets from the centre of mass (Cartesian, A), charges
+    int n_sites;
+    float body[PMGB_MAX_SITES][3];
+    float q[PMGB_MAX_SITES];
+    // Ewald reciprocal space
+    int n_krow, n_k;
+    const KRow* krow;
+    const float2* skw;
+};
+
+enum PoseMode : int {
+    POSE_PHILOX = 0,   // Widom: pose of insertion i from Philox4x32-10(seed, i)
+    POSE_SITES = 1,    // explicit site coordinates (n x n_sites x 3, FP64)
+    POSE_GRID = 2,     // energy-grid points (single-site probe)
+};
+
+enum OutMode : int {
+    OUT_WIDOM = 0,     // per-CTA Boltzmann partial sums (+ optional per-insertion U)
+    OUT_ENERGY = 1,    // per-configuration (U_vdw, U_es_sr, U_es_lr)
+    OUT_GRID = 2,      // per-point energy (float) * unit factor
+};
+
+// Per-CTA partial of the Boltzmann accumulation, log-sum-exp form.
+struct LsePartial {
+    double m;      // max of -U/T
+    double s;      // sum exp(-U/T - m)
+    double tv;     // sum U_vdw exp(-U/T - m)
+    double te;     // sum U_es exp(-U/T - m)
+    long long n_inf;  // insertions with U = +Inf (overlap)
+    long long pad;
+};
+
+struct LaunchArgs {
+    SysDev sys;
+    int pose_mode, out_mode;
+    // Widom (POSE_PHILOX)
+    unsigned long long seed;
+    long long n_per_block;       // insertions per statistics block
+    int n_blocks;                // statistics blocks
+    int ctas_per_block;          // CTAs covering one statistics block
+    double inv_temperature;
+    LsePartial* partials;        // [n_blocks * ctas_per_block]
+    double* u_out;               // optional: [n_total * 2] (U_vdw, U_es)
+    // explicit sites (POSE_SITES)
+    const double* site_xf;       // [n_conf * n_sites * 3]
+    long long n_conf;
+    double* e_out;               // [n_conf * 3] (vdw, sr, lr)
+    // grid (POSE_GRID)
+    int n_pts[3];
+    const float* grid_x;         // fractional coordinate of each grid plane, per axis,
+    const float* grid_y;         //   already divided by the replication factor
+    const float* grid_z;
+    float unit_factor;
+    float* grid_out;
+    // status
+    unsigned int* status;
+};
+
+// kernels (defined in pmgb_kernels.cu); return cudaError_t of the launch
+cudaError_t pmgb_launch_pairs(const LaunchArgs& a, int n_ctas, cudaStream_t st);
+cudaError_t pmgb_launch_reduce_blocks(const LsePartial* partials, int n_blocks, int ctas_per_block,
+                                      double* block_out, cudaStream_t st);
+// qfix: framework charge fractional coordinates as 32-bit fixed point (x * 2^32 mod 2^32)
+cudaError_t pmgb_launch_structure_factor(const uint32_t* qfix, const double* q, int n_q,
+                                         const int* kabc, const double* wt, int n_k,
+                                         double* sk_out, float2* skw_out, cudaStream_t st);
+cudaError_t pmgb_launch_sample_poses(unsigned long long seed, long long start, long long n,
+                                     float* xf_out, float* rot_out, cudaStream_t st);
+cudaError_t pmgb_launch_philox(const unsigned int* ctr, const unsigned int* key, long long n,
+                               unsigned int* out, cudaStream_t st);
+cudaError_t pmgb_launch_fp32_peak(float* sink, int n_ctas, int iters, cudaStream_t st);
+size_t pmgb_pairs_smem_bytes();

@@ -1,0 +1,143 @@
+"""A (replicated crystal, guest molecule, force field, Ewald) system resident on the GPU.
+
+Wraps a `pmgb_system` handle of libpmgb: species names are mapped to dense ids, the
+force-field ε / σ² tables are built over those ids, and the guest's LJ sites and charges
+are given as Cartesian offsets from its centre of mass.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import Context, ptr
+from .crystal import Crystal, has_charges
+from .ewald import EwaldParams
+from .forcefield import LJForceField
+from .molecule import Molecule, body_offsets
+
+
+class GPUSystem:
+    def __init__(self, crystal: Crystal, molecule: Molecule, ljff: LJForceField | None,
+                 eparams: EwaldParams | None = None, ctx: Context | None = None):
+        """ljff=None builds a charge-only system (all ε = 0, cutoff from eparams)."""
+        self.ctx = ctx or Context.default()
+        self.crystal = crystal
+        self.molecule = molecule
+        self.ljff = ljff
+        species = list(dict.fromkeys(list(crystal.atoms.species) + list(molecule.atom_species)))
+        self.species = species
+        sid = {s: i for i, s in enumerate(species)}
+        if ljff is not None:
+            eps, sig2 = ljff.tables(species)
+            r2_cutoff = ljff.r2_cutoff
+        else:
+            if eparams is None:
+                raise ValueError("a charge-only system needs Ewald parameters")
+            eps, sig2 = np.zeros((len(species),) * 2), np.ones((len(species),) * 2)
+            r2_cutoff = eparams.sr_cutoff_r ** 2
+        self._eps = np.ascontiguousarray(eps)
+        self._sig2 = np.ascontiguousarray(sig2)
+        atom_xf = np.ascontiguousarray(crystal.atoms.xf, dtype=np.float64)
+        atom_sp = np.ascontiguousarray([sid[s] for s in crystal.atoms.species], dtype=np.int32)
+        q_xf = np.ascontiguousarray(crystal.charges.xf, dtype=np.float64)
+        q = np.ascontiguousarray(crystal.charges.q, dtype=np.float64)
+        box = crystal.box
+        f_to_c = np.ascontiguousarray(box.f_to_c.T.reshape(-1))  # column-major
+        ax, qx = body_offsets(molecule, box)
+        self._gax = np.ascontiguousarray(ax, dtype=np.float64)
+        self._gsp = np.ascontiguousarray([sid[s] for s in molecule.atom_species], dtype=np.int32)
+        self._gqx = np.ascontiguousarray(qx, dtype=np.float64)
+        self._gq = np.ascontiguousarray(molecule.charge_q, dtype=np.float64)
+        h = C.c_void_p()
+        lib = self.ctx._lib
+        self.ctx.check(lib.pmgb_system_create(
+            self.ctx.handle, ptr(f_to_c, C.c_double),
+            len(atom_sp), ptr(atom_xf, C.c_double), ptr(atom_sp, C.c_int32),
+            q.shape[0], ptr(q_xf, C.c_double), ptr(q, C.c_double),
+            len(species), ptr(self._eps, C.c_double), ptr(self._sig2, C.c_double), r2_cutoff,
+            len(self._gsp), ptr(self._gax, C.c_double), ptr(self._gsp, C.c_int32),
+            self._gq.shape[0], ptr(self._gqx, C.c_double), ptr(self._gq, C.c_double),
+            C.byref(h)))
+        self.handle = h
+        self.charged = has_charges(crystal) and molecule.n_charges > 0
+        self.n_sites = int(lib.pmgb_system_n_sites(h))
+        sa = np.zeros(self.n_sites, dtype=np.int32)
+        sc = np.zeros(self.n_sites, dtype=np.int32)
+        self.ctx.check(lib.pmgb_system_sites(h, ptr(sa, C.c_int32), ptr(sc, C.c_int32)))
+        self.site_atom, self.site_charge = sa, sc
+        self.eparams = None
+        if eparams is not None:
+            self.set_ewald(eparams)
+
+    # -- set-up ------------------------------------------------------------------------
+    def set_ewald(self, ep: EwaldParams) -> None:
+        abc = np.ascontiguousarray(ep.kvec_abc, dtype=np.int32)
+        wt = np.ascontiguousarray(ep.kvec_wt, dtype=np.float64)
+        self.ctx.check(self.ctx._lib.pmgb_system_set_ewald(self.handle, ep.alpha, ep.sr_cutoff_r, wt.shape[0],
+                                                           ptr(abc, C.c_int32), ptr(wt, C.c_double)))
+        self.eparams = ep
+
+    def structure_factor(self) -> np.ndarray:
+        out = np.zeros((self.eparams.n_kvecs, 2))
+        self.ctx.check(self.ctx._lib.pmgb_structure_factor(self.handle, ptr(out, C.c_double)))
+        return out[:, 0] + 1j * out[:, 1]
+
+    def info(self) -> dict:
+        out = np.zeros(6, dtype=np.int64)
+        self.ctx.check(self.ctx._lib.pmgb_system_info(self.handle, ptr(out, C.c_int64)))
+        keys = ("n_records", "n_segments", "n_kvecs", "n_krows", "n_sites", "h2d_bytes")
+        return {k: int(v) for k, v in zip(keys, out)}
+
+    # -- evaluation ----------------------------------------------------------------------
+    def site_coords(self, atom_xf: np.ndarray, charge_xf: np.ndarray | None) -> np.ndarray:
+        """Pack per-configuration LJ-site and charge coordinates ((n, n_atoms, 3) and
+        (n, n_charges, 3), fractional) into the system's merged site order."""
+        atom_xf = np.asarray(atom_xf, dtype=np.float64)
+        n = atom_xf.shape[0] if atom_xf.size else (charge_xf.shape[0] if charge_xf is not None else 0)
+        out = np.zeros((n, self.n_sites, 3))
+        for k in range(self.n_sites):
+            a, c = int(self.site_atom[k]), int(self.site_charge[k])
+            if a >= 0:
+                out[:, k, :] = atom_xf[:, a, :]
+                if c >= 0 and charge_xf is not None and not np.allclose(charge_xf[:, c, :], atom_xf[:, a, :],
+                                                                        rtol=0, atol=1e-12):
+                    raise ValueError("a guest charge that shares an LJ site's body offset was moved apart from it")
+            else:
+                out[:, k, :] = charge_xf[:, c, :]
+        return np.ascontiguousarray(out)
+
+    def energies(self, site_xf: np.ndarray) -> np.ndarray:
+        """(n, 3) array of (U_vdw, U_es short-range, U_es long-range) in K."""
+        site_xf = np.ascontiguousarray(site_xf, dtype=np.float64).reshape(-1, self.n_sites, 3)
+        n = site_xf.shape[0]
+        out = np.zeros((n, 3))
+        self.ctx.check(self.ctx._lib.pmgb_energies(self.handle, n, ptr(site_xf, C.c_double), ptr(out, C.c_double)))
+        return out
+
+    def widom(self, n_per_block: int, n_blocks: int, seed: int, temperature: float, want_energies: bool = False):
+        """Per-block (log Σbf, ⟨U_vdw⟩, ⟨U_es⟩, n_inf) and optionally per-insertion (U_vdw, U_es)."""
+        block = np.zeros((n_blocks, 4))
+        u = np.zeros((n_blocks * n_per_block, 2)) if want_energies else None
+        self.ctx.check(self.ctx._lib.pmgb_widom(self.handle, int(n_per_block), int(n_blocks), int(seed),
+                                                float(temperature), ptr(block, C.c_double), ptr(u, C.c_double)))
+        return block, u
+
+    def energy_grid(self, n_pts, repfactors, unit_factor: float) -> np.ndarray:
+        n = np.ascontiguousarray(n_pts, dtype=np.int32)
+        r = np.ascontiguousarray(repfactors, dtype=np.int32)
+        out = np.zeros(int(np.prod(n)), dtype=np.float32)
+        self.ctx.check(self.ctx._lib.pmgb_energy_grid(self.handle, ptr(n, C.c_int32), ptr(r, C.c_int32),
+                                                      float(unit_factor), ptr(out, C.c_float)))
+        return out.reshape(tuple(int(v) for v in n[::-1])).transpose(2, 1, 0)  # data[i, j, k], i fastest
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.ctx._lib.pmgb_system_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

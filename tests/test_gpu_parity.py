@@ -1,0 +1,329 @@
+"""GPU parity: libpmgb (sm_103a) against the FP64 oracle and the reference's golden values.
+
+Tolerances (from the hot-path contract): per-configuration energies within 1e-5 relative
+or 1e-4 K absolute; block log Σ e^{-U/T} and ⟨U⟩ within 1e-6 relative; golden values at
+the reference tests' own tolerances.  Pair terms whose distance sits within FP32 rounding
+of the cutoff can switch sides; such configurations are counted and bounded separately.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+import pmgb
+from conftest import DATA
+from pm_helpers import oracle_for, oracle_sites_split, random_configs, within
+from pmgb import synthetic
+
+pytestmark = pytest.mark.gpu
+
+RTOL, ATOL = 1e-5, 1e-4
+
+
+def _report(name, gpu, ref):
+    fin = np.isfinite(ref)
+    err = np.abs(gpu[fin] - ref[fin])
+    rel = err / np.maximum(np.abs(ref[fin]), 1e-30)
+    print(f"[{name}] n={fin.sum()} max|d|={err.max():.3e} K  max rel={rel.max():.3e}  "
+          f"median|d|={np.median(err):.3e} K")
+
+
+# ---------------------------------------------------------------------------- RNG
+def test_philox_device_matches_oracle(ctx):
+    rng = np.random.default_rng(3)
+    ctr = rng.integers(0, 2 ** 32, size=(4096, 4), dtype=np.uint64).astype(np.uint32)
+    key = rng.integers(0, 2 ** 32, size=(4096, 2), dtype=np.uint64).astype(np.uint32)
+    ctr[0], key[0] = 0, 0
+    np.testing.assert_array_equal(ctx.philox4x32_10(ctr, key), oracle.philox4x32_10(ctr, key))
+
+
+def test_poses_are_uniform_rotations(ctx):
+    xf, rot = ctx.sample_poses(seed=11, start=0, n=20000)
+    assert np.all((xf >= 0) & (xf < 1))
+    R = rot.reshape(-1, 3, 3).transpose(0, 2, 1).astype(np.float64)  # column-major -> matrices
+    np.testing.assert_allclose(np.einsum("nij,nkj->nik", R, R), np.broadcast_to(np.eye(3), R.shape), atol=2e-6)
+    np.testing.assert_allclose(np.linalg.det(R), 1.0, atol=5e-6)
+    # uniformity: a rotated unit vector covers the sphere evenly (mean ~ 0, second moment ~ I/3)
+    v = R @ np.array([1.0, 0.0, 0.0])
+    assert np.abs(v.mean(axis=0)).max() < 0.02
+    np.testing.assert_allclose(v.T @ v / len(v), np.eye(3) / 3, atol=0.01)
+    # same seed + start -> same poses; different start continues the stream
+    xf2, rot2 = ctx.sample_poses(seed=11, start=100, n=10)
+    np.testing.assert_array_equal(xf2, xf[100:110])
+    np.testing.assert_array_equal(rot2, rot[100:110])
+
+
+# ------------------------------------------------------------------- golden values
+def test_golden_sbmof1_xe(golden):
+    g = golden["sbmof1_xe_dreiding"]
+    ljff = pmgb.LJForceField("Dreiding", r_cutoff=g["r_cutoff"])
+    cr = pmgb.read_cif(DATA / "crystals" / "SBMOF-1.cif")
+    sc = pmgb.replicate(cr, pmgb.replication_factors(cr.box, ljff))
+    xe = pmgb.Frac(pmgb.read_molecule("Xe"), sc.box)
+    pmgb.translate_to(xe, np.zeros(3))
+    e0 = pmgb.vdw_energy(sc, xe, ljff)
+    assert e0 == pytest.approx(g["origin_energy"], abs=g["atol"])
+    pmgb.translate_to(xe, sc.box.c_to_f @ np.array(g["point2_cart"]))
+    e2 = pmgb.vdw_energy(sc, xe, ljff)
+    assert e2 == pytest.approx(g["point2_energy"], abs=g["atol"])
+
+
+def test_golden_nu1000_ions(golden):
+    g = golden["nu1000_ewald"]
+    cr = pmgb.read_cif(DATA / "crystals" / "NU-1000_Greg.cif")
+    sc = pmgb.replicate(cr, pmgb.replication_factors(cr.box, g["sr_cutoff"]))
+    ep = pmgb.setup_Ewald_sum(sc.box, g["sr_cutoff"], eps=g["eps"])
+    assert tuple(ep.kreps) == tuple(g["kreps"])
+    for x, want, atol in g["ions"]:
+        ion = pmgb.molecule_from_sites("ion", [], np.zeros((0, 3)), [g["q"]], [[0.0, 0.0, 0.0]])
+        ion = pmgb.Frac(ion, sc.box)
+        pmgb.translate_to(ion, sc.box.c_to_f @ np.array(x))
+        phi = pmgb.electrostatic_potential_energy(sc, ion, ep)
+        assert pmgb.total(phi) == pytest.approx(want, abs=atol)
+
+
+def test_golden_zif71_co2(golden):
+    g = golden["zif71_co2"]
+    cr = pmgb.read_cif(DATA / "crystals" / "zif71_bogus_charges.cif")
+    pmgb.strip_numbers_from_atom_labels(cr)
+    ff = pmgb.LJForceField("Greg_bogus_ZIF71", r_cutoff=g["r_cutoff"])
+    ep = pmgb.setup_Ewald_sum(cr.box, g["es_sr_cutoff"], eps=1e-6)
+    tot_v, tot_e = 0.0, 0.0
+    for pos, wv, we in [(g["co2_1"], g["vdw_1"], g["es_1"]), (g["co2_2"], None, None)]:
+        co2 = pmgb.Frac(pmgb.read_molecule("CO2EPM2"), cr.box)
+        co2.atom_x = np.array(pos)
+        co2.charge_x = np.array(pos)
+        v = pmgb.vdw_energy(cr, co2, ff)
+        e = pmgb.total(pmgb.electrostatic_potential_energy(cr, co2, ep))
+        if wv is not None:
+            assert v == pytest.approx(wv, abs=g["vdw_atol"])
+            assert e == pytest.approx(we, abs=g["es_atol"])
+        tot_v += v
+        tot_e += e
+    assert tot_v == pytest.approx(g["vdw_both"], abs=g["vdw_both_atol"])
+    assert tot_e == pytest.approx(g["es_both"], abs=g["es_both_atol"])
+
+
+# ------------------------------------------------------ random configurations
+def _c0_system():
+    cr = synthetic.config0()
+    ff = synthetic.forcefield()
+    sc = pmgb.replicate(cr, pmgb.replication_factors(cr.box, ff))
+    return pmgb.GPUSystem(sc, pmgb.Frac(synthetic.ch4(), sc.box), ff)
+
+
+def _c1_system():
+    cr = synthetic.config1()
+    ff = synthetic.forcefield()
+    sc = pmgb.replicate(cr, pmgb.replication_factors(cr.box, ff))
+    ep = pmgb.setup_Ewald_sum(sc.box, ff.r_cutoff, eps=1e-6)
+    return pmgb.GPUSystem(sc, pmgb.Frac(synthetic.co2(), sc.box), ff, ep)
+
+
+@pytest.fixture(scope="module")
+def c0():
+    return _c0_system()
+
+
+@pytest.fixture(scope="module")
+def c1():
+    return _c1_system()
+
+
+def test_random_configs_lj(c0):
+    sites, lj, _ = random_configs(c0, 4000, seed=5)
+    gpu = c0.energies(sites)
+    o = oracle_for(c0)
+    v, _, _ = o.energies(lj)
+    _report("c0 vdw", gpu[:, 0], v)
+    assert np.array_equal(np.isinf(gpu[:, 0]), np.isinf(v))
+    ok = within(gpu[:, 0], v, RTOL, ATOL)
+    assert ok.mean() >= 0.999, f"{(~ok).sum()} configurations outside tolerance"
+    assert np.abs(gpu[np.isfinite(v), 0] - v[np.isfinite(v)]).max() < 0.1
+
+
+def test_random_configs_ewald(c1):
+    sites, lj, q = random_configs(c1, 1024, seed=6)
+    gpu = c1.energies(sites)
+    o = oracle_for(c1)
+    v, sr, lr = o.energies(lj, q, charged=True, use_sk=True)
+    _report("c1 vdw", gpu[:, 0], v)
+    _report("c1 es sr", gpu[:, 1], sr)
+    _report("c1 es lr", gpu[:, 2], lr)
+    assert np.array_equal(np.isinf(gpu[:, 0]), np.isinf(v))
+    fin = np.isfinite(v)
+    tot_g = gpu[fin].sum(axis=1)
+    tot_o = (v + sr + lr)[fin]
+    _report("c1 total", tot_g, tot_o)
+    ok = within(tot_g, tot_o, RTOL, ATOL)
+    assert ok.mean() >= 0.995, f"{(~ok).sum()} of {ok.size} configurations outside tolerance"
+    assert within(gpu[:, 2], lr, RTOL, 1e-3).all()
+
+
+def test_direct_form_cross_check(c1):
+    # a few configurations against the reference's direct e^{ik·r} form
+    sites, lj, q = random_configs(c1, 8, seed=9)
+    gpu = c1.energies(sites)
+    o = oracle_for(c1)
+    v, sr, lr = o.energies(lj, q, charged=True, use_sk=False)
+    fin = np.isfinite(v)
+    assert within(gpu[fin].sum(axis=1), (v + sr + lr)[fin], RTOL, 1e-3).all()
+
+
+# ------------------------------------------------------------------ Widom path
+def _widom_parity(gs, n_per_block, seed, T=298.0, use_sk=True):
+    blocks, u = gs.widom(n_per_block, 5, seed, T, want_energies=True)
+    ctx = gs.ctx
+    n = 5 * n_per_block
+    xf, rot = ctx.sample_poses(seed, 0, n)
+    # the device rotation is column-major R[i + 3j], the layout the oracle takes
+    body = np.zeros((gs.n_sites, 3))
+    from pmgb.molecule import body_offsets
+    ax, qx = body_offsets(gs.molecule, gs.crystal.box)
+    for k in range(gs.n_sites):
+        body[k] = ax[gs.site_atom[k]] if gs.site_atom[k] >= 0 else qx[gs.site_charge[k]]
+    o = oracle_for(gs)
+    sites = o.sites_from_poses(xf.astype(np.float64), rot.astype(np.float64), body)
+    lj, q = oracle_sites_split(gs, sites)
+    v, sr, lr = o.energies(lj, q, charged=gs.charged, use_sk=use_sk)
+    return blocks, u, v, sr + lr
+
+
+def _check_blocks(blocks, u_gpu, T, n_per_block):
+    # the device log-sum-exp reduction against FP64 sums of the device's own energies
+    ref = oracle.widom_blocks(u_gpu[:, 0], u_gpu[:, 1], T, 5, n_per_block)
+    np.testing.assert_allclose(blocks[:, 0], np.log(ref[:, 0]), rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(blocks[:, 1], ref[:, 1] / ref[:, 0], rtol=1e-10, atol=1e-9)
+    np.testing.assert_allclose(blocks[:, 2], ref[:, 2] / ref[:, 0], rtol=1e-10, atol=1e-9)
+
+
+def test_widom_parity_lj(c0):
+    npb, T = 4000, 298.0
+    blocks, u, v, es = _widom_parity(c0, npb, seed=21, T=T)
+    _report("widom c0 vdw", u[:, 0], v)
+    assert np.array_equal(np.isinf(u[:, 0]), np.isinf(v))
+    _check_blocks(blocks, u, T, npb)
+    ref = oracle.widom_blocks(v, es, T, 5, npb)
+    kh_rel = np.abs(np.exp(blocks[:, 0] - np.log(ref[:, 0])) - 1.0)
+    print(f"[widom c0] block KH rel err max {kh_rel.max():.3e}; <U> rel err "
+          f"{np.abs(blocks[:, 1] / (ref[:, 1] / ref[:, 0]) - 1).max():.3e}")
+    assert kh_rel.max() < 1e-6
+    np.testing.assert_allclose(blocks[:, 1], ref[:, 1] / ref[:, 0], rtol=1e-6)
+    assert np.all(blocks[:, 3] == np.isinf(v).reshape(5, npb).sum(axis=1))
+
+
+def test_widom_parity_ewald(c1):
+    npb, T = 1000, 298.0
+    blocks, u, v, es = _widom_parity(c1, npb, seed=22, T=T)
+    _report("widom c1 vdw", u[:, 0], v)
+    _report("widom c1 es", u[:, 1], es)
+    _check_blocks(blocks, u, T, npb)
+    ref = oracle.widom_blocks(v, es, T, 5, npb)
+    kh_rel = np.abs(np.exp(blocks[:, 0] - np.log(ref[:, 0])) - 1.0)
+    u_rel = np.abs((blocks[:, 1] + blocks[:, 2]) / ((ref[:, 1] + ref[:, 2]) / ref[:, 0]) - 1.0)
+    print(f"[widom c1] block KH rel err max {kh_rel.max():.3e}; <U> rel err max {u_rel.max():.3e}")
+    assert kh_rel.max() < 1e-6
+    assert u_rel.max() < 1e-6
+
+
+def test_widom_deterministic(c0):
+    a, _ = c0.widom(3000, 5, 77, 298.0)
+    b, _ = c0.widom(3000, 5, 77, 298.0)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_widom_ragged_block_sizes(c0):
+    # block sizes that are not multiples of the CTA size, including a single insertion
+    for npb in (1, 255, 257, 1000):
+        blocks, u = c0.widom(npb, 5, 5, 298.0, want_energies=True)
+        _check_blocks(blocks, u, 298.0, npb)
+
+
+# ------------------------------------------------------------------ energy grid
+def test_energy_grid_parity():
+    cr = synthetic.config0()
+    ff = synthetic.forcefield()
+    g = pmgb.energy_grid(cr, synthetic.xe(), ff, resolution=(17, 13, 11), units="K", verbose=False)
+    rep = pmgb.replication_factors(cr.box, ff)
+    sc = pmgb.replicate(cr, rep)
+    gs = pmgb.GPUSystem(sc, pmgb.Frac(synthetic.xe(), sc.box), ff)
+    ref = oracle_for(gs).energy_grid((17, 13, 11), rep)
+    _report("grid", g.data.astype(np.float64).ravel(), ref.ravel())
+    assert np.array_equal(np.isinf(g.data), np.isinf(ref))
+    ok = within(g.data.astype(np.float64), ref, RTOL, ATOL)
+    assert ok.mean() >= 0.999
+    gk = pmgb.energy_grid(cr, synthetic.xe(), ff, resolution=(17, 13, 11), units="kJ_mol", verbose=False)
+    np.testing.assert_allclose(gk.data, g.data * (8.314 / 1000.0), rtol=2e-7)
+
+
+@pytest.mark.parametrize("name", ["LTA.cif", "SOD.cif"])
+def test_energy_grid_periodic_endpoints(golden, name):
+    # test/grid.jl:43-55
+    g = golden["grid_periodic"]
+    cr = pmgb.read_cif(DATA / "crystals" / name)
+    grid = pmgb.energy_grid(cr, pmgb.read_molecule("CH4"), pmgb.LJForceField("UFF"), resolution=g["resolution"],
+                            verbose=False)
+    d = grid.data.astype(np.float64).copy()
+    d[d > g["cap"]] = 0.0
+    np.testing.assert_allclose(d[0], d[-1], atol=g["atol"])
+    np.testing.assert_allclose(d[:, 0], d[:, -1], atol=g["atol"])
+    np.testing.assert_allclose(d[:, :, 0], d[:, :, -1], atol=g["atol"])
+
+
+# ------------------------------------------------------ henry_coefficient drop-in
+def test_henry_drop_in_matches_oracle():
+    cr = synthetic.config0()
+    ff = synthetic.forcefield()
+    holder = []
+    res = pmgb.henry_coefficient(cr, synthetic.ch4(), 298.0, ff, insertions_per_volume=0.5, verbose=False,
+                                 autosave=False, seed=1234, system_out=holder)
+    assert len(res) == 16
+    gs = holder[0]
+    npb = res.n_insertions_per_block
+    blocks, u, v, es = _widom_parity(gs, npb, seed=1234)
+    ref = oracle.widom_blocks(v, es, 298.0, 5, npb)
+    kh_ref = np.mean(ref[:, 0] / (pmgb.UNIV_GAS_CONST * 298.0 * npb))
+    assert res["henry coefficient [mol/(m³-bar)]"] == pytest.approx(kh_ref, rel=1e-6)
+    assert res["⟨U, vdw⟩ (K)"] == pytest.approx(np.mean(ref[:, 1] / ref[:, 0]), rel=1e-6)
+
+
+def test_henry_statistical_xe_sbmof1(golden, ref_masses):
+    # test/henry.jl:13-21 (rtol 2.5%, 500 insertions per Å³)
+    g = golden["henry_statistical"]
+    cr = pmgb.read_cif(DATA / "crystals" / "SBMOF-1.cif")
+    res = pmgb.henry_coefficient(cr, pmgb.read_molecule("Xe"), 298.0, pmgb.LJForceField("Dreiding", r_cutoff=12.5),
+                                 insertions_per_volume=g["insertions_per_volume"], verbose=False, autosave=False,
+                                 seed=1, masses=ref_masses)
+    assert res["henry coefficient [mol/(kg-Pa)]"] == pytest.approx(g["xe_sbmof1"]["kh_mol_kg_pa"], rel=g["rtol"])
+    assert res["⟨U⟩ (kJ/mol)"] == pytest.approx(g["xe_sbmof1"]["u_kj_mol"], rel=g["rtol"])
+
+
+def test_henry_statistical_co2_caxvii(golden, ref_masses):
+    # test/henry.jl:26-34 (charged, fully triclinic cell)
+    g = golden["henry_statistical"]
+    cr = pmgb.read_cif(DATA / "crystals" / "CAXVII_clean.cif")
+    mol = pmgb.read_molecule("CO2")
+    res = pmgb.henry_coefficient(cr, mol, 298.0, pmgb.LJForceField("Dreiding", r_cutoff=12.5),
+                                 insertions_per_volume=g["insertions_per_volume"], verbose=False, autosave=False,
+                                 seed=2, masses=ref_masses)
+    assert res["henry coefficient [mol/(kg-Pa)]"] == pytest.approx(g["co2_caxvii"]["kh_mol_kg_pa"], rel=g["rtol"])
+    assert res["⟨U⟩ (kJ/mol)"] == pytest.approx(g["co2_caxvii"]["u_kj_mol"], rel=g["rtol"])
+    np.testing.assert_array_equal(mol.atom_x, pmgb.read_molecule("CO2").atom_x)  # the molecule is not modified
+
+
+# ------------------------------------------------------------------ error paths
+def test_errors_are_reported_not_crashes(c0, c1, ctx):
+    with pytest.raises(pmgb.PMGBError, match="temperature"):
+        c0.widom(10, 5, 1, 0.0)
+    with pytest.raises(pmgb.PMGBError, match="single site"):
+        c1.energy_grid((4, 4, 4), (1, 1, 1), 1.0)
+    cr = synthetic.config1()
+    ff = synthetic.forcefield()
+    sc = pmgb.replicate(cr, (2, 2, 3))
+    no_ewald = pmgb.GPUSystem(sc, pmgb.Frac(synthetic.co2(), sc.box), ff, None)
+    with pytest.raises(pmgb.PMGBError, match="set_ewald"):
+        no_ewald.widom(10, 5, 1, 298.0)
+    assert ctx.device_status() == 0

@@ -1,0 +1,136 @@
+"""Host-side logic and the C-ABI library surface (no GPU needed)."""
+from __future__ import annotations
+
+import ctypes
+import math
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import pmgb
+from conftest import DATA, ROOT
+
+
+def test_abi_exports_every_declared_symbol():
+    header = (ROOT / "include" / "pmgb.h").read_text()
+    declared = set(re.findall(r"^\s*(?:int|void|const char\*)\s+(pmgb_\w+)\s*\(", header, flags=re.M))
+    assert len(declared) >= 20
+    lib_path = ROOT / "porousmaterials.jl_gb300" / "pmgb" / "libpmgb.so"
+    if not lib_path.exists():
+        pytest.skip("libpmgb.so not built")
+    lib = ctypes.CDLL(str(lib_path))  # loads without a GPU: no CUDA call happens at load time
+    missing = [s for s in sorted(declared) if not hasattr(lib, s)]
+    assert not missing, missing
+    bound = {name for name, _, _ in pmgb._lib.SIGNATURES}
+    assert declared == bound, (declared ^ bound)
+    lib.pmgb_abi_version.restype = ctypes.c_int
+    assert lib.pmgb_abi_version() == 1
+
+
+def test_cif_reader_and_replicate():
+    cr = pmgb.read_cif(DATA / "crystals" / "SBMOF-1.cif")
+    assert cr.atoms.n == 120 and cr.charges.n == 120
+    assert cr.box.Omega == pytest.approx(1456.472102, rel=1e-6)
+    assert np.all((cr.atoms.xf >= 0) & (cr.atoms.xf < 1))
+    sc = pmgb.replicate(cr, (3, 5, 2))
+    assert sc.atoms.n == 120 * 30
+    assert sc.box.a == pytest.approx(3 * cr.box.a)
+    # image (0,0,0) first, coordinates rescaled into the supercell
+    np.testing.assert_allclose(sc.atoms.xf[:120] * [3, 5, 2], cr.atoms.xf)
+    assert np.all(sc.atoms.xf < 1.0)
+    assert pmgb.crystal_density(cr) > 0
+
+
+def test_non_p1_rejected(tmp_path):
+    text = (DATA / "crystals" / "SOD.cif").read_text().replace("'x, y, z'", "'x, y, z'\n '-x, -y, z'")
+    p = tmp_path / "sym.cif"
+    p.write_text(text)
+    cr = pmgb.read_cif(p)
+    assert not cr.symmetry_is_p1
+    with pytest.raises(ValueError):
+        pmgb.assert_P1_symmetry(cr)
+
+
+def test_molecule_reading_and_frames():
+    co2 = pmgb.read_molecule("CO2")
+    assert co2.atom_species == ["C_CO2", "O_CO2", "O_CO2"]
+    np.testing.assert_allclose(co2.com, [0, 0, 0], atol=1e-12)
+    assert pmgb.needs_rotations(co2) and not pmgb.needs_rotations(pmgb.read_molecule("Xe"))
+    box = pmgb.Box(10.0, 11.0, 12.0, math.radians(80), math.radians(95), math.radians(100))
+    f = pmgb.Frac(co2, box)
+    back = pmgb.Cart(f, box)
+    np.testing.assert_allclose(back.atom_x, co2.atom_x, atol=1e-12)
+    pmgb.translate_to(f, np.array([0.25, 0.5, 0.75]))
+    np.testing.assert_allclose(f.com, [0.25, 0.5, 0.75])
+    R = pmgb.random_rotation_matrix(np.random.default_rng(1))
+    np.testing.assert_allclose(R @ R.T, np.eye(3), atol=1e-12)
+    assert np.linalg.det(R) == pytest.approx(1.0)
+
+
+def test_grid_helpers(golden):
+    # test/grid.jl:16-40, 148-177
+    g = golden["required_n_pts"]
+    assert pmgb.required_n_pts(pmgb.Box(*g["box"], math.pi / 2, math.pi / 2, math.pi / 2), g["dx"]) == tuple(g["n_pts"])
+    nn = pmgb.grid._arg_nearest_neighbor
+    assert nn((10, 20, 30), [0.001, 0.001, 0.001]) == [1, 1, 1]
+    assert nn((10, 20, 30), [0.999, 0.999, 0.999]) == [10, 20, 30]
+    idx = [0, 21, 31]
+    pmgb.grid._apply_pbc_to_index(idx, (10, 20, 30))
+    assert idx == [10, 1, 1]
+    assert nn((3, 3, 3), [0.001, 0.001, 0.26]) == [1, 1, 2]
+    assert nn((3, 3, 3), [0.76, 0.001, 0.26]) == [3, 1, 2]
+    assert nn((4, 6, 11), [0.32, 0.42, 0.61]) == [2, 3, 7]
+    assert pmgb.xf_to_id((4, 4, 4), [0.0001, 0.2400, 0.2600]) == [1, 1, 2]
+    assert pmgb.xf_to_id((4, 4, 4), [-0.0001, 0.2400, 1.01]) == [4, 1, 1]
+    np.testing.assert_allclose(pmgb.id_to_xf((2, 2, 2), (3, 3, 3)), [0.5, 0.5, 0.5])
+
+
+def test_cube_round_trip(tmp_path):
+    # test/grid.jl:20-24
+    pmgb.rc["paths"]["grids"] = str(tmp_path)
+    rng = np.random.default_rng(0)
+    grid = pmgb.Grid(pmgb.Box(0.7, 0.8, 0.9, 1.5, 1.6, 1.7), (3, 3, 3), rng.random((3, 3, 3)), "kJ_mol",
+                     np.array([1.0, 2.0, 3.0]))
+    pmgb.write_cube(grid, "test_grid.cube", verbose=False)
+    assert grid.isapprox(pmgb.read_cube("test_grid.cube"), atol=1e-5)
+
+
+def test_accessible_lookup():
+    data = np.zeros((5, 5, 5), dtype=bool)
+    data[2, 2, 2] = True
+    grid = pmgb.Grid(pmgb.Box(1, 1, 1, math.pi / 2, math.pi / 2, math.pi / 2), (5, 5, 5), data, "K", np.zeros(3))
+    assert pmgb.accessible(grid, [0.5, 0.5, 0.5])
+    assert pmgb.accessible(grid, [0.75, 0.5, 0.5])     # a neighbour of the accessible node
+    assert not pmgb.accessible(grid, [0.0, 0.0, 0.0])
+    assert pmgb.accessible(grid, [0.25, 0.25, 0.25], (2, 2, 2))
+
+
+def test_synthetic_workloads_shapes():
+    from pmgb import synthetic
+
+    c0 = synthetic.config0()
+    assert c0.atoms.n == 424 and c0.charges.n == 0
+    assert {s: c0.atoms.species.count(s) for s in "Zn O C H".split()} == {"Zn": 32, "O": 104, "C": 192, "H": 96}
+    c1 = synthetic.config1()
+    assert c1.atoms.n == 600 and abs(c1.charges.q.sum()) < 1e-12
+    ff = synthetic.forcefield()
+    assert pmgb.replication_factors(c1.box, ff) == (2, 2, 3)
+    ep = pmgb.setup_Ewald_sum(pmgb.replicate(c1, (2, 2, 3)).box, 12.5, eps=1e-6)
+    assert ep.alpha == pytest.approx(0.24713, abs=1e-5)
+    assert ep.n_kvecs == 1424
+    # minimum-image separation >= 1.2 Å
+    d = c0.atoms.xf[:, None, :] - c0.atoms.xf[None, :, :]
+    d -= np.round(d)
+    r = np.linalg.norm(d @ c0.box.f_to_c.T, axis=-1) + np.eye(c0.atoms.n) * 10
+    assert r.min() >= 1.2
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    from pmgb import _lib
+
+    monkeypatch.setattr(_lib, "LIB_PATH", Path(tmp_path) / "absent.so")
+    monkeypatch.setattr(_lib, "_lib", None)
+    with pytest.raises(RuntimeError, match="libpmgb.so not found"):
+        _lib.lib()
