@@ -211,7 +211,8 @@ def ours(args, rank, world, local_rank):
     species = list(dict.fromkeys(list(sc.atoms.species) + list(mol.atom_species)))
     _tables = ff.tables(species)
     ctx = pmgb.Context(local_rank)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)          # a real (non-legacy) stream shared with the library
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     system = pmgb.GPUSystem(sc, pmgb.Frac(mol, sc.box), ff, ep, ctx=ctx)
     n_ins = args.insertions

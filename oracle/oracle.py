@@ -31,6 +31,7 @@ _SIGS = [
     ("or_structure_factor", None, [_vp]),
     ("or_get_structure_factor", None, [_vp, _dp, _dp]),
     ("or_energies", None, [_vp, C.c_int64, _dp, _dp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]),
+    ("or_energies_scaled", None, [_vp, C.c_int64, _dp, _dp, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]),
     ("or_widom_blocks", None, [_dp, _dp, C.c_int64, C.c_double, C.c_int, C.c_int64, _dp]),
     ("or_sites_from_poses", None, [_vp, C.c_int64, _dp, _dp, C.c_int, _dp, _dp]),
     ("or_energy_grid", None, [_vp, _ip, _ip, C.c_int, _dp]),
@@ -146,6 +147,29 @@ def widom_blocks(u_vdw, u_es, temperature, n_blocks, n_per_block):
     return out.reshape(n_blocks, 3)
 
 
+def widom_blocks_log(u_vdw, u_es, temperature, n_blocks, n_per_block):
+    """The same per-block sums in log space: (log Σbf, ΣU_vdw bf / Σbf, ΣU_es bf / Σbf, #U=+Inf),
+    for blocks whose plain FP64 Σ e^{-U/T} underflows."""
+    uv = np.asarray(u_vdw, dtype=np.float64).reshape(n_blocks, n_per_block)
+    ue = np.asarray(u_es, dtype=np.float64).reshape(n_blocks, n_per_block)
+    out = np.zeros((n_blocks, 4))
+    for b in range(n_blocks):
+        u = uv[b] + ue[b]
+        fin = np.isfinite(u)
+        out[b, 3] = (~fin).sum()
+        if not fin.any():
+            out[b, :3] = (-np.inf, np.nan, np.nan)
+            continue
+        x = -u[fin] / temperature
+        m = x.max()
+        w = np.exp(x - m)
+        s = w.sum()
+        out[b, 0] = m + np.log(s)
+        out[b, 1] = (w * uv[b][fin]).sum() / s
+        out[b, 2] = (w * ue[b][fin]).sum() / s
+    return out
+
+
 class OracleSystem:
     """Replicated crystal + force-field tables + guest description, FP64 on the CPU."""
 
@@ -174,16 +198,21 @@ class OracleSystem:
         lib().or_get_structure_factor(self.h, _p(re, C.c_double), _p(im, C.c_double))
         return re + 1j * im
 
-    def energies(self, lj_xf, q_xf=None, charged=False, use_sk=False, nthreads=0):
-        """(vdw, sr, lr) arrays for configurations (n, n_glj, 3) / (n, n_gq, 3)."""
+    def energies(self, lj_xf, q_xf=None, charged=False, use_sk=False, nthreads=0, scales=False):
+        """(vdw, sr, lr) arrays for configurations (n, n_glj, 3) / (n, n_gq, 3); with
+        scales=True also (Σ|LJ parts|, Σ|q_g| Σ|real-space terms|) per configuration."""
         lx = _d(lj_xf).reshape(-1, max(self.n_glj, 1) * 3) if self.n_glj else None
         n = lx.shape[0] if lx is not None else _d(q_xf).reshape(-1, self.n_gq * 3).shape[0]
         if lx is None:
             lx = np.zeros((n, 3))
         qx = _d(q_xf).reshape(n, -1) if (charged and self.n_gq) else np.zeros((n, 3))
         vdw, sr, lr = np.zeros(n), np.zeros(n), np.zeros(n)
-        lib().or_energies(self.h, n, _p(lx, C.c_double), _p(qx, C.c_double), int(charged), int(use_sk),
-                          int(nthreads), _p(vdw, C.c_double), _p(sr, C.c_double), _p(lr, C.c_double))
+        sv, ss = np.zeros(n), np.zeros(n)
+        lib().or_energies_scaled(self.h, n, _p(lx, C.c_double), _p(qx, C.c_double), int(charged), int(use_sk),
+                                 int(nthreads), _p(vdw, C.c_double), _p(sr, C.c_double), _p(lr, C.c_double),
+                                 _p(sv, C.c_double), _p(ss, C.c_double))
+        if scales:
+            return vdw, sr, lr, sv, ss
         return vdw, sr, lr
 
     def sites_from_poses(self, xf_com, rot, body):

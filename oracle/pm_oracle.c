@@ -251,8 +251,8 @@ void or_system_destroy(or_system *s) {
 
 /* ---- vdw_energy(atoms_i, atoms_j, box, ljff): src/vdw_energetics.jl:25-47,
  *      reached via vdw_energy(crystal, molecule, ljff) at :62-64. --------- */
-double or_vdw_energy_sys(const or_system *s, const double *g_xf) {
-    double energy = 0.0;
+static double vdw_energy_scaled(const or_system *s, const double *g_xf, double *scale) {
+    double energy = 0.0, mag = 0.0;
     for (int i = 0; i < s->n_glj; i++) {
         const double *xi = g_xf + 3 * i;
         int si = s->g_sp[i];
@@ -263,14 +263,22 @@ double or_vdw_energy_sys(const or_system *s, const double *g_xf) {
             matvec(s->f_to_c, dxf, dx);
             double r2 = dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2];
             if (r2 < s->r2_cut) {
-                if (r2 < OR_R2_OVERLAP) return INFINITY;
+                if (r2 < OR_R2_OVERLAP) { if (scale) *scale = INFINITY; return INFINITY; }
                 int sj = s->fw_sp[j];
-                energy += or_lennard_jones(r2, s->sig2[si * s->n_species + sj], s->eps[si * s->n_species + sj]);
+                double e = or_lennard_jones(r2, s->sig2[si * s->n_species + sj], s->eps[si * s->n_species + sj]);
+                energy += e;
+                /* magnitude of the repulsive and attractive parts separately */
+                double ratio = s->sig2[si * s->n_species + sj] / r2;
+                ratio = ratio * ratio * ratio;
+                mag += 4.0 * fabs(s->eps[si * s->n_species + sj]) * ratio * (ratio + 1.0);
             }
         }
     }
+    if (scale) *scale = mag;
     return energy;
 }
+
+double or_vdw_energy_sys(const or_system *s, const double *g_xf) { return vdw_energy_scaled(s, g_xf, NULL); }
 
 /* ---- _ϕ direct e^{ik·r} form: src/electrostatics.jl:347-388 with fill_eikr!
  *      :288-306.  Scratch arrays are per calling thread (Eikr, :90-101). ---- */
@@ -381,7 +389,7 @@ void or_get_structure_factor(const or_system *s, double *re, double *im) {
     memcpy(im, s->sk_im, sizeof(double) * s->n_k);
 }
 
-static void phi_sk(const or_system *s, const double xf[3], double *sr, double *lr) {
+static void phi_sk(const or_system *s, const double xf[3], double *sr, double *lr, double *sr_mag) {
     double plr = 0.0;
     for (int k = 0; k < s->n_k; k++) {
         int ka = s->kabc[3 * k], kb = s->kabc[3 * k + 1], kc = s->kabc[3 * k + 2];
@@ -396,18 +404,24 @@ static void phi_sk(const or_system *s, const double xf[3], double *sr, double *l
         double v[3];
         matvec(s->f_to_c, d, v);
         double r = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-        if (r < s->sr_cut) psr += s->q[c] / r * erfc(r * s->alpha) / fpe;
+        if (r < s->sr_cut) {
+            double t = s->q[c] / r * erfc(r * s->alpha) / fpe;
+            psr += t;
+            if (sr_mag) *sr_mag += fabs(t);
+        }
     }
     *sr = psr; *lr = plr;
 }
 
 /* ---- electrostatic_potential_energy(crystal, molecule, eparams, eikr):
  *      src/electrostatics.jl:331-342 ------------------------------------- */
-static void es_energy(const or_system *s, const double *gq_xf, or_eikr *e, int use_sk, double *sr, double *lr) {
+static void es_energy(const or_system *s, const double *gq_xf, or_eikr *e, int use_sk, double *sr, double *lr,
+                      double *sr_mag) {
     double tsr = 0.0, tlr = 0.0;
+    if (sr_mag) *sr_mag = 0.0;
     for (int c = 0; c < s->n_gq; c++) {
-        double psr, plr;
-        if (use_sk) phi_sk(s, gq_xf + 3 * c, &psr, &plr);
+        double psr, plr, m = 0.0;
+        if (use_sk) { phi_sk(s, gq_xf + 3 * c, &psr, &plr, &m); if (sr_mag) *sr_mag += fabs(s->g_q[c]) * m; }
         else phi_direct(s, gq_xf + 3 * c, e, &psr, &plr);
         tsr += s->g_q[c] * psr;
         tlr += s->g_q[c] * plr;
@@ -415,12 +429,24 @@ static void es_energy(const or_system *s, const double *gq_xf, or_eikr *e, int u
     *sr = tsr; *lr = tlr;
 }
 
+void or_energies_scaled(or_system *s, int64_t n_conf, const double *lj_xf, const double *q_xf,
+                        int charged, int use_sk, int nthreads, double *out_vdw, double *out_sr,
+                        double *out_lr, double *scale_vdw, double *scale_sr);
+
 /* Batched single-configuration energies: for each configuration, the guest's
  * LJ sites (n_glj x 3 frac) and charges (n_gq x 3 frac).  es only when
  * `charged` (henry.jl:93,227-229).  out_vdw may be +Inf (overlap). */
 void or_energies(or_system *s, int64_t n_conf, const double *lj_xf, const double *q_xf,
                  int charged, int use_sk, int nthreads,
                  double *out_vdw, double *out_sr, double *out_lr) {
+    or_energies_scaled(s, n_conf, lj_xf, q_xf, charged, use_sk, nthreads, out_vdw, out_sr, out_lr, NULL, NULL);
+}
+
+/* Same, plus the magnitude scales Σ|LJ repulsive| + Σ|LJ attractive| and Σ|q_g| Σ|real-space
+ * term| (S(k) form only) that bound the rounding error of an FP32 evaluation. */
+void or_energies_scaled(or_system *s, int64_t n_conf, const double *lj_xf, const double *q_xf,
+                        int charged, int use_sk, int nthreads, double *out_vdw, double *out_sr,
+                        double *out_lr, double *scale_vdw, double *scale_sr) {
     if (charged && use_sk && !s->sk_re) or_structure_factor(s);
 #ifdef _OPENMP
     if (nthreads <= 0) nthreads = omp_get_max_threads();
@@ -433,10 +459,13 @@ void or_energies(or_system *s, int64_t n_conf, const double *lj_xf, const double
 #pragma omp for schedule(dynamic, 4)
 #endif
         for (int64_t i = 0; i < n_conf; i++) {
-            out_vdw[i] = or_vdw_energy_sys(s, lj_xf + 3 * s->n_glj * i);
+            double vm = 0.0, sm = 0.0;
+            out_vdw[i] = vdw_energy_scaled(s, lj_xf + 3 * s->n_glj * i, &vm);
             double sr = 0.0, lr = 0.0;
-            if (charged) es_energy(s, q_xf + 3 * s->n_gq * i, &e, use_sk, &sr, &lr);
+            if (charged) es_energy(s, q_xf + 3 * s->n_gq * i, &e, use_sk, &sr, &lr, &sm);
             out_sr[i] = sr; out_lr[i] = lr;
+            if (scale_vdw) scale_vdw[i] = vm;
+            if (scale_sr) scale_sr[i] = sm;
         }
         if (charged && !use_sk) eikr_free(&e);
     }

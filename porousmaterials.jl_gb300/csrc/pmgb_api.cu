@@ -1,9 +1,9 @@
 // pmgb_api.cu -- the extern "C" boundary of libpmgb (declared in include/pmgb.h).
 //
 // Host-side preparation of a system: wrap and species-sort the replicated framework
-// into padded float4 segments, merge framework charges onto LJ sites that share their
+// into fixed-point int4 segments, merge framework charges onto LJ sites that share their
 // coordinates, merge guest LJ sites and charges, build per (segment, site) LJ
-// parameters, group Ewald k-vectors into kc rows; then launches and status checks.
+// parameters, group Ewald k-vectors into kc half-rows; then launches and status checks.
 #include "pmgb.h"
 #include "pmgb_internal.h"
 
@@ -49,7 +49,7 @@ struct pmgb_system {
     pmgb_ctx* ctx = nullptr;
     SysDev dev{};
     // device allocations
-    float4* d_rec = nullptr;
+    int4* d_rec = nullptr;
     SegDesc* d_seg = nullptr;
     SitePar* d_segpar = nullptr;
     uint32_t* d_qfix = nullptr;
@@ -58,8 +58,9 @@ struct pmgb_system {
     KRow* d_krow = nullptr;
     float2* d_skw = nullptr;
     double* d_sk = nullptr;
-    int* d_kabc = nullptr;
+    int* d_kabc = nullptr;          // k-vectors in half-row traversal order
     double* d_wt = nullptr;
+    std::vector<int> k_order;       // traversal position -> caller's k index
     int n_k = 0;
     bool ewald_set = false;
     int n_sites = 0;
@@ -114,6 +115,12 @@ int upload(pmgb_ctx* ctx, T** dst, const std::vector<T>& v, int64_t* counter = n
     if (!v.empty())
         PMGB_CK(ctx, cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
     return PMGB_OK;
+}
+
+// fractional coordinate -> 32-bit fixed point (x * 2^32 mod 2^32), exact rounding in FP64
+uint32_t to_fix(double x) {
+    const double u = x - std::floor(x);
+    return static_cast<uint32_t>(static_cast<uint64_t>(std::llround(u * 4294967296.0)) & 0xffffffffull);
 }
 
 // Read back and clear the device status word; synchronises the stream.
@@ -353,14 +360,13 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
             recs.push_back(Rec{std::get<0>(key), std::get<1>(key), std::get<2>(key), charge_q[c], -1});
         }
     }
-    // species-sorted segments, each padded with NaN records to PMGB_SEG_ALIGN
+    // species-sorted contiguous segments of fixed-point records
     std::vector<int> order(recs.size());
     for (size_t i = 0; i < recs.size(); ++i) order[i] = static_cast<int>(i);
     auto sp_key = [&](int i) { return recs[i].species < 0 ? n_species : recs[i].species; };
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sp_key(a) < sp_key(b); });
-    std::vector<float4> h_rec;
+    std::vector<int4> h_rec;
     std::vector<SegDesc> h_seg;
-    const float qnan = std::nanf("");
     for (size_t p = 0; p < order.size();) {
         const int sp = recs[order[p]].species;
         size_t e = p;
@@ -369,10 +375,12 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
         d.lo = static_cast<int>(h_rec.size());
         for (size_t k = p; k < e; ++k) {
             const Rec& r = recs[order[k]];
-            h_rec.push_back(make_float4(static_cast<float>(r.x), static_cast<float>(r.y), static_cast<float>(r.z),
-                                        static_cast<float>(r.q)));
+            const float qf = static_cast<float>(r.q);
+            int qbits;
+            std::memcpy(&qbits, &qf, sizeof(qbits));
+            h_rec.push_back(make_int4(static_cast<int>(to_fix(r.x)), static_cast<int>(to_fix(r.y)),
+                                      static_cast<int>(to_fix(r.z)), qbits));
         }
-        while (h_rec.size() % PMGB_SEG_ALIGN) h_rec.push_back(make_float4(qnan, qnan, qnan, 0.0f));
         d.hi = static_cast<int>(h_rec.size());
         d.species = sp;
         d.has_lj = sp >= 0;
@@ -444,10 +452,7 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     std::vector<uint32_t> h_qfix;
     std::vector<double> h_q;
     for (int c = 0; c < n_charges; ++c) {
-        for (int d = 0; d < 3; ++d) {
-            const double u = wrap01(charge_xf[3 * c + d]);
-            h_qfix.push_back(static_cast<uint32_t>(static_cast<uint64_t>(std::llround(u * 4294967296.0)) & 0xffffffffull));
-        }
+        for (int d = 0; d < 3; ++d) h_qfix.push_back(to_fix(charge_xf[3 * c + d]));
         h_q.push_back(charge_q[c]);
     }
     s->n_q = n_charges;
@@ -475,12 +480,19 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     D.n_seg = static_cast<int>(h_seg.size());
     D.seg = s->d_seg;
     D.segpar = s->d_segpar;
-    D.h00 = static_cast<float>(R[0]);
-    D.h01 = static_cast<float>(R[3]);
-    D.h02 = static_cast<float>(R[6]);
-    D.h11 = static_cast<float>(R[4]);
-    D.h12 = static_cast<float>(R[7]);
-    D.h22 = static_cast<float>(R[8]);
+    const double fix_unit = 1.0 / 4294967296.0;  // one fixed-point step of a fractional coordinate
+    D.h00 = static_cast<float>(R[0] * fix_unit);
+    D.h01 = static_cast<float>(R[3] * fix_unit);
+    D.h02 = static_cast<float>(R[6] * fix_unit);
+    D.h11 = static_cast<float>(R[4] * fix_unit);
+    D.h12 = static_cast<float>(R[7] * fix_unit);
+    D.h22 = static_cast<float>(R[8] * fix_unit);
+    D.p00 = static_cast<float>(R[0] * fix_unit - static_cast<double>(D.h00));
+    D.p01 = static_cast<float>(R[3] * fix_unit - static_cast<double>(D.h01));
+    D.p02 = static_cast<float>(R[6] * fix_unit - static_cast<double>(D.h02));
+    D.p11 = static_cast<float>(R[4] * fix_unit - static_cast<double>(D.h11));
+    D.p12 = static_cast<float>(R[7] * fix_unit - static_cast<double>(D.h12));
+    D.p22 = static_cast<float>(R[8] * fix_unit - static_cast<double>(D.h22));
     D.g00 = static_cast<float>(G[0]);
     D.g01 = static_cast<float>(G[3]);
     D.g02 = static_cast<float>(G[6]);
@@ -520,20 +532,44 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
     if (n_kvecs < 0 || (n_kvecs > 0 && (!kvec_abc || !kvec_wt)))
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "bad k-vector arrays");
     PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    for (int k = 0; k < n_kvecs; ++k)
+        if (!std::isfinite(kvec_wt[k])) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "k-vector %d weight not finite", k);
+    // group runs of constant (ka, kb) and consecutive kc, then split each run at kc = 0 into
+    // half-rows that start at the kc nearest 0 and step outward
     std::vector<KRow> rows;
-    std::vector<int> kabc(kvec_abc, kvec_abc + 3 * static_cast<size_t>(n_kvecs));
-    std::vector<double> wt(kvec_wt, kvec_wt + n_kvecs);
-    for (int k = 0; k < n_kvecs; ++k) {
-        if (!std::isfinite(wt[k])) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "k-vector %d weight not finite", k);
-        const int ka = kabc[3 * k], kb = kabc[3 * k + 1], kc = kabc[3 * k + 2];
-        if (!rows.empty()) {
-            KRow& r = rows.back();
-            if (r.ka == ka && r.kb == kb && r.kc0 + r.n == kc) {
+    std::vector<int> order;
+    std::vector<int> kabc;
+    std::vector<double> wt;
+    for (int k = 0; k < n_kvecs;) {
+        const int ka = kvec_abc[3 * k], kb = kvec_abc[3 * k + 1], lo = kvec_abc[3 * k + 2];
+        int e = k + 1;
+        while (e < n_kvecs && kvec_abc[3 * e] == ka && kvec_abc[3 * e + 1] == kb &&
+               kvec_abc[3 * e + 2] == kvec_abc[3 * (e - 1) + 2] + 1)
+            ++e;
+        const int hi = lo + (e - k) - 1;
+        auto add_row = [&](int kc_start, int kc_end, int dir) {
+            KRow r{ka, kb, kc_start, 0, static_cast<int>(order.size()), dir, 0, 0};
+            for (int kc = kc_start;; kc += dir) {
+                const int idx = k + (kc - lo);
+                order.push_back(idx);
+                kabc.push_back(ka);
+                kabc.push_back(kb);
+                kabc.push_back(kc);
+                wt.push_back(kvec_wt[idx]);
                 ++r.n;
-                continue;
+                if (kc == kc_end) break;
             }
+            rows.push_back(r);
+        };
+        if (lo >= 0) {
+            add_row(lo, hi, +1);
+        } else if (hi < 0) {
+            add_row(hi, lo, -1);
+        } else {
+            add_row(0, hi, +1);
+            add_row(-1, lo, -1);
         }
-        rows.push_back(KRow{ka, kb, kc, 1, k, 0, 0, 0});
+        k = e;
     }
     // drop previous Ewald state
     void* old[] = {s->d_krow, s->d_skw, s->d_sk, s->d_kabc, s->d_wt};
@@ -554,6 +590,7 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
                                               s->d_skw, ctx->stream));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
     s->n_k = n_kvecs;
+    s->k_order = order;
     s->ewald_set = true;
     s->dev.alpha = static_cast<float>(alpha);
     s->dev.rc2e = static_cast<float>(sr_cutoff * sr_cutoff);
@@ -599,9 +636,15 @@ extern "C" int pmgb_structure_factor(pmgb_system* s, double* sk_out) {
     pmgb_ctx* ctx = s->ctx;
     if (!s->ewald_set) return fail(ctx, PMGB_ERR_NOT_READY, "pmgb_structure_factor: Ewald parameters not set");
     PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    std::vector<double> trav(2 * static_cast<size_t>(s->n_k));
     if (s->n_k > 0)
-        PMGB_CK(ctx, cudaMemcpyAsync(sk_out, s->d_sk, 2 * sizeof(double) * s->n_k, cudaMemcpyDeviceToHost, ctx->stream));
+        PMGB_CK(ctx, cudaMemcpyAsync(trav.data(), s->d_sk, 2 * sizeof(double) * s->n_k, cudaMemcpyDeviceToHost,
+                                     ctx->stream));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < s->n_k; ++i) {
+        sk_out[2 * s->k_order[i]] = trav[2 * i];
+        sk_out[2 * s->k_order[i] + 1] = trav[2 * i + 1];
+    }
     return PMGB_OK;
 }
 
@@ -632,21 +675,27 @@ extern "C" int pmgb_energies(pmgb_system* s, int64_t n_conf, const double* site_
     if (n_conf > (int64_t(1) << 31) * PMGB_THREADS / 2)
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energies: n_conf too large");
     PMGB_CK(ctx, cudaSetDevice(ctx->device));
-    const size_t in_bytes = sizeof(double) * 3 * s->n_sites * static_cast<size_t>(n_conf);
+    const size_t n_coord = 3 * static_cast<size_t>(s->n_sites) * static_cast<size_t>(n_conf);
+    for (size_t i = 0; i < n_coord; ++i)
+        if (!std::isfinite(site_xf[i]))
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energies: non-finite site coordinate at %zu", i);
+    std::vector<uint32_t> fix(n_coord);
+    for (size_t i = 0; i < n_coord; ++i) fix[i] = to_fix(site_xf[i]);
+    const size_t in_bytes = sizeof(uint32_t) * n_coord;
     const size_t out_bytes = sizeof(double) * 3 * static_cast<size_t>(n_conf);
     int rc;
     if ((rc = ensure(ctx, s->in_buf, in_bytes)) || (rc = ensure(ctx, s->out_buf, out_bytes))) return rc;
-    PMGB_CK(ctx, cudaMemcpyAsync(s->in_buf.p, site_xf, in_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    PMGB_CK(ctx, cudaMemcpyAsync(s->in_buf.p, fix.data(), in_bytes, cudaMemcpyHostToDevice, ctx->stream));
     LaunchArgs a = base_args(s);
     a.pose_mode = POSE_SITES;
     a.out_mode = OUT_ENERGY;
-    a.site_xf = static_cast<const double*>(s->in_buf.p);
+    a.site_fix = static_cast<const uint32_t*>(s->in_buf.p);
     a.n_conf = n_conf;
     a.e_out = static_cast<double*>(s->out_buf.p);
     const int n_ctas = static_cast<int>((n_conf + PMGB_THREADS - 1) / PMGB_THREADS);
     PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
     PMGB_CK(ctx, cudaMemcpyAsync(out, s->out_buf.p, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
-    return check_status(ctx);
+    return check_status(ctx);  // synchronises: the host staging vector outlives the copy
 }
 
 extern "C" int pmgb_widom_device(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
@@ -722,17 +771,18 @@ extern "C" int pmgb_sample_poses(pmgb_ctx* ctx, uint64_t seed, int64_t start, in
 
 static int grid_axes(pmgb_system* s, const int32_t n_pts[3], const int32_t rep[3]) {
     pmgb_ctx* ctx = s->ctx;
-    std::vector<float> ax;
+    std::vector<uint32_t> ax;
     for (int d = 0; d < 3; ++d)
         for (int i = 0; i < n_pts[d]; ++i) {
             double f = (n_pts[d] > 1) ? static_cast<double>(i) / static_cast<double>(n_pts[d] - 1) : 0.0;
             // the end plane (f = 1) is the periodic image of the first one: evaluate the
             // identical position so both planes hold bit-identical energies
             if (f >= 1.0) f -= 1.0;
-            ax.push_back(static_cast<float>(f / rep[d]));
+            ax.push_back(to_fix(f / rep[d]));
         }
-    if (int rc = ensure(ctx, s->axes, sizeof(float) * ax.size())) return rc;
-    PMGB_CK(ctx, cudaMemcpyAsync(s->axes.p, ax.data(), sizeof(float) * ax.size(), cudaMemcpyHostToDevice, ctx->stream));
+    if (int rc = ensure(ctx, s->axes, sizeof(uint32_t) * ax.size())) return rc;
+    PMGB_CK(ctx, cudaMemcpyAsync(s->axes.p, ax.data(), sizeof(uint32_t) * ax.size(), cudaMemcpyHostToDevice,
+                                 ctx->stream));
     // the staging vector is released on return: make the copy complete first
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
     return PMGB_OK;
@@ -762,7 +812,7 @@ extern "C" int pmgb_energy_grid_device(pmgb_system* s, const int32_t n_pts[3], c
     a.pose_mode = POSE_GRID;
     a.out_mode = OUT_GRID;
     for (int d = 0; d < 3; ++d) a.n_pts[d] = n_pts[d];
-    const float* ax = static_cast<const float*>(s->axes.p);
+    const uint32_t* ax = static_cast<const uint32_t*>(s->axes.p);
     a.grid_x = ax;
     a.grid_y = ax + n_pts[0];
     a.grid_z = ax + n_pts[0] + n_pts[1];

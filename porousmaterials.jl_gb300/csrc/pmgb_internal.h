@@ -1,22 +1,22 @@
 // pmgb_internal.h -- device data layout shared by the kernels and the C-ABI layer.
 //
 // Layout in HBM (all owned by a pmgb_system):
-//   rec[n_rec]      float4 (xf, yf, zf, q) of every framework site of the replicated
-//                   crystal, sorted by LJ species; each species segment starts on a
-//                   multiple of PMGB_SEG_ALIGN and is padded with NaN records (which
-//                   fail every cutoff comparison and so contribute nothing).
+//   rec[n_rec]      int4 (x, y, z, q) of every framework site of the replicated crystal:
+//                   fractional coordinates as 32-bit fixed point (x * 2^32 mod 2^32) and
+//                   the charge as FP32 bits, sorted by LJ species into contiguous segments.
 //   seg[n_seg]      [lo, hi) record range of each species segment.
 //   segpar[n_seg * PMGB_MAX_SITES]  per (segment, guest site): sigma^2, 4*epsilon,
 //                   overlap radius^2 (0.1, or -1 when the pair has no LJ term).
-//   krow[n_krow]    k-vectors grouped in rows of constant (ka, kb) and consecutive kc.
-//   skw[n_k]        wt_k * S(k), FP32 (re, im), S(k) built on the device in FP64.
+//   krow[n_krow]    k-vectors grouped in half-rows of constant (ka, kb) running outward in
+//                   kc from the kc nearest 0.
+//   skw[n_k]        wt_k * S(k) in half-row traversal order, FP32 (re, im); S(k) is
+//                   accumulated on the device in FP64.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
 
 #define PMGB_MAX_SITES 8      // guest sites (merged LJ atoms + point charges)
 #define PMGB_MAX_SEG 64       // framework species segments
-#define PMGB_SEG_ALIGN 4      // record alignment of a species segment
 #define PMGB_TILE 2048        // framework records per shared-memory stage (32 KB)
 #define PMGB_NSTAGE 3         // stages in the TMA ring
 #define PMGB_THREADS 256      // insertions per CTA (one per thread)
@@ -26,7 +26,7 @@
 #define PMGB_DEVERR_BAD_ARGS 0x2u
 
 struct SegDesc {
-    int lo, hi;        // record range [lo, hi), both multiples of PMGB_SEG_ALIGN
+    int lo, hi;        // record range [lo, hi)
     int species;       // species id in the caller's force-field table (-1: charge-only sites)
     int has_lj;
 };
@@ -36,20 +36,23 @@ struct SitePar {
 };
 
 struct KRow {
-    int ka, kb, kc0, n;   // k = (ka, kb, kc0 .. kc0+n-1)
-    int off;              // index of the first k-vector of the row in skw
-    int pad0, pad1, pad2;
+    int ka, kb, kc0, n;   // k = (ka, kb, kc0 + dir * m) for m = 0 .. n-1
+    int off;              // index of the first k-vector of the row in skw (traversal order)
+    int dir;              // +1 or -1
+    int pad1, pad2;
 };
 
 // Everything a kernel needs to know about one (framework, guest) system.
 struct SysDev {
-    const float4* rec;
+    const int4* rec;
     int n_rec, n_tiles;
     int n_seg;
     const SegDesc* seg;
     const SitePar* segpar;
-    // upper-triangular f_to_c (Cartesian = H * fractional) and c_to_f, FP32
+    // upper-triangular f_to_c scaled by 2^-32 (Cartesian = H' * fixed-point displacement)
+    // and c_to_f (unscaled), FP32
     float h00, h01, h02, h11, h12, h22;
+    float p00, p01, p02, p11, p12, p22;   // FP32 residual of the scaled f_to_c (h + p = FP64 value)
     float g00, g01, g02, g11, g12, g22;
     float rc2;                     // LJ cutoff radius^2 (ljff.r²_cutoff)
     float rc2e;                    // Ewald real-space cutoff radius^2
@@ -100,14 +103,14 @@ struct LaunchArgs {
     LsePartial* partials;        // [n_blocks * ctas_per_block]
     double* u_out;               // optional: [n_total * 2] (U_vdw, U_es)
     // explicit sites (POSE_SITES)
-    const double* site_xf;       // [n_conf * n_sites * 3]
+    const uint32_t* site_fix;    // [n_conf * n_sites * 3] fixed-point fractional coordinates
     long long n_conf;
     double* e_out;               // [n_conf * 3] (vdw, sr, lr)
     // grid (POSE_GRID)
     int n_pts[3];
-    const float* grid_x;         // fractional coordinate of each grid plane, per axis,
-    const float* grid_y;         //   already divided by the replication factor
-    const float* grid_z;
+    const uint32_t* grid_x;      // fixed-point fractional coordinate of each grid plane, per
+    const uint32_t* grid_y;      //   axis, already divided by the replication factor
+    const uint32_t* grid_z;
     float unit_factor;
     float* grid_out;
     // status

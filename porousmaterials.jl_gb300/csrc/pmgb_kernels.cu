@@ -1,8 +1,11 @@
 // pmgb_kernels.cu -- sm_103a kernels for the Widom-insertion / energy-grid path.
 //
 // One thread owns one insertion (or one grid point / explicit configuration) and
-// keeps its guest sites in registers.  The CTA streams the replicated framework
-// (species-sorted float4 records) through a ring of shared-memory stages filled by
+// keeps its guest sites in registers.  Fractional coordinates are 32-bit fixed point
+// (x * 2^32 mod 2^32): the wrapping integer difference of two positions is exactly the
+// minimum-image fractional displacement (|d| <= 1/2), converted once to FP32 with a
+// single rounding.  The CTA streams the replicated framework (species-sorted int4
+// records: x, y, z fixed point, q as float bits) through a ring of shared-memory stages filled by
 // 1-D TMA bulk copies (cp.async.bulk + mbarrier complete_tx); every thread of the
 // CTA reads each record with a broadcast shared load and evaluates it against all
 // of its guest sites.  Pair math is FP32; per-insertion sums are compensated
@@ -26,7 +29,6 @@
 
 namespace {
 
-constexpr float kMagic = 12582912.0f;   // 1.5 * 2^23: (x + M) - M == rint(x) for |x| < 2^22
 constexpr int kChunk = 64;              // records per compensated fold
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s bound on any mbarrier wait
 
@@ -139,100 +141,249 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
     lo = __fadd_rn(lo, e);
 }
 
-// minimum image of a fractional difference (|d| < 2^22): d - rint(d)
-__device__ __forceinline__ float min_image(float d) {
-    return __fsub_rn(d, __fsub_rn(__fadd_rn(d, kMagic), kMagic));
+// FP32 fractional coordinate -> 32-bit fixed point, wrapping modulo 1
+__device__ __forceinline__ uint32_t frac2fix(float x) {
+    return static_cast<uint32_t>(__float2ll_rn(x * 4294967296.0f));
 }
 
 struct Geo {
-    float h00, h01, h02, h11, h12, h22, rc2, rc2e, alpha;
+    // f_to_c scaled by 2^-32 as an FP32 value h plus its FP32 residual p (h + p equals the
+    // FP64 matrix to ~1e-15), so that Cartesian = (h + p) * fixed-point displacement
+    float h00, h01, h02, h11, h12, h22;
+    float p00, p01, p02, p11, p12, p22;
+    float rc2, rc2e, alpha;
 };
+
+// erfc(x) for x >= 0: t exp(-x^2) Q(3t - 2) with t = 1/(1 + x/2) and Q the degree-7
+// polynomial of csrc/fit_erfc.py (max relative error 3.3e-7 on [0, 3.2]).
+__device__ __forceinline__ float erfc_fit(float x) {
+    const float t = __fdividef(1.0f, fmaf(0.5f, x, 1.0f));
+    const float y = fmaf(t, 3.0f, -2.0f);
+    float q = -1.1504688e-05f;
+    q = fmaf(q, y, 0.00012701178f);
+    q = fmaf(q, y, 1.719709e-05f);
+    q = fmaf(q, y, -0.002622572f);
+    q = fmaf(q, y, 0.00045600548f);
+    q = fmaf(q, y, 0.06661939f);
+    q = fmaf(q, y, 0.29403913f);
+    q = fmaf(q, y, 0.6413754f);
+    float e;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(x * (x * -1.4426950408889634f)));
+    return q * t * e;
+}
+
+// Cartesian squared distance of a fixed-point fractional displacement
+__device__ __forceinline__ float dist2(const int4 r, const uint32_t ux, const uint32_t uy, const uint32_t uz,
+                                       const Geo& g) {
+    // the wrapping difference is the minimum-image displacement in units of 2^-32
+    const float dx = __int2float_rn(static_cast<int>(static_cast<uint32_t>(r.x) - ux));
+    const float dy = __int2float_rn(static_cast<int>(static_cast<uint32_t>(r.y) - uy));
+    const float dz = __int2float_rn(static_cast<int>(static_cast<uint32_t>(r.z) - uz));
+    const float rx = fmaf(g.p00, dx, fmaf(g.p01, dy, g.p02 * dz));
+    const float ry = fmaf(g.p11, dy, g.p12 * dz);
+    const float rz = g.p22 * dz;
+    const float cx = fmaf(g.h00, dx, fmaf(g.h01, dy, fmaf(g.h02, dz, rx)));
+    const float cy = fmaf(g.h11, dy, fmaf(g.h12, dz, ry));
+    const float cz = fmaf(g.h22, dz, rz);
+    return fmaf(cx, cx, fmaf(cy, cy, cz * cz));
+}
 
 // One framework record against one guest site.
 template <bool CHARGED>
-__device__ __forceinline__ void pair_fwd(const float4 r, const float sx, const float sy, const float sz,
+__device__ __forceinline__ void pair_fwd(const int4 r, const uint32_t ux, const uint32_t uy, const uint32_t uz,
                                          const Geo& g, const float sig2, const float eps4, float& segmin,
                                          float& ljp, float& php) {
-    float dx = min_image(__fsub_rn(r.x, sx));
-    float dy = min_image(__fsub_rn(r.y, sy));
-    float dz = min_image(__fsub_rn(r.z, sz));
-    const float cx = fmaf(g.h00, dx, fmaf(g.h01, dy, g.h02 * dz));
-    const float cy = fmaf(g.h11, dy, g.h12 * dz);
-    const float cz = g.h22 * dz;
-    const float r2 = fmaf(cx, cx, fmaf(cy, cy, cz * cz));
+    const float r2 = dist2(r, ux, uy, uz, g);
     segmin = fminf(segmin, r2);
-    const bool in = r2 < g.rc2;  // false for NaN padding records
-    float ir2, ri = 0.0f;
+    const bool in = r2 < g.rc2;
+    float ir2, y = 0.0f;
     if (CHARGED) {
-        ri = rsqrtf(r2);
-        ir2 = ri * ri;
+        // rsqrt estimate refined by one Newton step: y <- y + y/2 (1 - r2 y^2)
+        y = rsqrtf(r2);
+        const float e = fmaf(-r2 * y, y, 1.0f);
+        y = fmaf(0.5f * y, e, y);
+        ir2 = y * y;
     } else {
-        ir2 = __fdividef(1.0f, r2);
+        ir2 = __frcp_rn(r2);
     }
     const float s = sig2 * ir2;
     const float s3 = s * s * s;
     const float t = fmaf(s3, s3, -s3);
     ljp = fmaf(eps4, in ? t : 0.0f, ljp);
     if (CHARGED) {
-        const float rr = r2 * ri;
-        const float e = erfcf(g.alpha * rr) * ri;
-        php = fmaf(r.w, (r2 < g.rc2e) ? e : 0.0f, php);
+        const float e = erfc_fit(g.alpha * (r2 * y)) * y;
+        php = fmaf(__int_as_float(r.w), (r2 < g.rc2e) ? e : 0.0f, php);
     }
 }
 
-// Reciprocal-space potential at each charged site: sum_k Re[wt_k S(k) e^{-ik.x}].
-// Phases are exact in 32-bit fixed point (fractional coordinate * 2^32, wrapping
-// mod 1); each row starts from sincospif of its exact phase and steps along kc
-// by complex multiplication.
+// ---- packed (f32x2) form: two framework records against one guest site -------------
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+struct Geo2 {
+    float2 h00, h01, h02, h11, h12, h22;
+    float2 p00, p01, p02, p11, p12, p22;
+    float rc2, rc2e;
+    float2 alpha;
+};
+
+__device__ __forceinline__ float2 erfc_fit2(float2 x) {
+    const float2 a = fma2(f2(0.5f), x, f2(1.0f));
+    const float2 t = make_float2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y));
+    const float2 y = fma2(t, f2(3.0f), f2(-2.0f));
+    float2 q = f2(-1.1504688e-05f);
+    q = fma2(q, y, f2(0.00012701178f));
+    q = fma2(q, y, f2(1.719709e-05f));
+    q = fma2(q, y, f2(-0.002622572f));
+    q = fma2(q, y, f2(0.00045600548f));
+    q = fma2(q, y, f2(0.06661939f));
+    q = fma2(q, y, f2(0.29403913f));
+    q = fma2(q, y, f2(0.6413754f));
+    const float2 arg = mul2(x, mul2(x, f2(-1.4426950408889634f)));
+    float ex, ey;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ex) : "f"(arg.x));
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ey) : "f"(arg.y));
+    return mul2(mul2(q, t), make_float2(ex, ey));
+}
+
+template <bool CHARGED>
+__device__ __forceinline__ void pair2_fwd(const int4 ra, const int4 rb, const uint32_t ux, const uint32_t uy,
+                                          const uint32_t uz, const Geo2& g, const float2 sig2, const float2 eps4,
+                                          float& segmin, float2& ljp, float2& php) {
+    const float2 dx = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.x) - ux)),
+                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.x) - ux)));
+    const float2 dy = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.y) - uy)),
+                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.y) - uy)));
+    const float2 dz = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.z) - uz)),
+                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.z) - uz)));
+    const float2 rx = fma2(g.p00, dx, fma2(g.p01, dy, mul2(g.p02, dz)));
+    const float2 ry = fma2(g.p11, dy, mul2(g.p12, dz));
+    const float2 rz = mul2(g.p22, dz);
+    const float2 cx = fma2(g.h00, dx, fma2(g.h01, dy, fma2(g.h02, dz, rx)));
+    const float2 cy = fma2(g.h11, dy, fma2(g.h12, dz, ry));
+    const float2 cz = fma2(g.h22, dz, rz);
+    const float2 r2 = fma2(cx, cx, fma2(cy, cy, mul2(cz, cz)));
+    segmin = fminf(segmin, fminf(r2.x, r2.y));
+    float2 ir2, y = f2(0.0f);
+    if (CHARGED) {
+        y = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+        const float2 e = fma2(neg2(mul2(r2, y)), y, f2(1.0f));
+        y = fma2(mul2(f2(0.5f), y), e, y);
+        ir2 = mul2(y, y);
+    } else {
+        const float2 r0 = make_float2(__fdividef(1.0f, r2.x), __fdividef(1.0f, r2.y));
+        const float2 e = fma2(neg2(r2), r0, f2(1.0f));
+        ir2 = fma2(r0, e, r0);
+    }
+    const float2 s = mul2(sig2, ir2);
+    const float2 s3 = mul2(mul2(s, s), s);
+    const float2 t = fma2(s3, s3, neg2(s3));
+    ljp = fma2(eps4, make_float2(r2.x < g.rc2 ? t.x : 0.0f, r2.y < g.rc2 ? t.y : 0.0f), ljp);
+    if (CHARGED) {
+        const float2 e = mul2(erfc_fit2(mul2(g.alpha, mul2(r2, y))), y);
+        php = fma2(make_float2(__int_as_float(ra.w), __int_as_float(rb.w)),
+                   make_float2(r2.x < g.rc2e ? e.x : 0.0f, r2.y < g.rc2e ? e.y : 0.0f), php);
+    }
+}
+
+// Reciprocal-space energy of the whole guest, sum_k Re[wt_k S(k) G(k)] with
+// G(k) = sum_g q_g e^{-ik.x_g} = e^{-ik.x_0} (q_tot + sum_g q_g (e^{-ik.(x_g - x_0)} - 1)).
+// Combining the guest's charges per k before multiplying by the (large) wt_k S(k) keeps
+// the sum free of the cancellation between per-site potentials of a neutral molecule;
+// D_g = e^{-ik.d_g} - 1 is carried by the recurrence D <- D w + (w - 1), whose error is
+// relative to |D|.  Phases are exact 32-bit fixed-point turns.  Rows of constant (ka, kb)
+// start at the kc nearest 0 and step outward in kc by `dir`.
 template <int NS>
-__device__ __forceinline__ void kspace_fwd(const SysDev& S, const float sx[NS], const float sy[NS],
-                                           const float sz[NS], float plr_hi[NS], float plr_lo[NS]) {
-    uint32_t Ua[NS], Ub[NS], Uc[NS];
-    float wr[NS], wi[NS];
+__device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua[NS], const uint32_t Ub[NS],
+                                           const uint32_t Uc[NS], float& plr_hi, float& plr_lo) {
+    constexpr float kTurn = 4.656612873077393e-10f;  // 2^-31: int32 fixed point -> half turns
+    plr_hi = 0.0f;
+    plr_lo = 0.0f;
+    // offsets of sites 1.. from site 0 (exact small integers) and their charges
+    int da[NS], db[NS], dc[NS];
+    float qg[NS];
+    float qtot = 0.0f;
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
-        plr_hi[k] = 0.0f;
-        plr_lo[k] = 0.0f;
-        // sites past n_sites are NaN placeholders with zero charge: give them phase 0
-        const bool real = k < S.n_sites;
-        const float fa = real ? sx[k] - floorf(sx[k]) : 0.0f;
-        const float fb = real ? sy[k] - floorf(sy[k]) : 0.0f;
-        const float fc = real ? sz[k] - floorf(sz[k]) : 0.0f;
-        Ua[k] = static_cast<uint32_t>(static_cast<unsigned long long>(static_cast<double>(fa) * 4294967296.0));
-        Ub[k] = static_cast<uint32_t>(static_cast<unsigned long long>(static_cast<double>(fb) * 4294967296.0));
-        Uc[k] = static_cast<uint32_t>(static_cast<unsigned long long>(static_cast<double>(fc) * 4294967296.0));
+        da[k] = static_cast<int>(Ua[k] - Ua[0]);
+        db[k] = static_cast<int>(Ub[k] - Ub[0]);
+        dc[k] = static_cast<int>(Uc[k] - Uc[0]);
+        qg[k] = (k < S.n_sites) ? S.q[k] : 0.0f;
+        qtot += qg[k];
+    }
+    // step factors along +kc: w0 = e^{-2 pi i uc0} for site 0; for site g: wd = e^{-2 pi i dc_g},
+    // dw = wd - 1 = (-2 sin^2(pi dc), -sin(2 pi dc)) evaluated without cancellation
+    float w0r, w0i;
+    {
         float sn, cs;
-        sincospif(static_cast<float>(static_cast<int32_t>(Uc[k])) * 4.656612873077393e-10f, &sn, &cs);
-        wr[k] = cs;
-        wi[k] = -sn;
+        sincospif(static_cast<float>(static_cast<int32_t>(Uc[0])) * kTurn, &sn, &cs);
+        w0r = cs;
+        w0i = -sn;
+    }
+    float wdr[NS], wdi[NS], dwr[NS], dwi[NS];
+#pragma unroll
+    for (int k = 1; k < NS; ++k) {
+        float sn, cs;
+        sincospif(static_cast<float>(dc[k]) * (0.5f * kTurn), &sn, &cs);  // half angle
+        dwr[k] = -2.0f * sn * sn;
+        dwi[k] = -2.0f * sn * cs;
+        wdr[k] = 1.0f + dwr[k];
+        wdi[k] = dwi[k];
     }
     for (int row = 0; row < S.n_krow; ++row) {
         const KRow R = S.krow[row];
-        float er[NS], ei[NS], part[NS];
-#pragma unroll
-        for (int k = 0; k < NS; ++k) {
-            const uint32_t P = static_cast<uint32_t>(R.ka) * Ua[k] + static_cast<uint32_t>(R.kb) * Ub[k] +
-                               static_cast<uint32_t>(R.kc0) * Uc[k];
+        const float sgn = static_cast<float>(R.dir);  // +1 or -1: direction along kc
+        // site-0 phasor at the row start
+        float er, ei;
+        {
+            const uint32_t P = static_cast<uint32_t>(R.ka) * Ua[0] + static_cast<uint32_t>(R.kb) * Ub[0] +
+                               static_cast<uint32_t>(R.kc0) * Uc[0];
             float sn, cs;
-            sincospif(static_cast<float>(static_cast<int32_t>(P)) * 4.656612873077393e-10f, &sn, &cs);
-            er[k] = cs;
-            ei[k] = -sn;
-            part[k] = 0.0f;
+            sincospif(static_cast<float>(static_cast<int32_t>(P)) * kTurn, &sn, &cs);
+            er = cs;
+            ei = -sn;
         }
+        const float sw0i = sgn * w0i;  // conj for the downward direction
+        float Dr[NS], Di[NS], swdi[NS], sdwi[NS];
+#pragma unroll
+        for (int k = 1; k < NS; ++k) {
+            const int p = R.ka * da[k] + R.kb * db[k] + R.kc0 * dc[k];
+            float sn, cs;
+            sincospif(static_cast<float>(p) * (0.5f * kTurn), &sn, &cs);  // half angle
+            Dr[k] = -2.0f * sn * sn;
+            Di[k] = -2.0f * sn * cs;
+            swdi[k] = sgn * wdi[k];
+            sdwi[k] = sgn * dwi[k];
+        }
+        float part = 0.0f;
         const float2* sw = S.skw + R.off;
         for (int m = 0; m < R.n; ++m) {
             const float2 w = __ldg(sw + m);
+            // H = q_tot + sum_g q_g D_g
+            float hr = qtot, hi = 0.0f;
 #pragma unroll
-            for (int k = 0; k < NS; ++k) {
-                part[k] = fmaf(w.x, er[k], fmaf(-w.y, ei[k], part[k]));
-                const float nr = fmaf(er[k], wr[k], -ei[k] * wi[k]);
-                const float ni = fmaf(er[k], wi[k], ei[k] * wr[k]);
-                er[k] = nr;
-                ei[k] = ni;
+            for (int k = 1; k < NS; ++k) {
+                hr = fmaf(qg[k], Dr[k], hr);
+                hi = fmaf(qg[k], Di[k], hi);
+            }
+            // T = wt S e^{-ik.x0};  part += Re[T H]
+            const float tr = fmaf(w.x, er, -w.y * ei);
+            const float ti = fmaf(w.x, ei, w.y * er);
+            part = fmaf(tr, hr, fmaf(-ti, hi, part));
+            // advance one step in kc
+            const float nr = fmaf(er, w0r, -ei * sw0i);
+            ei = fmaf(er, sw0i, ei * w0r);
+            er = nr;
+#pragma unroll
+            for (int k = 1; k < NS; ++k) {
+                const float dr2 = fmaf(Dr[k], wdr[k], fmaf(-Di[k], swdi[k], dwr[k]));
+                Di[k] = fmaf(Dr[k], swdi[k], fmaf(Di[k], wdr[k], sdwi[k]));
+                Dr[k] = dr2;
             }
         }
-#pragma unroll
-        for (int k = 0; k < NS; ++k) two_sum_acc(plr_hi[k], plr_lo[k], part[k]);
+        two_sum_acc(plr_hi, plr_lo, part);
     }
 }
 
@@ -242,13 +393,12 @@ __device__ __forceinline__ void kspace_fwd(const SysDev& S, const float sx[NS], 
 template <int NS, bool CHARGED>
 __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_constant__ LaunchArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float4* stage = reinterpret_cast<float4*>(smem_raw);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + size_t(PMGB_NSTAGE) * PMGB_TILE * sizeof(float4));
+    int4* stage = reinterpret_cast<int4*>(smem_raw);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + size_t(PMGB_NSTAGE) * PMGB_TILE * sizeof(int4));
     __shared__ LsePartial red[PMGB_THREADS / 32];
 
     const SysDev& S = a.sys;
     const int tid = threadIdx.x;
-    const float qnan = __int_as_float(0x7fffffff);
 
     // ---- which item this thread owns -------------------------------------
     long long item = 0;
@@ -266,34 +416,34 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
         valid = item < static_cast<long long>(a.n_pts[0]) * a.n_pts[1] * a.n_pts[2];
     }
 
-    // ---- guest site positions (supercell fractional coordinates) ----------
-    float sx[NS], sy[NS], sz[NS];
+    // ---- guest site positions, 32-bit fixed-point fractions of the supercell ----
+    uint32_t ux[NS], uy[NS], uz[NS];
 #pragma unroll
-    for (int k = 0; k < NS; ++k) sx[k] = sy[k] = sz[k] = qnan;
+    for (int k = 0; k < NS; ++k) ux[k] = uy[k] = uz[k] = 0u;
     if (valid) {
         if (a.pose_mode == POSE_PHILOX) {
             float xf[3], R[9];
             make_pose(a.seed, static_cast<unsigned long long>(item), xf, R);
+            // the centre of mass is a 24-bit uniform: exact in fixed point
+            const uint32_t cx = frac2fix(xf[0]), cy = frac2fix(xf[1]), cz = frac2fix(xf[2]);
 #pragma unroll
             for (int k = 0; k < NS; ++k) {
-                if (k < S.n_sites) {
-                    const float bx = S.body[k][0], by = S.body[k][1], bz = S.body[k][2];
-                    const float ox = R[0] * bx + R[3] * by + R[6] * bz;
-                    const float oy = R[1] * bx + R[4] * by + R[7] * bz;
-                    const float oz = R[2] * bx + R[5] * by + R[8] * bz;
-                    sx[k] = xf[0] + (S.g00 * ox + S.g01 * oy + S.g02 * oz);
-                    sy[k] = xf[1] + (S.g11 * oy + S.g12 * oz);
-                    sz[k] = xf[2] + S.g22 * oz;
-                }
+                const float bx = S.body[k][0], by = S.body[k][1], bz = S.body[k][2];
+                const float ox = R[0] * bx + R[3] * by + R[6] * bz;
+                const float oy = R[1] * bx + R[4] * by + R[7] * bz;
+                const float oz = R[2] * bx + R[5] * by + R[8] * bz;
+                ux[k] = cx + frac2fix(S.g00 * ox + S.g01 * oy + S.g02 * oz);
+                uy[k] = cy + frac2fix(S.g11 * oy + S.g12 * oz);
+                uz[k] = cz + frac2fix(S.g22 * oz);
             }
         } else if (a.pose_mode == POSE_SITES) {
-            const double* p = a.site_xf + static_cast<size_t>(item) * S.n_sites * 3;
+            const uint32_t* p = a.site_fix + static_cast<size_t>(item) * S.n_sites * 3;
 #pragma unroll
             for (int k = 0; k < NS; ++k) {
                 if (k < S.n_sites) {
-                    sx[k] = static_cast<float>(p[3 * k + 0]);
-                    sy[k] = static_cast<float>(p[3 * k + 1]);
-                    sz[k] = static_cast<float>(p[3 * k + 2]);
+                    ux[k] = p[3 * k + 0];
+                    uy[k] = p[3 * k + 1];
+                    uz[k] = p[3 * k + 2];
                 }
             }
         } else {
@@ -301,9 +451,9 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
             const int i = static_cast<int>(item % n1);
             const int j = static_cast<int>((item / n1) % n2);
             const int kk = static_cast<int>(item / (n1 * n2));
-            sx[0] = a.grid_x[i];
-            sy[0] = a.grid_y[j];
-            sz[0] = a.grid_z[kk];
+            ux[0] = a.grid_x[i];
+            uy[0] = a.grid_y[j];
+            uz[0] = a.grid_z[kk];
         }
     }
 
@@ -319,7 +469,7 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
         const int slot = t % PMGB_NSTAGE;
         const int t0 = t * PMGB_TILE;
         const int cnt = min(PMGB_TILE, S.n_rec - t0);
-        const uint32_t bytes = static_cast<uint32_t>(cnt) * sizeof(float4);
+        const uint32_t bytes = static_cast<uint32_t>(cnt) * sizeof(int4);
         mbar_expect_tx(&bars[slot], bytes);
         bulk_g2s(stage + size_t(slot) * PMGB_TILE, S.rec + t0, bytes, &bars[slot]);
         last_issued = t;
@@ -329,11 +479,15 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
         for (int t = 0; t < n0; ++t) issue(t);
     }
 
-    const Geo g{S.h00, S.h01, S.h02, S.h11, S.h12, S.h22, S.rc2, S.rc2e, S.alpha};
-    float lj_hi = 0.0f, lj_lo = 0.0f;
-    float ph_hi[NS], ph_lo[NS];
+    const Geo g{S.h00, S.h01, S.h02, S.h11, S.h12, S.h22, S.p00, S.p01, S.p02, S.p11, S.p12, S.p22,
+                S.rc2, S.rc2e, S.alpha};
+    const Geo2 g2{f2(S.h00), f2(S.h01), f2(S.h02), f2(S.h11), f2(S.h12), f2(S.h22),
+                  f2(S.p00), f2(S.p01), f2(S.p02), f2(S.p11), f2(S.p12), f2(S.p22),
+                  S.rc2, S.rc2e, f2(S.alpha)};
+    // per-site compensated accumulators (sites past n_sites are placeholders)
+    float lj_hi[NS], lj_lo[NS], ph_hi[NS], ph_lo[NS];
 #pragma unroll
-    for (int k = 0; k < NS; ++k) ph_hi[k] = ph_lo[k] = 0.0f;
+    for (int k = 0; k < NS; ++k) lj_hi[k] = lj_lo[k] = ph_hi[k] = ph_lo[k] = 0.0f;
     bool ovl = false;
     bool abort = false;
     int fail_tile = 0;
@@ -347,7 +501,7 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
             fail_tile = t;
             break;
         }
-        const float4* T = stage + size_t(slot) * PMGB_TILE;
+        const int4* T = stage + size_t(slot) * PMGB_TILE;
         const int t0 = t * PMGB_TILE;
         const int t1 = min(t0 + PMGB_TILE, S.n_rec);
         for (int sg = 0; sg < S.n_seg; ++sg) {
@@ -365,23 +519,35 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
             }
             for (int j0 = lo; j0 < hi; j0 += kChunk) {
                 const int j1 = min(j0 + kChunk, hi);
-                float ljp = 0.0f;
-                float php[NS];
+                float2 ljp2[NS], php2[NS];
 #pragma unroll
-                for (int k = 0; k < NS; ++k) php[k] = 0.0f;
-                for (int j = j0; j < j1; j += PMGB_SEG_ALIGN) {
+                for (int k = 0; k < NS; ++k) ljp2[k] = php2[k] = f2(0.0f);
+                int j = j0;
+                for (; j + 4 <= j1; j += 4) {
+                    const int4 r0 = T[j - t0], r1 = T[j + 1 - t0], r2 = T[j + 2 - t0], r3 = T[j + 3 - t0];
 #pragma unroll
-                    for (int u = 0; u < PMGB_SEG_ALIGN; ++u) {
-                        const float4 r = T[j + u - t0];
-#pragma unroll
-                        for (int k = 0; k < NS; ++k)
-                            pair_fwd<CHARGED>(r, sx[k], sy[k], sz[k], g, sig2[k], eps4[k], segmin[k], ljp, php[k]);
+                    for (int k = 0; k < NS; ++k) {
+                        const float2 sg = f2(sig2[k]), ep = f2(eps4[k]);
+                        pair2_fwd<CHARGED>(r0, r1, ux[k], uy[k], uz[k], g2, sg, ep, segmin[k], ljp2[k], php2[k]);
+                        pair2_fwd<CHARGED>(r2, r3, ux[k], uy[k], uz[k], g2, sg, ep, segmin[k], ljp2[k], php2[k]);
                     }
                 }
-                two_sum_acc(lj_hi, lj_lo, ljp);
-                if (CHARGED) {
+                float ljp[NS], php[NS];
 #pragma unroll
-                    for (int k = 0; k < NS; ++k) two_sum_acc(ph_hi[k], ph_lo[k], php[k]);
+                for (int k = 0; k < NS; ++k) {
+                    ljp[k] = ljp2[k].x + ljp2[k].y;
+                    php[k] = php2[k].x + php2[k].y;
+                }
+                for (; j < j1; ++j) {
+                    const int4 r = T[j - t0];
+#pragma unroll
+                    for (int k = 0; k < NS; ++k)
+                        pair_fwd<CHARGED>(r, ux[k], uy[k], uz[k], g, sig2[k], eps4[k], segmin[k], ljp[k], php[k]);
+                }
+#pragma unroll
+                for (int k = 0; k < NS; ++k) {
+                    two_sum_acc(lj_hi[k], lj_lo[k], ljp[k]);
+                    if (CHARGED) two_sum_acc(ph_hi[k], ph_lo[k], php[k]);
                 }
             }
 #pragma unroll
@@ -404,26 +570,25 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
     }
 
     // ---- reciprocal space ----------------------------------------------------
-    float pl_hi[NS], pl_lo[NS];
-#pragma unroll
-    for (int k = 0; k < NS; ++k) pl_hi[k] = pl_lo[k] = 0.0f;
-    if (CHARGED && valid) kspace_fwd<NS>(S, sx, sy, sz, pl_hi, pl_lo);
+    float pl_hi = 0.0f, pl_lo = 0.0f;
+    if (CHARGED && valid) kspace_fwd<NS>(S, ux, uy, uz, pl_hi, pl_lo);
 
     // ---- per-item energies (FP64) ----------------------------------------------
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
-    double uv = ovl ? inf : (static_cast<double>(lj_hi) + static_cast<double>(lj_lo));
-    double usr = 0.0, ulr = 0.0;
-    if (CHARGED) {
+    double uv = 0.0, usr = 0.0, ulr = 0.0;
 #pragma unroll
-        for (int k = 0; k < NS; ++k) {
-            if (k < S.n_sites) {
+    for (int k = 0; k < NS; ++k) {
+        if (k < S.n_sites) {
+            uv += static_cast<double>(lj_hi[k]) + static_cast<double>(lj_lo[k]);
+            if (CHARGED) {
                 const double qk = static_cast<double>(S.q[k]);
-                usr += qk * (static_cast<double>(ph_hi[k]) + static_cast<double>(ph_lo[k]));
-                ulr += qk * (static_cast<double>(pl_hi[k]) + static_cast<double>(pl_lo[k]));
+                if (qk != 0.0) usr += qk * (static_cast<double>(ph_hi[k]) + static_cast<double>(ph_lo[k]));
             }
         }
-        usr *= S.coul;
     }
+    if (ovl) uv = inf;
+    usr *= S.coul;
+    if (CHARGED) ulr = static_cast<double>(pl_hi) + static_cast<double>(pl_lo);
 
     if (a.out_mode == OUT_ENERGY) {
         if (valid) {
@@ -621,7 +786,7 @@ cudaError_t launch_ns(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
 }  // namespace
 
 size_t pmgb_pairs_smem_bytes() {
-    return size_t(PMGB_NSTAGE) * PMGB_TILE * sizeof(float4) + PMGB_NSTAGE * sizeof(uint64_t);
+    return size_t(PMGB_NSTAGE) * PMGB_TILE * sizeof(int4) + PMGB_NSTAGE * sizeof(uint64_t);
 }
 
 cudaError_t pmgb_launch_pairs(const LaunchArgs& a, int n_ctas, cudaStream_t st) {

@@ -118,6 +118,14 @@ def config1(seed: int = 1001) -> Crystal:
     return framework("synthetic_c1", Box(13.2, 18.9, 9.8, d, math.radians(102.0), d), 600, seed, charged=True)
 
 
+def config1_porous(seed: int = 1101, n_atoms: int = 150) -> Crystal:
+    """The config1 cell with a quarter of the atoms: open enough for CO2 to bind, so the
+    Boltzmann-weighted averages are not dominated by a single insertion."""
+    d = math.pi / 2
+    return framework("synthetic_c1_porous", Box(13.2, 18.9, 9.8, d, math.radians(102.0), d), n_atoms, seed,
+                     charged=True)
+
+
 def config4(seed: int = 1004) -> Crystal:
     """Orthorhombic 52 Å cube, 20,000 charged atoms."""
     d = math.pi / 2
