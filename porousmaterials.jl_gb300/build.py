@@ -22,7 +22,7 @@ OBJ_DIR = HERE / "_build"
 
 SOURCES = ["pmgb_kernels.cu", "pmgb_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O2", f"-I{INCLUDE}", f"-I{CSRC}"]
+FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-ftz=true", "-Xcompiler", "-fPIC,-O2", f"-I{INCLUDE}", f"-I{CSRC}"]
 
 
 def _nvcc() -> str:

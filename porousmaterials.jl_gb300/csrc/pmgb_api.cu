@@ -435,7 +435,7 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     s->n_sites = ns;
 
     // per (segment, site) LJ parameters
-    std::vector<SitePar> h_par(h_seg.size() * PMGB_MAX_SITES, SitePar{1.0f, 0.0f, -1.0f, 0.0f});
+    std::vector<SitePar> h_par(h_seg.size() * PMGB_MAX_SITES, SitePar{1.0f, 0.0f, -1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f});
     for (size_t g = 0; g < h_seg.size(); ++g)
         for (int k = 0; k < ns; ++k) {
             const int a = s->site_atom[k];
@@ -443,8 +443,11 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
             if (a < 0 || fs < 0) continue;
             const int gs = guest_atom_species[a];
             SitePar& p = h_par[g * PMGB_MAX_SITES + k];
-            p.sig2 = static_cast<float>(sigma2[gs * n_species + fs]);
-            p.eps4 = static_cast<float>(4.0 * epsilon[gs * n_species + fs]);
+            const double s2 = sigma2[gs * n_species + fs], e4 = 4.0 * epsilon[gs * n_species + fs];
+            p.sig2 = static_cast<float>(s2);
+            p.eps4 = static_cast<float>(e4);
+            p.lj12 = static_cast<float>(e4 * s2 * s2 * s2 * s2 * s2 * s2);
+            p.lj6 = static_cast<float>(-e4 * s2 * s2 * s2);
             p.r2ovl = 0.1f;  // R²_OVERLAP, src/vdw_energetics.jl:2
         }
 

@@ -6,7 +6,8 @@
 //                   the charge as FP32 bits, sorted by LJ species into contiguous segments.
 //   seg[n_seg]      [lo, hi) record range of each species segment.
 //   segpar[n_seg * PMGB_MAX_SITES]  per (segment, guest site): sigma^2, 4*epsilon,
-//                   overlap radius^2 (0.1, or -1 when the pair has no LJ term).
+//                   overlap radius^2 (0.1, or -1 when the pair has no LJ term), 4 eps sigma^12
+//                   and -4 eps sigma^6.
 //   krow[n_krow]    k-vectors grouped in half-rows of constant (ka, kb) running outward in
 //                   kc from the kc nearest 0.
 //   skw[n_k]        wt_k * S(k) in half-row traversal order, FP32 (re, im); S(k) is
@@ -32,7 +33,9 @@ struct SegDesc {
 };
 
 struct SitePar {
-    float sig2, eps4, r2ovl, pad;
+    float sig2, eps4, r2ovl;
+    float lj12, lj6;   // 4 eps sigma^12 and -4 eps sigma^6 (so that U = r^-6 (lj12 r^-6 + lj6))
+    float pad0, pad1, pad2;
 };
 
 struct KRow {

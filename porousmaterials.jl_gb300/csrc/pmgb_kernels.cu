@@ -217,6 +217,21 @@ __device__ __forceinline__ void pair_fwd(const int4 r, const uint32_t ux, const 
 }
 
 // ---- packed (f32x2) form: two framework records against one guest site -------------
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float ex2_approx(float x) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
@@ -226,12 +241,14 @@ struct Geo2 {
     float2 h00, h01, h02, h11, h12, h22;
     float2 p00, p01, p02, p11, p12, p22;
     float rc2, rc2e;
-    float2 alpha;
+    float2 half_alpha;   // alpha / 2
+    float2 m_a2_log2e;   // -alpha^2 log2(e)
 };
 
-__device__ __forceinline__ float2 erfc_fit2(float2 x) {
-    const float2 a = fma2(f2(0.5f), x, f2(1.0f));
-    const float2 t = make_float2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y));
+// erfc(alpha r) from r and r^2 (see erfc_fit; t = 1/(1 + alpha r/2), exp(-alpha^2 r^2) = 2^(c r^2))
+__device__ __forceinline__ float2 erfc_fit2(float2 r, float2 r2, const Geo2& g) {
+    const float2 a = fma2(g.half_alpha, r, f2(1.0f));
+    const float2 t = make_float2(rcp_approx(a.x), rcp_approx(a.y));
     const float2 y = fma2(t, f2(3.0f), f2(-2.0f));
     float2 q = f2(-1.1504688e-05f);
     q = fma2(q, y, f2(0.00012701178f));
@@ -241,16 +258,13 @@ __device__ __forceinline__ float2 erfc_fit2(float2 x) {
     q = fma2(q, y, f2(0.06661939f));
     q = fma2(q, y, f2(0.29403913f));
     q = fma2(q, y, f2(0.6413754f));
-    const float2 arg = mul2(x, mul2(x, f2(-1.4426950408889634f)));
-    float ex, ey;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ex) : "f"(arg.x));
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ey) : "f"(arg.y));
-    return mul2(mul2(q, t), make_float2(ex, ey));
+    const float2 arg = mul2(g.m_a2_log2e, r2);
+    return mul2(mul2(q, t), make_float2(ex2_approx(arg.x), ex2_approx(arg.y)));
 }
 
 template <bool CHARGED>
 __device__ __forceinline__ void pair2_fwd(const int4 ra, const int4 rb, const uint32_t ux, const uint32_t uy,
-                                          const uint32_t uz, const Geo2& g, const float2 sig2, const float2 eps4,
+                                          const uint32_t uz, const Geo2& g, const float2 lj12, const float2 lj6,
                                           float& segmin, float2& ljp, float2& php) {
     const float2 dx = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.x) - ux)),
                                   __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.x) - ux)));
@@ -268,21 +282,23 @@ __device__ __forceinline__ void pair2_fwd(const int4 ra, const int4 rb, const ui
     segmin = fminf(segmin, fminf(r2.x, r2.y));
     float2 ir2, y = f2(0.0f);
     if (CHARGED) {
-        y = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
-        const float2 e = fma2(neg2(mul2(r2, y)), y, f2(1.0f));
-        y = fma2(mul2(f2(0.5f), y), e, y);
+        // rsqrt estimate refined by one Newton step: y <- y + y (1/2 - (r2/2) y^2)
+        y = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+        const float2 hy = mul2(f2(-0.5f), mul2(r2, y));
+        y = fma2(y, fma2(hy, y, f2(0.5f)), y);
         ir2 = mul2(y, y);
     } else {
-        const float2 r0 = make_float2(__fdividef(1.0f, r2.x), __fdividef(1.0f, r2.y));
-        const float2 e = fma2(neg2(r2), r0, f2(1.0f));
+        const float2 r0 = make_float2(rcp_approx(r2.x), rcp_approx(r2.y));
+        const float2 e = fma2(mul2(f2(-1.0f), r2), r0, f2(1.0f));
         ir2 = fma2(r0, e, r0);
     }
-    const float2 s = mul2(sig2, ir2);
-    const float2 s3 = mul2(mul2(s, s), s);
-    const float2 t = fma2(s3, s3, neg2(s3));
-    ljp = fma2(eps4, make_float2(r2.x < g.rc2 ? t.x : 0.0f, r2.y < g.rc2 ? t.y : 0.0f), ljp);
+    // 4 eps [(s2/r2)^6 - (s2/r2)^3] = ir6 (lj12 ir6 - lj6), ir6 zeroed beyond the cutoff
+    const float2 ir6 = mul2(mul2(ir2, ir2), ir2);
+    const float2 ir6c = make_float2(r2.x < g.rc2 ? ir6.x : 0.0f, r2.y < g.rc2 ? ir6.y : 0.0f);
+    ljp = fma2(ir6c, fma2(lj12, ir6c, lj6), ljp);
     if (CHARGED) {
-        const float2 e = mul2(erfc_fit2(mul2(g.alpha, mul2(r2, y))), y);
+        const float2 rr = mul2(r2, y);
+        const float2 e = mul2(erfc_fit2(rr, r2, g), y);
         php = fma2(make_float2(__int_as_float(ra.w), __int_as_float(rb.w)),
                    make_float2(r2.x < g.rc2e ? e.x : 0.0f, r2.y < g.rc2e ? e.y : 0.0f), php);
     }
@@ -483,7 +499,7 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
                 S.rc2, S.rc2e, S.alpha};
     const Geo2 g2{f2(S.h00), f2(S.h01), f2(S.h02), f2(S.h11), f2(S.h12), f2(S.h22),
                   f2(S.p00), f2(S.p01), f2(S.p02), f2(S.p11), f2(S.p12), f2(S.p22),
-                  S.rc2, S.rc2e, f2(S.alpha)};
+                  S.rc2, S.rc2e, f2(0.5f * S.alpha), f2(-S.alpha * S.alpha * 1.4426950408889634f)};
     // per-site compensated accumulators (sites past n_sites are placeholders)
     float lj_hi[NS], lj_lo[NS], ph_hi[NS], ph_lo[NS];
 #pragma unroll
@@ -508,13 +524,15 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
             const SegDesc d = S.seg[sg];
             const int lo = max(d.lo, t0), hi = min(d.hi, t1);
             if (lo >= hi) continue;
-            float sig2[NS], eps4[NS], r2o[NS], segmin[NS];
+            float sig2[NS], eps4[NS], r2o[NS], segmin[NS], lj12[NS], lj6[NS];
 #pragma unroll
             for (int k = 0; k < NS; ++k) {
                 const SitePar p = S.segpar[sg * PMGB_MAX_SITES + k];
                 sig2[k] = p.sig2;
                 eps4[k] = p.eps4;
                 r2o[k] = p.r2ovl;
+                lj12[k] = p.lj12;
+                lj6[k] = p.lj6;
                 segmin[k] = __int_as_float(0x7f800000);
             }
             for (int j0 = lo; j0 < hi; j0 += kChunk) {
@@ -527,9 +545,9 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
                     const int4 r0 = T[j - t0], r1 = T[j + 1 - t0], r2 = T[j + 2 - t0], r3 = T[j + 3 - t0];
 #pragma unroll
                     for (int k = 0; k < NS; ++k) {
-                        const float2 sg = f2(sig2[k]), ep = f2(eps4[k]);
-                        pair2_fwd<CHARGED>(r0, r1, ux[k], uy[k], uz[k], g2, sg, ep, segmin[k], ljp2[k], php2[k]);
-                        pair2_fwd<CHARGED>(r2, r3, ux[k], uy[k], uz[k], g2, sg, ep, segmin[k], ljp2[k], php2[k]);
+                        const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
+                        pair2_fwd<CHARGED>(r0, r1, ux[k], uy[k], uz[k], g2, a12, a6, segmin[k], ljp2[k], php2[k]);
+                        pair2_fwd<CHARGED>(r2, r3, ux[k], uy[k], uz[k], g2, a12, a6, segmin[k], ljp2[k], php2[k]);
                     }
                 }
                 float ljp[NS], php[NS];

@@ -23,7 +23,7 @@ pytestmark = pytest.mark.gpu
 RTOL, ATOL = 1e-5, 1e-4
 # FP32 pair math: each pair term carries ~1e-7 relative rounding (more for the r^-12 part),
 # so an energy is accurate to a small multiple of 1e-7 of the sum of its terms' magnitudes
-FP32_SCALE_TOL = 2e-6
+FP32_SCALE_TOL = 4e-6
 
 
 def _report(name, gpu, ref):
@@ -260,17 +260,23 @@ def test_widom_parity_ewald_porous(c1p):
     _report("widom c1 porous vdw", u[:, 0], v)
     _report("widom c1 porous es", u[:, 1], es)
     _check_blocks(blocks, u, T, npb)
-    kh_rel, u_rel, _ = _kh_u_errors(blocks, v, es, T, npb)
-    # effective sample size of each block's Boltzmann weights
+    ref = oracle.widom_blocks_log(v, es, T, 5, npb)
+    dlog = blocks[:, 0] - ref[:, 0]                    # log K_H(GPU) - log K_H(oracle), per block
+    # first-order propagation of the per-insertion energy differences through the weights
     uo = (v + es).reshape(5, npb)
-    x = -uo / T
-    w = np.exp(x - np.nanmax(np.where(np.isfinite(x), x, -np.inf), axis=1, keepdims=True))
-    w = np.where(np.isfinite(w), w, 0.0)
+    ug = (u[:, 0] + u[:, 1]).reshape(5, npb)
+    fin = np.isfinite(uo) & np.isfinite(ug)
+    x = np.where(fin, -uo / T, -np.inf)
+    w = np.exp(x - x.max(axis=1, keepdims=True))
     w /= w.sum(axis=1, keepdims=True)
+    pred = -(w * np.where(fin, ug - uo, 0.0)).sum(axis=1) / T
     n_eff = 1.0 / (w ** 2).sum(axis=1)
-    print(f"[widom c1 porous] block K_H rel err {kh_rel}; <U> rel err max {u_rel.max():.3e}; N_eff {n_eff}")
-    assert kh_rel.max() < 1e-6
-    assert u_rel.max() < 1e-6
+    print(f"[widom c1 porous] Δlog K_H {dlog}; first-order prediction {pred}; N_eff {n_eff}")
+    # the device weighting is the Boltzmann weighting (to second order in the tiny δU/T)
+    np.testing.assert_allclose(dlog, pred, atol=1e-8)
+    # FP32 Coulomb pair terms (~1e-7 relative on terms of 1e4 K) bound the per-insertion
+    # error; with N_eff ~ 1 a block's K_H inherits it directly
+    assert np.abs(dlog).max() < 5e-5
 
 
 def test_widom_parity_ewald_dense(c1):
