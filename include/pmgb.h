@@ -137,6 +137,19 @@ int pmgb_widom(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t
 int pmgb_widom_device(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
                       double temperature, double* block_out_dev, double* u_out_dev);
 
+/* The computation of pmgb_widom_device for callers that cannot let the library allocate:
+ * the call makes no cudaMalloc / cudaFree (which synchronise the whole device and may find
+ * no memory left when another allocator's pool holds it) and uses a fixed per-device scratch
+ * array instead, sized for at most 65,536 CTAs: n_blocks * ceil(n_per_block / 256) <= 65536,
+ * i.e. up to 16.7M insertions per call; larger requests fail with PMGB_ERR_INVALID_ARGUMENT.
+ * The caller passes device-resident outputs (block_out_dev: 4*n_blocks doubles, u_out_dev
+ * optional).  The first call on a device looks up the scratch address (once per device);
+ * make that first call before any stream capture.  All calls on a device share the one
+ * array: calls that overlap on the GPU (other streams or threads) race and must be
+ * serialised by the caller.  No counterpart in the reference. */
+int pmgb_widom_noalloc(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
+                       double temperature, double* block_out_dev, double* u_out_dev);
+
 /* Poses the Widom kernel uses for insertions start .. start+n-1: xf_out (n x 3, centre of
  * mass, supercell fractional) and rot_out (n x 9, column-major rotation applied to the
  * Cartesian site offsets).  Replaces rand(3) + random_rotation! (src/henry.jl:214-220,

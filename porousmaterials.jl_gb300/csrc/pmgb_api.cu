@@ -731,6 +731,45 @@ extern "C" int pmgb_widom_device(pmgb_system* s, int64_t n_per_block, int32_t n_
     return PMGB_OK;
 }
 
+// Same launches as pmgb_widom_device, with the per-CTA partials in the library's fixed
+// device array instead of memory the system allocates; nothing is allocated or freed.
+extern "C" int pmgb_widom_noalloc(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
+                                  double temperature, double* block_out_dev, double* u_out_dev) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (n_per_block < 1 || n_blocks < 1 || !block_out_dev)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT,
+                    "pmgb_widom_noalloc: need n_per_block >= 1, n_blocks >= 1 and a device block_out");
+    if (!(temperature > 0.0) || !std::isfinite(temperature))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_noalloc: temperature must be positive (got %g)",
+                    temperature);
+    if (int rc = ready_for_charges(s)) return rc;
+    const int64_t cpb = (n_per_block + PMGB_THREADS - 1) / PMGB_THREADS;
+    if (cpb * n_blocks > PMGB_NOALLOC_MAX_CTAS)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT,
+                    "pmgb_widom_noalloc: %lld blocks of %lld insertions need %lld CTAs of %d insertions; the fixed "
+                    "scratch holds %d (at most %lld insertions per call)",
+                    static_cast<long long>(n_blocks), static_cast<long long>(n_per_block),
+                    static_cast<long long>(cpb * n_blocks), PMGB_THREADS, PMGB_NOALLOC_MAX_CTAS,
+                    static_cast<long long>(PMGB_NOALLOC_MAX_CTAS) * PMGB_THREADS);
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    LsePartial* scratch = nullptr;
+    PMGB_CK(ctx, pmgb_noalloc_scratch(ctx->device, &scratch));
+    LaunchArgs a = base_args(s);
+    a.pose_mode = POSE_PHILOX;
+    a.out_mode = OUT_WIDOM;
+    a.seed = seed;
+    a.n_per_block = n_per_block;
+    a.n_blocks = n_blocks;
+    a.ctas_per_block = static_cast<int>(cpb);
+    a.inv_temperature = 1.0 / temperature;
+    a.partials = scratch;  // every entry the reduction reads is written by this launch first
+    a.u_out = u_out_dev;
+    PMGB_CK(ctx, pmgb_launch_pairs(a, static_cast<int>(cpb * n_blocks), ctx->stream));
+    PMGB_CK(ctx, pmgb_launch_reduce_blocks(a.partials, n_blocks, a.ctas_per_block, block_out_dev, ctx->stream));
+    return PMGB_OK;
+}
+
 extern "C" int pmgb_widom(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uint64_t seed, double temperature,
                           double* block_out, double* u_out) {
     if (!s) return PMGB_ERR_INVALID_ARGUMENT;

@@ -134,3 +134,8 @@ cudaError_t pmgb_launch_philox(const unsigned int* ctr, const unsigned int* key,
                                unsigned int* out, cudaStream_t st);
 cudaError_t pmgb_launch_fp32_peak(float* sink, int n_ctas, int iters, cudaStream_t st);
 size_t pmgb_pairs_smem_bytes();
+
+// fixed per-device scratch of pmgb_widom_noalloc (defined in pmgb_kernels.cu)
+#define PMGB_NOALLOC_MAX_CTAS 65536   // LsePartial entries: 3 MiB, up to 16.7M insertions per call
+#define PMGB_NOALLOC_MAX_DEVICES 64
+cudaError_t pmgb_noalloc_scratch(int device, LsePartial** ptr);

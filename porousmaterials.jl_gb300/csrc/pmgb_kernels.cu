@@ -846,3 +846,33 @@ cudaError_t pmgb_launch_fp32_peak(float* sink, int n_ctas, int iters, cudaStream
     fp32_peak_kernel<<<n_ctas, 256, 0, st>>>(sink, iters);
     return cudaGetLastError();
 }
+
+// ============================================================================
+// Fixed scratch for pmgb_widom_noalloc.
+//
+// Some callers cannot let the library call cudaMalloc / cudaFree during a run: cudaFree
+// (and often cudaMalloc) synchronises the whole device, which stalls a host that keeps
+// other work in flight on the same GPU, and processes whose device memory is already
+// reserved by another allocator's pool (a Julia or Python framework's caching allocator)
+// may have nothing left to hand out.  For them the per-CTA Boltzmann partials live in this
+// file-scope array, reserved once when the library is loaded on a device.
+// ============================================================================
+namespace {
+__device__ __align__(256) LsePartial g_noalloc_partials[PMGB_NOALLOC_MAX_CTAS];
+}
+
+// Device address of g_noalloc_partials on `device` (which must be current).  Host code must
+// not use the symbol itself: on the host it names a stand-in, not device memory.  The
+// lookup runs once per device and is cached; it allocates nothing.
+cudaError_t pmgb_noalloc_scratch(int device, LsePartial** ptr) {
+    static void* cached[PMGB_NOALLOC_MAX_DEVICES] = {};
+    if (device < 0 || device >= PMGB_NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+    if (!cached[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        if (e != cudaSuccess) return e;
+        cached[device] = p;
+    }
+    *ptr = static_cast<LsePartial*>(cached[device]);
+    return cudaSuccess;
+}
