@@ -256,6 +256,22 @@ def ours(args, rank, world, local_rank):
     ms_max = float(t.item())
     value = world * n_ins * args.steps / (ms_max * 1e-3)
 
+    # forward + adjoint in one pass (pmgb_widom_adjoint: energies, dK_H/d(eps, sigma, lambda))
+    adj = None
+    if not args.skip_e2e:
+        import numpy as _np
+        system.widom_adjoint(npb, N_BLOCKS, 7, T)  # warm-up (allocates its scratch)
+        a_times = []
+        for s in range(max(3, args.steps // 2)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            system.widom_adjoint(npb, N_BLOCKS, 100 + s, T)
+            a_times.append(time.perf_counter() - t0)
+        adj = {"value": n_ins * len(a_times) / sum(a_times), "unit": UNIT,
+               "ms_per_step": 1e3 * sum(a_times) / len(a_times),
+               "what": "pmgb_widom_adjoint: forward energies + dK_H/d(epsilon, sigma^2) per species pair + "
+                       "dK_H/d(charge scale), pair terms recomputed (host call, includes the D2H of the sums)"}
+
     # end to end through the reference-facing call (host buffers, copies inside)
     e2e = None
     if not args.skip_e2e:
@@ -303,6 +319,7 @@ def ours(args, rank, world, local_rank):
                         "peak_source": "in-run FFMA probe (pmgb_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                         "flops_per_insertion": fpi,
                         "kernel": "pairs_kernel<3,true> + reduce_blocks_kernel per step"},
+           "forward_plus_adjoint": adj,
            "clocks": clk.summary(),
            "wall_s_timed_region": t_wall,
            "e2e": e2e,

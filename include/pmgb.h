@@ -157,6 +157,25 @@ int pmgb_widom_noalloc(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, 
 int pmgb_sample_poses(pmgb_ctx* ctx, uint64_t seed, int64_t start, int64_t n,
                       float* xf_out, float* rot_out);
 
+/* ---- adjoint (no reference counterpart: the reference has no derivatives) ------------------
+ * Widom insertions as pmgb_widom plus the Boltzmann-weighted parameter derivatives, recomputing
+ * every pair term instead of storing it.  With w_i = exp(-U_i/T - M), M = dtheta[0]:
+ *   dtheta[0] = M (= max_b block_out[4b]),  dtheta[1] = Σ_i w_i,  dtheta[2] = Σ_i w_i U_es,i,
+ *   dtheta[3 + 2(a*n_species + b)]     = Σ_i w_i ∂U_i/∂ε_ab,
+ *   dtheta[3 + 2(a*n_species + b) + 1] = Σ_i w_i ∂U_i/∂σ²_ab   (a: guest species, b: framework).
+ * dK_H/dθ = -e^M Σ_i w_i ∂U_i/∂θ / (T · R T n_per_block · n_blocks) for the block-mean K_H of
+ * src/henry.jl:120,141; ∂U_es/∂λ = U_es for framework charges scaled by λ.  grad_out (optional,
+ * n x 3 floats) receives dU/dx of each insertion's centre of mass (K/Å; the force is minus it).
+ * The (a, b) derivatives of a symmetric table entry used in both orders add. */
+int pmgb_widom_adjoint(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
+                       double temperature, double* block_out, double* dtheta, double* u_out,
+                       float* grad_out);
+
+/* pmgb_energies plus dU/dx of the configuration's reference point (all sites moved rigidly;
+ * grad_out: n_conf x 3 floats, K/Å). */
+int pmgb_energies_grad(pmgb_system* sys, int64_t n_conf, const double* site_xf, double* out,
+                       float* grad_out);
+
 /* ---- energy grid -----------------------------------------------------------------------
  * Replaces energy_grid(crystal, molecule, ljff; resolution=(n1,n2,n3)) for single-site
  * probes (src/grid.jl:291-362): point (i,j,k) sits at (i/(n1-1), j/(n2-1), k/(n3-1)) of
@@ -166,6 +185,14 @@ int pmgb_energy_grid(pmgb_system* sys, const int32_t n_pts[3], const int32_t rep
                      double unit_factor, float* out);
 int pmgb_energy_grid_device(pmgb_system* sys, const int32_t n_pts[3], const int32_t repfactors[3],
                             double unit_factor, float* out_dev);
+
+/* Energy grid plus its adjoint: grad_out (optional, 3 floats per point) = dU/dr at each point
+ * (K/Å, Cartesian), and dtheta as for pmgb_widom_adjoint with the grid points as the samples
+ * (w_p = exp(-U_p/T - M), M = max_p -U_p/T): the grid estimate
+ * K_H,grid = Σ_p e^{-U_p/T} / (R T n_points) has dK/dθ = -e^M Σ_p w_p ∂U_p/∂θ / (T R T n_points). */
+int pmgb_energy_grid_adjoint(pmgb_system* sys, const int32_t n_pts[3], const int32_t repfactors[3],
+                             double unit_factor, double temperature, float* out, float* grad_out,
+                             double* dtheta);
 
 /* ---- utilities -------------------------------------------------------------------------- */
 

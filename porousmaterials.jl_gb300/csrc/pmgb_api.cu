@@ -65,10 +65,16 @@ struct pmgb_system {
     bool ewald_set = false;
     int n_sites = 0;
     int64_t h2d_bytes = 0;
+    // host copies for the adjoint's species-pair assembly
+    int n_species = 0;
+    std::vector<double> eps, sig2;
+    std::vector<int> seg_species;   // framework species of each segment (-1: charge-only)
+    std::vector<int> site_species;  // guest LJ species of each site (-1: charge-only site)
     int site_atom[PMGB_MAX_SITES];
     int site_charge[PMGB_MAX_SITES];
     // grow-only scratch used by launches
     DevBuf partials, block_out, in_buf, out_buf, axes;
+    DevBuf g_u, g_dsum, g_grad, g_part, g_cols;  // adjoint scratch
 };
 
 namespace {
@@ -267,8 +273,10 @@ extern "C" int pmgb_device_status(pmgb_ctx* ctx, uint32_t* status_out) {
 // system
 // ============================================================================
 static void free_system_device(pmgb_system* s) {
-    void* ptrs[] = {s->d_rec, s->d_seg, s->d_segpar, s->d_qfix, s->d_q, s->d_krow, s->d_skw, s->d_sk,
-                    s->d_kabc, s->d_wt, s->partials.p, s->block_out.p, s->in_buf.p, s->out_buf.p, s->axes.p};
+    void* ptrs[] = {s->d_rec,      s->d_seg,       s->d_segpar,  s->d_qfix,   s->d_q,     s->d_krow,
+                    s->d_skw,      s->d_sk,        s->d_kabc,    s->d_wt,     s->partials.p, s->block_out.p,
+                    s->in_buf.p,   s->out_buf.p,   s->axes.p,    s->g_u.p,    s->g_dsum.p, s->g_grad.p,
+                    s->g_part.p,   s->g_cols.p};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -433,6 +441,11 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
         sq[hit] = guest_charge_q[c];
     }
     s->n_sites = ns;
+    s->n_species = n_species;
+    s->eps.assign(epsilon, epsilon + static_cast<size_t>(n_species) * n_species);
+    s->sig2.assign(sigma2, sigma2 + static_cast<size_t>(n_species) * n_species);
+    for (const SegDesc& d : h_seg) s->seg_species.push_back(d.species);
+    for (int k = 0; k < ns; ++k) s->site_species.push_back(s->site_atom[k] >= 0 ? guest_atom_species[s->site_atom[k]] : -1);
 
     // per (segment, site) LJ parameters
     std::vector<SitePar> h_par(h_seg.size() * PMGB_MAX_SITES, SitePar{1.0f, 0.0f, -1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f});
@@ -789,6 +802,191 @@ extern "C" int pmgb_widom(pmgb_system* s, int64_t n_per_block, int32_t n_blocks,
                                  ctx->stream));
     if (u_out) PMGB_CK(ctx, cudaMemcpyAsync(u_out, s->out_buf.p, u_bytes, cudaMemcpyDeviceToHost, ctx->stream));
     return check_status(ctx);
+}
+
+// ---------------------------------------------------------------------------- adjoint
+static int grid_axes(pmgb_system* s, const int32_t n_pts[3], const int32_t rep[3]);
+static int template_sites(int n) { return n <= 1 ? 1 : n <= 2 ? 2 : n <= 3 ? 3 : n <= 4 ? 4 : n <= 6 ? 6 : 8; }
+
+// Assemble Σ w ∂U/∂ε_ab and Σ w ∂U/∂σ²_ab (a: guest species, b: framework species) from the
+// per (segment, site) weighted sums of r^-12 and r^-6:  U = 4ε(σ^12 r^-12 - σ^6 r^-6).
+static void assemble_species(const pmgb_system* s, int nst, const double* cols, double* dtheta) {
+    const int n = s->n_species;
+    for (int i = 0; i < 2 * n * n; ++i) dtheta[3 + i] = 0.0;
+    for (size_t sg = 0; sg < s->seg_species.size(); ++sg) {
+        const int b = s->seg_species[sg];
+        if (b < 0) continue;
+        for (int k = 0; k < s->n_sites; ++k) {
+            const int ga = s->site_species[k];
+            if (ga < 0) continue;
+            const double i12 = cols[(sg * nst + k) * 2], i6 = cols[(sg * nst + k) * 2 + 1];
+            const double s2 = s->sig2[ga * n + b], e = s->eps[ga * n + b];
+            const double s4 = s2 * s2, s6 = s4 * s2, s10 = s6 * s4, s12 = s6 * s6;
+            dtheta[3 + 2 * (ga * n + b)] += 4.0 * (s12 * i12 - s6 * i6);
+            dtheta[3 + 2 * (ga * n + b) + 1] += 4.0 * e * (6.0 * s10 * i12 - 3.0 * s4 * i6);
+        }
+    }
+}
+
+extern "C" int pmgb_widom_adjoint(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
+                                  double temperature, double* block_out, double* dtheta, double* u_out,
+                                  float* grad_out) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (n_per_block < 1 || n_blocks < 1 || !block_out || !dtheta)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_adjoint: bad arguments");
+    if (!(temperature > 0.0) || !std::isfinite(temperature))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_adjoint: temperature must be positive");
+    if (int rc = ready_for_charges(s)) return rc;
+    const int64_t cpb = (n_per_block + PMGB_THREADS - 1) / PMGB_THREADS;
+    if (cpb * n_blocks > INT32_MAX) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_adjoint: too many insertions");
+    const int nst = template_sites(s->n_sites);
+    const int n_cols = static_cast<int>(s->seg_species.size()) * nst * 2;
+    const int64_t n = n_per_block * n_blocks;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    const int n_ctas = static_cast<int>(cpb * n_blocks);
+    const int n_chunks = static_cast<int>(std::min<int64_t>(1024, (n + 4095) / 4096));
+    int rc;
+    if ((rc = ensure(ctx, s->partials, sizeof(LsePartial) * n_ctas)) ||
+        (rc = ensure(ctx, s->block_out, sizeof(double) * 4 * n_blocks)) ||
+        (rc = ensure(ctx, s->g_u, sizeof(double) * 2 * n)) ||
+        (rc = ensure(ctx, s->g_dsum, sizeof(float) * std::max<int64_t>(1, n_cols) * n)) ||
+        (rc = ensure(ctx, s->g_part, sizeof(double) * n_chunks * (n_cols + 2))) ||
+        (rc = ensure(ctx, s->g_cols, sizeof(double) * (n_cols + 2))) ||
+        (grad_out && (rc = ensure(ctx, s->g_grad, sizeof(float) * 3 * n))))
+        return rc;
+    LaunchArgs a = base_args(s);
+    a.pose_mode = POSE_PHILOX;
+    a.out_mode = OUT_WIDOM;
+    a.seed = seed;
+    a.n_per_block = n_per_block;
+    a.n_blocks = n_blocks;
+    a.ctas_per_block = static_cast<int>(cpb);
+    a.inv_temperature = 1.0 / temperature;
+    a.partials = static_cast<LsePartial*>(s->partials.p);
+    a.u_out = static_cast<double*>(s->g_u.p);
+    a.dsum = static_cast<float*>(s->g_dsum.p);
+    a.dsum_stride = n;
+    a.grad_u = grad_out ? static_cast<float*>(s->g_grad.p) : nullptr;
+    double* d_block = static_cast<double*>(s->block_out.p);
+    PMGB_CK(ctx, pmgb_launch_pairs_grad(a, n_ctas, ctx->stream));
+    PMGB_CK(ctx, pmgb_launch_reduce_blocks(a.partials, n_blocks, a.ctas_per_block, d_block, ctx->stream));
+    PMGB_CK(ctx, pmgb_launch_weighted_columns(a.u_out, 2, n, a.inv_temperature, d_block, n_blocks, a.dsum, n_cols, n,
+                                              static_cast<double*>(s->g_part.p), n_chunks,
+                                              static_cast<double*>(s->g_cols.p), ctx->stream));
+    std::vector<double> cols(n_cols + 2);
+    PMGB_CK(ctx, cudaMemcpyAsync(block_out, d_block, sizeof(double) * 4 * n_blocks, cudaMemcpyDeviceToHost, ctx->stream));
+    PMGB_CK(ctx, cudaMemcpyAsync(cols.data(), s->g_cols.p, sizeof(double) * (n_cols + 2), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    if (u_out) PMGB_CK(ctx, cudaMemcpyAsync(u_out, a.u_out, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (grad_out) PMGB_CK(ctx, cudaMemcpyAsync(grad_out, a.grad_u, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((rc = check_status(ctx))) return rc;
+    double M = -INFINITY;
+    for (int b = 0; b < n_blocks; ++b) M = std::max(M, block_out[4 * b]);
+    dtheta[0] = M;
+    dtheta[1] = cols[n_cols];
+    dtheta[2] = cols[n_cols + 1];
+    assemble_species(s, nst, cols.data(), dtheta);
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_energies_grad(pmgb_system* s, int64_t n_conf, const double* site_xf, double* out,
+                                  float* grad_out) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (n_conf < 0 || (n_conf > 0 && (!site_xf || !out || !grad_out)))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energies_grad: bad arguments");
+    if (int rc = ready_for_charges(s)) return rc;
+    if (n_conf == 0) return PMGB_OK;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    const size_t n_coord = 3 * static_cast<size_t>(s->n_sites) * static_cast<size_t>(n_conf);
+    std::vector<uint32_t> fix(n_coord);
+    for (size_t i = 0; i < n_coord; ++i) {
+        if (!std::isfinite(site_xf[i])) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "non-finite site coordinate");
+        fix[i] = to_fix(site_xf[i]);
+    }
+    const int nst = template_sites(s->n_sites);
+    const int n_cols = static_cast<int>(s->seg_species.size()) * nst * 2;
+    int rc;
+    if ((rc = ensure(ctx, s->in_buf, sizeof(uint32_t) * n_coord)) || (rc = ensure(ctx, s->out_buf, sizeof(double) * 3 * n_conf)) ||
+        (rc = ensure(ctx, s->g_grad, sizeof(float) * 3 * n_conf)) ||
+        (rc = ensure(ctx, s->g_dsum, sizeof(float) * std::max(1, n_cols) * n_conf)))
+        return rc;
+    PMGB_CK(ctx, cudaMemcpyAsync(s->in_buf.p, fix.data(), sizeof(uint32_t) * n_coord, cudaMemcpyHostToDevice, ctx->stream));
+    LaunchArgs a = base_args(s);
+    a.pose_mode = POSE_SITES;
+    a.out_mode = OUT_ENERGY;
+    a.site_fix = static_cast<const uint32_t*>(s->in_buf.p);
+    a.n_conf = n_conf;
+    a.e_out = static_cast<double*>(s->out_buf.p);
+    a.dsum = static_cast<float*>(s->g_dsum.p);
+    a.dsum_stride = n_conf;
+    a.grad_u = static_cast<float*>(s->g_grad.p);
+    PMGB_CK(ctx, pmgb_launch_pairs_grad(a, static_cast<int>((n_conf + PMGB_THREADS - 1) / PMGB_THREADS), ctx->stream));
+    PMGB_CK(ctx, cudaMemcpyAsync(out, s->out_buf.p, sizeof(double) * 3 * n_conf, cudaMemcpyDeviceToHost, ctx->stream));
+    PMGB_CK(ctx, cudaMemcpyAsync(grad_out, s->g_grad.p, sizeof(float) * 3 * n_conf, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_status(ctx);
+}
+
+extern "C" int pmgb_energy_grid_adjoint(pmgb_system* s, const int32_t n_pts[3], const int32_t repfactors[3],
+                                        double unit_factor, double temperature, float* out, float* grad_out,
+                                        double* dtheta) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (!n_pts || !repfactors || !out || !dtheta || !(temperature > 0.0))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid_adjoint: bad arguments");
+    for (int d = 0; d < 3; ++d)
+        if (n_pts[d] < 1 || repfactors[d] < 1)
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid_adjoint: n_pts and repfactors must be >= 1");
+    if (s->n_sites != 1)
+        return fail(ctx, PMGB_ERR_UNSUPPORTED, "pmgb_energy_grid_adjoint: the probe must be a single site");
+    const int64_t total = int64_t(n_pts[0]) * n_pts[1] * n_pts[2];
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    if (int rc = grid_axes(s, n_pts, repfactors)) return rc;
+    const int n_cols = static_cast<int>(s->seg_species.size()) * 1 * 2;
+    const int n_chunks = static_cast<int>(std::min<int64_t>(1024, (total + 4095) / 4096));
+    int rc;
+    if ((rc = ensure(ctx, s->out_buf, sizeof(float) * total)) || (rc = ensure(ctx, s->g_u, sizeof(double) * total)) ||
+        (rc = ensure(ctx, s->g_dsum, sizeof(float) * std::max(1, n_cols) * total)) ||
+        (rc = ensure(ctx, s->g_grad, sizeof(float) * 3 * total)) ||
+        (rc = ensure(ctx, s->block_out, sizeof(double) * 4)) ||
+        (rc = ensure(ctx, s->g_part, sizeof(double) * n_chunks * (n_cols + 2))) ||
+        (rc = ensure(ctx, s->g_cols, sizeof(double) * (n_cols + 2))))
+        return rc;
+    LaunchArgs a = base_args(s);
+    a.sys.charged = 0;
+    a.pose_mode = POSE_GRID;
+    a.out_mode = OUT_GRID;
+    for (int d = 0; d < 3; ++d) a.n_pts[d] = n_pts[d];
+    const uint32_t* ax = static_cast<const uint32_t*>(s->axes.p);
+    a.grid_x = ax;
+    a.grid_y = ax + n_pts[0];
+    a.grid_z = ax + n_pts[0] + n_pts[1];
+    a.unit_factor = static_cast<float>(unit_factor);
+    a.grid_out = static_cast<float*>(s->out_buf.p);
+    a.u_out = static_cast<double*>(s->g_u.p);
+    a.dsum = static_cast<float*>(s->g_dsum.p);
+    a.dsum_stride = total;
+    a.grad_u = static_cast<float*>(s->g_grad.p);
+    const double inv_t = 1.0 / temperature;
+    double* d_scale = static_cast<double*>(s->block_out.p);
+    PMGB_CK(ctx, pmgb_launch_pairs_grad(a, static_cast<int>((total + PMGB_THREADS - 1) / PMGB_THREADS), ctx->stream));
+    PMGB_CK(ctx, pmgb_launch_max_neg_u(a.u_out, total, inv_t, d_scale, ctx->stream));
+    PMGB_CK(ctx, pmgb_launch_weighted_columns(a.u_out, 1, total, inv_t, d_scale, 1, a.dsum, n_cols, total,
+                                              static_cast<double*>(s->g_part.p), n_chunks,
+                                              static_cast<double*>(s->g_cols.p), ctx->stream));
+    std::vector<double> cols(n_cols + 2);
+    double M = 0.0;
+    PMGB_CK(ctx, cudaMemcpyAsync(out, a.grid_out, sizeof(float) * total, cudaMemcpyDeviceToHost, ctx->stream));
+    if (grad_out) PMGB_CK(ctx, cudaMemcpyAsync(grad_out, a.grad_u, sizeof(float) * 3 * total, cudaMemcpyDeviceToHost, ctx->stream));
+    PMGB_CK(ctx, cudaMemcpyAsync(cols.data(), s->g_cols.p, sizeof(double) * (n_cols + 2), cudaMemcpyDeviceToHost, ctx->stream));
+    PMGB_CK(ctx, cudaMemcpyAsync(&M, d_scale, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if ((rc = check_status(ctx))) return rc;
+    dtheta[0] = M;
+    dtheta[1] = cols[n_cols];
+    dtheta[2] = 0.0;
+    assemble_species(s, 1, cols.data(), dtheta);
+    return PMGB_OK;
 }
 
 extern "C" int pmgb_sample_poses(pmgb_ctx* ctx, uint64_t seed, int64_t start, int64_t n, float* xf_out,

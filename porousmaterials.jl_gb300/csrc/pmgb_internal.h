@@ -116,12 +116,24 @@ struct LaunchArgs {
     const uint32_t* grid_z;
     float unit_factor;
     float* grid_out;
+    // adjoint (GRAD kernels)
+    float* dsum;                 // [(seg * NS + site) * 2 + {0: sum r^-12, 1: sum r^-6}][item], within cutoff
+    long long dsum_stride;       // items per column
+    float* grad_u;               // optional: [item * 3] dU/dx of the centre of mass (K/A)
     // status
     unsigned int* status;
 };
 
+cudaError_t pmgb_launch_max_neg_u(const double* u, long long n, double inv_t, double* out, cudaStream_t st);
+// Weighted sums of per-item adjoint columns: out[c] = sum_i w_i col_c[i], w_i = exp(-U_i/T - M)
+cudaError_t pmgb_launch_weighted_columns(const double* u, int u_stride, long long n, double inv_t,
+                                         const double* log_scale, int n_log, const float* cols,
+                                         int n_cols, long long col_stride, double* partials, int n_chunks,
+                                         double* out, cudaStream_t st);
+
 // kernels (defined in pmgb_kernels.cu); return cudaError_t of the launch
 cudaError_t pmgb_launch_pairs(const LaunchArgs& a, int n_ctas, cudaStream_t st);
+cudaError_t pmgb_launch_pairs_grad(const LaunchArgs& a, int n_ctas, cudaStream_t st);
 cudaError_t pmgb_launch_reduce_blocks(const LsePartial* partials, int n_blocks, int ctas_per_block,
                                       double* block_out, cudaStream_t st);
 // qfix: framework charge fractional coordinates as 32-bit fixed point (x * 2^32 mod 2^32)

@@ -262,6 +262,87 @@ __device__ __forceinline__ float2 erfc_fit2(float2 r, float2 r2, const Geo2& g) 
     return mul2(mul2(q, t), make_float2(ex2_approx(arg.x), ex2_approx(arg.y)));
 }
 
+// erfc(alpha r) and exp(-alpha^2 r^2), for the adjoint
+__device__ __forceinline__ float2 erfc_fit2_exp(float2 r, float2 r2, const Geo2& g, float2& ex) {
+    const float2 a = fma2(g.half_alpha, r, f2(1.0f));
+    const float2 t = make_float2(rcp_approx(a.x), rcp_approx(a.y));
+    const float2 y = fma2(t, f2(3.0f), f2(-2.0f));
+    float2 q = f2(-1.1504688e-05f);
+    q = fma2(q, y, f2(0.00012701178f));
+    q = fma2(q, y, f2(1.719709e-05f));
+    q = fma2(q, y, f2(-0.002622572f));
+    q = fma2(q, y, f2(0.00045600548f));
+    q = fma2(q, y, f2(0.06661939f));
+    q = fma2(q, y, f2(0.29403913f));
+    q = fma2(q, y, f2(0.6413754f));
+    const float2 arg = mul2(g.m_a2_log2e, r2);
+    ex = make_float2(ex2_approx(arg.x), ex2_approx(arg.y));
+    return mul2(mul2(q, t), ex);
+}
+
+// Per (record pair, site) adjoint accumulators
+struct Grad2 {
+    float2 i12, i6;        // sum r^-12, sum r^-6 within the LJ cutoff
+    float2 gx, gy, gz;     // sum c (dU/dr^2) with the site's charge folded into the Coulomb part
+};
+
+// The forward pair terms plus the adjoint ones.  c = x_framework - x_site (Cartesian, the
+// frame of the upper-triangular box); dU/dx_site = -2 sum_j c_j dU_j/d(r^2).
+template <bool CHARGED>
+__device__ __forceinline__ void pair2_grad(const int4 ra, const int4 rb, const uint32_t ux, const uint32_t uy,
+                                           const uint32_t uz, const Geo2& g, const float2 lj12, const float2 lj6,
+                                           const float2 qcoul, const float2 c1, const float2 lane_mask,
+                                           float& segmin, float2& ljp, float2& php, Grad2& G) {
+    const float2 dx = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.x) - ux)),
+                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.x) - ux)));
+    const float2 dy = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.y) - uy)),
+                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.y) - uy)));
+    const float2 dz = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.z) - uz)),
+                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.z) - uz)));
+    const float2 rx = fma2(g.p00, dx, fma2(g.p01, dy, mul2(g.p02, dz)));
+    const float2 ry = fma2(g.p11, dy, mul2(g.p12, dz));
+    const float2 rz = mul2(g.p22, dz);
+    const float2 cx = fma2(g.h00, dx, fma2(g.h01, dy, fma2(g.h02, dz, rx)));
+    const float2 cy = fma2(g.h11, dy, fma2(g.h12, dz, ry));
+    const float2 cz = fma2(g.h22, dz, rz);
+    const float2 r2 = fma2(cx, cx, fma2(cy, cy, mul2(cz, cz)));
+    segmin = fminf(segmin, fminf(r2.x, r2.y));
+    float2 ir2, y = f2(0.0f);
+    if (CHARGED) {
+        y = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+        const float2 hy = mul2(f2(-0.5f), mul2(r2, y));
+        y = fma2(y, fma2(hy, y, f2(0.5f)), y);
+        ir2 = mul2(y, y);
+    } else {
+        const float2 r0 = make_float2(rcp_approx(r2.x), rcp_approx(r2.y));
+        const float2 e = fma2(mul2(f2(-1.0f), r2), r0, f2(1.0f));
+        ir2 = fma2(r0, e, r0);
+    }
+    const float2 ir6 = mul2(mul2(ir2, ir2), ir2);
+    const float2 ir6c = mul2(lane_mask, make_float2(r2.x < g.rc2 ? ir6.x : 0.0f, r2.y < g.rc2 ? ir6.y : 0.0f));
+    const float2 ir12c = mul2(ir6c, ir6c);
+    ljp = fma2(ir6c, fma2(lj12, ir6c, lj6), ljp);
+    G.i12 = __fadd2_rn(G.i12, ir12c);
+    G.i6 = __fadd2_rn(G.i6, ir6c);
+    // dU_LJ/d(r^2) = -r^-2 r^-6 (6 lj12 r^-6 + 3 lj6)
+    float2 du = mul2(mul2(f2(-1.0f), ir2), mul2(ir6c, fma2(mul2(f2(6.0f), lj12), ir6c, mul2(f2(3.0f), lj6))));
+    if (CHARGED) {
+        const float2 rr = mul2(r2, y);
+        float2 ex;
+        const float2 erfcv = erfc_fit2_exp(rr, r2, g, ex);
+        const float2 e = mul2(erfcv, y);
+        const float2 qj = make_float2(__int_as_float(ra.w), __int_as_float(rb.w));
+        const float2 in_e = mul2(lane_mask, make_float2(r2.x < g.rc2e ? 1.0f : 0.0f, r2.y < g.rc2e ? 1.0f : 0.0f));
+        php = fma2(mul2(qj, in_e), e, php);
+        // d(q_j erfc(a r)/r)/d(r^2) = -q_j r^-2 / 2 [c1 exp(-a^2 r^2) + erfc(a r)/r], c1 = 2a/sqrt(pi)
+        const float2 dc = mul2(mul2(mul2(f2(-0.5f), mul2(qj, in_e)), ir2), fma2(c1, ex, e));
+        du = fma2(qcoul, dc, du);
+    }
+    G.gx = fma2(cx, du, G.gx);
+    G.gy = fma2(cy, du, G.gy);
+    G.gz = fma2(cz, du, G.gz);
+}
+
 template <bool CHARGED>
 __device__ __forceinline__ void pair2_fwd(const int4 ra, const int4 rb, const uint32_t ux, const uint32_t uy,
                                           const uint32_t uz, const Geo2& g, const float2 lj12, const float2 lj6,
@@ -311,9 +392,11 @@ __device__ __forceinline__ void pair2_fwd(const int4 ra, const int4 rb, const ui
 // D_g = e^{-ik.d_g} - 1 is carried by the recurrence D <- D w + (w - 1), whose error is
 // relative to |D|.  Phases are exact 32-bit fixed-point turns.  Rows of constant (ka, kb)
 // start at the kc nearest 0 and step outward in kc by `dir`.
-template <int NS>
+template <int NS, bool GRAD = false>
 __device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua[NS], const uint32_t Ub[NS],
-                                           const uint32_t Uc[NS], float& plr_hi, float& plr_lo) {
+                                           const uint32_t Uc[NS], float& plr_hi, float& plr_lo,
+                                           float (*gu)[3] = nullptr) {
+    // GRAD: gu[g][d] receives dU_lr/du_g (fractional coordinates of site g)
     constexpr float kTurn = 4.656612873077393e-10f;  // 2^-31: int32 fixed point -> half turns
     plr_hi = 0.0f;
     plr_lo = 0.0f;
@@ -374,6 +457,10 @@ __device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua[NS
             sdwi[k] = sgn * dwi[k];
         }
         float part = 0.0f;
+        float vs[NS], vk[NS];  // GRAD: sum_m Im[T E_g] and sum_m kc Im[T E_g] along the row
+#pragma unroll
+        for (int k = 0; k < NS; ++k) vs[k] = vk[k] = 0.0f;
+        float kcf = static_cast<float>(R.kc0);
         const float2* sw = S.skw + R.off;
         for (int m = 0; m < R.n; ++m) {
             const float2 w = __ldg(sw + m);
@@ -388,6 +475,16 @@ __device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua[NS
             const float tr = fmaf(w.x, er, -w.y * ei);
             const float ti = fmaf(w.x, ei, w.y * er);
             part = fmaf(tr, hr, fmaf(-ti, hi, part));
+            if (GRAD) {
+                // Im[T (1 + D_g)] for every site (D_0 = 0)
+#pragma unroll
+                for (int k = 0; k < NS; ++k) {
+                    const float v = (k == 0) ? ti : fmaf(tr, Di[k], fmaf(ti, Dr[k], ti));
+                    vs[k] += v;
+                    vk[k] = fmaf(kcf, v, vk[k]);
+                }
+                kcf += sgn;
+            }
             // advance one step in kc
             const float nr = fmaf(er, w0r, -ei * sw0i);
             ei = fmaf(er, sw0i, ei * w0r);
@@ -400,6 +497,16 @@ __device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua[NS
             }
         }
         two_sum_acc(plr_hi, plr_lo, part);
+        if (GRAD) {
+            // dU/du_g = 2 pi q_g sum_k k Im[T E_g]
+#pragma unroll
+            for (int k = 0; k < NS; ++k) {
+                const float f = 6.283185307179586f * qg[k];
+                gu[k][0] = fmaf(f * static_cast<float>(R.ka), vs[k], gu[k][0]);
+                gu[k][1] = fmaf(f * static_cast<float>(R.kb), vs[k], gu[k][1]);
+                gu[k][2] = fmaf(f, vk[k], gu[k][2]);
+            }
+        }
     }
 }
 
@@ -675,6 +782,364 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
     }
 }
 
+// The adjoint: the forward pair kernel plus, per item, dU/dx of the centre of mass and, per
+// (species segment, guest site), the sums of r^-12 and r^-6 within the LJ cutoff, from which
+// the host forms dU/d(epsilon) and dU/d(sigma^2) of every (guest, framework) species pair.
+// Pair terms are recomputed here rather than stored by the forward pass.
+template <int NS, bool CHARGED>
+__global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_grad_kernel(const __grid_constant__ LaunchArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    int4* stage = reinterpret_cast<int4*>(smem_raw);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + size_t(PMGB_NSTAGE) * PMGB_TILE * sizeof(int4));
+    __shared__ LsePartial red[PMGB_THREADS / 32];
+
+    const SysDev& S = a.sys;
+    const int tid = threadIdx.x;
+    long long item = 0;
+    bool valid = false;
+    if (a.pose_mode == POSE_PHILOX) {
+        const int b = blockIdx.x / a.ctas_per_block;
+        const long long within = static_cast<long long>(blockIdx.x % a.ctas_per_block) * PMGB_THREADS + tid;
+        valid = within < a.n_per_block;
+        item = static_cast<long long>(b) * a.n_per_block + within;
+    } else if (a.pose_mode == POSE_SITES) {
+        item = static_cast<long long>(blockIdx.x) * PMGB_THREADS + tid;
+        valid = item < a.n_conf;
+    } else {
+        item = static_cast<long long>(blockIdx.x) * PMGB_THREADS + tid;
+        valid = item < static_cast<long long>(a.n_pts[0]) * a.n_pts[1] * a.n_pts[2];
+    }
+    uint32_t ux[NS], uy[NS], uz[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) ux[k] = uy[k] = uz[k] = 0u;
+    if (valid) {
+        if (a.pose_mode == POSE_PHILOX) {
+            float xf[3], R[9];
+            make_pose(a.seed, static_cast<unsigned long long>(item), xf, R);
+            const uint32_t cx = frac2fix(xf[0]), cy = frac2fix(xf[1]), cz = frac2fix(xf[2]);
+#pragma unroll
+            for (int k = 0; k < NS; ++k) {
+                const float bx = S.body[k][0], by = S.body[k][1], bz = S.body[k][2];
+                const float ox = R[0] * bx + R[3] * by + R[6] * bz;
+                const float oy = R[1] * bx + R[4] * by + R[7] * bz;
+                const float oz = R[2] * bx + R[5] * by + R[8] * bz;
+                ux[k] = cx + frac2fix(S.g00 * ox + S.g01 * oy + S.g02 * oz);
+                uy[k] = cy + frac2fix(S.g11 * oy + S.g12 * oz);
+                uz[k] = cz + frac2fix(S.g22 * oz);
+            }
+        } else if (a.pose_mode == POSE_SITES) {
+            const uint32_t* p = a.site_fix + static_cast<size_t>(item) * S.n_sites * 3;
+#pragma unroll
+            for (int k = 0; k < NS; ++k)
+                if (k < S.n_sites) {
+                    ux[k] = p[3 * k + 0];
+                    uy[k] = p[3 * k + 1];
+                    uz[k] = p[3 * k + 2];
+                }
+        } else {
+            const long long n1 = a.n_pts[0], n2 = a.n_pts[1];
+            ux[0] = a.grid_x[static_cast<int>(item % n1)];
+            uy[0] = a.grid_y[static_cast<int>((item / n1) % n2)];
+            uz[0] = a.grid_z[static_cast<int>(item / (n1 * n2))];
+        }
+    }
+    if (tid == 0) {
+#pragma unroll
+        for (int s = 0; s < PMGB_NSTAGE; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    int last_issued = -1;
+    auto issue = [&](int t) {
+        const int slot = t % PMGB_NSTAGE;
+        const int t0 = t * PMGB_TILE;
+        const int cnt = min(PMGB_TILE, S.n_rec - t0);
+        const uint32_t bytes = static_cast<uint32_t>(cnt) * sizeof(int4);
+        mbar_expect_tx(&bars[slot], bytes);
+        bulk_g2s(stage + size_t(slot) * PMGB_TILE, S.rec + t0, bytes, &bars[slot]);
+        last_issued = t;
+    };
+    if (tid == 0) {
+        const int n0 = min(PMGB_NSTAGE, S.n_tiles);
+        for (int t = 0; t < n0; ++t) issue(t);
+    }
+    const Geo2 g2{f2(S.h00), f2(S.h01), f2(S.h02), f2(S.h11), f2(S.h12), f2(S.h22),
+                  f2(S.p00), f2(S.p01), f2(S.p02), f2(S.p11), f2(S.p12), f2(S.p22),
+                  S.rc2, S.rc2e, f2(0.5f * S.alpha), f2(-S.alpha * S.alpha * 1.4426950408889634f)};
+    const float2 c1 = f2(1.1283791670955126f * S.alpha);  // 2 alpha / sqrt(pi)
+    float lj_hi[NS], lj_lo[NS], ph_hi[NS], ph_lo[NS];
+    float2 gx[NS], gy[NS], gz[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+        lj_hi[k] = lj_lo[k] = ph_hi[k] = ph_lo[k] = 0.0f;
+        gx[k] = gy[k] = gz[k] = f2(0.0f);
+    }
+    bool ovl = false, abort = false;
+    int fail_tile = 0;
+    for (int t = 0; t < S.n_tiles; ++t) {
+        const int slot = t % PMGB_NSTAGE;
+        const uint32_t parity = static_cast<uint32_t>(t / PMGB_NSTAGE) & 1u;
+        const bool ok = mbar_wait_bounded(&bars[slot], parity);
+        if (__syncthreads_or(!ok)) {
+            abort = true;
+            fail_tile = t;
+            break;
+        }
+        const int4* T = stage + size_t(slot) * PMGB_TILE;
+        const int t0 = t * PMGB_TILE;
+        const int t1 = min(t0 + PMGB_TILE, S.n_rec);
+        for (int sg = 0; sg < S.n_seg; ++sg) {
+            const SegDesc d = S.seg[sg];
+            const int lo = max(d.lo, t0), hi = min(d.hi, t1);
+            if (lo >= hi) continue;
+            float r2o[NS], segmin[NS], lj12[NS], lj6[NS];
+#pragma unroll
+            for (int k = 0; k < NS; ++k) {
+                const SitePar p = S.segpar[sg * PMGB_MAX_SITES + k];
+                r2o[k] = p.r2ovl;
+                lj12[k] = p.lj12;
+                lj6[k] = p.lj6;
+                segmin[k] = __int_as_float(0x7f800000);
+            }
+            float2 i12[NS], i6[NS];
+#pragma unroll
+            for (int k = 0; k < NS; ++k) i12[k] = i6[k] = f2(0.0f);
+            for (int j0 = lo; j0 < hi; j0 += kChunk) {
+                const int j1 = min(j0 + kChunk, hi);
+                float2 ljp2[NS], php2[NS];
+#pragma unroll
+                for (int k = 0; k < NS; ++k) ljp2[k] = php2[k] = f2(0.0f);
+                for (int j = j0; j < j1; j += 2) {
+                    const bool pair = j + 1 < j1;
+                    const int4 ra = T[j - t0];
+                    const int4 rb = pair ? T[j + 1 - t0] : ra;
+                    const float2 mask = make_float2(1.0f, pair ? 1.0f : 0.0f);
+#pragma unroll
+                    for (int k = 0; k < NS; ++k) {
+                        Grad2 G{i12[k], i6[k], gx[k], gy[k], gz[k]};
+                        pair2_grad<CHARGED>(ra, rb, ux[k], uy[k], uz[k], g2, f2(lj12[k]), f2(lj6[k]),
+                                            f2(S.q[k] * static_cast<float>(S.coul)), c1, mask, segmin[k], ljp2[k],
+                                            php2[k], G);
+                        i12[k] = G.i12;
+                        i6[k] = G.i6;
+                        gx[k] = G.gx;
+                        gy[k] = G.gy;
+                        gz[k] = G.gz;
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < NS; ++k) {
+                    two_sum_acc(lj_hi[k], lj_lo[k], ljp2[k].x + ljp2[k].y);
+                    if (CHARGED) two_sum_acc(ph_hi[k], ph_lo[k], php2[k].x + php2[k].y);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < NS; ++k) ovl = ovl || (segmin[k] < r2o[k]);
+            // this thread owns its item's columns: write on the segment's first tile, add after
+            if (valid) {
+                const bool first = (lo == d.lo);
+#pragma unroll
+                for (int k = 0; k < NS; ++k) {
+                    float* c12 = a.dsum + static_cast<size_t>((sg * NS + k) * 2) * a.dsum_stride + item;
+                    float* c6 = c12 + a.dsum_stride;
+                    const float v12 = i12[k].x + i12[k].y, v6 = i6[k].x + i6[k].y;
+                    *c12 = first ? v12 : *c12 + v12;
+                    *c6 = first ? v6 : *c6 + v6;
+                }
+            }
+        }
+        __syncthreads();
+        if (tid == 0 && t + PMGB_NSTAGE < S.n_tiles) {
+            fence_proxy_async_smem();
+            issue(t + PMGB_NSTAGE);
+        }
+    }
+    if (abort) {
+        if (tid == 0) {
+            atomicOr(a.status, PMGB_DEVERR_TMA_TIMEOUT);
+            for (int t = fail_tile; t <= last_issued; ++t)
+                (void)mbar_wait_bounded(&bars[t % PMGB_NSTAGE], static_cast<uint32_t>(t / PMGB_NSTAGE) & 1u);
+        }
+        return;
+    }
+    float pl_hi = 0.0f, pl_lo = 0.0f;
+    float gu[NS][3];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) gu[k][0] = gu[k][1] = gu[k][2] = 0.0f;
+    if (CHARGED && valid) kspace_fwd<NS, true>(S, ux, uy, uz, pl_hi, pl_lo, gu);
+
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    double uv = 0.0, usr = 0.0, ulr = 0.0;
+    float gcx = 0.0f, gcy = 0.0f, gcz = 0.0f;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+        if (k < S.n_sites) {
+            uv += static_cast<double>(lj_hi[k]) + static_cast<double>(lj_lo[k]);
+            if (CHARGED && S.q[k] != 0.0f)
+                usr += static_cast<double>(S.q[k]) * (static_cast<double>(ph_hi[k]) + static_cast<double>(ph_lo[k]));
+            // real space: dU/dx_site = -2 sum c dU/dr^2; reciprocal space: G^T dU/du
+            gcx += -2.0f * (gx[k].x + gx[k].y) + S.g00 * gu[k][0];
+            gcy += -2.0f * (gy[k].x + gy[k].y) + S.g01 * gu[k][0] + S.g11 * gu[k][1];
+            gcz += -2.0f * (gz[k].x + gz[k].y) + S.g02 * gu[k][0] + S.g12 * gu[k][1] + S.g22 * gu[k][2];
+        }
+    }
+    if (ovl) uv = inf;
+    usr *= S.coul;
+    if (CHARGED) ulr = static_cast<double>(pl_hi) + static_cast<double>(pl_lo);
+    if (valid && a.grad_u) {
+        a.grad_u[3 * item + 0] = gcx;
+        a.grad_u[3 * item + 1] = gcy;
+        a.grad_u[3 * item + 2] = gcz;
+    }
+    if (a.out_mode == OUT_ENERGY) {
+        if (valid) {
+            a.e_out[3 * item + 0] = uv;
+            a.e_out[3 * item + 1] = usr;
+            a.e_out[3 * item + 2] = ulr;
+        }
+        return;
+    }
+    if (a.out_mode == OUT_GRID) {
+        if (valid) {
+            a.grid_out[item] = static_cast<float>(uv * static_cast<double>(a.unit_factor));
+            if (a.u_out) a.u_out[item] = uv;
+        }
+        return;
+    }
+    const double ues = usr + ulr;
+    if (valid && a.u_out) {
+        a.u_out[2 * item + 0] = uv;
+        a.u_out[2 * item + 1] = ues;
+    }
+    double x = -inf, ev = 0.0, ee = 0.0;
+    long long ninf = 0;
+    if (valid) {
+        const double u = uv + ues;
+        if (isfinite(u)) {
+            x = -u * a.inv_temperature;
+            ev = uv;
+            ee = ues;
+        } else {
+            ninf = 1;
+        }
+    }
+    const unsigned full = 0xffffffffu;
+    double m = x;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(full, m, o));
+    double w = (m == -inf || x == -inf) ? 0.0 : exp(x - m);
+    double s = w, tv = w * ev, te = w * ee;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(full, s, o);
+        tv += __shfl_xor_sync(full, tv, o);
+        te += __shfl_xor_sync(full, te, o);
+        ninf += __shfl_xor_sync(full, ninf, o);
+    }
+    const int warp = tid >> 5, lane = tid & 31;
+    if (lane == 0) red[warp] = LsePartial{m, s, tv, te, ninf, 0};
+    __syncthreads();
+    if (warp == 0) {
+        constexpr int NW = PMGB_THREADS / 32;
+        LsePartial p = (lane < NW) ? red[lane] : LsePartial{-inf, 0.0, 0.0, 0.0, 0, 0};
+        double M = p.m;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) M = fmax(M, __shfl_xor_sync(full, M, o));
+        const double f = (M == -inf || p.m == -inf) ? 0.0 : exp(p.m - M);
+        double s2 = p.s * f, tv2 = p.tv * f, te2 = p.te * f;
+        long long n2 = p.n_inf;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s2 += __shfl_xor_sync(full, s2, o);
+            tv2 += __shfl_xor_sync(full, tv2, o);
+            te2 += __shfl_xor_sync(full, te2, o);
+            n2 += __shfl_xor_sync(full, n2, o);
+        }
+        if (lane == 0) a.partials[blockIdx.x] = LsePartial{M, s2, tv2, te2, n2, 0};
+    }
+}
+
+// log_scale[0] = max_i (-U_i / T) over finite U (one CTA, fixed order)
+__global__ void max_neg_u_kernel(const double* __restrict__ u, long long n, double inv_t, double* __restrict__ out) {
+    __shared__ double red[32];
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    double m = -inf;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x)
+        if (isfinite(u[i])) m = fmax(m, -u[i] * inv_t);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = -inf;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v = fmax(v, red[w]);
+        out[0] = v;
+    }
+}
+
+// Per-chunk weighted column sums: partials[chunk * (n_cols + 2) + c] = sum_{i in chunk} w_i col_c[i],
+// with two extra columns sum w_i and sum w_i U_es,i.  w_i = exp(-(U_vdw + U_es)/T - M) where M is
+// the largest log-sum of the statistics blocks (so every w_i <= 1), 0 for infinite energies.
+__global__ void weighted_columns_kernel(const double* __restrict__ u, int u_stride, long long n, double inv_t,
+                                        const double* __restrict__ log_scale, int n_log,
+                                        const float* __restrict__ cols, int n_cols, long long col_stride,
+                                        double* __restrict__ partials) {
+    __shared__ double red[8][34];
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    double M = -inf;
+    for (int b = 0; b < n_log; ++b) M = fmax(M, log_scale[4 * b]);
+    const long long chunk = (n + gridDim.x - 1) / gridDim.x;
+    const long long i0 = blockIdx.x * chunk, i1 = min(n, i0 + chunk);
+    const int nc = n_cols + 2;
+    for (int c0 = 0; c0 < nc; c0 += 32) {
+        double acc[32];
+#pragma unroll
+        for (int c = 0; c < 32; ++c) acc[c] = 0.0;
+        for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+            double ue = 0.0, uu = inf;
+            if (u_stride == 2) {
+                ue = u[2 * i + 1];
+                uu = u[2 * i] + ue;
+            } else {
+                uu = u[i];
+            }
+            const double w = (isfinite(uu) && M > -inf) ? exp(-uu * inv_t - M) : 0.0;
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                const int cc = c0 + c;
+                if (cc < n_cols) acc[c] = fma(w, static_cast<double>(cols[static_cast<size_t>(cc) * col_stride + i]), acc[c]);
+                else if (cc == n_cols) acc[c] += w;
+                else if (cc == n_cols + 1) acc[c] = fma(w, isfinite(uu) ? ue : 0.0, acc[c]);
+            }
+        }
+        // block reduction in a fixed order
+#pragma unroll
+        for (int c = 0; c < 32; ++c) {
+            double v = acc[c];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][c] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double v = 0.0;
+            for (int wv = 0; wv < (int)(blockDim.x >> 5); ++wv) v += red[wv][threadIdx.x];
+            const int cc = c0 + threadIdx.x;
+            if (cc < nc) partials[static_cast<size_t>(blockIdx.x) * nc + cc] = v;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void sum_partials_kernel(const double* __restrict__ partials, int n_chunks, int nc,
+                                    double* __restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    double v = 0.0;
+    for (int k = 0; k < n_chunks; ++k) v += partials[static_cast<size_t>(k) * nc + c];
+    out[c] = v;
+}
+
 // Combine the per-CTA partials of each statistics block in a fixed order.
 // block_out[4b..4b+3] = (log sum e^{-U/T}, <U_vdw>_bf, <U_es>_bf, #insertions with U=+Inf)
 __global__ void reduce_blocks_kernel(const LsePartial* __restrict__ partials, int ctas_per_block,
@@ -790,6 +1255,27 @@ cudaError_t launch_one(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+template <int NS, bool CH>
+cudaError_t launch_grad_one(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
+    const size_t smem = pmgb_pairs_smem_bytes();
+    cudaError_t e = cudaFuncSetAttribute(pairs_grad_kernel<NS, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    pairs_grad_kernel<NS, CH><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <bool CH>
+cudaError_t launch_grad_ns(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
+    const int n = a.sys.n_sites;
+    if (n <= 1) return launch_grad_one<1, CH>(a, n_ctas, st);
+    if (n <= 2) return launch_grad_one<2, CH>(a, n_ctas, st);
+    if (n <= 3) return launch_grad_one<3, CH>(a, n_ctas, st);
+    if (n <= 4) return launch_grad_one<4, CH>(a, n_ctas, st);
+    if (n <= 6) return launch_grad_one<6, CH>(a, n_ctas, st);
+    return launch_grad_one<8, CH>(a, n_ctas, st);
+}
+
 template <bool CH>
 cudaError_t launch_ns(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
     const int n = a.sys.n_sites;
@@ -810,6 +1296,29 @@ size_t pmgb_pairs_smem_bytes() {
 cudaError_t pmgb_launch_pairs(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
     if (n_ctas <= 0) return cudaSuccess;
     return a.sys.charged ? launch_ns<true>(a, n_ctas, st) : launch_ns<false>(a, n_ctas, st);
+}
+
+cudaError_t pmgb_launch_pairs_grad(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
+    if (n_ctas <= 0) return cudaSuccess;
+    return a.sys.charged ? launch_grad_ns<true>(a, n_ctas, st) : launch_grad_ns<false>(a, n_ctas, st);
+}
+
+cudaError_t pmgb_launch_max_neg_u(const double* u, long long n, double inv_t, double* out, cudaStream_t st) {
+    max_neg_u_kernel<<<1, 1024, 0, st>>>(u, n, inv_t, out);
+    return cudaGetLastError();
+}
+
+cudaError_t pmgb_launch_weighted_columns(const double* u, int u_stride, long long n, double inv_t,
+                                         const double* log_scale, int n_log, const float* cols, int n_cols,
+                                         long long col_stride, double* partials, int n_chunks, double* out,
+                                         cudaStream_t st) {
+    weighted_columns_kernel<<<n_chunks, 256, 0, st>>>(u, u_stride, n, inv_t, log_scale, n_log, cols, n_cols,
+                                                      col_stride, partials);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int nc = n_cols + 2;
+    sum_partials_kernel<<<(nc + 127) / 128, 128, 0, st>>>(partials, n_chunks, nc, out);
+    return cudaGetLastError();
 }
 
 cudaError_t pmgb_launch_reduce_blocks(const LsePartial* partials, int n_blocks, int ctas_per_block,

@@ -145,3 +145,39 @@ def henry_coefficient(crystal: Crystal, molecule: Molecule, temperature: float, 
         for key in ["henry coefficient [mmol/(g-bar)]", "⟨U, vdw⟩ (kJ/mol)", "⟨U, es⟩ (kJ/mol)", "Qst (kJ/mol)"]:
             print(f"\t{key} = {r[key]:f} +/- {r['err ' + key]:f}")
     return r
+
+
+def henry_coefficient_gradient(crystal: Crystal, molecule: Molecule, temperature: float,
+                               ljforcefield: LJForceField, *, insertions_per_volume: float = 200,
+                               ewald_precision: float = 1e-6, seed: int | None = None,
+                               want_forces: bool = False, system_out: list | None = None):
+    """K_H and its derivatives from one adjoint pass (pair terms recomputed, not stored).
+
+    Returns a dict: 'henry coefficient [mol/(m³-bar)]' (block mean, as henry_coefficient),
+    'dKH/d epsilon' and 'dKH/d sigma' (per species, the pure LJ parameters, through the force
+    field's mixing rule), 'dKH/d charge scale' (framework charges scaled by λ at λ = 1), and
+    with want_forces the per-insertion dU/dx of the centre of mass (K/Å; force = -dU/dx)."""
+    from .adjoint import henry_gradients
+
+    assert_P1_symmetry(crystal)
+    temperature = float(temperature)
+    nb_insertions = max(N_BLOCKS, math.ceil(insertions_per_volume * crystal.box.Omega))
+    nb_per_block = math.ceil(nb_insertions / N_BLOCKS)
+    repfactors = replication_factors(crystal.box, ljforcefield)
+    sc = replicate(crystal, repfactors)
+    charged = has_charges(sc) and molecule.n_charges > 0
+    eparams = setup_Ewald_sum(sc.box, ljforcefield.r_cutoff, eps=ewald_precision) if charged else None
+    if seed is None:
+        seed = secrets.randbits(63)
+    system = GPUSystem(sc, Frac(molecule, sc.box), ljforcefield, eparams)
+    if system_out is not None:
+        system_out.append(system)
+    blocks, adj = system.widom_adjoint(nb_per_block, N_BLOCKS, seed, temperature, want_grad=want_forces)
+    kh = np.exp(blocks[:, 0] - math.log(UNIV_GAS_CONST * temperature * nb_per_block))
+    d_eps, d_sig, d_lam = henry_gradients(system, blocks, adj, temperature, nb_per_block)
+    out = {"henry coefficient [mol/(m³-bar)]": float(np.mean(kh)), "dKH/d epsilon": d_eps, "dKH/d sigma": d_sig,
+           "dKH/d charge scale": d_lam if charged else 0.0, "blocks": blocks, "seed": int(seed),
+           "n_insertions_per_block": nb_per_block}
+    if want_forces:
+        out["dU/dx"] = adj["grad"]
+    return out

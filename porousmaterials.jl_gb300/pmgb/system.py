@@ -123,6 +123,53 @@ class GPUSystem:
                                                 float(temperature), ptr(block, C.c_double), ptr(u, C.c_double)))
         return block, u
 
+    def widom_adjoint(self, n_per_block: int, n_blocks: int, seed: int, temperature: float,
+                      want_energies: bool = False, want_grad: bool = False):
+        """Widom block results plus Σ_i w_i ∂U_i/∂θ (see pmgb_widom_adjoint) as a dict:
+        log_scale M, sum_w, sum_w_ues, d_eps / d_sig2 (n_species x n_species over self.species,
+        row = guest species, column = framework species); optional per-insertion energies and
+        dU/dx_COM."""
+        ns = len(self.species)
+        block = np.zeros((n_blocks, 4))
+        dth = np.zeros(3 + 2 * ns * ns)
+        u = np.zeros((n_blocks * n_per_block, 2)) if want_energies else None
+        g = np.zeros((n_blocks * n_per_block, 3), dtype=np.float32) if want_grad else None
+        self.ctx.check(self.ctx._lib.pmgb_widom_adjoint(self.handle, int(n_per_block), int(n_blocks), int(seed),
+                                                        float(temperature), ptr(block, C.c_double),
+                                                        ptr(dth, C.c_double), ptr(u, C.c_double), ptr(g, C.c_float)))
+        pair = dth[3:].reshape(ns, ns, 2)
+        return block, {"log_scale": dth[0], "sum_w": dth[1], "sum_w_ues": dth[2], "d_eps": pair[:, :, 0].copy(),
+                       "d_sig2": pair[:, :, 1].copy(), "u": u, "grad": g}
+
+    def energies_grad(self, site_xf: np.ndarray):
+        """((n, 3) energies as in energies(), (n, 3) dU/dx of the rigid configuration, K/Å)."""
+        site_xf = np.ascontiguousarray(site_xf, dtype=np.float64).reshape(-1, self.n_sites, 3)
+        n = site_xf.shape[0]
+        out = np.zeros((n, 3))
+        g = np.zeros((n, 3), dtype=np.float32)
+        self.ctx.check(self.ctx._lib.pmgb_energies_grad(self.handle, n, ptr(site_xf, C.c_double), ptr(out, C.c_double),
+                                                        ptr(g, C.c_float)))
+        return out, g
+
+    def energy_grid_adjoint(self, n_pts, repfactors, unit_factor: float, temperature: float):
+        n = np.ascontiguousarray(n_pts, dtype=np.int32)
+        r = np.ascontiguousarray(repfactors, dtype=np.int32)
+        total = int(np.prod(n))
+        out = np.zeros(total, dtype=np.float32)
+        g = np.zeros((total, 3), dtype=np.float32)
+        ns = len(self.species)
+        dth = np.zeros(3 + 2 * ns * ns)
+        self.ctx.check(self.ctx._lib.pmgb_energy_grid_adjoint(self.handle, ptr(n, C.c_int32), ptr(r, C.c_int32),
+                                                              float(unit_factor), float(temperature),
+                                                              ptr(out, C.c_float), ptr(g, C.c_float),
+                                                              ptr(dth, C.c_double)))
+        shape = tuple(int(v) for v in n[::-1])
+        data = out.reshape(shape).transpose(2, 1, 0)
+        grad = g.reshape(shape + (3,)).transpose(2, 1, 0, 3)
+        pair = dth[3:].reshape(ns, ns, 2)
+        return data, grad, {"log_scale": dth[0], "sum_w": dth[1], "d_eps": pair[:, :, 0].copy(),
+                            "d_sig2": pair[:, :, 1].copy()}
+
     def energy_grid(self, n_pts, repfactors, unit_factor: float) -> np.ndarray:
         n = np.ascontiguousarray(n_pts, dtype=np.int32)
         r = np.ascontiguousarray(repfactors, dtype=np.int32)

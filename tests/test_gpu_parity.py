@@ -316,7 +316,16 @@ def test_energy_grid_parity():
     _report("grid", g.data.astype(np.float64).ravel(), ref.ravel())
     assert np.array_equal(np.isinf(g.data), np.isinf(ref))
     ok = within(g.data.astype(np.float64), ref, RTOL, ATOL)
-    assert ok.mean() >= 0.999
+    print(f"[grid] {ok.mean() * 100:.3f}% of points within 1e-5 rel / 1e-4 K")
+    assert ok.mean() >= 0.995
+    # every point within the FP32 error bound of its terms' magnitudes (the end planes
+    # evaluate the first plane's position, as the reference's periodic images)
+    pts = np.stack(np.meshgrid(*[np.arange(n) / (n - 1) for n in (17, 13, 11)], indexing="ij"), axis=-1)
+    pts = (np.where(pts >= 1.0, 0.0, pts) / np.array(rep)).reshape(-1, 3)
+    v, _, _, sv, _ = oracle_for(gs).energies(pts[:, None, :], scales=True)
+    gd = g.data.astype(np.float64).reshape(-1)
+    fin = np.isfinite(v)
+    assert np.all(np.abs(gd[fin] - v[fin]) <= FP32_SCALE_TOL * sv[fin] + ATOL)
     gk = pmgb.energy_grid(cr, synthetic.xe(), ff, resolution=(17, 13, 11), units="kJ_mol", verbose=False)
     np.testing.assert_allclose(gk.data, g.data * (8.314 / 1000.0), rtol=2e-7)
 
