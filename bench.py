@@ -47,6 +47,9 @@ def parse():
     p.add_argument("--insertions", type=int, default=N_INS)
     p.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline leg (profiling runs)")
     p.add_argument("--skip-e2e", action="store_true", help="omit the end-to-end leg (profiling runs)")
+    p.add_argument("--batch-frameworks", type=int, default=512,
+                   help="frameworks in the batched-screening leg (each with CH4 and CO2; 0 = skip)")
+    p.add_argument("--batch-insertions", type=int, default=20000, help="insertions per (framework, guest)")
     return p.parse_args()
 
 
@@ -197,6 +200,107 @@ def reference_arm(args, rank, world):
     print(json.dumps(out), flush=True)
 
 
+# ------------------------------------------------------------------ batched screening leg
+def batched_leg(args, ctx, stream):
+    """Batched vs plain forward + adjoint Widom over uneven synthetic frameworks.
+
+    Frameworks: atoms log-uniform 50-5000, cell lengths U(8, 40) Å, angles U(80, 110)°,
+    neutralised N(0, 0.4) charges, replicated for the 12.5 Å cutoff; each with CH4 (LJ) and
+    CO2 (LJ + Ewald 1e-6); args.batch_insertions insertions per system in 5 blocks.
+      plain   : GPUSystem.widom_adjoint per system, one after another (each call returns its
+                results to the host, as henry_coefficient_gradient does per framework)
+      batched : BatchScreen.run -- one graph replay of the persistent kernel + per-system
+                reduction, then the results copy (the same outputs for every system)
+    Systems are built once, outside both timings."""
+    import numpy as np
+    import torch
+
+    from pmgb import synthetic
+    from pmgb.batch import BatchScreen, build_systems
+
+    t0 = time.perf_counter()
+    fws = synthetic.batch_frameworks(args.batch_frameworks)
+    ff = synthetic.forcefield(12.5)
+    systems = build_systems(fws, synthetic.ch4(), ff, ctx=ctx) + build_systems(fws, synthetic.co2(), ff, ctx=ctx)
+    t_setup = time.perf_counter() - t0
+    npb = max(1, args.batch_insertions // N_BLOCKS)
+    n_ins = npb * N_BLOCKS * len(systems)
+    sizes = np.array([gs.info()["n_records"] for gs in systems[:len(fws)]])
+
+    def plain(adjoint):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for s, gs in enumerate(systems):
+            if adjoint:
+                gs.widom_adjoint(npb, N_BLOCKS, 900 + s, T)
+            else:
+                gs.widom(npb, N_BLOCKS, 900 + s, T)
+        return time.perf_counter() - t
+
+    def dropin(adjoint):
+        """The drop-in call per (framework, guest), set-up included, as a screening loop over
+        henry_coefficient / henry_coefficient_gradient would run it."""
+        import pmgb
+
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        s = 0
+        for mol in (synthetic.ch4(), synthetic.co2()):
+            for cr in fws:
+                ipv = npb * N_BLOCKS / cr.box.Omega
+                if adjoint:
+                    pmgb.henry_coefficient_gradient(cr, mol, T, ff, insertions_per_volume=ipv, seed=700 + s)
+                else:
+                    pmgb.henry_coefficient(cr, mol, T, ff, insertions_per_volume=ipv, seed=700 + s, verbose=False,
+                                           autosave=False)
+                s += 1
+        return time.perf_counter() - t
+
+    out = {}
+    for adjoint in (False, True):
+        t_dropin = dropin(adjoint)
+        plain(adjoint)  # warm-up: per-system scratch allocations
+        t_plain = min(plain(adjoint) for _ in range(2))
+        screen = BatchScreen(systems, npb, N_BLOCKS, with_adjoint=adjoint, ctx=ctx)
+        tuned_ms = screen.tune(1, T, repeats=2)
+        info = screen.info()
+        for w in range(args.warmup):
+            screen.run(2 + w, T)
+        k = max(3, args.steps // 2)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for i in range(k):
+            ev[i][0].record(stream)
+            screen.launch(100 + i, T)
+            ev[i][1].record(stream)
+            screen.results()
+        t_batched = (time.perf_counter() - t) / k
+        ms_dev = sum(a.elapsed_time(b) for a, b in ev) / k
+        screen.close()
+        key = "forward_plus_adjoint" if adjoint else "forward"
+        out[key] = {"plain_dropin_insertions_per_s": n_ins / t_dropin, "plain_dropin_s": t_dropin,
+                    "speedup_vs_plain_dropin": t_dropin / t_batched,
+                    "plain_insertions_per_s": n_ins / t_plain, "plain_s": t_plain,
+                    "batched_insertions_per_s": n_ins / t_batched, "batched_s": t_batched,
+                    "batched_device_ms": ms_dev, "batched_device_insertions_per_s": n_ins / (ms_dev * 1e-3),
+                    "speedup_vs_plain": t_plain / t_batched, "tuned": {"n_ctas": info["n_ctas"],
+                    "order": ["cost-descending", "by-system"][info["order"]], "ms": tuned_ms},
+                    "work_units": info["n_units"], "gpu_launches_per_run": 2}
+    assert ctx.device_status() == 0
+    out.update({"systems": len(systems), "frameworks": len(fws), "guests": ["CH4", "CO2"],
+                "insertions_per_system": npb * N_BLOCKS, "insertions_per_run": n_ins,
+                "framework_sites": {"min": int(sizes.min()), "median": float(np.median(sizes)),
+                                    "max": int(sizes.max()), "total": int(sizes.sum())},
+                "setup_s": t_setup,
+                "timing": "plain_dropin: wall clock of henry_coefficient(_gradient) per (framework, guest), "
+                          "set-up included (one pass); plain: wall clock of the per-system loop over pre-built "
+                          "systems (best of 2); batched: wall clock of launch + results per run over the same "
+                          "pre-built systems, and CUDA events around the graph replay; setup_s: building the "
+                          "batch's systems once"})
+    return out
+
+
 # ------------------------------------------------------------------ GPU arm
 def ours(args, rank, world, local_rank):
     global _tables
@@ -295,6 +399,10 @@ def ours(args, rank, world, local_rank):
                "d2h_bytes_per_step": N_BLOCKS * 4 * 8, "call": "pmgb.henry_coefficient (host set-up + "
                "pmgb_system_create + pmgb_system_set_ewald + pmgb_widom)"}
 
+    batched = None
+    if args.batch_frameworks > 0 and rank == 0:
+        batched = batched_leg(args, ctx, stream)
+
     if rank != 0:
         return
     fpi = flops_per_insertion(sc, mol, ep)
@@ -320,6 +428,7 @@ def ours(args, rank, world, local_rank):
                         "flops_per_insertion": fpi,
                         "kernel": "pairs_kernel<3,true> + reduce_blocks_kernel per step"},
            "forward_plus_adjoint": adj,
+           "batched": batched,
            "clocks": clk.summary(),
            "wall_s_timed_region": t_wall,
            "e2e": e2e,

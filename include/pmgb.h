@@ -48,7 +48,8 @@ typedef struct pmgb_system pmgb_system;
 int pmgb_abi_version(void);
 
 /* Create a context on CUDA device `device` with its own stream.  No reference
- * counterpart: the reference runs in Julia worker processes (src/henry.jl:109). */
+ * counterpart: the reference runs in Julia worker processes (src/henry.jl:109).
+ * Systems and batches keep their context alive: handles may be destroyed in any order. */
 int pmgb_create(int device, pmgb_ctx** out);
 void pmgb_destroy(pmgb_ctx* ctx);
 
@@ -132,6 +133,15 @@ int pmgb_energies(pmgb_system* sys, int64_t n_conf, const double* site_xf, doubl
 int pmgb_widom(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
                double temperature, double* block_out, double* u_out);
 
+/* FP64 refinement of the Boltzmann tail for this system's Widom runs (pmgb_widom,
+ * pmgb_widom_device, pmgb_widom_adjoint; default off): after the FP32 pass, the insertions that
+ * carry all but `tail_fraction` of each block's Boltzmann weight are re-evaluated in FP64 (LJ,
+ * real-space erfc, reciprocal space on the FP64 S(k)) and the block results corrected, so that
+ * log K_H is exact to tail_fraction x the FP32 error of the remainder.  Refined insertions
+ * report their FP64 energies in u_out.  0 switches it off.  No reference counterpart: the
+ * reference is FP64 throughout (src/henry.jl:212-244). */
+int pmgb_system_set_refine(pmgb_system* sys, double tail_fraction);
+
 /* Same computation on device-resident outputs, enqueued on the context stream without
  * synchronising (block_out_dev: 4*n_blocks doubles, u_out_dev optional). */
 int pmgb_widom_device(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
@@ -193,6 +203,46 @@ int pmgb_energy_grid_device(pmgb_system* sys, const int32_t n_pts[3], const int3
 int pmgb_energy_grid_adjoint(pmgb_system* sys, const int32_t n_pts[3], const int32_t repfactors[3],
                              double unit_factor, double temperature, float* out, float* grad_out,
                              double* dtheta);
+
+/* ---- batched screening (no reference counterpart: henry_coefficient takes one framework
+ * per call, src/henry.jl:34) ---------------------------------------------------------------
+ * Widom insertions for many systems (each its own framework and guest, of any size) in one
+ * persistent kernel launch, captured once in a CUDA graph and replayed.  System s runs
+ * n_blocks blocks of n_per_block[s] insertions with Philox key seed + s * 0x9E3779B97F4A7C15
+ * (mod 2^64): the insertions, energies and block results of pmgb_widom with that seed.
+ * with_adjoint adds the Boltzmann-weighted parameter sums of pmgb_widom_adjoint (dtheta),
+ * accumulated inside the launch with weights relative to M = max_i -U_i/T of each system.
+ * All systems must belong to ctx and stay alive while the batch exists. */
+typedef struct pmgb_batch pmgb_batch;
+int pmgb_batch_create(pmgb_ctx* ctx, int32_t n_systems, pmgb_system* const* systems,
+                      const int64_t* n_per_block, int32_t n_blocks, int32_t with_adjoint,
+                      pmgb_batch** out);
+void pmgb_batch_destroy(pmgb_batch* batch);
+
+/* Launch shape: n_ctas resident CTAs pulling work units (0 = two per SM, the maximum), the
+ * unit order (0: estimated cost, largest first; 1: system by system) and the insertion tile
+ * of a unit: runs of 256-insertion chunks of one block worth about unit_mflop MFLOP, over
+ * which a framework that fits the shared-memory ring stays resident (0: one chunk per unit).
+ * Re-captures the graph; results of earlier runs are no longer available. */
+int pmgb_batch_configure(pmgb_batch* batch, int32_t n_ctas, int32_t order, double unit_mflop);
+
+/* Autotuner: times candidate launch shapes (unit work 0/32/128/512 MFLOP, then 1 or 1.5 or 2
+ * CTAs per SM, then unit order) over `repeats` graph replays each with CUDA events, keeps the
+ * fastest and returns its ms per run. */
+int pmgb_batch_tune(pmgb_batch* batch, uint64_t seed, double temperature, int32_t repeats,
+                    double* best_ms_out);
+
+/* Enqueue one run (one graph replay) on the context stream; does not synchronise. */
+int pmgb_batch_launch(pmgb_batch* batch, uint64_t seed, double temperature);
+
+/* Wait for the last run and copy out its results: block_out[(s*n_blocks + b)*4 ..] as
+ * pmgb_widom's, and with the adjoint dtheta: per system, in order, 3 + 2*n_species(s)^2
+ * doubles laid out as pmgb_widom_adjoint's (dtheta may be NULL without the adjoint). */
+int pmgb_batch_results(pmgb_batch* batch, double* block_out, double* dtheta);
+
+/* out8 = (work units, n_ctas, order, dtheta length, device bytes held, insertions per run,
+ *         256-insertion chunks, unit MFLOP target). */
+int pmgb_batch_info(const pmgb_batch* batch, int64_t* out8);
 
 /* ---- utilities -------------------------------------------------------------------------- */
 

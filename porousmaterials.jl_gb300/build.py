@@ -20,7 +20,7 @@ OUT_DIR = HERE / "pmgb"
 LIB = OUT_DIR / "libpmgb.so"
 OBJ_DIR = HERE / "_build"
 
-SOURCES = ["pmgb_kernels.cu", "pmgb_api.cu"]
+SOURCES = ["pmgb_kernels.cu", "pmgb_batch.cu", "pmgb_refine.cu", "pmgb_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-ftz=true", "-Xcompiler", "-fPIC,-O2", f"-I{INCLUDE}", f"-I{CSRC}"]
 

@@ -38,6 +38,7 @@ struct DevBuf {
 }  // namespace
 
 struct pmgb_ctx {
+    int refs = 1;                   // the handle itself + one per live system or batch
     int device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
@@ -50,9 +51,12 @@ struct pmgb_system {
     SysDev dev{};
     // device allocations
     int4* d_rec = nullptr;
+    double* d_rec_q = nullptr;
+    double2* d_segpar64 = nullptr;
     SegDesc* d_seg = nullptr;
     SitePar* d_segpar = nullptr;
-    uint32_t* d_qfix = nullptr;
+    double* d_qxf = nullptr;         // framework charge fractional coordinates (S(k))
+    double* d_rec_xf = nullptr;
     double* d_q = nullptr;
     int n_q = 0;
     KRow* d_krow = nullptr;
@@ -72,7 +76,9 @@ struct pmgb_system {
     std::vector<int> site_species;  // guest LJ species of each site (-1: charge-only site)
     int site_atom[PMGB_MAX_SITES];
     int site_charge[PMGB_MAX_SITES];
+    double refine_tail = 0.0;       // FP64 refinement of the Boltzmann tail (0: off)
     // grow-only scratch used by launches
+    DevBuf r_hist, r_cut, r_counts, r_offsets, r_list, r_ref;  // refinement scratch
     DevBuf partials, block_out, in_buf, out_buf, axes;
     DevBuf g_u, g_dsum, g_grad, g_part, g_cols;  // adjoint scratch
 };
@@ -232,13 +238,24 @@ extern "C" int pmgb_create(int device, pmgb_ctx** out) {
     return PMGB_OK;
 }
 
+// Systems and batches hold a reference to their context, so handles may be destroyed in any
+// order (garbage-collected hosts finalise in no particular order); the context is freed with
+// its last holder.
+static void ctx_release(pmgb_ctx* ctx) {
+    if (--ctx->refs > 0) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+    if (ctx->d_status) cudaFree(ctx->d_status);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
 extern "C" void pmgb_destroy(pmgb_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    if (ctx->d_status) cudaFree(ctx->d_status);
-    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
-    delete ctx;
+    ctx->stream = ctx->own_stream;  // a caller's stream may not outlive this handle
+    ctx_release(ctx);
 }
 
 extern "C" const char* pmgb_last_error(const pmgb_ctx* ctx) {
@@ -273,10 +290,11 @@ extern "C" int pmgb_device_status(pmgb_ctx* ctx, uint32_t* status_out) {
 // system
 // ============================================================================
 static void free_system_device(pmgb_system* s) {
-    void* ptrs[] = {s->d_rec,      s->d_seg,       s->d_segpar,  s->d_qfix,   s->d_q,     s->d_krow,
+    void* ptrs[] = {s->d_rec,      s->d_rec_q,     s->d_segpar64, s->d_seg,   s->d_segpar,  s->d_qxf,    s->d_rec_xf, s->d_q,     s->d_krow,
                     s->d_skw,      s->d_sk,        s->d_kabc,    s->d_wt,     s->partials.p, s->block_out.p,
                     s->in_buf.p,   s->out_buf.p,   s->axes.p,    s->g_u.p,    s->g_dsum.p, s->g_grad.p,
-                    s->g_part.p,   s->g_cols.p};
+                    s->g_part.p,   s->g_cols.p,   s->r_hist.p,  s->r_cut.p,  s->r_counts.p, s->r_offsets.p,
+                    s->r_list.p,   s->r_ref.p};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -374,6 +392,8 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     auto sp_key = [&](int i) { return recs[i].species < 0 ? n_species : recs[i].species; };
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sp_key(a) < sp_key(b); });
     std::vector<int4> h_rec;
+    std::vector<double> h_rec_q;   // FP64 charge of each record
+    std::vector<double> h_rec_xf;  // its exact fractional coordinates
     std::vector<SegDesc> h_seg;
     for (size_t p = 0; p < order.size();) {
         const int sp = recs[order[p]].species;
@@ -388,6 +408,10 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
             std::memcpy(&qbits, &qf, sizeof(qbits));
             h_rec.push_back(make_int4(static_cast<int>(to_fix(r.x)), static_cast<int>(to_fix(r.y)),
                                       static_cast<int>(to_fix(r.z)), qbits));
+            h_rec_q.push_back(r.q);
+            h_rec_xf.push_back(r.x);
+            h_rec_xf.push_back(r.y);
+            h_rec_xf.push_back(r.z);
         }
         d.hi = static_cast<int>(h_rec.size());
         d.species = sp;
@@ -449,6 +473,7 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
 
     // per (segment, site) LJ parameters
     std::vector<SitePar> h_par(h_seg.size() * PMGB_MAX_SITES, SitePar{1.0f, 0.0f, -1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f});
+    std::vector<double2> h_par64(h_seg.size() * PMGB_MAX_SITES, make_double2(-1.0, 0.0));  // -1: no LJ
     for (size_t g = 0; g < h_seg.size(); ++g)
         for (int k = 0; k < ns; ++k) {
             const int a = s->site_atom[k];
@@ -462,21 +487,24 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
             p.lj12 = static_cast<float>(e4 * s2 * s2 * s2 * s2 * s2 * s2);
             p.lj6 = static_cast<float>(-e4 * s2 * s2 * s2);
             p.r2ovl = 0.1f;  // R²_OVERLAP, src/vdw_energetics.jl:2
+            h_par64[g * PMGB_MAX_SITES + k] = make_double2(s2, e4);
         }
 
-    // charge fixed-point coordinates for S(k)
-    std::vector<uint32_t> h_qfix;
+    // charge fractional coordinates for S(k), FP64
+    std::vector<double> h_qxf;
     std::vector<double> h_q;
     for (int c = 0; c < n_charges; ++c) {
-        for (int d = 0; d < 3; ++d) h_qfix.push_back(to_fix(charge_xf[3 * c + d]));
+        for (int d = 0; d < 3; ++d) h_qxf.push_back(wrap01(charge_xf[3 * c + d]));
         h_q.push_back(charge_q[c]);
     }
     s->n_q = n_charges;
 
     int rc = PMGB_OK;
     int64_t* nb = &s->h2d_bytes;
-    if ((rc = upload(ctx, &s->d_rec, h_rec, nb)) || (rc = upload(ctx, &s->d_seg, h_seg, nb)) ||
-        (rc = upload(ctx, &s->d_segpar, h_par, nb)) || (rc = upload(ctx, &s->d_qfix, h_qfix, nb)) ||
+    if ((rc = upload(ctx, &s->d_rec, h_rec, nb)) || (rc = upload(ctx, &s->d_rec_q, h_rec_q, nb)) ||
+        (rc = upload(ctx, &s->d_segpar64, h_par64, nb)) || (rc = upload(ctx, &s->d_seg, h_seg, nb)) ||
+        (rc = upload(ctx, &s->d_segpar, h_par, nb)) || (rc = upload(ctx, &s->d_qxf, h_qxf, nb)) ||
+        (rc = upload(ctx, &s->d_rec_xf, h_rec_xf, nb)) ||
         (rc = upload(ctx, &s->d_q, h_q, nb))) {
         free_system_device(s);
         delete s;
@@ -515,9 +543,23 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     D.g11 = static_cast<float>(G[4]);
     D.g12 = static_cast<float>(G[7]);
     D.g22 = static_cast<float>(G[8]);
+    const int up[6] = {0, 3, 6, 4, 7, 8};  // column-major indices of the upper triangle
+    for (int i = 0; i < 6; ++i) {
+        D.f2c64[i] = R[up[i]];
+        D.g64[i] = G[up[i]];
+    }
     D.rc2 = static_cast<float>(r2_cutoff);
     D.rc2e = static_cast<float>(r2_cutoff);
     D.alpha = 0.0f;
+    D.rc2_64 = r2_cutoff;
+    D.rc2e_64 = r2_cutoff;
+    D.alpha64 = 0.0;
+    D.rec_q = s->d_rec_q;
+    D.rec_xf = s->d_rec_xf;
+    D.segpar64 = s->d_segpar64;
+    D.sk64 = nullptr;
+    D.wt64 = nullptr;
+    D.kabc = nullptr;
     D.coul = coulomb_constant();
     D.charged = (n_charges > 0 && n_guest_charges > 0) ? 1 : 0;
     D.n_sites = ns;
@@ -528,13 +570,16 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
             if (k < ns)
                 for (int m = 0; m < 3; ++m) v += Q[m + 3 * d] * body[k][m];
             D.body[k][d] = static_cast<float>(v);
+            D.body64[k][d] = v;
         }
         D.q[k] = (k < ns) ? static_cast<float>(sq[k]) : 0.0f;
+        D.q64[k] = (k < ns) ? sq[k] : 0.0;
     }
     D.n_krow = 0;
     D.n_k = 0;
     D.krow = nullptr;
     D.skw = nullptr;
+    ++ctx->refs;
     *out = s;
     return PMGB_OK;
 }
@@ -602,7 +647,7 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
         return rc;
     PMGB_CK(ctx, cudaMalloc(&s->d_skw, std::max<size_t>(sizeof(float2) * n_kvecs, 16)));
     PMGB_CK(ctx, cudaMalloc(&s->d_sk, std::max<size_t>(2 * sizeof(double) * n_kvecs, 16)));
-    PMGB_CK(ctx, pmgb_launch_structure_factor(s->d_qfix, s->d_q, s->n_q, s->d_kabc, s->d_wt, n_kvecs, s->d_sk,
+    PMGB_CK(ctx, pmgb_launch_structure_factor(s->d_qxf, s->d_q, s->n_q, s->d_kabc, s->d_wt, n_kvecs, s->d_sk,
                                               s->d_skw, ctx->stream));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
     s->n_k = n_kvecs;
@@ -610,6 +655,11 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
     s->ewald_set = true;
     s->dev.alpha = static_cast<float>(alpha);
     s->dev.rc2e = static_cast<float>(sr_cutoff * sr_cutoff);
+    s->dev.alpha64 = alpha;
+    s->dev.rc2e_64 = sr_cutoff * sr_cutoff;
+    s->dev.sk64 = s->d_sk;
+    s->dev.wt64 = s->d_wt;
+    s->dev.kabc = s->d_kabc;
     s->dev.n_krow = static_cast<int>(rows.size());
     s->dev.n_k = n_kvecs;
     s->dev.krow = s->d_krow;
@@ -619,10 +669,12 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
 
 extern "C" void pmgb_system_destroy(pmgb_system* s) {
     if (!s) return;
-    cudaSetDevice(s->ctx->device);
-    cudaStreamSynchronize(s->ctx->stream);
+    pmgb_ctx* ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
     free_system_device(s);
     delete s;
+    ctx_release(ctx);
 }
 
 extern "C" int pmgb_system_info(const pmgb_system* s, int64_t* out6) {
@@ -714,6 +766,50 @@ extern "C" int pmgb_energies(pmgb_system* s, int64_t n_conf, const double* site_
     return check_status(ctx);  // synchronises: the host staging vector outlives the copy
 }
 
+// Enqueue the FP64 refinement of the Boltzmann tail of a Widom run whose block results are
+// in block_out_dev and per-insertion energies in u_dev (both corrected in place).
+static int run_refine(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uint64_t seed, double temperature,
+                      double* block_out_dev, double* u_dev) {
+    pmgb_ctx* ctx = s->ctx;
+    const int64_t cpb = (n_per_block + PMGB_THREADS - 1) / PMGB_THREADS;
+    const int n_ctas = static_cast<int>(cpb * n_blocks);
+    const int64_t n = n_per_block * n_blocks;
+    int rc;
+    if ((rc = ensure(ctx, s->r_hist, sizeof(unsigned long long) * pmgb_refine_hist_words() * n_blocks)) ||
+        (rc = ensure(ctx, s->r_cut, sizeof(int) * n_blocks)) || (rc = ensure(ctx, s->r_counts, sizeof(int) * n_ctas)) ||
+        (rc = ensure(ctx, s->r_offsets, sizeof(int) * (n_ctas + 1))) ||
+        (rc = ensure(ctx, s->r_list, sizeof(long long) * n)) || (rc = ensure(ctx, s->r_ref, sizeof(double) * 3 * n)))
+        return rc;
+    RefineArgs r{};
+    r.sys = s->dev;
+    r.n_per_block = n_per_block;
+    r.n_blocks = n_blocks;
+    r.ctas_per_block = static_cast<int>(cpb);
+    r.seed = seed;
+    r.inv_temperature = 1.0 / temperature;
+    r.tail = s->refine_tail;
+    r.block_out = block_out_dev;
+    r.u = u_dev;
+    r.hist = static_cast<unsigned long long*>(s->r_hist.p);
+    r.cut = static_cast<int*>(s->r_cut.p);
+    r.counts = static_cast<int*>(s->r_counts.p);
+    r.offsets = static_cast<int*>(s->r_offsets.p);
+    r.list = static_cast<long long*>(s->r_list.p);
+    r.ref_u = static_cast<double*>(s->r_ref.p);
+    int n_sm = 0;
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device);
+    PMGB_CK(ctx, pmgb_launch_refine(r, n_ctas, std::max(1, n_sm), ctx->stream));
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_system_set_refine(pmgb_system* s, double tail_fraction) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    if (!(tail_fraction >= 0.0 && tail_fraction < 1.0))
+        return fail(s->ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_system_set_refine: tail fraction in [0, 1)");
+    s->refine_tail = tail_fraction;
+    return PMGB_OK;
+}
+
 extern "C" int pmgb_widom_device(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
                                  double temperature, double* block_out_dev, double* u_out_dev) {
     if (!s) return PMGB_ERR_INVALID_ARGUMENT;
@@ -739,8 +835,14 @@ extern "C" int pmgb_widom_device(pmgb_system* s, int64_t n_per_block, int32_t n_
     a.inv_temperature = 1.0 / temperature;
     a.partials = static_cast<LsePartial*>(s->partials.p);
     a.u_out = u_out_dev;
+    const bool refine = s->refine_tail > 0.0;
+    if (refine && !u_out_dev) {  // the refinement needs every insertion's FP32 energy
+        if (int rc = ensure(ctx, s->g_u, sizeof(double) * 2 * static_cast<size_t>(n_per_block) * n_blocks)) return rc;
+        a.u_out = static_cast<double*>(s->g_u.p);
+    }
     PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
     PMGB_CK(ctx, pmgb_launch_reduce_blocks(a.partials, n_blocks, a.ctas_per_block, block_out_dev, ctx->stream));
+    if (refine) return run_refine(s, n_per_block, n_blocks, seed, temperature, block_out_dev, a.u_out);
     return PMGB_OK;
 }
 
@@ -874,7 +976,12 @@ extern "C" int pmgb_widom_adjoint(pmgb_system* s, int64_t n_per_block, int32_t n
     PMGB_CK(ctx, pmgb_launch_weighted_columns(a.u_out, 2, n, a.inv_temperature, d_block, n_blocks, a.dsum, n_cols, n,
                                               static_cast<double*>(s->g_part.p), n_chunks,
                                               static_cast<double*>(s->g_cols.p), ctx->stream));
-    std::vector<double> cols(n_cols + 2);
+    std::vector<double> cols(n_cols + 2), fp32_blocks(4 * static_cast<size_t>(n_blocks));
+    // the column weights are relative to the FP32 block sums: keep those for M
+    PMGB_CK(ctx, cudaMemcpyAsync(fp32_blocks.data(), d_block, sizeof(double) * 4 * n_blocks, cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    if (s->refine_tail > 0.0)
+        if ((rc = run_refine(s, n_per_block, n_blocks, seed, temperature, d_block, a.u_out))) return rc;
     PMGB_CK(ctx, cudaMemcpyAsync(block_out, d_block, sizeof(double) * 4 * n_blocks, cudaMemcpyDeviceToHost, ctx->stream));
     PMGB_CK(ctx, cudaMemcpyAsync(cols.data(), s->g_cols.p, sizeof(double) * (n_cols + 2), cudaMemcpyDeviceToHost,
                                  ctx->stream));
@@ -882,7 +989,7 @@ extern "C" int pmgb_widom_adjoint(pmgb_system* s, int64_t n_per_block, int32_t n
     if (grad_out) PMGB_CK(ctx, cudaMemcpyAsync(grad_out, a.grad_u, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
     if ((rc = check_status(ctx))) return rc;
     double M = -INFINITY;
-    for (int b = 0; b < n_blocks; ++b) M = std::max(M, block_out[4 * b]);
+    for (int b = 0; b < n_blocks; ++b) M = std::max(M, fp32_blocks[4 * b]);
     dtheta[0] = M;
     dtheta[1] = cols[n_cols];
     dtheta[2] = cols[n_cols + 1];
@@ -1121,5 +1228,350 @@ extern "C" int pmgb_fp32_peak(pmgb_ctx* ctx, int n_ctas, int iters, double* tflo
     if (e != cudaSuccess) return cuda_fail(ctx, e, "pmgb_fp32_peak");
     const double flops = 2.0 * 8.0 * 16.0 * double(iters) * 256.0 * double(n_ctas);
     *tflops_out = flops / (double(ms) * 1e-3) / 1e12;
+    return PMGB_OK;
+}
+
+// ============================================================================
+// batched screening
+// ============================================================================
+struct pmgb_batch {
+    pmgb_ctx* ctx = nullptr;
+    std::vector<pmgb_system*> systems;
+    std::vector<BatchSystem> host_sys;
+    std::vector<double> chunk_flops;   // per system: algorithmic flops of one chunk
+    std::vector<BatchUnit> units;      // current work units
+    std::vector<double> unit_cost;
+    int n_blocks = 0;
+    bool grad = false;
+    int n_ctas = 0, order = 0, max_ctas = 0, sm_count = 0, max_cols = 0;
+    double unit_mflop = 0.0;           // target work per unit (0: one chunk per unit)
+    int64_t n_chunks = 0, n_out_cols = 0, n_insertions = 0, dtheta_len = 0, device_bytes = 0;
+    // device memory
+    BatchSystem* d_sys = nullptr;
+    BatchUnit* d_units = nullptr;
+    int* d_order = nullptr;
+    int* d_counter = nullptr;
+    BatchRun* d_run = nullptr;
+    LsePartial* d_partials = nullptr;
+    float* d_dsum = nullptr;
+    double* d_unit_cols = nullptr;
+    double* d_block_out = nullptr;
+    double* d_out_cols = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool launched = false;
+};
+
+namespace {
+
+void batch_free(pmgb_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+    void* ptrs[] = {b->d_sys, b->d_units, b->d_order, b->d_counter, b->d_run, b->d_partials,
+                    b->d_dsum, b->d_unit_cols, b->d_block_out, b->d_out_cols};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+}
+
+template <class T>
+int batch_alloc(pmgb_batch* b, T** p, size_t count) {
+    const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+    PMGB_CK(b->ctx, cudaMalloc(reinterpret_cast<void**>(p), bytes));
+    b->device_bytes += static_cast<int64_t>(bytes);
+    return PMGB_OK;
+}
+
+// Capture memset(counter) + persistent kernel + per-system reduction as one graph.
+int batch_capture(pmgb_batch* b) {
+    pmgb_ctx* ctx = b->ctx;
+    if (b->exec) {
+        PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    BatchArgs a{};
+    a.systems = b->d_sys;
+    a.units = b->d_units;
+    a.order = b->d_order;
+    a.n_units = static_cast<int>(b->units.size());
+    a.counter = b->d_counter;
+    a.run = b->d_run;
+    a.partials = b->d_partials;
+    a.status = ctx->d_status;
+    a.dsum = b->d_dsum;
+    a.max_cols = b->max_cols;
+    a.unit_cols = b->d_unit_cols;
+    cudaStream_t st = ctx->stream;
+    PMGB_CK(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaMemsetAsync(b->d_counter, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = pmgb_launch_batch(a, b->grad, b->n_ctas, st);
+    if (e == cudaSuccess)
+        e = pmgb_launch_batch_reduce(b->d_sys, static_cast<int>(b->systems.size()), b->n_blocks, b->d_partials,
+                                     b->d_unit_cols, b->grad, b->d_block_out, b->d_out_cols, st);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e_end = cudaStreamEndCapture(st, &g);
+    if (e == cudaSuccess) e = e_end;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "pmgb_batch: graph capture");
+    return PMGB_OK;
+}
+
+// Cut every system's chunks into work units of about unit_mflop of work (whole blocks at
+// most; one chunk per unit for frameworks that do not fit the ring) and upload them with
+// their processing order: 0 = estimated cost, largest first; 1 = system by system.
+int batch_build_units(pmgb_batch* b, double unit_mflop, int order) {
+    b->units.clear();
+    b->unit_cost.clear();
+    for (size_t i = 0; i < b->host_sys.size(); ++i) {
+        const BatchSystem& bs = b->host_sys[i];
+        const int cpb = bs.ctas_per_block;
+        int g = 1;
+        if (unit_mflop > 0.0 && bs.sys.n_tiles <= PMGB_NSTAGE)
+            g = static_cast<int>(std::min<double>(cpb, std::max(1.0, std::ceil(unit_mflop * 1e6 / b->chunk_flops[i]))));
+        for (int blk = 0; blk < b->n_blocks; ++blk)
+            for (int c0 = 0; c0 < cpb; c0 += g) {
+                const int n = std::min(g, cpb - c0);
+                b->units.push_back(BatchUnit{static_cast<int>(i), blk, c0, n});
+                b->unit_cost.push_back(n * b->chunk_flops[i]);
+            }
+    }
+    const int n = static_cast<int>(b->units.size());
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; ++i) idx[i] = i;
+    if (order == 0)
+        std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return b->unit_cost[x] > b->unit_cost[y]; });
+    pmgb_ctx* ctx = b->ctx;
+    PMGB_CK(ctx, cudaMemcpyAsync(b->d_units, b->units.data(), sizeof(BatchUnit) * n, cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    PMGB_CK(ctx, cudaMemcpyAsync(b->d_order, idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // idx is a local
+    b->order = order;
+    b->unit_mflop = unit_mflop;
+    return PMGB_OK;
+}
+
+int batch_enqueue(pmgb_batch* b, uint64_t seed, double temperature) {
+    pmgb_ctx* ctx = b->ctx;
+    const BatchRun run{static_cast<unsigned long long>(seed), 1.0 / temperature};
+    // pageable source: staged at once, so the local may go out of scope
+    PMGB_CK(ctx, cudaMemcpyAsync(b->d_run, &run, sizeof(run), cudaMemcpyHostToDevice, ctx->stream));
+    PMGB_CK(ctx, cudaGraphLaunch(b->exec, ctx->stream));
+    b->launched = true;
+    return PMGB_OK;
+}
+
+}  // namespace
+
+extern "C" int pmgb_batch_create(pmgb_ctx* ctx, int32_t n_systems, pmgb_system* const* systems,
+                                 const int64_t* n_per_block, int32_t n_blocks, int32_t with_adjoint,
+                                 pmgb_batch** out) {
+    if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
+    if (!out || n_systems < 1 || !systems || !n_per_block || n_blocks < 1)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_batch_create: bad arguments");
+    *out = nullptr;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    auto* b = new pmgb_batch();
+    b->ctx = ctx;
+    b->n_blocks = n_blocks;
+    b->grad = with_adjoint != 0;
+    int64_t col_base = 0, out_base = 0, n_chunks = 0;
+    for (int32_t i = 0; i < n_systems; ++i) {
+        pmgb_system* s = systems[i];
+        const char* why = nullptr;
+        if (!s) why = "NULL system";
+        else if (s->ctx != ctx) why = "system belongs to another context";
+        else if (s->dev.charged && !s->ewald_set) why = "charged system without pmgb_system_set_ewald";
+        else if (n_per_block[i] < 1) why = "n_per_block < 1";
+        if (why) {
+            delete b;
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_batch_create: system %d: %s", i, why);
+        }
+        const int variant = pmgb_batch_variant(s->n_sites, s->dev.charged != 0);
+        if (variant < 0) {
+            delete b;
+            return fail(ctx, PMGB_ERR_UNSUPPORTED, "pmgb_batch_create: system %d: %d guest sites", i, s->n_sites);
+        }
+        const int64_t cpb = (n_per_block[i] + PMGB_THREADS - 1) / PMGB_THREADS;
+        const int nst = template_sites(s->n_sites);
+        BatchSystem bs{};
+        bs.sys = s->dev;
+        bs.n_per_block = n_per_block[i];
+        bs.variant = variant;
+        bs.n_cols = b->grad ? s->dev.n_seg * nst * 2 : 0;
+        bs.chunk_first = static_cast<int>(n_chunks);
+        bs.ctas_per_block = static_cast<int>(cpb);
+        bs.col_base = col_base;
+        bs.out_base = out_base;
+        // cost model of one chunk: algorithmic flops of its pair and reciprocal-space terms
+        const double pair = s->dev.charged ? 68.0 : 28.0;
+        b->chunk_flops.push_back(PMGB_THREADS * nst *
+                                 (pair * s->dev.n_rec + (s->dev.charged ? 17.0 * s->dev.n_k : 0.0)) + 1.0);
+        n_chunks += cpb * n_blocks;
+        if (n_chunks > INT32_MAX / 2) {
+            delete b;
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_batch_create: too many insertions");
+        }
+        col_base += cpb * n_blocks * bs.n_cols;
+        out_base += 3 + bs.n_cols;
+        b->max_cols = std::max(b->max_cols, bs.n_cols);
+        b->n_insertions += n_per_block[i] * n_blocks;
+        b->dtheta_len += 3 + 2 * static_cast<int64_t>(s->n_species) * s->n_species;
+        b->host_sys.push_back(bs);
+        b->systems.push_back(s);
+    }
+    b->n_chunks = n_chunks;
+    b->n_out_cols = out_base;
+    cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
+    int rc = PMGB_OK;
+    cudaError_t e = pmgb_batch_prepare(b->grad);
+    if (e != cudaSuccess) rc = cuda_fail(ctx, e, "pmgb_batch_create: kernel attributes");
+    b->max_ctas = std::max(1, 2 * b->sm_count);
+    b->n_ctas = b->max_ctas;
+    if (!rc) rc = batch_alloc(b, &b->d_sys, b->host_sys.size());
+    if (!rc) rc = batch_alloc(b, &b->d_units, static_cast<size_t>(n_chunks));  // one chunk per unit at most
+    if (!rc) rc = batch_alloc(b, &b->d_order, static_cast<size_t>(n_chunks));
+    if (!rc) rc = batch_alloc(b, &b->d_counter, 1);
+    if (!rc) rc = batch_alloc(b, &b->d_run, 1);
+    if (!rc) rc = batch_alloc(b, &b->d_partials, static_cast<size_t>(n_chunks));
+    if (!rc) rc = batch_alloc(b, &b->d_block_out, b->host_sys.size() * 4 * n_blocks);
+    if (!rc && b->grad) rc = batch_alloc(b, &b->d_dsum, static_cast<size_t>(b->max_ctas) * b->max_cols * PMGB_THREADS);
+    if (!rc && b->grad) rc = batch_alloc(b, &b->d_unit_cols, static_cast<size_t>(col_base));
+    if (!rc && b->grad) rc = batch_alloc(b, &b->d_out_cols, static_cast<size_t>(out_base));
+    if (!rc) {
+        e = cudaMemcpyAsync(b->d_sys, b->host_sys.data(), sizeof(BatchSystem) * b->host_sys.size(),
+                            cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) rc = cuda_fail(ctx, e, "pmgb_batch_create: upload");
+    }
+    if (!rc) rc = batch_build_units(b, 0.0, 0);  // synchronises: the upload above reads host_sys
+    if (!rc) rc = batch_capture(b);
+    if (rc) {
+        batch_free(b);
+        delete b;
+        return rc;
+    }
+    ++ctx->refs;
+    *out = b;
+    return PMGB_OK;
+}
+
+extern "C" void pmgb_batch_destroy(pmgb_batch* b) {
+    if (!b) return;
+    pmgb_ctx* ctx = b->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    batch_free(b);
+    delete b;
+    ctx_release(ctx);
+}
+
+extern "C" int pmgb_batch_configure(pmgb_batch* b, int32_t n_ctas, int32_t order, double unit_mflop) {
+    if (!b) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = b->ctx;
+    if (n_ctas < 0 || n_ctas > b->max_ctas || (order != 0 && order != 1) || !(unit_mflop >= 0.0))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT,
+                    "pmgb_batch_configure: n_ctas in [0, %d], order 0 or 1, unit_mflop >= 0", b->max_ctas);
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    b->n_ctas = n_ctas == 0 ? b->max_ctas : n_ctas;
+    if (int rc = batch_build_units(b, unit_mflop, order)) return rc;
+    b->launched = false;
+    return batch_capture(b);
+}
+
+extern "C" int pmgb_batch_launch(pmgb_batch* b, uint64_t seed, double temperature) {
+    if (!b) return PMGB_ERR_INVALID_ARGUMENT;
+    if (!(temperature > 0.0) || !std::isfinite(temperature))
+        return fail(b->ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_batch_launch: temperature must be positive");
+    PMGB_CK(b->ctx, cudaSetDevice(b->ctx->device));
+    return batch_enqueue(b, seed, temperature);
+}
+
+extern "C" int pmgb_batch_tune(pmgb_batch* b, uint64_t seed, double temperature, int32_t repeats,
+                               double* best_ms_out) {
+    if (!b) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = b->ctx;
+    if (repeats < 1 || !(temperature > 0.0))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_batch_tune: repeats >= 1 and a positive temperature");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    cudaEvent_t e0, e1;
+    PMGB_CK(ctx, cudaEventCreate(&e0));
+    PMGB_CK(ctx, cudaEventCreate(&e1));
+    struct Shape {
+        int n_ctas, order;
+        double mflop;
+    };
+    double best = INFINITY;
+    Shape best_s{b->max_ctas, 0, 0.0};
+    int rc = PMGB_OK;
+    auto time_shape = [&](const Shape& sh) -> int {
+        if (int r = pmgb_batch_configure(b, sh.n_ctas, sh.order, sh.mflop)) return r;
+        if (int r = batch_enqueue(b, seed, temperature)) return r;  // warm-up
+        cudaEventRecord(e0, ctx->stream);
+        for (int i = 0; i < repeats; ++i)
+            if (int r = batch_enqueue(b, seed + 1 + i, temperature)) return r;
+        cudaEventRecord(e1, ctx->stream);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "pmgb_batch_tune");
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms / repeats < best) {
+            best = ms / repeats;
+            best_s = sh;
+        }
+        return PMGB_OK;
+    };
+    // coordinate search: insertion-tile work per unit, then resident CTAs per SM, then unit order
+    for (double mflop : {0.0, 32.0, 128.0, 512.0})
+        if (!rc) rc = time_shape(Shape{b->max_ctas, 0, mflop});
+    for (int twice : {2, 3})
+        if (!rc) rc = time_shape(Shape{std::max(1, twice * b->sm_count / 2), 0, best_s.mflop});
+    if (!rc) rc = time_shape(Shape{best_s.n_ctas, 1, best_s.mflop});
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if ((rc = check_status(ctx))) return rc;
+    if ((rc = pmgb_batch_configure(b, best_s.n_ctas, best_s.order, best_s.mflop))) return rc;
+    if (best_ms_out) *best_ms_out = best;
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_batch_results(pmgb_batch* b, double* block_out, double* dtheta) {
+    if (!b) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = b->ctx;
+    if (!block_out || (b->grad && !dtheta))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_batch_results: block_out (and dtheta with the adjoint)");
+    if (!b->launched) return fail(ctx, PMGB_ERR_NOT_READY, "pmgb_batch_results: no run since the batch was configured");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    const size_t nb = b->host_sys.size() * 4 * static_cast<size_t>(b->n_blocks);
+    PMGB_CK(ctx, cudaMemcpyAsync(block_out, b->d_block_out, sizeof(double) * nb, cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<double> cols(b->grad ? b->n_out_cols : 0);
+    if (b->grad)
+        PMGB_CK(ctx, cudaMemcpyAsync(cols.data(), b->d_out_cols, sizeof(double) * cols.size(), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+    if (int rc = check_status(ctx)) return rc;
+    if (!b->grad) return PMGB_OK;
+    double* d = dtheta;
+    for (size_t i = 0; i < b->systems.size(); ++i) {
+        const pmgb_system* s = b->systems[i];
+        const double* c = cols.data() + b->host_sys[i].out_base;
+        d[0] = c[0];
+        d[1] = c[1];
+        d[2] = c[2];
+        assemble_species(s, template_sites(s->n_sites), c + 3, d);
+        d += 3 + 2 * s->n_species * s->n_species;
+    }
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_batch_info(const pmgb_batch* b, int64_t* out8) {
+    if (!b || !out8) return PMGB_ERR_INVALID_ARGUMENT;
+    out8[0] = static_cast<int64_t>(b->units.size());
+    out8[1] = b->n_ctas;
+    out8[2] = b->order;
+    out8[3] = b->dtheta_len;
+    out8[4] = b->device_bytes;
+    out8[5] = b->n_insertions;
+    out8[6] = b->n_chunks;
+    out8[7] = static_cast<int64_t>(std::llround(b->unit_mflop));
     return PMGB_OK;
 }

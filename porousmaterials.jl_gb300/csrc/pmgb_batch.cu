@@ -1,0 +1,229 @@
+// pmgb_batch.cu -- persistent Widom screening of many frameworks in one launch.
+//
+// The batch is a list of systems (framework + guest) of uneven sizes.  Each system's
+// insertions are cut into units of PMGB_THREADS (one statistics block at a time, as the
+// single-system kernel does), and a grid of resident CTAs pulls units from one atomic
+// counter in a host-chosen order (largest frameworks first by default), so that the
+// tail of the launch is made of small units.  A CTA keeps its TMA ring between units and
+// copies each unit's system descriptor into shared memory.  The adjoint variant reduces
+// its Boltzmann-weighted r^-12 / r^-6 columns inside the unit (weights relative to the
+// unit's own maximum of -U/T), so no per-insertion columns reach HBM; a per-system
+// reduction combines units in a fixed order.
+#include "pmgb_device.cuh"
+
+namespace {
+
+// (n_sites template, charged) of each compiled variant
+constexpr int kVariantSites[6] = {1, 2, 3, 4, 6, 8};
+
+// Each variant is its own function so that ptxas allocates its registers separately.
+template <int NS, bool CHARGED, bool GRAD>
+__device__ __noinline__ bool run_unit_fn(const SysDev& S, const UnitIO& io, int4* stage, uint64_t* bars,
+                                         LsePartial* red, uint32_t (&fills)[PMGB_NSTAGE], unsigned int* status) {
+    return run_unit<NS, CHARGED, GRAD>(S, io, stage, bars, red, fills, status);
+}
+
+template <bool GRAD>
+__device__ __forceinline__ bool run_variant(int variant, const SysDev& S, const UnitIO& io, int4* stage,
+                                            uint64_t* bars, LsePartial* red, uint32_t (&fills)[PMGB_NSTAGE],
+                                            unsigned int* status) {
+    switch (variant) {
+        case 0: return run_unit_fn<1, false, GRAD>(S, io, stage, bars, red, fills, status);
+        case 1: return run_unit_fn<2, false, GRAD>(S, io, stage, bars, red, fills, status);
+        case 2: return run_unit_fn<3, false, GRAD>(S, io, stage, bars, red, fills, status);
+        case 3: return run_unit_fn<4, false, GRAD>(S, io, stage, bars, red, fills, status);
+        case 4: return run_unit_fn<6, false, GRAD>(S, io, stage, bars, red, fills, status);
+        case 5: return run_unit_fn<8, false, GRAD>(S, io, stage, bars, red, fills, status);
+        case 6: return run_unit_fn<1, true, GRAD>(S, io, stage, bars, red, fills, status);
+        case 7: return run_unit_fn<2, true, GRAD>(S, io, stage, bars, red, fills, status);
+        case 8: return run_unit_fn<3, true, GRAD>(S, io, stage, bars, red, fills, status);
+        case 9: return run_unit_fn<4, true, GRAD>(S, io, stage, bars, red, fills, status);
+        case 10: return run_unit_fn<6, true, GRAD>(S, io, stage, bars, red, fills, status);
+        default: return run_unit_fn<8, true, GRAD>(S, io, stage, bars, red, fills, status);
+    }
+}
+
+static_assert(sizeof(BatchSystem) % 4 == 0, "BatchSystem is copied to shared memory as 32-bit words");
+
+template <bool GRAD>
+__global__ void __launch_bounds__(PMGB_THREADS, 2) batch_kernel(const __grid_constant__ BatchArgs b) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    int4* stage = reinterpret_cast<int4*>(smem_raw);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + size_t(PMGB_NSTAGE) * PMGB_TILE * sizeof(int4));
+    __shared__ LsePartial red[PMGB_THREADS / 32];
+    __shared__ __align__(16) BatchSystem s_bs;
+    __shared__ double s_m;
+    __shared__ double s_w[GRAD ? PMGB_THREADS : 1];
+    __shared__ int s_unit;
+    const int tid = threadIdx.x;
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    ring_init(bars);
+    uint32_t fills[PMGB_NSTAGE] = {};
+    const BatchRun run = *b.run;
+    float* my_dsum = GRAD ? b.dsum + static_cast<size_t>(blockIdx.x) * b.max_cols * PMGB_THREADS : nullptr;
+    for (;;) {
+        if (tid == 0) s_unit = atomicAdd(b.counter, 1);
+        __syncthreads();
+        const int u = s_unit;
+        if (u >= b.n_units) break;  // uniform: every thread read the same s_unit
+        const BatchUnit unit = b.units[b.order[u]];
+        {
+            const int* src = reinterpret_cast<const int*>(b.systems + unit.system);
+            int* dst = reinterpret_cast<int*>(&s_bs);
+            for (int i = tid; i < static_cast<int>(sizeof(BatchSystem) / 4); i += PMGB_THREADS) dst[i] = src[i];
+        }
+        __syncthreads();
+        const long long npb = s_bs.n_per_block;
+        // a framework that fits the ring stays resident across the unit's chunks
+        const bool fits = s_bs.sys.n_tiles <= PMGB_NSTAGE;
+        for (int c = 0; c < unit.n_chunks; ++c) {
+            const int chunk = unit.chunk0 + c;
+            const int slot = s_bs.chunk_first + unit.block * s_bs.ctas_per_block + chunk;
+            UnitIO io{};
+            io.pose_mode = POSE_PHILOX;
+            io.out_mode = OUT_WIDOM;
+            const long long within = static_cast<long long>(chunk) * PMGB_THREADS + tid;
+            io.valid = within < npb;
+            io.item = static_cast<long long>(unit.block) * npb + within;
+            io.seed = run.seed + static_cast<unsigned long long>(unit.system) * 0x9E3779B97F4A7C15ull;
+            io.inv_temperature = run.inv_temperature;
+            io.dsum = my_dsum;
+            io.dsum_stride = PMGB_THREADS;
+            io.col_item = tid;
+            io.partial = b.partials + slot;
+            io.resident = fits && c > 0;
+            double x = -inf;
+            io.x_out = &x;
+            io.m_out = &s_m;
+            if (!run_variant<GRAD>(s_bs.variant, s_bs.sys, io, stage, bars, red, fills, b.status)) return;
+            if (GRAD) {
+                __syncthreads();  // s_m and every thread's columns are written
+                const double M = s_m;
+                s_w[tid] = (x == -inf || M == -inf) ? 0.0 : exp(x - M);
+                __syncthreads();
+                const int nc = s_bs.n_cols;
+                double* out = b.unit_cols + s_bs.col_base + static_cast<long long>(slot - s_bs.chunk_first) * nc;
+                const int warp = tid >> 5, lane = tid & 31;
+                for (int cc = warp; cc < nc; cc += PMGB_THREADS / 32) {
+                    const float* col = my_dsum + static_cast<size_t>(cc) * PMGB_THREADS;
+                    double v = 0.0;
+#pragma unroll
+                    for (int i = lane; i < PMGB_THREADS; i += 32) {
+                        const double w = s_w[i];
+                        // w = 0 marks an empty slot or U = +Inf, whose column may be garbage or Inf
+                        if (w > 0.0) v = fma(w, static_cast<double>(col[i]), v);
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    if (lane == 0) out[cc] = v;
+                }
+            }
+            __syncthreads();  // red, s_m, s_w and the columns are free for the next chunk
+        }
+        __syncthreads();  // s_bs, s_w and the ring are free for the next unit
+    }
+}
+
+// One CTA per system: block results (as reduce_blocks_kernel) and, with the adjoint, the
+// combined columns relative to m = max over the system's chunks of max -U/T.
+__global__ void batch_reduce_kernel(const BatchSystem* __restrict__ systems, int n_blocks,
+                                    const LsePartial* __restrict__ partials, const double* __restrict__ unit_cols,
+                                    bool grad, double* __restrict__ block_out, double* __restrict__ out_cols) {
+    const int s = blockIdx.x;
+    const BatchSystem& bs = systems[s];
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    const unsigned full = 0xffffffffu;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nw = blockDim.x >> 5;
+    const int cpb = bs.ctas_per_block;
+    for (int blk = warp; blk < n_blocks; blk += nw) {
+        const LsePartial* p = partials + bs.chunk_first + static_cast<size_t>(blk) * cpb;
+        double m = -inf;
+        for (int c = lane; c < cpb; c += 32) m = fmax(m, p[c].m);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(full, m, o));
+        double sum = 0.0, tv = 0.0, te = 0.0;
+        long long n = 0;
+        for (int c = lane; c < cpb; c += 32) {
+            const LsePartial q = p[c];
+            const double f = (m == -inf || q.m == -inf) ? 0.0 : exp(q.m - m);
+            sum += q.s * f;
+            tv += q.tv * f;
+            te += q.te * f;
+            n += q.n_inf;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sum += __shfl_xor_sync(full, sum, o);
+            tv += __shfl_xor_sync(full, tv, o);
+            te += __shfl_xor_sync(full, te, o);
+            n += __shfl_xor_sync(full, n, o);
+        }
+        if (lane == 0) {
+            double* o = block_out + (static_cast<size_t>(s) * n_blocks + blk) * 4;
+            o[0] = (sum > 0.0) ? m + log(sum) : -inf;
+            o[1] = tv / sum;
+            o[2] = te / sum;
+            o[3] = static_cast<double>(n);
+        }
+    }
+    if (!grad) return;
+    __shared__ double s_max;
+    const int n_units = n_blocks * cpb;
+    const LsePartial* p = partials + bs.chunk_first;
+    if (warp == 0) {
+        double m = -inf;
+        for (int c = lane; c < n_units; c += 32) m = fmax(m, p[c].m);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(full, m, o));
+        if (lane == 0) s_max = m;
+    }
+    __syncthreads();
+    const double M = s_max;
+    const int nc = bs.n_cols;
+    double* out = out_cols + bs.out_base;
+    // entry e: 0 -> M, 1 -> sum w, 2 -> sum w U_es, 3 + c -> sum w col_c; units in a fixed order
+    for (int e = threadIdx.x; e < 3 + nc; e += blockDim.x) {
+        if (e == 0) {
+            out[0] = M;
+            continue;
+        }
+        double v = 0.0;
+        for (int k = 0; k < n_units; ++k) {
+            const double f = (M == -inf || p[k].m == -inf) ? 0.0 : exp(p[k].m - M);
+            if (f == 0.0) continue;
+            const double x = (e == 1) ? p[k].s : (e == 2) ? p[k].te : unit_cols[bs.col_base + static_cast<size_t>(k) * nc + (e - 3)];
+            v = fma(f, x, v);
+        }
+        out[e] = v;
+    }
+}
+
+}  // namespace
+
+int pmgb_batch_variant(int n_sites, bool charged) {
+    for (int i = 0; i < 6; ++i)
+        if (n_sites <= kVariantSites[i]) return i + (charged ? 6 : 0);
+    return -1;
+}
+
+cudaError_t pmgb_batch_prepare(bool grad) {
+    const int smem = static_cast<int>(pmgb_pairs_smem_bytes());
+    return grad ? cudaFuncSetAttribute(batch_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+                : cudaFuncSetAttribute(batch_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+cudaError_t pmgb_launch_batch(const BatchArgs& b, bool grad, int n_ctas, cudaStream_t st) {
+    const size_t smem = pmgb_pairs_smem_bytes();
+    if (grad) batch_kernel<true><<<n_ctas, PMGB_THREADS, smem, st>>>(b);
+    else batch_kernel<false><<<n_ctas, PMGB_THREADS, smem, st>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t pmgb_launch_batch_reduce(const BatchSystem* systems, int n_systems, int n_blocks,
+                                     const LsePartial* partials, const double* unit_cols, bool grad,
+                                     double* block_out, double* out_cols, cudaStream_t st) {
+    if (n_systems <= 0) return cudaSuccess;
+    batch_reduce_kernel<<<n_systems, 128, 0, st>>>(systems, n_blocks, partials, unit_cols, grad, block_out, out_cols);
+    return cudaGetLastError();
+}

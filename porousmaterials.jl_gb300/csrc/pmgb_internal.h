@@ -70,6 +70,19 @@ struct SysDev {
     int n_krow, n_k;
     const KRow* krow;
     const float2* skw;
+    // FP64 copies: guest poses are composed in FP64, and the Boltzmann-tail refinement
+    // re-evaluates selected insertions entirely in FP64
+    double f2c64[6];                        // f_to_c, upper triangular (00 01 02 11 12 22)
+    double g64[6];                          // c_to_f, upper triangular
+    double body64[PMGB_MAX_SITES][3];       // guest site offsets (Cartesian, A)
+    double q64[PMGB_MAX_SITES];             // guest site charges
+    double rc2_64, rc2e_64, alpha64;
+    const double* rec_q;                    // [n_rec] framework charge of each record
+    const double* rec_xf;                   // [3 n_rec] exact fractional coordinates of each record
+    const double2* segpar64;                // [n_seg * PMGB_MAX_SITES] (sigma^2, 4 epsilon); 4 eps = 0: no LJ
+    const double* sk64;                     // [2 n_k] S(k) (re, im) in half-row order
+    const double* wt64;                     // [n_k] k-vector weights in half-row order
+    const int* kabc;                        // [3 n_k] k-vectors in half-row order
 };
 
 enum PoseMode : int {
@@ -131,13 +144,82 @@ cudaError_t pmgb_launch_weighted_columns(const double* u, int u_stride, long lon
                                          int n_cols, long long col_stride, double* partials, int n_chunks,
                                          double* out, cudaStream_t st);
 
+// ---- batched persistent screening ----------------------------------------------------
+// A chunk is PMGB_THREADS insertions of one system: insertion block * n_per_block +
+// chunk * PMGB_THREADS + tid.  Chunks of a system are numbered block-major from chunk_first;
+// each has its own partial (and adjoint column) slot.  A work unit is a run of consecutive
+// chunks of one block; a CTA keeps a framework that fits its ring resident across them.
+struct BatchSystem {
+    SysDev sys;
+    long long n_per_block;
+    int variant;          // template variant: index of (NS, charged), see pmgb_batch_variant
+    int n_cols;           // adjoint columns (segments x template sites x 2), 0 without adjoint
+    int chunk_first;      // first chunk slot of this system
+    int ctas_per_block;   // chunks per insertion block
+    long long col_base;   // adjoint: first of this system's chunk column partials (n_cols per chunk)
+    long long out_base;   // adjoint: first of this system's 3 + n_cols combined outputs
+};
+struct BatchUnit {
+    int system, block, chunk0, n_chunks;
+};
+struct BatchRun {
+    unsigned long long seed;  // Philox key of system s: seed + s * 0x9E3779B97F4A7C15 (mod 2^64)
+    double inv_temperature;
+};
+struct BatchArgs {
+    const BatchSystem* systems;
+    const BatchUnit* units;
+    const int* order;         // processing order of the units
+    int n_units;              // work units in the queue
+    int* counter;             // work-queue head, zeroed before each run
+    const BatchRun* run;      // device memory, so that a captured graph takes new seeds
+    LsePartial* partials;     // [total chunks]
+    unsigned int* status;
+    // adjoint only
+    float* dsum;              // per-CTA column scratch: [gridDim.x][max_cols][PMGB_THREADS]
+    int max_cols;
+    double* unit_cols;        // per-chunk weighted column sums, weights exp(-U/T - m_chunk)
+};
+
+// ---- FP64 refinement of the Boltzmann tail (pmgb_refine.cu) ---------------------------
+struct RefineArgs {
+    SysDev sys;
+    long long n_per_block;
+    int n_blocks, ctas_per_block;   // insertion i of block b: b * n_per_block + i; 256 per chunk
+    unsigned long long seed;
+    double inv_temperature;
+    double tail;                    // weight fraction left unrefined per block (at most)
+    double* block_out;              // [4 n_blocks] FP32-pass results, corrected in place
+    double* u;                      // [2 n] per-insertion (U_vdw, U_es); refined entries replaced
+    unsigned long long* hist;       // [n_blocks * pmgb_refine_hist_words()]
+    int* cut;                       // [n_blocks]
+    int* counts;                    // [n_blocks * ctas_per_block]
+    int* offsets;                   // [n_blocks * ctas_per_block + 1]
+    long long* list;                // [n] refined insertions, index order
+    double* ref_u;                  // [3 n] their FP64 (U_vdw, U_sr, U_lr)
+};
+cudaError_t pmgb_launch_refine(const RefineArgs& a, int n_ctas, int n_sm, cudaStream_t st);
+size_t pmgb_refine_hist_words();
+
+// Index of the compiled template variant for n_sites guest sites with or without charges;
+// -1 if there is none.
+int pmgb_batch_variant(int n_sites, bool charged);
+
 // kernels (defined in pmgb_kernels.cu); return cudaError_t of the launch
 cudaError_t pmgb_launch_pairs(const LaunchArgs& a, int n_ctas, cudaStream_t st);
 cudaError_t pmgb_launch_pairs_grad(const LaunchArgs& a, int n_ctas, cudaStream_t st);
+// persistent batch (defined in pmgb_batch.cu)
+cudaError_t pmgb_batch_prepare(bool grad);  // function attributes, before any stream capture
+cudaError_t pmgb_launch_batch(const BatchArgs& b, bool grad, int n_ctas, cudaStream_t st);
+// per system: block_out[(s * n_blocks + b) * 4 ..] and, with grad, the combined columns
+// out_cols[out_base ..] = (m, sum w, sum w U_es, sum w col_0, ...), w = exp(-U/T - m)
+cudaError_t pmgb_launch_batch_reduce(const BatchSystem* systems, int n_systems, int n_blocks,
+                                     const LsePartial* partials, const double* unit_cols, bool grad,
+                                     double* block_out, double* out_cols, cudaStream_t st);
 cudaError_t pmgb_launch_reduce_blocks(const LsePartial* partials, int n_blocks, int ctas_per_block,
                                       double* block_out, cudaStream_t st);
-// qfix: framework charge fractional coordinates as 32-bit fixed point (x * 2^32 mod 2^32)
-cudaError_t pmgb_launch_structure_factor(const uint32_t* qfix, const double* q, int n_q,
+// qxf: framework charge fractional coordinates (FP64, 3 per charge)
+cudaError_t pmgb_launch_structure_factor(const double* qxf, const double* q, int n_q,
                                          const int* kabc, const double* wt, int n_k,
                                          double* sk_out, float2* skw_out, cudaStream_t st);
 cudaError_t pmgb_launch_sample_poses(unsigned long long seed, long long start, long long n,

@@ -1,1062 +1,53 @@
-// pmgb_kernels.cu -- sm_103a kernels for the Widom-insertion / energy-grid path.
-//
-// One thread owns one insertion (or one grid point / explicit configuration) and
-// keeps its guest sites in registers.  Fractional coordinates are 32-bit fixed point
-// (x * 2^32 mod 2^32): the wrapping integer difference of two positions is exactly the
-// minimum-image fractional displacement (|d| <= 1/2), converted once to FP32 with a
-// single rounding.  The CTA streams the replicated framework (species-sorted int4
-// records: x, y, z fixed point, q as float bits) through a ring of shared-memory stages filled by
-// 1-D TMA bulk copies (cp.async.bulk + mbarrier complete_tx); every thread of the
-// CTA reads each record with a broadcast shared load and evaluates it against all
-// of its guest sites.  Pair math is FP32; per-insertion sums are compensated
-// (TwoSum every 64 records); the Boltzmann accumulation across insertions is FP64
-// log-sum-exp.  Ewald reciprocal space uses the framework structure factor
-// S(k) = sum_c q_c e^{ik.r_c} (built once per system in FP64) against a per-site
-// e^{-ik.x} recurrence along kc.
-//
-// Reference semantics restated here (PorousMaterials.jl v0.4.2):
-//   src/vdw_energetics.jl:19-47   LJ 12-6, strict r^2 < rc^2, r^2 < 0.1 -> +Inf
-//   src/electrostatics.jl:347-388 Ewald real space q erfc(alpha r)/(4 pi eps0 r), r < rc,
-//                                 reciprocal space sum_k wt_k sum_c q_c cos(k.(r_c - x))
-//   src/henry.jl:212-244          Boltzmann factor sums per statistics block, +Inf
-//                                 insertions excluded from the weighted-energy sums
-//   src/molecule.jl:233-281       uniform random rotation (Arvo) about the centre of mass
-//   src/grid.jl:313-359           energy-grid points xf = (i/(n-1), ...) ./ repfactors
-#include "pmgb_internal.h"
-
-#include <cmath>
-#include <cstdint>
+// pmgb_kernels.cu -- single-system sm_103a kernels for the Widom-insertion / energy-grid
+// path (one CTA per unit of PMGB_THREADS items), the FP64 reductions behind them, and the
+// exported launchers.  The per-unit device body lives in pmgb_device.cuh.
+#include "pmgb_device.cuh"
 
 namespace {
 
-constexpr int kChunk = 64;              // records per compensated fold
-constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s bound on any mbarrier wait
-
-// ----------------------------------------------------------------------------
-// PTX helpers: mbarrier + 1-D bulk (TMA) copies global -> shared
-// ----------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void fence_mbar_init() {
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void fence_proxy_async_smem() {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_addr(dst)),
-        "l"(src), "r"(bytes), "r"(smem_addr(bar))
-        : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-// Spin on an mbarrier phase for at most kWaitLimitNs (and a hard iteration cap).
-__device__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-    unsigned long long t0 = global_ns();
-    for (uint32_t it = 0; it < (1u << 28); ++it) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 63u) == 63u && global_ns() - t0 > kWaitLimitNs) return false;
-    }
-    return false;
-}
-
-// ----------------------------------------------------------------------------
-// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11)
-// ----------------------------------------------------------------------------
-__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
-        uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
-        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
-        k.x += 0x9E3779B9u;
-        k.y += 0xBB67AE85u;
-    }
-    return c;
-}
-__device__ __forceinline__ float u24(uint32_t x) { return static_cast<float>(x >> 8) * 5.9604644775390625e-08f; }
-
-// Pose of Widom insertion `idx`: centre of mass uniform in the supercell's
-// fractional cube (henry.jl:214) and a uniform rotation by Arvo's method
-// (molecule.jl:233-244): M = -(I - 2 v v^T) Rz(2 pi u1), v from (u2, u3).
-// R is column-major (R[i + 3j]).
-__device__ __forceinline__ void make_pose(unsigned long long seed, unsigned long long idx, float xf[3],
-                                          float R[9]) {
-    const uint2 key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
-    const uint4 a = philox4x32_10(make_uint4(static_cast<uint32_t>(idx), static_cast<uint32_t>(idx >> 32), 0u, 0u), key);
-    const uint4 b = philox4x32_10(make_uint4(static_cast<uint32_t>(idx), static_cast<uint32_t>(idx >> 32), 1u, 0u), key);
-    xf[0] = u24(a.x);
-    xf[1] = u24(a.y);
-    xf[2] = u24(a.z);
-    const float u1 = u24(a.w), u2 = u24(b.x), u3 = u24(b.y);
-    float s1, c1, s2, c2;
-    sincospif(2.0f * u1, &s1, &c1);
-    sincospif(2.0f * u2, &s2, &c2);
-    const float sq = sqrtf(u3);
-    const float v0 = c2 * sq, v1 = s2 * sq, v2 = sqrtf(1.0f - u3);
-    // A = 2 v v^T - I ; M = A * Rz with Rz columns (c1, -s1, 0), (s1, c1, 0), (0, 0, 1)
-    const float A[3][3] = {{2.0f * v0 * v0 - 1.0f, 2.0f * v0 * v1, 2.0f * v0 * v2},
-                           {2.0f * v1 * v0, 2.0f * v1 * v1 - 1.0f, 2.0f * v1 * v2},
-                           {2.0f * v2 * v0, 2.0f * v2 * v1, 2.0f * v2 * v2 - 1.0f}};
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        R[i + 0] = A[i][0] * c1 - A[i][1] * s1;
-        R[i + 3] = A[i][0] * s1 + A[i][1] * c1;
-        R[i + 6] = A[i][2];
-    }
-}
-
-// ----------------------------------------------------------------------------
-// compensated accumulation
-// ----------------------------------------------------------------------------
-__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
-    const float s = __fadd_rn(hi, x);
-    const float bp = __fsub_rn(s, hi);
-    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
-    hi = s;
-    lo = __fadd_rn(lo, e);
-}
-
-// FP32 fractional coordinate -> 32-bit fixed point, wrapping modulo 1
-__device__ __forceinline__ uint32_t frac2fix(float x) {
-    return static_cast<uint32_t>(__float2ll_rn(x * 4294967296.0f));
-}
-
-struct Geo {
-    // f_to_c scaled by 2^-32 as an FP32 value h plus its FP32 residual p (h + p equals the
-    // FP64 matrix to ~1e-15), so that Cartesian = (h + p) * fixed-point displacement
-    float h00, h01, h02, h11, h12, h22;
-    float p00, p01, p02, p11, p12, p22;
-    float rc2, rc2e, alpha;
-};
-
-// erfc(x) for x >= 0: t exp(-x^2) Q(3t - 2) with t = 1/(1 + x/2) and Q the degree-7
-// polynomial of csrc/fit_erfc.py (max relative error 3.3e-7 on [0, 3.2]).
-__device__ __forceinline__ float erfc_fit(float x) {
-    const float t = __fdividef(1.0f, fmaf(0.5f, x, 1.0f));
-    const float y = fmaf(t, 3.0f, -2.0f);
-    float q = -1.1504688e-05f;
-    q = fmaf(q, y, 0.00012701178f);
-    q = fmaf(q, y, 1.719709e-05f);
-    q = fmaf(q, y, -0.002622572f);
-    q = fmaf(q, y, 0.00045600548f);
-    q = fmaf(q, y, 0.06661939f);
-    q = fmaf(q, y, 0.29403913f);
-    q = fmaf(q, y, 0.6413754f);
-    float e;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(x * (x * -1.4426950408889634f)));
-    return q * t * e;
-}
-
-// Cartesian squared distance of a fixed-point fractional displacement
-__device__ __forceinline__ float dist2(const int4 r, const uint32_t ux, const uint32_t uy, const uint32_t uz,
-                                       const Geo& g) {
-    // the wrapping difference is the minimum-image displacement in units of 2^-32
-    const float dx = __int2float_rn(static_cast<int>(static_cast<uint32_t>(r.x) - ux));
-    const float dy = __int2float_rn(static_cast<int>(static_cast<uint32_t>(r.y) - uy));
-    const float dz = __int2float_rn(static_cast<int>(static_cast<uint32_t>(r.z) - uz));
-    const float rx = fmaf(g.p00, dx, fmaf(g.p01, dy, g.p02 * dz));
-    const float ry = fmaf(g.p11, dy, g.p12 * dz);
-    const float rz = g.p22 * dz;
-    const float cx = fmaf(g.h00, dx, fmaf(g.h01, dy, fmaf(g.h02, dz, rx)));
-    const float cy = fmaf(g.h11, dy, fmaf(g.h12, dz, ry));
-    const float cz = fmaf(g.h22, dz, rz);
-    return fmaf(cx, cx, fmaf(cy, cy, cz * cz));
-}
-
-// One framework record against one guest site.
-template <bool CHARGED>
-__device__ __forceinline__ void pair_fwd(const int4 r, const uint32_t ux, const uint32_t uy, const uint32_t uz,
-                                         const Geo& g, const float sig2, const float eps4, float& segmin,
-                                         float& ljp, float& php) {
-    const float r2 = dist2(r, ux, uy, uz, g);
-    segmin = fminf(segmin, r2);
-    const bool in = r2 < g.rc2;
-    float ir2, y = 0.0f;
-    if (CHARGED) {
-        // rsqrt estimate refined by one Newton step: y <- y + y/2 (1 - r2 y^2)
-        y = rsqrtf(r2);
-        const float e = fmaf(-r2 * y, y, 1.0f);
-        y = fmaf(0.5f * y, e, y);
-        ir2 = y * y;
-    } else {
-        ir2 = __frcp_rn(r2);
-    }
-    const float s = sig2 * ir2;
-    const float s3 = s * s * s;
-    const float t = fmaf(s3, s3, -s3);
-    ljp = fmaf(eps4, in ? t : 0.0f, ljp);
-    if (CHARGED) {
-        const float e = erfc_fit(g.alpha * (r2 * y)) * y;
-        php = fmaf(__int_as_float(r.w), (r2 < g.rc2e) ? e : 0.0f, php);
-    }
-}
-
-// ---- packed (f32x2) form: two framework records against one guest site -------------
-__device__ __forceinline__ float rcp_approx(float x) {
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-__device__ __forceinline__ float rsqrt_approx(float x) {
-    float r;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-__device__ __forceinline__ float ex2_approx(float x) {
-    float r;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
-
-struct Geo2 {
-    float2 h00, h01, h02, h11, h12, h22;
-    float2 p00, p01, p02, p11, p12, p22;
-    float rc2, rc2e;
-    float2 half_alpha;   // alpha / 2
-    float2 m_a2_log2e;   // -alpha^2 log2(e)
-};
-
-// erfc(alpha r) from r and r^2 (see erfc_fit; t = 1/(1 + alpha r/2), exp(-alpha^2 r^2) = 2^(c r^2))
-__device__ __forceinline__ float2 erfc_fit2(float2 r, float2 r2, const Geo2& g) {
-    const float2 a = fma2(g.half_alpha, r, f2(1.0f));
-    const float2 t = make_float2(rcp_approx(a.x), rcp_approx(a.y));
-    const float2 y = fma2(t, f2(3.0f), f2(-2.0f));
-    float2 q = f2(-1.1504688e-05f);
-    q = fma2(q, y, f2(0.00012701178f));
-    q = fma2(q, y, f2(1.719709e-05f));
-    q = fma2(q, y, f2(-0.002622572f));
-    q = fma2(q, y, f2(0.00045600548f));
-    q = fma2(q, y, f2(0.06661939f));
-    q = fma2(q, y, f2(0.29403913f));
-    q = fma2(q, y, f2(0.6413754f));
-    const float2 arg = mul2(g.m_a2_log2e, r2);
-    return mul2(mul2(q, t), make_float2(ex2_approx(arg.x), ex2_approx(arg.y)));
-}
-
-// erfc(alpha r) and exp(-alpha^2 r^2), for the adjoint
-__device__ __forceinline__ float2 erfc_fit2_exp(float2 r, float2 r2, const Geo2& g, float2& ex) {
-    const float2 a = fma2(g.half_alpha, r, f2(1.0f));
-    const float2 t = make_float2(rcp_approx(a.x), rcp_approx(a.y));
-    const float2 y = fma2(t, f2(3.0f), f2(-2.0f));
-    float2 q = f2(-1.1504688e-05f);
-    q = fma2(q, y, f2(0.00012701178f));
-    q = fma2(q, y, f2(1.719709e-05f));
-    q = fma2(q, y, f2(-0.002622572f));
-    q = fma2(q, y, f2(0.00045600548f));
-    q = fma2(q, y, f2(0.06661939f));
-    q = fma2(q, y, f2(0.29403913f));
-    q = fma2(q, y, f2(0.6413754f));
-    const float2 arg = mul2(g.m_a2_log2e, r2);
-    ex = make_float2(ex2_approx(arg.x), ex2_approx(arg.y));
-    return mul2(mul2(q, t), ex);
-}
-
-// Per (record pair, site) adjoint accumulators
-struct Grad2 {
-    float2 i12, i6;        // sum r^-12, sum r^-6 within the LJ cutoff
-    float2 gx, gy, gz;     // sum c (dU/dr^2) with the site's charge folded into the Coulomb part
-};
-
-// The forward pair terms plus the adjoint ones.  c = x_framework - x_site (Cartesian, the
-// frame of the upper-triangular box); dU/dx_site = -2 sum_j c_j dU_j/d(r^2).
-template <bool CHARGED>
-__device__ __forceinline__ void pair2_grad(const int4 ra, const int4 rb, const uint32_t ux, const uint32_t uy,
-                                           const uint32_t uz, const Geo2& g, const float2 lj12, const float2 lj6,
-                                           const float2 qcoul, const float2 c1, const float2 lane_mask,
-                                           float& segmin, float2& ljp, float2& php, Grad2& G) {
-    const float2 dx = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.x) - ux)),
-                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.x) - ux)));
-    const float2 dy = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.y) - uy)),
-                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.y) - uy)));
-    const float2 dz = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.z) - uz)),
-                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.z) - uz)));
-    const float2 rx = fma2(g.p00, dx, fma2(g.p01, dy, mul2(g.p02, dz)));
-    const float2 ry = fma2(g.p11, dy, mul2(g.p12, dz));
-    const float2 rz = mul2(g.p22, dz);
-    const float2 cx = fma2(g.h00, dx, fma2(g.h01, dy, fma2(g.h02, dz, rx)));
-    const float2 cy = fma2(g.h11, dy, fma2(g.h12, dz, ry));
-    const float2 cz = fma2(g.h22, dz, rz);
-    const float2 r2 = fma2(cx, cx, fma2(cy, cy, mul2(cz, cz)));
-    segmin = fminf(segmin, fminf(r2.x, r2.y));
-    float2 ir2, y = f2(0.0f);
-    if (CHARGED) {
-        y = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
-        const float2 hy = mul2(f2(-0.5f), mul2(r2, y));
-        y = fma2(y, fma2(hy, y, f2(0.5f)), y);
-        ir2 = mul2(y, y);
-    } else {
-        const float2 r0 = make_float2(rcp_approx(r2.x), rcp_approx(r2.y));
-        const float2 e = fma2(mul2(f2(-1.0f), r2), r0, f2(1.0f));
-        ir2 = fma2(r0, e, r0);
-    }
-    const float2 ir6 = mul2(mul2(ir2, ir2), ir2);
-    const float2 ir6c = mul2(lane_mask, make_float2(r2.x < g.rc2 ? ir6.x : 0.0f, r2.y < g.rc2 ? ir6.y : 0.0f));
-    const float2 ir12c = mul2(ir6c, ir6c);
-    ljp = fma2(ir6c, fma2(lj12, ir6c, lj6), ljp);
-    G.i12 = __fadd2_rn(G.i12, ir12c);
-    G.i6 = __fadd2_rn(G.i6, ir6c);
-    // dU_LJ/d(r^2) = -r^-2 r^-6 (6 lj12 r^-6 + 3 lj6)
-    float2 du = mul2(mul2(f2(-1.0f), ir2), mul2(ir6c, fma2(mul2(f2(6.0f), lj12), ir6c, mul2(f2(3.0f), lj6))));
-    if (CHARGED) {
-        const float2 rr = mul2(r2, y);
-        float2 ex;
-        const float2 erfcv = erfc_fit2_exp(rr, r2, g, ex);
-        const float2 e = mul2(erfcv, y);
-        const float2 qj = make_float2(__int_as_float(ra.w), __int_as_float(rb.w));
-        const float2 in_e = mul2(lane_mask, make_float2(r2.x < g.rc2e ? 1.0f : 0.0f, r2.y < g.rc2e ? 1.0f : 0.0f));
-        php = fma2(mul2(qj, in_e), e, php);
-        // d(q_j erfc(a r)/r)/d(r^2) = -q_j r^-2 / 2 [c1 exp(-a^2 r^2) + erfc(a r)/r], c1 = 2a/sqrt(pi)
-        const float2 dc = mul2(mul2(mul2(f2(-0.5f), mul2(qj, in_e)), ir2), fma2(c1, ex, e));
-        du = fma2(qcoul, dc, du);
-    }
-    G.gx = fma2(cx, du, G.gx);
-    G.gy = fma2(cy, du, G.gy);
-    G.gz = fma2(cz, du, G.gz);
-}
-
-template <bool CHARGED>
-__device__ __forceinline__ void pair2_fwd(const int4 ra, const int4 rb, const uint32_t ux, const uint32_t uy,
-                                          const uint32_t uz, const Geo2& g, const float2 lj12, const float2 lj6,
-                                          float& segmin, float2& ljp, float2& php) {
-    const float2 dx = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.x) - ux)),
-                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.x) - ux)));
-    const float2 dy = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.y) - uy)),
-                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.y) - uy)));
-    const float2 dz = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.z) - uz)),
-                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.z) - uz)));
-    const float2 rx = fma2(g.p00, dx, fma2(g.p01, dy, mul2(g.p02, dz)));
-    const float2 ry = fma2(g.p11, dy, mul2(g.p12, dz));
-    const float2 rz = mul2(g.p22, dz);
-    const float2 cx = fma2(g.h00, dx, fma2(g.h01, dy, fma2(g.h02, dz, rx)));
-    const float2 cy = fma2(g.h11, dy, fma2(g.h12, dz, ry));
-    const float2 cz = fma2(g.h22, dz, rz);
-    const float2 r2 = fma2(cx, cx, fma2(cy, cy, mul2(cz, cz)));
-    segmin = fminf(segmin, fminf(r2.x, r2.y));
-    float2 ir2, y = f2(0.0f);
-    if (CHARGED) {
-        // rsqrt estimate refined by one Newton step: y <- y + y (1/2 - (r2/2) y^2)
-        y = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
-        const float2 hy = mul2(f2(-0.5f), mul2(r2, y));
-        y = fma2(y, fma2(hy, y, f2(0.5f)), y);
-        ir2 = mul2(y, y);
-    } else {
-        const float2 r0 = make_float2(rcp_approx(r2.x), rcp_approx(r2.y));
-        const float2 e = fma2(mul2(f2(-1.0f), r2), r0, f2(1.0f));
-        ir2 = fma2(r0, e, r0);
-    }
-    // 4 eps [(s2/r2)^6 - (s2/r2)^3] = ir6 (lj12 ir6 - lj6), ir6 zeroed beyond the cutoff
-    const float2 ir6 = mul2(mul2(ir2, ir2), ir2);
-    const float2 ir6c = make_float2(r2.x < g.rc2 ? ir6.x : 0.0f, r2.y < g.rc2 ? ir6.y : 0.0f);
-    ljp = fma2(ir6c, fma2(lj12, ir6c, lj6), ljp);
-    if (CHARGED) {
-        const float2 rr = mul2(r2, y);
-        const float2 e = mul2(erfc_fit2(rr, r2, g), y);
-        php = fma2(make_float2(__int_as_float(ra.w), __int_as_float(rb.w)),
-                   make_float2(r2.x < g.rc2e ? e.x : 0.0f, r2.y < g.rc2e ? e.y : 0.0f), php);
-    }
-}
-
-// Reciprocal-space energy of the whole guest, sum_k Re[wt_k S(k) G(k)] with
-// G(k) = sum_g q_g e^{-ik.x_g} = e^{-ik.x_0} (q_tot + sum_g q_g (e^{-ik.(x_g - x_0)} - 1)).
-// Combining the guest's charges per k before multiplying by the (large) wt_k S(k) keeps
-// the sum free of the cancellation between per-site potentials of a neutral molecule;
-// D_g = e^{-ik.d_g} - 1 is carried by the recurrence D <- D w + (w - 1), whose error is
-// relative to |D|.  Phases are exact 32-bit fixed-point turns.  Rows of constant (ka, kb)
-// start at the kc nearest 0 and step outward in kc by `dir`.
-template <int NS, bool GRAD = false>
-__device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua[NS], const uint32_t Ub[NS],
-                                           const uint32_t Uc[NS], float& plr_hi, float& plr_lo,
-                                           float (*gu)[3] = nullptr) {
-    // GRAD: gu[g][d] receives dU_lr/du_g (fractional coordinates of site g)
-    constexpr float kTurn = 4.656612873077393e-10f;  // 2^-31: int32 fixed point -> half turns
-    plr_hi = 0.0f;
-    plr_lo = 0.0f;
-    // offsets of sites 1.. from site 0 (exact small integers) and their charges
-    int da[NS], db[NS], dc[NS];
-    float qg[NS];
-    float qtot = 0.0f;
-#pragma unroll
-    for (int k = 0; k < NS; ++k) {
-        da[k] = static_cast<int>(Ua[k] - Ua[0]);
-        db[k] = static_cast<int>(Ub[k] - Ub[0]);
-        dc[k] = static_cast<int>(Uc[k] - Uc[0]);
-        qg[k] = (k < S.n_sites) ? S.q[k] : 0.0f;
-        qtot += qg[k];
-    }
-    // step factors along +kc: w0 = e^{-2 pi i uc0} for site 0; for site g: wd = e^{-2 pi i dc_g},
-    // dw = wd - 1 = (-2 sin^2(pi dc), -sin(2 pi dc)) evaluated without cancellation
-    float w0r, w0i;
-    {
-        float sn, cs;
-        sincospif(static_cast<float>(static_cast<int32_t>(Uc[0])) * kTurn, &sn, &cs);
-        w0r = cs;
-        w0i = -sn;
-    }
-    float wdr[NS], wdi[NS], dwr[NS], dwi[NS];
-#pragma unroll
-    for (int k = 1; k < NS; ++k) {
-        float sn, cs;
-        sincospif(static_cast<float>(dc[k]) * (0.5f * kTurn), &sn, &cs);  // half angle
-        dwr[k] = -2.0f * sn * sn;
-        dwi[k] = -2.0f * sn * cs;
-        wdr[k] = 1.0f + dwr[k];
-        wdi[k] = dwi[k];
-    }
-    for (int row = 0; row < S.n_krow; ++row) {
-        const KRow R = S.krow[row];
-        const float sgn = static_cast<float>(R.dir);  // +1 or -1: direction along kc
-        // site-0 phasor at the row start
-        float er, ei;
-        {
-            const uint32_t P = static_cast<uint32_t>(R.ka) * Ua[0] + static_cast<uint32_t>(R.kb) * Ub[0] +
-                               static_cast<uint32_t>(R.kc0) * Uc[0];
-            float sn, cs;
-            sincospif(static_cast<float>(static_cast<int32_t>(P)) * kTurn, &sn, &cs);
-            er = cs;
-            ei = -sn;
-        }
-        const float sw0i = sgn * w0i;  // conj for the downward direction
-        float Dr[NS], Di[NS], swdi[NS], sdwi[NS];
-#pragma unroll
-        for (int k = 1; k < NS; ++k) {
-            const int p = R.ka * da[k] + R.kb * db[k] + R.kc0 * dc[k];
-            float sn, cs;
-            sincospif(static_cast<float>(p) * (0.5f * kTurn), &sn, &cs);  // half angle
-            Dr[k] = -2.0f * sn * sn;
-            Di[k] = -2.0f * sn * cs;
-            swdi[k] = sgn * wdi[k];
-            sdwi[k] = sgn * dwi[k];
-        }
-        float part = 0.0f;
-        float vs[NS], vk[NS];  // GRAD: sum_m Im[T E_g] and sum_m kc Im[T E_g] along the row
-#pragma unroll
-        for (int k = 0; k < NS; ++k) vs[k] = vk[k] = 0.0f;
-        float kcf = static_cast<float>(R.kc0);
-        const float2* sw = S.skw + R.off;
-        for (int m = 0; m < R.n; ++m) {
-            const float2 w = __ldg(sw + m);
-            // H = q_tot + sum_g q_g D_g
-            float hr = qtot, hi = 0.0f;
-#pragma unroll
-            for (int k = 1; k < NS; ++k) {
-                hr = fmaf(qg[k], Dr[k], hr);
-                hi = fmaf(qg[k], Di[k], hi);
-            }
-            // T = wt S e^{-ik.x0};  part += Re[T H]
-            const float tr = fmaf(w.x, er, -w.y * ei);
-            const float ti = fmaf(w.x, ei, w.y * er);
-            part = fmaf(tr, hr, fmaf(-ti, hi, part));
-            if (GRAD) {
-                // Im[T (1 + D_g)] for every site (D_0 = 0)
-#pragma unroll
-                for (int k = 0; k < NS; ++k) {
-                    const float v = (k == 0) ? ti : fmaf(tr, Di[k], fmaf(ti, Dr[k], ti));
-                    vs[k] += v;
-                    vk[k] = fmaf(kcf, v, vk[k]);
-                }
-                kcf += sgn;
-            }
-            // advance one step in kc
-            const float nr = fmaf(er, w0r, -ei * sw0i);
-            ei = fmaf(er, sw0i, ei * w0r);
-            er = nr;
-#pragma unroll
-            for (int k = 1; k < NS; ++k) {
-                const float dr2 = fmaf(Dr[k], wdr[k], fmaf(-Di[k], swdi[k], dwr[k]));
-                Di[k] = fmaf(Dr[k], swdi[k], fmaf(Di[k], wdr[k], sdwi[k]));
-                Dr[k] = dr2;
-            }
-        }
-        two_sum_acc(plr_hi, plr_lo, part);
-        if (GRAD) {
-            // dU/du_g = 2 pi q_g sum_k k Im[T E_g]
-#pragma unroll
-            for (int k = 0; k < NS; ++k) {
-                const float f = 6.283185307179586f * qg[k];
-                gu[k][0] = fmaf(f * static_cast<float>(R.ka), vs[k], gu[k][0]);
-                gu[k][1] = fmaf(f * static_cast<float>(R.kb), vs[k], gu[k][1]);
-                gu[k][2] = fmaf(f, vk[k], gu[k][2]);
-            }
-        }
-    }
-}
-
-// ----------------------------------------------------------------------------
-// the pair kernel
-// ----------------------------------------------------------------------------
-template <int NS, bool CHARGED>
+// Single-system launch: CTA b runs unit b.
+template <int NS, bool CHARGED, bool GRAD>
 __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_constant__ LaunchArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     int4* stage = reinterpret_cast<int4*>(smem_raw);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + size_t(PMGB_NSTAGE) * PMGB_TILE * sizeof(int4));
     __shared__ LsePartial red[PMGB_THREADS / 32];
-
-    const SysDev& S = a.sys;
     const int tid = threadIdx.x;
-
-    // ---- which item this thread owns -------------------------------------
-    long long item = 0;
-    bool valid = false;
+    UnitIO io{};
+    io.pose_mode = a.pose_mode;
+    io.out_mode = a.out_mode;
     if (a.pose_mode == POSE_PHILOX) {
         const int b = blockIdx.x / a.ctas_per_block;
         const long long within = static_cast<long long>(blockIdx.x % a.ctas_per_block) * PMGB_THREADS + tid;
-        valid = within < a.n_per_block;
-        item = static_cast<long long>(b) * a.n_per_block + within;
+        io.valid = within < a.n_per_block;
+        io.item = static_cast<long long>(b) * a.n_per_block + within;
     } else if (a.pose_mode == POSE_SITES) {
-        item = static_cast<long long>(blockIdx.x) * PMGB_THREADS + tid;
-        valid = item < a.n_conf;
+        io.item = static_cast<long long>(blockIdx.x) * PMGB_THREADS + tid;
+        io.valid = io.item < a.n_conf;
     } else {
-        item = static_cast<long long>(blockIdx.x) * PMGB_THREADS + tid;
-        valid = item < static_cast<long long>(a.n_pts[0]) * a.n_pts[1] * a.n_pts[2];
+        io.item = static_cast<long long>(blockIdx.x) * PMGB_THREADS + tid;
+        io.valid = io.item < static_cast<long long>(a.n_pts[0]) * a.n_pts[1] * a.n_pts[2];
     }
-
-    // ---- guest site positions, 32-bit fixed-point fractions of the supercell ----
-    uint32_t ux[NS], uy[NS], uz[NS];
-#pragma unroll
-    for (int k = 0; k < NS; ++k) ux[k] = uy[k] = uz[k] = 0u;
-    if (valid) {
-        if (a.pose_mode == POSE_PHILOX) {
-            float xf[3], R[9];
-            make_pose(a.seed, static_cast<unsigned long long>(item), xf, R);
-            // the centre of mass is a 24-bit uniform: exact in fixed point
-            const uint32_t cx = frac2fix(xf[0]), cy = frac2fix(xf[1]), cz = frac2fix(xf[2]);
-#pragma unroll
-            for (int k = 0; k < NS; ++k) {
-                const float bx = S.body[k][0], by = S.body[k][1], bz = S.body[k][2];
-                const float ox = R[0] * bx + R[3] * by + R[6] * bz;
-                const float oy = R[1] * bx + R[4] * by + R[7] * bz;
-                const float oz = R[2] * bx + R[5] * by + R[8] * bz;
-                ux[k] = cx + frac2fix(S.g00 * ox + S.g01 * oy + S.g02 * oz);
-                uy[k] = cy + frac2fix(S.g11 * oy + S.g12 * oz);
-                uz[k] = cz + frac2fix(S.g22 * oz);
-            }
-        } else if (a.pose_mode == POSE_SITES) {
-            const uint32_t* p = a.site_fix + static_cast<size_t>(item) * S.n_sites * 3;
-#pragma unroll
-            for (int k = 0; k < NS; ++k) {
-                if (k < S.n_sites) {
-                    ux[k] = p[3 * k + 0];
-                    uy[k] = p[3 * k + 1];
-                    uz[k] = p[3 * k + 2];
-                }
-            }
-        } else {
-            const long long n1 = a.n_pts[0], n2 = a.n_pts[1];
-            const int i = static_cast<int>(item % n1);
-            const int j = static_cast<int>((item / n1) % n2);
-            const int kk = static_cast<int>(item / (n1 * n2));
-            ux[0] = a.grid_x[i];
-            uy[0] = a.grid_y[j];
-            uz[0] = a.grid_z[kk];
-        }
-    }
-
-    // ---- TMA ring set-up --------------------------------------------------
-    if (tid == 0) {
-#pragma unroll
-        for (int s = 0; s < PMGB_NSTAGE; ++s) mbar_init(&bars[s], 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    int last_issued = -1;
-    auto issue = [&](int t) {
-        const int slot = t % PMGB_NSTAGE;
-        const int t0 = t * PMGB_TILE;
-        const int cnt = min(PMGB_TILE, S.n_rec - t0);
-        const uint32_t bytes = static_cast<uint32_t>(cnt) * sizeof(int4);
-        mbar_expect_tx(&bars[slot], bytes);
-        bulk_g2s(stage + size_t(slot) * PMGB_TILE, S.rec + t0, bytes, &bars[slot]);
-        last_issued = t;
-    };
-    if (tid == 0) {
-        const int n0 = min(PMGB_NSTAGE, S.n_tiles);
-        for (int t = 0; t < n0; ++t) issue(t);
-    }
-
-    const Geo g{S.h00, S.h01, S.h02, S.h11, S.h12, S.h22, S.p00, S.p01, S.p02, S.p11, S.p12, S.p22,
-                S.rc2, S.rc2e, S.alpha};
-    const Geo2 g2{f2(S.h00), f2(S.h01), f2(S.h02), f2(S.h11), f2(S.h12), f2(S.h22),
-                  f2(S.p00), f2(S.p01), f2(S.p02), f2(S.p11), f2(S.p12), f2(S.p22),
-                  S.rc2, S.rc2e, f2(0.5f * S.alpha), f2(-S.alpha * S.alpha * 1.4426950408889634f)};
-    // per-site compensated accumulators (sites past n_sites are placeholders)
-    float lj_hi[NS], lj_lo[NS], ph_hi[NS], ph_lo[NS];
-#pragma unroll
-    for (int k = 0; k < NS; ++k) lj_hi[k] = lj_lo[k] = ph_hi[k] = ph_lo[k] = 0.0f;
-    bool ovl = false;
-    bool abort = false;
-    int fail_tile = 0;
-
-    for (int t = 0; t < S.n_tiles; ++t) {
-        const int slot = t % PMGB_NSTAGE;
-        const uint32_t parity = static_cast<uint32_t>(t / PMGB_NSTAGE) & 1u;
-        const bool ok = mbar_wait_bounded(&bars[slot], parity);
-        if (__syncthreads_or(!ok)) {
-            abort = true;
-            fail_tile = t;
-            break;
-        }
-        const int4* T = stage + size_t(slot) * PMGB_TILE;
-        const int t0 = t * PMGB_TILE;
-        const int t1 = min(t0 + PMGB_TILE, S.n_rec);
-        for (int sg = 0; sg < S.n_seg; ++sg) {
-            const SegDesc d = S.seg[sg];
-            const int lo = max(d.lo, t0), hi = min(d.hi, t1);
-            if (lo >= hi) continue;
-            float sig2[NS], eps4[NS], r2o[NS], segmin[NS], lj12[NS], lj6[NS];
-#pragma unroll
-            for (int k = 0; k < NS; ++k) {
-                const SitePar p = S.segpar[sg * PMGB_MAX_SITES + k];
-                sig2[k] = p.sig2;
-                eps4[k] = p.eps4;
-                r2o[k] = p.r2ovl;
-                lj12[k] = p.lj12;
-                lj6[k] = p.lj6;
-                segmin[k] = __int_as_float(0x7f800000);
-            }
-            for (int j0 = lo; j0 < hi; j0 += kChunk) {
-                const int j1 = min(j0 + kChunk, hi);
-                float2 ljp2[NS], php2[NS];
-#pragma unroll
-                for (int k = 0; k < NS; ++k) ljp2[k] = php2[k] = f2(0.0f);
-                int j = j0;
-                for (; j + 4 <= j1; j += 4) {
-                    const int4 r0 = T[j - t0], r1 = T[j + 1 - t0], r2 = T[j + 2 - t0], r3 = T[j + 3 - t0];
-#pragma unroll
-                    for (int k = 0; k < NS; ++k) {
-                        const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
-                        pair2_fwd<CHARGED>(r0, r1, ux[k], uy[k], uz[k], g2, a12, a6, segmin[k], ljp2[k], php2[k]);
-                        pair2_fwd<CHARGED>(r2, r3, ux[k], uy[k], uz[k], g2, a12, a6, segmin[k], ljp2[k], php2[k]);
-                    }
-                }
-                float ljp[NS], php[NS];
-#pragma unroll
-                for (int k = 0; k < NS; ++k) {
-                    ljp[k] = ljp2[k].x + ljp2[k].y;
-                    php[k] = php2[k].x + php2[k].y;
-                }
-                for (; j < j1; ++j) {
-                    const int4 r = T[j - t0];
-#pragma unroll
-                    for (int k = 0; k < NS; ++k)
-                        pair_fwd<CHARGED>(r, ux[k], uy[k], uz[k], g, sig2[k], eps4[k], segmin[k], ljp[k], php[k]);
-                }
-#pragma unroll
-                for (int k = 0; k < NS; ++k) {
-                    two_sum_acc(lj_hi[k], lj_lo[k], ljp[k]);
-                    if (CHARGED) two_sum_acc(ph_hi[k], ph_lo[k], php[k]);
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < NS; ++k) ovl = ovl || (segmin[k] < r2o[k]);
-        }
-        __syncthreads();  // every thread is done with this slot
-        if (tid == 0 && t + PMGB_NSTAGE < S.n_tiles) {
-            fence_proxy_async_smem();
-            issue(t + PMGB_NSTAGE);
-        }
-    }
-    if (abort) {
-        if (tid == 0) {
-            atomicOr(a.status, PMGB_DEVERR_TMA_TIMEOUT);
-            // let copies still in flight land before the CTA's shared memory is released
-            for (int t = fail_tile; t <= last_issued; ++t)
-                (void)mbar_wait_bounded(&bars[t % PMGB_NSTAGE], static_cast<uint32_t>(t / PMGB_NSTAGE) & 1u);
-        }
-        return;
-    }
-
-    // ---- reciprocal space ----------------------------------------------------
-    float pl_hi = 0.0f, pl_lo = 0.0f;
-    if (CHARGED && valid) kspace_fwd<NS>(S, ux, uy, uz, pl_hi, pl_lo);
-
-    // ---- per-item energies (FP64) ----------------------------------------------
-    const double inf = __longlong_as_double(0x7ff0000000000000ll);
-    double uv = 0.0, usr = 0.0, ulr = 0.0;
-#pragma unroll
-    for (int k = 0; k < NS; ++k) {
-        if (k < S.n_sites) {
-            uv += static_cast<double>(lj_hi[k]) + static_cast<double>(lj_lo[k]);
-            if (CHARGED) {
-                const double qk = static_cast<double>(S.q[k]);
-                if (qk != 0.0) usr += qk * (static_cast<double>(ph_hi[k]) + static_cast<double>(ph_lo[k]));
-            }
-        }
-    }
-    if (ovl) uv = inf;
-    usr *= S.coul;
-    if (CHARGED) ulr = static_cast<double>(pl_hi) + static_cast<double>(pl_lo);
-
-    if (a.out_mode == OUT_ENERGY) {
-        if (valid) {
-            a.e_out[3 * item + 0] = uv;
-            a.e_out[3 * item + 1] = usr;
-            a.e_out[3 * item + 2] = ulr;
-        }
-        return;
-    }
-    if (a.out_mode == OUT_GRID) {
-        if (valid) a.grid_out[item] = static_cast<float>(uv * static_cast<double>(a.unit_factor));
-        return;
-    }
-
-    // ---- Widom: log-sum-exp Boltzmann partials of this CTA ------------------------
-    const double ues = usr + ulr;
-    if (valid && a.u_out) {
-        a.u_out[2 * item + 0] = uv;
-        a.u_out[2 * item + 1] = ues;
-    }
-    double x = -inf, ev = 0.0, ee = 0.0;
-    long long ninf = 0;
-    if (valid) {
-        const double u = uv + ues;
-        if (isfinite(u)) {
-            x = -u * a.inv_temperature;
-            ev = uv;
-            ee = ues;
-        } else {
-            ninf = 1;
-        }
-    }
-    const unsigned full = 0xffffffffu;
-    double m = x;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(full, m, o));
-    double w = (m == -inf || x == -inf) ? 0.0 : exp(x - m);
-    double s = w, tv = w * ev, te = w * ee;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        s += __shfl_xor_sync(full, s, o);
-        tv += __shfl_xor_sync(full, tv, o);
-        te += __shfl_xor_sync(full, te, o);
-        ninf += __shfl_xor_sync(full, ninf, o);
-    }
-    const int warp = tid >> 5, lane = tid & 31;
-    if (lane == 0) red[warp] = LsePartial{m, s, tv, te, ninf, 0};
-    __syncthreads();
-    if (warp == 0) {
-        constexpr int NW = PMGB_THREADS / 32;
-        LsePartial p = (lane < NW) ? red[lane] : LsePartial{-inf, 0.0, 0.0, 0.0, 0, 0};
-        double M = p.m;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) M = fmax(M, __shfl_xor_sync(full, M, o));
-        const double f = (M == -inf || p.m == -inf) ? 0.0 : exp(p.m - M);
-        double s2 = p.s * f, tv2 = p.tv * f, te2 = p.te * f;
-        long long n2 = p.n_inf;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            s2 += __shfl_xor_sync(full, s2, o);
-            tv2 += __shfl_xor_sync(full, tv2, o);
-            te2 += __shfl_xor_sync(full, te2, o);
-            n2 += __shfl_xor_sync(full, n2, o);
-        }
-        if (lane == 0) a.partials[blockIdx.x] = LsePartial{M, s2, tv2, te2, n2, 0};
-    }
-}
-
-// The adjoint: the forward pair kernel plus, per item, dU/dx of the centre of mass and, per
-// (species segment, guest site), the sums of r^-12 and r^-6 within the LJ cutoff, from which
-// the host forms dU/d(epsilon) and dU/d(sigma^2) of every (guest, framework) species pair.
-// Pair terms are recomputed here rather than stored by the forward pass.
-template <int NS, bool CHARGED>
-__global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_grad_kernel(const __grid_constant__ LaunchArgs a) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    int4* stage = reinterpret_cast<int4*>(smem_raw);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + size_t(PMGB_NSTAGE) * PMGB_TILE * sizeof(int4));
-    __shared__ LsePartial red[PMGB_THREADS / 32];
-
-    const SysDev& S = a.sys;
-    const int tid = threadIdx.x;
-    long long item = 0;
-    bool valid = false;
-    if (a.pose_mode == POSE_PHILOX) {
-        const int b = blockIdx.x / a.ctas_per_block;
-        const long long within = static_cast<long long>(blockIdx.x % a.ctas_per_block) * PMGB_THREADS + tid;
-        valid = within < a.n_per_block;
-        item = static_cast<long long>(b) * a.n_per_block + within;
-    } else if (a.pose_mode == POSE_SITES) {
-        item = static_cast<long long>(blockIdx.x) * PMGB_THREADS + tid;
-        valid = item < a.n_conf;
-    } else {
-        item = static_cast<long long>(blockIdx.x) * PMGB_THREADS + tid;
-        valid = item < static_cast<long long>(a.n_pts[0]) * a.n_pts[1] * a.n_pts[2];
-    }
-    uint32_t ux[NS], uy[NS], uz[NS];
-#pragma unroll
-    for (int k = 0; k < NS; ++k) ux[k] = uy[k] = uz[k] = 0u;
-    if (valid) {
-        if (a.pose_mode == POSE_PHILOX) {
-            float xf[3], R[9];
-            make_pose(a.seed, static_cast<unsigned long long>(item), xf, R);
-            const uint32_t cx = frac2fix(xf[0]), cy = frac2fix(xf[1]), cz = frac2fix(xf[2]);
-#pragma unroll
-            for (int k = 0; k < NS; ++k) {
-                const float bx = S.body[k][0], by = S.body[k][1], bz = S.body[k][2];
-                const float ox = R[0] * bx + R[3] * by + R[6] * bz;
-                const float oy = R[1] * bx + R[4] * by + R[7] * bz;
-                const float oz = R[2] * bx + R[5] * by + R[8] * bz;
-                ux[k] = cx + frac2fix(S.g00 * ox + S.g01 * oy + S.g02 * oz);
-                uy[k] = cy + frac2fix(S.g11 * oy + S.g12 * oz);
-                uz[k] = cz + frac2fix(S.g22 * oz);
-            }
-        } else if (a.pose_mode == POSE_SITES) {
-            const uint32_t* p = a.site_fix + static_cast<size_t>(item) * S.n_sites * 3;
-#pragma unroll
-            for (int k = 0; k < NS; ++k)
-                if (k < S.n_sites) {
-                    ux[k] = p[3 * k + 0];
-                    uy[k] = p[3 * k + 1];
-                    uz[k] = p[3 * k + 2];
-                }
-        } else {
-            const long long n1 = a.n_pts[0], n2 = a.n_pts[1];
-            ux[0] = a.grid_x[static_cast<int>(item % n1)];
-            uy[0] = a.grid_y[static_cast<int>((item / n1) % n2)];
-            uz[0] = a.grid_z[static_cast<int>(item / (n1 * n2))];
-        }
-    }
-    if (tid == 0) {
-#pragma unroll
-        for (int s = 0; s < PMGB_NSTAGE; ++s) mbar_init(&bars[s], 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    int last_issued = -1;
-    auto issue = [&](int t) {
-        const int slot = t % PMGB_NSTAGE;
-        const int t0 = t * PMGB_TILE;
-        const int cnt = min(PMGB_TILE, S.n_rec - t0);
-        const uint32_t bytes = static_cast<uint32_t>(cnt) * sizeof(int4);
-        mbar_expect_tx(&bars[slot], bytes);
-        bulk_g2s(stage + size_t(slot) * PMGB_TILE, S.rec + t0, bytes, &bars[slot]);
-        last_issued = t;
-    };
-    if (tid == 0) {
-        const int n0 = min(PMGB_NSTAGE, S.n_tiles);
-        for (int t = 0; t < n0; ++t) issue(t);
-    }
-    const Geo2 g2{f2(S.h00), f2(S.h01), f2(S.h02), f2(S.h11), f2(S.h12), f2(S.h22),
-                  f2(S.p00), f2(S.p01), f2(S.p02), f2(S.p11), f2(S.p12), f2(S.p22),
-                  S.rc2, S.rc2e, f2(0.5f * S.alpha), f2(-S.alpha * S.alpha * 1.4426950408889634f)};
-    const float2 c1 = f2(1.1283791670955126f * S.alpha);  // 2 alpha / sqrt(pi)
-    float lj_hi[NS], lj_lo[NS], ph_hi[NS], ph_lo[NS];
-    float2 gx[NS], gy[NS], gz[NS];
-#pragma unroll
-    for (int k = 0; k < NS; ++k) {
-        lj_hi[k] = lj_lo[k] = ph_hi[k] = ph_lo[k] = 0.0f;
-        gx[k] = gy[k] = gz[k] = f2(0.0f);
-    }
-    bool ovl = false, abort = false;
-    int fail_tile = 0;
-    for (int t = 0; t < S.n_tiles; ++t) {
-        const int slot = t % PMGB_NSTAGE;
-        const uint32_t parity = static_cast<uint32_t>(t / PMGB_NSTAGE) & 1u;
-        const bool ok = mbar_wait_bounded(&bars[slot], parity);
-        if (__syncthreads_or(!ok)) {
-            abort = true;
-            fail_tile = t;
-            break;
-        }
-        const int4* T = stage + size_t(slot) * PMGB_TILE;
-        const int t0 = t * PMGB_TILE;
-        const int t1 = min(t0 + PMGB_TILE, S.n_rec);
-        for (int sg = 0; sg < S.n_seg; ++sg) {
-            const SegDesc d = S.seg[sg];
-            const int lo = max(d.lo, t0), hi = min(d.hi, t1);
-            if (lo >= hi) continue;
-            float r2o[NS], segmin[NS], lj12[NS], lj6[NS];
-#pragma unroll
-            for (int k = 0; k < NS; ++k) {
-                const SitePar p = S.segpar[sg * PMGB_MAX_SITES + k];
-                r2o[k] = p.r2ovl;
-                lj12[k] = p.lj12;
-                lj6[k] = p.lj6;
-                segmin[k] = __int_as_float(0x7f800000);
-            }
-            float2 i12[NS], i6[NS];
-#pragma unroll
-            for (int k = 0; k < NS; ++k) i12[k] = i6[k] = f2(0.0f);
-            for (int j0 = lo; j0 < hi; j0 += kChunk) {
-                const int j1 = min(j0 + kChunk, hi);
-                float2 ljp2[NS], php2[NS];
-#pragma unroll
-                for (int k = 0; k < NS; ++k) ljp2[k] = php2[k] = f2(0.0f);
-                for (int j = j0; j < j1; j += 2) {
-                    const bool pair = j + 1 < j1;
-                    const int4 ra = T[j - t0];
-                    const int4 rb = pair ? T[j + 1 - t0] : ra;
-                    const float2 mask = make_float2(1.0f, pair ? 1.0f : 0.0f);
-#pragma unroll
-                    for (int k = 0; k < NS; ++k) {
-                        Grad2 G{i12[k], i6[k], gx[k], gy[k], gz[k]};
-                        pair2_grad<CHARGED>(ra, rb, ux[k], uy[k], uz[k], g2, f2(lj12[k]), f2(lj6[k]),
-                                            f2(S.q[k] * static_cast<float>(S.coul)), c1, mask, segmin[k], ljp2[k],
-                                            php2[k], G);
-                        i12[k] = G.i12;
-                        i6[k] = G.i6;
-                        gx[k] = G.gx;
-                        gy[k] = G.gy;
-                        gz[k] = G.gz;
-                    }
-                }
-#pragma unroll
-                for (int k = 0; k < NS; ++k) {
-                    two_sum_acc(lj_hi[k], lj_lo[k], ljp2[k].x + ljp2[k].y);
-                    if (CHARGED) two_sum_acc(ph_hi[k], ph_lo[k], php2[k].x + php2[k].y);
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < NS; ++k) ovl = ovl || (segmin[k] < r2o[k]);
-            // this thread owns its item's columns: write on the segment's first tile, add after
-            if (valid) {
-                const bool first = (lo == d.lo);
-#pragma unroll
-                for (int k = 0; k < NS; ++k) {
-                    float* c12 = a.dsum + static_cast<size_t>((sg * NS + k) * 2) * a.dsum_stride + item;
-                    float* c6 = c12 + a.dsum_stride;
-                    const float v12 = i12[k].x + i12[k].y, v6 = i6[k].x + i6[k].y;
-                    *c12 = first ? v12 : *c12 + v12;
-                    *c6 = first ? v6 : *c6 + v6;
-                }
-            }
-        }
-        __syncthreads();
-        if (tid == 0 && t + PMGB_NSTAGE < S.n_tiles) {
-            fence_proxy_async_smem();
-            issue(t + PMGB_NSTAGE);
-        }
-    }
-    if (abort) {
-        if (tid == 0) {
-            atomicOr(a.status, PMGB_DEVERR_TMA_TIMEOUT);
-            for (int t = fail_tile; t <= last_issued; ++t)
-                (void)mbar_wait_bounded(&bars[t % PMGB_NSTAGE], static_cast<uint32_t>(t / PMGB_NSTAGE) & 1u);
-        }
-        return;
-    }
-    float pl_hi = 0.0f, pl_lo = 0.0f;
-    float gu[NS][3];
-#pragma unroll
-    for (int k = 0; k < NS; ++k) gu[k][0] = gu[k][1] = gu[k][2] = 0.0f;
-    if (CHARGED && valid) kspace_fwd<NS, true>(S, ux, uy, uz, pl_hi, pl_lo, gu);
-
-    const double inf = __longlong_as_double(0x7ff0000000000000ll);
-    double uv = 0.0, usr = 0.0, ulr = 0.0;
-    float gcx = 0.0f, gcy = 0.0f, gcz = 0.0f;
-#pragma unroll
-    for (int k = 0; k < NS; ++k) {
-        if (k < S.n_sites) {
-            uv += static_cast<double>(lj_hi[k]) + static_cast<double>(lj_lo[k]);
-            if (CHARGED && S.q[k] != 0.0f)
-                usr += static_cast<double>(S.q[k]) * (static_cast<double>(ph_hi[k]) + static_cast<double>(ph_lo[k]));
-            // real space: dU/dx_site = -2 sum c dU/dr^2; reciprocal space: G^T dU/du
-            gcx += -2.0f * (gx[k].x + gx[k].y) + S.g00 * gu[k][0];
-            gcy += -2.0f * (gy[k].x + gy[k].y) + S.g01 * gu[k][0] + S.g11 * gu[k][1];
-            gcz += -2.0f * (gz[k].x + gz[k].y) + S.g02 * gu[k][0] + S.g12 * gu[k][1] + S.g22 * gu[k][2];
-        }
-    }
-    if (ovl) uv = inf;
-    usr *= S.coul;
-    if (CHARGED) ulr = static_cast<double>(pl_hi) + static_cast<double>(pl_lo);
-    if (valid && a.grad_u) {
-        a.grad_u[3 * item + 0] = gcx;
-        a.grad_u[3 * item + 1] = gcy;
-        a.grad_u[3 * item + 2] = gcz;
-    }
-    if (a.out_mode == OUT_ENERGY) {
-        if (valid) {
-            a.e_out[3 * item + 0] = uv;
-            a.e_out[3 * item + 1] = usr;
-            a.e_out[3 * item + 2] = ulr;
-        }
-        return;
-    }
-    if (a.out_mode == OUT_GRID) {
-        if (valid) {
-            a.grid_out[item] = static_cast<float>(uv * static_cast<double>(a.unit_factor));
-            if (a.u_out) a.u_out[item] = uv;
-        }
-        return;
-    }
-    const double ues = usr + ulr;
-    if (valid && a.u_out) {
-        a.u_out[2 * item + 0] = uv;
-        a.u_out[2 * item + 1] = ues;
-    }
-    double x = -inf, ev = 0.0, ee = 0.0;
-    long long ninf = 0;
-    if (valid) {
-        const double u = uv + ues;
-        if (isfinite(u)) {
-            x = -u * a.inv_temperature;
-            ev = uv;
-            ee = ues;
-        } else {
-            ninf = 1;
-        }
-    }
-    const unsigned full = 0xffffffffu;
-    double m = x;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(full, m, o));
-    double w = (m == -inf || x == -inf) ? 0.0 : exp(x - m);
-    double s = w, tv = w * ev, te = w * ee;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        s += __shfl_xor_sync(full, s, o);
-        tv += __shfl_xor_sync(full, tv, o);
-        te += __shfl_xor_sync(full, te, o);
-        ninf += __shfl_xor_sync(full, ninf, o);
-    }
-    const int warp = tid >> 5, lane = tid & 31;
-    if (lane == 0) red[warp] = LsePartial{m, s, tv, te, ninf, 0};
-    __syncthreads();
-    if (warp == 0) {
-        constexpr int NW = PMGB_THREADS / 32;
-        LsePartial p = (lane < NW) ? red[lane] : LsePartial{-inf, 0.0, 0.0, 0.0, 0, 0};
-        double M = p.m;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) M = fmax(M, __shfl_xor_sync(full, M, o));
-        const double f = (M == -inf || p.m == -inf) ? 0.0 : exp(p.m - M);
-        double s2 = p.s * f, tv2 = p.tv * f, te2 = p.te * f;
-        long long n2 = p.n_inf;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            s2 += __shfl_xor_sync(full, s2, o);
-            tv2 += __shfl_xor_sync(full, tv2, o);
-            te2 += __shfl_xor_sync(full, te2, o);
-            n2 += __shfl_xor_sync(full, n2, o);
-        }
-        if (lane == 0) a.partials[blockIdx.x] = LsePartial{M, s2, tv2, te2, n2, 0};
-    }
+    io.seed = a.seed;
+    io.inv_temperature = a.inv_temperature;
+    io.site_fix = a.site_fix;
+    io.grid_x = a.grid_x;
+    io.grid_y = a.grid_y;
+    io.grid_z = a.grid_z;
+    io.n1 = a.n_pts[0];
+    io.n2 = a.n_pts[1];
+    io.u_out = a.u_out;
+    io.e_out = a.e_out;
+    io.grid_out = a.grid_out;
+    io.unit_factor = a.unit_factor;
+    io.dsum = a.dsum;
+    io.dsum_stride = a.dsum_stride;
+    io.col_item = io.item;
+    io.grad_u = a.grad_u;
+    io.partial = a.partials ? a.partials + blockIdx.x : nullptr;
+    ring_init(bars);
+    uint32_t fills[PMGB_NSTAGE] = {};
+    (void)run_unit<NS, CHARGED, GRAD>(a.sys, io, stage, bars, red, fills, a.status);
 }
 
 // log_scale[0] = max_i (-U_i / T) over finite U (one CTA, fixed order)
@@ -1107,7 +98,10 @@ __global__ void weighted_columns_kernel(const double* __restrict__ u, int u_stri
 #pragma unroll
             for (int c = 0; c < 32; ++c) {
                 const int cc = c0 + c;
-                if (cc < n_cols) acc[c] = fma(w, static_cast<double>(cols[static_cast<size_t>(cc) * col_stride + i]), acc[c]);
+                // w = 0 for U = +Inf, whose columns may hold Inf: skip rather than form 0 * Inf
+                if (cc < n_cols) {
+                    if (w > 0.0) acc[c] = fma(w, static_cast<double>(cols[static_cast<size_t>(cc) * col_stride + i]), acc[c]);
+                }
                 else if (cc == n_cols) acc[c] += w;
                 else if (cc == n_cols + 1) acc[c] = fma(w, isfinite(uu) ? ue : 0.0, acc[c]);
             }
@@ -1178,23 +172,23 @@ __global__ void reduce_blocks_kernel(const LsePartial* __restrict__ partials, in
     }
 }
 
-// S(k) = sum_c q_c e^{2 pi i (ka fa + kb fb + kc fc)}; one warp per k-vector, FP64
-// accumulation of terms whose phase is exact in 32-bit fixed point.
-__global__ void structure_factor_kernel(const uint32_t* __restrict__ qfix, const double* __restrict__ q,
+// S(k) = sum_c q_c e^{2 pi i (ka fa + kb fb + kc fc)}; one warp per k-vector, FP64 terms and
+// accumulation from the exact FP64 charge positions.
+__global__ void structure_factor_kernel(const double* __restrict__ qxf, const double* __restrict__ q,
                                         int n_q, const int* __restrict__ kabc, const double* __restrict__ wt,
                                         int n_k, double* __restrict__ sk_out, float2* __restrict__ skw_out) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= n_k) return;
-    const uint32_t ka = static_cast<uint32_t>(kabc[3 * warp]), kb = static_cast<uint32_t>(kabc[3 * warp + 1]),
-                   kc = static_cast<uint32_t>(kabc[3 * warp + 2]);
+    const double ka = kabc[3 * warp], kb = kabc[3 * warp + 1], kc = kabc[3 * warp + 2];
     double re = 0.0, im = 0.0;
     for (int c = lane; c < n_q; c += 32) {
-        const uint32_t P = ka * qfix[3 * c] + kb * qfix[3 * c + 1] + kc * qfix[3 * c + 2];
-        float sn, cs;
-        sincospif(static_cast<float>(static_cast<int32_t>(P)) * 4.656612873077393e-10f, &sn, &cs);
-        re = fma(q[c], static_cast<double>(cs), re);
-        im = fma(q[c], static_cast<double>(sn), im);
+        // phase k.x in turns from the exact FP64 fractional coordinates
+        const double t = ka * qxf[3 * c] + kb * qxf[3 * c + 1] + kc * qxf[3 * c + 2];
+        double sn, cs;
+        sincospi(2.0 * t, &sn, &cs);
+        re = fma(q[c], cs, re);
+        im = fma(q[c], sn, im);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -1248,20 +242,20 @@ __global__ void __launch_bounds__(256) fp32_peak_kernel(float* sink, int iters) 
 template <int NS, bool CH>
 cudaError_t launch_one(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
     const size_t smem = pmgb_pairs_smem_bytes();
-    cudaError_t e = cudaFuncSetAttribute(pairs_kernel<NS, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(pairs_kernel<NS, CH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    pairs_kernel<NS, CH><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
+    pairs_kernel<NS, CH, false><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
     return cudaGetLastError();
 }
 
 template <int NS, bool CH>
 cudaError_t launch_grad_one(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
     const size_t smem = pmgb_pairs_smem_bytes();
-    cudaError_t e = cudaFuncSetAttribute(pairs_grad_kernel<NS, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(pairs_kernel<NS, CH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    pairs_grad_kernel<NS, CH><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
+    pairs_kernel<NS, CH, true><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -1327,13 +321,13 @@ cudaError_t pmgb_launch_reduce_blocks(const LsePartial* partials, int n_blocks, 
     return cudaGetLastError();
 }
 
-cudaError_t pmgb_launch_structure_factor(const uint32_t* qfix, const double* q, int n_q, const int* kabc,
+cudaError_t pmgb_launch_structure_factor(const double* qxf, const double* q, int n_q, const int* kabc,
                                          const double* wt, int n_k, double* sk_out, float2* skw_out,
                                          cudaStream_t st) {
     if (n_k <= 0) return cudaSuccess;
     const int warps_per_cta = 8;
     const int ctas = (n_k + warps_per_cta - 1) / warps_per_cta;
-    structure_factor_kernel<<<ctas, 32 * warps_per_cta, 0, st>>>(qfix, q, n_q, kabc, wt, n_k, sk_out, skw_out);
+    structure_factor_kernel<<<ctas, 32 * warps_per_cta, 0, st>>>(qxf, q, n_q, kabc, wt, n_k, sk_out, skw_out);
     return cudaGetLastError();
 }
 

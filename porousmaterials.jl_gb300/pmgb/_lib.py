@@ -47,6 +47,7 @@ SIGNATURES = [
     ("pmgb_system_sites", C.c_int, [_vp, _ip, _ip]),
     ("pmgb_structure_factor", C.c_int, [_vp, _dp]),
     ("pmgb_energies", C.c_int, [_vp, C.c_int64, _dp, _dp]),
+    ("pmgb_system_set_refine", C.c_int, [_vp, C.c_double]),
     ("pmgb_widom", C.c_int, [_vp, C.c_int64, C.c_int32, C.c_uint64, C.c_double, _dp, _dp]),
     ("pmgb_widom_device", C.c_int, [_vp, C.c_int64, C.c_int32, C.c_uint64, C.c_double, _vp, _vp]),
     ("pmgb_widom_noalloc", C.c_int, [_vp, C.c_int64, C.c_int32, C.c_uint64, C.c_double, _vp, _vp]),
@@ -56,6 +57,14 @@ SIGNATURES = [
     ("pmgb_sample_poses", C.c_int, [_vp, C.c_uint64, C.c_int64, C.c_int64, _fp, _fp]),
     ("pmgb_energy_grid", C.c_int, [_vp, _ip, _ip, C.c_double, _fp]),
     ("pmgb_energy_grid_device", C.c_int, [_vp, _ip, _ip, C.c_double, _vp]),
+    ("pmgb_batch_create", C.c_int, [_vp, C.c_int32, C.POINTER(_vp), C.POINTER(C.c_int64), C.c_int32, C.c_int32,
+                                     C.POINTER(_vp)]),
+    ("pmgb_batch_destroy", None, [_vp]),
+    ("pmgb_batch_configure", C.c_int, [_vp, C.c_int32, C.c_int32, C.c_double]),
+    ("pmgb_batch_tune", C.c_int, [_vp, C.c_uint64, C.c_double, C.c_int32, _dp]),
+    ("pmgb_batch_launch", C.c_int, [_vp, C.c_uint64, C.c_double]),
+    ("pmgb_batch_results", C.c_int, [_vp, _dp, _dp]),
+    ("pmgb_batch_info", C.c_int, [_vp, C.POINTER(C.c_int64)]),
     ("pmgb_philox4x32_10", C.c_int, [_vp, C.c_int64, _up, _up, _up]),
     ("pmgb_fp32_peak", C.c_int, [_vp, C.c_int, C.c_int, _dp]),
     ("pmgb_device_status", C.c_int, [_vp, _up]),

@@ -8,7 +8,10 @@ Differences from the reference, by design:
   * each insertion applies a fresh uniform rotation to the molecule's reference
     orientation (the reference composes rotations, which has the same uniform
     distribution), so there is no bond-length drift to check (henry.jl:247-261);
-  * the five statistics blocks are CTAs on one GPU instead of Julia worker processes.
+  * the five statistics blocks are CTAs on one GPU instead of Julia worker processes;
+  * pair terms are FP32 (the reference is FP64); the insertions carrying all but
+    `refine_tail` of each block's Boltzmann weight are re-evaluated in FP64, so K_H and
+    <U> agree with an FP64 evaluation of the same insertions to ~1e-8.
 """
 from __future__ import annotations
 
@@ -31,6 +34,9 @@ from .system import GPUSystem
 UNIV_GAS_CONST = 8.3144598e-5   # m³ bar / (K mol), src/PorousMaterials.jl:11
 K_TO_KJ_PER_MOL = 8.3144598e-3  # kJ / (mol K), src/PorousMaterials.jl:12
 N_BLOCKS = 5                    # src/mc_helpers.jl:11
+# Boltzmann weight per block left to the FP32 energies; the rest is re-evaluated in FP64, which
+# holds K_H and <U> to ~1e-8 of the FP64 result (pmgb_system_set_refine)
+REFINE_TAIL = 1e-3
 
 
 class HenryResult(dict):
@@ -59,8 +65,8 @@ def _std(x: np.ndarray) -> float:
 def henry_coefficient(crystal: Crystal, molecule: Molecule, temperature: float, ljforcefield: LJForceField, *,
                       insertions_per_volume: float = 200, verbose: bool = True, ewald_precision: float = 1e-6,
                       autosave: bool = True, filename_comment: str = "", accessibility_grid=None,
-                      seed: int | None = None, masses: dict | None = None, system_out: list | None = None
-                      ) -> HenryResult:
+                      seed: int | None = None, masses: dict | None = None, system_out: list | None = None,
+                      refine_tail: float = REFINE_TAIL) -> HenryResult:
     assert_P1_symmetry(crystal)
     if accessibility_grid is not None:
         raise NotImplementedError("accessibility-gated Widom insertions are not supported by this build")
@@ -85,7 +91,7 @@ def henry_coefficient(crystal: Crystal, molecule: Molecule, temperature: float, 
                               verbose=verbose and charged) if charged else None
     if seed is None:
         seed = secrets.randbits(63)
-    system = GPUSystem(crystal, fmol, ljforcefield, eparams)
+    system = GPUSystem(crystal, fmol, ljforcefield, eparams, refine_tail=refine_tail)
     if system_out is not None:
         system_out.append(system)
     blocks, _ = system.widom(nb_per_block, N_BLOCKS, seed, temperature)
@@ -150,7 +156,8 @@ def henry_coefficient(crystal: Crystal, molecule: Molecule, temperature: float, 
 def henry_coefficient_gradient(crystal: Crystal, molecule: Molecule, temperature: float,
                                ljforcefield: LJForceField, *, insertions_per_volume: float = 200,
                                ewald_precision: float = 1e-6, seed: int | None = None,
-                               want_forces: bool = False, system_out: list | None = None):
+                               want_forces: bool = False, system_out: list | None = None,
+                               refine_tail: float = REFINE_TAIL):
     """K_H and its derivatives from one adjoint pass (pair terms recomputed, not stored).
 
     Returns a dict: 'henry coefficient [mol/(m³-bar)]' (block mean, as henry_coefficient),
@@ -169,7 +176,7 @@ def henry_coefficient_gradient(crystal: Crystal, molecule: Molecule, temperature
     eparams = setup_Ewald_sum(sc.box, ljforcefield.r_cutoff, eps=ewald_precision) if charged else None
     if seed is None:
         seed = secrets.randbits(63)
-    system = GPUSystem(sc, Frac(molecule, sc.box), ljforcefield, eparams)
+    system = GPUSystem(sc, Frac(molecule, sc.box), ljforcefield, eparams, refine_tail=refine_tail)
     if system_out is not None:
         system_out.append(system)
     blocks, adj = system.widom_adjoint(nb_per_block, N_BLOCKS, seed, temperature, want_grad=want_forces)

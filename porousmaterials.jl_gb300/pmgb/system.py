@@ -19,8 +19,9 @@ from .molecule import Molecule, body_offsets
 
 class GPUSystem:
     def __init__(self, crystal: Crystal, molecule: Molecule, ljff: LJForceField | None,
-                 eparams: EwaldParams | None = None, ctx: Context | None = None):
-        """ljff=None builds a charge-only system (all ε = 0, cutoff from eparams)."""
+                 eparams: EwaldParams | None = None, ctx: Context | None = None, refine_tail: float = 0.0):
+        """ljff=None builds a charge-only system (all ε = 0, cutoff from eparams); refine_tail > 0
+        turns on the FP64 refinement of the Boltzmann tail of Widom runs (set_refine)."""
         self.ctx = ctx or Context.default()
         self.crystal = crystal
         self.molecule = molecule
@@ -67,8 +68,11 @@ class GPUSystem:
         self.ctx.check(lib.pmgb_system_sites(h, ptr(sa, C.c_int32), ptr(sc, C.c_int32)))
         self.site_atom, self.site_charge = sa, sc
         self.eparams = None
+        self.refine_tail = 0.0
         if eparams is not None:
             self.set_ewald(eparams)
+        if refine_tail:
+            self.set_refine(refine_tail)
 
     # -- set-up ------------------------------------------------------------------------
     def set_ewald(self, ep: EwaldParams) -> None:
@@ -114,6 +118,12 @@ class GPUSystem:
         out = np.zeros((n, 3))
         self.ctx.check(self.ctx._lib.pmgb_energies(self.handle, n, ptr(site_xf, C.c_double), ptr(out, C.c_double)))
         return out
+
+    def set_refine(self, tail_fraction: float) -> None:
+        """FP64 refinement of the Boltzmann tail of Widom runs (see pmgb_system_set_refine);
+        0 switches it off."""
+        self.ctx.check(self.ctx._lib.pmgb_system_set_refine(self.handle, float(tail_fraction)))
+        self.refine_tail = float(tail_fraction)
 
     def widom(self, n_per_block: int, n_blocks: int, seed: int, temperature: float, want_energies: bool = False):
         """Per-block (log Σbf, ⟨U_vdw⟩, ⟨U_es⟩, n_inf) and optionally per-insertion (U_vdw, U_es)."""

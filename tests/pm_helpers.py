@@ -73,3 +73,22 @@ def within(a, b, rtol, atol):
 
 def deg(x):
     return math.radians(x)
+
+
+def widom_with_oracle(gs, n_per_block, seed, T=298.0, use_sk=True, n_blocks=5):
+    """GPU Widom blocks and per-insertion energies, and the oracle's FP64 energies of the exact
+    device poses: (blocks, u (n, 2), U_vdw, U_es)."""
+    from pmgb.molecule import body_offsets
+
+    blocks, u = gs.widom(n_per_block, n_blocks, seed, T, want_energies=True)
+    xf, rot = gs.ctx.sample_poses(seed, 0, n_blocks * n_per_block)
+    # the device rotation is column-major R[i + 3j], the layout the oracle takes
+    body = np.zeros((gs.n_sites, 3))
+    ax, qx = body_offsets(gs.molecule, gs.crystal.box)
+    for k in range(gs.n_sites):
+        body[k] = ax[gs.site_atom[k]] if gs.site_atom[k] >= 0 else qx[gs.site_charge[k]]
+    o = oracle_for(gs)
+    sites = o.sites_from_poses(xf.astype(np.float64), rot.astype(np.float64), body)
+    lj, q = oracle_sites_split(gs, sites)
+    v, sr, lr = o.energies(lj, q, charged=gs.charged, use_sk=use_sk)
+    return blocks, u, v, sr + lr

@@ -1,0 +1,166 @@
+"""Batched persistent screening (pmgb_batch_*) against the single-system entry points.
+
+Every system of a batch must see exactly the insertions of pmgb_widom with its own seed
+system_seed(seed, s), so block results agree to the last bit; the adjoint sums are
+accumulated in another order and with other weight offsets, so they agree to 1e-9
+relative.  The single-system results are themselves checked against the FP64 oracle and
+finite differences in test_gpu_parity.py and test_gpu_adjoint.py; the LJ-only members are
+also checked against the oracle here.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+import pmgb
+from pmgb import synthetic
+from pmgb.adjoint import henry_gradients
+from pmgb.batch import BatchScreen, build_systems, henry_coefficient_screen, system_seed
+from pm_helpers import oracle_for
+
+pytestmark = pytest.mark.gpu
+T = 298.0
+
+
+@pytest.fixture(scope="module")
+def mixed_systems():
+    """Frameworks of uneven size, each with CH4 (LJ only) and CO2 (LJ + Ewald)."""
+    ff = synthetic.forcefield()
+    fws = synthetic.batch_frameworks(6, seed=77)
+    ctx = pmgb.Context.default()
+    systems = build_systems(fws, synthetic.ch4(), ff, ctx=ctx) + build_systems(fws, synthetic.co2(), ff, ctx=ctx)
+    sizes = [gs.info()["n_records"] for gs in systems]
+    assert max(sizes) > 4 * min(sizes)  # uneven on purpose
+    return systems
+
+
+def test_batch_forward_matches_single_system(mixed_systems):
+    npb, nb, seed = 700, 5, 1234
+    screen = BatchScreen(mixed_systems, npb, nb)
+    blocks, adj = screen.run(seed, T)
+    assert adj is None
+    for s, gs in enumerate(mixed_systems):
+        ref, _ = gs.widom(npb, nb, system_seed(seed, s), T)
+        np.testing.assert_array_equal(blocks[s], ref)
+    # a replay with the same seed reproduces the run; another seed changes it
+    again, _ = screen.run(seed, T)
+    np.testing.assert_array_equal(again, blocks)
+    other, _ = screen.run(seed + 1, T)
+    assert not np.array_equal(other[:, :, 0], blocks[:, :, 0])
+    assert screen.ctx.device_status() == 0
+
+
+def test_batch_orders_and_shapes_agree(mixed_systems):
+    npb, nb, seed = 300, 5, 99
+    screen = BatchScreen(mixed_systems, npb, nb)
+    base, _ = screen.run(seed, T)
+    for n_ctas, order, mflop in ((1, 0, 0.0), (7, 1, 0.0), (0, 1, 1.0), (0, 0, 64.0), (3, 0, 1e6), (0, 0, 0.0)):
+        screen.configure(n_ctas, order, mflop)
+        got, _ = screen.run(seed, T)
+        np.testing.assert_array_equal(got, base)
+    screen.configure(0, 0, 0.0)
+    with pytest.raises(pmgb.PMGBError, match="no run"):
+        screen.results()  # configure discards the previous run
+    ms = screen.tune(seed, T, repeats=2)
+    assert ms > 0.0
+    got, _ = screen.run(seed, T)
+    np.testing.assert_array_equal(got, base)
+
+
+def test_batch_ragged_insertion_counts(mixed_systems):
+    npb = [1 + 97 * i for i in range(len(mixed_systems))]  # 1 insertion per block up to several units
+    screen = BatchScreen(mixed_systems, npb, 5)
+    blocks, _ = screen.run(5, T)
+    for s, gs in enumerate(mixed_systems):
+        ref, _ = gs.widom(npb[s], 5, system_seed(5, s), T)
+        np.testing.assert_array_equal(blocks[s], ref)
+
+
+@pytest.mark.parametrize("unit_mflop", [0.0, 64.0])
+def test_batch_adjoint_matches_single_system(mixed_systems, unit_mflop):
+    npb, nb, seed = 600, 5, 4321
+    screen = BatchScreen(mixed_systems, npb, nb, with_adjoint=True)
+    screen.configure(0, 0, unit_mflop)  # 64 MFLOP: several chunks per unit over a resident framework
+    assert (screen.info()["n_units"] < screen.info()["n_chunks"]) == (unit_mflop > 0)
+    blocks, adj = screen.run(seed, T)
+    for s, gs in enumerate(mixed_systems):
+        ref_b, ref_a = gs.widom_adjoint(npb, nb, system_seed(seed, s), T)
+        np.testing.assert_array_equal(blocks[s], ref_b)
+        got = henry_gradients(gs, blocks[s], adj[s], T, npb)
+        want = henry_gradients(gs, ref_b, ref_a, T, npb)
+        for g, w in zip(got[:2], want[:2]):
+            scale = max(abs(v) for v in w.values())
+            for sp in w:
+                assert g[sp] == pytest.approx(w[sp], rel=1e-9, abs=1e-12 * scale), (s, sp)
+        assert got[2] == pytest.approx(want[2], rel=1e-9, abs=1e-12 * abs(want[2]) + 1e-300)
+
+
+def test_batch_lj_members_match_oracle(mixed_systems):
+    """Block K_H of LJ members against the FP64 oracle on the same poses.
+
+    The porous frameworks (config0, the porous config1 cell) meet 1e-6 relative.  In the dense
+    random frameworks a block's Boltzmann weight can sit on one or two strongly repulsive
+    insertions; there the log-sum may differ by no more than the FP32 error bound of those
+    insertions' energies (4e-6 x the sum of |pair terms| + 1e-4 K) divided by T."""
+    ff = synthetic.forcefield()
+    porous = build_systems([synthetic.config0(), synthetic.config1_porous()], synthetic.ch4(), ff,
+                           ctx=mixed_systems[0].ctx)
+    lj_systems = porous + [gs for gs in mixed_systems if not gs.charged]
+    npb, nb, seed = 400, 5, 2024
+    screen = BatchScreen(lj_systems, npb, nb)
+    blocks, _ = screen.run(seed, T)
+    for s, gs in enumerate(lj_systems):
+        o = oracle_for(gs)
+        xf, _ = gs.ctx.sample_poses(system_seed(seed, s), 0, npb * nb)
+        v, _, _, scale, _ = o.energies(xf.astype(np.float64)[:, None, :], scales=True)  # one bead at the COM
+        ref = oracle.widom_blocks_log(v, np.zeros_like(v), T, nb, npb)
+        tol = 4e-6 * scale + 1e-4
+        for b in range(nb):
+            vb, tb = v[b * npb:(b + 1) * npb], tol[b * npb:(b + 1) * npb]
+            fin = np.isfinite(vb)
+            assert blocks[s, b, 3] == np.count_nonzero(~fin)
+            if not fin.any():
+                assert blocks[s, b, 0] == -np.inf
+                continue
+            x = -vb[fin] / T
+            p = np.exp(x - x.max())
+            bound = float(np.sum(p * tb[fin]) / np.sum(p)) / T
+            d = abs(blocks[s, b, 0] - ref[b, 0])
+            assert d <= bound + 1e-12, (s, b, d, bound)
+            if s < len(porous):
+                assert d <= 1e-6, (s, b, d)  # K_H within 1e-6 relative
+
+
+def test_screen_driver(mixed_systems):
+    res = henry_coefficient_screen(None, None, T, synthetic.forcefield(), insertions=1000, seed=8,
+                                   systems=mixed_systems, tune=False)
+    assert len(res) == len(mixed_systems)
+    for s, (r, gs) in enumerate(zip(res, mixed_systems)):
+        out = gs.widom_adjoint(200, 5, system_seed(8, s), T)[0]  # the adjoint kernel's energies
+        kh = float(np.mean(np.exp(out[:, 0] - math.log(pmgb.UNIV_GAS_CONST * T * 200))))
+        assert r["henry coefficient [mol/(m³-bar)]"] == kh
+        assert set(r["dKH/d epsilon"]) == set(gs.species)
+
+
+def test_batch_errors(mixed_systems):
+    ctx = mixed_systems[0].ctx
+    with pytest.raises(pmgb.PMGBError, match="n_per_block"):
+        BatchScreen(mixed_systems[:2], 0, 5)
+    other = pmgb.Context(0)
+    cr = synthetic.config0()
+    ff = synthetic.forcefield()
+    sc = pmgb.replicate(cr, pmgb.replication_factors(cr.box, ff))
+    foreign = pmgb.GPUSystem(sc, pmgb.Frac(synthetic.ch4(), sc.box), ff, ctx=other)
+    with pytest.raises(pmgb.PMGBError, match="another context"):
+        BatchScreen([mixed_systems[0], foreign], 10, 5, ctx=ctx)
+    screen = BatchScreen(mixed_systems[:2], 10, 5)
+    with pytest.raises(pmgb.PMGBError, match="no run"):
+        screen.results()
+    with pytest.raises(pmgb.PMGBError, match="n_ctas"):
+        screen.configure(10 ** 6, 0)
+    with pytest.raises(pmgb.PMGBError, match="unit_mflop"):
+        screen.configure(0, 0, -1.0)
+    assert ctx.device_status() == 0

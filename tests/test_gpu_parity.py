@@ -15,7 +15,7 @@ import pytest
 import oracle
 import pmgb
 from conftest import DATA
-from pm_helpers import oracle_for, oracle_sites_split, random_configs, within
+from pm_helpers import oracle_for, oracle_sites_split, random_configs, widom_with_oracle, within
 from pmgb import synthetic
 
 pytestmark = pytest.mark.gpu
@@ -205,21 +205,7 @@ def test_direct_form_cross_check(c1):
 
 # ------------------------------------------------------------------ Widom path
 def _widom_parity(gs, n_per_block, seed, T=298.0, use_sk=True):
-    blocks, u = gs.widom(n_per_block, 5, seed, T, want_energies=True)
-    ctx = gs.ctx
-    n = 5 * n_per_block
-    xf, rot = ctx.sample_poses(seed, 0, n)
-    # the device rotation is column-major R[i + 3j], the layout the oracle takes
-    body = np.zeros((gs.n_sites, 3))
-    from pmgb.molecule import body_offsets
-    ax, qx = body_offsets(gs.molecule, gs.crystal.box)
-    for k in range(gs.n_sites):
-        body[k] = ax[gs.site_atom[k]] if gs.site_atom[k] >= 0 else qx[gs.site_charge[k]]
-    o = oracle_for(gs)
-    sites = o.sites_from_poses(xf.astype(np.float64), rot.astype(np.float64), body)
-    lj, q = oracle_sites_split(gs, sites)
-    v, sr, lr = o.energies(lj, q, charged=gs.charged, use_sk=use_sk)
-    return blocks, u, v, sr + lr
+    return widom_with_oracle(gs, n_per_block, seed, T, use_sk)
 
 
 def _check_blocks(blocks, u_gpu, T, n_per_block):
