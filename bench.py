@@ -7,8 +7,10 @@ charges) replicated 2x2x3 (7,200 framework sites), 12.5 Å cutoff, Ewald precisi
 (α = 0.24713 / Å, 1,424 k-vectors), 1e6 insertions in 5 blocks at 298 K, seeded synthetic
 inputs.  A step is one Widom pass over the 1e6 insertions.
 
-  value : insertions/s of pmgb_widom_device on the resident system (CUDA events on the
-          launching stream, L2 flushed before every timed step)
+  value : insertions/s of pmgb_widom_device on the resident system with the FP64 refinement
+          of the Boltzmann tail (K_H within 1e-6 of FP64), CUDA events on the launching
+          stream, L2 flushed before every timed step; the FP32 pass alone is timed too
+          (precision.fp32_only_*) and gives the roofline's kernel time
   e2e   : insertions/s of pmgb.henry_coefficient(...) -- the reference-facing call: host
           set-up, host->device copies, S(k), the Widom launch and the device->host read
   --impl reference : the reference's algorithm on the host cores (the FP64 oracle port:
@@ -36,6 +38,10 @@ N_BLOCKS = 5
 N_INS = 1_000_000
 # algorithmic flops per pair / k-term (FMA = 2, MUFU = 1, erfc = 10): LJ 28, Ewald real 40, k-term 17
 F_LJ, F_COUL, F_K = 28, 40, 17
+REFINE_TAIL = 1e-3
+# kernels per Widom step: pairs, block reduction, and the refinement's hist, cut, count, scan,
+# scatter, FP64 energies (thread and warp passes), correction
+LAUNCHES_PER_STEP = 10
 
 
 def parse():
@@ -222,6 +228,8 @@ def batched_leg(args, ctx, stream):
     fws = synthetic.batch_frameworks(args.batch_frameworks)
     ff = synthetic.forcefield(12.5)
     systems = build_systems(fws, synthetic.ch4(), ff, ctx=ctx) + build_systems(fws, synthetic.co2(), ff, ctx=ctx)
+    for gs in systems:
+        gs.set_refine(REFINE_TAIL)  # as the drop-in calls: K_H within 1e-6 of FP64
     t_setup = time.perf_counter() - t0
     npb = max(1, args.batch_insertions // N_BLOCKS)
     n_ins = npb * N_BLOCKS * len(systems)
@@ -261,7 +269,7 @@ def batched_leg(args, ctx, stream):
         t_dropin = dropin(adjoint)
         plain(adjoint)  # warm-up: per-system scratch allocations
         t_plain = min(plain(adjoint) for _ in range(2))
-        screen = BatchScreen(systems, npb, N_BLOCKS, with_adjoint=adjoint, ctx=ctx)
+        screen = BatchScreen(systems, npb, N_BLOCKS, with_adjoint=adjoint, ctx=ctx, refine_tail=REFINE_TAIL)
         tuned_ms = screen.tune(1, T, repeats=2)
         info = screen.info()
         for w in range(args.warmup):
@@ -286,7 +294,7 @@ def batched_leg(args, ctx, stream):
                     "batched_device_ms": ms_dev, "batched_device_insertions_per_s": n_ins / (ms_dev * 1e-3),
                     "speedup_vs_plain": t_plain / t_batched, "tuned": {"n_ctas": info["n_ctas"],
                     "order": ["cost-descending", "by-system"][info["order"]], "ms": tuned_ms},
-                    "work_units": info["n_units"], "gpu_launches_per_run": 2}
+                    "work_units": info["n_units"], "gpu_launches_per_run": 10}  # batch kernel, per-system reduction, 8 refinement kernels
     assert ctx.device_status() == 0
     out.update({"systems": len(systems), "frameworks": len(fws), "guests": ["CH4", "CO2"],
                 "insertions_per_system": npb * N_BLOCKS, "insertions_per_run": n_ins,
@@ -318,7 +326,8 @@ def ours(args, rank, world, local_rank):
     stream = torch.cuda.Stream(dev)          # a real (non-legacy) stream shared with the library
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
-    system = pmgb.GPUSystem(sc, pmgb.Frac(mol, sc.box), ff, ep, ctx=ctx)
+    # FP32 pair pass + FP64 refinement of the Boltzmann tail: K_H within 1e-6 of FP64
+    system = pmgb.GPUSystem(sc, pmgb.Frac(mol, sc.box), ff, ep, ctx=ctx, refine_tail=REFINE_TAIL)
     n_ins = args.insertions
     npb = n_ins // N_BLOCKS
     n_ins = npb * N_BLOCKS
@@ -359,6 +368,20 @@ def ours(args, rank, world, local_rank):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     ms_max = float(t.item())
     value = world * n_ins * args.steps / (ms_max * 1e-3)
+
+    # the FP32 pair pass alone (pairs_kernel + block reduction): the roofline's kernel time
+    system.set_refine(0.0)
+    for w in range(2):
+        step(20_000 + w)
+    ev32 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for s_ in range(args.steps):
+        flush.zero_()
+        ev32[s_][0].record(stream)
+        step(30_000 + s_)
+        ev32[s_][1].record(stream)
+    torch.cuda.synchronize()
+    ms32 = sum(a.elapsed_time(b) for a, b in ev32) / args.steps
+    system.set_refine(REFINE_TAIL)
 
     # forward + adjoint in one pass (pmgb_widom_adjoint: energies, dK_H/d(eps, sigma, lambda))
     adj = None
@@ -406,7 +429,7 @@ def ours(args, rank, world, local_rank):
     if rank != 0:
         return
     fpi = flops_per_insertion(sc, mol, ep)
-    achieved = fpi * n_ins / (ms_total / args.steps * 1e-3) / 1e12
+    achieved = fpi * n_ins / (ms32 * 1e-3) / 1e12
     cpu = None
     if not args.skip_cpu:
         r, cores, n, dt = cpu_rate(sc, mol, ep, budget_s=15.0)
@@ -421,12 +444,20 @@ def ours(args, rank, world, local_rank):
                       "guest": "CO2 (3 LJ sites, 3 charges)", "temperature_K": T, "blocks": N_BLOCKS,
                       "l2": "flushed (256 MB write) before every timed step",
                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-           "gpu_launches": 2 * args.steps,
+           "gpu_launches": LAUNCHES_PER_STEP * args.steps,
+           "precision": {"pairs": "FP32 (compensated per-site sums)", "accumulation": "FP64 log-sum-exp",
+                         "refine_tail": REFINE_TAIL,
+                         "kh_error": "insertions carrying all but 1e-3 of each block's Boltzmann weight "
+                                     "re-evaluated in FP64 from exact positions: K_H within 1e-6 relative of "
+                                     "the FP64 oracle (tests/test_gpu_refine.py, this framework: ~5e-10)",
+                         "fp32_only_insertions_per_s": n_ins / (ms32 * 1e-3),
+                         "fp32_only_ms_per_step": ms32},
            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                         "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
                         "peak_source": "in-run FFMA probe (pmgb_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                         "flops_per_insertion": fpi,
-                        "kernel": "pairs_kernel<3,true> + reduce_blocks_kernel per step"},
+                        "kernel": "pairs_kernel<3,true,false> + reduce_blocks_kernel (FP32 pass, timed "
+                                  "without the FP64 tail refinement)"},
            "forward_plus_adjoint": adj,
            "batched": batched,
            "clocks": clk.summary(),

@@ -142,6 +142,9 @@ int pmgb_widom(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t
  * reference is FP64 throughout (src/henry.jl:212-244). */
 int pmgb_system_set_refine(pmgb_system* sys, double tail_fraction);
 
+/* Number of insertions the last refined Widom run re-evaluated in FP64 (synchronises). */
+int pmgb_system_refined_count(pmgb_system* sys, int64_t* count_out);
+
 /* Same computation on device-resident outputs, enqueued on the context stream without
  * synchronising (block_out_dev: 4*n_blocks doubles, u_out_dev optional). */
 int pmgb_widom_device(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
@@ -231,6 +234,13 @@ int pmgb_batch_configure(pmgb_batch* batch, int32_t n_ctas, int32_t order, doubl
  * fastest and returns its ms per run. */
 int pmgb_batch_tune(pmgb_batch* batch, uint64_t seed, double temperature, int32_t repeats,
                     double* best_ms_out);
+
+/* FP64 refinement of the Boltzmann tail of every system's blocks, as pmgb_system_set_refine
+ * (0: off, the default).  Allocates per-insertion scratch on first use and re-captures the graph. */
+int pmgb_batch_set_refine(pmgb_batch* batch, double tail_fraction);
+
+/* Insertions of each system the last run re-evaluated in FP64 (n_systems values; synchronises). */
+int pmgb_batch_refined_counts(pmgb_batch* batch, int64_t* per_system);
 
 /* Enqueue one run (one graph replay) on the context stream; does not synchronise. */
 int pmgb_batch_launch(pmgb_batch* batch, uint64_t seed, double temperature);

@@ -77,6 +77,7 @@ struct pmgb_system {
     int site_atom[PMGB_MAX_SITES];
     int site_charge[PMGB_MAX_SITES];
     double refine_tail = 0.0;       // FP64 refinement of the Boltzmann tail (0: off)
+    int last_refine_ctas = 0;       // chunks of the last refined run (its refined count sits after them)
     // grow-only scratch used by launches
     DevBuf r_hist, r_cut, r_counts, r_offsets, r_list, r_ref;  // refinement scratch
     DevBuf partials, block_out, in_buf, out_buf, axes;
@@ -777,11 +778,12 @@ static int run_refine(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uin
     int rc;
     if ((rc = ensure(ctx, s->r_hist, sizeof(unsigned long long) * pmgb_refine_hist_words() * n_blocks)) ||
         (rc = ensure(ctx, s->r_cut, sizeof(int) * n_blocks)) || (rc = ensure(ctx, s->r_counts, sizeof(int) * n_ctas)) ||
-        (rc = ensure(ctx, s->r_offsets, sizeof(int) * (n_ctas + 1))) ||
+        (rc = ensure(ctx, s->r_offsets, sizeof(int) * (n_ctas + 2))) ||
         (rc = ensure(ctx, s->r_list, sizeof(long long) * n)) || (rc = ensure(ctx, s->r_ref, sizeof(double) * 3 * n)))
         return rc;
     RefineArgs r{};
     r.sys = s->dev;
+    r.n_systems = 1;
     r.n_per_block = n_per_block;
     r.n_blocks = n_blocks;
     r.ctas_per_block = static_cast<int>(cpb);
@@ -796,9 +798,25 @@ static int run_refine(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uin
     r.offsets = static_cast<int*>(s->r_offsets.p);
     r.list = static_cast<long long*>(s->r_list.p);
     r.ref_u = static_cast<double*>(s->r_ref.p);
+    r.counter = static_cast<int*>(s->r_offsets.p) + n_ctas + 1;
     int n_sm = 0;
     cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device);
     PMGB_CK(ctx, pmgb_launch_refine(r, n_ctas, std::max(1, n_sm), ctx->stream));
+    s->last_refine_ctas = n_ctas;
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_system_refined_count(pmgb_system* s, int64_t* count_out) {
+    if (!s || !count_out) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    *count_out = 0;
+    if (s->last_refine_ctas <= 0) return PMGB_OK;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    int n = 0;
+    PMGB_CK(ctx, cudaMemcpyAsync(&n, static_cast<int*>(s->r_offsets.p) + s->last_refine_ctas, sizeof(int),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    *count_out = n;
     return PMGB_OK;
 }
 
@@ -1257,6 +1275,14 @@ struct pmgb_batch {
     double* d_unit_cols = nullptr;
     double* d_block_out = nullptr;
     double* d_out_cols = nullptr;
+    // FP64 tail refinement (off when refine_tail == 0)
+    double refine_tail = 0.0;
+    int* d_chunk_sys = nullptr;
+    double* d_u = nullptr;
+    unsigned long long* d_hist = nullptr;
+    int *d_cut = nullptr, *d_counts = nullptr, *d_offsets = nullptr;
+    long long* d_list = nullptr;
+    double* d_ref_u = nullptr;
     cudaGraphExec_t exec = nullptr;
     bool launched = false;
 };
@@ -1267,7 +1293,8 @@ void batch_free(pmgb_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
     void* ptrs[] = {b->d_sys, b->d_units, b->d_order, b->d_counter, b->d_run, b->d_partials,
-                    b->d_dsum, b->d_unit_cols, b->d_block_out, b->d_out_cols};
+                    b->d_dsum, b->d_unit_cols, b->d_block_out, b->d_out_cols, b->d_chunk_sys, b->d_u,
+                    b->d_hist, b->d_cut, b->d_counts, b->d_offsets, b->d_list, b->d_ref_u};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -1300,6 +1327,25 @@ int batch_capture(pmgb_batch* b) {
     a.dsum = b->d_dsum;
     a.max_cols = b->max_cols;
     a.unit_cols = b->d_unit_cols;
+    a.u = b->refine_tail > 0.0 ? b->d_u : nullptr;
+    RefineArgs r{};
+    if (b->refine_tail > 0.0) {
+        r.systems = b->d_sys;
+        r.chunk_sys = b->d_chunk_sys;
+        r.run = b->d_run;
+        r.n_systems = static_cast<int>(b->systems.size());
+        r.n_blocks = b->n_blocks;
+        r.tail = b->refine_tail;
+        r.block_out = b->d_block_out;
+        r.u = b->d_u;
+        r.hist = b->d_hist;
+        r.cut = b->d_cut;
+        r.counts = b->d_counts;
+        r.offsets = b->d_offsets;
+        r.list = b->d_list;
+        r.ref_u = b->d_ref_u;
+        r.counter = b->d_offsets + b->n_chunks + 1;
+    }
     cudaStream_t st = ctx->stream;
     PMGB_CK(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaMemsetAsync(b->d_counter, 0, sizeof(int), st);
@@ -1307,6 +1353,8 @@ int batch_capture(pmgb_batch* b) {
     if (e == cudaSuccess)
         e = pmgb_launch_batch_reduce(b->d_sys, static_cast<int>(b->systems.size()), b->n_blocks, b->d_partials,
                                      b->d_unit_cols, b->grad, b->d_block_out, b->d_out_cols, st);
+    if (e == cudaSuccess && b->refine_tail > 0.0)
+        e = pmgb_launch_refine(r, static_cast<int>(b->n_chunks), b->sm_count, st);
     cudaGraph_t g = nullptr;
     const cudaError_t e_end = cudaStreamEndCapture(st, &g);
     if (e == cudaSuccess) e = e_end;
@@ -1402,6 +1450,7 @@ extern "C" int pmgb_batch_create(pmgb_ctx* ctx, int32_t n_systems, pmgb_system* 
         bs.ctas_per_block = static_cast<int>(cpb);
         bs.col_base = col_base;
         bs.out_base = out_base;
+        bs.u_base = b->n_insertions;
         // cost model of one chunk: algorithmic flops of its pair and reciprocal-space terms
         const double pair = s->dev.charged ? 68.0 : 28.0;
         b->chunk_flops.push_back(PMGB_THREADS * nst *
@@ -1474,6 +1523,38 @@ extern "C" int pmgb_batch_configure(pmgb_batch* b, int32_t n_ctas, int32_t order
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
     b->n_ctas = n_ctas == 0 ? b->max_ctas : n_ctas;
     if (int rc = batch_build_units(b, unit_mflop, order)) return rc;
+    b->launched = false;
+    return batch_capture(b);
+}
+
+extern "C" int pmgb_batch_set_refine(pmgb_batch* b, double tail_fraction) {
+    if (!b) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = b->ctx;
+    if (!(tail_fraction >= 0.0 && tail_fraction < 1.0))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_batch_set_refine: tail fraction in [0, 1)");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (tail_fraction > 0.0 && !b->d_u) {
+        // scratch sized for the worst case: every insertion refined
+        const size_t n = static_cast<size_t>(b->n_insertions), g = b->systems.size() * b->n_blocks;
+        std::vector<int> chunk_sys(static_cast<size_t>(b->n_chunks));
+        for (size_t i = 0; i < b->host_sys.size(); ++i) {
+            const BatchSystem& bs = b->host_sys[i];
+            const int64_t n_c = static_cast<int64_t>(bs.ctas_per_block) * b->n_blocks;
+            for (int64_t c = 0; c < n_c; ++c) chunk_sys[bs.chunk_first + c] = static_cast<int>(i);
+        }
+        int rc;
+        if ((rc = batch_alloc(b, &b->d_chunk_sys, chunk_sys.size())) || (rc = batch_alloc(b, &b->d_u, 2 * n)) ||
+            (rc = batch_alloc(b, &b->d_hist, g * pmgb_refine_hist_words())) || (rc = batch_alloc(b, &b->d_cut, g)) ||
+            (rc = batch_alloc(b, &b->d_counts, chunk_sys.size())) ||
+            (rc = batch_alloc(b, &b->d_offsets, chunk_sys.size() + 2)) || (rc = batch_alloc(b, &b->d_list, n)) ||
+            (rc = batch_alloc(b, &b->d_ref_u, 3 * n)))
+            return rc;
+        PMGB_CK(ctx, cudaMemcpyAsync(b->d_chunk_sys, chunk_sys.data(), sizeof(int) * chunk_sys.size(),
+                                     cudaMemcpyHostToDevice, ctx->stream));
+        PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // chunk_sys is a local
+    }
+    b->refine_tail = tail_fraction;
     b->launched = false;
     return batch_capture(b);
 }
@@ -1559,6 +1640,24 @@ extern "C" int pmgb_batch_results(pmgb_batch* b, double* block_out, double* dthe
         d[2] = c[2];
         assemble_species(s, template_sites(s->n_sites), c + 3, d);
         d += 3 + 2 * s->n_species * s->n_species;
+    }
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_batch_refined_counts(pmgb_batch* b, int64_t* per_system) {
+    if (!b || !per_system) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = b->ctx;
+    for (size_t i = 0; i < b->systems.size(); ++i) per_system[i] = 0;
+    if (!(b->refine_tail > 0.0) || !b->launched) return PMGB_OK;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    std::vector<int> off(static_cast<size_t>(b->n_chunks) + 1);
+    PMGB_CK(ctx, cudaMemcpyAsync(off.data(), b->d_offsets, sizeof(int) * off.size(), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    for (size_t i = 0; i < b->host_sys.size(); ++i) {
+        const BatchSystem& bs = b->host_sys[i];
+        const int64_t c1 = bs.chunk_first + static_cast<int64_t>(bs.ctas_per_block) * b->n_blocks;
+        per_system[i] = off[c1] - off[bs.chunk_first];
     }
     return PMGB_OK;
 }

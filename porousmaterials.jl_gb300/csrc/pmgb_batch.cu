@@ -91,6 +91,7 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) batch_kernel(const __grid_con
             io.dsum_stride = PMGB_THREADS;
             io.col_item = tid;
             io.partial = b.partials + slot;
+            io.u_out = b.u ? b.u + 2 * s_bs.u_base : nullptr;
             io.resident = fits && c > 0;
             double x = -inf;
             io.x_out = &x;

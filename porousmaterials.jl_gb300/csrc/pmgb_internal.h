@@ -158,6 +158,7 @@ struct BatchSystem {
     int ctas_per_block;   // chunks per insertion block
     long long col_base;   // adjoint: first of this system's chunk column partials (n_cols per chunk)
     long long out_base;   // adjoint: first of this system's 3 + n_cols combined outputs
+    long long u_base;     // first of this system's insertions in the batch's per-insertion energies
 };
 struct BatchUnit {
     int system, block, chunk0, n_chunks;
@@ -179,24 +180,30 @@ struct BatchArgs {
     float* dsum;              // per-CTA column scratch: [gridDim.x][max_cols][PMGB_THREADS]
     int max_cols;
     double* unit_cols;        // per-chunk weighted column sums, weights exp(-U/T - m_chunk)
+    double* u;                // optional: per-insertion (U_vdw, U_es), system s at 2 * u_base
 };
 
 // ---- FP64 refinement of the Boltzmann tail (pmgb_refine.cu) ---------------------------
 struct RefineArgs {
-    SysDev sys;
-    long long n_per_block;
+    SysDev sys;                     // single-system mode
+    const BatchSystem* systems;     // batch mode when non-null: chunk c belongs to system chunk_sys[c]
+    const int* chunk_sys;
+    const BatchRun* run;            // batch mode: seed and 1/T (device memory, for graph replays)
+    int n_systems;                  // 1 in single-system mode
+    long long n_per_block;          // single-system mode (batch: per system)
     int n_blocks, ctas_per_block;   // insertion i of block b: b * n_per_block + i; 256 per chunk
     unsigned long long seed;
     double inv_temperature;
     double tail;                    // weight fraction left unrefined per block (at most)
-    double* block_out;              // [4 n_blocks] FP32-pass results, corrected in place
+    double* block_out;              // [4 n_systems n_blocks] FP32-pass results, corrected in place
     double* u;                      // [2 n] per-insertion (U_vdw, U_es); refined entries replaced
-    unsigned long long* hist;       // [n_blocks * pmgb_refine_hist_words()]
-    int* cut;                       // [n_blocks]
-    int* counts;                    // [n_blocks * ctas_per_block]
-    int* offsets;                   // [n_blocks * ctas_per_block + 1]
-    long long* list;                // [n] refined insertions, index order
+    unsigned long long* hist;       // [n_systems * n_blocks * pmgb_refine_hist_words()]
+    int* cut;                       // [n_systems * n_blocks]
+    int* counts;                    // [chunks]
+    int* offsets;                   // [chunks + 1]
+    long long* list;                // [n] refined insertions (system << 40 | insertion), index order
     double* ref_u;                  // [3 n] their FP64 (U_vdw, U_sr, U_lr)
+    int* counter;                   // [1] work counter of the warp-per-insertion pass
 };
 cudaError_t pmgb_launch_refine(const RefineArgs& a, int n_ctas, int n_sm, cudaStream_t st);
 size_t pmgb_refine_hist_words();

@@ -9,7 +9,7 @@
 //      gap L_b - x_i, in integer fixed point (order-independent, so deterministic);
 //   2. per block, the smallest gap cut that leaves at most `tail` of the weight above it;
 //   3. stable compaction of the selected insertions (count, scan, scatter in index order);
-//   4. FP64 energies of each selected insertion, one CTA each: LJ with the reference's strict
+//   4. FP64 energies of each selected insertion, one warp each: LJ with the reference's strict
 //      cutoff and overlap rule, real-space q erfc(alpha r)/r, and the reciprocal-space sum
 //      against the FP64 S(k) with exact fixed-point phases;
 //   5. per block, the FP64 minus FP32 differences of e^{x}, U_vdw e^{x} and U_es e^{x}, added
@@ -24,17 +24,46 @@ constexpr int kBins = 256;             // histogram bins of the gap L - x
 constexpr double kBinWidth = 0.25;     // in units of kT: the histogram spans 64 kT
 constexpr double kWeightScale = 1099511627776.0;  // 2^40: fixed-point weight (weights sum to 1)
 
-__device__ __forceinline__ bool tail_item(const RefineArgs& a, int cta, int tid, long long& item, int& blk) {
-    blk = cta / a.ctas_per_block;
-    const long long within = static_cast<long long>(cta % a.ctas_per_block) * PMGB_THREADS + tid;
-    item = static_cast<long long>(blk) * a.n_per_block + within;
-    return within < a.n_per_block;
+// Where thread `tid` of chunk `cta` sits: its system, statistics block (global index over
+// systems x blocks), insertion index within the system and slot in the energy array u.
+struct TailRef {
+    int sys, gblk;
+    long long item, ui;
+    bool valid;
+};
+
+__device__ __forceinline__ TailRef tail_locate(const RefineArgs& a, int cta, int tid) {
+    TailRef t;
+    if (a.systems) {
+        t.sys = a.chunk_sys[cta];
+        const BatchSystem& bs = a.systems[t.sys];
+        const int local = cta - bs.chunk_first;
+        const int blk = local / bs.ctas_per_block;
+        const long long within = static_cast<long long>(local % bs.ctas_per_block) * PMGB_THREADS + tid;
+        t.valid = within < bs.n_per_block;
+        t.item = static_cast<long long>(blk) * bs.n_per_block + within;
+        t.gblk = t.sys * a.n_blocks + blk;
+        t.ui = bs.u_base + t.item;
+    } else {
+        t.sys = 0;
+        const int blk = cta / a.ctas_per_block;
+        const long long within = static_cast<long long>(cta % a.ctas_per_block) * PMGB_THREADS + tid;
+        t.valid = within < a.n_per_block;
+        t.item = static_cast<long long>(blk) * a.n_per_block + within;
+        t.gblk = blk;
+        t.ui = t.item;
+    }
+    return t;
 }
 
-// bin of insertion `item` (-1: not eligible: infinite energy or empty block)
-__device__ __forceinline__ int tail_bin(const RefineArgs& a, long long item, int blk, double* w_out) {
-    const double L = a.block_out[4 * blk];
-    const double x = -(a.u[2 * item] + a.u[2 * item + 1]) * a.inv_temperature;
+__device__ __forceinline__ double inv_temp(const RefineArgs& a) {
+    return a.run ? a.run->inv_temperature : a.inv_temperature;
+}
+
+// bin of an insertion (-1: not eligible: infinite energy or empty block)
+__device__ __forceinline__ int tail_bin(const RefineArgs& a, const TailRef& t, double* w_out) {
+    const double L = a.block_out[4 * t.gblk];
+    const double x = -(a.u[2 * t.ui] + a.u[2 * t.ui + 1]) * inv_temp(a);
     if (!isfinite(x) || !isfinite(L)) return -1;
     const double g = fmax(L - x, 0.0);
     if (w_out) *w_out = exp(-g);
@@ -45,26 +74,24 @@ __global__ void tail_hist_kernel(const __grid_constant__ RefineArgs a) {
     __shared__ unsigned long long sh[kBins];
     for (int i = threadIdx.x; i < kBins; i += blockDim.x) sh[i] = 0ull;
     __syncthreads();
-    long long item;
-    int blk;
-    if (tail_item(a, blockIdx.x, threadIdx.x, item, blk)) {
+    const TailRef t = tail_locate(a, blockIdx.x, threadIdx.x);  // one (system, block) per chunk
+    if (t.valid) {
         double w = 0.0;
-        const int bin = tail_bin(a, item, blk, &w);
+        const int bin = tail_bin(a, t, &w);
         // rounded up: the tail weight is never under-estimated
         const unsigned long long q = (bin >= 0) ? static_cast<unsigned long long>(ceil(w * kWeightScale)) : 0ull;
         if (q) atomicAdd(&sh[bin], q);
     }
     __syncthreads();
-    const int b = blockIdx.x / a.ctas_per_block;
     for (int i = threadIdx.x; i < kBins; i += blockDim.x)
-        if (sh[i]) atomicAdd(&a.hist[static_cast<size_t>(b) * kBins + i], sh[i]);
+        if (sh[i]) atomicAdd(&a.hist[static_cast<size_t>(t.gblk) * kBins + i], sh[i]);
 }
 
-// cut[b] = number of leading bins to refine: the bins from cut[b] on hold at most tail x total
+// cut[g] = number of leading bins to refine: the bins from cut[g] on hold at most tail x total
 __global__ void tail_cut_kernel(const __grid_constant__ RefineArgs a) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= a.n_blocks) return;
-    const unsigned long long* h = a.hist + static_cast<size_t>(b) * kBins;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= a.n_systems * a.n_blocks) return;
+    const unsigned long long* h = a.hist + static_cast<size_t>(g) * kBins;
     double total = 0.0;
     for (int i = 0; i < kBins; ++i) total += static_cast<double>(h[i]);
     const double allowed = a.tail * total;
@@ -74,19 +101,18 @@ __global__ void tail_cut_kernel(const __grid_constant__ RefineArgs a) {
         above += static_cast<double>(h[cut - 1]);
         --cut;
     }
-    a.cut[b] = cut;
+    a.cut[g] = cut;
 }
 
-__device__ __forceinline__ bool selected(const RefineArgs& a, int cta, int tid, long long& item) {
-    int blk;
-    if (!tail_item(a, cta, tid, item, blk)) return false;
-    const int bin = tail_bin(a, item, blk, nullptr);
-    return bin >= 0 && bin < a.cut[blk];
+__device__ __forceinline__ bool selected(const RefineArgs& a, const TailRef& t) {
+    if (!t.valid) return false;
+    const int bin = tail_bin(a, t, nullptr);
+    return bin >= 0 && bin < a.cut[t.gblk];
 }
 
 __global__ void tail_count_kernel(const __grid_constant__ RefineArgs a) {
-    long long item;
-    const int c = __syncthreads_count(selected(a, blockIdx.x, threadIdx.x, item) ? 1 : 0);
+    const TailRef t = tail_locate(a, blockIdx.x, threadIdx.x);
+    const int c = __syncthreads_count(selected(a, t) ? 1 : 0);
     if (threadIdx.x == 0) a.counts[blockIdx.x] = c;
 }
 
@@ -112,13 +138,16 @@ __global__ void tail_scan_kernel(const __grid_constant__ RefineArgs a, int n_cta
         if (threadIdx.x == blockDim.x - 1) carry += sh[threadIdx.x];
         __syncthreads();
     }
-    if (threadIdx.x == 0) a.offsets[n_ctas] = carry;
+    if (threadIdx.x == 0) {
+        a.offsets[n_ctas] = carry;
+        *a.counter = 0;  // work counter of refine_large_kernel
+    }
 }
 
 __global__ void tail_scatter_kernel(const __grid_constant__ RefineArgs a) {
     __shared__ int warp_base[PMGB_THREADS / 32];
-    long long item;
-    const bool sel = selected(a, blockIdx.x, threadIdx.x, item);
+    const TailRef t = tail_locate(a, blockIdx.x, threadIdx.x);
+    const bool sel = selected(a, t);
     const unsigned ballot = __ballot_sync(0xffffffffu, sel);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0) warp_base[warp] = __popc(ballot);
@@ -132,136 +161,219 @@ __global__ void tail_scatter_kernel(const __grid_constant__ RefineArgs a) {
         }
     }
     __syncthreads();
-    if (sel) a.list[warp_base[warp] + __popc(ballot & ((1u << lane) - 1u))] = item;
+    if (sel)
+        a.list[warp_base[warp] + __popc(ballot & ((1u << lane) - 1u))] =
+            (static_cast<long long>(t.sys) << 40) | t.item;
 }
 
-// FP64 energies (U_vdw, U_sr, U_lr) of one insertion whose guest sites are at the FP64
-// fractional coordinates xs[k][3], evaluated by the whole CTA from the exact FP64 framework
-// coordinates (nearest image by rounding each fractional difference, as Xtals' nearest_image!).
-__device__ void energy_fp64(const SysDev& S, const double (*xs)[3], double* out3) {
-    __shared__ double red[3][PMGB_THREADS / 32];
-    __shared__ int red_ovl;
-    const int tid = threadIdx.x;
-    if (tid == 0) red_ovl = 0;
+// 1/x in FP64 from the FP32 hardware estimate and two Newton steps y <- y + y (1 - x y)
+// (quadratic convergence: ~1e-7 -> ~1e-14 -> last-bit accuracy), for x > 0 in FP32 range.
+__device__ __forceinline__ double rcp64(double x) {
+    double y = static_cast<double>(__frcp_rn(static_cast<float>(x)));
+    y = fma(y, fma(-x, y, 1.0), y);
+    y = fma(y, fma(-x, y, 1.0), y);
+    return y;
+}
+
+// Pair terms of one (record, guest site) in FP64: LJ (strict cutoff, overlap flag) and the
+// unscaled real-space Coulomb term q_k q_j erfc(alpha r) / r.
+__device__ __forceinline__ void pair_fp64(const SysDev& S, int sg, int k, double rx, double ry, double rz, double qj,
+                                          const double* x, double& v, double& sr, bool& ovl) {
+    double fx = rx - x[0], fy = ry - x[1], fz = rz - x[2];
+    fx -= rint(fx);  // nearest image, one shift per axis (Xtals nearest_image!)
+    fy -= rint(fy);
+    fz -= rint(fz);
+    const double cx = S.f2c64[0] * fx + S.f2c64[1] * fy + S.f2c64[2] * fz;
+    const double cy = S.f2c64[3] * fy + S.f2c64[4] * fz;
+    const double cz = S.f2c64[5] * fz;
+    const double r2 = cx * cx + cy * cy + cz * cz;
+    const double2 p = S.segpar64[sg * PMGB_MAX_SITES + k];  // (sigma^2, 4 eps); sigma^2 < 0: no LJ
+    if (p.x >= 0.0) {
+        if (r2 < 0.1) {
+            ovl = true;  // R²_OVERLAP, src/vdw_energetics.jl:2,36-37
+        } else if (r2 < S.rc2_64) {
+            const double t = p.x * rcp64(r2);
+            const double t3 = t * t * t;
+            v += p.y * (t3 * t3 - t3);
+        }
+    }
+    if (S.charged && qj != 0.0 && S.q64[k] != 0.0 && r2 < S.rc2e_64 && r2 > 0.0) {
+        const double rr = sqrt(r2);
+        sr += S.q64[k] * qj * erfc(S.alpha64 * rr) * rcp64(rr);
+    }
+}
+
+// Reciprocal-space energy of guest site k over the half-rows [row0, row_end) stepping by
+// row_step: Sum_k wt Re[S(k) e^{-ik.x}], the phasor carried along kc by an FP64 recurrence
+// from one sincospi per row (rows hold at most a few dozen k-vectors).
+__device__ __forceinline__ double kspace_fp64(const SysDev& S, const double* x, int row0, int row_step) {
+    double lr = 0.0;
+    double wr, wi;  // e^{-2 pi i x_c}: one step along +kc
+    sincospi(-2.0 * x[2], &wi, &wr);
+    for (int row = row0; row < S.n_krow; row += row_step) {
+        const KRow R = S.krow[row];
+        double er, ei;  // e^{-ik.x} at the row start
+        sincospi(-2.0 * (R.ka * x[0] + R.kb * x[1] + R.kc0 * x[2]), &ei, &er);
+        const double swi = R.dir * wi;  // downward rows step by the conjugate
+        const double* sk = S.sk64 + 2 * R.off;
+        const double* wt = S.wt64 + R.off;
+        for (int m = 0; m < R.n; ++m) {
+            lr = fma(wt[m], fma(sk[2 * m], er, -sk[2 * m + 1] * ei), lr);  // Re[S e] with e = er + i ei
+            const double nr = fma(er, wr, -ei * swi);
+            ei = fma(er, swi, ei * wr);
+            er = nr;
+        }
+    }
+    return lr;
+}
+
+// FP64 energies of one insertion (guest sites at FP64 fractional coordinates xs), evaluated
+// by one thread.
+__device__ void energy_fp64_thread(const SysDev& S, const double (*xs)[3], double* out3) {
     const int ns = S.n_sites;
     double v = 0.0, sr = 0.0, lr = 0.0;
-    int ovl = 0;
+    bool ovl = false;
     for (int sg = 0; sg < S.n_seg; ++sg) {
         const SegDesc d = S.seg[sg];
-        for (int j = d.lo + tid; j < d.hi; j += blockDim.x) {
+        for (int j = d.lo; j < d.hi; ++j) {
             const double qj = S.rec_q[j];
             const double rx = S.rec_xf[3 * j], ry = S.rec_xf[3 * j + 1], rz = S.rec_xf[3 * j + 2];
-            for (int k = 0; k < ns; ++k) {
-                double fx = rx - xs[k][0], fy = ry - xs[k][1], fz = rz - xs[k][2];
-                fx -= rint(fx);
-                fy -= rint(fy);
-                fz -= rint(fz);
-                const double cx = S.f2c64[0] * fx + S.f2c64[1] * fy + S.f2c64[2] * fz;
-                const double cy = S.f2c64[3] * fy + S.f2c64[4] * fz;
-                const double cz = S.f2c64[5] * fz;
-                const double r2 = cx * cx + cy * cy + cz * cz;
-                const double2 p = S.segpar64[sg * PMGB_MAX_SITES + k];  // (sigma^2, 4 eps); sigma^2 < 0: no LJ
-                if (p.x >= 0.0) {
-                    if (r2 < 0.1) {
-                        ovl = 1;  // R²_OVERLAP, src/vdw_energetics.jl:2,36-37
-                    } else if (r2 < S.rc2_64) {
-                        const double t = p.x / r2;
-                        const double t3 = t * t * t;
-                        v += p.y * (t3 * t3 - t3);
-                    }
-                }
-                if (S.charged && qj != 0.0 && S.q64[k] != 0.0 && r2 < S.rc2e_64) {
-                    const double rr = sqrt(r2);
-                    sr += S.q64[k] * qj * erfc(S.alpha64 * rr) / rr;
-                }
-            }
+            for (int k = 0; k < ns; ++k) pair_fp64(S, sg, k, rx, ry, rz, qj, xs[k], v, sr, ovl);
         }
     }
-    if (S.charged) {
-        for (int kk = tid; kk < S.n_k; kk += blockDim.x) {
-            const double ka = S.kabc[3 * kk], kb = S.kabc[3 * kk + 1], kc = S.kabc[3 * kk + 2];
-            const double sre = S.sk64[2 * kk], sim = S.sk64[2 * kk + 1], wt = S.wt64[kk];
-            for (int k = 0; k < ns; ++k) {
-                if (S.q64[k] == 0.0) continue;
-                const double t = ka * xs[k][0] + kb * xs[k][1] + kc * xs[k][2];  // k.x in turns
-                double sn, cs;
-                sincospi(2.0 * t, &sn, &cs);
-                lr += S.q64[k] * wt * (sre * cs + sim * sn);  // Re[S(k) e^{-ik.x}]
-            }
+    if (S.charged)
+        for (int k = 0; k < ns; ++k)
+            if (S.q64[k] != 0.0) lr += S.q64[k] * kspace_fp64(S, xs[k], 0, 1);
+    out3[0] = ovl ? __longlong_as_double(0x7ff0000000000000ll) : v;
+    out3[1] = sr * S.coul;
+    out3[2] = lr;
+}
+
+// The same, evaluated by one warp: lanes stride over records and k-space rows; the reduction
+// is a fixed shuffle tree, so the result does not depend on scheduling.
+__device__ void energy_fp64_warp(const SysDev& S, const double (*xs)[3], double* out3) {
+    const int lane = threadIdx.x & 31;
+    const int ns = S.n_sites;
+    double v = 0.0, sr = 0.0, lr = 0.0;
+    bool ovl = false;
+    for (int sg = 0; sg < S.n_seg; ++sg) {
+        const SegDesc d = S.seg[sg];
+        for (int j = d.lo + lane; j < d.hi; j += 32) {
+            const double qj = S.rec_q[j];
+            const double rx = S.rec_xf[3 * j], ry = S.rec_xf[3 * j + 1], rz = S.rec_xf[3 * j + 2];
+            for (int k = 0; k < ns; ++k) pair_fp64(S, sg, k, rx, ry, rz, qj, xs[k], v, sr, ovl);
         }
     }
-    // CTA reduction in a fixed order
+    if (S.charged)
+        for (int k = 0; k < ns; ++k)
+            if (S.q64[k] != 0.0) lr += S.q64[k] * kspace_fp64(S, xs[k], lane, 32);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         v += __shfl_xor_sync(0xffffffffu, v, o);
         sr += __shfl_xor_sync(0xffffffffu, sr, o);
         lr += __shfl_xor_sync(0xffffffffu, lr, o);
     }
-    const int warp = tid >> 5, lane = tid & 31;
-    __syncthreads();  // red_ovl initialised
-    if (ovl) atomicOr(&red_ovl, 1);
+    ovl = __any_sync(0xffffffffu, ovl);
     if (lane == 0) {
-        red[0][warp] = v;
-        red[1][warp] = sr;
-        red[2][warp] = lr;
+        out3[0] = ovl ? __longlong_as_double(0x7ff0000000000000ll) : v;
+        out3[1] = sr * S.coul;
+        out3[2] = lr;
     }
-    __syncthreads();
-    if (tid == 0) {
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) {
-            a0 += red[0][w];
-            a1 += red[1][w];
-            a2 += red[2][w];
-        }
-        out3[0] = red_ovl ? __longlong_as_double(0x7ff0000000000000ll) : a0;
-        out3[1] = a1 * S.coul;
-        out3[2] = a2;
-    }
-    __syncthreads();  // red and red_ovl are reused by the next call
 }
 
-__global__ void __launch_bounds__(PMGB_THREADS) refine_kernel(const __grid_constant__ RefineArgs a, int n_ctas) {
+// FP64 work of one insertion (pair terms + reciprocal-space terms): small ones are evaluated
+// by one thread each, the others by a whole warp
+__device__ __forceinline__ bool small_system(const SysDev& S) {
+    return static_cast<long long>(S.n_sites) * (S.n_rec + (S.charged ? S.n_k : 0)) <= 512;
+}
+
+__device__ __forceinline__ void refined_entry(const RefineArgs& a, long long e, const SysDev*& S, double (*xs)[3]) {
+    const int sys = static_cast<int>(e >> 40);
+    const long long item = e & ((1ll << 40) - 1);
+    S = a.systems ? &a.systems[sys].sys : &a.sys;
+    const unsigned long long seed =
+        a.run ? a.run->seed + static_cast<unsigned long long>(sys) * 0x9E3779B97F4A7C15ull : a.seed;
+    // the insertion's pose applied to the FP64 site offsets, kept in FP64 (no fixed point)
+    float xf[3], R[9];
+    make_pose(seed, static_cast<unsigned long long>(item), xf, R);
+    for (int k = 0; k < S->n_sites; ++k) {
+        const double bx = S->body64[k][0], by = S->body64[k][1], bz = S->body64[k][2];
+        const double ox = static_cast<double>(R[0]) * bx + static_cast<double>(R[3]) * by + static_cast<double>(R[6]) * bz;
+        const double oy = static_cast<double>(R[1]) * bx + static_cast<double>(R[4]) * by + static_cast<double>(R[7]) * bz;
+        const double oz = static_cast<double>(R[2]) * bx + static_cast<double>(R[5]) * by + static_cast<double>(R[8]) * bz;
+        xs[k][0] = static_cast<double>(xf[0]) + (S->g64[0] * ox + S->g64[1] * oy + S->g64[2] * oz);
+        xs[k][1] = static_cast<double>(xf[1]) + (S->g64[3] * oy + S->g64[4] * oz);
+        xs[k][2] = static_cast<double>(xf[2]) + S->g64[5] * oz;
+    }
+}
+
+__device__ __forceinline__ const SysDev& entry_system(const RefineArgs& a, long long e) {
+    return a.systems ? a.systems[static_cast<int>(e >> 40)].sys : a.sys;
+}
+
+// Entries of small systems: one thread each (grid-stride).
+__global__ void __launch_bounds__(PMGB_THREADS) refine_small_kernel(const __grid_constant__ RefineArgs a, int n_ctas) {
     const int n_ref = a.offsets[n_ctas];
-    for (int r = blockIdx.x; r < n_ref; r += gridDim.x) {
-        const long long item = a.list[r];
-        // the insertion's pose applied to the FP64 site offsets, kept in FP64 (no fixed point)
-        float xf[3], R[9];
-        make_pose(a.seed, static_cast<unsigned long long>(item), xf, R);
-        __shared__ double xs[PMGB_MAX_SITES][3];
-        if (threadIdx.x < PMGB_MAX_SITES) {
-            const SysDev& S = a.sys;
-            const int k = threadIdx.x;
-            const double bx = S.body64[k][0], by = S.body64[k][1], bz = S.body64[k][2];
-            const double ox = static_cast<double>(R[0]) * bx + static_cast<double>(R[3]) * by + static_cast<double>(R[6]) * bz;
-            const double oy = static_cast<double>(R[1]) * bx + static_cast<double>(R[4]) * by + static_cast<double>(R[7]) * bz;
-            const double oz = static_cast<double>(R[2]) * bx + static_cast<double>(R[5]) * by + static_cast<double>(R[8]) * bz;
-            xs[k][0] = static_cast<double>(xf[0]) + (S.g64[0] * ox + S.g64[1] * oy + S.g64[2] * oz);
-            xs[k][1] = static_cast<double>(xf[1]) + (S.g64[3] * oy + S.g64[4] * oz);
-            xs[k][2] = static_cast<double>(xf[2]) + S.g64[5] * oz;
-        }
-        __syncthreads();
-        energy_fp64(a.sys, xs, a.ref_u + 3 * static_cast<size_t>(r));  // ends with a barrier
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_ref; r += gridDim.x * blockDim.x) {
+        const long long e = a.list[r];
+        if (!small_system(entry_system(a, e))) continue;
+        const SysDev* S;
+        double xs[PMGB_MAX_SITES][3];
+        refined_entry(a, e, S, xs);
+        energy_fp64_thread(*S, xs, a.ref_u + 3 * static_cast<size_t>(r));
     }
 }
 
-// Per block: add the FP64 - FP32 differences of the refined insertions (index order) to the
-// block results and store the refined energies in u.
+// Entries of the other systems: one warp each, taken from a work counter so that the long
+// evaluations spread over every SM.  Which path an entry takes depends only on its system,
+// so results are reproducible.
+__global__ void __launch_bounds__(PMGB_THREADS) refine_large_kernel(const __grid_constant__ RefineArgs a, int n_ctas) {
+    const int n_ref = a.offsets[n_ctas];
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int r = 0;
+        if (lane == 0) r = atomicAdd(a.counter, 1);
+        r = __shfl_sync(0xffffffffu, r, 0);
+        if (r >= n_ref) break;
+        const long long e = a.list[r];
+        if (small_system(entry_system(a, e))) continue;
+        const SysDev* S;
+        double xs[PMGB_MAX_SITES][3];
+        refined_entry(a, e, S, xs);
+        energy_fp64_warp(*S, xs, a.ref_u + 3 * static_cast<size_t>(r));
+    }
+}
+
+// Per (system, block): add the FP64 - FP32 differences of the refined insertions (index order)
+// to the block results and store the refined energies in u.
 __global__ void tail_correct_kernel(const __grid_constant__ RefineArgs a) {
-    const int b = blockIdx.x;
+    const int g = blockIdx.x;
     const int lane = threadIdx.x;
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
-    const int r0 = a.offsets[b * a.ctas_per_block], r1 = a.offsets[(b + 1) * a.ctas_per_block];
-    double* bo = a.block_out + 4 * b;
+    const double inv_t = inv_temp(a);
+    int c0, cpb;
+    long long u_base = 0;
+    if (a.systems) {
+        const BatchSystem& bs = a.systems[g / a.n_blocks];
+        cpb = bs.ctas_per_block;
+        c0 = bs.chunk_first + (g % a.n_blocks) * cpb;
+        u_base = bs.u_base;
+    } else {
+        cpb = a.ctas_per_block;
+        c0 = g * cpb;
+    }
+    const int r0 = a.offsets[c0], r1 = a.offsets[c0 + cpb];
+    double* bo = a.block_out + 4 * g;
     const double L = bo[0];
     double ds = 0.0, dv = 0.0, de = 0.0;
     long long dn = 0;
     for (int r = r0 + lane; r < r1; r += 32) {
-        const long long item = a.list[r];
-        const double uv32 = a.u[2 * item], ue32 = a.u[2 * item + 1];
+        const long long ui = u_base + (a.list[r] & ((1ll << 40) - 1));
+        const double uv32 = a.u[2 * ui], ue32 = a.u[2 * ui + 1];
         const double* f = a.ref_u + 3 * static_cast<size_t>(r);
         const double uv64 = f[0], ue64 = f[1] + f[2];
-        const double x32 = -(uv32 + ue32) * a.inv_temperature;
-        const double x64 = -(uv64 + ue64) * a.inv_temperature;
+        const double x32 = -(uv32 + ue32) * inv_t;
+        const double x64 = -(uv64 + ue64) * inv_t;
         const double w32 = exp(x32 - L);
         if (isfinite(x64)) {
             const double w64 = w32 * exp(x64 - x32);
@@ -274,8 +386,8 @@ __global__ void tail_correct_kernel(const __grid_constant__ RefineArgs a) {
             de -= ue32 * w32;
             dn += 1;
         }
-        a.u[2 * item] = uv64;
-        a.u[2 * item + 1] = ue64;
+        a.u[2 * ui] = uv64;
+        a.u[2 * ui + 1] = ue64;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -306,15 +418,17 @@ __global__ void tail_correct_kernel(const __grid_constant__ RefineArgs a) {
 
 cudaError_t pmgb_launch_refine(const RefineArgs& a, int n_ctas, int n_sm, cudaStream_t st) {
     if (n_ctas <= 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(a.hist, 0, sizeof(unsigned long long) * kBins * a.n_blocks, st);
+    const int n_g = a.n_systems * a.n_blocks;
+    cudaError_t e = cudaMemsetAsync(a.hist, 0, sizeof(unsigned long long) * kBins * n_g, st);
     if (e != cudaSuccess) return e;
     tail_hist_kernel<<<n_ctas, PMGB_THREADS, 0, st>>>(a);
-    tail_cut_kernel<<<(a.n_blocks + 31) / 32, 32, 0, st>>>(a);
+    tail_cut_kernel<<<(n_g + 127) / 128, 128, 0, st>>>(a);
     tail_count_kernel<<<n_ctas, PMGB_THREADS, 0, st>>>(a);
     tail_scan_kernel<<<1, 1024, 0, st>>>(a, n_ctas);
     tail_scatter_kernel<<<n_ctas, PMGB_THREADS, 0, st>>>(a);
-    refine_kernel<<<4 * n_sm, PMGB_THREADS, 0, st>>>(a, n_ctas);
-    tail_correct_kernel<<<a.n_blocks, 32, 0, st>>>(a);
+    refine_small_kernel<<<4 * n_sm, PMGB_THREADS, 0, st>>>(a, n_ctas);
+    refine_large_kernel<<<4 * n_sm, PMGB_THREADS, 0, st>>>(a, n_ctas);
+    tail_correct_kernel<<<n_g, 32, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -48,6 +48,7 @@ SIGNATURES = [
     ("pmgb_structure_factor", C.c_int, [_vp, _dp]),
     ("pmgb_energies", C.c_int, [_vp, C.c_int64, _dp, _dp]),
     ("pmgb_system_set_refine", C.c_int, [_vp, C.c_double]),
+    ("pmgb_system_refined_count", C.c_int, [_vp, C.POINTER(C.c_int64)]),
     ("pmgb_widom", C.c_int, [_vp, C.c_int64, C.c_int32, C.c_uint64, C.c_double, _dp, _dp]),
     ("pmgb_widom_device", C.c_int, [_vp, C.c_int64, C.c_int32, C.c_uint64, C.c_double, _vp, _vp]),
     ("pmgb_widom_noalloc", C.c_int, [_vp, C.c_int64, C.c_int32, C.c_uint64, C.c_double, _vp, _vp]),
@@ -62,6 +63,8 @@ SIGNATURES = [
     ("pmgb_batch_destroy", None, [_vp]),
     ("pmgb_batch_configure", C.c_int, [_vp, C.c_int32, C.c_int32, C.c_double]),
     ("pmgb_batch_tune", C.c_int, [_vp, C.c_uint64, C.c_double, C.c_int32, _dp]),
+    ("pmgb_batch_set_refine", C.c_int, [_vp, C.c_double]),
+    ("pmgb_batch_refined_counts", C.c_int, [_vp, C.POINTER(C.c_int64)]),
     ("pmgb_batch_launch", C.c_int, [_vp, C.c_uint64, C.c_double]),
     ("pmgb_batch_results", C.c_int, [_vp, _dp, _dp]),
     ("pmgb_batch_info", C.c_int, [_vp, C.POINTER(C.c_int64)]),

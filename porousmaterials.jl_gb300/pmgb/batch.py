@@ -37,7 +37,7 @@ class BatchScreen:
     """pmgb_batch handle over a list of GPUSystems (kept alive by this object)."""
 
     def __init__(self, systems: list[GPUSystem], n_per_block, n_blocks: int = 5, with_adjoint: bool = False,
-                 ctx: Context | None = None):
+                 ctx: Context | None = None, refine_tail: float = 0.0):
         if not systems:
             raise ValueError("BatchScreen needs at least one system")
         self.ctx = ctx or systems[0].ctx
@@ -53,6 +53,14 @@ class BatchScreen:
                                                        self.n_blocks, int(self.with_adjoint), C.byref(h)))
         self.handle = h.value
         self._n_species = [len(s.species) for s in systems]
+        self.refine_tail = 0.0
+        if refine_tail:
+            self.set_refine(refine_tail)
+
+    def set_refine(self, tail_fraction: float) -> None:
+        """FP64 refinement of the Boltzmann tail of every system (see pmgb_batch_set_refine)."""
+        self.ctx.check(self.ctx._lib.pmgb_batch_set_refine(self.handle, float(tail_fraction)))
+        self.refine_tail = float(tail_fraction)
 
     def close(self):
         if getattr(self, "handle", None):
@@ -77,6 +85,12 @@ class BatchScreen:
         self.ctx.check(self.ctx._lib.pmgb_batch_tune(self.handle, int(seed) % (1 << 64), float(temperature),
                                                      int(repeats), C.byref(ms)))
         return ms.value
+
+    def refined_counts(self) -> np.ndarray:
+        """Insertions of each system the last run re-evaluated in FP64."""
+        out = np.zeros(len(self.systems), dtype=np.int64)
+        self.ctx.check(self.ctx._lib.pmgb_batch_refined_counts(self.handle, out.ctypes.data_as(C.POINTER(C.c_int64))))
+        return out
 
     def launch(self, seed: int, temperature: float):
         """Enqueue one run on the context stream (asynchronous)."""
@@ -121,7 +135,8 @@ def build_systems(crystals: list[Crystal], molecule: Molecule | list[Molecule], 
 def henry_coefficient_screen(crystals: list[Crystal], molecule: Molecule | list[Molecule], temperature: float,
                              ljforcefield: LJForceField, *, insertions: int = 20000, n_blocks: int = 5,
                              seed: int = 0, with_gradient: bool = True, ewald_precision: float = 1e-6,
-                             tune: bool = True, systems: list[GPUSystem] | None = None) -> list[dict]:
+                             tune: bool = True, systems: list[GPUSystem] | None = None,
+                             refine_tail: float = 1e-3) -> list[dict]:
     """K_H (mol/(m³ bar), block mean as henry_coefficient) of every crystal, and with_gradient the
     derivatives of henry_coefficient_gradient, from one batched run."""
     from .adjoint import henry_gradients
@@ -131,7 +146,7 @@ def henry_coefficient_screen(crystals: list[Crystal], molecule: Molecule | list[
     if systems is None:
         systems = build_systems(crystals, molecule, ljforcefield, ewald_precision=ewald_precision)
     npb = max(1, math.ceil(insertions / n_blocks))
-    screen = BatchScreen(systems, npb, n_blocks, with_adjoint=with_gradient)
+    screen = BatchScreen(systems, npb, n_blocks, with_adjoint=with_gradient, refine_tail=refine_tail)
     if tune:
         screen.tune(seed + 1, temperature)
     blocks, adj = screen.run(seed, temperature)

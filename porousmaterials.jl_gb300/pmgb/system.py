@@ -125,6 +125,12 @@ class GPUSystem:
         self.ctx.check(self.ctx._lib.pmgb_system_set_refine(self.handle, float(tail_fraction)))
         self.refine_tail = float(tail_fraction)
 
+    def refined_count(self) -> int:
+        """Insertions the last refined Widom run re-evaluated in FP64."""
+        out = C.c_int64()
+        self.ctx.check(self.ctx._lib.pmgb_system_refined_count(self.handle, C.byref(out)))
+        return out.value
+
     def widom(self, n_per_block: int, n_blocks: int, seed: int, temperature: float, want_energies: bool = False):
         """Per-block (log Σbf, ⟨U_vdw⟩, ⟨U_es⟩, n_inf) and optionally per-insertion (U_vdw, U_es)."""
         block = np.zeros((n_blocks, 4))

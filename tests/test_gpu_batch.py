@@ -101,10 +101,10 @@ def test_batch_adjoint_matches_single_system(mixed_systems, unit_mflop):
 def test_batch_lj_members_match_oracle(mixed_systems):
     """Block K_H of LJ members against the FP64 oracle on the same poses.
 
-    The porous frameworks (config0, the porous config1 cell) meet 1e-6 relative.  In the dense
-    random frameworks a block's Boltzmann weight can sit on one or two strongly repulsive
-    insertions; there the log-sum may differ by no more than the FP32 error bound of those
-    insertions' energies (4e-6 x the sum of |pair terms| + 1e-4 K) divided by T."""
+    FP32 alone, the log-sum may differ by no more than the Boltzmann-weighted FP32 error bound
+    of the insertions' energies (4e-6 x the sum of |pair terms| + 1e-4 K) divided by T: up to
+    ~1e-5 where a block's weight sits on a few deep sites.  With the FP64 tail refinement every
+    block is within 1e-6 relative."""
     ff = synthetic.forcefield()
     porous = build_systems([synthetic.config0(), synthetic.config1_porous()], synthetic.ch4(), ff,
                            ctx=mixed_systems[0].ctx)
@@ -112,6 +112,8 @@ def test_batch_lj_members_match_oracle(mixed_systems):
     npb, nb, seed = 400, 5, 2024
     screen = BatchScreen(lj_systems, npb, nb)
     blocks, _ = screen.run(seed, T)
+    screen.set_refine(1e-3)
+    refined, _ = screen.run(seed, T)
     for s, gs in enumerate(lj_systems):
         o = oracle_for(gs)
         xf, _ = gs.ctx.sample_poses(system_seed(seed, s), 0, npb * nb)
@@ -123,20 +125,34 @@ def test_batch_lj_members_match_oracle(mixed_systems):
             fin = np.isfinite(vb)
             assert blocks[s, b, 3] == np.count_nonzero(~fin)
             if not fin.any():
-                assert blocks[s, b, 0] == -np.inf
+                assert blocks[s, b, 0] == -np.inf and refined[s, b, 0] == -np.inf
                 continue
             x = -vb[fin] / T
             p = np.exp(x - x.max())
             bound = float(np.sum(p * tb[fin]) / np.sum(p)) / T
             d = abs(blocks[s, b, 0] - ref[b, 0])
             assert d <= bound + 1e-12, (s, b, d, bound)
-            if s < len(porous):
-                assert d <= 1e-6, (s, b, d)  # K_H within 1e-6 relative
+            assert abs(refined[s, b, 0] - ref[b, 0]) <= 1e-6, (s, b)  # K_H within 1e-6 relative
+
+
+def test_batch_refine_matches_single_system(mixed_systems):
+    npb, nb, seed = 500, 5, 66
+    screen = BatchScreen(mixed_systems, npb, nb, refine_tail=1e-3)
+    blocks, _ = screen.run(seed, T)
+    try:
+        for s, gs in enumerate(mixed_systems):
+            gs.set_refine(1e-3)
+            ref, _ = gs.widom(npb, nb, system_seed(seed, s), T)
+            np.testing.assert_array_equal(blocks[s], ref)
+    finally:
+        for gs in mixed_systems:
+            gs.set_refine(0.0)
+    assert screen.ctx.device_status() == 0
 
 
 def test_screen_driver(mixed_systems):
     res = henry_coefficient_screen(None, None, T, synthetic.forcefield(), insertions=1000, seed=8,
-                                   systems=mixed_systems, tune=False)
+                                   systems=mixed_systems, tune=False, refine_tail=0.0)
     assert len(res) == len(mixed_systems)
     for s, (r, gs) in enumerate(zip(res, mixed_systems)):
         out = gs.widom_adjoint(200, 5, system_seed(8, s), T)[0]  # the adjoint kernel's energies
