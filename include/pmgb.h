@@ -142,6 +142,13 @@ int pmgb_widom(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t
  * reference is FP64 throughout (src/henry.jl:212-244). */
 int pmgb_system_set_refine(pmgb_system* sys, double tail_fraction);
 
+/* Spatially ordered evaluation (default on) for pmgb_widom / pmgb_widom_device and the energy
+ * grid: insertions of each block are processed in Z-order of their centre of mass (grid points
+ * in 4 x 4 x 2 bricks), and a warp skips the pair terms of framework records beyond the cutoff
+ * of all its items.  The skipped terms are exact zeros and the block sums are formed in
+ * insertion order, so results are bit-identical with it on or off.  No reference counterpart. */
+int pmgb_system_set_cull(pmgb_system* sys, int32_t on);
+
 /* Number of insertions the last refined Widom run re-evaluated in FP64 (synchronises). */
 int pmgb_system_refined_count(pmgb_system* sys, int64_t* count_out);
 

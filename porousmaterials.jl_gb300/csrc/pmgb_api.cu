@@ -77,6 +77,8 @@ struct pmgb_system {
     int site_atom[PMGB_MAX_SITES];
     int site_charge[PMGB_MAX_SITES];
     double refine_tail = 0.0;       // FP64 refinement of the Boltzmann tail (0: off)
+    bool cull = true;               // spatially ordered processing with cutoff culling
+    DevBuf o_counts, o_perm;        // Widom processing order scratch
     int last_refine_ctas = 0;       // chunks of the last refined run (its refined count sits after them)
     // grow-only scratch used by launches
     DevBuf r_hist, r_cut, r_counts, r_offsets, r_list, r_ref;  // refinement scratch
@@ -295,7 +297,7 @@ static void free_system_device(pmgb_system* s) {
                     s->d_skw,      s->d_sk,        s->d_kabc,    s->d_wt,     s->partials.p, s->block_out.p,
                     s->in_buf.p,   s->out_buf.p,   s->axes.p,    s->g_u.p,    s->g_dsum.p, s->g_grad.p,
                     s->g_part.p,   s->g_cols.p,   s->r_hist.p,  s->r_cut.p,  s->r_counts.p, s->r_offsets.p,
-                    s->r_list.p,   s->r_ref.p};
+                    s->r_list.p,   s->r_ref.p,    s->o_counts.p, s->o_perm.p};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -391,7 +393,19 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     std::vector<int> order(recs.size());
     for (size_t i = 0; i < recs.size(); ++i) order[i] = static_cast<int>(i);
     auto sp_key = [&](int i) { return recs[i].species < 0 ? n_species : recs[i].species; };
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sp_key(a) < sp_key(b); });
+    // within a segment, Z-order of the position (10 bits per axis): consecutive records are
+    // spatially close, so a warp can skip groups of them that lie beyond the cutoff
+    std::vector<uint32_t> zkey(recs.size());
+    for (size_t i = 0; i < recs.size(); ++i) {
+        const uint32_t c[3] = {to_fix(recs[i].x) >> 22, to_fix(recs[i].y) >> 22, to_fix(recs[i].z) >> 22};
+        uint32_t z = 0;
+        for (int bit = 0; bit < 10; ++bit)
+            for (int d = 0; d < 3; ++d) z |= ((c[d] >> bit) & 1u) << (3 * bit + d);
+        zkey[i] = z;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return sp_key(a) != sp_key(b) ? sp_key(a) < sp_key(b) : zkey[a] < zkey[b];
+    });
     std::vector<int4> h_rec;
     std::vector<double> h_rec_q;   // FP64 charge of each record
     std::vector<double> h_rec_xf;  // its exact fractional coordinates
@@ -820,6 +834,12 @@ extern "C" int pmgb_system_refined_count(pmgb_system* s, int64_t* count_out) {
     return PMGB_OK;
 }
 
+extern "C" int pmgb_system_set_cull(pmgb_system* s, int32_t on) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    s->cull = on != 0;
+    return PMGB_OK;
+}
+
 extern "C" int pmgb_system_set_refine(pmgb_system* s, double tail_fraction) {
     if (!s) return PMGB_ERR_INVALID_ARGUMENT;
     if (!(tail_fraction >= 0.0 && tail_fraction < 1.0))
@@ -854,11 +874,27 @@ extern "C" int pmgb_widom_device(pmgb_system* s, int64_t n_per_block, int32_t n_
     a.partials = static_cast<LsePartial*>(s->partials.p);
     a.u_out = u_out_dev;
     const bool refine = s->refine_tail > 0.0;
-    if (refine && !u_out_dev) {  // the refinement needs every insertion's FP32 energy
-        if (int rc = ensure(ctx, s->g_u, sizeof(double) * 2 * static_cast<size_t>(n_per_block) * n_blocks)) return rc;
+    const size_t n_ins = static_cast<size_t>(n_per_block) * n_blocks;
+    if ((refine || s->cull) && !u_out_dev) {  // both need every insertion's FP32 energy
+        if (int rc = ensure(ctx, s->g_u, sizeof(double) * 2 * n_ins)) return rc;
         a.u_out = static_cast<double*>(s->g_u.p);
     }
-    PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
+    if (s->cull) {
+        // spatially sorted processing order, so that warps can skip out-of-cutoff records; the
+        // block sums are then formed from the energies in insertion order
+        int rc;
+        if ((rc = ensure(ctx, s->o_counts, sizeof(int) * pmgb_widom_order_cells() * n_blocks)) ||
+            (rc = ensure(ctx, s->o_perm, sizeof(int) * n_ins)))
+            return rc;
+        a.perm = static_cast<const int*>(s->o_perm.p);
+        PMGB_CK(ctx, pmgb_launch_widom_order(seed, n_per_block, n_blocks, static_cast<int*>(s->o_counts.p),
+                                             static_cast<int*>(s->o_perm.p), ctx->stream));
+        PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
+        PMGB_CK(ctx, pmgb_launch_lse_from_u(a.u_out, n_per_block, n_blocks, a.ctas_per_block, a.inv_temperature,
+                                            a.partials, ctx->stream));
+    } else {
+        PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
+    }
     PMGB_CK(ctx, pmgb_launch_reduce_blocks(a.partials, n_blocks, a.ctas_per_block, block_out_dev, ctx->stream));
     if (refine) return run_refine(s, n_per_block, n_blocks, seed, temperature, block_out_dev, a.u_out);
     return PMGB_OK;
@@ -1183,7 +1219,8 @@ extern "C" int pmgb_energy_grid_device(pmgb_system* s, const int32_t n_pts[3], c
     a.grid_z = ax + n_pts[0] + n_pts[1];
     a.unit_factor = static_cast<float>(unit_factor);
     a.grid_out = out_dev;
-    const int n_ctas = static_cast<int>((total + PMGB_THREADS - 1) / PMGB_THREADS);
+    a.grid_bricks = s->cull ? 1 : 0;  // warps over compact bricks, skipping out-of-cutoff records
+    const int n_ctas = s->cull ? pmgb_grid_brick_ctas(n_pts) : static_cast<int>((total + PMGB_THREADS - 1) / PMGB_THREADS);
     PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
     return PMGB_OK;
 }

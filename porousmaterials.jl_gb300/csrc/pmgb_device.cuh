@@ -274,6 +274,7 @@ struct Geo2 {
     float2 h00, h01, h02, h11, h12, h22;
     float2 p00, p01, p02, p11, p12, p22;
     float rc2, rc2e;
+    float rcmax2;        // the larger cutoff^2: beyond it a pair contributes nothing
     float2 half_alpha;   // alpha / 2
     float2 m_a2_log2e;   // -alpha^2 log2(e)
 };
@@ -374,6 +375,49 @@ __device__ __forceinline__ void pair2_grad(const int4 ra, const int4 rb, const u
     G.gx = fma2(cx, du, G.gx);
     G.gy = fma2(cy, du, G.gy);
     G.gz = fma2(cz, du, G.gz);
+}
+
+// Squared minimum-image distances of two records from one guest site.
+__device__ __forceinline__ float2 pair2_r2(const int4 ra, const int4 rb, const uint32_t ux, const uint32_t uy,
+                                           const uint32_t uz, const Geo2& g) {
+    const float2 dx = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.x) - ux)),
+                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.x) - ux)));
+    const float2 dy = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.y) - uy)),
+                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.y) - uy)));
+    const float2 dz = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.z) - uz)),
+                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.z) - uz)));
+    const float2 rx = fma2(g.p00, dx, fma2(g.p01, dy, mul2(g.p02, dz)));
+    const float2 ry = fma2(g.p11, dy, mul2(g.p12, dz));
+    const float2 rz = mul2(g.p22, dz);
+    const float2 cx = fma2(g.h00, dx, fma2(g.h01, dy, fma2(g.h02, dz, rx)));
+    const float2 cy = fma2(g.h11, dy, fma2(g.h12, dz, ry));
+    const float2 cz = fma2(g.h22, dz, rz);
+    return fma2(cx, cx, fma2(cy, cy, mul2(cz, cz)));
+}
+
+// LJ and real-space terms of two records at squared distances r2 (charges qa, qb).
+template <bool CHARGED>
+__device__ __forceinline__ void pair2_energy(const float2 r2, const float qa, const float qb, const Geo2& g,
+                                             const float2 lj12, const float2 lj6, float2& ljp, float2& php) {
+    float2 ir2, y = f2(0.0f);
+    if (CHARGED) {
+        y = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+        const float2 hy = mul2(f2(-0.5f), mul2(r2, y));
+        y = fma2(y, fma2(hy, y, f2(0.5f)), y);
+        ir2 = mul2(y, y);
+    } else {
+        const float2 r0 = make_float2(rcp_approx(r2.x), rcp_approx(r2.y));
+        const float2 e = fma2(mul2(f2(-1.0f), r2), r0, f2(1.0f));
+        ir2 = fma2(r0, e, r0);
+    }
+    const float2 ir6 = mul2(mul2(ir2, ir2), ir2);
+    const float2 ir6c = make_float2(r2.x < g.rc2 ? ir6.x : 0.0f, r2.y < g.rc2 ? ir6.y : 0.0f);
+    ljp = fma2(ir6c, fma2(lj12, ir6c, lj6), ljp);
+    if (CHARGED) {
+        const float2 rr = mul2(r2, y);
+        const float2 e = mul2(erfc_fit2(rr, r2, g), y);
+        php = fma2(make_float2(qa, qb), make_float2(r2.x < g.rc2e ? e.x : 0.0f, r2.y < g.rc2e ? e.y : 0.0f), php);
+    }
 }
 
 template <bool CHARGED>
@@ -548,6 +592,52 @@ __device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua[NS
 // points) of one system against its whole framework.  Used once per CTA by the
 // single-system kernels and repeatedly by the persistent batch kernel.
 // ----------------------------------------------------------------------------
+// Log-sum-exp Boltzmann partial of one CTA: every thread passes its x = -U/T (-inf: no
+// insertion or U = +Inf), U_vdw, U_es and overlap count; thread 0 of warp 0 writes
+// (max x, sum e^{x - max}, sum U_vdw e^{..}, sum U_es e^{..}, n_inf).  A fixed shuffle tree,
+// so the partial depends only on which insertions the CTA holds.
+__device__ __forceinline__ void lse_cta(double x, double ev, double ee, long long ninf, LsePartial* red,
+                                        LsePartial* partial, double* m_out) {
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    const unsigned full = 0xffffffffu;
+    double m = x;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(full, m, o));
+    double w = (m == -inf || x == -inf) ? 0.0 : exp(x - m);
+    double s = w, tv = w * ev, te = w * ee;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(full, s, o);
+        tv += __shfl_xor_sync(full, tv, o);
+        te += __shfl_xor_sync(full, te, o);
+        ninf += __shfl_xor_sync(full, ninf, o);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) red[warp] = LsePartial{m, s, tv, te, ninf, 0};
+    __syncthreads();
+    if (warp == 0) {
+        constexpr int NW = PMGB_THREADS / 32;
+        LsePartial p = (lane < NW) ? red[lane] : LsePartial{-inf, 0.0, 0.0, 0.0, 0, 0};
+        double M = p.m;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) M = fmax(M, __shfl_xor_sync(full, M, o));
+        const double f = (M == -inf || p.m == -inf) ? 0.0 : exp(p.m - M);
+        double s2 = p.s * f, tv2 = p.tv * f, te2 = p.te * f;
+        long long n2 = p.n_inf;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s2 += __shfl_xor_sync(full, s2, o);
+            tv2 += __shfl_xor_sync(full, tv2, o);
+            te2 += __shfl_xor_sync(full, te2, o);
+            n2 += __shfl_xor_sync(full, n2, o);
+        }
+        if (lane == 0) {
+            *partial = LsePartial{M, s2, tv2, te2, n2, 0};
+            if (m_out) *m_out = M;
+        }
+    }
+}
+
 struct UnitIO {
     int pose_mode, out_mode;
     long long item;              // this thread's item index within its system
@@ -568,6 +658,7 @@ struct UnitIO {
     double* x_out;               // OUT_WIDOM, optional: this thread's -U/T (-inf if none)
     double* m_out;               // OUT_WIDOM, optional (shared): the unit's max of -U/T
     bool resident;               // the ring already holds this framework (n_tiles <= PMGB_NSTAGE)
+    bool cull;                   // the warp's items are spatially ordered: skip out-of-cutoff terms
 };
 
 // Returns false if a bounded wait gave up (the status word is set); every thread of the CTA
@@ -628,7 +719,8 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                 S.rc2, S.rc2e, S.alpha};
     const Geo2 g2{f2(S.h00), f2(S.h01), f2(S.h02), f2(S.h11), f2(S.h12), f2(S.h22),
                   f2(S.p00), f2(S.p01), f2(S.p02), f2(S.p11), f2(S.p12), f2(S.p22),
-                  S.rc2, S.rc2e, f2(0.5f * S.alpha), f2(-S.alpha * S.alpha * 1.4426950408889634f)};
+                  S.rc2, S.rc2e, fmaxf(S.rc2, CHARGED ? S.rc2e : 0.0f), f2(0.5f * S.alpha),
+                  f2(-S.alpha * S.alpha * 1.4426950408889634f)};
     const float2 c1 = f2(1.1283791670955126f * S.alpha);  // 2 alpha / sqrt(pi)
     float qcoul[NS];
 #pragma unroll
@@ -702,6 +794,40 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                     for (int k = 0; k < NS; ++k) {
                         ljp[k] = ljp2[k].x + ljp2[k].y;
                         php[k] = php2[k].x + php2[k].y;
+                    }
+                } else if (io.cull) {
+                    // the warp's insertions are spatially close: after the distances, skip the
+                    // pair terms of four records when no lane has the site inside the cutoff
+                    // (those terms are exact zeros, so the sums are unchanged)
+                    int j = j0;
+                    for (; j + 4 <= j1; j += 4) {
+                        const int4 r0 = T[j - t0], r1 = T[j + 1 - t0], r2 = T[j + 2 - t0], r3 = T[j + 3 - t0];
+#pragma unroll
+                        for (int k = 0; k < NS; ++k) {
+                            const float2 d01 = pair2_r2(r0, r1, ux[k], uy[k], uz[k], g2);
+                            const float2 d23 = pair2_r2(r2, r3, ux[k], uy[k], uz[k], g2);
+                            const float dmin = fminf(fminf(d01.x, d01.y), fminf(d23.x, d23.y));
+                            segmin[k] = fminf(segmin[k], dmin);
+                            if (__any_sync(0xffffffffu, valid && dmin < g2.rcmax2)) {
+                                const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
+                                pair2_energy<CHARGED>(d01, __int_as_float(r0.w), __int_as_float(r1.w), g2, a12, a6,
+                                                      ljp2[k], php2[k]);
+                                pair2_energy<CHARGED>(d23, __int_as_float(r2.w), __int_as_float(r3.w), g2, a12, a6,
+                                                      ljp2[k], php2[k]);
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < NS; ++k) {
+                        ljp[k] = ljp2[k].x + ljp2[k].y;
+                        php[k] = php2[k].x + php2[k].y;
+                    }
+                    for (; j < j1; ++j) {
+                        const int4 r = T[j - t0];
+#pragma unroll
+                        for (int k = 0; k < NS; ++k)
+                            pair_fwd<CHARGED>(r, ux[k], uy[k], uz[k], g, sig2[k], eps4[k], segmin[k], ljp[k],
+                                              php[k]);
                     }
                 } else {
                     int j = j0;
@@ -841,43 +967,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
         }
     }
     if (io.x_out) *io.x_out = x;
-    const unsigned full = 0xffffffffu;
-    double m = x;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(full, m, o));
-    double w = (m == -inf || x == -inf) ? 0.0 : exp(x - m);
-    double s = w, tv = w * ev, te = w * ee;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        s += __shfl_xor_sync(full, s, o);
-        tv += __shfl_xor_sync(full, tv, o);
-        te += __shfl_xor_sync(full, te, o);
-        ninf += __shfl_xor_sync(full, ninf, o);
-    }
-    const int warp = tid >> 5, lane = tid & 31;
-    if (lane == 0) red[warp] = LsePartial{m, s, tv, te, ninf, 0};
-    __syncthreads();
-    if (warp == 0) {
-        constexpr int NW = PMGB_THREADS / 32;
-        LsePartial p = (lane < NW) ? red[lane] : LsePartial{-inf, 0.0, 0.0, 0.0, 0, 0};
-        double M = p.m;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) M = fmax(M, __shfl_xor_sync(full, M, o));
-        const double f = (M == -inf || p.m == -inf) ? 0.0 : exp(p.m - M);
-        double s2 = p.s * f, tv2 = p.tv * f, te2 = p.te * f;
-        long long n2 = p.n_inf;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            s2 += __shfl_xor_sync(full, s2, o);
-            tv2 += __shfl_xor_sync(full, tv2, o);
-            te2 += __shfl_xor_sync(full, te2, o);
-            n2 += __shfl_xor_sync(full, n2, o);
-        }
-        if (lane == 0) {
-            *io.partial = LsePartial{M, s2, tv2, te2, n2, 0};
-            if (io.m_out) *io.m_out = M;
-        }
-    }
+    if (io.partial) lse_cta(x, ev, ee, ninf, red, io.partial, io.m_out);
     return true;
 }
 

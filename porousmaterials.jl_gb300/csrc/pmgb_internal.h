@@ -116,8 +116,10 @@ struct LaunchArgs {
     int n_blocks;                // statistics blocks
     int ctas_per_block;          // CTAs covering one statistics block
     double inv_temperature;
-    LsePartial* partials;        // [n_blocks * ctas_per_block]
-    double* u_out;               // optional: [n_total * 2] (U_vdw, U_es)
+    LsePartial* partials;        // [n_blocks * ctas_per_block]; NULL with perm (reduced from u_out)
+    double* u_out;               // optional: [n_total * 2] (U_vdw, U_es); required with perm
+    const int* perm;             // optional: processing order within each block (spatially sorted),
+                                 //   slot s of block b evaluates insertion b * n_per_block + perm[..]
     // explicit sites (POSE_SITES)
     const uint32_t* site_fix;    // [n_conf * n_sites * 3] fixed-point fractional coordinates
     long long n_conf;
@@ -129,6 +131,7 @@ struct LaunchArgs {
     const uint32_t* grid_z;
     float unit_factor;
     float* grid_out;
+    int grid_bricks;             // warps take 4 x 4 x 2 bricks of points (spatially compact)
     // adjoint (GRAD kernels)
     float* dsum;                 // [(seg * NS + site) * 2 + {0: sum r^-12, 1: sum r^-6}][item], within cutoff
     long long dsum_stride;       // items per column
@@ -138,6 +141,18 @@ struct LaunchArgs {
 };
 
 cudaError_t pmgb_launch_max_neg_u(const double* u, long long n, double inv_t, double* out, cudaStream_t st);
+// Spatial processing order of a Widom run: per block, a counting sort of the insertions by the
+// Z-order cell (32^3 cells) of their centre of mass.  counts: [n_blocks * 32768] scratch;
+// perm: [n_blocks * n_per_block] within-block insertion indices in processing order.
+cudaError_t pmgb_launch_widom_order(unsigned long long seed, long long n_per_block, int n_blocks, int* counts,
+                                    int* perm, cudaStream_t st);
+size_t pmgb_widom_order_cells();
+// Per-CTA log-sum-exp partials of a Widom run from its per-insertion energies, in insertion
+// order (the partials the pair kernel forms itself when it runs without a permutation).
+cudaError_t pmgb_launch_lse_from_u(const double* u, long long n_per_block, int n_blocks, int ctas_per_block,
+                                   double inv_temperature, LsePartial* partials, cudaStream_t st);
+// CTAs covering a grid of n_pts points taken in 4 x 4 x 2 bricks per warp
+int pmgb_grid_brick_ctas(const int n_pts[3]);
 // Weighted sums of per-item adjoint columns: out[c] = sum_i w_i col_c[i], w_i = exp(-U_i/T - M)
 cudaError_t pmgb_launch_weighted_columns(const double* u, int u_stride, long long n, double inv_t,
                                          const double* log_scale, int n_log, const float* cols,

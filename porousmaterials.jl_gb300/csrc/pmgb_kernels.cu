@@ -18,12 +18,27 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
     io.out_mode = a.out_mode;
     if (a.pose_mode == POSE_PHILOX) {
         const int b = blockIdx.x / a.ctas_per_block;
-        const long long within = static_cast<long long>(blockIdx.x % a.ctas_per_block) * PMGB_THREADS + tid;
-        io.valid = within < a.n_per_block;
+        const long long slot = static_cast<long long>(blockIdx.x % a.ctas_per_block) * PMGB_THREADS + tid;
+        io.valid = slot < a.n_per_block;
+        long long within = slot;
+        if (a.perm && io.valid) within = a.perm[static_cast<size_t>(b) * a.n_per_block + slot];
         io.item = static_cast<long long>(b) * a.n_per_block + within;
+        io.cull = a.perm != nullptr;
     } else if (a.pose_mode == POSE_SITES) {
         io.item = static_cast<long long>(blockIdx.x) * PMGB_THREADS + tid;
         io.valid = io.item < a.n_conf;
+    } else if (a.grid_bricks) {
+        // warp w takes brick (bi, bj, bk) of 4 x 4 x 2 points; i fastest inside it
+        const int n1 = a.n_pts[0], n2 = a.n_pts[1], n3 = a.n_pts[2];
+        const long long B1 = (n1 + 3) / 4, B2 = (n2 + 3) / 4;
+        const long long w = static_cast<long long>(blockIdx.x) * (PMGB_THREADS / 32) + (tid >> 5);
+        const int lane = tid & 31;
+        const int i = static_cast<int>(w % B1) * 4 + (lane & 3);
+        const int j = static_cast<int>((w / B1) % B2) * 4 + ((lane >> 2) & 3);
+        const long long k = (w / (B1 * B2)) * 2 + (lane >> 4);
+        io.valid = i < n1 && j < n2 && k < n3;
+        io.item = io.valid ? i + static_cast<long long>(n1) * (j + static_cast<long long>(n2) * k) : 0;
+        io.cull = true;
     } else {
         io.item = static_cast<long long>(blockIdx.x) * PMGB_THREADS + tid;
         io.valid = io.item < static_cast<long long>(a.n_pts[0]) * a.n_pts[1] * a.n_pts[2];
@@ -44,10 +59,99 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
     io.dsum_stride = a.dsum_stride;
     io.col_item = io.item;
     io.grad_u = a.grad_u;
-    io.partial = a.partials ? a.partials + blockIdx.x : nullptr;
+    io.partial = (a.partials && !a.perm) ? a.partials + blockIdx.x : nullptr;
     ring_init(bars);
     uint32_t fills[PMGB_NSTAGE] = {};
     (void)run_unit<NS, CHARGED, GRAD>(a.sys, io, stage, bars, red, fills, a.status);
+}
+
+// ---- spatial processing order of a Widom run ----------------------------------------
+constexpr int kOrderBits = 5;                       // 32 cells per axis
+constexpr int kOrderCells = 1 << (3 * kOrderBits);  // 32768 Z-order cells
+
+// Z-order cell of insertion idx: the top 5 bits of each 24-bit centre-of-mass coordinate
+// (the first Philox draw of make_pose), bits interleaved
+__device__ __forceinline__ int widom_cell(unsigned long long seed, unsigned long long idx) {
+    const uint2 key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    const uint4 a = philox4x32_10(make_uint4(static_cast<uint32_t>(idx), static_cast<uint32_t>(idx >> 32), 0u, 0u), key);
+    const uint32_t cx = a.x >> (32 - kOrderBits), cy = a.y >> (32 - kOrderBits), cz = a.z >> (32 - kOrderBits);
+    int code = 0;
+#pragma unroll
+    for (int b = 0; b < kOrderBits; ++b)
+        code |= static_cast<int>(((cx >> b) & 1u) << (3 * b) | ((cy >> b) & 1u) << (3 * b + 1) |
+                                 ((cz >> b) & 1u) << (3 * b + 2));
+    return code;
+}
+
+__global__ void order_count_kernel(unsigned long long seed, long long n_per_block, long long n, int* counts) {
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long long b = i / n_per_block;
+    atomicAdd(&counts[b * kOrderCells + widom_cell(seed, static_cast<unsigned long long>(i))], 1);
+}
+
+// exclusive scan of one block's 32768 cell counts (1024 threads x 32 consecutive cells)
+__global__ void __launch_bounds__(1024) order_scan_kernel(int* counts) {
+    __shared__ int part[1024];
+    int* c = counts + static_cast<size_t>(blockIdx.x) * kOrderCells;
+    constexpr int per = kOrderCells / 1024;
+    const int t = threadIdx.x;
+    int v[per], sum = 0;
+#pragma unroll
+    for (int q = 0; q < per; ++q) {
+        v[q] = c[t * per + q];
+        sum += v[q];
+    }
+    part[t] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int add = (t >= o) ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += add;
+        __syncthreads();
+    }
+    int run = part[t] - sum;
+#pragma unroll
+    for (int q = 0; q < per; ++q) {
+        c[t * per + q] = run;
+        run += v[q];
+    }
+}
+
+// Insertions go to their cell's next slot; the order inside a cell is whatever the atomics give,
+// which changes nothing: each insertion's energy does not depend on its slot, and the block
+// sums are formed afterwards in insertion order.
+__global__ void order_scatter_kernel(unsigned long long seed, long long n_per_block, long long n, int* offsets,
+                                     int* perm) {
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long long b = i / n_per_block;
+    const int pos = atomicAdd(&offsets[b * kOrderCells + widom_cell(seed, static_cast<unsigned long long>(i))], 1);
+    perm[b * n_per_block + pos] = static_cast<int>(i - b * n_per_block);
+}
+
+__global__ void __launch_bounds__(PMGB_THREADS) lse_from_u_kernel(const double* __restrict__ u, long long n_per_block,
+                                                                 int ctas_per_block, double inv_t,
+                                                                 LsePartial* __restrict__ partials) {
+    __shared__ LsePartial red[PMGB_THREADS / 32];
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    const int b = blockIdx.x / ctas_per_block;
+    const long long within = static_cast<long long>(blockIdx.x % ctas_per_block) * PMGB_THREADS + threadIdx.x;
+    double x = -inf, ev = 0.0, ee = 0.0;
+    long long ninf = 0;
+    if (within < n_per_block) {
+        const long long item = static_cast<long long>(b) * n_per_block + within;
+        const double uv = u[2 * item], ues = u[2 * item + 1];
+        const double uu = uv + ues;
+        if (isfinite(uu)) {
+            x = -uu * inv_t;
+            ev = uv;
+            ee = ues;
+        } else {
+            ninf = 1;
+        }
+    }
+    lse_cta(x, ev, ee, ninf, red, partials + blockIdx.x, nullptr);
 }
 
 // log_scale[0] = max_i (-U_i / T) over finite U (one CTA, fixed order)
@@ -295,6 +399,33 @@ cudaError_t pmgb_launch_pairs(const LaunchArgs& a, int n_ctas, cudaStream_t st) 
 cudaError_t pmgb_launch_pairs_grad(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
     if (n_ctas <= 0) return cudaSuccess;
     return a.sys.charged ? launch_grad_ns<true>(a, n_ctas, st) : launch_grad_ns<false>(a, n_ctas, st);
+}
+
+size_t pmgb_widom_order_cells() { return kOrderCells; }
+
+cudaError_t pmgb_launch_widom_order(unsigned long long seed, long long n_per_block, int n_blocks, int* counts,
+                                    int* perm, cudaStream_t st) {
+    const long long n = n_per_block * n_blocks;
+    if (n <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * kOrderCells * static_cast<size_t>(n_blocks), st);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = static_cast<unsigned>((n + 255) / 256);
+    order_count_kernel<<<grid, 256, 0, st>>>(seed, n_per_block, n, counts);
+    order_scan_kernel<<<n_blocks, 1024, 0, st>>>(counts);
+    order_scatter_kernel<<<grid, 256, 0, st>>>(seed, n_per_block, n, counts, perm);
+    return cudaGetLastError();
+}
+
+cudaError_t pmgb_launch_lse_from_u(const double* u, long long n_per_block, int n_blocks, int ctas_per_block,
+                                   double inv_temperature, LsePartial* partials, cudaStream_t st) {
+    lse_from_u_kernel<<<n_blocks * ctas_per_block, PMGB_THREADS, 0, st>>>(u, n_per_block, ctas_per_block,
+                                                                          inv_temperature, partials);
+    return cudaGetLastError();
+}
+
+int pmgb_grid_brick_ctas(const int n_pts[3]) {
+    const long long bricks = static_cast<long long>((n_pts[0] + 3) / 4) * ((n_pts[1] + 3) / 4) * ((n_pts[2] + 1) / 2);
+    return static_cast<int>((bricks + PMGB_THREADS / 32 - 1) / (PMGB_THREADS / 32));
 }
 
 cudaError_t pmgb_launch_max_neg_u(const double* u, long long n, double inv_t, double* out, cudaStream_t st) {

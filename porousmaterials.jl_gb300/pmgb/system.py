@@ -125,6 +125,10 @@ class GPUSystem:
         self.ctx.check(self.ctx._lib.pmgb_system_set_refine(self.handle, float(tail_fraction)))
         self.refine_tail = float(tail_fraction)
 
+    def set_cull(self, on: bool) -> None:
+        """Spatially ordered evaluation with cutoff culling (pmgb_system_set_cull; default on)."""
+        self.ctx.check(self.ctx._lib.pmgb_system_set_cull(self.handle, int(bool(on))))
+
     def refined_count(self) -> int:
         """Insertions the last refined Widom run re-evaluated in FP64."""
         out = C.c_int64()
