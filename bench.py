@@ -36,8 +36,9 @@ UNIT = "insertions/s"
 T = 298.0
 N_BLOCKS = 5
 N_INS = 1_000_000
-# algorithmic flops per pair / k-term (FMA = 2, MUFU = 1, erfc = 10): LJ 28, Ewald real 40, k-term 17
-F_LJ, F_COUL, F_K = 28, 40, 17
+# algorithmic flops (FMA = 2, MUFU = 1): distance of a pair 26; inside the cutoff LJ 11 and the
+# real-space erfc term 30 more; a reciprocal-space term 17 per (k-vector, guest charge)
+F_DIST, F_LJ_IN, F_ES_IN, F_K = 26, 11, 30, 17
 REFINE_TAIL = 1e-3
 # kernels per Widom step: pairs, block reduction, and the refinement's hist, cut, count, scan,
 # scatter, FP64 energies (thread and warp passes), correction
@@ -56,6 +57,8 @@ def parse():
     p.add_argument("--batch-frameworks", type=int, default=512,
                    help="frameworks in the batched-screening leg (each with CH4 and CO2; 0 = skip)")
     p.add_argument("--batch-insertions", type=int, default=20000, help="insertions per (framework, guest)")
+    p.add_argument("--c4-insertions", type=int, default=10_000_000, help="insertions of the large-cell leg")
+    p.add_argument("--skip-configs", action="store_true", help="omit the large-cell and energy-grid legs")
     return p.parse_args()
 
 
@@ -71,10 +74,21 @@ def workload():
     return cr, sc, ff, ep, synthetic.co2(), rep
 
 
-def flops_per_insertion(sc, mol, ep):
-    n_lj = mol.n_atoms * sc.atoms.n
-    n_q = mol.n_charges * sc.charges.n
-    return F_LJ * n_lj + F_COUL * n_q + F_K * mol.n_charges * ep.n_kvecs
+def flops_per_insertion(sc, mol, ff, ep):
+    """Algorithmic FP32 flops of one insertion (FMA = 2, MUFU = 1): the minimum-image distance
+    of every (framework record, guest site) pair; the LJ and real-space terms of the pairs inside
+    their cutoffs -- a uniform insertion has n (4/3) pi rc^3 / V framework sites inside rc on
+    average (minimum image, rc at most half the smallest width); reciprocal-space terms."""
+    import numpy as np
+
+    sph = lambda r: 4.0 / 3.0 * math.pi * r ** 3 / sc.box.Omega
+    n_rec = len({tuple(np.round(np.mod(x, 1.0), 12)) for x in np.vstack([sc.atoms.xf, sc.charges.xf])}) \
+        if sc.charges.n else sc.atoms.n
+    sites = max(mol.n_atoms, mol.n_charges)
+    f = F_DIST * sites * n_rec + F_LJ_IN * mol.n_atoms * sc.atoms.n * sph(ff.r_cutoff)
+    if ep is not None and mol.n_charges:
+        f += F_ES_IN * mol.n_charges * sc.charges.n * sph(ep.sr_cutoff_r) + F_K * mol.n_charges * ep.n_kvecs
+    return f
 
 
 # ------------------------------------------------------------------ clocks sampling
@@ -309,6 +323,73 @@ def batched_leg(args, ctx, stream):
     return out
 
 
+# ------------------------------------------------------------------ the other configurations
+def other_configs(args, ctx, stream):
+    """The large Ewald cell (config4) and the energy grid (config2), one timed pass each after a
+    warm-up, CUDA events on the launching stream.
+
+    config4: CO2 in an orthorhombic 52 x 52 x 52 A cell of 20,000 atoms (same species mix and
+      charges), Ewald precision 1e-6, 1e7 insertions in 5 blocks; forward with the FP64 tail
+      refinement, forward FP32 only, and forward + adjoint.
+    config2: Xe over a 96^3 fractional grid of config0's framework (FP32 output), and the grid
+      adjoint (dU/dr per point and dK_H/d(eps, sigma^2)) at 298 K."""
+    import torch
+
+    import pmgb
+    from pmgb import synthetic
+
+    out = {}
+
+    def timed(fn, reps=1):
+        fn()  # warm-up (allocates scratch)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ff = synthetic.forcefield(12.5)
+    cr = synthetic.config4()
+    sc = pmgb.replicate(cr, pmgb.replication_factors(cr.box, ff))
+    ep = pmgb.setup_Ewald_sum(sc.box, ff.r_cutoff, eps=1e-6)
+    mol = synthetic.co2()
+    gs = pmgb.GPUSystem(sc, pmgb.Frac(mol, sc.box), ff, ep, ctx=ctx, refine_tail=REFINE_TAIL)
+    npb = args.c4_insertions // N_BLOCKS
+    n = npb * N_BLOCKS
+    ms_ref = timed(lambda: gs.widom(npb, N_BLOCKS, 41, T))
+    refined = gs.refined_count()
+    gs.set_refine(0.0)
+    ms32 = timed(lambda: gs.widom(npb, N_BLOCKS, 42, T))
+    ms_adj = timed(lambda: gs.widom_adjoint(npb, N_BLOCKS, 43, T))
+    fpi = flops_per_insertion(sc, mol, ff, ep)
+    out["config4_large_ewald"] = {
+        "workload": "CO2 in a 20,000-atom 52x52x52 A cell, Ewald 1e-6", "framework_sites": sc.atoms.n,
+        "kvectors": ep.n_kvecs, "insertions": n,
+        "insertions_per_s": n / (ms_ref * 1e-3), "refined_insertions": refined,
+        "fp32_only_insertions_per_s": n / (ms32 * 1e-3),
+        "forward_plus_adjoint_insertions_per_s": n / (ms_adj * 1e-3),
+        "flops_per_insertion": fpi, "fp32_only_tflops": fpi * n / (ms32 * 1e-3) / 1e12}
+    del gs
+
+    c0 = synthetic.config0()
+    rep = pmgb.replication_factors(c0.box, ff)
+    sc0 = pmgb.replicate(c0, rep)
+    gx = pmgb.GPUSystem(sc0, pmgb.Frac(synthetic.xe(), sc0.box), ff, ctx=ctx)
+    pts = (96, 96, 96)
+    n_pts = 96 ** 3
+    ms_g = timed(lambda: gx.energy_grid(pts, rep, 1.0), reps=3)
+    ms_ga = timed(lambda: gx.energy_grid_adjoint(pts, rep, 1.0, T), reps=3)
+    out["config2_energy_grid"] = {
+        "workload": "Xe over a 96^3 grid of config0 (424 atoms, 25.832 A cubic)", "points": n_pts,
+        "points_per_s": n_pts / (ms_g * 1e-3), "adjoint_points_per_s": n_pts / (ms_ga * 1e-3),
+        "timing": "host call including the device-to-host copy of the grid (and gradients)"}
+    assert ctx.device_status() == 0
+    return out
+
+
 # ------------------------------------------------------------------ GPU arm
 def ours(args, rank, world, local_rank):
     global _tables
@@ -425,10 +506,13 @@ def ours(args, rank, world, local_rank):
     batched = None
     if args.batch_frameworks > 0 and rank == 0:
         batched = batched_leg(args, ctx, stream)
+    others = None
+    if not args.skip_configs and rank == 0:
+        others = other_configs(args, ctx, stream)
 
     if rank != 0:
         return
-    fpi = flops_per_insertion(sc, mol, ep)
+    fpi = flops_per_insertion(sc, mol, ff, ep)
     achieved = fpi * n_ins / (ms32 * 1e-3) / 1e12
     cpu = None
     if not args.skip_cpu:
@@ -460,6 +544,7 @@ def ours(args, rank, world, local_rank):
                                   "without the FP64 tail refinement)"},
            "forward_plus_adjoint": adj,
            "batched": batched,
+           "other_configs": others,
            "clocks": clk.summary(),
            "wall_s_timed_region": t_wall,
            "e2e": e2e,

@@ -1025,7 +1025,19 @@ extern "C" int pmgb_widom_adjoint(pmgb_system* s, int64_t n_per_block, int32_t n
     a.dsum_stride = n;
     a.grad_u = grad_out ? static_cast<float*>(s->g_grad.p) : nullptr;
     double* d_block = static_cast<double*>(s->block_out.p);
-    PMGB_CK(ctx, pmgb_launch_pairs_grad(a, n_ctas, ctx->stream));
+    if (s->cull) {  // spatially ordered, block sums from the energies in insertion order
+        if ((rc = ensure(ctx, s->o_counts, sizeof(int) * pmgb_widom_order_cells() * n_blocks)) ||
+            (rc = ensure(ctx, s->o_perm, sizeof(int) * n)))
+            return rc;
+        a.perm = static_cast<const int*>(s->o_perm.p);
+        PMGB_CK(ctx, pmgb_launch_widom_order(seed, n_per_block, n_blocks, static_cast<int*>(s->o_counts.p),
+                                             static_cast<int*>(s->o_perm.p), ctx->stream));
+        PMGB_CK(ctx, pmgb_launch_pairs_grad(a, n_ctas, ctx->stream));
+        PMGB_CK(ctx, pmgb_launch_lse_from_u(a.u_out, n_per_block, n_blocks, a.ctas_per_block, a.inv_temperature,
+                                            a.partials, ctx->stream));
+    } else {
+        PMGB_CK(ctx, pmgb_launch_pairs_grad(a, n_ctas, ctx->stream));
+    }
     PMGB_CK(ctx, pmgb_launch_reduce_blocks(a.partials, n_blocks, a.ctas_per_block, d_block, ctx->stream));
     PMGB_CK(ctx, pmgb_launch_weighted_columns(a.u_out, 2, n, a.inv_temperature, d_block, n_blocks, a.dsum, n_cols, n,
                                               static_cast<double*>(s->g_part.p), n_chunks,
@@ -1131,7 +1143,10 @@ extern "C" int pmgb_energy_grid_adjoint(pmgb_system* s, const int32_t n_pts[3], 
     a.grad_u = static_cast<float*>(s->g_grad.p);
     const double inv_t = 1.0 / temperature;
     double* d_scale = static_cast<double*>(s->block_out.p);
-    PMGB_CK(ctx, pmgb_launch_pairs_grad(a, static_cast<int>((total + PMGB_THREADS - 1) / PMGB_THREADS), ctx->stream));
+    a.grid_bricks = s->cull ? 1 : 0;
+    PMGB_CK(ctx, pmgb_launch_pairs_grad(a, s->cull ? pmgb_grid_brick_ctas(n_pts)
+                                                   : static_cast<int>((total + PMGB_THREADS - 1) / PMGB_THREADS),
+                                        ctx->stream));
     PMGB_CK(ctx, pmgb_launch_max_neg_u(a.u_out, total, inv_t, d_scale, ctx->stream));
     PMGB_CK(ctx, pmgb_launch_weighted_columns(a.u_out, 1, total, inv_t, d_scale, 1, a.dsum, n_cols, total,
                                               static_cast<double*>(s->g_part.p), n_chunks,

@@ -780,6 +780,12 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                         const float2 mask = make_float2(1.0f, two ? 1.0f : 0.0f);
 #pragma unroll
                         for (int k = 0; k < NS; ++k) {
+                            if (io.cull) {
+                                // no lane has the site within the cutoff of either record: every
+                                // term below would be an exact zero (no overlap is possible either)
+                                const float2 d = pair2_r2(ra, rb, ux[k], uy[k], uz[k], g2);
+                                if (!__any_sync(0xffffffffu, valid && fminf(d.x, d.y) < g2.rcmax2)) continue;
+                            }
                             Grad2 G{i12[k], i6[k], gx[k], gy[k], gz[k]};
                             pair2_grad<CHARGED>(ra, rb, ux[k], uy[k], uz[k], g2, f2(lj12[k]), f2(lj6[k]),
                                                 f2(qcoul[k]), c1, mask, segmin[k], ljp2[k], php2[k], G);

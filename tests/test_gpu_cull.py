@@ -61,3 +61,35 @@ def test_culled_grid_is_bit_identical(n_pts):
     gs.set_cull(True)
     g1 = gs.energy_grid(n_pts, rep, 1.0)
     np.testing.assert_array_equal(g1, g0)
+
+
+@pytest.mark.parametrize("case", ["co2_porous", "ch4_config0"])
+def test_culled_adjoint_is_bit_identical(case):
+    make = {"co2_porous": (synthetic.config1_porous, synthetic.co2, True),
+            "ch4_config0": (synthetic.config0, synthetic.ch4, False)}[case]
+    gs = _system(make[0](), make[1](), make[2])
+    out = []
+    for cull in (False, True):
+        gs.set_cull(cull)
+        b, adj = gs.widom_adjoint(3000, 5, 77, T, want_energies=True, want_grad=True)
+        out.append((b, adj))
+    (b0, a0), (b1, a1) = out
+    np.testing.assert_array_equal(b1, b0)
+    for key in ("log_scale", "sum_w", "sum_w_ues", "d_eps", "d_sig2", "u", "grad"):
+        np.testing.assert_array_equal(a1[key], a0[key])
+
+
+def test_culled_grid_adjoint_is_bit_identical():
+    cr = synthetic.config0()
+    ff = synthetic.forcefield()
+    rep = pmgb.replication_factors(cr.box, ff)
+    sc = pmgb.replicate(cr, rep)
+    gs = pmgb.GPUSystem(sc, pmgb.Frac(synthetic.xe(), sc.box), ff)
+    res = []
+    for cull in (False, True):
+        gs.set_cull(cull)
+        res.append(gs.energy_grid_adjoint((19, 18, 17), rep, 1.0, T))
+    for x, y in zip(res[0][:2], res[1][:2]):
+        np.testing.assert_array_equal(y, x)
+    for key in ("log_scale", "d_eps", "d_sig2"):
+        np.testing.assert_array_equal(res[1][2][key], res[0][2][key])
