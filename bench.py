@@ -40,9 +40,10 @@ N_INS = 1_000_000
 # real-space erfc term 30 more; a reciprocal-space term 17 per (k-vector, guest charge)
 F_DIST, F_LJ_IN, F_ES_IN, F_K = 26, 11, 30, 17
 REFINE_TAIL = 1e-3
-# kernels per Widom step: pairs, block reduction, and the refinement's hist, cut, count, scan,
-# scatter, FP64 energies (thread and warp passes), correction
-LAUNCHES_PER_STEP = 10
+# kernels per Widom step: spatial order (count, scan, scatter), pairs, insertion-order partials,
+# block reduction, and the refinement's hist, cut, count, scan, scatter, FP64 energies (thread
+# and warp passes), correction
+LAUNCHES_PER_STEP = 14
 
 
 def parse():

@@ -81,7 +81,7 @@ struct pmgb_system {
     DevBuf o_counts, o_perm;        // Widom processing order scratch
     int last_refine_ctas = 0;       // chunks of the last refined run (its refined count sits after them)
     // grow-only scratch used by launches
-    DevBuf r_hist, r_cut, r_counts, r_offsets, r_list, r_ref;  // refinement scratch
+    DevBuf r_hist, r_cut, r_counts, r_offsets, r_list, r_ref, r_plan, r_done, r_part;  // refinement scratch
     DevBuf partials, block_out, in_buf, out_buf, axes;
     DevBuf g_u, g_dsum, g_grad, g_part, g_cols;  // adjoint scratch
 };
@@ -297,7 +297,8 @@ static void free_system_device(pmgb_system* s) {
                     s->d_skw,      s->d_sk,        s->d_kabc,    s->d_wt,     s->partials.p, s->block_out.p,
                     s->in_buf.p,   s->out_buf.p,   s->axes.p,    s->g_u.p,    s->g_dsum.p, s->g_grad.p,
                     s->g_part.p,   s->g_cols.p,   s->r_hist.p,  s->r_cut.p,  s->r_counts.p, s->r_offsets.p,
-                    s->r_list.p,   s->r_ref.p,    s->o_counts.p, s->o_perm.p};
+                    s->r_list.p,   s->r_ref.p,    s->o_counts.p, s->o_perm.p,  s->r_plan.p,  s->r_done.p,
+                    s->r_part.p};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -793,7 +794,9 @@ static int run_refine(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uin
     if ((rc = ensure(ctx, s->r_hist, sizeof(unsigned long long) * pmgb_refine_hist_words() * n_blocks)) ||
         (rc = ensure(ctx, s->r_cut, sizeof(int) * n_blocks)) || (rc = ensure(ctx, s->r_counts, sizeof(int) * n_ctas)) ||
         (rc = ensure(ctx, s->r_offsets, sizeof(int) * (n_ctas + 2))) ||
-        (rc = ensure(ctx, s->r_list, sizeof(long long) * n)) || (rc = ensure(ctx, s->r_ref, sizeof(double) * 3 * n)))
+        (rc = ensure(ctx, s->r_list, sizeof(long long) * n)) || (rc = ensure(ctx, s->r_ref, sizeof(double) * 3 * n)) ||
+        (rc = ensure(ctx, s->r_plan, sizeof(int) * 4)) || (rc = ensure(ctx, s->r_done, sizeof(int) * n)) ||
+        (rc = ensure(ctx, s->r_part, sizeof(double) * 4 * (2 * n + 4096))))
         return rc;
     RefineArgs r{};
     r.sys = s->dev;
@@ -813,6 +816,12 @@ static int run_refine(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uin
     r.list = static_cast<long long*>(s->r_list.p);
     r.ref_u = static_cast<double*>(s->r_ref.p);
     r.counter = static_cast<int*>(s->r_offsets.p) + n_ctas + 1;
+    r.plan = static_cast<int*>(s->r_plan.p);
+    r.one_chunk = r.plan + 2;
+    r.done = static_cast<int*>(s->r_done.p);
+    r.part = static_cast<double*>(s->r_part.p);
+    r.cap_entries = n;
+    r.cap_items = 2 * n + 4096;
     int n_sm = 0;
     cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device);
     PMGB_CK(ctx, pmgb_launch_refine(r, n_ctas, std::max(1, n_sm), ctx->stream));
@@ -1335,6 +1344,8 @@ struct pmgb_batch {
     int *d_cut = nullptr, *d_counts = nullptr, *d_offsets = nullptr;
     long long* d_list = nullptr;
     double* d_ref_u = nullptr;
+    int *d_plan = nullptr, *d_done = nullptr;
+    double* d_part = nullptr;
     cudaGraphExec_t exec = nullptr;
     bool launched = false;
 };
@@ -1346,7 +1357,8 @@ void batch_free(pmgb_batch* b) {
     b->exec = nullptr;
     void* ptrs[] = {b->d_sys, b->d_units, b->d_order, b->d_counter, b->d_run, b->d_partials,
                     b->d_dsum, b->d_unit_cols, b->d_block_out, b->d_out_cols, b->d_chunk_sys, b->d_u,
-                    b->d_hist, b->d_cut, b->d_counts, b->d_offsets, b->d_list, b->d_ref_u};
+                    b->d_hist, b->d_cut, b->d_counts, b->d_offsets, b->d_list, b->d_ref_u,
+                    b->d_plan, b->d_done, b->d_part};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -1397,6 +1409,12 @@ int batch_capture(pmgb_batch* b) {
         r.list = b->d_list;
         r.ref_u = b->d_ref_u;
         r.counter = b->d_offsets + b->n_chunks + 1;
+        r.plan = b->d_plan;
+        r.one_chunk = b->d_plan + b->systems.size() + 1;
+        r.done = b->d_done;
+        r.part = b->d_part;
+        r.cap_entries = b->n_insertions;
+        r.cap_items = 2 * b->n_insertions + 4096;
     }
     cudaStream_t st = ctx->stream;
     PMGB_CK(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -1600,7 +1618,8 @@ extern "C" int pmgb_batch_set_refine(pmgb_batch* b, double tail_fraction) {
             (rc = batch_alloc(b, &b->d_hist, g * pmgb_refine_hist_words())) || (rc = batch_alloc(b, &b->d_cut, g)) ||
             (rc = batch_alloc(b, &b->d_counts, chunk_sys.size())) ||
             (rc = batch_alloc(b, &b->d_offsets, chunk_sys.size() + 2)) || (rc = batch_alloc(b, &b->d_list, n)) ||
-            (rc = batch_alloc(b, &b->d_ref_u, 3 * n)))
+            (rc = batch_alloc(b, &b->d_ref_u, 3 * n)) || (rc = batch_alloc(b, &b->d_plan, b->systems.size() + 2)) ||
+            (rc = batch_alloc(b, &b->d_done, n)) || (rc = batch_alloc(b, &b->d_part, 4 * (2 * n + 4096))))
             return rc;
         PMGB_CK(ctx, cudaMemcpyAsync(b->d_chunk_sys, chunk_sys.data(), sizeof(int) * chunk_sys.size(),
                                      cudaMemcpyHostToDevice, ctx->stream));

@@ -218,7 +218,12 @@ struct RefineArgs {
     int* offsets;                   // [chunks + 1]
     long long* list;                // [n] refined insertions (system << 40 | insertion), index order
     double* ref_u;                  // [3 n] their FP64 (U_vdw, U_sr, U_lr)
-    int* counter;                   // [1] work counter of the warp-per-insertion pass
+    int* counter;                   // [1] work counter of the chunked pass
+    int* plan;                      // [n_systems + 1] first chunk-item of each system, then the total
+    int* one_chunk;                 // [1] set when the chunk-items would exceed cap_items
+    int* done;                      // [cap_entries] chunks finished per refined insertion
+    double* part;                   // [4 cap_items] chunk partials (U_vdw, U_sr / coul, U_lr, overlap)
+    long long cap_items, cap_entries;
 };
 cudaError_t pmgb_launch_refine(const RefineArgs& a, int n_ctas, int n_sm, cudaStream_t st);
 size_t pmgb_refine_hist_words();

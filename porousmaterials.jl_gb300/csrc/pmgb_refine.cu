@@ -138,10 +138,7 @@ __global__ void tail_scan_kernel(const __grid_constant__ RefineArgs a, int n_cta
         if (threadIdx.x == blockDim.x - 1) carry += sh[threadIdx.x];
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        a.offsets[n_ctas] = carry;
-        *a.counter = 0;  // work counter of refine_large_kernel
-    }
+    if (threadIdx.x == 0) a.offsets[n_ctas] = carry;
 }
 
 __global__ void tail_scatter_kernel(const __grid_constant__ RefineArgs a) {
@@ -206,11 +203,12 @@ __device__ __forceinline__ void pair_fp64(const SysDev& S, int sg, int k, double
 // Reciprocal-space energy of guest site k over the half-rows [row0, row_end) stepping by
 // row_step: Sum_k wt Re[S(k) e^{-ik.x}], the phasor carried along kc by an FP64 recurrence
 // from one sincospi per row (rows hold at most a few dozen k-vectors).
-__device__ __forceinline__ double kspace_fp64(const SysDev& S, const double* x, int row0, int row_step) {
+__device__ __forceinline__ double kspace_fp64_rows(const SysDev& S, const double* x, int row0, int row_end,
+                                                   int row_step) {
     double lr = 0.0;
     double wr, wi;  // e^{-2 pi i x_c}: one step along +kc
     sincospi(-2.0 * x[2], &wi, &wr);
-    for (int row = row0; row < S.n_krow; row += row_step) {
+    for (int row = row0; row < row_end; row += row_step) {
         const KRow R = S.krow[row];
         double er, ei;  // e^{-ik.x} at the row start
         sincospi(-2.0 * (R.ka * x[0] + R.kb * x[1] + R.kc0 * x[2]), &ei, &er);
@@ -243,30 +241,32 @@ __device__ void energy_fp64_thread(const SysDev& S, const double (*xs)[3], doubl
     }
     if (S.charged)
         for (int k = 0; k < ns; ++k)
-            if (S.q64[k] != 0.0) lr += S.q64[k] * kspace_fp64(S, xs[k], 0, 1);
+            if (S.q64[k] != 0.0) lr += S.q64[k] * kspace_fp64_rows(S, xs[k], 0, S.n_krow, 1);
     out3[0] = ovl ? __longlong_as_double(0x7ff0000000000000ll) : v;
     out3[1] = sr * S.coul;
     out3[2] = lr;
 }
 
-// The same, evaluated by one warp: lanes stride over records and k-space rows; the reduction
-// is a fixed shuffle tree, so the result does not depend on scheduling.
-__device__ void energy_fp64_warp(const SysDev& S, const double (*xs)[3], double* out3) {
+// Part of the FP64 energies evaluated by one warp: framework records [j0, j1) and k-space half-rows
+// [k0, k1); lanes stride over both.  out4 = (U_vdw part, U_sr part / coul, U_lr part, overlap).
+__device__ void energy_fp64_warp_part(const SysDev& S, const double (*xs)[3], int j0, int j1, int k0, int k1,
+                                      double* out4) {
     const int lane = threadIdx.x & 31;
     const int ns = S.n_sites;
     double v = 0.0, sr = 0.0, lr = 0.0;
     bool ovl = false;
     for (int sg = 0; sg < S.n_seg; ++sg) {
         const SegDesc d = S.seg[sg];
-        for (int j = d.lo + lane; j < d.hi; j += 32) {
+        const int lo = max(d.lo, j0), hi = min(d.hi, j1);
+        for (int j = lo + lane; j < hi; j += 32) {
             const double qj = S.rec_q[j];
             const double rx = S.rec_xf[3 * j], ry = S.rec_xf[3 * j + 1], rz = S.rec_xf[3 * j + 2];
             for (int k = 0; k < ns; ++k) pair_fp64(S, sg, k, rx, ry, rz, qj, xs[k], v, sr, ovl);
         }
     }
-    if (S.charged)
+    if (S.charged && k1 > k0)
         for (int k = 0; k < ns; ++k)
-            if (S.q64[k] != 0.0) lr += S.q64[k] * kspace_fp64(S, xs[k], lane, 32);
+            if (S.q64[k] != 0.0) lr += S.q64[k] * kspace_fp64_rows(S, xs[k], k0 + lane, k1, 32);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -275,16 +275,23 @@ __device__ void energy_fp64_warp(const SysDev& S, const double (*xs)[3], double*
     }
     ovl = __any_sync(0xffffffffu, ovl);
     if (lane == 0) {
-        out3[0] = ovl ? __longlong_as_double(0x7ff0000000000000ll) : v;
-        out3[1] = sr * S.coul;
-        out3[2] = lr;
+        out4[0] = v;
+        out4[1] = sr;
+        out4[2] = lr;
+        out4[3] = ovl ? 1.0 : 0.0;
     }
 }
 
-// FP64 work of one insertion (pair terms + reciprocal-space terms): small ones are evaluated
-// by one thread each, the others by a whole warp
-__device__ __forceinline__ bool small_system(const SysDev& S) {
-    return static_cast<long long>(S.n_sites) * (S.n_rec + (S.charged ? S.n_k : 0)) <= 512;
+// FP64 work units of one insertion (pair terms + reciprocal-space terms).  Small insertions are
+// evaluated by one thread each; the others are cut into chunks of ~4096 units (records and
+// k-space half-rows in proportion), one warp per chunk, so that one large insertion spreads over
+// many SMs instead of waiting on one warp's FP64 latency.
+__device__ __forceinline__ long long fp64_work(const SysDev& S) {
+    return static_cast<long long>(S.n_sites) * (S.n_rec + (S.charged ? S.n_k : 0));
+}
+__device__ __forceinline__ bool small_system(const SysDev& S) { return fp64_work(S) <= 512; }
+__device__ __forceinline__ int fp64_chunks(const SysDev& S) {
+    return small_system(S) ? 0 : static_cast<int>(min(64ll, (fp64_work(S) + 4095) / 4096));
 }
 
 __device__ __forceinline__ void refined_entry(const RefineArgs& a, long long e, const SysDev*& S, double (*xs)[3]) {
@@ -324,23 +331,120 @@ __global__ void __launch_bounds__(PMGB_THREADS) refine_small_kernel(const __grid
     }
 }
 
-// Entries of the other systems: one warp each, taken from a work counter so that the long
-// evaluations spread over every SM.  Which path an entry takes depends only on its system,
-// so results are reproducible.
+__device__ __forceinline__ int system_entry_first(const RefineArgs& a, int sys) {
+    return a.systems ? a.offsets[a.systems[sys].chunk_first] : 0;
+}
+__device__ __forceinline__ int system_entry_count(const RefineArgs& a, int sys, int n_ctas) {
+    if (!a.systems) return a.offsets[n_ctas];
+    const BatchSystem& bs = a.systems[sys];
+    return a.offsets[bs.chunk_first + bs.ctas_per_block * a.n_blocks] - a.offsets[bs.chunk_first];
+}
+
+// plan[s] = first chunk-item of system s (exclusive scan of entries x chunks over systems);
+// plan[n_systems] = the total.  If the total would exceed the partials' capacity, every large
+// insertion takes one chunk (the total is then at most the number of insertions).
+__global__ void __launch_bounds__(1024) refine_plan_kernel(const __grid_constant__ RefineArgs a, int n_ctas) {
+    __shared__ long long part[1024];
+    __shared__ long long carry;
+    __shared__ int one_chunk;
+    if (threadIdx.x == 0) {
+        carry = 0;
+        one_chunk = 0;
+        a.counter[0] = 0;
+    }
+    __syncthreads();
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int base = 0; base < a.n_systems; base += blockDim.x) {
+            const int sys = base + threadIdx.x;
+            long long items = 0;
+            if (sys < a.n_systems) {
+                const SysDev& S = a.systems ? a.systems[sys].sys : a.sys;
+                const int c = fp64_chunks(S);
+                items = static_cast<long long>(system_entry_count(a, sys, n_ctas)) * (one_chunk && c ? 1 : c);
+            }
+            part[threadIdx.x] = items;
+            __syncthreads();
+            for (int o = 1; o < static_cast<int>(blockDim.x); o <<= 1) {
+                const long long t = (static_cast<int>(threadIdx.x) >= o) ? part[threadIdx.x - o] : 0;
+                __syncthreads();
+                part[threadIdx.x] += t;
+                __syncthreads();
+            }
+            if (sys < a.n_systems) a.plan[sys] = static_cast<int>(min(carry + part[threadIdx.x] - items, 0x7fffffffll));
+            __syncthreads();
+            if (threadIdx.x == blockDim.x - 1) carry += part[threadIdx.x];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            if (pass == 0 && carry > a.cap_items) {
+                one_chunk = 1;  // too many chunk-items for the partials: one chunk per insertion
+                carry = 0;
+            } else {
+                a.plan[a.n_systems] = static_cast<int>(carry);
+                a.one_chunk[0] = one_chunk;
+            }
+        }
+        __syncthreads();
+        if (!one_chunk || pass == 1) break;
+    }
+}
+
+// Chunk-items of the large insertions: one warp each, from a work counter.  The warp that
+// completes an insertion's last chunk adds the chunk partials in chunk order (the same sum
+// whatever the scheduling) and stores the insertion's FP64 energies.
 __global__ void __launch_bounds__(PMGB_THREADS) refine_large_kernel(const __grid_constant__ RefineArgs a, int n_ctas) {
-    const int n_ref = a.offsets[n_ctas];
     const int lane = threadIdx.x & 31;
+    const int total = a.plan[a.n_systems];
     for (;;) {
-        int r = 0;
-        if (lane == 0) r = atomicAdd(a.counter, 1);
-        r = __shfl_sync(0xffffffffu, r, 0);
-        if (r >= n_ref) break;
-        const long long e = a.list[r];
-        if (small_system(entry_system(a, e))) continue;
-        const SysDev* S;
+        int i = 0;
+        if (lane == 0) i = atomicAdd(a.counter, 1);
+        i = __shfl_sync(0xffffffffu, i, 0);
+        if (i >= total) break;
+        // the system of item i: the last s with plan[s] <= i
+        int lo = 0, hi = a.n_systems - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (a.plan[mid] <= i) lo = mid;
+            else hi = mid - 1;
+        }
+        const int sys = lo;
+        const SysDev& S = a.systems ? a.systems[sys].sys : a.sys;
+        const int C = a.one_chunk[0] ? 1 : fp64_chunks(S);
+        const int local = i - a.plan[sys];
+        const int r = system_entry_first(a, sys) + local / C;
+        const int c = local % C;
+        const SysDev* Sp;
         double xs[PMGB_MAX_SITES][3];
-        refined_entry(a, e, S, xs);
-        energy_fp64_warp(*S, xs, a.ref_u + 3 * static_cast<size_t>(r));
+        refined_entry(a, a.list[r], Sp, xs);
+        const int j0 = static_cast<int>(static_cast<long long>(S.n_rec) * c / C);
+        const int j1 = static_cast<int>(static_cast<long long>(S.n_rec) * (c + 1) / C);
+        const int k0 = static_cast<int>(static_cast<long long>(S.n_krow) * c / C);
+        const int k1 = static_cast<int>(static_cast<long long>(S.n_krow) * (c + 1) / C);
+        double* p = a.part + 4 * static_cast<size_t>(i);
+        energy_fp64_warp_part(S, xs, j0, j1, k0, k1, p);
+        if (lane == 0 && C == 1) {  // the whole insertion in one chunk
+            double* out = a.ref_u + 3 * static_cast<size_t>(r);
+            out[0] = p[3] > 0.0 ? __longlong_as_double(0x7ff0000000000000ll) : p[0];
+            out[1] = p[1] * S.coul;
+            out[2] = p[2];
+        } else if (lane == 0) {
+            __threadfence();  // this chunk's partial before the count
+            if (atomicAdd(&a.done[r], 1) == C - 1) {
+                __threadfence();  // every other chunk's partial is visible
+                const volatile double* q = a.part + 4 * static_cast<size_t>(i - c);
+                double v = 0.0, sr = 0.0, lr = 0.0, ov = 0.0;
+                for (int cc = 0; cc < C; ++cc) {
+                    v += q[4 * cc];
+                    sr += q[4 * cc + 1];
+                    lr += q[4 * cc + 2];
+                    ov += q[4 * cc + 3];
+                }
+                double* out = a.ref_u + 3 * static_cast<size_t>(r);
+                out[0] = ov > 0.0 ? __longlong_as_double(0x7ff0000000000000ll) : v;
+                out[1] = sr * S.coul;
+                out[2] = lr;
+            }
+        }
     }
 }
 
@@ -426,7 +530,10 @@ cudaError_t pmgb_launch_refine(const RefineArgs& a, int n_ctas, int n_sm, cudaSt
     tail_count_kernel<<<n_ctas, PMGB_THREADS, 0, st>>>(a);
     tail_scan_kernel<<<1, 1024, 0, st>>>(a, n_ctas);
     tail_scatter_kernel<<<n_ctas, PMGB_THREADS, 0, st>>>(a);
+    e = cudaMemsetAsync(a.done, 0, sizeof(int) * static_cast<size_t>(a.cap_entries), st);
+    if (e != cudaSuccess) return e;
     refine_small_kernel<<<4 * n_sm, PMGB_THREADS, 0, st>>>(a, n_ctas);
+    refine_plan_kernel<<<1, 1024, 0, st>>>(a, n_ctas);
     refine_large_kernel<<<4 * n_sm, PMGB_THREADS, 0, st>>>(a, n_ctas);
     tail_correct_kernel<<<n_g, 32, 0, st>>>(a);
     return cudaGetLastError();
