@@ -36,9 +36,12 @@ UNIT = "insertions/s"
 T = 298.0
 N_BLOCKS = 5
 N_INS = 1_000_000
-# algorithmic flops (FMA = 2, MUFU = 1): distance of a pair 26; inside the cutoff LJ 11 and the
-# real-space erfc term 30 more; a reciprocal-space term 17 per (k-vector, guest charge)
-F_DIST, F_LJ_IN, F_ES_IN, F_K = 26, 11, 30, 17
+# algorithmic flops, fixed counting convention (FMA = 2, MUFU = 1, erfc = 10): every pair counted,
+# LJ 28 and real-space Coulomb 40; a reciprocal-space term 17 per (k-vector, guest charge)
+F_LJ, F_COUL, F_K = 28, 40, 17
+# the same work counted by what the cutoff keeps: the distance of every pair 26; inside the
+# cutoff the LJ terms 11 and the real-space terms 30 more
+F_DIST, F_LJ_IN, F_ES_IN = 26, 11, 30
 REFINE_TAIL = 1e-3
 # kernels per Widom step: spatial order (count, scan, scatter), pairs, insertion-order partials,
 # block reduction, and the refinement's hist, cut, count, scan, scatter, FP64 energies (thread
@@ -75,7 +78,18 @@ def workload():
     return cr, sc, ff, ep, synthetic.co2(), rep
 
 
-def flops_per_insertion(sc, mol, ff, ep):
+def flops_per_insertion(sc, mol, ep):
+    """Algorithmic FP32 flops of one insertion under the fixed convention: every (framework, guest)
+    LJ pair 28, every real-space charge pair 40, every (k-vector, guest charge) term 17."""
+    n_lj = mol.n_atoms * sc.atoms.n
+    n_q = mol.n_charges * sc.charges.n
+    f = F_LJ * n_lj
+    if ep is not None and mol.n_charges:
+        f += F_COUL * n_q + F_K * mol.n_charges * ep.n_kvecs
+    return f
+
+
+def flops_inside_cutoff(sc, mol, ff, ep):
     """Algorithmic FP32 flops of one insertion (FMA = 2, MUFU = 1): the minimum-image distance
     of every (framework record, guest site) pair; the LJ and real-space terms of the pairs inside
     their cutoffs -- a uniform insertion has n (4/3) pi rc^3 / V framework sites inside rc on
@@ -365,14 +379,18 @@ def other_configs(args, ctx, stream):
     gs.set_refine(0.0)
     ms32 = timed(lambda: gs.widom(npb, N_BLOCKS, 42, T))
     ms_adj = timed(lambda: gs.widom_adjoint(npb, N_BLOCKS, 43, T))
-    fpi = flops_per_insertion(sc, mol, ff, ep)
+    fpi = flops_per_insertion(sc, mol, ep)
     out["config4_large_ewald"] = {
         "workload": "CO2 in a 20,000-atom 52x52x52 A cell, Ewald 1e-6", "framework_sites": sc.atoms.n,
         "kvectors": ep.n_kvecs, "insertions": n,
         "insertions_per_s": n / (ms_ref * 1e-3), "refined_insertions": refined,
         "fp32_only_insertions_per_s": n / (ms32 * 1e-3),
         "forward_plus_adjoint_insertions_per_s": n / (ms_adj * 1e-3),
-        "flops_per_insertion": fpi, "fp32_only_tflops": fpi * n / (ms32 * 1e-3) / 1e12}
+        "flops_per_insertion": fpi, "fp32_only_tflops": fpi * n / (ms32 * 1e-3) / 1e12,
+        "fp32_only_tflops_inside_cutoff": flops_inside_cutoff(sc, mol, ff, ep) * n / (ms32 * 1e-3) / 1e12,
+        "note": "fp32_only_tflops follows the every-pair convention; cutoff culling skips the energy terms of "
+                "~89% of record groups in this 52 A cell, so that figure exceeds the FP32 peak; "
+                "fp32_only_tflops_inside_cutoff counts distances of all pairs and energy terms inside the cutoff"}
     del gs
 
     c0 = synthetic.config0()
@@ -513,8 +531,9 @@ def ours(args, rank, world, local_rank):
 
     if rank != 0:
         return
-    fpi = flops_per_insertion(sc, mol, ff, ep)
+    fpi = flops_per_insertion(sc, mol, ep)
     achieved = fpi * n_ins / (ms32 * 1e-3) / 1e12
+    fpi_in = flops_inside_cutoff(sc, mol, ff, ep)
     cpu = None
     if not args.skip_cpu:
         r, cores, n, dt = cpu_rate(sc, mol, ep, budget_s=15.0)
@@ -541,6 +560,16 @@ def ours(args, rank, world, local_rank):
                         "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
                         "peak_source": "in-run FFMA probe (pmgb_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                         "flops_per_insertion": fpi,
+                        "convention": "every pair counted: LJ 28, real-space 40, k-term 17 flops (FMA=2, MUFU=1, "
+                                      "erfc=10); with cutoff culling the kernel skips the energy terms of records "
+                                      "outside every lane's cutoff, so this credits skipped pairs",
+                        "inside_cutoff": {"flops_per_insertion": fpi_in,
+                                          "achieved": fpi_in * n_ins / (ms32 * 1e-3) / 1e12,
+                                          "frac": (fpi_in * n_ins / (ms32 * 1e-3) / 1e12) / fp32_peak
+                                          if fp32_peak else None,
+                                          "counting": "distance of every pair 26, LJ 11 and real-space 30 "
+                                                      "more per pair inside the cutoff (n 4/3 pi rc^3 / V per "
+                                                      "insertion), k-term 17"},
                         "kernel": "pairs_kernel<3,true,false> + reduce_blocks_kernel (FP32 pass, timed "
                                   "without the FP64 tail refinement)"},
            "forward_plus_adjoint": adj,

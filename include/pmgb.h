@@ -142,6 +142,15 @@ int pmgb_widom(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t
  * reference is FP64 throughout (src/henry.jl:212-244). */
 int pmgb_system_set_refine(pmgb_system* sys, double tail_fraction);
 
+/* Accessibility gate for this system's Widom runs (the accessibility_grid branch of
+ * src/henry.jl:225 -> accessible, src/grid.jl:778-836): data is a Bool grid over the UNIT
+ * cell, n_pts[0]*n_pts[1]*n_pts[2] bytes with i fastest (0 = inaccessible), repfactors the
+ * replication of this system's supercell.  An insertion whose centre of mass, scaled into the
+ * unit cell, has its nearest grid node and all 26 neighbours inaccessible gets U_vdw = U_es =
+ * +Inf.  data = NULL removes the gate. */
+int pmgb_system_set_accessibility(pmgb_system* sys, const int32_t n_pts[3], const int32_t repfactors[3],
+                                  const uint8_t* data);
+
 /* Spatially ordered evaluation (default on) for pmgb_widom / pmgb_widom_device and the energy
  * grid: insertions of each block are processed in Z-order of their centre of mass (grid points
  * in 4 x 4 x 2 bricks), and a warp skips the pair terms of framework records beyond the cutoff

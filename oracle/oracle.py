@@ -234,3 +234,25 @@ class OracleSystem:
             lib().or_system_destroy(self.h)
         except Exception:
             pass
+
+
+def accessible(grid_data, xf, repfactors):
+    """Vectorised restatement of the accessibility gate (src/grid.jl:778-836; henry.jl:225).
+
+    grid_data: Bool array (n1, n2, n3) over the unit cell; xf: (n, 3) supercell fractional
+    centres of mass; repfactors: the supercell's replication.  The point scaled into the unit
+    cell, mod 1, has nearest node 1 + round(x (n - 1)) (ties to even, as Julia's round); it is
+    accessible iff that node or any of its 26 neighbours is (index 0 -> n, n + 1 -> 1)."""
+    g = np.asarray(grid_data, dtype=bool)
+    n = np.array(g.shape)
+    x = np.mod(np.asarray(xf, dtype=np.float64) * np.asarray(repfactors), 1.0)
+    nn = 1 + np.rint(x * (n - 1)).astype(np.int64)      # numpy rint: ties to even
+    out = np.zeros(x.shape[0], dtype=bool)
+    for i in (-1, 0, 1):
+        for j in (-1, 0, 1):
+            for k in (-1, 0, 1):
+                v = nn + np.array([i, j, k])
+                v = np.where(v == 0, n, v)
+                v = np.where(v == n + 1, 1, v)
+                out |= g[v[:, 0] - 1, v[:, 1] - 1, v[:, 2] - 1]
+    return out

@@ -79,6 +79,7 @@ struct pmgb_system {
     double refine_tail = 0.0;       // FP64 refinement of the Boltzmann tail (0: off)
     bool cull = true;               // spatially ordered processing with cutoff culling
     DevBuf o_counts, o_perm;        // Widom processing order scratch
+    DevBuf acc;                     // accessibility grid (uint8, i fastest)
     int last_refine_ctas = 0;       // chunks of the last refined run (its refined count sits after them)
     // grow-only scratch used by launches
     DevBuf r_hist, r_cut, r_counts, r_offsets, r_list, r_ref, r_plan, r_done, r_part;  // refinement scratch
@@ -298,7 +299,7 @@ static void free_system_device(pmgb_system* s) {
                     s->in_buf.p,   s->out_buf.p,   s->axes.p,    s->g_u.p,    s->g_dsum.p, s->g_grad.p,
                     s->g_part.p,   s->g_cols.p,   s->r_hist.p,  s->r_cut.p,  s->r_counts.p, s->r_offsets.p,
                     s->r_list.p,   s->r_ref.p,    s->o_counts.p, s->o_perm.p,  s->r_plan.p,  s->r_done.p,
-                    s->r_part.p};
+                    s->r_part.p,   s->acc.p};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -840,6 +841,36 @@ extern "C" int pmgb_system_refined_count(pmgb_system* s, int64_t* count_out) {
                                  cudaMemcpyDeviceToHost, ctx->stream));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
     *count_out = n;
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_system_set_accessibility(pmgb_system* s, const int32_t n_pts[3], const int32_t repfactors[3],
+                                             const uint8_t* data) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (!data) {
+        s->dev.acc = nullptr;
+        return PMGB_OK;
+    }
+    if (!n_pts || !repfactors)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_system_set_accessibility: n_pts and repfactors required");
+    for (int d = 0; d < 3; ++d)
+        if (n_pts[d] < 1 || repfactors[d] < 1)
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT,
+                        "pmgb_system_set_accessibility: n_pts and repfactors must be >= 1");
+    const size_t n = static_cast<size_t>(n_pts[0]) * n_pts[1] * n_pts[2];
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // no run may still read the old grid
+    if (int rc = ensure(ctx, s->acc, n)) return rc;
+    std::vector<uint8_t> h(data, data + n);
+    for (auto& v : h) v = v ? 1 : 0;
+    PMGB_CK(ctx, cudaMemcpyAsync(s->acc.p, h.data(), n, cudaMemcpyHostToDevice, ctx->stream));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    s->dev.acc = static_cast<const uint8_t*>(s->acc.p);
+    for (int d = 0; d < 3; ++d) {
+        s->dev.acc_n[d] = n_pts[d];
+        s->dev.acc_rep[d] = repfactors[d];
+    }
     return PMGB_OK;
 }
 

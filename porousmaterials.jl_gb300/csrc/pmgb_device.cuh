@@ -160,9 +160,14 @@ __device__ __forceinline__ uint32_t frac2fix64(double x) {
 // as the oracle composes them from the same pose.
 template <int NS>
 __device__ __forceinline__ void pose_sites(const SysDev& S, unsigned long long seed, unsigned long long item,
-                                           uint32_t* ux, uint32_t* uy, uint32_t* uz) {
+                                           uint32_t* ux, uint32_t* uy, uint32_t* uz, float* com = nullptr) {
     float xf[3], R[9];
     make_pose(seed, item, xf, R);
+    if (com) {
+        com[0] = xf[0];
+        com[1] = xf[1];
+        com[2] = xf[2];
+    }
     const uint32_t cx = frac2fix(xf[0]), cy = frac2fix(xf[1]), cz = frac2fix(xf[2]);
     double r[9];
 #pragma unroll
@@ -177,6 +182,33 @@ __device__ __forceinline__ void pose_sites(const SysDev& S, unsigned long long s
         uy[k] = cy + frac2fix64(S.g64[3] * oy + S.g64[4] * oz);
         uz[k] = cz + frac2fix64(S.g64[5] * oz);
     }
+}
+
+// The accessibility gate of src/grid.jl:778-836: the supercell fraction xf scaled by the
+// replication factors (mod 1) into the grid's cell, its nearest node 1 + round(x (n - 1))
+// (ties to even, as Julia's round), and the node with its 26 neighbours (index 0 -> n,
+// n + 1 -> 1); accessible iff any of the 27 is.
+__device__ __forceinline__ bool accessible_com(const SysDev& S, const float* xf) {
+    int id[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        double x = static_cast<double>(xf[d]) * S.acc_rep[d];
+        x -= floor(x);
+        id[d] = 1 + static_cast<int>(rint(x * (S.acc_n[d] - 1)));
+    }
+    for (int i = -1; i <= 1; ++i)
+        for (int j = -1; j <= 1; ++j)
+            for (int k = -1; k <= 1; ++k) {
+                int v[3] = {id[0] + i, id[1] + j, id[2] + k};
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    if (v[d] == 0) v[d] = S.acc_n[d];
+                    if (v[d] == S.acc_n[d] + 1) v[d] = 1;
+                }
+                if (S.acc[(v[0] - 1) + static_cast<size_t>(S.acc_n[0]) * ((v[1] - 1) + static_cast<size_t>(S.acc_n[1]) * (v[2] - 1))])
+                    return true;
+            }
+    return false;
 }
 
 struct Geo {
@@ -675,9 +707,12 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
     uint32_t ux[NS], uy[NS], uz[NS];
 #pragma unroll
     for (int k = 0; k < NS; ++k) ux[k] = uy[k] = uz[k] = 0u;
+    bool blocked = false;  // inaccessible pocket: U = +Inf without its pair terms mattering
     if (valid) {
         if (io.pose_mode == POSE_PHILOX) {
-            pose_sites<NS>(S, io.seed, static_cast<unsigned long long>(item), ux, uy, uz);
+            float com[3];
+            pose_sites<NS>(S, io.seed, static_cast<unsigned long long>(item), ux, uy, uz, com);
+            if (S.acc) blocked = !accessible_com(S, com);
         } else if (io.pose_mode == POSE_SITES) {
             const uint32_t* p = io.site_fix + static_cast<size_t>(item) * S.n_sites * 3;
 #pragma unroll
@@ -784,7 +819,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                                 // no lane has the site within the cutoff of either record: every
                                 // term below would be an exact zero (no overlap is possible either)
                                 const float2 d = pair2_r2(ra, rb, ux[k], uy[k], uz[k], g2);
-                                if (!__any_sync(0xffffffffu, valid && fminf(d.x, d.y) < g2.rcmax2)) continue;
+                                if (!__any_sync(0xffffffffu, valid && !blocked && fminf(d.x, d.y) < g2.rcmax2)) continue;
                             }
                             Grad2 G{i12[k], i6[k], gx[k], gy[k], gz[k]};
                             pair2_grad<CHARGED>(ra, rb, ux[k], uy[k], uz[k], g2, f2(lj12[k]), f2(lj6[k]),
@@ -814,7 +849,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                             const float2 d23 = pair2_r2(r2, r3, ux[k], uy[k], uz[k], g2);
                             const float dmin = fminf(fminf(d01.x, d01.y), fminf(d23.x, d23.y));
                             segmin[k] = fminf(segmin[k], dmin);
-                            if (__any_sync(0xffffffffu, valid && dmin < g2.rcmax2)) {
+                            if (__any_sync(0xffffffffu, valid && !blocked && dmin < g2.rcmax2)) {
                                 const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
                                 pair2_energy<CHARGED>(d01, __int_as_float(r0.w), __int_as_float(r1.w), g2, a12, a6,
                                                       ljp2[k], php2[k]);
@@ -933,6 +968,12 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
     if (ovl) uv = inf;
     usr *= S.coul;
     if (CHARGED) ulr = static_cast<double>(pl_hi) + static_cast<double>(pl_lo);
+    if (blocked) {  // src/henry.jl:230-233: energy.vdw = energy.es = Inf
+        uv = inf;
+        usr = inf;
+        ulr = 0.0;
+        gcx = gcy = gcz = 0.0f;
+    }
     if (GRAD && valid && io.grad_u) {
         io.grad_u[3 * item + 0] = gcx;
         io.grad_u[3 * item + 1] = gcy;

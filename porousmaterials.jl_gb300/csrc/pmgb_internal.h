@@ -83,6 +83,10 @@ struct SysDev {
     const double* sk64;                     // [2 n_k] S(k) (re, im) in half-row order
     const double* wt64;                     // [n_k] k-vector weights in half-row order
     const int* kabc;                        // [3 n_k] k-vectors in half-row order
+    // optional accessibility gate (src/henry.jl:225): blocked insertions get U = +Inf
+    const uint8_t* acc;                     // [acc_n0 * acc_n1 * acc_n2], i fastest; 0 = inaccessible
+    int acc_n[3];                           // grid points per axis of the unit-cell grid
+    int acc_rep[3];                         // replication factors of the supercell
 };
 
 enum PoseMode : int {

@@ -68,13 +68,16 @@ def henry_coefficient(crystal: Crystal, molecule: Molecule, temperature: float, 
                       seed: int | None = None, masses: dict | None = None, system_out: list | None = None,
                       refine_tail: float = REFINE_TAIL) -> HenryResult:
     assert_P1_symmetry(crystal)
-    if accessibility_grid is not None:
-        raise NotImplementedError("accessibility-gated Widom insertions are not supported by this build")
+    if accessibility_grid is not None and not np.allclose(accessibility_grid.box.f_to_c, crystal.box.f_to_c,
+                                                          rtol=1e-6, atol=1e-6):
+        raise ValueError(f"accessibility grid box does not match box of {crystal.name}.")  # henry.jl:58-61
     t0 = time.time()
     temperature = float(temperature)
     if verbose:
         print(f"Simulating Henry coefficient of {molecule.species} in {crystal.name} at {temperature} K, using "
               f"{ljforcefield.name} force field with {insertions_per_volume} insertions per Å³.")
+        if accessibility_grid is not None:
+            print("Using provided accessibility grid to block inaccessible pockets")
     nb_insertions = max(N_BLOCKS, math.ceil(insertions_per_volume * crystal.box.Omega))
     if verbose:
         print(f"\t{nb_insertions} total # particle insertions")
@@ -92,6 +95,8 @@ def henry_coefficient(crystal: Crystal, molecule: Molecule, temperature: float, 
     if seed is None:
         seed = secrets.randbits(63)
     system = GPUSystem(crystal, fmol, ljforcefield, eparams, refine_tail=refine_tail)
+    if accessibility_grid is not None:
+        system.set_accessibility(accessibility_grid, repfactors)
     if system_out is not None:
         system_out.append(system)
     blocks, _ = system.widom(nb_per_block, N_BLOCKS, seed, temperature)

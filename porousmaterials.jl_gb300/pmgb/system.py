@@ -125,6 +125,20 @@ class GPUSystem:
         self.ctx.check(self.ctx._lib.pmgb_system_set_refine(self.handle, float(tail_fraction)))
         self.refine_tail = float(tail_fraction)
 
+    def set_accessibility(self, grid, repfactors) -> None:
+        """Gate Widom insertions by a Bool `Grid` over the unit cell (src/henry.jl:225): blocked
+        insertions get U = +Inf.  grid=None removes the gate."""
+        if grid is None:
+            self.ctx.check(self.ctx._lib.pmgb_system_set_accessibility(self.handle, None, None, None))
+            return
+        data = np.asarray(grid.data, dtype=bool)
+        n = np.ascontiguousarray(data.shape, dtype=np.int32)
+        r = np.ascontiguousarray(repfactors, dtype=np.int32)
+        flat = np.ascontiguousarray(data.transpose(2, 1, 0).reshape(-1).astype(np.uint8))  # i fastest
+        self._acc = flat
+        self.ctx.check(self.ctx._lib.pmgb_system_set_accessibility(self.handle, ptr(n, C.c_int32), ptr(r, C.c_int32),
+                                                                   ptr(flat, C.c_uint8)))
+
     def set_cull(self, on: bool) -> None:
         """Spatially ordered evaluation with cutoff culling (pmgb_system_set_cull; default on)."""
         self.ctx.check(self.ctx._lib.pmgb_system_set_cull(self.handle, int(bool(on))))

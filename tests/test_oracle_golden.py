@@ -220,3 +220,19 @@ def test_direct_and_sk_forms_agree_triclinic():
     _, sr_s, lr_s = osys.energies(np.zeros((20, 0, 3)), pos, charged=True, use_sk=True)
     np.testing.assert_array_equal(sr_d, sr_s)
     np.testing.assert_allclose(lr_s, lr_d, rtol=1e-11, atol=1e-9)
+
+
+def test_oracle_accessible_matches_host_mirror():
+    """The oracle's vectorised gate and the Python mirror of grid.jl:813-836 agree, including
+    points on the periodic faces and rounding ties."""
+    import pmgb
+    from pmgb.grid import Grid, accessible
+
+    rng = np.random.default_rng(8)
+    data = rng.random((4, 5, 3)) < 0.15
+    g = Grid(pmgb.Box(10.0, 11.0, 12.0, np.pi / 2, np.pi / 2, np.pi / 2), data.shape, data, "K", np.zeros(3))
+    rep = (2, 1, 3)
+    xf = np.vstack([rng.random((400, 3)), [[0.0, 0.0, 0.0], [0.5 / 2, 0.5, 0.5 / 3], [0.999999, 0.5, 0.25]]])
+    got = oracle.accessible(data, xf, rep)
+    want = np.array([accessible(g, x, rep) for x in xf])
+    np.testing.assert_array_equal(got, want)
