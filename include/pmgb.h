@@ -200,6 +200,18 @@ int pmgb_widom_adjoint(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, 
                        double temperature, double* block_out, double* dtheta, double* u_out,
                        float* grad_out);
 
+/* ---- Monte Carlo moves (guest-host energy of a few configurations at low latency) ------
+ * The guest-host part of the energy a GCMC move needs (src/gcmc.jl:111-124 -> vdw_energy,
+ * src/vdw_energetics.jl:62-64; plus the Ewald terms when the system is charged), as
+ * pmgb_energies computes it, through a CUDA graph captured once: pinned staging, copy in,
+ * one CTA per configuration with the framework split over its threads, copy out.  A handle
+ * serves 1..max_conf configurations per call; calls are synchronous.  pmgb_energies itself
+ * switches to the same kernel for up to 64 configurations. */
+typedef struct pmgb_move pmgb_move;
+int pmgb_move_create(pmgb_system* sys, int32_t max_conf, pmgb_move** out);
+int pmgb_move_energies(pmgb_move* move, int32_t n_conf, const double* site_xf, double* out);
+void pmgb_move_destroy(pmgb_move* move);
+
 /* pmgb_energies plus dU/dx of the configuration's reference point (all sites moved rigidly;
  * grad_out: n_conf x 3 floats, K/Å). */
 int pmgb_energies_grad(pmgb_system* sys, int64_t n_conf, const double* site_xf, double* out,

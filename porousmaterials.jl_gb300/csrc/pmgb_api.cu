@@ -22,6 +22,7 @@ namespace {
 thread_local std::string g_create_error;
 
 constexpr double kPi = 3.14159265358979323846;
+constexpr int64_t kLatencyConfs = 64;  // pmgb_energies: up to this many, one CTA per configuration
 
 // 1/(4 pi eps0) with eps0 in e^2/(A K), following src/electrostatics.jl:6-7.
 double coulomb_constant() {
@@ -777,10 +778,114 @@ extern "C" int pmgb_energies(pmgb_system* s, int64_t n_conf, const double* site_
     a.site_fix = static_cast<const uint32_t*>(s->in_buf.p);
     a.n_conf = n_conf;
     a.e_out = static_cast<double*>(s->out_buf.p);
-    const int n_ctas = static_cast<int>((n_conf + PMGB_THREADS - 1) / PMGB_THREADS);
-    PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
+    if (n_conf <= kLatencyConfs) {
+        // few configurations (a Monte Carlo move): one CTA each, the framework split over its threads
+        PMGB_CK(ctx, pmgb_launch_energies_latency(a, static_cast<int>(n_conf), ctx->stream));
+    } else {
+        const int n_ctas = static_cast<int>((n_conf + PMGB_THREADS - 1) / PMGB_THREADS);
+        PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
+    }
     PMGB_CK(ctx, cudaMemcpyAsync(out, s->out_buf.p, out_bytes, cudaMemcpyDeviceToHost, ctx->stream));
     return check_status(ctx);  // synchronises: the host staging vector outlives the copy
+}
+
+// ---------------------------------------------------------------------------- Monte Carlo moves
+struct pmgb_move {
+    pmgb_system* sys = nullptr;
+    int max_conf = 0;
+    uint32_t* h_stage = nullptr;  // pinned: [0] = n_conf, then fixed-point site coordinates
+    double* h_out = nullptr;      // pinned: 3 per configuration
+    uint32_t* d_stage = nullptr;
+    double* d_out = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+static void move_free(pmgb_move* m) {
+    if (m->exec) cudaGraphExecDestroy(m->exec);
+    if (m->h_stage) cudaFreeHost(m->h_stage);
+    if (m->h_out) cudaFreeHost(m->h_out);
+    if (m->d_stage) cudaFree(m->d_stage);
+    if (m->d_out) cudaFree(m->d_out);
+}
+
+extern "C" int pmgb_move_create(pmgb_system* s, int32_t max_conf, pmgb_move** out) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (!out || max_conf < 1 || max_conf > 65535)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_move_create: max_conf in [1, 65535]");
+    if (int rc = ready_for_charges(s)) return rc;
+    *out = nullptr;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    auto* m = new pmgb_move();
+    m->sys = s;
+    m->max_conf = max_conf;
+    const size_t words = 1 + static_cast<size_t>(max_conf) * s->n_sites * 3;
+    cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&m->h_stage), sizeof(uint32_t) * words, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void**>(&m->h_out), sizeof(double) * 3 * max_conf,
+                                            cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_stage, sizeof(uint32_t) * words);
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_out, sizeof(double) * 3 * max_conf);
+    if (e == cudaSuccess) {
+        // one graph: copy in (count + coordinates), evaluate, copy out
+        LaunchArgs a = base_args(s);
+        a.pose_mode = POSE_SITES;
+        a.out_mode = OUT_ENERGY;
+        a.site_fix = m->d_stage + 1;
+        a.n_conf = max_conf;
+        a.n_conf_dev = reinterpret_cast<const int*>(m->d_stage);
+        a.e_out = m->d_out;
+        cudaStream_t st = ctx->stream;
+        e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t e2 = cudaMemcpyAsync(m->d_stage, m->h_stage, sizeof(uint32_t) * words, cudaMemcpyHostToDevice, st);
+            if (e2 == cudaSuccess) e2 = pmgb_launch_energies_latency(a, max_conf, st);
+            if (e2 == cudaSuccess)
+                e2 = cudaMemcpyAsync(m->h_out, m->d_out, sizeof(double) * 3 * max_conf, cudaMemcpyDeviceToHost, st);
+            cudaGraph_t g = nullptr;
+            e = cudaStreamEndCapture(st, &g);
+            if (e == cudaSuccess) e = e2;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&m->exec, g, 0);
+            if (g) cudaGraphDestroy(g);
+        }
+    }
+    if (e != cudaSuccess) {
+        move_free(m);
+        delete m;
+        return cuda_fail(ctx, e, "pmgb_move_create");
+    }
+    ++ctx->refs;
+    *out = m;
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_move_energies(pmgb_move* m, int32_t n_conf, const double* site_xf, double* out) {
+    if (!m) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = m->sys->ctx;
+    if (n_conf < 0 || n_conf > m->max_conf || (n_conf > 0 && (!site_xf || !out)))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_move_energies: 0 <= n_conf <= %d", m->max_conf);
+    if (n_conf == 0) return PMGB_OK;
+    const size_t n_coord = 3 * static_cast<size_t>(m->sys->n_sites) * n_conf;
+    for (size_t i = 0; i < n_coord; ++i) {
+        if (!std::isfinite(site_xf[i]))
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_move_energies: non-finite site coordinate at %zu", i);
+        m->h_stage[1 + i] = to_fix(site_xf[i]);
+    }
+    m->h_stage[0] = static_cast<uint32_t>(n_conf);
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, cudaGraphLaunch(m->exec, ctx->stream));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    std::memcpy(out, m->h_out, sizeof(double) * 3 * n_conf);
+    return PMGB_OK;
+}
+
+extern "C" void pmgb_move_destroy(pmgb_move* m) {
+    if (!m) return;
+    pmgb_ctx* ctx = m->sys->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    move_free(m);
+    delete m;
+    ctx_release(ctx);
 }
 
 // Enqueue the FP64 refinement of the Boltzmann tail of a Widom run whose block results are

@@ -504,7 +504,7 @@ __device__ __forceinline__ void pair2_fwd(const int4 ra, const int4 rb, const ui
 template <int NS, bool GRAD = false>
 __device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua[NS], const uint32_t Ub[NS],
                                            const uint32_t Uc[NS], float& plr_hi, float& plr_lo,
-                                           float (*gu)[3] = nullptr) {
+                                           float (*gu)[3] = nullptr, int row0 = 0, int row_step = 1) {
     // GRAD: gu[g][d] receives dU_lr/du_g (fractional coordinates of site g)
     constexpr float kTurn = 4.656612873077393e-10f;  // 2^-31: int32 fixed point -> half turns
     plr_hi = 0.0f;
@@ -540,7 +540,7 @@ __device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua[NS
         wdr[k] = 1.0f + dwr[k];
         wdi[k] = dwi[k];
     }
-    for (int row = 0; row < S.n_krow; ++row) {
+    for (int row = row0; row < S.n_krow; row += row_step) {
         const KRow R = S.krow[row];
         const float sgn = static_cast<float>(R.dir);  // +1 or -1: direction along kc
         // site-0 phasor at the row start

@@ -127,6 +127,7 @@ struct LaunchArgs {
     // explicit sites (POSE_SITES)
     const uint32_t* site_fix;    // [n_conf * n_sites * 3] fixed-point fractional coordinates
     long long n_conf;
+    const int* n_conf_dev;       // optional: n_conf read from device memory (latency path)
     double* e_out;               // [n_conf * 3] (vdw, sr, lr)
     // grid (POSE_GRID)
     int n_pts[3];
@@ -145,6 +146,9 @@ struct LaunchArgs {
 };
 
 cudaError_t pmgb_launch_max_neg_u(const double* u, long long n, double inv_t, double* out, cudaStream_t st);
+// Few explicit configurations (POSE_SITES, OUT_ENERGY), one CTA each with the framework split
+// over its threads: the latency path of Monte Carlo moves.
+cudaError_t pmgb_launch_energies_latency(const LaunchArgs& a, int n_ctas, cudaStream_t st);
 // Spatial processing order of a Widom run: per block, a counting sort of the insertions by the
 // Z-order cell (32^3 cells) of their centre of mass.  counts: [n_blocks * 32768] scratch;
 // perm: [n_blocks * n_per_block] within-block insertion indices in processing order.

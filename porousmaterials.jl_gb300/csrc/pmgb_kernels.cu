@@ -65,6 +65,111 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
     (void)run_unit<NS, CHARGED, GRAD>(a.sys, io, stage, bars, red, fills, a.status);
 }
 
+// ---- latency path: few configurations, one CTA each -----------------------------------
+// For Monte Carlo moves (one molecule per call, src/gcmc.jl:111-124 -> vdw_energy): the CTA's
+// threads split the framework records (and the k-space half-rows) of one configuration and
+// the partial sums meet in a fixed-order FP64 reduction.  Same FP32 pair terms as the Widom
+// kernel's scalar path; n_conf comes from device memory when n_conf_dev is set (a captured
+// graph serves any count up to its CTA count).
+template <int NS, bool CHARGED>
+__global__ void __launch_bounds__(PMGB_THREADS) energies_latency_kernel(const __grid_constant__ LaunchArgs a) {
+    __shared__ double red[3][PMGB_THREADS / 32];
+    __shared__ int red_ovl;
+    const SysDev& S = a.sys;
+    const long long n_conf = a.n_conf_dev ? static_cast<long long>(*a.n_conf_dev) : a.n_conf;
+    const int c = blockIdx.x;
+    if (c >= n_conf) return;  // uniform over the CTA
+    const int tid = threadIdx.x;
+    if (tid == 0) red_ovl = 0;
+    uint32_t ux[NS], uy[NS], uz[NS];
+    const uint32_t* p = a.site_fix + static_cast<size_t>(c) * S.n_sites * 3;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+        ux[k] = k < S.n_sites ? p[3 * k] : 0u;
+        uy[k] = k < S.n_sites ? p[3 * k + 1] : 0u;
+        uz[k] = k < S.n_sites ? p[3 * k + 2] : 0u;
+    }
+    const Geo g{S.h00, S.h01, S.h02, S.h11, S.h12, S.h22, S.p00, S.p01, S.p02, S.p11, S.p12, S.p22,
+                S.rc2, S.rc2e, S.alpha};
+    float lj[NS], ph[NS];
+    bool ovl = false;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) lj[k] = ph[k] = 0.0f;
+    for (int sg = 0; sg < S.n_seg; ++sg) {
+        const SegDesc d = S.seg[sg];
+        float sig2[NS], eps4[NS], r2o[NS], segmin[NS];
+#pragma unroll
+        for (int k = 0; k < NS; ++k) {
+            const SitePar sp = S.segpar[sg * PMGB_MAX_SITES + k];
+            sig2[k] = sp.sig2;
+            eps4[k] = sp.eps4;
+            r2o[k] = sp.r2ovl;
+            segmin[k] = __int_as_float(0x7f800000);
+        }
+        for (int j = d.lo + tid; j < d.hi; j += blockDim.x) {
+            const int4 r = __ldg(S.rec + j);
+#pragma unroll
+            for (int k = 0; k < NS; ++k)
+                pair_fwd<CHARGED>(r, ux[k], uy[k], uz[k], g, sig2[k], eps4[k], segmin[k], lj[k], ph[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < NS; ++k) ovl = ovl || (segmin[k] < r2o[k]);
+    }
+    double v = 0.0, sr = 0.0, lr = 0.0;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+        if (k < S.n_sites) {
+            v += static_cast<double>(lj[k]);
+            if (CHARGED) sr += static_cast<double>(S.q[k]) * static_cast<double>(ph[k]);
+        }
+    }
+    if (CHARGED) {
+        float hi = 0.0f, lo = 0.0f;
+        kspace_fwd<NS>(S, ux, uy, uz, hi, lo, nullptr, tid, blockDim.x);
+        lr = static_cast<double>(hi) + static_cast<double>(lo);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+        sr += __shfl_xor_sync(0xffffffffu, sr, o);
+        lr += __shfl_xor_sync(0xffffffffu, lr, o);
+    }
+    __syncthreads();  // red_ovl initialised
+    if (ovl) atomicOr(&red_ovl, 1);
+    const int warp = tid >> 5, lane = tid & 31;
+    if (lane == 0) {
+        red[0][warp] = v;
+        red[1][warp] = sr;
+        red[2][warp] = lr;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        for (int w = 0; w < PMGB_THREADS / 32; ++w) {
+            a0 += red[0][w];
+            a1 += red[1][w];
+            a2 += red[2][w];
+        }
+        a.e_out[3 * c + 0] = red_ovl ? __longlong_as_double(0x7ff0000000000000ll) : a0;
+        a.e_out[3 * c + 1] = a1 * S.coul;
+        a.e_out[3 * c + 2] = a2;
+    }
+}
+
+template <bool CH>
+cudaError_t launch_latency_ns(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
+    switch (a.sys.n_sites <= 1 ? 1 : a.sys.n_sites <= 2 ? 2 : a.sys.n_sites <= 3 ? 3 : a.sys.n_sites <= 4 ? 4
+                                                                : a.sys.n_sites <= 6 ? 6 : 8) {
+        case 1: energies_latency_kernel<1, CH><<<n_ctas, PMGB_THREADS, 0, st>>>(a); break;
+        case 2: energies_latency_kernel<2, CH><<<n_ctas, PMGB_THREADS, 0, st>>>(a); break;
+        case 3: energies_latency_kernel<3, CH><<<n_ctas, PMGB_THREADS, 0, st>>>(a); break;
+        case 4: energies_latency_kernel<4, CH><<<n_ctas, PMGB_THREADS, 0, st>>>(a); break;
+        case 6: energies_latency_kernel<6, CH><<<n_ctas, PMGB_THREADS, 0, st>>>(a); break;
+        default: energies_latency_kernel<8, CH><<<n_ctas, PMGB_THREADS, 0, st>>>(a); break;
+    }
+    return cudaGetLastError();
+}
+
 // ---- spatial processing order of a Widom run ----------------------------------------
 constexpr int kOrderBits = 5;                       // 32 cells per axis
 constexpr int kOrderCells = 1 << (3 * kOrderBits);  // 32768 Z-order cells
@@ -399,6 +504,11 @@ cudaError_t pmgb_launch_pairs(const LaunchArgs& a, int n_ctas, cudaStream_t st) 
 cudaError_t pmgb_launch_pairs_grad(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
     if (n_ctas <= 0) return cudaSuccess;
     return a.sys.charged ? launch_grad_ns<true>(a, n_ctas, st) : launch_grad_ns<false>(a, n_ctas, st);
+}
+
+cudaError_t pmgb_launch_energies_latency(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
+    if (n_ctas <= 0) return cudaSuccess;
+    return a.sys.charged ? launch_latency_ns<true>(a, n_ctas, st) : launch_latency_ns<false>(a, n_ctas, st);
 }
 
 size_t pmgb_widom_order_cells() { return kOrderCells; }

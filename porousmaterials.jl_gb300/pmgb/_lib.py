@@ -56,6 +56,9 @@ SIGNATURES = [
     ("pmgb_widom_noalloc", C.c_int, [_vp, C.c_int64, C.c_int32, C.c_uint64, C.c_double, _vp, _vp]),
     ("pmgb_widom_adjoint", C.c_int, [_vp, C.c_int64, C.c_int32, C.c_uint64, C.c_double, _dp, _dp, _dp, _fp]),
     ("pmgb_energies_grad", C.c_int, [_vp, C.c_int64, _dp, _dp, _fp]),
+    ("pmgb_move_create", C.c_int, [_vp, C.c_int32, C.POINTER(_vp)]),
+    ("pmgb_move_energies", C.c_int, [_vp, C.c_int32, _dp, _dp]),
+    ("pmgb_move_destroy", None, [_vp]),
     ("pmgb_energy_grid_adjoint", C.c_int, [_vp, _ip, _ip, C.c_double, C.c_double, _fp, _fp, _dp]),
     ("pmgb_sample_poses", C.c_int, [_vp, C.c_uint64, C.c_int64, C.c_int64, _fp, _fp]),
     ("pmgb_energy_grid", C.c_int, [_vp, _ip, _ip, C.c_double, _fp]),

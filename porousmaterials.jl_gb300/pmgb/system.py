@@ -175,6 +175,10 @@ class GPUSystem:
         return block, {"log_scale": dth[0], "sum_w": dth[1], "sum_w_ues": dth[2], "d_eps": pair[:, :, 0].copy(),
                        "d_sig2": pair[:, :, 1].copy(), "u": u, "grad": g}
 
+    def move_evaluator(self, max_conf: int = 1) -> "MoveEvaluator":
+        """A low-latency evaluator of up to max_conf configurations per call (pmgb_move_*)."""
+        return MoveEvaluator(self, max_conf)
+
     def energies_grad(self, site_xf: np.ndarray):
         """((n, 3) energies as in energies(), (n, 3) dU/dx of the rigid configuration, K/Å)."""
         site_xf = np.ascontiguousarray(site_xf, dtype=np.float64).reshape(-1, self.n_sites, 3)
@@ -215,6 +219,38 @@ class GPUSystem:
     def close(self) -> None:
         if getattr(self, "handle", None):
             self.ctx._lib.pmgb_system_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MoveEvaluator:
+    """Guest-host energies of a few configurations per call through a captured CUDA graph: the
+    per-move energy of a Monte Carlo simulation (src/gcmc.jl:111-124).  energies() takes and
+    returns what GPUSystem.energies does."""
+
+    def __init__(self, system: GPUSystem, max_conf: int = 1):
+        self.system = system
+        self.max_conf = int(max_conf)
+        h = C.c_void_p()
+        system.ctx.check(system.ctx._lib.pmgb_move_create(system.handle, self.max_conf, C.byref(h)))
+        self.handle = h.value
+        self._out = np.zeros((self.max_conf, 3))
+
+    def energies(self, site_xf: np.ndarray) -> np.ndarray:
+        site_xf = np.ascontiguousarray(site_xf, dtype=np.float64).reshape(-1, self.system.n_sites, 3)
+        n = site_xf.shape[0]
+        self.system.ctx.check(self.system.ctx._lib.pmgb_move_energies(self.handle, n, ptr(site_xf, C.c_double),
+                                                                      ptr(self._out, C.c_double)))
+        return self._out[:n].copy()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.system.ctx._lib.pmgb_move_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

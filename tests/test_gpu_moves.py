@@ -1,0 +1,73 @@
+"""Latency path for Monte Carlo moves: pmgb_energies with up to 64 configurations (one CTA
+each) and the graph-captured pmgb_move_* evaluator, against the FP64 oracle with the FP32
+error model of the parity tests (per-term 4e-6 x the sum of term magnitudes + 1e-4 K), and
+against the many-configuration kernel."""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+import pytest
+
+import pmgb
+from pm_helpers import oracle_for, random_configs
+from pmgb import synthetic
+
+pytestmark = pytest.mark.gpu
+TOL, ATOL = 4e-6, 1e-4
+
+
+def _system(cr, mol, charged):
+    ff = synthetic.forcefield()
+    sc = pmgb.replicate(cr, pmgb.replication_factors(cr.box, ff))
+    ep = pmgb.setup_Ewald_sum(sc.box, ff.r_cutoff, eps=1e-6) if charged else None
+    return pmgb.GPUSystem(sc, pmgb.Frac(mol, sc.box), ff, ep)
+
+
+@pytest.mark.parametrize("case", ["co2_ewald", "ch4"])
+def test_latency_path_matches_oracle(case):
+    gs = _system(synthetic.config1(), synthetic.co2(), True) if case == "co2_ewald" else \
+        _system(synthetic.config0(), synthetic.ch4(), False)
+    sites, lj, q = random_configs(gs, 64, seed=71)
+    small = gs.energies(sites)                       # 64 configurations: latency kernel
+    big = gs.energies(np.concatenate([sites, sites[:1]]))[:64]  # 65: the many-configuration kernel
+    o = oracle_for(gs)
+    if gs.charged:
+        v, sr, lr, sv, ss = o.energies(lj, q, charged=True, use_sk=True, scales=True)
+    else:
+        v, sr, lr, sv, ss = o.energies(lj, scales=True)
+    for gpu in (small, big):
+        assert np.array_equal(np.isinf(gpu[:, 0]), np.isinf(v))
+        fin = np.isfinite(v)
+        assert np.all(np.abs(gpu[fin, 0] - v[fin]) <= TOL * sv[fin] + ATOL)
+        if gs.charged:
+            assert np.all(np.abs(gpu[:, 1] - sr) <= TOL * ss + ATOL)
+    if gs.charged:
+        # reciprocal space: the same FP32 recurrence, rows split over threads instead of one thread
+        # per configuration (checked against the oracle with its own error scale in the parity tests)
+        assert np.all(np.abs(small[:, 2] - big[:, 2]) <= 2e-3 + 1e-6 * np.abs(big[:, 2]))
+
+
+def test_move_evaluator_matches_energies():
+    gs = _system(synthetic.config1(), synthetic.co2(), True)
+    sites, _, _ = random_configs(gs, 40, seed=72)
+    ev = gs.move_evaluator(max_conf=8)
+    ref = gs.energies(sites)
+    for k in range(0, 40, 8):
+        got = ev.energies(sites[k:k + 8])
+        np.testing.assert_array_equal(got, ref[k:k + 8])  # same kernel, same inputs
+    one = ev.energies(sites[3])
+    np.testing.assert_array_equal(one[0], ref[3])
+    with pytest.raises(pmgb.PMGBError, match="n_conf"):
+        ev.energies(sites[:9])
+    # latency of one move (host call, graph replay), printed for the record
+    ev1 = gs.move_evaluator(1)
+    for _ in range(20):
+        ev1.energies(sites[0])
+    t = time.perf_counter()
+    n = 200
+    for i in range(n):
+        ev1.energies(sites[i % 40])
+    dt = (time.perf_counter() - t) / n
+    print(f"[move] CO2 + Ewald in 7,200 sites: {dt * 1e6:.1f} us per single-configuration call")
+    assert gs.ctx.device_status() == 0
