@@ -13,8 +13,8 @@ from .energetics import (Eikr, EwaldSum, PotentialEnergy, electrostatic_potentia
 from .ewald import (EPS0, FOUR_PI_EPS0, EwaldParams, determine_ewald_params, precompute_kvec_wts,
                     required_kreps, setup_Ewald_sum)
 from .forcefield import LJForceField, forcefield_coverage, replication_factors
-from .grid import (Grid, accessible, energy_grid, id_to_xf, read_cube, required_n_pts, write_cube,
-                   xf_to_id)
+from .grid import (Grid, accessible, compute_accessibility_grid, energy_grid, id_to_xf, read_cube,
+                   required_n_pts, write_cube, xf_to_id)
 from .henry import (K_TO_KJ_PER_MOL, N_BLOCKS, UNIV_GAS_CONST, HenryResult, henry_coefficient,
                     henry_coefficient_gradient)
 from .molecule import (Cart, Frac, Molecule, molecule_from_sites, needs_rotations, random_rotation_matrix,

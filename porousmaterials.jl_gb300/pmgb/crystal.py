@@ -135,8 +135,14 @@ def _tokenize(line: str) -> list[str]:
 def read_cif(path: str | Path, species_col=("_atom_site_type_symbol", "_atom_site_label"),
              wrap_coords: bool = True, include_zero_charges: bool = True,
              check_neutrality: bool = True, net_charge_tol: float = 1e-3) -> Crystal:
-    """Read a CIF in P1 (or whose symmetry operations are the identity only)."""
+    """Read a CIF in P1 (or whose symmetry operations are the identity only).  A bare file name
+    that does not exist where it is given is looked up in rc["paths"]["crystals"], as Xtals'
+    Crystal(filename) does."""
+    from .paths import rc
+
     path = Path(path)
+    if not path.exists() and not path.is_absolute() and rc["paths"].get("crystals"):
+        path = Path(rc["paths"]["crystals"]) / path
     text = path.read_text()
     lines = [ln.split("#", 1)[0].rstrip() if not ln.lstrip().startswith(";") else ln for ln in text.splitlines()]
     scalars: dict[str, str] = {}

@@ -170,3 +170,216 @@ def read_cube(filename: str, has_units: bool = True) -> Grid:
         vals = [float(t) for t in f.read().split()]
     data = np.array(vals).reshape(n_pts)
     return Grid(Box.from_f_to_c(f_to_c), n_pts, data, units, origin)
+
+
+# ---------------------------------------------------------------------------- accessibility
+def _segment_grid(data: np.ndarray, energy_tol: float) -> tuple[np.ndarray, int]:
+    """Flood fill (src/grid.jl:383-456): label the 26-connected regions of points with energy
+    below energy_tol (1, 2, ... in the reference's scan order), -1 elsewhere.  The grid's
+    faces are not wrapped here: connections across the unit-cell faces are the graph's job."""
+    from scipy import ndimage
+
+    accessible_pts = data < energy_tol
+    labels, n = ndimage.label(accessible_pts, structure=np.ones((3, 3, 3), dtype=bool))
+    # renumber in the reference's scan order (i slowest, k fastest: the array's C order)
+    order = np.zeros(n + 1, dtype=np.int64)
+    first = {}
+    flat = labels.reshape(-1)
+    nz = np.flatnonzero(flat)
+    _, idx = np.unique(flat[nz], return_index=True)
+    for new, lab in enumerate(flat[nz][np.sort(idx)], start=1):
+        first[int(lab)] = new
+    for lab, new in first.items():
+        order[lab] = new
+    seg = np.where(labels > 0, order[labels], -1)
+    return seg, n
+
+
+def _segment_connections(seg: np.ndarray) -> list[tuple[int, int, tuple[int, int, int]]]:
+    """Directed segment connections across the unit-cell faces (src/grid.jl:490-545): the end
+    plane and the first plane of each axis are the same points (endpoints included), each
+    connection noted once with its reverse."""
+    conns: list[tuple[int, int, tuple[int, int, int]]] = []
+    seen = set()
+
+    def note(a: int, b: int, d: tuple[int, int, int]):
+        if a == -1 or b == -1:
+            return
+        if (a, b, d) in seen:
+            return
+        seen.add((a, b, d))
+        conns.append((a, b, d))
+        rev = (b, a, (-d[0], -d[1], -d[2]))
+        seen.add(rev)
+        conns.append(rev)
+
+    n1, n2, n3 = seg.shape
+    for i in range(n1):
+        for j in range(n2):
+            note(int(seg[i, j, -1]), int(seg[i, j, 0]), (0, 0, 1))
+    for j in range(n2):
+        for k in range(n3):
+            note(int(seg[-1, j, k]), int(seg[0, j, k]), (1, 0, 0))
+    for i in range(n1):
+        for k in range(n3):
+            note(int(seg[i, -1, k]), int(seg[i, 0, k]), (0, 1, 0))
+    return conns
+
+
+def _simple_cycles(adj: dict[int, list[int]]):
+    """All simple cycles of a directed graph (Johnson's algorithm, 1975), each as a vertex list
+    starting at its smallest vertex."""
+    def scc_of(nodes: set[int]) -> list[set[int]]:
+        index, low, onstack, stack, out = {}, {}, set(), [], []
+        counter = [0]
+        for root in sorted(nodes):
+            if root in index:
+                continue
+            work = [(root, iter(adj.get(root, ())))]
+            index[root] = low[root] = counter[0]
+            counter[0] += 1
+            stack.append(root)
+            onstack.add(root)
+            while work:
+                v, it = work[-1]
+                advanced = False
+                for w in it:
+                    if w not in nodes:
+                        continue
+                    if w not in index:
+                        index[w] = low[w] = counter[0]
+                        counter[0] += 1
+                        stack.append(w)
+                        onstack.add(w)
+                        work.append((w, iter(adj.get(w, ()))))
+                        advanced = True
+                        break
+                    if w in onstack:
+                        low[v] = min(low[v], index[w])
+                if advanced:
+                    continue
+                work.pop()
+                if work:
+                    low[work[-1][0]] = min(low[work[-1][0]], low[v])
+                if low[v] == index[v]:
+                    comp = set()
+                    while True:
+                        w = stack.pop()
+                        onstack.discard(w)
+                        comp.add(w)
+                        if w == v:
+                            break
+                    out.append(comp)
+        return out
+
+    remaining = set(adj) | {w for ws in adj.values() for w in ws}
+    while remaining:
+        comps = [c for c in scc_of(remaining) if len(c) > 1 or any(v in adj.get(v, ()) for v in c)]
+        if not comps:
+            break
+        s = min(min(c) for c in comps)
+        comp = next(c for c in comps if s in c)
+        blocked, bmap, path = {s}, {}, [s]
+        stack = [(s, iter([w for w in adj.get(s, ()) if w in comp]))]
+        closed = [False]
+        while stack:
+            v, it = stack[-1]
+            nxt = next(it, None)
+            if nxt is not None:
+                if nxt == s:
+                    yield list(path)
+                    closed[-1] = True
+                elif nxt not in blocked:
+                    path.append(nxt)
+                    blocked.add(nxt)
+                    stack.append((nxt, iter([w for w in adj.get(nxt, ()) if w in comp])))
+                    closed.append(False)
+                continue
+            stack.pop()
+            done = closed.pop()
+            if done:
+                # unblock v and everything waiting on it
+                todo = [v]
+                while todo:
+                    u = todo.pop()
+                    if u in blocked:
+                        blocked.discard(u)
+                        todo.extend(bmap.pop(u, ()))
+            else:
+                for w in adj.get(v, ()):
+                    if w in comp:
+                        bmap.setdefault(w, set()).add(v)
+            path.pop()
+            if closed:
+                closed[-1] = closed[-1] or done
+        remaining.discard(s)
+
+
+def _classify_segments(n_segments: int, conns) -> np.ndarray:
+    """1 for segments on a simple cycle of the segment graph that ends in another unit cell
+    (src/grid.jl:548-616), 0 otherwise.  As in the reference, each connection is a vertex of
+    its own carrying the face it crosses."""
+    adj: dict[int, list[int]] = {v: [] for v in range(1, n_segments + 1)}
+    direction: dict[int, tuple[int, int, int]] = {}
+    for a, b, d in conns:
+        c = n_segments + 1 + len(direction)
+        direction[c] = d
+        adj.setdefault(a, []).append(c)
+        adj[c] = [b]
+    cls = np.zeros(n_segments + 1, dtype=np.int64)
+    for cyc in _simple_cycles(adj):
+        cell = np.zeros(3, dtype=np.int64)
+        for v in cyc:
+            if v in direction:
+                cell += direction[v]
+        if np.any(cell != 0):
+            for v in cyc:
+                if v not in direction:
+                    cls[v] = 1
+    # the reference then marks segments with a direct edge into an accessible one; every
+    # segment edge runs through a connection vertex, so that step adds nothing
+    return cls[1:]
+
+
+def compute_accessibility_grid(crystal: Crystal, probe: Molecule, forcefield: LJForceField, *,
+                               resolution=1.0, energy_tol: float = 10.0, energy_units="kJ_mol",
+                               verbose: bool = True, write_b4_after_grids: bool = True,
+                               block_inaccessible_pockets: bool = True):
+    """(accessibility Grid of Bool, nb_segments_blocked, porosity) of src/grid.jl:689-774: the
+    probe's energy grid (on the GPU), points below energy_tol occupiable, and with
+    block_inaccessible_pockets the occupiable regions that do not connect to their own images
+    in another unit cell blocked.  porosity is a float without blocking, else a dict with
+    'b4_blocking' and 'after_blocking'."""
+    assert_P1_symmetry(crystal)
+    units = _units(energy_units)
+    if verbose:
+        print(f"Computing accessibility grid of {crystal.name} using {energy_tol:f} {units} potential energy tol "
+              f"and {probe.species} probe...")
+    grid = energy_grid(crystal, probe, forcefield, resolution=resolution, verbose=verbose, units=units)
+    data = np.asarray(grid.data, dtype=np.float64)
+    if not block_inaccessible_pockets:
+        acc = Grid(grid.box, grid.n_pts, data < energy_tol, "accessibility", grid.origin)
+        return acc, 0, float(np.mean(acc.data))
+    seg, n_segments = _segment_grid(data, energy_tol)
+    if verbose:
+        print(f"Found {n_segments} segments")
+    name = crystal.name.replace(".cif", "").replace(".cssr", "")
+    ffname = forcefield.name.replace(".csv", "")
+    if write_b4_after_grids:
+        write_cube(Grid(grid.box, grid.n_pts, np.where(seg != -1, 1, -1), "Segment_No", grid.origin),
+                   f"{probe.species}_in_{name}_{ffname}_b4_pocket_blocking.cube", verbose=verbose)
+    cls = _classify_segments(n_segments, _segment_connections(seg))
+    for s in range(1, n_segments + 1):
+        if cls[s - 1] == 0:
+            seg[seg == s] = -1
+    out = np.where(seg != -1, 1, -1)
+    if write_b4_after_grids:
+        write_cube(Grid(grid.box, grid.n_pts, out, "Segment_No", grid.origin),
+                   f"{probe.species}_in_{name}_{ffname}_after_pocket_blocking.cube", verbose=verbose)
+    nb_blocked = int(np.sum(cls == 0))
+    acc = Grid(grid.box, grid.n_pts, out == 1, "accessibility", grid.origin)
+    porosity = {"b4_blocking": float(np.mean(data < energy_tol)), "after_blocking": float(np.mean(acc.data))}
+    if verbose and nb_blocked:
+        print(f"\t{nb_blocked} pockets in {crystal.name} were found to be inaccessible to {probe.species} "
+              f"and blocked.")
+    return acc, nb_blocked, porosity

@@ -82,3 +82,65 @@ def test_drop_in_with_accessibility_grid():
     with pytest.raises(ValueError, match="accessibility grid box"):
         pmgb.henry_coefficient(cr, synthetic.co2(), T, ff, insertions_per_volume=10, verbose=False,
                                autosave=False, accessibility_grid=wrong)
+
+
+# ---- compute_accessibility_grid: the reference's own expectations (test/grid.jl:43-146) ----
+def _uff_ch4():
+    return pmgb.LJForceField("UFF"), pmgb.read_molecule("CH4")
+
+
+@pytest.mark.parametrize("zeolite", ["LTA", "SOD"])
+def test_accessibility_grid_zeolites(zeolite):
+    ff, ch4 = _uff_ch4()
+    cr = pmgb.read_cif(f"{zeolite}.cif")
+    acc, nb, por = pmgb.compute_accessibility_grid(cr, ch4, ff, resolution=2.0, energy_tol=0.0, verbose=False,
+                                                   write_b4_after_grids=True)
+    print(f"[{zeolite}] blocked segments {nb}; porosity {por}")
+    assert nb > 0
+    if zeolite == "LTA":
+        assert nb == 8
+    assert por["b4_blocking"] > por["after_blocking"]
+    assert np.allclose(acc.box.f_to_c, cr.box.f_to_c)
+    if zeolite == "SOD":
+        assert not acc.data.any()
+    # random insertions: the gate with and without unit repfactors agree
+    xf = np.random.default_rng(3).random((20000, 3))
+    a1 = oracle.accessible(acc.data, xf, (1, 1, 1))
+    if zeolite == "SOD":
+        assert not a1.any()
+    acc_nb, nb_nb, por_nb = pmgb.compute_accessibility_grid(cr, ch4, ff, resolution=2.0, energy_tol=0.0,
+                                                            verbose=False, write_b4_after_grids=False,
+                                                            block_inaccessible_pockets=False)
+    assert nb_nb == 0
+    assert por_nb > por["after_blocking"]
+    assert por_nb == pytest.approx(por["b4_blocking"])
+
+
+def test_accessibility_grid_replication():
+    ff, ch4 = _uff_ch4()
+    cr = pmgb.read_cif("LTA.cif")
+    acc, nb, _ = pmgb.compute_accessibility_grid(cr, ch4, ff, resolution=2.0, energy_tol=0.0, verbose=False,
+                                                 write_b4_after_grids=False)
+    rep = (2, 3, 1)
+    rep_acc, rep_nb, _ = pmgb.compute_accessibility_grid(pmgb.replicate(cr, rep), ch4, ff, resolution=2.0,
+                                                         energy_tol=0.0, verbose=False, write_b4_after_grids=False)
+    assert np.array_equal(acc.data, rep_acc.data[:7, :7, :7])
+    assert rep_nb > 0
+    xf = np.random.default_rng(4).random((10000, 3))
+    np.testing.assert_array_equal(oracle.accessible(rep_acc.data, xf, (1, 1, 1)),
+                                  oracle.accessible(acc.data, xf, rep))
+
+
+@pytest.mark.parametrize("name", ["SBMOF-1", "CAXVII_clean"])
+def test_accessibility_grid_no_pockets(name):
+    ff, ch4 = _uff_ch4()
+    cr = pmgb.read_cif(f"{name}.cif")
+    acc, nb, por = pmgb.compute_accessibility_grid(cr, ch4, ff, energy_tol=5.0, verbose=False,
+                                                   write_b4_after_grids=True, energy_units="kJ_mol")
+    assert nb == 0
+    acc_nb, nb_nb, por_nb = pmgb.compute_accessibility_grid(cr, ch4, ff, energy_tol=5.0, verbose=False,
+                                                            energy_units="kJ_mol", write_b4_after_grids=True,
+                                                            block_inaccessible_pockets=False)
+    assert por_nb == pytest.approx(por["b4_blocking"])
+    assert nb_nb == 0
+    assert np.array_equal(acc.data, acc_nb.data)
