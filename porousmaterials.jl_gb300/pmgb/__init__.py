@@ -12,6 +12,7 @@ from .energetics import (Eikr, EwaldSum, PotentialEnergy, electrostatic_potentia
                          guest_host_energies, total, vdw_energy)
 from .ewald import (EPS0, FOUR_PI_EPS0, EwaldParams, determine_ewald_params, precompute_kvec_wts,
                     required_kreps, setup_Ewald_sum)
+from .energy_min import find_energy_minimum, find_energy_minimum_gridsearch
 from .forcefield import LJForceField, forcefield_coverage, replication_factors
 from .grid import (Grid, accessible, compute_accessibility_grid, energy_grid, id_to_xf, read_cube,
                    required_n_pts, write_cube, xf_to_id)

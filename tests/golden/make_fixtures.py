@@ -16,7 +16,7 @@ OUT = Path(__file__).resolve().parent / "data"
 
 FILES = {
     "crystals": ["SBMOF-1.cif", "NU-1000_Greg.cif", "zif71_bogus_charges.cif", "test_structure.cif",
-                 "LTA.cif", "SOD.cif", "CAXVII_clean.cif"],
+                 "LTA.cif", "SOD.cif", "CAXVII_clean.cif", "FIQCEN_clean.cif", "cage_in_space.cif"],
     "forcefields": ["Dreiding.csv", "UFF.csv", "Greg_bogus_ZIF71.csv", "NIST.csv"],
     "molecules": ["Xe", "CO2", "CH4", "CO2EPM2", "X", "He"],
 }
