@@ -267,6 +267,12 @@ int pmgb_batch_tune(pmgb_batch* batch, uint64_t seed, double temperature, int32_
  * (0: off, the default).  Allocates per-insertion scratch on first use and re-captures the graph. */
 int pmgb_batch_set_refine(pmgb_batch* batch, double tail_fraction);
 
+/* Spatially ordered processing with cutoff culling, as pmgb_system_set_cull (on by default):
+ * each (system, block)'s insertions are sorted into 16^3 Z-ordered cells of the unit cell, and
+ * block results are formed from the per-insertion energies in insertion order, so they equal
+ * those of an unordered run bit for bit.  Allocates scratch on first use and re-captures. */
+int pmgb_batch_set_cull(pmgb_batch* batch, int32_t on);
+
 /* Insertions of each system the last run re-evaluated in FP64 (n_systems values; synchronises). */
 int pmgb_batch_refined_counts(pmgb_batch* batch, int64_t* per_system);
 

@@ -1482,6 +1482,11 @@ struct pmgb_batch {
     double* d_ref_u = nullptr;
     int *d_plan = nullptr, *d_done = nullptr;
     double* d_part = nullptr;
+    // spatial order with cutoff culling (off: insertions in index order)
+    bool cull = false;
+    int* d_perm = nullptr;
+    int* d_cells = nullptr;
+    double* d_unit_m = nullptr;
     cudaGraphExec_t exec = nullptr;
     bool launched = false;
 };
@@ -1494,7 +1499,7 @@ void batch_free(pmgb_batch* b) {
     void* ptrs[] = {b->d_sys, b->d_units, b->d_order, b->d_counter, b->d_run, b->d_partials,
                     b->d_dsum, b->d_unit_cols, b->d_block_out, b->d_out_cols, b->d_chunk_sys, b->d_u,
                     b->d_hist, b->d_cut, b->d_counts, b->d_offsets, b->d_list, b->d_ref_u,
-                    b->d_plan, b->d_done, b->d_part};
+                    b->d_plan, b->d_done, b->d_part, b->d_perm, b->d_cells, b->d_unit_m};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -1527,7 +1532,9 @@ int batch_capture(pmgb_batch* b) {
     a.dsum = b->d_dsum;
     a.max_cols = b->max_cols;
     a.unit_cols = b->d_unit_cols;
-    a.u = b->refine_tail > 0.0 ? b->d_u : nullptr;
+    a.u = (b->refine_tail > 0.0 || b->cull) ? b->d_u : nullptr;
+    a.perm = b->cull ? b->d_perm : nullptr;
+    a.unit_m = b->cull ? b->d_unit_m : nullptr;
     RefineArgs r{};
     if (b->refine_tail > 0.0) {
         r.systems = b->d_sys;
@@ -1554,11 +1561,17 @@ int batch_capture(pmgb_batch* b) {
     }
     cudaStream_t st = ctx->stream;
     PMGB_CK(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int n_sys = static_cast<int>(b->systems.size()), n_chunks = static_cast<int>(b->n_chunks);
     cudaError_t e = cudaMemsetAsync(b->d_counter, 0, sizeof(int), st);
+    if (e == cudaSuccess && b->cull)
+        e = pmgb_launch_batch_order(b->d_sys, b->d_chunk_sys, n_chunks, n_sys, b->n_blocks, b->d_run, b->d_cells,
+                                    b->d_perm, st);
     if (e == cudaSuccess) e = pmgb_launch_batch(a, b->grad, b->n_ctas, st);
+    if (e == cudaSuccess && b->cull)
+        e = pmgb_launch_batch_lse(b->d_sys, b->d_chunk_sys, n_chunks, b->d_run, b->d_u, b->d_partials, st);
     if (e == cudaSuccess)
-        e = pmgb_launch_batch_reduce(b->d_sys, static_cast<int>(b->systems.size()), b->n_blocks, b->d_partials,
-                                     b->d_unit_cols, b->grad, b->d_block_out, b->d_out_cols, st);
+        e = pmgb_launch_batch_reduce(b->d_sys, n_sys, b->n_blocks, b->d_partials, b->d_unit_cols, a.unit_m, b->grad,
+                                     b->d_block_out, b->d_out_cols, st);
     if (e == cudaSuccess && b->refine_tail > 0.0)
         e = pmgb_launch_refine(r, static_cast<int>(b->n_chunks), b->sm_count, st);
     cudaGraph_t g = nullptr;
@@ -1601,6 +1614,27 @@ int batch_build_units(pmgb_batch* b, double unit_mflop, int order) {
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // idx is a local
     b->order = order;
     b->unit_mflop = unit_mflop;
+    return PMGB_OK;
+}
+
+// Per-insertion energies and the chunk -> system map, shared by the refinement and the
+// spatial order; allocated on first use.
+int batch_ensure_u(pmgb_batch* b) {
+    if (b->d_u) return PMGB_OK;
+    pmgb_ctx* ctx = b->ctx;
+    std::vector<int> chunk_sys(static_cast<size_t>(b->n_chunks));
+    for (size_t i = 0; i < b->host_sys.size(); ++i) {
+        const BatchSystem& bs = b->host_sys[i];
+        const int64_t n_c = static_cast<int64_t>(bs.ctas_per_block) * b->n_blocks;
+        for (int64_t c = 0; c < n_c; ++c) chunk_sys[bs.chunk_first + c] = static_cast<int>(i);
+    }
+    int rc;
+    if ((rc = batch_alloc(b, &b->d_chunk_sys, chunk_sys.size())) ||
+        (rc = batch_alloc(b, &b->d_u, 2 * static_cast<size_t>(b->n_insertions))))
+        return rc;
+    PMGB_CK(ctx, cudaMemcpyAsync(b->d_chunk_sys, chunk_sys.data(), sizeof(int) * chunk_sys.size(),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // chunk_sys is a local
     return PMGB_OK;
 }
 
@@ -1698,7 +1732,7 @@ extern "C" int pmgb_batch_create(pmgb_ctx* ctx, int32_t n_systems, pmgb_system* 
         if (e != cudaSuccess) rc = cuda_fail(ctx, e, "pmgb_batch_create: upload");
     }
     if (!rc) rc = batch_build_units(b, 0.0, 0);  // synchronises: the upload above reads host_sys
-    if (!rc) rc = batch_capture(b);
+    if (!rc) rc = pmgb_batch_set_cull(b, 1);      // on by default, as for a system; captures the graph
     if (rc) {
         batch_free(b);
         delete b;
@@ -1740,28 +1774,37 @@ extern "C" int pmgb_batch_set_refine(pmgb_batch* b, double tail_fraction) {
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_batch_set_refine: tail fraction in [0, 1)");
     PMGB_CK(ctx, cudaSetDevice(ctx->device));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
-    if (tail_fraction > 0.0 && !b->d_u) {
+    if (tail_fraction > 0.0 && !b->d_hist) {
         // scratch sized for the worst case: every insertion refined
         const size_t n = static_cast<size_t>(b->n_insertions), g = b->systems.size() * b->n_blocks;
-        std::vector<int> chunk_sys(static_cast<size_t>(b->n_chunks));
-        for (size_t i = 0; i < b->host_sys.size(); ++i) {
-            const BatchSystem& bs = b->host_sys[i];
-            const int64_t n_c = static_cast<int64_t>(bs.ctas_per_block) * b->n_blocks;
-            for (int64_t c = 0; c < n_c; ++c) chunk_sys[bs.chunk_first + c] = static_cast<int>(i);
-        }
+        const size_t n_chunks = static_cast<size_t>(b->n_chunks);
         int rc;
-        if ((rc = batch_alloc(b, &b->d_chunk_sys, chunk_sys.size())) || (rc = batch_alloc(b, &b->d_u, 2 * n)) ||
-            (rc = batch_alloc(b, &b->d_hist, g * pmgb_refine_hist_words())) || (rc = batch_alloc(b, &b->d_cut, g)) ||
-            (rc = batch_alloc(b, &b->d_counts, chunk_sys.size())) ||
-            (rc = batch_alloc(b, &b->d_offsets, chunk_sys.size() + 2)) || (rc = batch_alloc(b, &b->d_list, n)) ||
+        if ((rc = batch_ensure_u(b)) || (rc = batch_alloc(b, &b->d_hist, g * pmgb_refine_hist_words())) ||
+            (rc = batch_alloc(b, &b->d_cut, g)) || (rc = batch_alloc(b, &b->d_counts, n_chunks)) ||
+            (rc = batch_alloc(b, &b->d_offsets, n_chunks + 2)) || (rc = batch_alloc(b, &b->d_list, n)) ||
             (rc = batch_alloc(b, &b->d_ref_u, 3 * n)) || (rc = batch_alloc(b, &b->d_plan, b->systems.size() + 2)) ||
             (rc = batch_alloc(b, &b->d_done, n)) || (rc = batch_alloc(b, &b->d_part, 4 * (2 * n + 4096))))
             return rc;
-        PMGB_CK(ctx, cudaMemcpyAsync(b->d_chunk_sys, chunk_sys.data(), sizeof(int) * chunk_sys.size(),
-                                     cudaMemcpyHostToDevice, ctx->stream));
-        PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // chunk_sys is a local
     }
     b->refine_tail = tail_fraction;
+    b->launched = false;
+    return batch_capture(b);
+}
+
+extern "C" int pmgb_batch_set_cull(pmgb_batch* b, int32_t on) {
+    if (!b) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = b->ctx;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (on && !b->d_perm) {
+        const size_t cells = b->systems.size() * b->n_blocks * pmgb_batch_order_cells();
+        int rc;
+        if ((rc = batch_ensure_u(b)) || (rc = batch_alloc(b, &b->d_perm, static_cast<size_t>(b->n_insertions))) ||
+            (rc = batch_alloc(b, &b->d_cells, cells)) ||
+            (b->grad && (rc = batch_alloc(b, &b->d_unit_m, static_cast<size_t>(b->n_chunks)))))
+            return rc;
+    }
+    b->cull = on != 0;
     b->launched = false;
     return batch_capture(b);
 }

@@ -53,6 +53,7 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) batch_kernel(const __grid_con
     __shared__ LsePartial red[PMGB_THREADS / 32];
     __shared__ __align__(16) BatchSystem s_bs;
     __shared__ double s_m;
+    __shared__ double s_wm[PMGB_THREADS / 32];
     __shared__ double s_w[GRAD ? PMGB_THREADS : 1];
     __shared__ int s_unit;
     const int tid = threadIdx.x;
@@ -82,15 +83,19 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) batch_kernel(const __grid_con
             UnitIO io{};
             io.pose_mode = POSE_PHILOX;
             io.out_mode = OUT_WIDOM;
-            const long long within = static_cast<long long>(chunk) * PMGB_THREADS + tid;
-            io.valid = within < npb;
+            const long long slot_in_block = static_cast<long long>(chunk) * PMGB_THREADS + tid;
+            io.valid = slot_in_block < npb;
+            long long within = slot_in_block;
+            if (b.perm && io.valid)
+                within = b.perm[s_bs.u_base + static_cast<long long>(unit.block) * npb + slot_in_block];
             io.item = static_cast<long long>(unit.block) * npb + within;
+            io.cull = b.perm != nullptr;
             io.seed = run.seed + static_cast<unsigned long long>(unit.system) * 0x9E3779B97F4A7C15ull;
             io.inv_temperature = run.inv_temperature;
             io.dsum = my_dsum;
             io.dsum_stride = PMGB_THREADS;
             io.col_item = tid;
-            io.partial = b.partials + slot;
+            io.partial = b.perm ? nullptr : b.partials + slot;
             io.u_out = b.u ? b.u + 2 * s_bs.u_base : nullptr;
             io.resident = fits && c > 0;
             double x = -inf;
@@ -98,6 +103,20 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) batch_kernel(const __grid_con
             io.m_out = &s_m;
             if (!run_variant<GRAD>(s_bs.variant, s_bs.sys, io, stage, bars, red, fills, b.status)) return;
             if (GRAD) {
+                if (b.perm) {
+                    // this processing chunk's own max of -U/T (the partials come from u later)
+                    double m = x;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+                    if ((tid & 31) == 0) s_wm[tid >> 5] = m;
+                    __syncthreads();
+                    if (tid == 0) {
+                        double mm = s_wm[0];
+                        for (int w = 1; w < PMGB_THREADS / 32; ++w) mm = fmax(mm, s_wm[w]);
+                        s_m = mm;
+                        b.unit_m[slot] = mm;
+                    }
+                }
                 __syncthreads();  // s_m and every thread's columns are written
                 const double M = s_m;
                 s_w[tid] = (x == -inf || M == -inf) ? 0.0 : exp(x - M);
@@ -129,7 +148,8 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) batch_kernel(const __grid_con
 // combined columns relative to m = max over the system's chunks of max -U/T.
 __global__ void batch_reduce_kernel(const BatchSystem* __restrict__ systems, int n_blocks,
                                     const LsePartial* __restrict__ partials, const double* __restrict__ unit_cols,
-                                    bool grad, double* __restrict__ block_out, double* __restrict__ out_cols) {
+                                    const double* __restrict__ unit_m, bool grad, double* __restrict__ block_out,
+                                    double* __restrict__ out_cols) {
     const int s = blockIdx.x;
     const BatchSystem& bs = systems[s];
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
@@ -191,7 +211,10 @@ __global__ void batch_reduce_kernel(const BatchSystem* __restrict__ systems, int
         }
         double v = 0.0;
         for (int k = 0; k < n_units; ++k) {
-            const double f = (M == -inf || p[k].m == -inf) ? 0.0 : exp(p[k].m - M);
+            // columns were weighted relative to their processing chunk's max (unit_m with a spatial
+            // order, else the same chunk's partial)
+            const double mk = (e >= 3 && unit_m) ? unit_m[bs.chunk_first + k] : p[k].m;
+            const double f = (M == -inf || mk == -inf) ? 0.0 : exp(mk - M);
             if (f == 0.0) continue;
             const double x = (e == 1) ? p[k].s : (e == 2) ? p[k].te : unit_cols[bs.col_base + static_cast<size_t>(k) * nc + (e - 3)];
             v = fma(f, x, v);
@@ -200,7 +223,132 @@ __global__ void batch_reduce_kernel(const BatchSystem* __restrict__ systems, int
     }
 }
 
+// ---- spatial order of a batch ------------------------------------------------------------
+constexpr int kBatchOrderBits = 4;                           // 16 cells per axis
+constexpr int kBatchOrderCells = 1 << (3 * kBatchOrderBits);  // 4096
+
+__device__ __forceinline__ int batch_cell(unsigned long long seed, unsigned long long idx) {
+    const uint2 key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+    const uint4 a = philox4x32_10(make_uint4(static_cast<uint32_t>(idx), static_cast<uint32_t>(idx >> 32), 0u, 0u), key);
+    const uint32_t cx = a.x >> (32 - kBatchOrderBits), cy = a.y >> (32 - kBatchOrderBits),
+                   cz = a.z >> (32 - kBatchOrderBits);
+    int code = 0;
+#pragma unroll
+    for (int bit = 0; bit < kBatchOrderBits; ++bit)
+        code |= static_cast<int>(((cx >> bit) & 1u) << (3 * bit) | ((cy >> bit) & 1u) << (3 * bit + 1) |
+                                 ((cz >> bit) & 1u) << (3 * bit + 2));
+    return code;
+}
+
+struct ChunkRef {
+    int sys, blk;
+    long long within, npb;
+    bool valid;
+};
+
+__device__ __forceinline__ ChunkRef chunk_ref(const BatchSystem* systems, const int* chunk_sys, int c, int tid) {
+    ChunkRef r;
+    r.sys = chunk_sys[c];
+    const BatchSystem& bs = systems[r.sys];
+    const int local = c - bs.chunk_first;
+    r.blk = local / bs.ctas_per_block;
+    r.within = static_cast<long long>(local % bs.ctas_per_block) * PMGB_THREADS + tid;
+    r.npb = bs.n_per_block;
+    r.valid = r.within < r.npb;
+    return r;
+}
+
+__global__ void batch_order_count_kernel(const BatchSystem* systems, const int* chunk_sys, int n_blocks,
+                                         const BatchRun* run, int* counts) {
+    const ChunkRef r = chunk_ref(systems, chunk_sys, blockIdx.x, threadIdx.x);
+    if (!r.valid) return;
+    const unsigned long long seed = run->seed + static_cast<unsigned long long>(r.sys) * 0x9E3779B97F4A7C15ull;
+    const int cell = batch_cell(seed, static_cast<unsigned long long>(r.blk * r.npb + r.within));
+    atomicAdd(&counts[(static_cast<size_t>(r.sys) * n_blocks + r.blk) * kBatchOrderCells + cell], 1);
+}
+
+// exclusive scan of one (system, block)'s 4096 cell counts
+__global__ void __launch_bounds__(1024) batch_order_scan_kernel(int* counts) {
+    __shared__ int part[1024];
+    int* c = counts + static_cast<size_t>(blockIdx.x) * kBatchOrderCells;
+    constexpr int per = kBatchOrderCells / 1024;
+    const int t = threadIdx.x;
+    int v[per], sum = 0;
+#pragma unroll
+    for (int q = 0; q < per; ++q) {
+        v[q] = c[t * per + q];
+        sum += v[q];
+    }
+    part[t] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int add = (t >= o) ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += add;
+        __syncthreads();
+    }
+    int run = part[t] - sum;
+#pragma unroll
+    for (int q = 0; q < per; ++q) {
+        c[t * per + q] = run;
+        run += v[q];
+    }
+}
+
+__global__ void batch_order_scatter_kernel(const BatchSystem* systems, const int* chunk_sys, int n_blocks,
+                                           const BatchRun* run, int* offsets, int* perm) {
+    const ChunkRef r = chunk_ref(systems, chunk_sys, blockIdx.x, threadIdx.x);
+    if (!r.valid) return;
+    const unsigned long long seed = run->seed + static_cast<unsigned long long>(r.sys) * 0x9E3779B97F4A7C15ull;
+    const int cell = batch_cell(seed, static_cast<unsigned long long>(r.blk * r.npb + r.within));
+    const int pos = atomicAdd(&offsets[(static_cast<size_t>(r.sys) * n_blocks + r.blk) * kBatchOrderCells + cell], 1);
+    perm[systems[r.sys].u_base + r.blk * r.npb + pos] = static_cast<int>(r.within);
+}
+
+// per-chunk log-sum-exp partials in insertion order (what the kernel forms without a spatial order)
+__global__ void __launch_bounds__(PMGB_THREADS) batch_lse_kernel(const BatchSystem* systems, const int* chunk_sys,
+                                                                const BatchRun* run, const double* __restrict__ u,
+                                                                LsePartial* __restrict__ partials) {
+    __shared__ LsePartial red[PMGB_THREADS / 32];
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    const ChunkRef r = chunk_ref(systems, chunk_sys, blockIdx.x, threadIdx.x);
+    double x = -inf, ev = 0.0, ee = 0.0;
+    long long ninf = 0;
+    if (r.valid) {
+        const long long ui = systems[r.sys].u_base + r.blk * r.npb + r.within;
+        const double uv = u[2 * ui], ues = u[2 * ui + 1];
+        const double uu = uv + ues;
+        if (isfinite(uu)) {
+            x = -uu * run->inv_temperature;
+            ev = uv;
+            ee = ues;
+        } else {
+            ninf = 1;
+        }
+    }
+    lse_cta(x, ev, ee, ninf, red, partials + blockIdx.x, nullptr);
+}
+
 }  // namespace
+
+size_t pmgb_batch_order_cells() { return kBatchOrderCells; }
+
+cudaError_t pmgb_launch_batch_order(const BatchSystem* systems, const int* chunk_sys, int n_chunks, int n_systems,
+                                    int n_blocks, const BatchRun* run, int* counts, int* perm, cudaStream_t st) {
+    const size_t n_counts = static_cast<size_t>(n_systems) * n_blocks * kBatchOrderCells;
+    cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * n_counts, st);
+    if (e != cudaSuccess) return e;
+    batch_order_count_kernel<<<n_chunks, PMGB_THREADS, 0, st>>>(systems, chunk_sys, n_blocks, run, counts);
+    batch_order_scan_kernel<<<n_systems * n_blocks, 1024, 0, st>>>(counts);
+    batch_order_scatter_kernel<<<n_chunks, PMGB_THREADS, 0, st>>>(systems, chunk_sys, n_blocks, run, counts, perm);
+    return cudaGetLastError();
+}
+
+cudaError_t pmgb_launch_batch_lse(const BatchSystem* systems, const int* chunk_sys, int n_chunks, const BatchRun* run,
+                                  const double* u, LsePartial* partials, cudaStream_t st) {
+    batch_lse_kernel<<<n_chunks, PMGB_THREADS, 0, st>>>(systems, chunk_sys, run, u, partials);
+    return cudaGetLastError();
+}
 
 int pmgb_batch_variant(int n_sites, bool charged) {
     for (int i = 0; i < 6; ++i)
@@ -222,9 +370,10 @@ cudaError_t pmgb_launch_batch(const BatchArgs& b, bool grad, int n_ctas, cudaStr
 }
 
 cudaError_t pmgb_launch_batch_reduce(const BatchSystem* systems, int n_systems, int n_blocks,
-                                     const LsePartial* partials, const double* unit_cols, bool grad,
-                                     double* block_out, double* out_cols, cudaStream_t st) {
+                                     const LsePartial* partials, const double* unit_cols, const double* unit_m,
+                                     bool grad, double* block_out, double* out_cols, cudaStream_t st) {
     if (n_systems <= 0) return cudaSuccess;
-    batch_reduce_kernel<<<n_systems, 128, 0, st>>>(systems, n_blocks, partials, unit_cols, grad, block_out, out_cols);
+    batch_reduce_kernel<<<n_systems, 128, 0, st>>>(systems, n_blocks, partials, unit_cols, unit_m, grad, block_out,
+                                                   out_cols);
     return cudaGetLastError();
 }

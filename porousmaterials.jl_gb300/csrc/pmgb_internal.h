@@ -204,6 +204,10 @@ struct BatchArgs {
     int max_cols;
     double* unit_cols;        // per-chunk weighted column sums, weights exp(-U/T - m_chunk)
     double* u;                // optional: per-insertion (U_vdw, U_es), system s at 2 * u_base
+    // spatial order (optional): perm[u_base + block * n_per_block + slot] = insertion within the
+    // block evaluated in that slot; the partials are then formed from u in insertion order
+    const int* perm;
+    double* unit_m;           // adjoint with perm: the max of -U/T of each processing chunk
 };
 
 // ---- FP64 refinement of the Boltzmann tail (pmgb_refine.cu) ---------------------------
@@ -249,8 +253,15 @@ cudaError_t pmgb_launch_batch(const BatchArgs& b, bool grad, int n_ctas, cudaStr
 // per system: block_out[(s * n_blocks + b) * 4 ..] and, with grad, the combined columns
 // out_cols[out_base ..] = (m, sum w, sum w U_es, sum w col_0, ...), w = exp(-U/T - m)
 cudaError_t pmgb_launch_batch_reduce(const BatchSystem* systems, int n_systems, int n_blocks,
-                                     const LsePartial* partials, const double* unit_cols, bool grad,
-                                     double* block_out, double* out_cols, cudaStream_t st);
+                                     const LsePartial* partials, const double* unit_cols, const double* unit_m,
+                                     bool grad, double* block_out, double* out_cols, cudaStream_t st);
+// Spatial order of every system's insertions (16^3 Z-order cells per (system, block)) and the
+// insertion-order partials of a culled batch run; chunk_sys maps chunks to systems.
+size_t pmgb_batch_order_cells();
+cudaError_t pmgb_launch_batch_order(const BatchSystem* systems, const int* chunk_sys, int n_chunks, int n_systems,
+                                    int n_blocks, const BatchRun* run, int* counts, int* perm, cudaStream_t st);
+cudaError_t pmgb_launch_batch_lse(const BatchSystem* systems, const int* chunk_sys, int n_chunks, const BatchRun* run,
+                                  const double* u, LsePartial* partials, cudaStream_t st);
 cudaError_t pmgb_launch_reduce_blocks(const LsePartial* partials, int n_blocks, int ctas_per_block,
                                       double* block_out, cudaStream_t st);
 // qxf: framework charge fractional coordinates (FP64, 3 per charge)

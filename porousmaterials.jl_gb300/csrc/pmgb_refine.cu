@@ -283,15 +283,22 @@ __device__ void energy_fp64_warp_part(const SysDev& S, const double (*xs)[3], in
 }
 
 // FP64 work units of one insertion (pair terms + reciprocal-space terms).  Small insertions are
-// evaluated by one thread each; the others are cut into chunks of ~4096 units (records and
-// k-space half-rows in proportion), one warp per chunk, so that one large insertion spreads over
-// many SMs instead of waiting on one warp's FP64 latency.
+// evaluated by one thread each; the others are cut into chunks (records and k-space half-rows in
+// proportion), one warp per chunk, so that one large insertion spreads over many SMs instead of
+// waiting on one warp's FP64 latency.  The chunk size adapts to the system's number of refined
+// insertions: ~1024 units while its chunk-items stay within 4096 (a few insertions: the pass is
+// latency-bound, finer chunks fill more SMs), else ~4096 units (many insertions: fewer partials
+// and less per-chunk overhead).  The count is the same for a system alone or in a batch, so the
+// two evaluate identical chunks.
 __device__ __forceinline__ long long fp64_work(const SysDev& S) {
     return static_cast<long long>(S.n_sites) * (S.n_rec + (S.charged ? S.n_k : 0));
 }
 __device__ __forceinline__ bool small_system(const SysDev& S) { return fp64_work(S) <= 512; }
-__device__ __forceinline__ int fp64_chunks(const SysDev& S) {
-    return small_system(S) ? 0 : static_cast<int>(min(64ll, (fp64_work(S) + 4095) / 4096));
+__device__ __forceinline__ int fp64_chunks(const SysDev& S, long long count) {
+    if (small_system(S)) return 0;
+    const long long fine = min(64ll, (fp64_work(S) + 1023) / 1024);
+    if (count * fine <= 4096) return static_cast<int>(fine);
+    return static_cast<int>(min(64ll, (fp64_work(S) + 4095) / 4096));
 }
 
 __device__ __forceinline__ void refined_entry(const RefineArgs& a, long long e, const SysDev*& S, double (*xs)[3]) {
@@ -359,8 +366,9 @@ __global__ void __launch_bounds__(1024) refine_plan_kernel(const __grid_constant
             long long items = 0;
             if (sys < a.n_systems) {
                 const SysDev& S = a.systems ? a.systems[sys].sys : a.sys;
-                const int c = fp64_chunks(S);
-                items = static_cast<long long>(system_entry_count(a, sys, n_ctas)) * (one_chunk && c ? 1 : c);
+                const long long count = system_entry_count(a, sys, n_ctas);
+                const int c = fp64_chunks(S, count);
+                items = count * (one_chunk && c ? 1 : c);
             }
             part[threadIdx.x] = items;
             __syncthreads();
@@ -409,7 +417,7 @@ __global__ void __launch_bounds__(PMGB_THREADS) refine_large_kernel(const __grid
         }
         const int sys = lo;
         const SysDev& S = a.systems ? a.systems[sys].sys : a.sys;
-        const int C = a.one_chunk[0] ? 1 : fp64_chunks(S);
+        const int C = a.one_chunk[0] ? 1 : fp64_chunks(S, system_entry_count(a, sys, n_ctas));
         const int local = i - a.plan[sys];
         const int r = system_entry_first(a, sys) + local / C;
         const int c = local % C;

@@ -69,6 +69,7 @@ SIGNATURES = [
     ("pmgb_batch_configure", C.c_int, [_vp, C.c_int32, C.c_int32, C.c_double]),
     ("pmgb_batch_tune", C.c_int, [_vp, C.c_uint64, C.c_double, C.c_int32, _dp]),
     ("pmgb_batch_set_refine", C.c_int, [_vp, C.c_double]),
+    ("pmgb_batch_set_cull", C.c_int, [_vp, C.c_int32]),
     ("pmgb_batch_refined_counts", C.c_int, [_vp, C.POINTER(C.c_int64)]),
     ("pmgb_batch_launch", C.c_int, [_vp, C.c_uint64, C.c_double]),
     ("pmgb_batch_results", C.c_int, [_vp, _dp, _dp]),

@@ -37,7 +37,7 @@ class BatchScreen:
     """pmgb_batch handle over a list of GPUSystems (kept alive by this object)."""
 
     def __init__(self, systems: list[GPUSystem], n_per_block, n_blocks: int = 5, with_adjoint: bool = False,
-                 ctx: Context | None = None, refine_tail: float = 0.0):
+                 ctx: Context | None = None, refine_tail: float = 0.0, cull: bool = True):
         if not systems:
             raise ValueError("BatchScreen needs at least one system")
         self.ctx = ctx or systems[0].ctx
@@ -54,13 +54,21 @@ class BatchScreen:
         self.handle = h.value
         self._n_species = [len(s.species) for s in systems]
         self.refine_tail = 0.0
+        self.cull = True  # the library's default
         if refine_tail:
             self.set_refine(refine_tail)
+        if not cull:
+            self.set_cull(False)
 
     def set_refine(self, tail_fraction: float) -> None:
         """FP64 refinement of the Boltzmann tail of every system (see pmgb_batch_set_refine)."""
         self.ctx.check(self.ctx._lib.pmgb_batch_set_refine(self.handle, float(tail_fraction)))
         self.refine_tail = float(tail_fraction)
+
+    def set_cull(self, on: bool) -> None:
+        """Spatially ordered processing with cutoff culling (see pmgb_batch_set_cull)."""
+        self.ctx.check(self.ctx._lib.pmgb_batch_set_cull(self.handle, int(bool(on))))
+        self.cull = bool(on)
 
     def close(self):
         if getattr(self, "handle", None):

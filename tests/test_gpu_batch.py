@@ -150,6 +150,48 @@ def test_batch_refine_matches_single_system(mixed_systems):
     assert screen.ctx.device_status() == 0
 
 
+def test_batch_cull_matches_unordered(mixed_systems):
+    """Spatial order + cutoff culling: block results equal the unordered run's bit for bit
+    (ragged counts, several unit shapes, with and without the FP64 refinement)."""
+    npb = [1 + 251 * i for i in range(len(mixed_systems))]
+    seed = 31
+    plain = BatchScreen(mixed_systems, npb, 5, cull=False)
+    base, _ = plain.run(seed, T)
+    culled = BatchScreen(mixed_systems, npb, 5)
+    for n_ctas, order, mflop in ((0, 0, 0.0), (5, 1, 64.0), (0, 0, 1e6)):
+        culled.configure(n_ctas, order, mflop)
+        got, _ = culled.run(seed, T)
+        np.testing.assert_array_equal(got, base)
+    plain.set_refine(1e-3)
+    culled.set_refine(1e-3)
+    np.testing.assert_array_equal(culled.run(seed, T)[0], plain.run(seed, T)[0])
+    np.testing.assert_array_equal(culled.refined_counts(), plain.refined_counts())
+    culled.set_cull(False)
+    np.testing.assert_array_equal(culled.run(seed, T)[0], plain.run(seed, T)[0])
+    assert culled.ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("unit_mflop", [0.0, 64.0])
+def test_batch_cull_adjoint(mixed_systems, unit_mflop):
+    """With culling, the adjoint's columns are weighted relative to each processing chunk's own
+    maximum: same blocks, gradients equal to 1e-9 relative."""
+    npb, nb, seed = 600, 5, 4321
+    plain = BatchScreen(mixed_systems, npb, nb, with_adjoint=True, cull=False)
+    culled = BatchScreen(mixed_systems, npb, nb, with_adjoint=True)
+    culled.configure(0, 0, unit_mflop)
+    b0, a0 = plain.run(seed, T)
+    b1, a1 = culled.run(seed, T)
+    np.testing.assert_array_equal(b1, b0)
+    for s, gs in enumerate(mixed_systems):
+        got = henry_gradients(gs, b1[s], a1[s], T, npb)
+        want = henry_gradients(gs, b0[s], a0[s], T, npb)
+        for g, w in zip(got[:2], want[:2]):
+            scale = max(abs(v) for v in w.values())
+            for sp in w:
+                assert g[sp] == pytest.approx(w[sp], rel=1e-9, abs=1e-12 * scale), (s, sp)
+        assert got[2] == pytest.approx(want[2], rel=1e-9, abs=1e-12 * abs(want[2]) + 1e-300)
+
+
 def test_screen_driver(mixed_systems):
     res = henry_coefficient_screen(None, None, T, synthetic.forcefield(), insertions=1000, seed=8,
                                    systems=mixed_systems, tune=False, refine_tail=0.0)
