@@ -99,8 +99,11 @@ int pmgb_system_set_ewald(pmgb_system* sys, double alpha, double sr_cutoff,
 void pmgb_system_destroy(pmgb_system* sys);
 
 /* Sizes of the device-resident system: out[0..5] = (framework records incl. padding,
- * species segments, k-vectors, k-rows, guest sites, bytes copied host->device when the
- * system and its Ewald state were built).  No reference counterpart (diagnostics). */
+ * species segments, k-vectors given, k-vectors evaluated, guest sites, bytes copied
+ * host->device when the system and its Ewald state were built).  Fewer k-vectors are
+ * evaluated than given when the framework is a replicated cell: S(k) then vanishes for
+ * every k that is not a multiple of the replication factors, and those are skipped.
+ * No reference counterpart (diagnostics). */
 int pmgb_system_info(const pmgb_system* sys, int64_t* out6);
 
 /* Number of guest sites and, for each site, the guest atom / guest charge it carries

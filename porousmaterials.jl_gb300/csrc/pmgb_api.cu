@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <numeric>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -66,6 +67,7 @@ struct pmgb_system {
     int* d_kabc = nullptr;          // k-vectors in half-row traversal order
     double* d_wt = nullptr;
     std::vector<int> k_order;       // traversal position -> caller's k index
+    std::vector<double> h_sk;       // S(k) of every caller k-vector (re, im), caller order
     int n_k = 0;
     bool ewald_set = false;
     int n_sites = 0;
@@ -597,6 +599,7 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     D.n_k = 0;
     D.krow = nullptr;
     D.skw = nullptr;
+    D.ks[0] = D.ks[1] = D.ks[2] = 1;
     ++ctx->refs;
     *out = s;
     return PMGB_OK;
@@ -659,18 +662,90 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
     s->d_sk = nullptr;
     s->d_kabc = nullptr;
     s->d_wt = nullptr;
+    s->ewald_set = false;
     int rc;
-    if ((rc = upload(ctx, &s->d_krow, rows, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_kabc, kabc, &s->h2d_bytes)) ||
-        (rc = upload(ctx, &s->d_wt, wt, &s->h2d_bytes)))
+    if ((rc = upload(ctx, &s->d_kabc, kabc, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_wt, wt, &s->h2d_bytes)))
         return rc;
     PMGB_CK(ctx, cudaMalloc(&s->d_skw, std::max<size_t>(sizeof(float2) * n_kvecs, 16)));
     PMGB_CK(ctx, cudaMalloc(&s->d_sk, std::max<size_t>(2 * sizeof(double) * n_kvecs, 16)));
     PMGB_CK(ctx, pmgb_launch_structure_factor(s->d_qxf, s->d_q, s->n_q, s->d_kabc, s->d_wt, n_kvecs, s->d_sk,
                                               s->d_skw, ctx->stream));
+    std::vector<double> sk(2 * static_cast<size_t>(n_kvecs));
+    if (n_kvecs > 0)
+        PMGB_CK(ctx, cudaMemcpyAsync(sk.data(), s->d_sk, sizeof(double) * sk.size(), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    s->h_sk.assign(sk.size(), 0.0);
+    for (int i = 0; i < n_kvecs; ++i) {
+        s->h_sk[2 * order[i]] = sk[2 * i];
+        s->h_sk[2 * order[i] + 1] = sk[2 * i + 1];
+    }
+    // Replicated frameworks: S(k) of n_a x n_b x n_c copies of a cell vanishes unless n_d | k_d
+    // for every d (the sum over copies of e^{2 pi i k_d j / n_d} is zero otherwise), so those
+    // k-vectors add nothing.  The strides ks_d = gcd of k_d over the k-vectors whose |S(k)|
+    // exceeds 1e-10 max |S| (the others are FP64 rounding of an exact zero); the k-vectors that
+    // are not multiples are dropped if the most they could add, sum wt |S(k)| sum_g |q_g|, stays
+    // under 1e-9 K.  A framework that is not a replica keeps every k-vector (ks = 1).
+    int ks[3] = {1, 1, 1};
+    {
+        double smax = 0.0;
+        for (int i = 0; i < n_kvecs; ++i) smax = std::max(smax, std::hypot(sk[2 * i], sk[2 * i + 1]));
+        int g[3] = {0, 0, 0};
+        for (int i = 0; i < n_kvecs; ++i)
+            if (std::hypot(sk[2 * i], sk[2 * i + 1]) > 1e-10 * smax)
+                for (int d = 0; d < 3; ++d) g[d] = std::gcd(g[d], std::abs(kabc[3 * i + d]));
+        for (int d = 0; d < 3; ++d) ks[d] = g[d] > 0 ? g[d] : 1;
+        double qg = 0.0;
+        for (int k = 0; k < s->n_sites; ++k) qg += std::fabs(s->dev.q64[k]);
+        double dropped = 0.0;
+        for (int i = 0; i < n_kvecs; ++i)
+            if (kabc[3 * i] % ks[0] || kabc[3 * i + 1] % ks[1] || kabc[3 * i + 2] % ks[2])
+                dropped += std::fabs(wt[i]) * std::hypot(sk[2 * i], sk[2 * i + 1]) * qg;
+        if (dropped > 1e-9) ks[0] = ks[1] = ks[2] = 1;
+    }
+    int n_eval = n_kvecs;
+    if (ks[0] * ks[1] * ks[2] > 1) {
+        // kept k-vectors: the multiples, each half-row thinned to every ks2-th kc, rows in k / ks
+        std::vector<KRow> rows_p;
+        std::vector<int> kabc_p;
+        std::vector<double> wt_p, sk_p;
+        std::vector<float2> skw_p;
+        for (const KRow& r : rows) {
+            if (r.ka % ks[0] || r.kb % ks[1]) continue;
+            KRow q{r.ka / ks[0], r.kb / ks[1], 0, 0, static_cast<int>(wt_p.size()), r.dir, 0, 0};
+            for (int m = 0; m < r.n; ++m) {
+                const int kc = r.kc0 + r.dir * m;
+                if (kc % ks[2]) continue;
+                const int i = r.off + m;
+                if (q.n == 0) q.kc0 = kc / ks[2];
+                ++q.n;
+                kabc_p.insert(kabc_p.end(), {r.ka, r.kb, kc});
+                wt_p.push_back(wt[i]);
+                sk_p.push_back(sk[2 * i]);
+                sk_p.push_back(sk[2 * i + 1]);
+                skw_p.push_back(make_float2(static_cast<float>(wt[i] * sk[2 * i]),
+                                            static_cast<float>(wt[i] * sk[2 * i + 1])));
+            }
+            if (q.n > 0) rows_p.push_back(q);
+        }
+        void* full[] = {s->d_skw, s->d_sk, s->d_kabc, s->d_wt};
+        for (void* p : full) cudaFree(p);
+        s->d_skw = nullptr;
+        s->d_sk = nullptr;
+        s->d_kabc = nullptr;
+        s->d_wt = nullptr;
+        if ((rc = upload(ctx, &s->d_kabc, kabc_p, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_wt, wt_p, &s->h2d_bytes)) ||
+            (rc = upload(ctx, &s->d_sk, sk_p, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_skw, skw_p, &s->h2d_bytes)))
+            return rc;
+        rows.swap(rows_p);
+        n_eval = static_cast<int>(wt_p.size());
+    }
+    if ((rc = upload(ctx, &s->d_krow, rows, &s->h2d_bytes))) return rc;
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // the uploads read host vectors
     s->n_k = n_kvecs;
     s->k_order = order;
     s->ewald_set = true;
+    for (int d = 0; d < 3; ++d) s->dev.ks[d] = ks[d];
     s->dev.alpha = static_cast<float>(alpha);
     s->dev.rc2e = static_cast<float>(sr_cutoff * sr_cutoff);
     s->dev.alpha64 = alpha;
@@ -679,7 +754,7 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
     s->dev.wt64 = s->d_wt;
     s->dev.kabc = s->d_kabc;
     s->dev.n_krow = static_cast<int>(rows.size());
-    s->dev.n_k = n_kvecs;
+    s->dev.n_k = n_eval;
     s->dev.krow = s->d_krow;
     s->dev.skw = s->d_skw;
     return PMGB_OK;
@@ -700,7 +775,7 @@ extern "C" int pmgb_system_info(const pmgb_system* s, int64_t* out6) {
     out6[0] = s->dev.n_rec;
     out6[1] = s->dev.n_seg;
     out6[2] = s->n_k;
-    out6[3] = s->dev.n_krow;
+    out6[3] = s->dev.n_k;
     out6[4] = s->n_sites;
     out6[5] = s->h2d_bytes;
     return PMGB_OK;
@@ -721,16 +796,7 @@ extern "C" int pmgb_structure_factor(pmgb_system* s, double* sk_out) {
     if (!s || !sk_out) return PMGB_ERR_INVALID_ARGUMENT;
     pmgb_ctx* ctx = s->ctx;
     if (!s->ewald_set) return fail(ctx, PMGB_ERR_NOT_READY, "pmgb_structure_factor: Ewald parameters not set");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
-    std::vector<double> trav(2 * static_cast<size_t>(s->n_k));
-    if (s->n_k > 0)
-        PMGB_CK(ctx, cudaMemcpyAsync(trav.data(), s->d_sk, 2 * sizeof(double) * s->n_k, cudaMemcpyDeviceToHost,
-                                     ctx->stream));
-    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
-    for (int i = 0; i < s->n_k; ++i) {
-        sk_out[2 * s->k_order[i]] = trav[2 * i];
-        sk_out[2 * s->k_order[i] + 1] = trav[2 * i + 1];
-    }
+    std::copy(s->h_sk.begin(), s->h_sk.end(), sk_out);  // every caller k-vector, kept or not
     return PMGB_OK;
 }
 

@@ -502,13 +502,21 @@ __device__ __forceinline__ void pair2_fwd(const int4 ra, const int4 rb, const ui
 // relative to |D|.  Phases are exact 32-bit fixed-point turns.  Rows of constant (ka, kb)
 // start at the kc nearest 0 and step outward in kc by `dir`.
 template <int NS, bool GRAD = false>
-__device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua[NS], const uint32_t Ub[NS],
-                                           const uint32_t Uc[NS], float& plr_hi, float& plr_lo,
+__device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua_in[NS], const uint32_t Ub_in[NS],
+                                           const uint32_t Uc_in[NS], float& plr_hi, float& plr_lo,
                                            float (*gu)[3] = nullptr, int row0 = 0, int row_step = 1) {
     // GRAD: gu[g][d] receives dU_lr/du_g (fractional coordinates of site g)
     constexpr float kTurn = 4.656612873077393e-10f;  // 2^-31: int32 fixed point -> half turns
     plr_hi = 0.0f;
     plr_lo = 0.0f;
+    // rows hold k / ks: evaluate them at ks u (exact in fixed point, modulo one cell)
+    uint32_t Ua[NS], Ub[NS], Uc[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+        Ua[k] = static_cast<uint32_t>(S.ks[0]) * Ua_in[k];
+        Ub[k] = static_cast<uint32_t>(S.ks[1]) * Ub_in[k];
+        Uc[k] = static_cast<uint32_t>(S.ks[2]) * Uc_in[k];
+    }
     // offsets of sites 1.. from site 0 (exact small integers) and their charges
     int da[NS], db[NS], dc[NS];
     float qg[NS];
@@ -557,9 +565,13 @@ __device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua[NS
         float Dr[NS], Di[NS], swdi[NS], sdwi[NS];
 #pragma unroll
         for (int k = 1; k < NS; ++k) {
-            const int p = R.ka * da[k] + R.kb * db[k] + R.kc0 * dc[k];
+            // k.d_g in fixed point, modulo one turn (a wrap flips the signs of both sn and cs,
+            // which leaves D unchanged)
+            const uint32_t p = static_cast<uint32_t>(R.ka) * static_cast<uint32_t>(da[k]) +
+                               static_cast<uint32_t>(R.kb) * static_cast<uint32_t>(db[k]) +
+                               static_cast<uint32_t>(R.kc0) * static_cast<uint32_t>(dc[k]);
             float sn, cs;
-            sincospif(static_cast<float>(p) * (0.5f * kTurn), &sn, &cs);  // half angle
+            sincospif(static_cast<float>(static_cast<int32_t>(p)) * (0.5f * kTurn), &sn, &cs);  // half angle
             Dr[k] = -2.0f * sn * sn;
             Di[k] = -2.0f * sn * cs;
             swdi[k] = sgn * wdi[k];
@@ -611,9 +623,9 @@ __device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua[NS
 #pragma unroll
             for (int k = 0; k < NS; ++k) {
                 const float f = 6.283185307179586f * qg[k];
-                gu[k][0] = fmaf(f * static_cast<float>(R.ka), vs[k], gu[k][0]);
-                gu[k][1] = fmaf(f * static_cast<float>(R.kb), vs[k], gu[k][1]);
-                gu[k][2] = fmaf(f, vk[k], gu[k][2]);
+                gu[k][0] = fmaf(f * static_cast<float>(R.ka * S.ks[0]), vs[k], gu[k][0]);
+                gu[k][1] = fmaf(f * static_cast<float>(R.kb * S.ks[1]), vs[k], gu[k][1]);
+                gu[k][2] = fmaf(f * static_cast<float>(S.ks[2]), vk[k], gu[k][2]);
             }
         }
     }

@@ -39,7 +39,8 @@ struct SitePar {
 };
 
 struct KRow {
-    int ka, kb, kc0, n;   // k = (ka, kb, kc0 + dir * m) for m = 0 .. n-1
+    // k = (ks0 ka, ks1 kb, ks2 (kc0 + dir * m)) for m = 0 .. n-1, ks = SysDev::ks
+    int ka, kb, kc0, n;
     int off;              // index of the first k-vector of the row in skw (traversal order)
     int dir;              // +1 or -1
     int pad1, pad2;
@@ -70,6 +71,10 @@ struct SysDev {
     int n_krow, n_k;
     const KRow* krow;
     const float2* skw;
+    // k-vector strides: when the framework is a replicated cell, S(k) vanishes unless every
+    // k_d is a multiple of the replication factor n_d, and only those k-vectors are kept;
+    // rows then hold k / ks and the kernels evaluate them at the coordinates ks_d u_d
+    int ks[3];
     // FP64 copies: guest poses are composed in FP64, and the Boltzmann-tail refinement
     // re-evaluates selected insertions entirely in FP64
     double f2c64[6];                        // f_to_c, upper triangular (00 01 02 11 12 22)

@@ -206,12 +206,14 @@ __device__ __forceinline__ void pair_fp64(const SysDev& S, int sg, int k, double
 __device__ __forceinline__ double kspace_fp64_rows(const SysDev& S, const double* x, int row0, int row_end,
                                                    int row_step) {
     double lr = 0.0;
-    double wr, wi;  // e^{-2 pi i x_c}: one step along +kc
-    sincospi(-2.0 * x[2], &wi, &wr);
+    double wr, wi;  // e^{-2 pi i ks2 x_c}: one step along +kc
+    sincospi(-2.0 * (S.ks[2] * x[2]), &wi, &wr);
     for (int row = row0; row < row_end; row += row_step) {
         const KRow R = S.krow[row];
-        double er, ei;  // e^{-ik.x} at the row start
-        sincospi(-2.0 * (R.ka * x[0] + R.kb * x[1] + R.kc0 * x[2]), &ei, &er);
+        double er, ei;  // e^{-ik.x} at the row start (integer products exact)
+        sincospi(-2.0 * (static_cast<double>(R.ka * S.ks[0]) * x[0] + static_cast<double>(R.kb * S.ks[1]) * x[1] +
+                         static_cast<double>(R.kc0 * S.ks[2]) * x[2]),
+                 &ei, &er);
         const double swi = R.dir * wi;  // downward rows step by the conjugate
         const double* sk = S.sk64 + 2 * R.off;
         const double* wt = S.wt64 + R.off;

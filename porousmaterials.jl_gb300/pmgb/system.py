@@ -90,7 +90,7 @@ class GPUSystem:
     def info(self) -> dict:
         out = np.zeros(6, dtype=np.int64)
         self.ctx.check(self.ctx._lib.pmgb_system_info(self.handle, ptr(out, C.c_int64)))
-        keys = ("n_records", "n_segments", "n_kvecs", "n_krows", "n_sites", "h2d_bytes")
+        keys = ("n_records", "n_segments", "n_kvecs", "n_kvecs_evaluated", "n_sites", "h2d_bytes")
         return {k: int(v) for k, v in zip(keys, out)}
 
     # -- evaluation ----------------------------------------------------------------------

@@ -193,6 +193,32 @@ def test_random_configs_ewald(c1):
           f"real {np.median(ss):.3g} K, recip {np.median(sl):.3g} K")
 
 
+def test_kvectors_of_replicated_cells(c1):
+    """A replicated framework: S(k) vanishes unless n_d | k_d for the replication factors n, so
+    only those k-vectors are evaluated; with one charge moved off its replica positions every
+    k-vector is kept.  Both agree with the oracle, which sums over every k-vector."""
+    from dataclasses import replace
+
+    cr, ff = synthetic.config1(), synthetic.forcefield()
+    reps = np.asarray(pmgb.replication_factors(cr.box, ff))
+    abc = c1.eparams.kvec_abc
+    info = c1.info()
+    assert info["n_kvecs"] == len(abc)
+    assert info["n_kvecs_evaluated"] == np.all(abc % reps == 0, axis=1).sum() < len(abc) // 4
+    sc = pmgb.replicate(cr, reps)
+    xf = sc.charges.xf.copy()
+    xf[0] += 1e-3
+    moved = replace(sc, charges=replace(sc.charges, xf=xf))
+    ep = pmgb.setup_Ewald_sum(moved.box, ff.r_cutoff, eps=1e-6)
+    gs = pmgb.GPUSystem(moved, pmgb.Frac(synthetic.co2(), moved.box), ff, ep)
+    assert gs.info()["n_kvecs_evaluated"] == len(ep.kvec_abc)
+    for sys_ in (c1, gs):
+        sites, lj, q = random_configs(sys_, 512, seed=16)
+        gpu = sys_.energies(sites)
+        _, _, lr, _, _ = oracle_for(sys_).energies(lj, q, charged=True, use_sk=True, scales=True)
+        assert np.all(np.abs(gpu[:, 2] - lr) <= FP32_SCALE_TOL * _lr_scale(sys_, q) + ATOL)
+
+
 def test_direct_form_cross_check(c1):
     # a few configurations against the reference's direct e^{ik·r} form
     sites, lj, q = random_configs(c1, 8, seed=9)
