@@ -200,6 +200,46 @@ __device__ __forceinline__ void pair_fp64(const SysDev& S, int sg, int k, double
     }
 }
 
+// FP32 screen of the (record, guest site) pairs.  The guest sites are taken to the records'
+// 32-bit fixed point once per insertion; a pair is passed on to pair_fp64 unless its FP32
+// distance lies beyond every cutoff plus 0.01 A (the FP32 distance is within ~1e-4 A of the
+// FP64 one) -- so the pairs skipped are exactly pairs to which the FP64 path adds nothing, and
+// the refined energies do not change.  A pair whose fixed-point difference lies within 2^-12 of
+// half a cell on some axis is always passed on: there the two nearest-image choices may differ.
+struct SiteScreen {
+    uint32_t x[PMGB_MAX_SITES], y[PMGB_MAX_SITES], z[PMGB_MAX_SITES];
+    float r2max;
+};
+
+__device__ __forceinline__ void screen_init(const SysDev& S, const double (*xs)[3], SiteScreen& sc) {
+    for (int k = 0; k < S.n_sites; ++k) {
+        sc.x[k] = frac2fix64(xs[k][0]);
+        sc.y[k] = frac2fix64(xs[k][1]);
+        sc.z[k] = frac2fix64(xs[k][2]);
+    }
+    const double rmax = sqrt(fmax(S.rc2_64, S.charged ? S.rc2e_64 : 0.0)) + 0.01;
+    sc.r2max = static_cast<float>(rmax * rmax);
+}
+
+__device__ __forceinline__ bool near_half_cell(int d) { return d > 0x7FF00000 || d < -0x7FF00000; }
+
+// bit k set: pair (record r, site k) may lie inside a cutoff
+__device__ __forceinline__ unsigned screen_pairs(const SysDev& S, const SiteScreen& sc, int4 r) {
+    unsigned near = 0;
+    for (int k = 0; k < S.n_sites; ++k) {
+        const int dx = static_cast<int>(static_cast<uint32_t>(r.x) - sc.x[k]);
+        const int dy = static_cast<int>(static_cast<uint32_t>(r.y) - sc.y[k]);
+        const int dz = static_cast<int>(static_cast<uint32_t>(r.z) - sc.z[k]);
+        const float fx = static_cast<float>(dx), fy = static_cast<float>(dy), fz = static_cast<float>(dz);
+        const float cx = fmaf(S.h00, fx, fmaf(S.h01, fy, S.h02 * fz));
+        const float cy = fmaf(S.h11, fy, S.h12 * fz);
+        const float cz = S.h22 * fz;
+        const float r2 = fmaf(cx, cx, fmaf(cy, cy, cz * cz));
+        if (r2 <= sc.r2max || near_half_cell(dx) || near_half_cell(dy) || near_half_cell(dz)) near |= 1u << k;
+    }
+    return near;
+}
+
 // Reciprocal-space energy of guest site k over the half-rows [row0, row_end) stepping by
 // row_step: Sum_k wt Re[S(k) e^{-ik.x}], the phasor carried along kc by an FP64 recurrence
 // from one sincospi per row (rows hold at most a few dozen k-vectors).
@@ -233,12 +273,17 @@ __device__ void energy_fp64_thread(const SysDev& S, const double (*xs)[3], doubl
     const int ns = S.n_sites;
     double v = 0.0, sr = 0.0, lr = 0.0;
     bool ovl = false;
+    SiteScreen sc;
+    screen_init(S, xs, sc);
     for (int sg = 0; sg < S.n_seg; ++sg) {
         const SegDesc d = S.seg[sg];
         for (int j = d.lo; j < d.hi; ++j) {
+            const unsigned near = screen_pairs(S, sc, S.rec[j]);
+            if (!near) continue;
             const double qj = S.rec_q[j];
             const double rx = S.rec_xf[3 * j], ry = S.rec_xf[3 * j + 1], rz = S.rec_xf[3 * j + 2];
-            for (int k = 0; k < ns; ++k) pair_fp64(S, sg, k, rx, ry, rz, qj, xs[k], v, sr, ovl);
+            for (int k = 0; k < ns; ++k)
+                if (near >> k & 1u) pair_fp64(S, sg, k, rx, ry, rz, qj, xs[k], v, sr, ovl);
         }
     }
     if (S.charged)
@@ -249,22 +294,62 @@ __device__ void energy_fp64_thread(const SysDev& S, const double (*xs)[3], doubl
     out3[2] = lr;
 }
 
+// Entries of the per-warp queue of screened pairs: record index << 3 | guest site.
+constexpr int kQueueLen = 32 + 32 * PMGB_MAX_SITES;  // a partial round + one batch of 32 records
+static_assert(PMGB_MAX_SITES <= 8, "queue entries keep the guest site in 3 bits");
+
+__device__ __forceinline__ void queued_pair(const SysDev& S, int sg, int e, const double (*xs)[3], double& v,
+                                            double& sr, bool& ovl) {
+    const int j = e >> 3, k = e & 7;
+    pair_fp64(S, sg, k, S.rec_xf[3 * j], S.rec_xf[3 * j + 1], S.rec_xf[3 * j + 2], S.rec_q[j], xs[k], v, sr, ovl);
+}
+
 // Part of the FP64 energies evaluated by one warp: framework records [j0, j1) and k-space half-rows
-// [k0, k1); lanes stride over both.  out4 = (U_vdw part, U_sr part / coul, U_lr part, overlap).
+// [k0, k1).  The lanes screen 32 records at a time in FP32 and queue the (record, site) pairs that
+// may lie inside a cutoff in `queue` (kQueueLen entries of this warp's shared memory); the FP64
+// terms run in full rounds of 32 queued pairs, so a warp pays FP64 work only for pairs near the
+// insertion however they are spread over its lanes.  k-space rows: lanes stride over them.
+// out4 = (U_vdw part, U_sr part / coul, U_lr part, overlap).
 __device__ void energy_fp64_warp_part(const SysDev& S, const double (*xs)[3], int j0, int j1, int k0, int k1,
-                                      double* out4) {
+                                      double* out4, int* queue) {
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int ns = S.n_sites;
     double v = 0.0, sr = 0.0, lr = 0.0;
     bool ovl = false;
+    SiteScreen sc;
+    screen_init(S, xs, sc);
     for (int sg = 0; sg < S.n_seg; ++sg) {
         const SegDesc d = S.seg[sg];
         const int lo = max(d.lo, j0), hi = min(d.hi, j1);
-        for (int j = lo + lane; j < hi; j += 32) {
-            const double qj = S.rec_q[j];
-            const double rx = S.rec_xf[3 * j], ry = S.rec_xf[3 * j + 1], rz = S.rec_xf[3 * j + 2];
-            for (int k = 0; k < ns; ++k) pair_fp64(S, sg, k, rx, ry, rz, qj, xs[k], v, sr, ovl);
+        int queued = 0;  // warp-uniform
+        for (int base = lo; base < hi; base += 32) {
+            const int j = base + lane;
+            const unsigned near = (j < hi) ? screen_pairs(S, sc, S.rec[j]) : 0u;
+            const int c = __popc(near);
+            int incl = c;  // inclusive prefix of the lanes' pair counts
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(full, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int total = __shfl_sync(full, incl, 31);
+            int pos = queued + incl - c;
+            for (unsigned m = near; m; m &= m - 1) queue[pos++] = (j << 3) | (__ffs(m) - 1);
+            queued += total;
+            __syncwarp();
+            int done = 0;
+            for (; queued - done >= 32; done += 32) queued_pair(S, sg, queue[done + lane], xs, v, sr, ovl);
+            // carry the partial round to the front of the queue
+            const int left = queued - done;
+            const int carry = (lane < left) ? queue[done + lane] : 0;
+            __syncwarp();
+            if (lane < left) queue[lane] = carry;
+            __syncwarp();
+            queued = left;
         }
+        if (lane < queued) queued_pair(S, sg, queue[lane], xs, v, sr, ovl);
+        __syncwarp();  // the queue is free for the next segment
     }
     if (S.charged && k1 > k0)
         for (int k = 0; k < ns; ++k)
@@ -403,6 +488,7 @@ __global__ void __launch_bounds__(1024) refine_plan_kernel(const __grid_constant
 // completes an insertion's last chunk adds the chunk partials in chunk order (the same sum
 // whatever the scheduling) and stores the insertion's FP64 energies.
 __global__ void __launch_bounds__(PMGB_THREADS) refine_large_kernel(const __grid_constant__ RefineArgs a, int n_ctas) {
+    __shared__ int s_queue[PMGB_THREADS / 32][kQueueLen];
     const int lane = threadIdx.x & 31;
     const int total = a.plan[a.n_systems];
     for (;;) {
@@ -431,7 +517,7 @@ __global__ void __launch_bounds__(PMGB_THREADS) refine_large_kernel(const __grid
         const int k0 = static_cast<int>(static_cast<long long>(S.n_krow) * c / C);
         const int k1 = static_cast<int>(static_cast<long long>(S.n_krow) * (c + 1) / C);
         double* p = a.part + 4 * static_cast<size_t>(i);
-        energy_fp64_warp_part(S, xs, j0, j1, k0, k1, p);
+        energy_fp64_warp_part(S, xs, j0, j1, k0, k1, p, s_queue[threadIdx.x >> 5]);
         if (lane == 0 && C == 1) {  // the whole insertion in one chunk
             double* out = a.ref_u + 3 * static_cast<size_t>(r);
             out[0] = p[3] > 0.0 ? __longlong_as_double(0x7ff0000000000000ll) : p[0];
