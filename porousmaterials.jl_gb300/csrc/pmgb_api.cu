@@ -53,6 +53,7 @@ struct pmgb_system {
     SysDev dev{};
     // device allocations
     int4* d_rec = nullptr;
+    ChunkBox* d_cbox = nullptr;
     double* d_rec_q = nullptr;
     double2* d_segpar64 = nullptr;
     SegDesc* d_seg = nullptr;
@@ -302,7 +303,7 @@ static void free_system_device(pmgb_system* s) {
                     s->in_buf.p,   s->out_buf.p,   s->axes.p,    s->g_u.p,    s->g_dsum.p, s->g_grad.p,
                     s->g_part.p,   s->g_cols.p,   s->r_hist.p,  s->r_cut.p,  s->r_counts.p, s->r_offsets.p,
                     s->r_list.p,   s->r_ref.p,    s->o_counts.p, s->o_perm.p,  s->r_plan.p,  s->r_done.p,
-                    s->r_part.p,   s->acc.p};
+                    s->r_part.p,   s->acc.p,      s->d_cbox};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -510,6 +511,39 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
             h_par64[g * PMGB_MAX_SITES + k] = make_double2(s2, e4);
         }
 
+    // bounding box of every chunk of records, in the kernels' traversal order
+    std::vector<ChunkBox> h_cbox;
+    {
+        const int n_rec = static_cast<int>(h_rec.size());
+        for (int t0 = 0; t0 < n_rec; t0 += PMGB_TILE) {
+            const int t1 = std::min(t0 + PMGB_TILE, n_rec);
+            for (const SegDesc& d : h_seg) {
+                const int lo = std::max(d.lo, t0), hi = std::min(d.hi, t1);
+                for (int j0 = lo; j0 < hi; j0 += PMGB_CHUNK) {
+                    const int j1 = std::min(j0 + PMGB_CHUNK, hi);
+                    uint32_t mn[3] = {UINT32_MAX, UINT32_MAX, UINT32_MAX}, mx[3] = {0, 0, 0};
+                    for (int j = j0; j < j1; ++j) {
+                        const uint32_t u[3] = {static_cast<uint32_t>(h_rec[j].x), static_cast<uint32_t>(h_rec[j].y),
+                                               static_cast<uint32_t>(h_rec[j].z)};
+                        for (int a = 0; a < 3; ++a) {
+                            mn[a] = std::min(mn[a], u[a]);
+                            mx[a] = std::max(mx[a], u[a]);
+                        }
+                    }
+                    ChunkBox b{};
+                    uint32_t* c = &b.cx;
+                    uint32_t* e = &b.ex;
+                    for (int a = 0; a < 3; ++a) {
+                        const uint32_t span = mx[a] - mn[a];
+                        c[a] = mn[a] + span / 2;
+                        e[a] = span - span / 2 + 1;  // every record within e of the centre
+                    }
+                    h_cbox.push_back(b);
+                }
+            }
+        }
+    }
+
     // charge fractional coordinates for S(k), FP64
     std::vector<double> h_qxf;
     std::vector<double> h_q;
@@ -521,7 +555,8 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
 
     int rc = PMGB_OK;
     int64_t* nb = &s->h2d_bytes;
-    if ((rc = upload(ctx, &s->d_rec, h_rec, nb)) || (rc = upload(ctx, &s->d_rec_q, h_rec_q, nb)) ||
+    if ((rc = upload(ctx, &s->d_rec, h_rec, nb)) || (rc = upload(ctx, &s->d_cbox, h_cbox, nb)) ||
+        (rc = upload(ctx, &s->d_rec_q, h_rec_q, nb)) ||
         (rc = upload(ctx, &s->d_segpar64, h_par64, nb)) || (rc = upload(ctx, &s->d_seg, h_seg, nb)) ||
         (rc = upload(ctx, &s->d_segpar, h_par, nb)) || (rc = upload(ctx, &s->d_qxf, h_qxf, nb)) ||
         (rc = upload(ctx, &s->d_rec_xf, h_rec_xf, nb)) ||
@@ -539,6 +574,52 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
 
     SysDev& D = s->dev;
     D.rec = s->d_rec;
+    D.cbox = s->d_cbox;
+    {
+        // chunk skipping pays only where chunks often lie beyond the cutoff of a compact group of
+        // sites: estimate the skipped fraction 1 - (4/3) pi (rc + rho)^3 / V per chunk (rho: the
+        // Cartesian radius of the chunk's box, largest over its corners) and keep the boxes only
+        // if it averages at least 0.1 (a box test costs ~2% where nothing is skipped)
+        const double vol = std::fabs(R[0] * R[4] * R[8]);
+        const double rc = std::sqrt(r2_cutoff);
+        double skip = 0.0;
+        for (const ChunkBox& b : h_cbox) {
+            const double e[3] = {b.ex / 4294967296.0, b.ey / 4294967296.0, b.ez / 4294967296.0};
+            double rho2 = 0.0;
+            for (int sgn = 0; sgn < 4; ++sgn) {
+                const double f[3] = {e[0], (sgn & 1) ? -e[1] : e[1], (sgn & 2) ? -e[2] : e[2]};
+                double v2 = 0.0;
+                for (int i = 0; i < 3; ++i) {
+                    const double v = R[i] * f[0] + R[i + 3] * f[1] + R[i + 6] * f[2];
+                    v2 += v * v;
+                }
+                rho2 = std::max(rho2, v2);
+            }
+            const double r = rc + std::sqrt(rho2);
+            skip += std::max(0.0, 1.0 - 4.0 / 3.0 * M_PI * r * r * r / vol);
+        }
+        if (h_cbox.empty() || skip < 0.1 * static_cast<double>(h_cbox.size())) D.cbox = nullptr;
+    }
+    {
+        // perpendicular width W_d = 1 / |row d of c_to_f|; unit face normals n_d = row / |row|
+        double n[3][3], w[3];
+        for (int d = 0; d < 3; ++d) {
+            const double r0 = G[d], r1 = G[d + 3], r2 = G[d + 6];
+            const double len = std::sqrt(r0 * r0 + r1 * r1 + r2 * r2);
+            w[d] = 1.0 / len;
+            n[d][0] = r0 / len;
+            n[d][1] = r1 / len;
+            n[d][2] = r2 / len;
+        }
+        double lam = 0.0;  // Gershgorin bound of the largest eigenvalue of (n_i . n_j)
+        for (int i = 0; i < 3; ++i) {
+            double row = 0.0;
+            for (int j = 0; j < 3; ++j) row += std::fabs(n[i][0] * n[j][0] + n[i][1] * n[j][1] + n[i][2] * n[j][2]);
+            lam = std::max(lam, row);
+        }
+        for (int d = 0; d < 3; ++d) D.cw[d] = static_cast<float>(w[d] / 4294967296.0 * (1.0 - 1e-6));
+        D.cw_inv_lam = static_cast<float>((1.0 - 1e-6) / lam);
+    }
     D.n_rec = static_cast<int>(h_rec.size());
     D.n_tiles = (D.n_rec + PMGB_TILE - 1) / PMGB_TILE;
     D.n_seg = static_cast<int>(h_seg.size());

@@ -33,7 +33,7 @@
 
 namespace {
 
-constexpr int kChunk = 64;              // records per compensated fold
+constexpr int kChunk = PMGB_CHUNK;      // records per compensated fold
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s bound on any mbarrier wait
 
 // ----------------------------------------------------------------------------
@@ -705,6 +705,41 @@ struct UnitIO {
     bool cull;                   // the warp's items are spatially ordered: skip out-of-cutoff terms
 };
 
+// Fixed-point gap between a site and a chunk box along one axis: |wrap(c - u)| - e, at least 0.
+// The circular distance obeys the triangle inequality, so every record of the chunk lies at
+// least this far (in fractions of the axis) from the site along that axis, in its nearest image.
+__device__ __forceinline__ float box_gap(uint32_t c, uint32_t u, uint32_t e) {
+    const int d = static_cast<int>(c - u);
+    const uint32_t a = d < 0 ? 0u - static_cast<uint32_t>(d) : static_cast<uint32_t>(d);
+    return a > e ? static_cast<float>(a - e) : 0.0f;
+}
+
+// Can any lane of the warp have a site within the cutoff of a record of chunk box B?  A record
+// at fractional gaps g_d (per axis, nearest image) lies at least g_d W_d from the site along the
+// unit normal n_d of face d (W_d: perpendicular width), so its distance r satisfies
+// r^2 >= max_d (g_d W_d)^2 and r^2 >= sum_d (g_d W_d)^2 / lambda_max(n_i . n_j).  The chunk is
+// skipped when that bound exceeds the cutoff by 1e-4 relative (far above FP32 rounding): every
+// pair term of it would be an exact zero, so the sums do not change.
+template <int NS>
+__device__ __forceinline__ bool chunk_near(const SysDev& S, const ChunkBox* box, const uint32_t* ux,
+                                           const uint32_t* uy, const uint32_t* uz, bool active, float rcmax2) {
+    const uint4 c = __ldg(reinterpret_cast<const uint4*>(box));
+    const uint4 e = __ldg(reinterpret_cast<const uint4*>(box) + 1);
+    bool near = false;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+        if (k < S.n_sites) {
+            const float gx = box_gap(c.x, ux[k], e.x) * S.cw[0];
+            const float gy = box_gap(c.y, uy[k], e.y) * S.cw[1];
+            const float gz = box_gap(c.z, uz[k], e.z) * S.cw[2];
+            const float sum = fmaf(gx, gx, fmaf(gy, gy, gz * gz)) * S.cw_inv_lam;
+            const float mx = fmaxf(fmaxf(gx * gx, gy * gy), gz * gz);
+            near = near || fmaxf(sum, mx) <= rcmax2 * 1.0001f;
+        }
+    }
+    return __any_sync(0xffffffffu, active && near);
+}
+
 // Returns false if a bounded wait gave up (the status word is set); every thread of the CTA
 // returns the same value.  fills[s] counts the completed fills of ring slot s so far; the
 // caller keeps it across units (the barriers are initialised once per CTA).
@@ -782,6 +817,8 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
     }
     bool ovl = false, abort = false;
     int fail_tile = 0;
+    int cb = 0;  // running chunk index: the order of S.cbox
+    const bool box_cull = io.cull && S.cbox != nullptr;
 
     for (int t = 0; t < n_tiles; ++t) {
         const int slot = t % PMGB_NSTAGE;
@@ -813,8 +850,10 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
             float2 i12[NS], i6[NS];
 #pragma unroll
             for (int k = 0; k < NS; ++k) i12[k] = i6[k] = f2(0.0f);
-            for (int j0 = lo; j0 < hi; j0 += kChunk) {
+            for (int j0 = lo; j0 < hi; j0 += kChunk, ++cb) {
                 const int j1 = min(j0 + kChunk, hi);
+                // spatially ordered warp: skip a chunk no lane can reach (no distances either)
+                if (box_cull && !chunk_near<NS>(S, S.cbox + cb, ux, uy, uz, valid && !blocked, g2.rcmax2)) continue;
                 float2 ljp2[NS], php2[NS];
 #pragma unroll
                 for (int k = 0; k < NS; ++k) ljp2[k] = php2[k] = f2(0.0f);

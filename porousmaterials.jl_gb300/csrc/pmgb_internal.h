@@ -21,6 +21,7 @@
 #define PMGB_TILE 2048        // framework records per shared-memory stage (32 KB)
 #define PMGB_NSTAGE 3         // stages in the TMA ring
 #define PMGB_THREADS 256      // insertions per CTA (one per thread)
+#define PMGB_CHUNK 64         // framework records per compensated fold (and per chunk box)
 
 // status word bits written by kernels (never a trap)
 #define PMGB_DEVERR_TMA_TIMEOUT 0x1u
@@ -30,6 +31,13 @@ struct SegDesc {
     int lo, hi;        // record range [lo, hi)
     int species;       // species id in the caller's force-field table (-1: charge-only sites)
     int has_lj;
+};
+
+// Fixed-point bounding box of one chunk of kChunk framework records (the kernels' compensated
+// fold): centre and half-extent per axis, as 32-bit fractions of the supercell.
+struct ChunkBox {
+    uint32_t cx, cy, cz, pad0;
+    uint32_t ex, ey, ez, pad1;
 };
 
 struct SitePar {
@@ -50,6 +58,11 @@ struct KRow {
 struct SysDev {
     const int4* rec;
     int n_rec, n_tiles;
+    // chunk boxes in the kernels' traversal order (tiles, then segments, then kChunk records)
+    // and the perpendicular widths of the supercell per fixed-point step; cw_inv_lam = 1 / an
+    // upper bound of the largest eigenvalue of the Gram matrix of the unit face normals
+    const ChunkBox* cbox;
+    float cw[3], cw_inv_lam;
     int n_seg;
     const SegDesc* seg;
     const SitePar* segpar;

@@ -1,8 +1,9 @@
 """Spatially ordered evaluation with cutoff culling (pmgb_system_set_cull).
 
 The ordered path sorts each block's insertions by the Z-order cell of their centre of mass,
-lets a warp skip framework records beyond the cutoff of all its items, and forms the block
-sums in insertion order.  Skipped terms are exact zeros, so every per-insertion energy and
+lets a warp skip framework records beyond the cutoff of all its items (whole chunks of records
+by their bounding boxes in large cells, groups of four after their distances otherwise), and
+forms the block sums in insertion order.  Skipped terms are exact zeros, so every per-insertion energy and
 every block result must be bit-identical to the unordered path; likewise the energy grid with
 brick-ordered warps.
 """
@@ -63,10 +64,12 @@ def test_culled_grid_is_bit_identical(n_pts):
     np.testing.assert_array_equal(g1, g0)
 
 
-@pytest.mark.parametrize("case", ["co2_porous", "ch4_config0"])
+@pytest.mark.parametrize("case", ["co2_porous", "ch4_config0", "co2_config4"])
 def test_culled_adjoint_is_bit_identical(case):
+    # config4 (a 52 A cell) is large enough that whole chunks of records are skipped
     make = {"co2_porous": (synthetic.config1_porous, synthetic.co2, True),
-            "ch4_config0": (synthetic.config0, synthetic.ch4, False)}[case]
+            "ch4_config0": (synthetic.config0, synthetic.ch4, False),
+            "co2_config4": (synthetic.config4, synthetic.co2, True)}[case]
     gs = _system(make[0](), make[1](), make[2])
     out = []
     for cull in (False, True):
