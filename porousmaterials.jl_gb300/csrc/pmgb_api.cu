@@ -511,7 +511,7 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
             h_par64[g * PMGB_MAX_SITES + k] = make_double2(s2, e4);
         }
 
-    // bounding box of every chunk of records, in the kernels' traversal order
+    // bounding box of every sub-chunk of records, in the kernels' traversal order
     std::vector<ChunkBox> h_cbox;
     {
         const int n_rec = static_cast<int>(h_rec.size());
@@ -519,8 +519,9 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
             const int t1 = std::min(t0 + PMGB_TILE, n_rec);
             for (const SegDesc& d : h_seg) {
                 const int lo = std::max(d.lo, t0), hi = std::min(d.hi, t1);
-                for (int j0 = lo; j0 < hi; j0 += PMGB_CHUNK) {
-                    const int j1 = std::min(j0 + PMGB_CHUNK, hi);
+                for (int c0 = lo; c0 < hi; c0 += PMGB_CHUNK)
+                for (int j0 = c0; j0 < std::min(c0 + PMGB_CHUNK, hi); j0 += PMGB_SUBCHUNK) {
+                    const int j1 = std::min({j0 + PMGB_SUBCHUNK, c0 + PMGB_CHUNK, hi});
                     uint32_t mn[3] = {UINT32_MAX, UINT32_MAX, UINT32_MAX}, mx[3] = {0, 0, 0};
                     for (int j = j0; j < j1; ++j) {
                         const uint32_t u[3] = {static_cast<uint32_t>(h_rec[j].x), static_cast<uint32_t>(h_rec[j].y),
@@ -576,10 +577,10 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     D.rec = s->d_rec;
     D.cbox = s->d_cbox;
     {
-        // chunk skipping pays only where chunks often lie beyond the cutoff of a compact group of
-        // sites: estimate the skipped fraction 1 - (4/3) pi (rc + rho)^3 / V per chunk (rho: the
-        // Cartesian radius of the chunk's box, largest over its corners) and keep the boxes only
-        // if it averages at least 0.1 (a box test costs ~2% where nothing is skipped)
+        // skipping pays only where sub-chunks often lie beyond the cutoff of a compact group of
+        // sites: estimate the skipped fraction 1 - (4/3) pi (rc + rho)^3 / V per sub-chunk (rho:
+        // the Cartesian radius of its box, largest over the corners) and keep the boxes only if
+        // it averages at least 0.1 (the box tests cost a few per cent where nothing is skipped)
         const double vol = std::fabs(R[0] * R[4] * R[8]);
         const double rc = std::sqrt(r2_cutoff);
         double skip = 0.0;

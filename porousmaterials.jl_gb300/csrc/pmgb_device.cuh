@@ -34,6 +34,8 @@
 namespace {
 
 constexpr int kChunk = PMGB_CHUNK;      // records per compensated fold
+constexpr int kSub = PMGB_SUBCHUNK;     // records per bounding box (a quarter of a chunk)
+static_assert(kChunk % kSub == 0 && kSub % 4 == 0 && kChunk / kSub <= 32, "sub-chunks tile a chunk");
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s bound on any mbarrier wait
 
 // ----------------------------------------------------------------------------
@@ -714,7 +716,7 @@ __device__ __forceinline__ float box_gap(uint32_t c, uint32_t u, uint32_t e) {
     return a > e ? static_cast<float>(a - e) : 0.0f;
 }
 
-// Can any lane of the warp have a site within the cutoff of a record of chunk box B?  A record
+// Can any lane of the warp have a site within the cutoff of a record of sub-chunk box B?  A record
 // at fractional gaps g_d (per axis, nearest image) lies at least g_d W_d from the site along the
 // unit normal n_d of face d (W_d: perpendicular width), so its distance r satisfies
 // r^2 >= max_d (g_d W_d)^2 and r^2 >= sum_d (g_d W_d)^2 / lambda_max(n_i . n_j).  The chunk is
@@ -817,7 +819,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
     }
     bool ovl = false, abort = false;
     int fail_tile = 0;
-    int cb = 0;  // running chunk index: the order of S.cbox
+    int cb = 0;  // running sub-chunk index: the order of S.cbox
     const bool box_cull = io.cull && S.cbox != nullptr;
 
     for (int t = 0; t < n_tiles; ++t) {
@@ -850,16 +852,28 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
             float2 i12[NS], i6[NS];
 #pragma unroll
             for (int k = 0; k < NS; ++k) i12[k] = i6[k] = f2(0.0f);
-            for (int j0 = lo; j0 < hi; j0 += kChunk, ++cb) {
+            for (int j0 = lo; j0 < hi; j0 += kChunk) {
                 const int j1 = min(j0 + kChunk, hi);
-                // spatially ordered warp: skip a chunk no lane can reach (no distances either)
-                if (box_cull && !chunk_near<NS>(S, S.cbox + cb, ux, uy, uz, valid && !blocked, g2.rcmax2)) continue;
+                const int n_sub = (j1 - j0 + kSub - 1) / kSub;
+                // spatially ordered warp: bit s set if some lane may reach a record of sub-chunk s;
+                // the others are skipped whole, distances included (warp-uniform)
+                unsigned near_sub = (1u << n_sub) - 1u;
+                if (box_cull) {
+                    for (int sb = 0; sb < n_sub; ++sb)
+                        if (!chunk_near<NS>(S, S.cbox + cb + sb, ux, uy, uz, valid && !blocked, g2.rcmax2))
+                            near_sub &= ~(1u << sb);
+                    cb += n_sub;
+                    if (near_sub == 0u) continue;
+                }
                 float2 ljp2[NS], php2[NS];
 #pragma unroll
                 for (int k = 0; k < NS; ++k) ljp2[k] = php2[k] = f2(0.0f);
                 float ljp[NS], php[NS];
                 if (GRAD) {
-                    for (int j = j0; j < j1; j += 2) {
+                    for (int sb = 0; sb < n_sub; ++sb) {
+                    if (!(near_sub >> sb & 1u)) continue;
+                    const int s_end = min(j0 + (sb + 1) * kSub, j1);
+                    for (int j = j0 + sb * kSub; j < s_end; j += 2) {
                         const bool two = j + 1 < j1;
                         const int4 ra = T[j - t0];
                         const int4 rb = two ? T[j + 1 - t0] : ra;
@@ -882,6 +896,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                             gz[k] = G.gz;
                         }
                     }
+                    }
 #pragma unroll
                     for (int k = 0; k < NS; ++k) {
                         ljp[k] = ljp2[k].x + ljp2[k].y;
@@ -891,8 +906,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                     // the warp's insertions are spatially close: after the distances, skip the
                     // pair terms of four records when no lane has the site inside the cutoff
                     // (those terms are exact zeros, so the sums are unchanged)
-                    int j = j0;
-                    for (; j + 4 <= j1; j += 4) {
+                    auto group4 = [&](int j) {
                         const int4 r0 = T[j - t0], r1 = T[j + 1 - t0], r2 = T[j + 2 - t0], r3 = T[j + 3 - t0];
 #pragma unroll
                         for (int k = 0; k < NS; ++k) {
@@ -907,6 +921,21 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                                 pair2_energy<CHARGED>(d23, __int_as_float(r2.w), __int_as_float(r3.w), g2, a12, a6,
                                                       ljp2[k], php2[k]);
                             }
+                        }
+                    };
+                    int j = j0;
+                    if (near_sub == (1u << n_sub) - 1u) {
+                        for (; j + 4 <= j1; j += 4) group4(j);
+                    } else {
+                        // sub-chunk by sub-chunk: the same groups of four, in the same order, as one
+                        // sweep over [j0, j1); a skipped last sub-chunk takes the remainder with it
+                        for (int sb = 0; sb < n_sub; ++sb) {
+                            const int s_end = min(j0 + (sb + 1) * kSub, j1);
+                            if (!(near_sub >> sb & 1u)) {
+                                j = (sb == n_sub - 1) ? j1 : s_end;
+                                continue;
+                            }
+                            for (; j + 4 <= s_end; j += 4) group4(j);
                         }
                     }
 #pragma unroll

@@ -21,7 +21,8 @@
 #define PMGB_TILE 2048        // framework records per shared-memory stage (32 KB)
 #define PMGB_NSTAGE 3         // stages in the TMA ring
 #define PMGB_THREADS 256      // insertions per CTA (one per thread)
-#define PMGB_CHUNK 64         // framework records per compensated fold (and per chunk box)
+#define PMGB_CHUNK 64         // framework records per compensated fold
+#define PMGB_SUBCHUNK 16      // framework records per bounding box (chunks are cut into these)
 
 // status word bits written by kernels (never a trap)
 #define PMGB_DEVERR_TMA_TIMEOUT 0x1u
@@ -33,8 +34,8 @@ struct SegDesc {
     int has_lj;
 };
 
-// Fixed-point bounding box of one chunk of kChunk framework records (the kernels' compensated
-// fold): centre and half-extent per axis, as 32-bit fractions of the supercell.
+// Fixed-point bounding box of one sub-chunk of PMGB_SUBCHUNK framework records: centre and
+// half-extent per axis, as 32-bit fractions of the supercell.
 struct ChunkBox {
     uint32_t cx, cy, cz, pad0;
     uint32_t ex, ey, ez, pad1;
@@ -58,7 +59,7 @@ struct KRow {
 struct SysDev {
     const int4* rec;
     int n_rec, n_tiles;
-    // chunk boxes in the kernels' traversal order (tiles, then segments, then kChunk records)
+    // sub-chunk boxes in the kernels' traversal order (tiles, segments, chunks, sub-chunks)
     // and the perpendicular widths of the supercell per fixed-point step; cw_inv_lam = 1 / an
     // upper bound of the largest eigenvalue of the Gram matrix of the unit face normals
     const ChunkBox* cbox;
