@@ -67,6 +67,7 @@ struct pmgb_system {
     double* d_sk = nullptr;
     int* d_kabc = nullptr;          // k-vectors in half-row traversal order
     double* d_wt = nullptr;
+    double* d_es = nullptr;         // erfc(alpha r)/r table of the FP64 refinement
     std::vector<int> k_order;       // traversal position -> caller's k index
     std::vector<double> h_sk;       // S(k) of every caller k-vector (re, im), caller order
     int n_k = 0;
@@ -303,7 +304,7 @@ static void free_system_device(pmgb_system* s) {
                     s->in_buf.p,   s->out_buf.p,   s->axes.p,    s->g_u.p,    s->g_dsum.p, s->g_grad.p,
                     s->g_part.p,   s->g_cols.p,   s->r_hist.p,  s->r_cut.p,  s->r_counts.p, s->r_offsets.p,
                     s->r_list.p,   s->r_ref.p,    s->o_counts.p, s->o_perm.p,  s->r_plan.p,  s->r_done.p,
-                    s->r_part.p,   s->acc.p,      s->d_cbox};
+                    s->r_part.p,   s->acc.p,      s->d_cbox,    s->d_es};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -687,6 +688,55 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     return PMGB_OK;
 }
 
+namespace {
+
+// Piecewise polynomial of f(s) = erfc(alpha sqrt(s)) / sqrt(s) for the FP64 refinement: octaves
+// of s from 2^PMGB_ES_E_LO up to the first power of two above s_max, each cut into PMGB_ES_SUB
+// intervals; on each, the degree-7 Chebyshev interpolant at 8 nodes (from the C library's erfc),
+// written out as monomial coefficients in t in [-1, 1].
+std::vector<double> erfc_over_r_table(double alpha, double s_max) {
+    int e_hi = 0;
+    std::frexp(s_max, &e_hi);  // s_max < 2^e_hi
+    const int n = PMGB_ES_COEF;
+    std::vector<double> tab;
+    tab.reserve(static_cast<size_t>(std::max(0, e_hi - PMGB_ES_E_LO)) * PMGB_ES_SUB * n);
+    for (int e = PMGB_ES_E_LO; e < e_hi; ++e)
+        for (int m = 0; m < PMGB_ES_SUB; ++m) {
+            const double a = std::ldexp(1.0 + static_cast<double>(m) / PMGB_ES_SUB, e);
+            const double b = std::ldexp(1.0 + static_cast<double>(m + 1) / PMGB_ES_SUB, e);
+            double fk[PMGB_ES_COEF], tk[PMGB_ES_COEF];
+            for (int k = 0; k < n; ++k) {
+                tk[k] = std::cos(M_PI * (k + 0.5) / n);
+                const double sv = 0.5 * (a + b) + 0.5 * (b - a) * tk[k];
+                const double r = std::sqrt(sv);
+                fk[k] = std::erfc(alpha * r) / r;
+            }
+            // Chebyshev coefficients c_j = (2/n) sum_k f_k T_j(t_k) (c_0 halved), then the sum of
+            // c_j T_j in the monomial basis through T_{j+1} = 2 t T_j - T_{j-1}
+            double poly[PMGB_ES_COEF] = {}, tm1[PMGB_ES_COEF] = {}, tj[PMGB_ES_COEF] = {};
+            tj[0] = 1.0;
+            for (int j = 0; j < n; ++j) {
+                double c = 0.0;
+                for (int k = 0; k < n; ++k) c += fk[k] * std::cos(j * M_PI * (k + 0.5) / n);
+                c *= (j == 0 ? 1.0 : 2.0) / n;
+                for (int i = 0; i < n; ++i) poly[i] += c * tj[i];
+                double next[PMGB_ES_COEF] = {};
+                for (int i = 0; i < n; ++i) {
+                    if (i + 1 < n) next[i + 1] += 2.0 * tj[i];
+                    next[i] -= (j == 0) ? 0.0 : tm1[i];
+                }
+                if (j == 0)  // T_1 = t
+                    for (int i = 0; i < n; ++i) next[i] = (i == 1) ? 1.0 : 0.0;
+                std::copy(tj, tj + n, tm1);
+                std::copy(next, next + n, tj);
+            }
+            tab.insert(tab.end(), poly, poly + n);
+        }
+    return tab;
+}
+
+}  // namespace
+
 extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cutoff, int32_t n_kvecs,
                                      const int32_t* kvec_abc, const double* kvec_wt) {
     if (!s) return PMGB_ERR_INVALID_ARGUMENT;
@@ -736,7 +786,7 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
         k = e;
     }
     // drop previous Ewald state
-    void* old[] = {s->d_krow, s->d_skw, s->d_sk, s->d_kabc, s->d_wt};
+    void* old[] = {s->d_krow, s->d_skw, s->d_sk, s->d_kabc, s->d_wt, s->d_es};
     for (void* p : old)
         if (p) cudaFree(p);
     s->d_krow = nullptr;
@@ -744,6 +794,7 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
     s->d_sk = nullptr;
     s->d_kabc = nullptr;
     s->d_wt = nullptr;
+    s->d_es = nullptr;
     s->ewald_set = false;
     int rc;
     if ((rc = upload(ctx, &s->d_kabc, kabc, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_wt, wt, &s->h2d_bytes)))
@@ -823,6 +874,8 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
         n_eval = static_cast<int>(wt_p.size());
     }
     if ((rc = upload(ctx, &s->d_krow, rows, &s->h2d_bytes))) return rc;
+    const std::vector<double> es = erfc_over_r_table(alpha, sr_cutoff * sr_cutoff);
+    if ((rc = upload(ctx, &s->d_es, es, &s->h2d_bytes))) return rc;
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // the uploads read host vectors
     s->n_k = n_kvecs;
     s->k_order = order;
@@ -832,6 +885,8 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
     s->dev.rc2e = static_cast<float>(sr_cutoff * sr_cutoff);
     s->dev.alpha64 = alpha;
     s->dev.rc2e_64 = sr_cutoff * sr_cutoff;
+    s->dev.es_tab = s->d_es;
+    s->dev.es_e_lo = PMGB_ES_E_LO;
     s->dev.sk64 = s->d_sk;
     s->dev.wt64 = s->d_wt;
     s->dev.kabc = s->d_kabc;

@@ -23,6 +23,9 @@
 #define PMGB_THREADS 256      // insertions per CTA (one per thread)
 #define PMGB_CHUNK 64         // framework records per compensated fold
 #define PMGB_SUBCHUNK 16      // framework records per bounding box (chunks are cut into these)
+#define PMGB_ES_COEF 8        // coefficients per interval of the FP64 erfc(alpha r)/r table
+#define PMGB_ES_SUB 32        // intervals per octave of r^2 in that table
+#define PMGB_ES_E_LO (-7)     // the table starts at r^2 = 2^-7 A^2 (closer pairs: direct formula)
 
 // status word bits written by kernels (never a trap)
 #define PMGB_DEVERR_TMA_TIMEOUT 0x1u
@@ -102,6 +105,11 @@ struct SysDev {
     const double* sk64;                     // [2 n_k] S(k) (re, im) in half-row order
     const double* wt64;                     // [n_k] k-vector weights in half-row order
     const int* kabc;                        // [3 n_k] k-vectors in half-row order
+    // erfc(alpha r) / r as a function of s = r^2 for the FP64 refinement: per interval
+    // [2^e (1 + m/32), 2^e (1 + (m+1)/32)), e >= es_e_lo, m < 32, a degree-7 polynomial in
+    // t = 64 x - (65 + 2 m) (x = s 2^-e), PMGB_ES_COEF coefficients from t^0 up
+    const double* es_tab;
+    int es_e_lo;
     // optional accessibility gate (src/henry.jl:225): blocked insertions get U = +Inf
     const uint8_t* acc;                     // [acc_n0 * acc_n1 * acc_n2], i fastest; 0 = inaccessible
     int acc_n[3];                           // grid points per axis of the unit-cell grid

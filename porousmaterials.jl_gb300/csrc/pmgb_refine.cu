@@ -172,6 +172,26 @@ __device__ __forceinline__ double rcp64(double x) {
     return y;
 }
 
+// erfc(alpha r) / r at s = r^2 from the system's piecewise polynomial table (built on the host
+// from the C library's erfc by Chebyshev interpolation at 8 nodes per interval; within ~2e-15 of
+// 1/r, i.e. of the bare Coulomb term); pairs closer than 2^-3.5 A use the direct formula.
+__device__ __forceinline__ double erfc_over_r(const SysDev& S, double s) {
+    const long long bits = __double_as_longlong(s);
+    const int oct = static_cast<int>((bits >> 52) & 0x7ff) - 1023 - S.es_e_lo;
+    if (oct < 0) {
+        const double r = sqrt(s);
+        return erfc(S.alpha64 * r) * rcp64(r);
+    }
+    const int m = static_cast<int>((bits >> 47) & (PMGB_ES_SUB - 1));
+    const double x = __longlong_as_double((bits & 0x000fffffffffffffll) | 0x3ff0000000000000ll);  // s 2^-e
+    const double t = fma(x, 2.0 * PMGB_ES_SUB, -(2.0 * PMGB_ES_SUB + 1.0 + 2.0 * m));
+    const double* c = S.es_tab + PMGB_ES_COEF * (oct * PMGB_ES_SUB + m);
+    double v = __ldg(c + PMGB_ES_COEF - 1);
+#pragma unroll
+    for (int j = PMGB_ES_COEF - 2; j >= 0; --j) v = fma(v, t, __ldg(c + j));
+    return v;
+}
+
 // Pair terms of one (record, guest site) in FP64: LJ (strict cutoff, overlap flag) and the
 // unscaled real-space Coulomb term q_k q_j erfc(alpha r) / r.
 __device__ __forceinline__ void pair_fp64(const SysDev& S, int sg, int k, double rx, double ry, double rz, double qj,
@@ -194,10 +214,8 @@ __device__ __forceinline__ void pair_fp64(const SysDev& S, int sg, int k, double
             v += p.y * (t3 * t3 - t3);
         }
     }
-    if (S.charged && qj != 0.0 && S.q64[k] != 0.0 && r2 < S.rc2e_64 && r2 > 0.0) {
-        const double rr = sqrt(r2);
-        sr += S.q64[k] * qj * erfc(S.alpha64 * rr) * rcp64(rr);
-    }
+    if (S.charged && qj != 0.0 && S.q64[k] != 0.0 && r2 < S.rc2e_64 && r2 > 0.0)
+        sr += S.q64[k] * qj * erfc_over_r(S, r2);
 }
 
 // FP32 screen of the (record, guest site) pairs.  The guest sites are taken to the records'
