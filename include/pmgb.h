@@ -57,7 +57,9 @@ void pmgb_destroy(pmgb_ctx* ctx);
  * failure of pmgb_create. */
 const char* pmgb_last_error(const pmgb_ctx* ctx);
 
-/* Run subsequent work on `stream` (a cudaStream_t); NULL restores the context's own stream. */
+/* Run subsequent work on `stream` (a cudaStream_t); NULL restores the context's own stream.
+ * Work already queued on the previous stream is waited for first: the context's device memory
+ * comes from a stream-ordered pool, ordered on the context's current stream. */
 int pmgb_set_stream(pmgb_ctx* ctx, void* stream);
 int pmgb_synchronize(pmgb_ctx* ctx);
 

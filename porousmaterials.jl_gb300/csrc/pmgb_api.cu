@@ -45,6 +45,9 @@ struct pmgb_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     unsigned int* d_status = nullptr;
+    // device memory of systems and batches: a stream-ordered pool that keeps freed memory for
+    // reuse (repeated set-up, as in a screening loop over the drop-in, allocates from the cache)
+    cudaMemPool_t pool = nullptr;
     std::string err;
 };
 
@@ -116,13 +119,22 @@ int cuda_fail(pmgb_ctx* ctx, cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call); \
     } while (0)
 
+// Device memory from the context's pool, ordered on its current stream (all of a context's
+// work runs on that stream; pmgb_set_stream waits for the previous one).
+cudaError_t dev_malloc(pmgb_ctx* ctx, void** p, size_t bytes) {
+    return cudaMallocFromPoolAsync(p, bytes, ctx->pool, ctx->stream);
+}
+void dev_free(pmgb_ctx* ctx, void* p) {
+    if (p) cudaFreeAsync(p, ctx->stream);
+}
+
 int ensure(pmgb_ctx* ctx, DevBuf& b, size_t bytes) {
     if (bytes <= b.n) return PMGB_OK;
-    if (b.p) cudaFree(b.p);
+    dev_free(ctx, b.p);
     b.p = nullptr;
     b.n = 0;
     const size_t want = std::max<size_t>(bytes, 256);
-    PMGB_CK(ctx, cudaMalloc(&b.p, want));
+    PMGB_CK(ctx, dev_malloc(ctx, &b.p, want));
     b.n = want;
     return PMGB_OK;
 }
@@ -132,7 +144,7 @@ int upload(pmgb_ctx* ctx, T** dst, const std::vector<T>& v, int64_t* counter = n
     *dst = nullptr;
     if (counter) *counter += static_cast<int64_t>(v.size() * sizeof(T));
     const size_t bytes = std::max<size_t>(v.size() * sizeof(T), 16);
-    PMGB_CK(ctx, cudaMalloc(reinterpret_cast<void**>(dst), bytes));
+    PMGB_CK(ctx, dev_malloc(ctx, reinterpret_cast<void**>(dst), bytes));
     if (!v.empty())
         PMGB_CK(ctx, cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
     return PMGB_OK;
@@ -236,7 +248,17 @@ extern "C" int pmgb_create(int device, pmgb_ctx** out) {
     e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(unsigned int));
+    if (e == cudaSuccess) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        e = cudaMemPoolCreate(&c->pool, &props);
+        uint64_t keep = UINT64_MAX;  // never trim: freed blocks stay cached until the context goes
+        if (e == cudaSuccess) e = cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     if (e != cudaSuccess) {
+        if (c->pool) cudaMemPoolDestroy(c->pool);
         if (c->d_status) cudaFree(c->d_status);
         if (c->own_stream) cudaStreamDestroy(c->own_stream);
         delete c;
@@ -254,6 +276,8 @@ static void ctx_release(pmgb_ctx* ctx) {
     if (--ctx->refs > 0) return;
     cudaSetDevice(ctx->device);
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+    cudaStreamSynchronize(ctx->stream);  // frees queued on a caller's stream
+    if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
@@ -273,6 +297,8 @@ extern "C" const char* pmgb_last_error(const pmgb_ctx* ctx) {
 
 extern "C" int pmgb_set_stream(pmgb_ctx* ctx, void* stream) {
     if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // pool memory is ordered on one stream
     ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
     return PMGB_OK;
 }
@@ -305,8 +331,7 @@ static void free_system_device(pmgb_system* s) {
                     s->g_part.p,   s->g_cols.p,   s->r_hist.p,  s->r_cut.p,  s->r_counts.p, s->r_offsets.p,
                     s->r_list.p,   s->r_ref.p,    s->o_counts.p, s->o_perm.p,  s->r_plan.p,  s->r_done.p,
                     s->r_part.p,   s->acc.p,      s->d_cbox,    s->d_es};
-    for (void* p : ptrs)
-        if (p) cudaFree(p);
+    for (void* p : ptrs) dev_free(s->ctx, p);
 }
 
 extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t n_atoms, const double* atom_xf,
@@ -379,17 +404,21 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     };
     std::vector<Rec> recs;
     recs.reserve(n_atoms + n_charges);
-    std::map<Key3, int> at_pos;
+    // atoms sorted by position (ties by index): a charge at exactly an atom's position merges into
+    // the first such atom, unless an earlier charge took it
+    std::vector<std::pair<Key3, int>> at_pos;
+    at_pos.reserve(n_atoms);
     for (int i = 0; i < n_atoms; ++i) {
         Rec r{wrap01(atom_xf[3 * i]), wrap01(atom_xf[3 * i + 1]), wrap01(atom_xf[3 * i + 2]), 0.0, atom_species[i]};
-        at_pos.emplace(Key3(r.x, r.y, r.z), static_cast<int>(recs.size()));
+        at_pos.emplace_back(Key3(r.x, r.y, r.z), static_cast<int>(recs.size()));
         recs.push_back(r);
     }
+    std::sort(at_pos.begin(), at_pos.end());
     std::vector<char> taken(recs.size(), 0);
     for (int c = 0; c < n_charges; ++c) {
         const Key3 key(wrap01(charge_xf[3 * c]), wrap01(charge_xf[3 * c + 1]), wrap01(charge_xf[3 * c + 2]));
-        auto it = at_pos.find(key);
-        if (it != at_pos.end() && !taken[it->second]) {
+        auto it = std::lower_bound(at_pos.begin(), at_pos.end(), std::make_pair(key, -1));
+        if (it != at_pos.end() && it->first == key && !taken[it->second]) {
             recs[it->second].q = charge_q[c];
             taken[it->second] = 1;
         } else {
@@ -787,8 +816,7 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
     }
     // drop previous Ewald state
     void* old[] = {s->d_krow, s->d_skw, s->d_sk, s->d_kabc, s->d_wt, s->d_es};
-    for (void* p : old)
-        if (p) cudaFree(p);
+    for (void* p : old) dev_free(ctx, p);
     s->d_krow = nullptr;
     s->d_skw = nullptr;
     s->d_sk = nullptr;
@@ -799,8 +827,8 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
     int rc;
     if ((rc = upload(ctx, &s->d_kabc, kabc, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_wt, wt, &s->h2d_bytes)))
         return rc;
-    PMGB_CK(ctx, cudaMalloc(&s->d_skw, std::max<size_t>(sizeof(float2) * n_kvecs, 16)));
-    PMGB_CK(ctx, cudaMalloc(&s->d_sk, std::max<size_t>(2 * sizeof(double) * n_kvecs, 16)));
+    PMGB_CK(ctx, dev_malloc(ctx, reinterpret_cast<void**>(&s->d_skw), std::max<size_t>(sizeof(float2) * n_kvecs, 16)));
+    PMGB_CK(ctx, dev_malloc(ctx, reinterpret_cast<void**>(&s->d_sk), std::max<size_t>(2 * sizeof(double) * n_kvecs, 16)));
     PMGB_CK(ctx, pmgb_launch_structure_factor(s->d_qxf, s->d_q, s->n_q, s->d_kabc, s->d_wt, n_kvecs, s->d_sk,
                                               s->d_skw, ctx->stream));
     std::vector<double> sk(2 * static_cast<size_t>(n_kvecs));
@@ -862,7 +890,7 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
             if (q.n > 0) rows_p.push_back(q);
         }
         void* full[] = {s->d_skw, s->d_sk, s->d_kabc, s->d_wt};
-        for (void* p : full) cudaFree(p);
+        for (void* p : full) dev_free(ctx, p);
         s->d_skw = nullptr;
         s->d_sk = nullptr;
         s->d_kabc = nullptr;
@@ -1703,14 +1731,13 @@ void batch_free(pmgb_batch* b) {
                     b->d_dsum, b->d_unit_cols, b->d_block_out, b->d_out_cols, b->d_chunk_sys, b->d_u,
                     b->d_hist, b->d_cut, b->d_counts, b->d_offsets, b->d_list, b->d_ref_u,
                     b->d_plan, b->d_done, b->d_part, b->d_perm, b->d_cells, b->d_unit_m};
-    for (void* p : ptrs)
-        if (p) cudaFree(p);
+    for (void* p : ptrs) dev_free(b->ctx, p);
 }
 
 template <class T>
 int batch_alloc(pmgb_batch* b, T** p, size_t count) {
     const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
-    PMGB_CK(b->ctx, cudaMalloc(reinterpret_cast<void**>(p), bytes));
+    PMGB_CK(b->ctx, dev_malloc(b->ctx, reinterpret_cast<void**>(p), bytes));
     b->device_bytes += static_cast<int64_t>(bytes);
     return PMGB_OK;
 }

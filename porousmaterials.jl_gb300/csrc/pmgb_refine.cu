@@ -398,7 +398,7 @@ __device__ void energy_fp64_warp_part(const SysDev& S, const double (*xs)[3], in
 __device__ __forceinline__ long long fp64_work(const SysDev& S) {
     return static_cast<long long>(S.n_sites) * (S.n_rec + (S.charged ? S.n_k : 0));
 }
-__device__ __forceinline__ bool small_system(const SysDev& S) { return fp64_work(S) <= 512; }
+__device__ __forceinline__ bool small_system(const SysDev& S) { return fp64_work(S) <= 64; }
 __device__ __forceinline__ int fp64_chunks(const SysDev& S, long long count) {
     if (small_system(S)) return 0;
     const long long fine = min(64ll, (fp64_work(S) + 1023) / 1024);
