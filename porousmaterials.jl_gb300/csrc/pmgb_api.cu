@@ -829,8 +829,16 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
         return rc;
     PMGB_CK(ctx, dev_malloc(ctx, reinterpret_cast<void**>(&s->d_skw), std::max<size_t>(sizeof(float2) * n_kvecs, 16)));
     PMGB_CK(ctx, dev_malloc(ctx, reinterpret_cast<void**>(&s->d_sk), std::max<size_t>(2 * sizeof(double) * n_kvecs, 16)));
-    PMGB_CK(ctx, pmgb_launch_structure_factor(s->d_qxf, s->d_q, s->n_q, s->d_kabc, s->d_wt, n_kvecs, s->d_sk,
-                                              s->d_skw, ctx->stream));
+    int kmax[3] = {0, 0, 0};
+    for (int i = 0; i < n_kvecs; ++i)
+        for (int d = 0; d < 3; ++d) kmax[d] = std::max(kmax[d], std::abs(kabc[3 * i + d]));
+    double2* d_table = nullptr;  // per-axis phasors of every charge, freed once S(k) is built
+    const size_t table_len = pmgb_structure_factor_table_len(s->n_q, kmax);
+    PMGB_CK(ctx, dev_malloc(ctx, reinterpret_cast<void**>(&d_table), std::max<size_t>(sizeof(double2) * table_len, 16)));
+    const cudaError_t e_sk = pmgb_launch_structure_factor(s->d_qxf, s->d_q, s->n_q, s->d_kabc, s->d_wt, n_kvecs, kmax,
+                                                          d_table, s->d_sk, s->d_skw, ctx->stream);
+    dev_free(ctx, d_table);
+    PMGB_CK(ctx, e_sk);
     std::vector<double> sk(2 * static_cast<size_t>(n_kvecs));
     if (n_kvecs > 0)
         PMGB_CK(ctx, cudaMemcpyAsync(sk.data(), s->d_sk, sizeof(double) * sk.size(), cudaMemcpyDeviceToHost,

@@ -292,9 +292,12 @@ cudaError_t pmgb_launch_batch_lse(const BatchSystem* systems, const int* chunk_s
 cudaError_t pmgb_launch_reduce_blocks(const LsePartial* partials, int n_blocks, int ctas_per_block,
                                       double* block_out, cudaStream_t st);
 // qxf: framework charge fractional coordinates (FP64, 3 per charge)
+// S(k) of every k-vector from per-axis phasor tables e^{2 pi i h x_c}, |h| <= kmax[d]; `table`
+// holds pmgb_structure_factor_table_len(n_q, kmax) entries of scratch
+size_t pmgb_structure_factor_table_len(int n_q, const int kmax[3]);
 cudaError_t pmgb_launch_structure_factor(const double* qxf, const double* q, int n_q,
-                                         const int* kabc, const double* wt, int n_k,
-                                         double* sk_out, float2* skw_out, cudaStream_t st);
+                                         const int* kabc, const double* wt, int n_k, const int kmax[3],
+                                         double2* table, double* sk_out, float2* skw_out, cudaStream_t st);
 cudaError_t pmgb_launch_sample_poses(unsigned long long seed, long long start, long long n,
                                      float* xf_out, float* rot_out, cudaStream_t st);
 cudaError_t pmgb_launch_philox(const unsigned int* ctr, const unsigned int* key, long long n,

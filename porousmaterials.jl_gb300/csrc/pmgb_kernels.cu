@@ -381,23 +381,49 @@ __global__ void reduce_blocks_kernel(const LsePartial* __restrict__ partials, in
     }
 }
 
-// S(k) = sum_c q_c e^{2 pi i (ka fa + kb fb + kc fc)}; one warp per k-vector, FP64 terms and
-// accumulation from the exact FP64 charge positions.
-__global__ void structure_factor_kernel(const double* __restrict__ qxf, const double* __restrict__ q,
-                                        int n_q, const int* __restrict__ kabc, const double* __restrict__ wt,
-                                        int n_k, double* __restrict__ sk_out, float2* __restrict__ skw_out) {
+// Phasor tables for S(k): table[(off_d + h + kmax_d) n_q + c] = e^{2 pi i h x_{c,d}} for each axis
+// d and |h| <= kmax_d, one FP64 sincospi each from the exact FP64 charge positions.
+__global__ void phasor_table_kernel(const double* __restrict__ qxf, int n_q, int3 kmax, double2* __restrict__ table,
+                                    long long n) {
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = static_cast<int>(i % n_q);
+    int row = static_cast<int>(i / n_q), d = 0, h;
+    const int w0 = 2 * kmax.x + 1, w1 = 2 * kmax.y + 1;
+    if (row < w0) {
+        h = row - kmax.x;
+    } else if (row < w0 + w1) {
+        d = 1;
+        h = row - w0 - kmax.y;
+    } else {
+        d = 2;
+        h = row - w0 - w1 - kmax.z;
+    }
+    double sn, cs;
+    sincospi(2.0 * static_cast<double>(h) * qxf[3 * c + d], &sn, &cs);
+    table[i] = make_double2(cs, sn);
+}
+
+// S(k) = sum_c q_c e^{2 pi i (ka fa + kb fb + kc fc)}, the phasor of each charge the product of its
+// three axis phasors; one warp per k-vector, lanes over charges, FP64 accumulation.
+__global__ void structure_factor_kernel(const double* __restrict__ q, int n_q, const int* __restrict__ kabc,
+                                        const double* __restrict__ wt, int n_k, int3 kmax,
+                                        const double2* __restrict__ table, double* __restrict__ sk_out,
+                                        float2* __restrict__ skw_out) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= n_k) return;
-    const double ka = kabc[3 * warp], kb = kabc[3 * warp + 1], kc = kabc[3 * warp + 2];
+    const int w0 = 2 * kmax.x + 1, w1 = 2 * kmax.y + 1;
+    const double2* ta = table + static_cast<size_t>(kabc[3 * warp] + kmax.x) * n_q;
+    const double2* tb = table + static_cast<size_t>(w0 + kabc[3 * warp + 1] + kmax.y) * n_q;
+    const double2* tc = table + static_cast<size_t>(w0 + w1 + kabc[3 * warp + 2] + kmax.z) * n_q;
     double re = 0.0, im = 0.0;
     for (int c = lane; c < n_q; c += 32) {
-        // phase k.x in turns from the exact FP64 fractional coordinates
-        const double t = ka * qxf[3 * c] + kb * qxf[3 * c + 1] + kc * qxf[3 * c + 2];
-        double sn, cs;
-        sincospi(2.0 * t, &sn, &cs);
-        re = fma(q[c], cs, re);
-        im = fma(q[c], sn, im);
+        const double2 a = ta[c], b = tb[c], e = tc[c];
+        const double abr = fma(a.x, b.x, -a.y * b.y), abi = fma(a.x, b.y, a.y * b.x);
+        const double pr = fma(abr, e.x, -abi * e.y), pi = fma(abr, e.y, abi * e.x);
+        re = fma(q[c], pr, re);
+        im = fma(q[c], pi, im);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -562,13 +588,21 @@ cudaError_t pmgb_launch_reduce_blocks(const LsePartial* partials, int n_blocks, 
     return cudaGetLastError();
 }
 
+size_t pmgb_structure_factor_table_len(int n_q, const int kmax[3]) {
+    return static_cast<size_t>(n_q) * static_cast<size_t>(2 * kmax[0] + 2 * kmax[1] + 2 * kmax[2] + 3);
+}
+
 cudaError_t pmgb_launch_structure_factor(const double* qxf, const double* q, int n_q, const int* kabc,
-                                         const double* wt, int n_k, double* sk_out, float2* skw_out,
-                                         cudaStream_t st) {
+                                         const double* wt, int n_k, const int kmax[3], double2* table,
+                                         double* sk_out, float2* skw_out, cudaStream_t st) {
     if (n_k <= 0) return cudaSuccess;
+    const int3 km = make_int3(kmax[0], kmax[1], kmax[2]);
+    const long long n = static_cast<long long>(pmgb_structure_factor_table_len(n_q, kmax));
+    if (n > 0)
+        phasor_table_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(qxf, n_q, km, table, n);
     const int warps_per_cta = 8;
     const int ctas = (n_k + warps_per_cta - 1) / warps_per_cta;
-    structure_factor_kernel<<<ctas, 32 * warps_per_cta, 0, st>>>(qxf, q, n_q, kabc, wt, n_k, sk_out, skw_out);
+    structure_factor_kernel<<<ctas, 32 * warps_per_cta, 0, st>>>(q, n_q, kabc, wt, n_k, km, table, sk_out, skw_out);
     return cudaGetLastError();
 }
 
