@@ -12,10 +12,8 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
-#include <map>
 #include <numeric>
 #include <string>
-#include <tuple>
 #include <vector>
 
 namespace {
@@ -218,7 +216,29 @@ bool upper_factor(const double H[9], double R[9], double Q[9]) {
     return true;
 }
 
-using Key3 = std::tuple<double, double, double>;
+// hash of an exact position (the bit patterns of three doubles in [0, 1))
+inline size_t pos_hash(double x, double y, double z) {
+    uint64_t a, b, c;
+    std::memcpy(&a, &x, 8);
+    std::memcpy(&b, &y, 8);
+    std::memcpy(&c, &z, 8);
+    uint64_t h = a * 0x9E3779B97F4A7C15ull;
+    h ^= (b + 0x632BE59BD9B4E019ull) * 0xC2B2AE3D27D4EB4Full;
+    h ^= h >> 29;
+    h += c * 0x165667B19E3779F9ull;
+    h ^= h >> 32;
+    return static_cast<size_t>(h);
+}
+
+// the low 10 bits of v moved to every third bit (bit i -> bit 3 i), for Z-order codes
+inline uint32_t spread10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
 
 }  // namespace
 
@@ -404,44 +424,54 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     };
     std::vector<Rec> recs;
     recs.reserve(n_atoms + n_charges);
-    // atoms sorted by position (ties by index): a charge at exactly an atom's position merges into
-    // the first such atom, unless an earlier charge took it
-    std::vector<std::pair<Key3, int>> at_pos;
-    at_pos.reserve(n_atoms);
+    for (int i = 0; i < n_atoms; ++i)
+        recs.push_back(Rec{wrap01(atom_xf[3 * i]), wrap01(atom_xf[3 * i + 1]), wrap01(atom_xf[3 * i + 2]), 0.0,
+                           atom_species[i]});
+    // a charge at exactly an atom's position merges into the first such atom, unless an earlier
+    // charge took it: an open-addressing table from exact positions to the first atom there
+    size_t cap = 16;
+    while (cap < 2 * static_cast<size_t>(n_atoms)) cap <<= 1;
+    std::vector<int> slot(cap, -1);
+    auto probe = [&](double x, double y, double z) {
+        size_t h = pos_hash(x, y, z) & (cap - 1);
+        while (slot[h] >= 0) {
+            const Rec& o = recs[slot[h]];
+            if (o.x == x && o.y == y && o.z == z) break;
+            h = (h + 1) & (cap - 1);
+        }
+        return h;
+    };
     for (int i = 0; i < n_atoms; ++i) {
-        Rec r{wrap01(atom_xf[3 * i]), wrap01(atom_xf[3 * i + 1]), wrap01(atom_xf[3 * i + 2]), 0.0, atom_species[i]};
-        at_pos.emplace_back(Key3(r.x, r.y, r.z), static_cast<int>(recs.size()));
-        recs.push_back(r);
+        const size_t h = probe(recs[i].x, recs[i].y, recs[i].z);
+        if (slot[h] < 0) slot[h] = i;
     }
-    std::sort(at_pos.begin(), at_pos.end());
     std::vector<char> taken(recs.size(), 0);
     for (int c = 0; c < n_charges; ++c) {
-        const Key3 key(wrap01(charge_xf[3 * c]), wrap01(charge_xf[3 * c + 1]), wrap01(charge_xf[3 * c + 2]));
-        auto it = std::lower_bound(at_pos.begin(), at_pos.end(), std::make_pair(key, -1));
-        if (it != at_pos.end() && it->first == key && !taken[it->second]) {
-            recs[it->second].q = charge_q[c];
-            taken[it->second] = 1;
+        const double x = wrap01(charge_xf[3 * c]), y = wrap01(charge_xf[3 * c + 1]), z = wrap01(charge_xf[3 * c + 2]);
+        const int hit = n_atoms > 0 ? slot[probe(x, y, z)] : -1;
+        if (hit >= 0 && !taken[hit]) {
+            recs[hit].q = charge_q[c];
+            taken[hit] = 1;
         } else {
-            recs.push_back(Rec{std::get<0>(key), std::get<1>(key), std::get<2>(key), charge_q[c], -1});
+            recs.push_back(Rec{x, y, z, charge_q[c], -1});
         }
     }
-    // species-sorted contiguous segments of fixed-point records
-    std::vector<int> order(recs.size());
-    for (size_t i = 0; i < recs.size(); ++i) order[i] = static_cast<int>(i);
-    auto sp_key = [&](int i) { return recs[i].species < 0 ? n_species : recs[i].species; };
-    // within a segment, Z-order of the position (10 bits per axis): consecutive records are
-    // spatially close, so a warp can skip groups of them that lie beyond the cutoff
-    std::vector<uint32_t> zkey(recs.size());
+    // species-sorted contiguous segments of fixed-point records; within a segment, Z-order of the
+    // position (10 bits per axis): consecutive records are spatially close, so a warp can skip
+    // groups of them that lie beyond the cutoff.  Sort keys (species, Z code, index) packed in 64
+    // bits: 7 + 30 + 27 (index last, so equal codes keep their input order).
+    if (recs.size() >= (size_t{1} << 27))
+        return fail(ctx, PMGB_ERR_UNSUPPORTED, "framework has %zu records (max 2^27)", recs.size());
+    std::vector<uint64_t> skey(recs.size());
     for (size_t i = 0; i < recs.size(); ++i) {
-        const uint32_t c[3] = {to_fix(recs[i].x) >> 22, to_fix(recs[i].y) >> 22, to_fix(recs[i].z) >> 22};
-        uint32_t z = 0;
-        for (int bit = 0; bit < 10; ++bit)
-            for (int d = 0; d < 3; ++d) z |= ((c[d] >> bit) & 1u) << (3 * bit + d);
-        zkey[i] = z;
+        const uint32_t zc = spread10(to_fix(recs[i].x) >> 22) | spread10(to_fix(recs[i].y) >> 22) << 1 |
+                            spread10(to_fix(recs[i].z) >> 22) << 2;
+        const uint64_t sp = static_cast<uint64_t>(recs[i].species < 0 ? n_species : recs[i].species);
+        skey[i] = (sp << 57) | (static_cast<uint64_t>(zc) << 27) | i;
     }
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        return sp_key(a) != sp_key(b) ? sp_key(a) < sp_key(b) : zkey[a] < zkey[b];
-    });
+    std::sort(skey.begin(), skey.end());
+    std::vector<int> order(recs.size());
+    for (size_t i = 0; i < recs.size(); ++i) order[i] = static_cast<int>(skey[i] & ((uint64_t{1} << 27) - 1));
     std::vector<int4> h_rec;
     std::vector<double> h_rec_q;   // FP64 charge of each record
     std::vector<double> h_rec_xf;  // its exact fractional coordinates

@@ -284,8 +284,11 @@ def replicate(crystal: Crystal, repfactors) -> Crystal:
 
 
 def crystal_density(crystal: Crystal, masses: dict | None = None) -> float:
-    """Mass density in kg/m³ (Xtals crystal_density; used at src/henry.jl:96,143)."""
-    total = sum(atomic_mass(s, masses) for s in crystal.atoms.species)
+    """Mass density in kg/m³ (Xtals crystal_density; used at src/henry.jl:96,143).  The mass is
+    summed per species (one table lookup per species, not per atom)."""
+    from collections import Counter
+
+    total = sum(atomic_mass(s, masses) * n for s, n in Counter(crystal.atoms.species).items())
     return total / crystal.box.Omega * 1660.5390666
 
 
