@@ -26,7 +26,7 @@ class GPUSystem:
         self.crystal = crystal
         self.molecule = molecule
         self.ljff = ljff
-        species = list(dict.fromkeys(list(crystal.atoms.species) + list(molecule.atom_species)))
+        species = list(dict.fromkeys([*dict.fromkeys(crystal.atoms.species), *molecule.atom_species]))
         self.species = species
         sid = {s: i for i, s in enumerate(species)}
         if ljff is not None:
@@ -40,7 +40,8 @@ class GPUSystem:
         self._eps = np.ascontiguousarray(eps)
         self._sig2 = np.ascontiguousarray(sig2)
         atom_xf = np.ascontiguousarray(crystal.atoms.xf, dtype=np.float64)
-        atom_sp = np.ascontiguousarray([sid[s] for s in crystal.atoms.species], dtype=np.int32)
+        atom_sp = np.fromiter(map(sid.__getitem__, crystal.atoms.species), dtype=np.int32,
+                              count=len(crystal.atoms.species))
         q_xf = np.ascontiguousarray(crystal.charges.xf, dtype=np.float64)
         q = np.ascontiguousarray(crystal.charges.q, dtype=np.float64)
         box = crystal.box
