@@ -1288,6 +1288,7 @@ extern "C" int pmgb_widom_device(pmgb_system* s, int64_t n_per_block, int32_t n_
     a.partials = static_cast<LsePartial*>(s->partials.p);
     a.u_out = u_out_dev;
     const bool refine = s->refine_tail > 0.0;
+    a.no_resid = refine ? 1 : 0;  // the refinement re-evaluates the insertions that matter in FP64
     const size_t n_ins = static_cast<size_t>(n_per_block) * n_blocks;
     if ((refine || s->cull) && !u_out_dev) {  // both need every insertion's FP32 energy
         if (int rc = ensure(ctx, s->g_u, sizeof(double) * 2 * n_ins)) return rc;
@@ -1803,6 +1804,7 @@ int batch_capture(pmgb_batch* b) {
     a.u = (b->refine_tail > 0.0 || b->cull) ? b->d_u : nullptr;
     a.perm = b->cull ? b->d_perm : nullptr;
     a.unit_m = b->cull ? b->d_unit_m : nullptr;
+    a.no_resid = (b->refine_tail > 0.0 && !b->grad) ? 1 : 0;
     RefineArgs r{};
     if (b->refine_tail > 0.0) {
         r.systems = b->d_sys;

@@ -412,6 +412,9 @@ __device__ __forceinline__ void pair2_grad(const int4 ra, const int4 rb, const u
 }
 
 // Squared minimum-image distances of two records from one guest site.
+// RESID = false: the FP32 box matrix alone (its rounding, ~6e-8 relative, biases every distance
+// of a system the same way; used only where an FP64 refinement follows)
+template <bool RESID = true>
 __device__ __forceinline__ float2 pair2_r2(const int4 ra, const int4 rb, const uint32_t ux, const uint32_t uy,
                                            const uint32_t uz, const Geo2& g) {
     const float2 dx = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.x) - ux)),
@@ -420,6 +423,12 @@ __device__ __forceinline__ float2 pair2_r2(const int4 ra, const int4 rb, const u
                                   __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.y) - uy)));
     const float2 dz = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.z) - uz)),
                                   __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.z) - uz)));
+    if (!RESID) {
+        const float2 cx = fma2(g.h00, dx, fma2(g.h01, dy, mul2(g.h02, dz)));
+        const float2 cy = fma2(g.h11, dy, mul2(g.h12, dz));
+        const float2 cz = mul2(g.h22, dz);
+        return fma2(cx, cx, fma2(cy, cy, mul2(cz, cz)));
+    }
     const float2 rx = fma2(g.p00, dx, fma2(g.p01, dy, mul2(g.p02, dz)));
     const float2 ry = fma2(g.p11, dy, mul2(g.p12, dz));
     const float2 rz = mul2(g.p22, dz);
@@ -454,23 +463,11 @@ __device__ __forceinline__ void pair2_energy(const float2 r2, const float qa, co
     }
 }
 
-template <bool CHARGED>
+template <bool CHARGED, bool RESID = true>
 __device__ __forceinline__ void pair2_fwd(const int4 ra, const int4 rb, const uint32_t ux, const uint32_t uy,
                                           const uint32_t uz, const Geo2& g, const float2 lj12, const float2 lj6,
                                           float& segmin, float2& ljp, float2& php) {
-    const float2 dx = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.x) - ux)),
-                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.x) - ux)));
-    const float2 dy = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.y) - uy)),
-                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.y) - uy)));
-    const float2 dz = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.z) - uz)),
-                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.z) - uz)));
-    const float2 rx = fma2(g.p00, dx, fma2(g.p01, dy, mul2(g.p02, dz)));
-    const float2 ry = fma2(g.p11, dy, mul2(g.p12, dz));
-    const float2 rz = mul2(g.p22, dz);
-    const float2 cx = fma2(g.h00, dx, fma2(g.h01, dy, fma2(g.h02, dz, rx)));
-    const float2 cy = fma2(g.h11, dy, fma2(g.h12, dz, ry));
-    const float2 cz = fma2(g.h22, dz, rz);
-    const float2 r2 = fma2(cx, cx, fma2(cy, cy, mul2(cz, cz)));
+    const float2 r2 = pair2_r2<RESID>(ra, rb, ux, uy, uz, g);  // the same distances as the culled loop
     segmin = fminf(segmin, fminf(r2.x, r2.y));
     float2 ir2, y = f2(0.0f);
     if (CHARGED) {
@@ -745,9 +742,10 @@ __device__ __forceinline__ bool chunk_near(const SysDev& S, const ChunkBox* box,
 // Returns false if a bounded wait gave up (the status word is set); every thread of the CTA
 // returns the same value.  fills[s] counts the completed fills of ring slot s so far; the
 // caller keeps it across units (the barriers are initialised once per CTA).
-template <int NS, bool CHARGED, bool GRAD>
+template <int NS, bool CHARGED, bool GRAD, bool RESID = true>
 __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4* stage, uint64_t* bars,
                                          LsePartial* red, uint32_t (&fills)[PMGB_NSTAGE], unsigned int* status) {
+    static_assert(RESID || !GRAD, "the adjoint keeps the box-matrix residual");
     const int tid = threadIdx.x;
     const bool valid = io.valid;
     const long long item = io.item;
@@ -910,8 +908,8 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                         const int4 r0 = T[j - t0], r1 = T[j + 1 - t0], r2 = T[j + 2 - t0], r3 = T[j + 3 - t0];
 #pragma unroll
                         for (int k = 0; k < NS; ++k) {
-                            const float2 d01 = pair2_r2(r0, r1, ux[k], uy[k], uz[k], g2);
-                            const float2 d23 = pair2_r2(r2, r3, ux[k], uy[k], uz[k], g2);
+                            const float2 d01 = pair2_r2<RESID>(r0, r1, ux[k], uy[k], uz[k], g2);
+                            const float2 d23 = pair2_r2<RESID>(r2, r3, ux[k], uy[k], uz[k], g2);
                             const float dmin = fminf(fminf(d01.x, d01.y), fminf(d23.x, d23.y));
                             segmin[k] = fminf(segmin[k], dmin);
                             if (__any_sync(0xffffffffu, valid && !blocked && dmin < g2.rcmax2)) {
@@ -957,10 +955,10 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
 #pragma unroll
                         for (int k = 0; k < NS; ++k) {
                             const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
-                            pair2_fwd<CHARGED>(r0, r1, ux[k], uy[k], uz[k], g2, a12, a6, segmin[k], ljp2[k],
-                                               php2[k]);
-                            pair2_fwd<CHARGED>(r2, r3, ux[k], uy[k], uz[k], g2, a12, a6, segmin[k], ljp2[k],
-                                               php2[k]);
+                            pair2_fwd<CHARGED, RESID>(r0, r1, ux[k], uy[k], uz[k], g2, a12, a6, segmin[k],
+                                                      ljp2[k], php2[k]);
+                            pair2_fwd<CHARGED, RESID>(r2, r3, ux[k], uy[k], uz[k], g2, a12, a6, segmin[k],
+                                                      ljp2[k], php2[k]);
                         }
                     }
 #pragma unroll

@@ -164,6 +164,9 @@ struct LaunchArgs {
     float unit_factor;
     float* grid_out;
     int grid_bricks;             // warps take 4 x 4 x 2 bricks of points (spatially compact)
+    // forward Widom whose Boltzmann tail is refined in FP64: distances from the FP32 box matrix
+    // alone (no residual), ~13% less work; the refinement re-evaluates the insertions that matter
+    int no_resid;
     // adjoint (GRAD kernels)
     float* dsum;                 // [(seg * NS + site) * 2 + {0: sum r^-12, 1: sum r^-6}][item], within cutoff
     long long dsum_stride;       // items per column
@@ -235,6 +238,7 @@ struct BatchArgs {
     // block evaluated in that slot; the partials are then formed from u in insertion order
     const int* perm;
     double* unit_m;           // adjoint with perm: the max of -U/T of each processing chunk
+    int no_resid;             // forward with FP64 refinement: no box-matrix residual (LaunchArgs)
 };
 
 // ---- FP64 refinement of the Boltzmann tail (pmgb_refine.cu) ---------------------------

@@ -6,7 +6,7 @@
 namespace {
 
 // Single-system launch: CTA b runs unit b.
-template <int NS, bool CHARGED, bool GRAD>
+template <int NS, bool CHARGED, bool GRAD, bool RESID = true>
 __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_constant__ LaunchArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     int4* stage = reinterpret_cast<int4*>(smem_raw);
@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
     io.partial = (a.partials && !a.perm) ? a.partials + blockIdx.x : nullptr;
     ring_init(bars);
     uint32_t fills[PMGB_NSTAGE] = {};
-    (void)run_unit<NS, CHARGED, GRAD>(a.sys, io, stage, bars, red, fills, a.status);
+    (void)run_unit<NS, CHARGED, GRAD, RESID>(a.sys, io, stage, bars, red, fills, a.status);
 }
 
 // ---- latency path: few configurations, one CTA each -----------------------------------
@@ -474,14 +474,19 @@ __global__ void __launch_bounds__(256) fp32_peak_kernel(float* sink, int iters) 
     if (r == 12345.678f) sink[blockIdx.x] = r;
 }
 
+template <int NS, bool CH, bool RESID>
+cudaError_t launch_one_r(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
+    const size_t smem = pmgb_pairs_smem_bytes();
+    cudaError_t e = cudaFuncSetAttribute(pairs_kernel<NS, CH, false, RESID>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    pairs_kernel<NS, CH, false, RESID><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
 template <int NS, bool CH>
 cudaError_t launch_one(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
-    const size_t smem = pmgb_pairs_smem_bytes();
-    cudaError_t e = cudaFuncSetAttribute(pairs_kernel<NS, CH, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
-    if (e != cudaSuccess) return e;
-    pairs_kernel<NS, CH, false><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
-    return cudaGetLastError();
+    return a.no_resid ? launch_one_r<NS, CH, false>(a, n_ctas, st) : launch_one_r<NS, CH, true>(a, n_ctas, st);
 }
 
 template <int NS, bool CH>

@@ -39,24 +39,33 @@ def test_refined_blocks_match_oracle(case):
     make_cr, make_mol, charged, npb = CASES[case]
     gs = _system(make_cr(), make_mol(), charged)
     seed = 51
-    b32, u32 = gs.widom(npb, 5, seed, T, want_energies=True)
+    b32, _ = gs.widom(npb, 5, seed, T, want_energies=True)
     gs.set_refine(1e-3)
     blocks, u, v, es = widom_with_oracle(gs, npb, seed, T)
     ref = oracle.widom_blocks_log(v, es, T, 5, npb)
     d32 = np.abs(b32[:, 0] - ref[:, 0]).max()
     d64 = np.abs(blocks[:, 0] - ref[:, 0]).max()
-    changed = np.any(u != u32, axis=1)
+    n_ref = gs.refined_count()
     print(f"[refine {case}] |Δ log K_H| FP32 {d32:.2e} -> refined {d64:.2e}; refined insertions "
-          f"{changed.sum()} of {u.shape[0]}")
+          f"{n_ref} of {u.shape[0]}")
     assert d64 <= 1e-6                                   # K_H within 1e-6 relative
     u_ref = ref[:, 1] + ref[:, 2]
     assert np.all(np.abs(blocks[:, 1] + blocks[:, 2] - u_ref) <= 1e-6 * np.abs(u_ref) + 1e-9)
     np.testing.assert_array_equal(blocks[:, 3], ref[:, 3])
-    # the refined insertions carry FP64 energies
-    assert changed.any()
-    fin = changed & np.isfinite(v)
-    np.testing.assert_allclose(u[fin, 0], v[fin], rtol=1e-10, atol=1e-8)
-    np.testing.assert_allclose(u[fin, 1], es[fin], rtol=1e-10, atol=1e-8)
+    # the refined insertions carry FP64 energies (the others keep the FP32 pass's, which with a
+    # refinement to follow skips the box-matrix residual), and they include every insertion
+    # among those carrying 99% of a block's Boltzmann weight
+    fin = np.isfinite(v)
+    exact = fin & (np.abs(u[:, 0] - v) <= 1e-10 * np.abs(v) + 1e-8) & (np.abs(u[:, 1] - es) <= 1e-10 * np.abs(es) + 1e-8)
+    assert n_ref > 0 and exact.sum() + np.count_nonzero(~fin) >= n_ref
+    x = np.where(fin, -(v + es) / T, -np.inf).reshape(5, npb)
+    for b in range(5):
+        if not np.isfinite(x[b]).any():
+            continue
+        w = np.exp(x[b] - x[b].max())
+        top = np.argsort(-w)
+        head = top[:np.searchsorted(np.cumsum(w[top]) / w.sum(), 0.99) + 1]
+        assert exact.reshape(5, npb)[b, head].all(), (case, b)
     # deterministic, and tail 0 restores the FP32 results
     again, _ = gs.widom(npb, 5, seed, T)
     np.testing.assert_array_equal(again, blocks)
