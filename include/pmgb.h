@@ -306,6 +306,13 @@ int pmgb_fp32_peak(pmgb_ctx* ctx, int n_ctas, int iters, double* tflops_out);
 /* Read and clear the device status word (0 = no kernel-side failure). */
 int pmgb_device_status(pmgb_ctx* ctx, uint32_t* status_out);
 
+/* Kernel timing (no reference counterpart; measurement): while on, every Widom pass records a
+ * CUDA event before and after its pair-kernel launch on the launching stream (at most 4096
+ * launches between two reads).  pmgb_kernel_timing synchronises on the recorded events and
+ * returns their summed duration (ms) and count since the last read, then clears them. */
+int pmgb_set_kernel_timing(pmgb_ctx* ctx, int32_t on);
+int pmgb_kernel_timing(pmgb_ctx* ctx, double* total_ms, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif

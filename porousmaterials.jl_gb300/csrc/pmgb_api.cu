@@ -46,6 +46,10 @@ struct pmgb_ctx {
     // device memory of systems and batches: a stream-ordered pool that keeps freed memory for
     // reuse (repeated set-up, as in a screening loop over the drop-in, allocates from the cache)
     cudaMemPool_t pool = nullptr;
+    // optional CUDA events around the Widom passes' pair-kernel launches (pmgb_set_kernel_timing)
+    bool timing = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timing_events;
+    size_t timing_used = 0;
     std::string err;
 };
 
@@ -124,6 +128,27 @@ cudaError_t dev_malloc(pmgb_ctx* ctx, void** p, size_t bytes) {
 }
 void dev_free(pmgb_ctx* ctx, void* p) {
     if (p) cudaFreeAsync(p, ctx->stream);
+}
+
+// The Widom passes' pair-kernel launch, between two CUDA events on the launching stream when
+// kernel timing is on (at most 4096 launches are timed between two reads).
+cudaError_t launch_pairs_timed(pmgb_ctx* ctx, const LaunchArgs& a, int n_ctas) {
+    if (!ctx->timing || ctx->timing_used >= 4096) return pmgb_launch_pairs(a, n_ctas, ctx->stream);
+    if (ctx->timing_used == ctx->timing_events.size()) {
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        cudaError_t e = cudaEventCreate(&e0);
+        if (e == cudaSuccess) e = cudaEventCreate(&e1);
+        if (e != cudaSuccess) {
+            if (e0) cudaEventDestroy(e0);
+            return e;
+        }
+        ctx->timing_events.emplace_back(e0, e1);
+    }
+    const auto& ev = ctx->timing_events[ctx->timing_used++];
+    cudaError_t e = cudaEventRecord(ev.first, ctx->stream);
+    if (e == cudaSuccess) e = pmgb_launch_pairs(a, n_ctas, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev.second, ctx->stream);
+    return e;
 }
 
 int ensure(pmgb_ctx* ctx, DevBuf& b, size_t bytes) {
@@ -297,6 +322,10 @@ static void ctx_release(pmgb_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
     cudaStreamSynchronize(ctx->stream);  // frees queued on a caller's stream
+    for (auto& ev : ctx->timing_events) {
+        cudaEventDestroy(ev.first);
+        cudaEventDestroy(ev.second);
+    }
     if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -320,6 +349,31 @@ extern "C" int pmgb_set_stream(pmgb_ctx* ctx, void* stream) {
     PMGB_CK(ctx, cudaSetDevice(ctx->device));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // pool memory is ordered on one stream
     ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_set_kernel_timing(pmgb_ctx* ctx, int32_t on) {
+    if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->timing = on != 0;
+    ctx->timing_used = 0;
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_kernel_timing(pmgb_ctx* ctx, double* total_ms, int64_t* launches) {
+    if (!ctx || !total_ms || !launches) return PMGB_ERR_INVALID_ARGUMENT;
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    double sum = 0.0;
+    for (size_t i = 0; i < ctx->timing_used; ++i) {
+        PMGB_CK(ctx, cudaEventSynchronize(ctx->timing_events[i].second));
+        float ms = 0.0f;
+        PMGB_CK(ctx, cudaEventElapsedTime(&ms, ctx->timing_events[i].first, ctx->timing_events[i].second));
+        sum += ms;
+    }
+    *total_ms = sum;
+    *launches = static_cast<int64_t>(ctx->timing_used);
+    ctx->timing_used = 0;
     return PMGB_OK;
 }
 
@@ -1304,11 +1358,11 @@ extern "C" int pmgb_widom_device(pmgb_system* s, int64_t n_per_block, int32_t n_
         a.perm = static_cast<const int*>(s->o_perm.p);
         PMGB_CK(ctx, pmgb_launch_widom_order(seed, n_per_block, n_blocks, static_cast<int*>(s->o_counts.p),
                                              static_cast<int*>(s->o_perm.p), ctx->stream));
-        PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
+        PMGB_CK(ctx, launch_pairs_timed(ctx, a, n_ctas));
         PMGB_CK(ctx, pmgb_launch_lse_from_u(a.u_out, n_per_block, n_blocks, a.ctas_per_block, a.inv_temperature,
                                             a.partials, ctx->stream));
     } else {
-        PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
+        PMGB_CK(ctx, launch_pairs_timed(ctx, a, n_ctas));
     }
     PMGB_CK(ctx, pmgb_launch_reduce_blocks(a.partials, n_blocks, a.ctas_per_block, block_out_dev, ctx->stream));
     if (refine) return run_refine(s, n_per_block, n_blocks, seed, temperature, block_out_dev, a.u_out);

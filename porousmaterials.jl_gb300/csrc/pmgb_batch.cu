@@ -20,7 +20,7 @@ constexpr int kVariantSites[6] = {1, 2, 3, 4, 6, 8};
 template <int NS, bool CHARGED, bool GRAD, bool RESID>
 __device__ __noinline__ bool run_unit_fn(const SysDev& S, const UnitIO& io, int4* stage, uint64_t* bars,
                                          LsePartial* red, uint32_t (&fills)[PMGB_NSTAGE], unsigned int* status) {
-    return run_unit<NS, CHARGED, GRAD, RESID>(S, io, stage, bars, red, fills, status);
+    return run_unit<NS, CHARGED, GRAD, RESID, false>(S, io, stage, bars, red, fills, status);  // no forces
 }
 
 template <bool GRAD, bool RESID>

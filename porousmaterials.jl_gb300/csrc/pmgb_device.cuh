@@ -255,11 +255,12 @@ __device__ __forceinline__ float dist2(const int4 r, const uint32_t ux, const ui
     return fmaf(cx, cx, fmaf(cy, cy, cz * cz));
 }
 
-// One framework record against one guest site.
-template <bool CHARGED>
+// One framework record against one guest site.  COLS: also r^-12 and r^-6 within the LJ cutoff
+// into *c12, *c6 (the adjoint's columns).
+template <bool CHARGED, bool COLS = false>
 __device__ __forceinline__ void pair_fwd(const int4 r, const uint32_t ux, const uint32_t uy, const uint32_t uz,
                                          const Geo& g, const float sig2, const float eps4, float& segmin,
-                                         float& ljp, float& php) {
+                                         float& ljp, float& php, float* c12 = nullptr, float* c6 = nullptr) {
     const float r2 = dist2(r, ux, uy, uz, g);
     segmin = fminf(segmin, r2);
     const bool in = r2 < g.rc2;
@@ -277,6 +278,11 @@ __device__ __forceinline__ void pair_fwd(const int4 r, const uint32_t ux, const 
     const float s3 = s * s * s;
     const float t = fmaf(s3, s3, -s3);
     ljp = fmaf(eps4, in ? t : 0.0f, ljp);
+    if (COLS) {
+        const float ir6 = in ? ir2 * ir2 * ir2 : 0.0f;
+        *c12 = fmaf(ir6, ir6, *c12);
+        *c6 += ir6;
+    }
     if (CHARGED) {
         const float e = erfc_fit(g.alpha * (r2 * y)) * y;
         php = fmaf(__int_as_float(r.w), (r2 < g.rc2e) ? e : 0.0f, php);
@@ -438,10 +444,12 @@ __device__ __forceinline__ float2 pair2_r2(const int4 ra, const int4 rb, const u
     return fma2(cx, cx, fma2(cy, cy, mul2(cz, cz)));
 }
 
-// LJ and real-space terms of two records at squared distances r2 (charges qa, qb).
-template <bool CHARGED>
+// LJ and real-space terms of two records at squared distances r2 (charges qa, qb); COLS: also
+// r^-12 and r^-6 within the LJ cutoff into *c12, *c6.
+template <bool CHARGED, bool COLS = false>
 __device__ __forceinline__ void pair2_energy(const float2 r2, const float qa, const float qb, const Geo2& g,
-                                             const float2 lj12, const float2 lj6, float2& ljp, float2& php) {
+                                             const float2 lj12, const float2 lj6, float2& ljp, float2& php,
+                                             float2* c12 = nullptr, float2* c6 = nullptr) {
     float2 ir2, y = f2(0.0f);
     if (CHARGED) {
         y = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
@@ -456,6 +464,10 @@ __device__ __forceinline__ void pair2_energy(const float2 r2, const float qa, co
     const float2 ir6 = mul2(mul2(ir2, ir2), ir2);
     const float2 ir6c = make_float2(r2.x < g.rc2 ? ir6.x : 0.0f, r2.y < g.rc2 ? ir6.y : 0.0f);
     ljp = fma2(ir6c, fma2(lj12, ir6c, lj6), ljp);
+    if (COLS) {
+        *c12 = __fadd2_rn(*c12, mul2(ir6c, ir6c));
+        *c6 = __fadd2_rn(*c6, ir6c);
+    }
     if (CHARGED) {
         const float2 rr = mul2(r2, y);
         const float2 e = mul2(erfc_fit2(rr, r2, g), y);
@@ -463,10 +475,11 @@ __device__ __forceinline__ void pair2_energy(const float2 r2, const float qa, co
     }
 }
 
-template <bool CHARGED, bool RESID = true>
+template <bool CHARGED, bool RESID = true, bool COLS = false>
 __device__ __forceinline__ void pair2_fwd(const int4 ra, const int4 rb, const uint32_t ux, const uint32_t uy,
                                           const uint32_t uz, const Geo2& g, const float2 lj12, const float2 lj6,
-                                          float& segmin, float2& ljp, float2& php) {
+                                          float& segmin, float2& ljp, float2& php, float2* c12 = nullptr,
+                                          float2* c6 = nullptr) {
     const float2 r2 = pair2_r2<RESID>(ra, rb, ux, uy, uz, g);  // the same distances as the culled loop
     segmin = fminf(segmin, fminf(r2.x, r2.y));
     float2 ir2, y = f2(0.0f);
@@ -485,6 +498,10 @@ __device__ __forceinline__ void pair2_fwd(const int4 ra, const int4 rb, const ui
     const float2 ir6 = mul2(mul2(ir2, ir2), ir2);
     const float2 ir6c = make_float2(r2.x < g.rc2 ? ir6.x : 0.0f, r2.y < g.rc2 ? ir6.y : 0.0f);
     ljp = fma2(ir6c, fma2(lj12, ir6c, lj6), ljp);
+    if (COLS) {
+        *c12 = __fadd2_rn(*c12, mul2(ir6c, ir6c));
+        *c6 = __fadd2_rn(*c6, ir6c);
+    }
     if (CHARGED) {
         const float2 rr = mul2(r2, y);
         const float2 e = mul2(erfc_fit2(rr, r2, g), y);
@@ -742,10 +759,15 @@ __device__ __forceinline__ bool chunk_near(const SysDev& S, const ChunkBox* box,
 // Returns false if a bounded wait gave up (the status word is set); every thread of the CTA
 // returns the same value.  fills[s] counts the completed fills of ring slot s so far; the
 // caller keeps it across units (the barriers are initialised once per CTA).
-template <int NS, bool CHARGED, bool GRAD, bool RESID = true>
+// GRAD: the adjoint's per-(segment, site) columns sum r^-12, sum r^-6; FORCES (with GRAD): also
+// dU/dx per item.  Without FORCES the adjoint runs the forward loops with the columns added, so
+// its energies are the forward kernel's.
+template <int NS, bool CHARGED, bool GRAD, bool RESID = true, bool FORCES = GRAD>
 __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4* stage, uint64_t* bars,
                                          LsePartial* red, uint32_t (&fills)[PMGB_NSTAGE], unsigned int* status) {
     static_assert(RESID || !GRAD, "the adjoint keeps the box-matrix residual");
+    static_assert(GRAD || !FORCES, "forces come with the adjoint");
+    constexpr bool COLS = GRAD && !FORCES;
     const int tid = threadIdx.x;
     const bool valid = io.valid;
     const long long item = io.item;
@@ -867,7 +889,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
 #pragma unroll
                 for (int k = 0; k < NS; ++k) ljp2[k] = php2[k] = f2(0.0f);
                 float ljp[NS], php[NS];
-                if (GRAD) {
+                if (FORCES) {
                     for (int sb = 0; sb < n_sub; ++sb) {
                     if (!(near_sub >> sb & 1u)) continue;
                     const int s_end = min(j0 + (sb + 1) * kSub, j1);
@@ -914,10 +936,10 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                             segmin[k] = fminf(segmin[k], dmin);
                             if (__any_sync(0xffffffffu, valid && !blocked && dmin < g2.rcmax2)) {
                                 const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
-                                pair2_energy<CHARGED>(d01, __int_as_float(r0.w), __int_as_float(r1.w), g2, a12, a6,
-                                                      ljp2[k], php2[k]);
-                                pair2_energy<CHARGED>(d23, __int_as_float(r2.w), __int_as_float(r3.w), g2, a12, a6,
-                                                      ljp2[k], php2[k]);
+                                pair2_energy<CHARGED, COLS>(d01, __int_as_float(r0.w), __int_as_float(r1.w), g2,
+                                                            a12, a6, ljp2[k], php2[k], &i12[k], &i6[k]);
+                                pair2_energy<CHARGED, COLS>(d23, __int_as_float(r2.w), __int_as_float(r3.w), g2,
+                                                            a12, a6, ljp2[k], php2[k], &i12[k], &i6[k]);
                             }
                         }
                     };
@@ -945,8 +967,8 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                         const int4 r = T[j - t0];
 #pragma unroll
                         for (int k = 0; k < NS; ++k)
-                            pair_fwd<CHARGED>(r, ux[k], uy[k], uz[k], g, sig2[k], eps4[k], segmin[k], ljp[k],
-                                              php[k]);
+                            pair_fwd<CHARGED, COLS>(r, ux[k], uy[k], uz[k], g, sig2[k], eps4[k], segmin[k], ljp[k],
+                                                    php[k], &i12[k].x, &i6[k].x);
                     }
                 } else {
                     int j = j0;
@@ -955,10 +977,10 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
 #pragma unroll
                         for (int k = 0; k < NS; ++k) {
                             const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
-                            pair2_fwd<CHARGED, RESID>(r0, r1, ux[k], uy[k], uz[k], g2, a12, a6, segmin[k],
-                                                      ljp2[k], php2[k]);
-                            pair2_fwd<CHARGED, RESID>(r2, r3, ux[k], uy[k], uz[k], g2, a12, a6, segmin[k],
-                                                      ljp2[k], php2[k]);
+                            pair2_fwd<CHARGED, RESID, COLS>(r0, r1, ux[k], uy[k], uz[k], g2, a12, a6, segmin[k],
+                                                            ljp2[k], php2[k], &i12[k], &i6[k]);
+                            pair2_fwd<CHARGED, RESID, COLS>(r2, r3, ux[k], uy[k], uz[k], g2, a12, a6, segmin[k],
+                                                            ljp2[k], php2[k], &i12[k], &i6[k]);
                         }
                     }
 #pragma unroll
@@ -970,8 +992,8 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                         const int4 r = T[j - t0];
 #pragma unroll
                         for (int k = 0; k < NS; ++k)
-                            pair_fwd<CHARGED>(r, ux[k], uy[k], uz[k], g, sig2[k], eps4[k], segmin[k], ljp[k],
-                                              php[k]);
+                            pair_fwd<CHARGED, COLS>(r, ux[k], uy[k], uz[k], g, sig2[k], eps4[k], segmin[k], ljp[k],
+                                                    php[k], &i12[k].x, &i6[k].x);
                     }
                 }
 #pragma unroll
@@ -1023,7 +1045,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
     float gu[NS][3];
 #pragma unroll
     for (int k = 0; k < NS; ++k) gu[k][0] = gu[k][1] = gu[k][2] = 0.0f;
-    if (CHARGED && valid) kspace_fwd<NS, GRAD>(S, ux, uy, uz, pl_hi, pl_lo, gu);
+    if (CHARGED && valid) kspace_fwd<NS, FORCES>(S, ux, uy, uz, pl_hi, pl_lo, gu);
 
     // ---- per-item energies (FP64) ----------------------------------------------
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
@@ -1035,7 +1057,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
             uv += static_cast<double>(lj_hi[k]) + static_cast<double>(lj_lo[k]);
             if (CHARGED && S.q[k] != 0.0f)
                 usr += static_cast<double>(S.q[k]) * (static_cast<double>(ph_hi[k]) + static_cast<double>(ph_lo[k]));
-            if (GRAD) {
+            if (FORCES) {
                 // real space: dU/dx_site = -2 sum c dU/dr^2; reciprocal space: G^T dU/du
                 gcx += -2.0f * (gx[k].x + gx[k].y) + S.g00 * gu[k][0];
                 gcy += -2.0f * (gy[k].x + gy[k].y) + S.g01 * gu[k][0] + S.g11 * gu[k][1];
@@ -1052,7 +1074,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
         ulr = 0.0;
         gcx = gcy = gcz = 0.0f;
     }
-    if (GRAD && valid && io.grad_u) {
+    if (FORCES && valid && io.grad_u) {
         io.grad_u[3 * item + 0] = gcx;
         io.grad_u[3 * item + 1] = gcy;
         io.grad_u[3 * item + 2] = gcz;

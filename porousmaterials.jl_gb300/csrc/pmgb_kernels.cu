@@ -6,7 +6,7 @@
 namespace {
 
 // Single-system launch: CTA b runs unit b.
-template <int NS, bool CHARGED, bool GRAD, bool RESID = true>
+template <int NS, bool CHARGED, bool GRAD, bool RESID = true, bool FORCES = GRAD>
 __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_constant__ LaunchArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     int4* stage = reinterpret_cast<int4*>(smem_raw);
@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
     io.partial = (a.partials && !a.perm) ? a.partials + blockIdx.x : nullptr;
     ring_init(bars);
     uint32_t fills[PMGB_NSTAGE] = {};
-    (void)run_unit<NS, CHARGED, GRAD, RESID>(a.sys, io, stage, bars, red, fills, a.status);
+    (void)run_unit<NS, CHARGED, GRAD, RESID, FORCES>(a.sys, io, stage, bars, red, fills, a.status);
 }
 
 // ---- latency path: few configurations, one CTA each -----------------------------------
@@ -489,14 +489,20 @@ cudaError_t launch_one(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
     return a.no_resid ? launch_one_r<NS, CH, false>(a, n_ctas, st) : launch_one_r<NS, CH, true>(a, n_ctas, st);
 }
 
+template <int NS, bool CH, bool FORCES>
+cudaError_t launch_grad_one_f(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
+    const size_t smem = pmgb_pairs_smem_bytes();
+    cudaError_t e = cudaFuncSetAttribute(pairs_kernel<NS, CH, true, true, FORCES>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    pairs_kernel<NS, CH, true, true, FORCES><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+// forces (dU/dx) only when the caller asked for them; the columns alone take the forward loops
 template <int NS, bool CH>
 cudaError_t launch_grad_one(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
-    const size_t smem = pmgb_pairs_smem_bytes();
-    cudaError_t e = cudaFuncSetAttribute(pairs_kernel<NS, CH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
-    if (e != cudaSuccess) return e;
-    pairs_kernel<NS, CH, true><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
-    return cudaGetLastError();
+    return a.grad_u ? launch_grad_one_f<NS, CH, true>(a, n_ctas, st) : launch_grad_one_f<NS, CH, false>(a, n_ctas, st);
 }
 
 template <bool CH>

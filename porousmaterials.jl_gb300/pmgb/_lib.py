@@ -70,6 +70,8 @@ SIGNATURES = [
     ("pmgb_batch_tune", C.c_int, [_vp, C.c_uint64, C.c_double, C.c_int32, _dp]),
     ("pmgb_batch_set_refine", C.c_int, [_vp, C.c_double]),
     ("pmgb_batch_set_cull", C.c_int, [_vp, C.c_int32]),
+    ("pmgb_set_kernel_timing", C.c_int, [_vp, C.c_int32]),
+    ("pmgb_kernel_timing", C.c_int, [_vp, _dp, C.POINTER(C.c_int64)]),
     ("pmgb_batch_refined_counts", C.c_int, [_vp, C.POINTER(C.c_int64)]),
     ("pmgb_batch_launch", C.c_int, [_vp, C.c_uint64, C.c_double]),
     ("pmgb_batch_results", C.c_int, [_vp, _dp, _dp]),
@@ -147,6 +149,16 @@ class Context:
 
     def synchronize(self) -> None:
         self.check(self._lib.pmgb_synchronize(self.handle))
+
+    def set_kernel_timing(self, on: bool) -> None:
+        """Record CUDA events around every Widom pass's pair-kernel launch (pmgb_set_kernel_timing)."""
+        self.check(self._lib.pmgb_set_kernel_timing(self.handle, int(bool(on))))
+
+    def kernel_timing(self) -> tuple[float, int]:
+        """(summed pair-kernel ms, launches) recorded since the last read; synchronises and clears."""
+        ms, n = C.c_double(0.0), C.c_int64(0)
+        self.check(self._lib.pmgb_kernel_timing(self.handle, C.byref(ms), C.byref(n)))
+        return ms.value, int(n.value)
 
     def device_status(self) -> int:
         st = C.c_uint32(0)

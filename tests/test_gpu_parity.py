@@ -303,6 +303,20 @@ def test_widom_parity_ewald_dense(c1):
     assert np.abs(blocks[:, 0] - ref[:, 0]).max() < 1e-6 * np.abs(ref[:, 0]).max()
 
 
+def test_kernel_timing(c0):
+    """pmgb_set_kernel_timing: one event pair per Widom pass around its pair kernel."""
+    ctx = c0.ctx
+    ctx.set_kernel_timing(True)
+    c0.widom(2000, 5, 1, 298.0)
+    c0.widom(2000, 5, 2, 298.0)
+    ms, n = ctx.kernel_timing()
+    assert n == 2 and ms > 0.0
+    assert ctx.kernel_timing() == (0.0, 0)  # cleared by the read
+    ctx.set_kernel_timing(False)
+    c0.widom(2000, 5, 3, 298.0)
+    assert ctx.kernel_timing() == (0.0, 0)
+
+
 def test_widom_deterministic(c0):
     a, _ = c0.widom(3000, 5, 77, 298.0)
     b, _ = c0.widom(3000, 5, 77, 298.0)
