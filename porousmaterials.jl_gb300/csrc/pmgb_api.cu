@@ -73,6 +73,11 @@ struct pmgb_system {
     int* d_kabc = nullptr;          // k-vectors in half-row traversal order
     double* d_wt = nullptr;
     double* d_es = nullptr;         // erfc(alpha r)/r table of the FP64 refinement
+    float2* d_es_df = nullptr;      // the same as double-float
+    float4* d_rec_rq = nullptr;     // double-float record data of the refinement
+    float* d_rec_qlo = nullptr;
+    float4* d_segpar_df = nullptr;
+    float4* d_tk_df = nullptr;       // wt S(k) of the evaluated k-vectors, double-float
     std::vector<int> k_order;       // traversal position -> caller's k index
     std::vector<double> h_sk;       // S(k) of every caller k-vector (re, im), caller order
     int n_k = 0;
@@ -241,6 +246,12 @@ bool upper_factor(const double H[9], double R[9], double Q[9]) {
     return true;
 }
 
+// x as a double-float (hi, lo): hi = x rounded to FP32, lo = the FP32 remainder
+inline float2 to_df(double x) {
+    const float hi = static_cast<float>(x);
+    return make_float2(hi, static_cast<float>(x - static_cast<double>(hi)));
+}
+
 // hash of an exact position (the bit patterns of three doubles in [0, 1))
 inline size_t pos_hash(double x, double y, double z) {
     uint64_t a, b, c;
@@ -404,7 +415,8 @@ static void free_system_device(pmgb_system* s) {
                     s->in_buf.p,   s->out_buf.p,   s->axes.p,    s->g_u.p,    s->g_dsum.p, s->g_grad.p,
                     s->g_part.p,   s->g_cols.p,   s->r_hist.p,  s->r_cut.p,  s->r_counts.p, s->r_offsets.p,
                     s->r_list.p,   s->r_ref.p,    s->o_counts.p, s->o_perm.p,  s->r_plan.p,  s->r_done.p,
-                    s->r_part.p,   s->acc.p,      s->d_cbox,    s->d_es};
+                    s->r_part.p,   s->acc.p,      s->d_cbox,    s->d_es,     s->d_es_df,  s->d_rec_rq,
+                    s->d_rec_qlo,  s->d_segpar_df, s->d_tk_df};
     for (void* p : ptrs) dev_free(s->ctx, p);
 }
 
@@ -529,6 +541,8 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     std::vector<int4> h_rec;
     std::vector<double> h_rec_q;   // FP64 charge of each record
     std::vector<double> h_rec_xf;  // its exact fractional coordinates
+    std::vector<float4> h_rec_rq;  // position beyond the fixed point (units of 2^-32), q hi
+    std::vector<float> h_rec_qlo;  // q lo
     std::vector<SegDesc> h_seg;
     for (size_t p = 0; p < order.size();) {
         const int sp = recs[order[p]].species;
@@ -547,6 +561,13 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
             h_rec_xf.push_back(r.x);
             h_rec_xf.push_back(r.y);
             h_rec_xf.push_back(r.z);
+            // the fixed point rounds u 2^32 to the nearest integer (mod 2^32): keep the remainder
+            const double rx = r.x * 4294967296.0 - static_cast<double>(std::llround(r.x * 4294967296.0));
+            const double ry = r.y * 4294967296.0 - static_cast<double>(std::llround(r.y * 4294967296.0));
+            const double rz = r.z * 4294967296.0 - static_cast<double>(std::llround(r.z * 4294967296.0));
+            const float2 qd = to_df(r.q);
+            h_rec_rq.push_back(make_float4(static_cast<float>(rx), static_cast<float>(ry), static_cast<float>(rz), qd.x));
+            h_rec_qlo.push_back(qd.y);
         }
         d.hi = static_cast<int>(h_rec.size());
         d.species = sp;
@@ -609,6 +630,7 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     // per (segment, site) LJ parameters
     std::vector<SitePar> h_par(h_seg.size() * PMGB_MAX_SITES, SitePar{1.0f, 0.0f, -1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f});
     std::vector<double2> h_par64(h_seg.size() * PMGB_MAX_SITES, make_double2(-1.0, 0.0));  // -1: no LJ
+    std::vector<float4> h_par_df(h_seg.size() * PMGB_MAX_SITES, make_float4(-1.0f, 0.0f, 0.0f, 0.0f));
     for (size_t g = 0; g < h_seg.size(); ++g)
         for (int k = 0; k < ns; ++k) {
             const int a = s->site_atom[k];
@@ -623,6 +645,8 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
             p.lj6 = static_cast<float>(-e4 * s2 * s2 * s2);
             p.r2ovl = 0.1f;  // R²_OVERLAP, src/vdw_energetics.jl:2
             h_par64[g * PMGB_MAX_SITES + k] = make_double2(s2, e4);
+            const float2 s2d = to_df(s2), e4d = to_df(e4);
+            h_par_df[g * PMGB_MAX_SITES + k] = make_float4(s2d.x, s2d.y, e4d.x, e4d.y);
         }
 
     // bounding box of every sub-chunk of records, in the kernels' traversal order
@@ -674,7 +698,8 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
         (rc = upload(ctx, &s->d_rec_q, h_rec_q, nb)) ||
         (rc = upload(ctx, &s->d_segpar64, h_par64, nb)) || (rc = upload(ctx, &s->d_seg, h_seg, nb)) ||
         (rc = upload(ctx, &s->d_segpar, h_par, nb)) || (rc = upload(ctx, &s->d_qxf, h_qxf, nb)) ||
-        (rc = upload(ctx, &s->d_rec_xf, h_rec_xf, nb)) ||
+        (rc = upload(ctx, &s->d_rec_xf, h_rec_xf, nb)) || (rc = upload(ctx, &s->d_rec_rq, h_rec_rq, nb)) ||
+        (rc = upload(ctx, &s->d_rec_qlo, h_rec_qlo, nb)) || (rc = upload(ctx, &s->d_segpar_df, h_par_df, nb)) ||
         (rc = upload(ctx, &s->d_q, h_q, nb))) {
         free_system_device(s);
         delete s;
@@ -763,7 +788,15 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     for (int i = 0; i < 6; ++i) {
         D.f2c64[i] = R[up[i]];
         D.g64[i] = G[up[i]];
+        D.h_df[i] = to_df(R[up[i]] * fix_unit);
     }
+    D.rec_rq = s->d_rec_rq;
+    D.rec_qlo = s->d_rec_qlo;
+    D.segpar_df = s->d_segpar_df;
+    D.rc2_df = to_df(r2_cutoff);
+    D.rc2e_df = D.rc2_df;
+    D.es_tab_df = nullptr;
+    D.es_n_oct = 0;
     D.rc2 = static_cast<float>(r2_cutoff);
     D.rc2e = static_cast<float>(r2_cutoff);
     D.alpha = 0.0f;
@@ -899,7 +932,7 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
         k = e;
     }
     // drop previous Ewald state
-    void* old[] = {s->d_krow, s->d_skw, s->d_sk, s->d_kabc, s->d_wt, s->d_es};
+    void* old[] = {s->d_krow, s->d_skw, s->d_sk, s->d_kabc, s->d_wt, s->d_es, s->d_es_df, s->d_tk_df};
     for (void* p : old) dev_free(ctx, p);
     s->d_krow = nullptr;
     s->d_skw = nullptr;
@@ -907,6 +940,8 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
     s->d_kabc = nullptr;
     s->d_wt = nullptr;
     s->d_es = nullptr;
+    s->d_es_df = nullptr;
+    s->d_tk_df = nullptr;
     s->ewald_set = false;
     int rc;
     if ((rc = upload(ctx, &s->d_kabc, kabc, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_wt, wt, &s->h2d_bytes)))
@@ -992,10 +1027,21 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
             return rc;
         rows.swap(rows_p);
         n_eval = static_cast<int>(wt_p.size());
+        wt.swap(wt_p);
+        sk.swap(sk_p);
     }
+    std::vector<float4> tk(static_cast<size_t>(n_eval));  // wt S(k) as double-float, the kept k-vectors
+    for (int i = 0; i < n_eval; ++i) {
+        const float2 re = to_df(wt[i] * sk[2 * i]), im = to_df(wt[i] * sk[2 * i + 1]);
+        tk[i] = make_float4(re.x, re.y, im.x, im.y);
+    }
+    if ((rc = upload(ctx, &s->d_tk_df, tk, &s->h2d_bytes))) return rc;
     if ((rc = upload(ctx, &s->d_krow, rows, &s->h2d_bytes))) return rc;
     const std::vector<double> es = erfc_over_r_table(alpha, sr_cutoff * sr_cutoff);
-    if ((rc = upload(ctx, &s->d_es, es, &s->h2d_bytes))) return rc;
+    std::vector<float2> es_df(es.size());
+    for (size_t i = 0; i < es.size(); ++i) es_df[i] = to_df(es[i]);
+    if ((rc = upload(ctx, &s->d_es, es, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_es_df, es_df, &s->h2d_bytes)))
+        return rc;
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // the uploads read host vectors
     s->n_k = n_kvecs;
     s->k_order = order;
@@ -1007,6 +1053,10 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
     s->dev.rc2e_64 = sr_cutoff * sr_cutoff;
     s->dev.es_tab = s->d_es;
     s->dev.es_e_lo = PMGB_ES_E_LO;
+    s->dev.es_n_oct = static_cast<int>(es.size() / (PMGB_ES_COEF * PMGB_ES_SUB));
+    s->dev.es_tab_df = s->d_es_df;
+    s->dev.tk_df = s->d_tk_df;
+    s->dev.rc2e_df = to_df(sr_cutoff * sr_cutoff);
     s->dev.sk64 = s->d_sk;
     s->dev.wt64 = s->d_wt;
     s->dev.kabc = s->d_kabc;

@@ -109,7 +109,16 @@ struct SysDev {
     // [2^e (1 + m/32), 2^e (1 + (m+1)/32)), e >= es_e_lo, m < 32, a degree-7 polynomial in
     // t = 64 x - (65 + 2 m) (x = s 2^-e), PMGB_ES_COEF coefficients from t^0 up
     const double* es_tab;
-    int es_e_lo;
+    int es_e_lo, es_n_oct;
+    // double-float copies (value = hi + lo, two FP32 numbers, ~48 significant bits) for the
+    // refinement's near-pair terms, which run on the FP32 pipes
+    const float4* rec_rq;                   // [n_rec] x, y, z beyond the 32-bit fixed point (units of 2^-32), q hi
+    const float* rec_qlo;                   // [n_rec] q lo
+    const float4* segpar_df;                // [n_seg * PMGB_MAX_SITES] sigma^2 (hi, lo), 4 eps (hi, lo)
+    const float2* es_tab_df;                // es_tab as (hi, lo)
+    const float4* tk_df;                    // [n_k] wt_k S(k) (re hi, re lo, im hi, im lo), half-row order
+    float2 h_df[6];                         // f2c64 * 2^-32: Cartesian per fixed-point unit
+    float2 rc2_df, rc2e_df;
     // optional accessibility gate (src/henry.jl:225): blocked insertions get U = +Inf
     const uint8_t* acc;                     // [acc_n0 * acc_n1 * acc_n2], i fastest; 0 = inaccessible
     int acc_n[3];                           // grid points per axis of the unit-cell grid

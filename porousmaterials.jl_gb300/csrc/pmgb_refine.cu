@@ -218,6 +218,156 @@ __device__ __forceinline__ void pair_fp64(const SysDev& S, int sg, int k, double
         sr += S.q64[k] * qj * erfc_over_r(S, r2);
 }
 
+// ---- double-float arithmetic (value = hi + lo, two FP32 numbers) ----------------------------
+// Error-free sums and products (Knuth's TwoSum, Dekker's Fast2Sum, the FMA product error) written
+// with the round-to-nearest intrinsics, which the compiler neither contracts nor reassociates; a
+// double-float carries ~48 significant bits and runs on the FP32 pipes (FP64 runs at 1/64 of
+// their rate on this GPU).
+struct dfl {
+    float hi, lo;
+};
+__device__ __forceinline__ dfl two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ dfl fast_two_sum(float a, float b) {  // |a| >= |b| (or a == 0)
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ dfl df_add(dfl x, dfl y) {
+    const dfl s = two_sum(x.hi, y.hi);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+__device__ __forceinline__ dfl df_add_f(dfl x, float y) {
+    const dfl s = two_sum(x.hi, y);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, x.lo));
+}
+__device__ __forceinline__ dfl df_mul(dfl x, dfl y) {
+    const float p = __fmul_rn(x.hi, y.hi);
+    float e = __fmaf_rn(x.hi, y.hi, -p);
+    e = __fmaf_rn(x.hi, y.lo, e);
+    e = __fmaf_rn(x.lo, y.hi, e);
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ dfl df_sqr(dfl x) {
+    const float p = __fmul_rn(x.hi, x.hi);
+    float e = __fmaf_rn(x.hi, x.hi, -p);
+    e = __fmaf_rn(__fmul_rn(2.0f, x.hi), x.lo, e);
+    return fast_two_sum(p, e);
+}
+// 1/x: the FP32 reciprocal q and one correction q r, r = 1 - x q evaluated in double-float
+__device__ __forceinline__ dfl df_rcp(dfl x) {
+    const float q = __frcp_rn(x.hi);
+    const float p = __fmul_rn(x.hi, q);
+    const float pe = __fmaf_rn(x.hi, q, -p);                            // x.hi q = p + pe exactly
+    const float r = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, p), pe), __fmul_rn(x.lo, q));
+    return fast_two_sum(q, __fmul_rn(r, q));
+}
+__device__ __forceinline__ bool df_lt(dfl a, float2 b) { return a.hi < b.x || (a.hi == b.x && a.lo < b.y); }
+__device__ __forceinline__ dfl df_of(float2 v) { return {v.x, v.y}; }
+__device__ __forceinline__ double df_to_double(dfl x) { return static_cast<double>(x.hi) + static_cast<double>(x.lo); }
+
+// erfc(alpha r)/r at s = r^2 (double-float) from the double-float table: interval from the FP32
+// bits of s.hi, t = 64 x - (65 + 2 m) exact in its high part; terms t^4.. in FP32 (they are below
+// 1e-3 of the value), t^3.. t^0 in double-float.  Outside the table: the FP64 form.
+__device__ __forceinline__ dfl erfc_over_r_df(const SysDev& S, dfl s) {
+    const uint32_t bits = __float_as_uint(s.hi);
+    const int e = static_cast<int>((bits >> 23) & 0xff) - 127;
+    const int oct = e - S.es_e_lo;
+    if (oct < 0 || oct >= S.es_n_oct) {
+        const double v = erfc_over_r(S, df_to_double(s));
+        const float hi = static_cast<float>(v);
+        return {hi, static_cast<float>(v - static_cast<double>(hi))};
+    }
+    const int m = static_cast<int>((bits >> 18) & (PMGB_ES_SUB - 1));
+    const float xh = __uint_as_float((bits & 0x007fffffu) | 0x3f800000u);          // s.hi 2^-e in [1, 2)
+    const float xl = __fmul_rn(s.lo, __uint_as_float(static_cast<uint32_t>(127 - e) << 23));  // s.lo 2^-e
+    const float th = __fmaf_rn(xh, 2.0f * PMGB_ES_SUB, -(2.0f * PMGB_ES_SUB + 1.0f + 2.0f * m));  // exact
+    const dfl t = fast_two_sum(th, __fmul_rn(xl, 2.0f * PMGB_ES_SUB));
+    const float2* c = S.es_tab_df + PMGB_ES_COEF * (oct * PMGB_ES_SUB + m);
+    float p = __ldg(c + PMGB_ES_COEF - 1).x;
+#pragma unroll
+    for (int j = PMGB_ES_COEF - 2; j >= 4; --j) p = fmaf(p, t.hi, __ldg(c + j).x);
+    dfl v{p, 0.0f};
+#pragma unroll
+    for (int j = 3; j >= 0; --j) v = df_add(df_mul(v, t), df_of(__ldg(c + j)));
+    return v;
+}
+
+// ---- reciprocal space in double-float ------------------------------------------------------
+struct dfc {
+    dfl re, im;
+};
+__device__ __forceinline__ dfl df_neg(dfl x) { return {-x.hi, -x.lo}; }
+__device__ __forceinline__ dfc dfc_mul(dfc a, dfc b) {
+    return {df_add(df_mul(a.re, b.re), df_neg(df_mul(a.im, b.im))), df_add(df_mul(a.re, b.im), df_mul(a.im, b.re))};
+}
+
+// e^{-2 pi i j / 256}, j < 256, as double-float (re hi, re lo, im hi, im lo): one per CTA in shared memory
+__device__ __forceinline__ void phase_table_init(float4* tab) {
+    for (int j = threadIdx.x; j < 256; j += blockDim.x) {
+        double sn, cs;
+        sincospi(-static_cast<double>(j) / 128.0, &sn, &cs);
+        const float ch = static_cast<float>(cs), sh = static_cast<float>(sn);
+        tab[j] = make_float4(ch, static_cast<float>(cs - static_cast<double>(ch)), sh,
+                             static_cast<float>(sn - static_cast<double>(sh)));
+    }
+}
+
+// e^{-2 pi i P / 2^64} for a 64-bit fixed-point phase P (exact modulo one turn): the table entry of
+// its top 8 bits times e^{-i phi}, phi = 2 pi (the next 48 bits) < 2 pi / 256, by the Taylor
+// series of sin and cos (truncation below 1e-19; the terms below 1e-8 of the value in FP32)
+__device__ __forceinline__ dfc phase64(uint64_t P, const float4* tab) {
+    const float4 t = tab[static_cast<int>(P >> 56)];
+    const float rh = __fmul_rn(__uint2float_rn(static_cast<uint32_t>(P >> 32) & 0xffffffu), 2.3283064365386963e-10f);
+    const float rl = __fmul_rn(__uint2float_rn(static_cast<uint32_t>(P >> 8) & 0xffffffu), 1.3877787807814457e-17f);
+    const dfl phi = df_mul(fast_two_sum(rh, rl), dfl{6.2831854820251465f, -1.7484556e-07f});  // x 2 pi
+    const dfl p2 = df_sqr(phi);
+    // sin phi = phi (1 - p2/6 + p2^2/120 - p2^3/5040)
+    const float ss = __fmul_rn(__fmul_rn(p2.hi, p2.hi), fmaf(p2.hi, -1.0f / 5040.0f, 1.0f / 120.0f));
+    const dfl sn = df_mul(phi, df_add_f(df_add(dfl{1.0f, 0.0f}, df_mul(p2, dfl{-0.16666667f, 4.9670538e-09f})), ss));
+    // cos phi = 1 - p2/2 + p2^2/24 - p2^3/720 + p2^4/40320
+    const dfl c4 = df_mul(df_sqr(p2), dfl{0.041666668f, -1.2417635e-09f});
+    const float cs6 = __fmul_rn(__fmul_rn(__fmul_rn(p2.hi, p2.hi), p2.hi), fmaf(p2.hi, 1.0f / 40320.0f, -1.0f / 720.0f));
+    const dfl cs = df_add_f(df_add(df_add(dfl{1.0f, 0.0f}, dfl{-0.5f * p2.hi, -0.5f * p2.lo}), c4), cs6);
+    return dfc_mul(dfc{dfl{t.x, t.y}, dfl{t.z, t.w}}, dfc{cs, df_neg(sn)});
+}
+
+// 64-bit fixed point of a fractional coordinate (x - floor(x)) 2^64, rounded
+__device__ __forceinline__ uint64_t frac2fix128(double x) {
+    double f = x - floor(x);
+    if (f >= 1.0) f = 0.0;
+    return __double2ull_rn(f * 18446744073709551616.0);
+}
+
+// Reciprocal-space potential of one guest site at fractional x over the half-rows [row0, row_end)
+// stepping by row_step, sum_k Re[wt S(k) e^{-ik.x}], in double-float: row starts from exact 64-bit
+// fixed-point phases (the strides ks applied in fixed point), steps along kc by the recurrence.
+__device__ dfl kspace_df_rows(const SysDev& S, const double* x, int row0, int row_end, int row_step,
+                              const float4* tab) {
+    const uint64_t U0 = static_cast<uint64_t>(S.ks[0]) * frac2fix128(x[0]);
+    const uint64_t U1 = static_cast<uint64_t>(S.ks[1]) * frac2fix128(x[1]);
+    const uint64_t U2 = static_cast<uint64_t>(S.ks[2]) * frac2fix128(x[2]);
+    const dfc w = phase64(U2, tab);  // one step along +kc
+    dfl lr{0.0f, 0.0f};
+    for (int row = row0; row < row_end; row += row_step) {
+        const KRow R = S.krow[row];
+        const uint64_t P = static_cast<uint64_t>(static_cast<int64_t>(R.ka)) * U0 +
+                           static_cast<uint64_t>(static_cast<int64_t>(R.kb)) * U1 +
+                           static_cast<uint64_t>(static_cast<int64_t>(R.kc0)) * U2;
+        dfc e = phase64(P, tab);
+        const dfc sw{w.re, R.dir > 0 ? w.im : df_neg(w.im)};  // downward rows step by the conjugate
+        const float4* T = S.tk_df + R.off;
+        for (int m = 0; m < R.n; ++m) {
+            const float4 t = __ldg(T + m);
+            lr = df_add(lr, df_add(df_mul(dfl{t.x, t.y}, e.re), df_neg(df_mul(dfl{t.z, t.w}, e.im))));
+            e = dfc_mul(e, sw);
+        }
+    }
+    return lr;
+}
+
 // FP32 screen of the (record, guest site) pairs.  The guest sites are taken to the records'
 // 32-bit fixed point once per insertion; a pair is passed on to pair_fp64 unless its FP32
 // distance lies beyond every cutoff plus 0.01 A (the FP32 distance is within ~1e-4 A of the
@@ -226,14 +376,23 @@ __device__ __forceinline__ void pair_fp64(const SysDev& S, int sg, int k, double
 // half a cell on some axis is always passed on: there the two nearest-image choices may differ.
 struct SiteScreen {
     uint32_t x[PMGB_MAX_SITES], y[PMGB_MAX_SITES], z[PMGB_MAX_SITES];
+    float rx[PMGB_MAX_SITES], ry[PMGB_MAX_SITES], rz[PMGB_MAX_SITES];  // beyond the fixed point (2^-32 units)
+    dfl q[PMGB_MAX_SITES];                                              // guest charges
     float r2max;
 };
 
 __device__ __forceinline__ void screen_init(const SysDev& S, const double (*xs)[3], SiteScreen& sc) {
     for (int k = 0; k < S.n_sites; ++k) {
-        sc.x[k] = frac2fix64(xs[k][0]);
-        sc.y[k] = frac2fix64(xs[k][1]);
-        sc.z[k] = frac2fix64(xs[k][2]);
+        const double ux = xs[k][0] * 4294967296.0, uy = xs[k][1] * 4294967296.0, uz = xs[k][2] * 4294967296.0;
+        const long long fx = __double2ll_rn(ux), fy = __double2ll_rn(uy), fz = __double2ll_rn(uz);
+        sc.x[k] = static_cast<uint32_t>(fx);  // as frac2fix64
+        sc.y[k] = static_cast<uint32_t>(fy);
+        sc.z[k] = static_cast<uint32_t>(fz);
+        sc.rx[k] = static_cast<float>(ux - static_cast<double>(fx));
+        sc.ry[k] = static_cast<float>(uy - static_cast<double>(fy));
+        sc.rz[k] = static_cast<float>(uz - static_cast<double>(fz));
+        const float qh = static_cast<float>(S.q64[k]);
+        sc.q[k] = {qh, static_cast<float>(S.q64[k] - static_cast<double>(qh))};
     }
     const double rmax = sqrt(fmax(S.rc2_64, S.charged ? S.rc2e_64 : 0.0)) + 0.01;
     sc.r2max = static_cast<float>(rmax * rmax);
@@ -316,24 +475,57 @@ __device__ void energy_fp64_thread(const SysDev& S, const double (*xs)[3], doubl
 constexpr int kQueueLen = 32 + 32 * PMGB_MAX_SITES;  // a partial round + one batch of 32 records
 static_assert(PMGB_MAX_SITES <= 8, "queue entries keep the guest site in 3 bits");
 
-__device__ __forceinline__ void queued_pair(const SysDev& S, int sg, int e, const double (*xs)[3], double& v,
-                                            double& sr, bool& ovl) {
+// One queued (record, site) pair in double-float: the displacement from the 32-bit fixed points
+// (exact nearest image, as the screen) plus the remainders beyond them, Cartesian through the
+// double-float box, then the terms of pair_fp64.
+__device__ __forceinline__ dfl fix_disp(uint32_t rf, float rr, uint32_t sf, float sr_) {
+    const int i = static_cast<int>(rf - sf);
+    const float ih = __int2float_rn(i);
+    const dfl di{ih, __int2float_rn(i - __float2int_rn(ih))};  // exact: |i - ih| < 2^8
+    return df_add_f(di, __fsub_rn(rr, sr_));
+}
+__device__ __forceinline__ void queued_pair(const SysDev& S, int sg, int e, const SiteScreen& sc, dfl& v, dfl& sr,
+                                            bool& ovl) {
     const int j = e >> 3, k = e & 7;
-    pair_fp64(S, sg, k, S.rec_xf[3 * j], S.rec_xf[3 * j + 1], S.rec_xf[3 * j + 2], S.rec_q[j], xs[k], v, sr, ovl);
+    const int4 rf = __ldg(S.rec + j);
+    const float4 rq = __ldg(S.rec_rq + j);
+    const dfl dx = fix_disp(static_cast<uint32_t>(rf.x), rq.x, sc.x[k], sc.rx[k]);
+    const dfl dy = fix_disp(static_cast<uint32_t>(rf.y), rq.y, sc.y[k], sc.ry[k]);
+    const dfl dz = fix_disp(static_cast<uint32_t>(rf.z), rq.z, sc.z[k], sc.rz[k]);
+    const dfl cx = df_add(df_add(df_mul(df_of(S.h_df[0]), dx), df_mul(df_of(S.h_df[1]), dy)), df_mul(df_of(S.h_df[2]), dz));
+    const dfl cy = df_add(df_mul(df_of(S.h_df[3]), dy), df_mul(df_of(S.h_df[4]), dz));
+    const dfl cz = df_mul(df_of(S.h_df[5]), dz);
+    const dfl r2 = df_add(df_add(df_sqr(cx), df_sqr(cy)), df_sqr(cz));
+    const float4 p = __ldg(S.segpar_df + sg * PMGB_MAX_SITES + k);  // sigma^2 (hi, lo), 4 eps (hi, lo)
+    if (p.x >= 0.0f) {
+        if (df_lt(r2, make_float2(0.1f, 1.4901161e-09f))) {  // 0.1 as a double-float (R²_OVERLAP)
+            ovl = true;
+        } else if (df_lt(r2, S.rc2_df)) {
+            const dfl t = df_mul(dfl{p.x, p.y}, df_rcp(r2));
+            const dfl t3 = df_mul(df_sqr(t), t);
+            const dfl u = df_add(df_sqr(t3), dfl{-t3.hi, -t3.lo});
+            v = df_add(v, df_mul(dfl{p.z, p.w}, u));
+        }
+    }
+    if (S.charged && rq.w != 0.0f && sc.q[k].hi != 0.0f && df_lt(r2, S.rc2e_df) && r2.hi > 0.0f) {
+        const dfl qq = df_mul(sc.q[k], dfl{rq.w, __ldg(S.rec_qlo + j)});
+        sr = df_add(sr, df_mul(qq, erfc_over_r_df(S, r2)));
+    }
 }
 
 // Part of the FP64 energies evaluated by one warp: framework records [j0, j1) and k-space half-rows
 // [k0, k1).  The lanes screen 32 records at a time in FP32 and queue the (record, site) pairs that
-// may lie inside a cutoff in `queue` (kQueueLen entries of this warp's shared memory); the FP64
-// terms run in full rounds of 32 queued pairs, so a warp pays FP64 work only for pairs near the
-// insertion however they are spread over its lanes.  k-space rows: lanes stride over them.
+// may lie inside a cutoff in `queue` (kQueueLen entries of this warp's shared memory); their terms
+// run in double-float in full rounds of 32 queued pairs, so a warp pays only for pairs near the
+// insertion however they are spread over its lanes.  k-space rows (FP64): lanes stride over them.
 // out4 = (U_vdw part, U_sr part / coul, U_lr part, overlap).
 __device__ void energy_fp64_warp_part(const SysDev& S, const double (*xs)[3], int j0, int j1, int k0, int k1,
-                                      double* out4, int* queue) {
+                                      double* out4, int* queue, const float4* phase_tab) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int ns = S.n_sites;
-    double v = 0.0, sr = 0.0, lr = 0.0;
+    double lr = 0.0;
+    dfl vd{0.0f, 0.0f}, srd{0.0f, 0.0f};  // this lane's pair sums (double-float)
     bool ovl = false;
     SiteScreen sc;
     screen_init(S, xs, sc);
@@ -357,7 +549,7 @@ __device__ void energy_fp64_warp_part(const SysDev& S, const double (*xs)[3], in
             queued += total;
             __syncwarp();
             int done = 0;
-            for (; queued - done >= 32; done += 32) queued_pair(S, sg, queue[done + lane], xs, v, sr, ovl);
+            for (; queued - done >= 32; done += 32) queued_pair(S, sg, queue[done + lane], sc, vd, srd, ovl);
             // carry the partial round to the front of the queue
             const int left = queued - done;
             const int carry = (lane < left) ? queue[done + lane] : 0;
@@ -366,12 +558,16 @@ __device__ void energy_fp64_warp_part(const SysDev& S, const double (*xs)[3], in
             __syncwarp();
             queued = left;
         }
-        if (lane < queued) queued_pair(S, sg, queue[lane], xs, v, sr, ovl);
+        if (lane < queued) queued_pair(S, sg, queue[lane], sc, vd, srd, ovl);
         __syncwarp();  // the queue is free for the next segment
     }
-    if (S.charged && k1 > k0)
+    if (S.charged && k1 > k0) {
+        dfl lrd{0.0f, 0.0f};
         for (int k = 0; k < ns; ++k)
-            if (S.q64[k] != 0.0) lr += S.q64[k] * kspace_fp64_rows(S, xs[k], k0 + lane, k1, 32);
+            if (S.q64[k] != 0.0) lrd = df_add(lrd, df_mul(sc.q[k], kspace_df_rows(S, xs[k], k0 + lane, k1, 32, phase_tab)));
+        lr = df_to_double(lrd);
+    }
+    double v = df_to_double(vd), sr = df_to_double(srd);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -507,6 +703,9 @@ __global__ void __launch_bounds__(1024) refine_plan_kernel(const __grid_constant
 // whatever the scheduling) and stores the insertion's FP64 energies.
 __global__ void __launch_bounds__(PMGB_THREADS) refine_large_kernel(const __grid_constant__ RefineArgs a, int n_ctas) {
     __shared__ int s_queue[PMGB_THREADS / 32][kQueueLen];
+    __shared__ float4 s_phase[256];
+    phase_table_init(s_phase);
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     const int total = a.plan[a.n_systems];
     for (;;) {
@@ -535,7 +734,7 @@ __global__ void __launch_bounds__(PMGB_THREADS) refine_large_kernel(const __grid
         const int k0 = static_cast<int>(static_cast<long long>(S.n_krow) * c / C);
         const int k1 = static_cast<int>(static_cast<long long>(S.n_krow) * (c + 1) / C);
         double* p = a.part + 4 * static_cast<size_t>(i);
-        energy_fp64_warp_part(S, xs, j0, j1, k0, k1, p, s_queue[threadIdx.x >> 5]);
+        energy_fp64_warp_part(S, xs, j0, j1, k0, k1, p, s_queue[threadIdx.x >> 5], s_phase);
         if (lane == 0 && C == 1) {  // the whole insertion in one chunk
             double* out = a.ref_u + 3 * static_cast<size_t>(r);
             out[0] = p[3] > 0.0 ? __longlong_as_double(0x7ff0000000000000ll) : p[0];
