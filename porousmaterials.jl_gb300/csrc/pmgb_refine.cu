@@ -583,14 +583,14 @@ __device__ void energy_fp64_warp_part(const SysDev& S, const double (*xs)[3], in
     }
 }
 
-// FP64 work units of one insertion (pair terms + reciprocal-space terms).  Small insertions are
+// Work units of one insertion (pair terms + reciprocal-space terms).  Tiny insertions are
 // evaluated by one thread each; the others are cut into chunks (records and k-space half-rows in
 // proportion), one warp per chunk, so that one large insertion spreads over many SMs instead of
-// waiting on one warp's FP64 latency.  The chunk size adapts to the system's number of refined
-// insertions: ~1024 units while its chunk-items stay within 4096 (a few insertions: the pass is
-// latency-bound, finer chunks fill more SMs), else ~4096 units (many insertions: fewer partials
-// and less per-chunk overhead).  The count is the same for a system alone or in a batch, so the
-// two evaluate identical chunks.
+// waiting on one warp.  The chunk size adapts to the system's number of refined insertions: ~1024
+// units while its chunk-items stay within 4096 (a few insertions: the pass is latency-bound, finer
+// chunks fill more SMs), else ~16384 units (many insertions: fewer repetitions of the per-chunk
+// set-up).  The count is the same for a system alone or in a batch, so the two evaluate identical
+// chunks.
 __device__ __forceinline__ long long fp64_work(const SysDev& S) {
     return static_cast<long long>(S.n_sites) * (S.n_rec + (S.charged ? S.n_k : 0));
 }
@@ -599,7 +599,7 @@ __device__ __forceinline__ int fp64_chunks(const SysDev& S, long long count) {
     if (small_system(S)) return 0;
     const long long fine = min(64ll, (fp64_work(S) + 1023) / 1024);
     if (count * fine <= 4096) return static_cast<int>(fine);
-    return static_cast<int>(min(64ll, (fp64_work(S) + 4095) / 4096));
+    return static_cast<int>(min(64ll, (fp64_work(S) + 16383) / 16384));
 }
 
 __device__ __forceinline__ void refined_entry(const RefineArgs& a, long long e, const SysDev*& S, double (*xs)[3]) {
