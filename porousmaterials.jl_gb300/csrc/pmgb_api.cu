@@ -46,6 +46,10 @@ struct pmgb_ctx {
     // device memory of systems and batches: a stream-ordered pool that keeps freed memory for
     // reuse (repeated set-up, as in a screening loop over the drop-in, allocates from the cache)
     cudaMemPool_t pool = nullptr;
+    // the last erfc(alpha r)/r table built (set-up of many systems with one Ewald precision and
+    // cutoff reuses it)
+    double es_alpha = 0.0, es_smax = 0.0;
+    std::vector<double> es_table;
     // optional CUDA events around the Widom passes' pair-kernel launches (pmgb_set_kernel_timing)
     bool timing = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timing_events;
@@ -844,6 +848,13 @@ std::vector<double> erfc_over_r_table(double alpha, double s_max) {
     int e_hi = 0;
     std::frexp(s_max, &e_hi);  // s_max < 2^e_hi
     const int n = PMGB_ES_COEF;
+    // cos(j pi (k + 1/2) / n): the Chebyshev nodes (j = 1) and the T_j values at them
+    static const auto cheb = [] {
+        std::vector<double> c(PMGB_ES_COEF * PMGB_ES_COEF);
+        for (int j = 0; j < PMGB_ES_COEF; ++j)
+            for (int k = 0; k < PMGB_ES_COEF; ++k) c[j * PMGB_ES_COEF + k] = std::cos(j * M_PI * (k + 0.5) / PMGB_ES_COEF);
+        return c;
+    }();
     std::vector<double> tab;
     tab.reserve(static_cast<size_t>(std::max(0, e_hi - PMGB_ES_E_LO)) * PMGB_ES_SUB * n);
     for (int e = PMGB_ES_E_LO; e < e_hi; ++e)
@@ -852,7 +863,7 @@ std::vector<double> erfc_over_r_table(double alpha, double s_max) {
             const double b = std::ldexp(1.0 + static_cast<double>(m + 1) / PMGB_ES_SUB, e);
             double fk[PMGB_ES_COEF], tk[PMGB_ES_COEF];
             for (int k = 0; k < n; ++k) {
-                tk[k] = std::cos(M_PI * (k + 0.5) / n);
+                tk[k] = cheb[n + k];
                 const double sv = 0.5 * (a + b) + 0.5 * (b - a) * tk[k];
                 const double r = std::sqrt(sv);
                 fk[k] = std::erfc(alpha * r) / r;
@@ -863,7 +874,7 @@ std::vector<double> erfc_over_r_table(double alpha, double s_max) {
             tj[0] = 1.0;
             for (int j = 0; j < n; ++j) {
                 double c = 0.0;
-                for (int k = 0; k < n; ++k) c += fk[k] * std::cos(j * M_PI * (k + 0.5) / n);
+                for (int k = 0; k < n; ++k) c += fk[k] * cheb[j * n + k];
                 c *= (j == 0 ? 1.0 : 2.0) / n;
                 for (int i = 0; i < n; ++i) poly[i] += c * tj[i];
                 double next[PMGB_ES_COEF] = {};
@@ -1037,7 +1048,12 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
     }
     if ((rc = upload(ctx, &s->d_tk_df, tk, &s->h2d_bytes))) return rc;
     if ((rc = upload(ctx, &s->d_krow, rows, &s->h2d_bytes))) return rc;
-    const std::vector<double> es = erfc_over_r_table(alpha, sr_cutoff * sr_cutoff);
+    if (ctx->es_table.empty() || ctx->es_alpha != alpha || ctx->es_smax != sr_cutoff * sr_cutoff) {
+        ctx->es_table = erfc_over_r_table(alpha, sr_cutoff * sr_cutoff);
+        ctx->es_alpha = alpha;
+        ctx->es_smax = sr_cutoff * sr_cutoff;
+    }
+    const std::vector<double>& es = ctx->es_table;
     std::vector<float2> es_df(es.size());
     for (size_t i = 0; i < es.size(); ++i) es_df[i] = to_df(es[i]);
     if ((rc = upload(ctx, &s->d_es, es, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_es_df, es_df, &s->h2d_bytes)))
