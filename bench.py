@@ -442,6 +442,19 @@ def other_configs(args, ctx, stream):
     return out
 
 
+def job_rate(ms_total: float, n_per_rank_step: int, steps: int, world: int, device="cpu"):
+    """The slowest rank bounds the job: (max over ranks of the timed ms, whole-job units/s with
+    every rank processing n_per_rank_step units per step).  Ranks are independent replicas; the
+    one collective is this max."""
+    import torch
+
+    t = torch.tensor([ms_total], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    return ms_max, world * n_per_rank_step * steps / (ms_max * 1e-3)
+
+
 # ------------------------------------------------------------------ GPU arm
 def ours(args, rank, world, local_rank):
     global _tables
@@ -499,12 +512,7 @@ def ours(args, rank, world, local_rank):
     blocks = block_out.cpu().numpy().reshape(N_BLOCKS, 4)
     assert np.all(np.isfinite(blocks[:, 0])), blocks
 
-    # the slowest rank bounds the job
-    t = torch.tensor([ms_total], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = world * n_ins * args.steps / (ms_max * 1e-3)
+    ms_max, value = job_rate(ms_total, n_ins, args.steps, world, dev)
 
     # the FP32 pair pass alone (pairs_kernel + block reduction): the roofline's kernel time
     system.set_refine(0.0)
