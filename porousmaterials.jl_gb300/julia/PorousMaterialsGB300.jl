@@ -67,7 +67,7 @@ mutable struct GPUSystem
     function GPUSystem(ctx::Context, crystal::Crystal, molecule::Molecule, ljff::LJForceField;
                        eparams::Union{Nothing, PorousMaterials.EwaldParams}=nothing, charge_scale::Float64=1.0,
                        pure_ϵ::Union{Nothing, Dict{Symbol, Float64}}=nothing,
-                       pure_σ::Union{Nothing, Dict{Symbol, Float64}}=nothing)
+                       pure_σ::Union{Nothing, Dict{Symbol, Float64}}=nothing, refine_tail::Float64=0.0)
         species = unique(vcat(crystal.atoms.species, molecule.atoms.species))
         sid = Dict(s => Int32(i - 1) for (i, s) in enumerate(species))
         n = length(species)
@@ -106,6 +106,9 @@ mutable struct GPUSystem
                 (Ptr{Cvoid}, Float64, Float64, Int32, Ptr{Int32}, Ptr{Float64}),
                 sys.ptr, eparams.α, eparams.sr_cutoff_r, length(wt), kabc, wt))
         end
+        if refine_tail > 0  # FP64-grade re-evaluation of the Boltzmann tail: K_H within 1e-6
+            check(ctx, ccall((:pmgb_system_set_refine, LIB), Cint, (Ptr{Cvoid}, Float64), sys.ptr, refine_tail))
+        end
         return sys
     end
 end
@@ -142,13 +145,15 @@ end
 # ---------------------------------------------------------------------------- drop-in bodies
 """
 Drop-in for `henry_coefficient` (src/henry.jl:34-181): the same set-up, statistics, result
-keys, units and autosave; the insertions run on the GPU.  `seed` makes a run reproducible.
+keys, units and autosave; the insertions run on the GPU.  `seed` makes a run reproducible;
+`refine_tail` (default 1e-3) re-evaluates in high precision the insertions that carry all but that
+fraction of each block's Boltzmann weight, which keeps K_H within 1e-6 of an FP64 evaluation.
 """
 function henry_coefficient(crystal::Crystal, molecule::Molecule, temperature::Float64,
                            ljforcefield::LJForceField; insertions_per_volume::Union{Int, Float64}=200,
                            verbose::Bool=true, ewald_precision::Float64=1e-6, autosave::Bool=true,
                            filename_comment::AbstractString="", seed::UInt64=rand(UInt64),
-                           ctx::Context=default_context())
+                           ctx::Context=default_context(), refine_tail::Float64=1e-3)
     assert_P1_symmetry(crystal)
     time_start = time()
     nb_insertions = max(N_BLOCKS, ceil(Int, insertions_per_volume * crystal.box.Ω))
@@ -160,7 +165,7 @@ function henry_coefficient(crystal::Crystal, molecule::Molecule, temperature::Fl
     ρ = crystal_density(crystal)
     eparams = charged_system ? setup_Ewald_sum(crystal.box, sqrt(ljforcefield.r²_cutoff);
                                                ϵ=ewald_precision, verbose=verbose) : nothing
-    sys = GPUSystem(ctx, crystal, molecule, ljforcefield; eparams=eparams)
+    sys = GPUSystem(ctx, crystal, molecule, ljforcefield; eparams=eparams, refine_tail=refine_tail)
     blocks = widom_blocks(sys, nb_insertions_per_block, temperature; seed=seed)
 
     henry_coefficients = exp.(blocks[1, :] .- log(PorousMaterials.UNIV_GAS_CONST * temperature *
@@ -299,7 +304,7 @@ K_H (mol/(m³ bar)) of every crystal from one persistent, graph-captured launch
 """
 function henry_screen(crystals::Vector{Crystal}, molecule::Molecule, temperature::Float64, ljff::LJForceField;
                       insertions::Int=20_000, seed::Integer=0, tune::Bool=true, ewald_precision=1e-6,
-                      ctx::Context=default_context())
+                      ctx::Context=default_context(), refine_tail::Float64=1e-3)
     nb = cld(insertions, N_BLOCKS)
     systems = GPUSystem[]
     for cr in crystals
@@ -312,6 +317,8 @@ function henry_screen(crystals::Vector{Crystal}, molecule::Molecule, temperature
         ctx.ptr, length(systems), [s.ptr for s in systems], fill(Int64(nb), length(systems)), N_BLOCKS, 0,
         handle))
     try
+        refine_tail > 0 && check(ctx, ccall((:pmgb_batch_set_refine, LIB), Cint, (Ptr{Cvoid}, Float64),
+                                            handle[], refine_tail))
         if tune
             best = Ref{Float64}(0.0)
             check(ctx, ccall((:pmgb_batch_tune, LIB), Cint, (Ptr{Cvoid}, UInt64, Float64, Int32, Ptr{Float64}),
