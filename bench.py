@@ -162,9 +162,9 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU legs
-def cpu_rate(sc, mol, ep, budget_s: float, seed: int = 99, poses=None):
-    """Insertions/s of the FP64 oracle (direct e^{ik.r} form, all host threads) on a bounded
-    sample of the workload's insertions."""
+def cpu_rate(sc, mol, ep, budget_s: float, seed: int = 99, poses=None, nthreads: int = 0):
+    """Insertions/s of the FP64 oracle (direct e^{ik.r} form, all host threads, or nthreads) on a
+    bounded sample of the workload's insertions."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import numpy as np
 
@@ -178,7 +178,7 @@ def cpu_rate(sc, mol, ep, budget_s: float, seed: int = 99, poses=None):
                             sc.charges.q, ff_eps, ff_sig2, 12.5 ** 2, [sid[s] for s in mol.atom_species],
                             mol.charge_q)
     o.set_ewald(ep.alpha, ep.sr_cutoff_r, ep.kreps, ep.kvec_abc, ep.kvec_wt)
-    cores = oracle.num_threads()
+    cores = nthreads if nthreads > 0 else oracle.num_threads()
     rng = np.random.default_rng(seed)
     ax, qx = body_offsets(mol, sc.box)
 
@@ -188,7 +188,7 @@ def cpu_rate(sc, mol, ep, budget_s: float, seed: int = 99, poses=None):
         lj = xf[:, None, :] + np.einsum("ij,njk,lk->nli", sc.box.c_to_f, R, ax)
         q = xf[:, None, :] + np.einsum("ij,njk,lk->nli", sc.box.c_to_f, R, qx)
         t0 = time.perf_counter()
-        o.energies(lj, q, charged=True, use_sk=False)
+        o.energies(lj, q, charged=True, use_sk=False, nthreads=nthreads)
         return time.perf_counter() - t0
 
     # calibrate on a few insertions per thread, then sample until the time budget is spent
@@ -582,9 +582,12 @@ def ours(args, rank, world, local_rank):
     cpu = None
     if not args.skip_cpu:
         r, cores, n, dt = cpu_rate(sc, mol, ep, budget_s=15.0)
+        r1, _, n1, dt1 = cpu_rate(sc, mol, ep, budget_s=4.0, seed=98, nthreads=1)
         cpu = {"value": r, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{n} insertions of the workload (random poses), FP64 direct e^(ik.r) Ewald sum + LJ "
-                         f"(the reference's algorithm), OpenMP over insertions, {dt:.1f} s"}
+                         f"(the reference's algorithm), OpenMP over insertions, {dt:.1f} s",
+               "single_core": {"value": r1, "unit": UNIT, "cores": 1,
+                               "sample": f"{n1} insertions on one thread, {dt1:.1f} s"}}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
