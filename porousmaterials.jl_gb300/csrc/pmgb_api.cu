@@ -828,12 +828,6 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
         D.q[k] = (k < ns) ? static_cast<float>(sq[k]) : 0.0f;
         D.q64[k] = (k < ns) ? sq[k] : 0.0;
     }
-    double anchor = 0.0;
-    for (int k = 1; k < ns; ++k)
-        anchor = std::max(anchor, std::sqrt((body[k][0] - body[0][0]) * (body[k][0] - body[0][0]) +
-                                            (body[k][1] - body[0][1]) * (body[k][1] - body[0][1]) +
-                                            (body[k][2] - body[0][2]) * (body[k][2] - body[0][2])));
-    D.anchor_r = static_cast<float>(anchor * (1.0 + 1e-6));
     D.n_krow = 0;
     D.n_k = 0;
     D.krow = nullptr;

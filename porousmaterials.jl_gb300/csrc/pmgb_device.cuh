@@ -826,8 +826,6 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                   S.rc2, S.rc2e, fmaxf(S.rc2, CHARGED ? S.rc2e : 0.0f), f2(0.5f * S.alpha),
                   f2(-S.alpha * S.alpha * 1.4426950408889634f)};
     const float2 c1 = f2(1.1283791670955126f * S.alpha);  // 2 alpha / sqrt(pi)
-    // (cutoff + the guest's extent about site 0 + 1e-3 A of FP32 rounding)^2
-    const float anchor2 = (sqrtf(g2.rcmax2) + S.anchor_r + 1e-3f) * (sqrtf(g2.rcmax2) + S.anchor_r + 1e-3f);
     float qcoul[NS];
 #pragma unroll
     for (int k = 0; k < NS; ++k) qcoul[k] = S.q[k] * static_cast<float>(S.coul);
@@ -930,17 +928,12 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                     // (those terms are exact zeros, so the sums are unchanged)
                     auto group4 = [&](int j) {
                         const int4 r0 = T[j - t0], r1 = T[j + 1 - t0], r2 = T[j + 2 - t0], r3 = T[j + 3 - t0];
-                        bool rest = true;  // the other sites may reach one of the four records
 #pragma unroll
                         for (int k = 0; k < NS; ++k) {
-                            if (k > 0 && !rest) break;  // warp-uniform
                             const float2 d01 = pair2_r2<RESID>(r0, r1, ux[k], uy[k], uz[k], g2);
                             const float2 d23 = pair2_r2<RESID>(r2, r3, ux[k], uy[k], uz[k], g2);
                             const float dmin = fminf(fminf(d01.x, d01.y), fminf(d23.x, d23.y));
                             segmin[k] = fminf(segmin[k], dmin);
-                            // every site lies within anchor_r of site 0: no lane has site 0 within the
-                            // cutoff + anchor_r of the group, so no site is within the cutoff of it
-                            if (NS > 1 && k == 0) rest = __any_sync(0xffffffffu, valid && !blocked && dmin < anchor2);
                             if (__any_sync(0xffffffffu, valid && !blocked && dmin < g2.rcmax2)) {
                                 const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
                                 pair2_energy<CHARGED, COLS>(d01, __int_as_float(r0.w), __int_as_float(r1.w), g2,

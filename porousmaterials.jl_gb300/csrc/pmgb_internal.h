@@ -67,9 +67,6 @@ struct SysDev {
     // upper bound of the largest eigenvalue of the Gram matrix of the unit face normals
     const ChunkBox* cbox;
     float cw[3], cw_inv_lam;
-    // largest distance of a guest site from site 0 (A): a group of records beyond the cutoff plus
-    // this from site 0 is beyond the cutoff of every site
-    float anchor_r;
     int n_seg;
     const SegDesc* seg;
     const SitePar* segpar;
