@@ -52,7 +52,7 @@ LAUNCHES_PER_STEP = 14
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=50)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--insertions", type=int, default=N_INS)
@@ -123,11 +123,18 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except (FileNotFoundError, OSError):
             self.proc = None
+            return self
+        # nvidia-smi takes a moment to start: wait (bounded) for its first sample, then keep only the
+        # samples taken from here on, i.e. during the timed region
+        t_end = time.perf_counter() + 5.0
+        while not self.lines and time.perf_counter() < t_end and self.proc.poll() is None:
+            time.sleep(0.01)
+        self.lines.clear()
         return self
 
     def _read(self):
