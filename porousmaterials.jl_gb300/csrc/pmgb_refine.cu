@@ -341,14 +341,13 @@ __device__ __forceinline__ uint64_t frac2fix128(double x) {
     return __double2ull_rn(f * 18446744073709551616.0);
 }
 
-// Reciprocal-space potential of one guest site at fractional x over the half-rows [row0, row_end)
-// stepping by row_step, sum_k Re[wt S(k) e^{-ik.x}], in double-float: row starts from exact 64-bit
-// fixed-point phases (the strides ks applied in fixed point), steps along kc by the recurrence.
-__device__ dfl kspace_df_rows(const SysDev& S, const double* x, int row0, int row_end, int row_step,
+// Reciprocal-space potential of one guest site over the half-rows [row0, row_end) stepping by
+// row_step, sum_k Re[wt S(k) e^{-ik.x}], in double-float: row starts from exact 64-bit fixed-point
+// phases, steps along kc by the recurrence.  U[d] = ks[d] times the site's fractional coordinate d
+// as a 64-bit fixed point (the strides applied in fixed point).
+__device__ dfl kspace_df_rows(const SysDev& S, const uint64_t* U, int row0, int row_end, int row_step,
                               const float4* tab) {
-    const uint64_t U0 = static_cast<uint64_t>(S.ks[0]) * frac2fix128(x[0]);
-    const uint64_t U1 = static_cast<uint64_t>(S.ks[1]) * frac2fix128(x[1]);
-    const uint64_t U2 = static_cast<uint64_t>(S.ks[2]) * frac2fix128(x[2]);
+    const uint64_t U0 = U[0], U1 = U[1], U2 = U[2];
     const dfc w = phase64(U2, tab);  // one step along +kc
     dfl lr{0.0f, 0.0f};
     for (int row = row0; row < row_end; row += row_step) {
@@ -378,14 +377,62 @@ struct SiteScreen {
     uint32_t x[PMGB_MAX_SITES], y[PMGB_MAX_SITES], z[PMGB_MAX_SITES];
     float rx[PMGB_MAX_SITES], ry[PMGB_MAX_SITES], rz[PMGB_MAX_SITES];  // beyond the fixed point (2^-32 units)
     dfl q[PMGB_MAX_SITES];                                              // guest charges
+    uint64_t U[PMGB_MAX_SITES][3];  // 64-bit fixed-point fractions times the k-vector strides (reciprocal space)
     float r2max;
 };
 
+// The guest sites of insertion `item`, set up once per warp: the pose is drawn as in make_pose,
+// and lane 3k + d (k < n_sites, d < 3) composes coordinate d of site k in FP64 from it -- the
+// same products as refined_entry -- then takes it to the 32-bit fixed point with its FP32
+// remainder and to the 64-bit fixed-point phase; lane 3k also splits the charge of site k into
+// a double-float.  The lanes then exchange the values, so the FP64 set-up costs a warp one pass
+// instead of one per site and coordinate.
+__device__ __forceinline__ void warp_site_setup(const SysDev& S, unsigned long long seed, unsigned long long item,
+                                                SiteScreen& sc) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    float xf[3], R[9];
+    make_pose(seed, item, xf, R);
+    const int k = min(lane / 3, S.n_sites - 1), d = lane % 3;
+    const double bx = S.body64[k][0], by = S.body64[k][1], bz = S.body64[k][2];
+    const double ox = static_cast<double>(R[0]) * bx + static_cast<double>(R[3]) * by + static_cast<double>(R[6]) * bz;
+    const double oy = static_cast<double>(R[1]) * bx + static_cast<double>(R[4]) * by + static_cast<double>(R[7]) * bz;
+    const double oz = static_cast<double>(R[2]) * bx + static_cast<double>(R[5]) * by + static_cast<double>(R[8]) * bz;
+    double x;
+    if (d == 0) x = static_cast<double>(xf[0]) + (S.g64[0] * ox + S.g64[1] * oy + S.g64[2] * oz);
+    else if (d == 1) x = static_cast<double>(xf[1]) + (S.g64[3] * oy + S.g64[4] * oz);
+    else x = static_cast<double>(xf[2]) + S.g64[5] * oz;
+    const double ux = x * 4294967296.0;
+    const long long fx = __double2ll_rn(ux);
+    const uint32_t fix = static_cast<uint32_t>(fx);  // as frac2fix64
+    const float rem = static_cast<float>(ux - static_cast<double>(fx));
+    const uint64_t U = S.charged ? static_cast<uint64_t>(S.ks[d]) * frac2fix128(x) : 0ull;
+    const float qh = static_cast<float>(S.q64[k]);
+    const float ql = static_cast<float>(S.q64[k] - static_cast<double>(qh));
+    for (int kk = 0; kk < S.n_sites; ++kk) {
+        const int l = 3 * kk;
+        sc.x[kk] = __shfl_sync(full, fix, l);
+        sc.y[kk] = __shfl_sync(full, fix, l + 1);
+        sc.z[kk] = __shfl_sync(full, fix, l + 2);
+        sc.rx[kk] = __shfl_sync(full, rem, l);
+        sc.ry[kk] = __shfl_sync(full, rem, l + 1);
+        sc.rz[kk] = __shfl_sync(full, rem, l + 2);
+        sc.U[kk][0] = __shfl_sync(full, U, l);
+        sc.U[kk][1] = __shfl_sync(full, U, l + 1);
+        sc.U[kk][2] = __shfl_sync(full, U, l + 2);
+        sc.q[kk] = {__shfl_sync(full, qh, l), __shfl_sync(full, ql, l)};
+    }
+    const float rmax = sqrtf(static_cast<float>(fmax(S.rc2_64, S.charged ? S.rc2e_64 : 0.0))) + 0.01f;
+    sc.r2max = rmax * rmax;
+}
+
+// The same set-up by one thread from the composed FP64 sites xs (the one-thread-per-insertion
+// path; the reciprocal-space phases are not needed there).
 __device__ __forceinline__ void screen_init(const SysDev& S, const double (*xs)[3], SiteScreen& sc) {
     for (int k = 0; k < S.n_sites; ++k) {
         const double ux = xs[k][0] * 4294967296.0, uy = xs[k][1] * 4294967296.0, uz = xs[k][2] * 4294967296.0;
         const long long fx = __double2ll_rn(ux), fy = __double2ll_rn(uy), fz = __double2ll_rn(uz);
-        sc.x[k] = static_cast<uint32_t>(fx);  // as frac2fix64
+        sc.x[k] = static_cast<uint32_t>(fx);
         sc.y[k] = static_cast<uint32_t>(fy);
         sc.z[k] = static_cast<uint32_t>(fz);
         sc.rx[k] = static_cast<float>(ux - static_cast<double>(fx));
@@ -394,8 +441,8 @@ __device__ __forceinline__ void screen_init(const SysDev& S, const double (*xs)[
         const float qh = static_cast<float>(S.q64[k]);
         sc.q[k] = {qh, static_cast<float>(S.q64[k] - static_cast<double>(qh))};
     }
-    const double rmax = sqrt(fmax(S.rc2_64, S.charged ? S.rc2e_64 : 0.0)) + 0.01;
-    sc.r2max = static_cast<float>(rmax * rmax);
+    const float rmax = sqrtf(static_cast<float>(fmax(S.rc2_64, S.charged ? S.rc2e_64 : 0.0))) + 0.01f;
+    sc.r2max = rmax * rmax;
 }
 
 __device__ __forceinline__ bool near_half_cell(int d) { return d > 0x7FF00000 || d < -0x7FF00000; }
@@ -517,18 +564,18 @@ __device__ __forceinline__ void queued_pair(const SysDev& S, int sg, int e, cons
 // [k0, k1).  The lanes screen 32 records at a time in FP32 and queue the (record, site) pairs that
 // may lie inside a cutoff in `queue` (kQueueLen entries of this warp's shared memory); their terms
 // run in double-float in full rounds of 32 queued pairs, so a warp pays only for pairs near the
-// insertion however they are spread over its lanes.  k-space rows (FP64): lanes stride over them.
+// insertion however they are spread over its lanes.  k-space half-rows: lanes stride over them.
+// The lane sums are added across the warp in double-float.
 // out4 = (U_vdw part, U_sr part / coul, U_lr part, overlap).
-__device__ void energy_fp64_warp_part(const SysDev& S, const double (*xs)[3], int j0, int j1, int k0, int k1,
-                                      double* out4, int* queue, const float4* phase_tab) {
+__device__ void energy_fp64_warp_part(const SysDev& S, unsigned long long seed, unsigned long long item, int j0, int j1,
+                                      int k0, int k1, double* out4, int* queue, const float4* phase_tab) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int ns = S.n_sites;
-    double lr = 0.0;
-    dfl vd{0.0f, 0.0f}, srd{0.0f, 0.0f};  // this lane's pair sums (double-float)
+    dfl vd{0.0f, 0.0f}, srd{0.0f, 0.0f}, lrd{0.0f, 0.0f};  // this lane's sums (double-float)
     bool ovl = false;
     SiteScreen sc;
-    screen_init(S, xs, sc);
+    warp_site_setup(S, seed, item, sc);
     for (int sg = 0; sg < S.n_seg; ++sg) {
         const SegDesc d = S.seg[sg];
         const int lo = max(d.lo, j0), hi = min(d.hi, j1);
@@ -562,23 +609,21 @@ __device__ void energy_fp64_warp_part(const SysDev& S, const double (*xs)[3], in
         __syncwarp();  // the queue is free for the next segment
     }
     if (S.charged && k1 > k0) {
-        dfl lrd{0.0f, 0.0f};
         for (int k = 0; k < ns; ++k)
-            if (S.q64[k] != 0.0) lrd = df_add(lrd, df_mul(sc.q[k], kspace_df_rows(S, xs[k], k0 + lane, k1, 32, phase_tab)));
-        lr = df_to_double(lrd);
+            if (sc.q[k].hi != 0.0f)
+                lrd = df_add(lrd, df_mul(sc.q[k], kspace_df_rows(S, sc.U[k], k0 + lane, k1, 32, phase_tab)));
     }
-    double v = df_to_double(vd), sr = df_to_double(srd);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        v += __shfl_xor_sync(0xffffffffu, v, o);
-        sr += __shfl_xor_sync(0xffffffffu, sr, o);
-        lr += __shfl_xor_sync(0xffffffffu, lr, o);
+        vd = df_add(vd, dfl{__shfl_xor_sync(full, vd.hi, o), __shfl_xor_sync(full, vd.lo, o)});
+        srd = df_add(srd, dfl{__shfl_xor_sync(full, srd.hi, o), __shfl_xor_sync(full, srd.lo, o)});
+        lrd = df_add(lrd, dfl{__shfl_xor_sync(full, lrd.hi, o), __shfl_xor_sync(full, lrd.lo, o)});
     }
-    ovl = __any_sync(0xffffffffu, ovl);
+    ovl = __any_sync(full, ovl);
     if (lane == 0) {
-        out4[0] = v;
-        out4[1] = sr;
-        out4[2] = lr;
+        out4[0] = df_to_double(vd);
+        out4[1] = df_to_double(srd);
+        out4[2] = df_to_double(lrd);
         out4[3] = ovl ? 1.0 : 0.0;
     }
 }
@@ -602,12 +647,19 @@ __device__ __forceinline__ int fp64_chunks(const SysDev& S, long long count) {
     return static_cast<int>(min(64ll, (fp64_work(S) + 16383) / 16384));
 }
 
+// Pose stream of refined entry e (system << 40 | insertion): its system's seed and insertion index.
+__device__ __forceinline__ void entry_pose(const RefineArgs& a, long long e, unsigned long long& seed,
+                                           unsigned long long& item) {
+    const int sys = static_cast<int>(e >> 40);
+    item = static_cast<unsigned long long>(e & ((1ll << 40) - 1));
+    seed = a.run ? a.run->seed + static_cast<unsigned long long>(sys) * 0x9E3779B97F4A7C15ull : a.seed;
+}
+
 __device__ __forceinline__ void refined_entry(const RefineArgs& a, long long e, const SysDev*& S, double (*xs)[3]) {
     const int sys = static_cast<int>(e >> 40);
-    const long long item = e & ((1ll << 40) - 1);
     S = a.systems ? &a.systems[sys].sys : &a.sys;
-    const unsigned long long seed =
-        a.run ? a.run->seed + static_cast<unsigned long long>(sys) * 0x9E3779B97F4A7C15ull : a.seed;
+    unsigned long long seed, item;
+    entry_pose(a, e, seed, item);
     // the insertion's pose applied to the FP64 site offsets, kept in FP64 (no fixed point)
     float xf[3], R[9];
     make_pose(seed, static_cast<unsigned long long>(item), xf, R);
@@ -726,15 +778,14 @@ __global__ void __launch_bounds__(PMGB_THREADS) refine_large_kernel(const __grid
         const int local = i - a.plan[sys];
         const int r = system_entry_first(a, sys) + local / C;
         const int c = local % C;
-        const SysDev* Sp;
-        double xs[PMGB_MAX_SITES][3];
-        refined_entry(a, a.list[r], Sp, xs);
+        unsigned long long seed, item;
+        entry_pose(a, a.list[r], seed, item);
         const int j0 = static_cast<int>(static_cast<long long>(S.n_rec) * c / C);
         const int j1 = static_cast<int>(static_cast<long long>(S.n_rec) * (c + 1) / C);
         const int k0 = static_cast<int>(static_cast<long long>(S.n_krow) * c / C);
         const int k1 = static_cast<int>(static_cast<long long>(S.n_krow) * (c + 1) / C);
         double* p = a.part + 4 * static_cast<size_t>(i);
-        energy_fp64_warp_part(S, xs, j0, j1, k0, k1, p, s_queue[threadIdx.x >> 5], s_phase);
+        energy_fp64_warp_part(S, seed, item, j0, j1, k0, k1, p, s_queue[threadIdx.x >> 5], s_phase);
         if (lane == 0 && C == 1) {  // the whole insertion in one chunk
             double* out = a.ref_u + 3 * static_cast<size_t>(r);
             out[0] = p[3] > 0.0 ? __longlong_as_double(0x7ff0000000000000ll) : p[0];
