@@ -163,6 +163,15 @@ int pmgb_system_set_accessibility(pmgb_system* sys, const int32_t n_pts[3], cons
  * insertion order, so results are bit-identical with it on or off.  No reference counterpart. */
 int pmgb_system_set_cull(pmgb_system* sys, int32_t on);
 
+/* Centre-image distances (default on) for Widom insertions of a guest with several sites: where
+ * every perpendicular width of the supercell is at least 2 (cutoff + the largest site distance
+ * from the pose centre) + 0.1 A, each framework record's minimum-image displacement from the pose
+ * centre is converted once and every site subtracts its offset.  The pairs inside the cutoff and
+ * their images are the per-site minimum images, so results differ from the per-site form (on = 0)
+ * by FP32 rounding only.  No reference counterpart; a batch takes the setting its systems have
+ * when it is created. */
+int pmgb_system_set_centre_image(pmgb_system* sys, int32_t on);
+
 /* Number of insertions the last refined Widom run re-evaluated in FP64 (synchronises). */
 int pmgb_system_refined_count(pmgb_system* sys, int64_t* count_out);
 
@@ -280,6 +289,13 @@ int pmgb_batch_set_cull(pmgb_batch* batch, int32_t on);
 
 /* Insertions of each system the last run re-evaluated in FP64 (n_systems values; synchronises). */
 int pmgb_batch_refined_counts(pmgb_batch* batch, int64_t* per_system);
+
+/* Per-insertion (U_vdw, U_es) in K of the last run, system after system, each system's insertions
+ * in index order (block-major), the refined insertions with their FP64 energies: 2 * total
+ * insertions doubles (synchronises).  Available when the batch culls or refines (both keep every
+ * insertion's energy); PMGB_ERR_NOT_READY otherwise or before the first run.  No reference
+ * counterpart (the per-insertion energies of _conduct_Widom_insertions, henry.jl:214-233). */
+int pmgb_batch_energies(pmgb_batch* batch, double* u_out);
 
 /* Enqueue one run (one graph replay) on the context stream; does not synchronise. */
 int pmgb_batch_launch(pmgb_batch* batch, uint64_t seed, double temperature);

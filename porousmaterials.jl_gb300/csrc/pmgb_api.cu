@@ -97,6 +97,7 @@ struct pmgb_system {
     int site_charge[PMGB_MAX_SITES];
     double refine_tail = 0.0;       // FP64 refinement of the Boltzmann tail (0: off)
     bool cull = true;               // spatially ordered processing with cutoff culling
+    bool centre_image = true;       // centre-image distances where the geometry allows them
     DevBuf o_counts, o_perm;        // Widom processing order scratch
     DevBuf acc;                     // accessibility grid (uint8, i fastest)
     int last_refine_ctas = 0;       // chunks of the last refined run (its refined count sits after them)
@@ -422,6 +423,30 @@ static void free_system_device(pmgb_system* s) {
                     s->r_part.p,   s->acc.p,      s->d_cbox,    s->d_es,     s->d_es_df,  s->d_rec_rq,
                     s->d_rec_qlo,  s->d_segpar_df, s->d_tk_df};
     for (void* p : ptrs) dev_free(s->ctx, p);
+}
+
+// Where the kernels may take every guest site's minimum image from the pose centre's (see
+// run_unit): every perpendicular width W_d = 1 / |row d of c_to_f| at least 2 (rc + reach) + 0.1 A
+// (rc: the larger cutoff; reach: the largest site distance from the centre).  Called whenever a
+// cutoff changes.
+static void set_centre_image(SysDev& D) {
+    D.com_axis = -2;
+    const double rc = std::sqrt(std::max(D.rc2_64, D.charged ? D.rc2e_64 : 0.0));
+    const double reach = D.com_reach;
+    D.com_reach2 = static_cast<float>((rc + reach) * (rc + reach) * (1.0 + 1e-6));
+    if (D.n_sites < 2 || reach <= 0.0) return;
+    for (int d = 0; d < 3; ++d) {
+        // rows of the upper-triangular c_to_f (00 01 02 11 12 22)
+        const double r0 = d == 0 ? D.g64[0] : 0.0, r1 = d == 0 ? D.g64[1] : (d == 1 ? D.g64[3] : 0.0);
+        const double r2 = d == 0 ? D.g64[2] : (d == 1 ? D.g64[4] : D.g64[5]);
+        if (1.0 / std::sqrt(r0 * r0 + r1 * r1 + r2 * r2) < 2.0 * (rc + reach) + 0.1) return;
+    }
+    D.com_axis = -1;
+}
+
+static void update_centre_image(pmgb_system* s) {
+    set_centre_image(s->dev);
+    if (!s->centre_image) s->dev.com_axis = -2;
 }
 
 extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t n_atoms, const double* atom_xf,
@@ -828,6 +853,14 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
         D.q[k] = (k < ns) ? static_cast<float>(sq[k]) : 0.0f;
         D.q64[k] = (k < ns) ? sq[k] : 0.0;
     }
+    {
+        double reach = 0.0;
+        for (int k = 0; k < ns; ++k)
+            reach = std::max(reach, std::sqrt(D.body64[k][0] * D.body64[k][0] + D.body64[k][1] * D.body64[k][1] +
+                                              D.body64[k][2] * D.body64[k][2]));
+        D.com_reach = reach > 0.0 ? static_cast<float>(reach * (1.0 + 1e-6) + 1e-4) : 0.0f;
+    }
+    update_centre_image(s);
     D.n_krow = 0;
     D.n_k = 0;
     D.krow = nullptr;
@@ -1067,6 +1100,7 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
     s->dev.rc2e = static_cast<float>(sr_cutoff * sr_cutoff);
     s->dev.alpha64 = alpha;
     s->dev.rc2e_64 = sr_cutoff * sr_cutoff;
+    update_centre_image(s);
     s->dev.es_tab = s->d_es;
     s->dev.es_e_lo = PMGB_ES_E_LO;
     s->dev.es_n_oct = static_cast<int>(es.size() / (PMGB_ES_COEF * PMGB_ES_SUB));
@@ -1371,6 +1405,13 @@ extern "C" int pmgb_system_set_accessibility(pmgb_system* s, const int32_t n_pts
 extern "C" int pmgb_system_set_cull(pmgb_system* s, int32_t on) {
     if (!s) return PMGB_ERR_INVALID_ARGUMENT;
     s->cull = on != 0;
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_system_set_centre_image(pmgb_system* s, int32_t on) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    s->centre_image = on != 0;
+    update_centre_image(s);
     return PMGB_OK;
 }
 
@@ -2299,6 +2340,18 @@ extern "C" int pmgb_batch_refined_counts(pmgb_batch* b, int64_t* per_system) {
         const int64_t c1 = bs.chunk_first + static_cast<int64_t>(bs.ctas_per_block) * b->n_blocks;
         per_system[i] = off[c1] - off[bs.chunk_first];
     }
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_batch_energies(pmgb_batch* b, double* u_out) {
+    if (!b || !u_out) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = b->ctx;
+    if (!b->launched || !(b->refine_tail > 0.0 || b->cull) || !b->d_u)
+        return fail(ctx, PMGB_ERR_NOT_READY, "pmgb_batch_energies: needs a run with culling or refinement on");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, cudaMemcpyAsync(u_out, b->d_u, sizeof(double) * 2 * static_cast<size_t>(b->n_insertions),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
     return PMGB_OK;
 }
 

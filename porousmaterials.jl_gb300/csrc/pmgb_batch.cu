@@ -17,41 +17,52 @@ namespace {
 constexpr int kVariantSites[6] = {1, 2, 3, 4, 6, 8};
 
 // Each variant is its own function so that ptxas allocates its registers separately.
-template <int NS, bool CHARGED, bool GRAD, bool RESID>
+template <int NS, bool CHARGED, bool GRAD, bool RESID, bool COMP>
 __device__ __noinline__ bool run_unit_fn(const SysDev& S, const UnitIO& io, int4* stage, uint64_t* bars,
                                          LsePartial* red, uint32_t (&fills)[PMGB_NSTAGE], unsigned int* status) {
-    return run_unit<NS, CHARGED, GRAD, RESID, false>(S, io, stage, bars, red, fills, status);  // no forces
+    return run_unit<NS, CHARGED, GRAD, RESID, false, COMP>(S, io, stage, bars, red, fills, status);  // no forces
+}
+
+// one guest site: no centre-image variant (the site is the centre); the centre-image variant keeps
+// the box-matrix residual whether or not refinement follows
+template <int NS, bool CHARGED, bool GRAD, bool RESID>
+__device__ __forceinline__ bool run_unit_c(bool comp, const SysDev& S, const UnitIO& io, int4* stage, uint64_t* bars,
+                                           LsePartial* red, uint32_t (&fills)[PMGB_NSTAGE], unsigned int* status) {
+    if constexpr (NS > 1)
+        if (comp) return run_unit_fn<NS, CHARGED, GRAD, true, true>(S, io, stage, bars, red, fills, status);
+    return run_unit_fn<NS, CHARGED, GRAD, RESID, false>(S, io, stage, bars, red, fills, status);
 }
 
 template <bool GRAD, bool RESID>
-__device__ __forceinline__ bool run_variant_r(int variant, const SysDev& S, const UnitIO& io, int4* stage,
+__device__ __forceinline__ bool run_variant_r(int variant, bool comp, const SysDev& S, const UnitIO& io, int4* stage,
                                               uint64_t* bars, LsePartial* red, uint32_t (&fills)[PMGB_NSTAGE],
                                               unsigned int* status) {
     switch (variant) {
-        case 0: return run_unit_fn<1, false, GRAD, RESID>(S, io, stage, bars, red, fills, status);
-        case 1: return run_unit_fn<2, false, GRAD, RESID>(S, io, stage, bars, red, fills, status);
-        case 2: return run_unit_fn<3, false, GRAD, RESID>(S, io, stage, bars, red, fills, status);
-        case 3: return run_unit_fn<4, false, GRAD, RESID>(S, io, stage, bars, red, fills, status);
-        case 4: return run_unit_fn<6, false, GRAD, RESID>(S, io, stage, bars, red, fills, status);
-        case 5: return run_unit_fn<8, false, GRAD, RESID>(S, io, stage, bars, red, fills, status);
-        case 6: return run_unit_fn<1, true, GRAD, RESID>(S, io, stage, bars, red, fills, status);
-        case 7: return run_unit_fn<2, true, GRAD, RESID>(S, io, stage, bars, red, fills, status);
-        case 8: return run_unit_fn<3, true, GRAD, RESID>(S, io, stage, bars, red, fills, status);
-        case 9: return run_unit_fn<4, true, GRAD, RESID>(S, io, stage, bars, red, fills, status);
-        case 10: return run_unit_fn<6, true, GRAD, RESID>(S, io, stage, bars, red, fills, status);
-        default: return run_unit_fn<8, true, GRAD, RESID>(S, io, stage, bars, red, fills, status);
+        case 0: return run_unit_c<1, false, GRAD, RESID>(comp, S, io, stage, bars, red, fills, status);
+        case 1: return run_unit_c<2, false, GRAD, RESID>(comp, S, io, stage, bars, red, fills, status);
+        case 2: return run_unit_c<3, false, GRAD, RESID>(comp, S, io, stage, bars, red, fills, status);
+        case 3: return run_unit_c<4, false, GRAD, RESID>(comp, S, io, stage, bars, red, fills, status);
+        case 4: return run_unit_c<6, false, GRAD, RESID>(comp, S, io, stage, bars, red, fills, status);
+        case 5: return run_unit_c<8, false, GRAD, RESID>(comp, S, io, stage, bars, red, fills, status);
+        case 6: return run_unit_c<1, true, GRAD, RESID>(comp, S, io, stage, bars, red, fills, status);
+        case 7: return run_unit_c<2, true, GRAD, RESID>(comp, S, io, stage, bars, red, fills, status);
+        case 8: return run_unit_c<3, true, GRAD, RESID>(comp, S, io, stage, bars, red, fills, status);
+        case 9: return run_unit_c<4, true, GRAD, RESID>(comp, S, io, stage, bars, red, fills, status);
+        case 10: return run_unit_c<6, true, GRAD, RESID>(comp, S, io, stage, bars, red, fills, status);
+        default: return run_unit_c<8, true, GRAD, RESID>(comp, S, io, stage, bars, red, fills, status);
     }
 }
 
-// the adjoint always keeps the box-matrix residual
+// the adjoint always keeps the box-matrix residual; comp: the centre-image variant (a guest with
+// several sites where the system's geometry allows it, SysDev::com_axis)
 template <bool GRAD>
-__device__ __forceinline__ bool run_variant(int variant, bool no_resid, const SysDev& S, const UnitIO& io,
+__device__ __forceinline__ bool run_variant(int variant, bool no_resid, bool comp, const SysDev& S, const UnitIO& io,
                                             int4* stage, uint64_t* bars, LsePartial* red,
                                             uint32_t (&fills)[PMGB_NSTAGE], unsigned int* status) {
     if constexpr (!GRAD) {
-        if (no_resid) return run_variant_r<false, false>(variant, S, io, stage, bars, red, fills, status);
+        if (no_resid) return run_variant_r<false, false>(variant, comp, S, io, stage, bars, red, fills, status);
     }
-    return run_variant_r<GRAD, true>(variant, S, io, stage, bars, red, fills, status);
+    return run_variant_r<GRAD, true>(variant, comp, S, io, stage, bars, red, fills, status);
 }
 
 static_assert(sizeof(BatchSystem) % 4 == 0, "BatchSystem is copied to shared memory as 32-bit words");
@@ -112,7 +123,9 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) batch_kernel(const __grid_con
             double x = -inf;
             io.x_out = &x;
             io.m_out = &s_m;
-            if (!run_variant<GRAD>(s_bs.variant, b.no_resid != 0, s_bs.sys, io, stage, bars, red, fills, b.status))
+            const bool comp = s_bs.sys.com_axis >= -1 && s_bs.sys.n_sites > 1;
+            if (!run_variant<GRAD>(s_bs.variant, b.no_resid != 0, comp, s_bs.sys, io, stage, bars, red, fills,
+                                   b.status))
                 return;
             if (GRAD) {
                 if (b.perm) {

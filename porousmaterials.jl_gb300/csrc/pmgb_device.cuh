@@ -125,13 +125,15 @@ __device__ __forceinline__ void make_pose(unsigned long long seed, unsigned long
     const float sq = sqrtf(u3);
     const float v0 = c2 * sq, v1 = s2 * sq, v2 = sqrtf(1.0f - u3);
     // A = 2 v v^T - I ; M = A * Rz with Rz columns (c1, -s1, 0), (s1, c1, 0), (0, 0, 1)
-    const float A[3][3] = {{2.0f * v0 * v0 - 1.0f, 2.0f * v0 * v1, 2.0f * v0 * v2},
-                           {2.0f * v1 * v0, 2.0f * v1 * v1 - 1.0f, 2.0f * v1 * v2},
-                           {2.0f * v2 * v0, 2.0f * v2 * v1, 2.0f * v2 * v2 - 1.0f}};
+    // (explicit fused operations throughout, so that every kernel that draws a pose rounds it
+    // the same way)
+    const float A[3][3] = {{fmaf(2.0f * v0, v0, -1.0f), 2.0f * v0 * v1, 2.0f * v0 * v2},
+                           {2.0f * v1 * v0, fmaf(2.0f * v1, v1, -1.0f), 2.0f * v1 * v2},
+                           {2.0f * v2 * v0, 2.0f * v2 * v1, fmaf(2.0f * v2, v2, -1.0f)}};
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        R[i + 0] = A[i][0] * c1 - A[i][1] * s1;
-        R[i + 3] = A[i][0] * s1 + A[i][1] * c1;
+        R[i + 0] = fmaf(A[i][0], c1, -(A[i][1] * s1));
+        R[i + 3] = fmaf(A[i][0], s1, A[i][1] * c1);
         R[i + 6] = A[i][2];
     }
 }
@@ -162,7 +164,8 @@ __device__ __forceinline__ uint32_t frac2fix64(double x) {
 // as the oracle composes them from the same pose.
 template <int NS>
 __device__ __forceinline__ void pose_sites(const SysDev& S, unsigned long long seed, unsigned long long item,
-                                           uint32_t* ux, uint32_t* uy, uint32_t* uz, float* com = nullptr) {
+                                           uint32_t* ux, uint32_t* uy, uint32_t* uz, float* com = nullptr,
+                                           uint32_t* cfix = nullptr) {
     float xf[3], R[9];
     make_pose(seed, item, xf, R);
     if (com) {
@@ -171,17 +174,22 @@ __device__ __forceinline__ void pose_sites(const SysDev& S, unsigned long long s
         com[2] = xf[2];
     }
     const uint32_t cx = frac2fix(xf[0]), cy = frac2fix(xf[1]), cz = frac2fix(xf[2]);
+    if (cfix) {
+        cfix[0] = cx;
+        cfix[1] = cy;
+        cfix[2] = cz;
+    }
     double r[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) r[i] = static_cast<double>(R[i]);
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
         const double bx = S.body64[k][0], by = S.body64[k][1], bz = S.body64[k][2];
-        const double ox = r[0] * bx + r[3] * by + r[6] * bz;
-        const double oy = r[1] * bx + r[4] * by + r[7] * bz;
-        const double oz = r[2] * bx + r[5] * by + r[8] * bz;
-        ux[k] = cx + frac2fix64(S.g64[0] * ox + S.g64[1] * oy + S.g64[2] * oz);
-        uy[k] = cy + frac2fix64(S.g64[3] * oy + S.g64[4] * oz);
+        const double ox = fma(r[0], bx, fma(r[3], by, r[6] * bz));
+        const double oy = fma(r[1], bx, fma(r[4], by, r[7] * bz));
+        const double oz = fma(r[2], bx, fma(r[5], by, r[8] * bz));
+        ux[k] = cx + frac2fix64(fma(S.g64[0], ox, fma(S.g64[1], oy, S.g64[2] * oz)));
+        uy[k] = cy + frac2fix64(fma(S.g64[3], oy, S.g64[4] * oz));
         uz[k] = cz + frac2fix64(S.g64[5] * oz);
     }
 }
@@ -444,6 +452,39 @@ __device__ __forceinline__ float2 pair2_r2(const int4 ra, const int4 rb, const u
     return fma2(cx, cx, fma2(cy, cy, mul2(cz, cz)));
 }
 
+// Cartesian minimum-image displacements of two records from the guest's pose centre (fixed
+// point cx, cy, cz), converted once per record for all guest sites (the centre-image path).
+template <bool RESID = true>
+__device__ __forceinline__ void com_disp2(const int4 ra, const int4 rb, const uint32_t cx, const uint32_t cy,
+                                          const uint32_t cz, const Geo2& g, float2& X, float2& Y, float2& Z) {
+    const float2 dx = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.x) - cx)),
+                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.x) - cx)));
+    const float2 dy = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.y) - cy)),
+                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.y) - cy)));
+    const float2 dz = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.z) - cz)),
+                                  __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.z) - cz)));
+    if (!RESID) {
+        X = fma2(g.h00, dx, fma2(g.h01, dy, mul2(g.h02, dz)));
+        Y = fma2(g.h11, dy, mul2(g.h12, dz));
+        Z = mul2(g.h22, dz);
+        return;
+    }
+    const float2 rx = fma2(g.p00, dx, fma2(g.p01, dy, mul2(g.p02, dz)));
+    const float2 ry = fma2(g.p11, dy, mul2(g.p12, dz));
+    const float2 rz = mul2(g.p22, dz);
+    X = fma2(g.h00, dx, fma2(g.h01, dy, fma2(g.h02, dz, rx)));
+    Y = fma2(g.h11, dy, fma2(g.h12, dz, ry));
+    Z = fma2(g.h22, dz, rz);
+}
+
+// Squared distances of a guest site from two records, given the records' displacements from
+// the pose centre and the site's negated Cartesian offset (nx, ny, nz).
+__device__ __forceinline__ float2 site_r2(const float2 X, const float2 Y, const float2 Z, const float nx,
+                                          const float ny, const float nz) {
+    const float2 ex = __fadd2_rn(X, f2(nx)), ey = __fadd2_rn(Y, f2(ny)), ez = __fadd2_rn(Z, f2(nz));
+    return fma2(ex, ex, fma2(ey, ey, mul2(ez, ez)));
+}
+
 // LJ and real-space terms of two records at squared distances r2 (charges qa, qb); COLS: also
 // r^-12 and r^-6 within the LJ cutoff into *c12, *c6.
 template <bool CHARGED, bool COLS = false>
@@ -561,7 +602,7 @@ __device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua_in
         sincospif(static_cast<float>(dc[k]) * (0.5f * kTurn), &sn, &cs);  // half angle
         dwr[k] = -2.0f * sn * sn;
         dwi[k] = -2.0f * sn * cs;
-        wdr[k] = 1.0f + dwr[k];
+        wdr[k] = __fadd_rn(1.0f, dwr[k]);  // not fused: the same rounding in every kernel
         wdi[k] = dwi[k];
     }
     for (int row = row0; row < S.n_krow; row += row_step) {
@@ -756,17 +797,34 @@ __device__ __forceinline__ bool chunk_near(const SysDev& S, const ChunkBox* box,
     return __any_sync(0xffffffffu, active && near);
 }
 
+// The same test for the centre-image path, from the pose centre: a record at distance r from the
+// centre lies at least r - com_reach from every guest site, so the sub-chunk can matter only if
+// the bound on r is within cutoff + com_reach (S.com_reach2 its square).
+__device__ __forceinline__ bool chunk_near_com(const SysDev& S, const ChunkBox* box, const uint32_t* cfix,
+                                               bool active) {
+    const uint4 c = __ldg(reinterpret_cast<const uint4*>(box));
+    const uint4 e = __ldg(reinterpret_cast<const uint4*>(box) + 1);
+    const float gx = box_gap(c.x, cfix[0], e.x) * S.cw[0];
+    const float gy = box_gap(c.y, cfix[1], e.y) * S.cw[1];
+    const float gz = box_gap(c.z, cfix[2], e.z) * S.cw[2];
+    const float sum = fmaf(gx, gx, fmaf(gy, gy, gz * gz)) * S.cw_inv_lam;
+    const float mx = fmaxf(fmaxf(gx * gx, gy * gy), gz * gz);
+    return __any_sync(0xffffffffu, active && fmaxf(sum, mx) <= S.com_reach2 * 1.0001f);
+}
+
 // Returns false if a bounded wait gave up (the status word is set); every thread of the CTA
 // returns the same value.  fills[s] counts the completed fills of ring slot s so far; the
 // caller keeps it across units (the barriers are initialised once per CTA).
 // GRAD: the adjoint's per-(segment, site) columns sum r^-12, sum r^-6; FORCES (with GRAD): also
 // dU/dx per item.  Without FORCES the adjoint runs the forward loops with the columns added, so
-// its energies are the forward kernel's.
-template <int NS, bool CHARGED, bool GRAD, bool RESID = true, bool FORCES = GRAD>
+// its energies are the forward kernel's.  COMP: the centre-image path (Widom poses of a guest
+// with several sites where S.com_axis >= -1; the caller checks both).
+template <int NS, bool CHARGED, bool GRAD, bool RESID = true, bool FORCES = GRAD, bool COMP = false>
 __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4* stage, uint64_t* bars,
                                          LsePartial* red, uint32_t (&fills)[PMGB_NSTAGE], unsigned int* status) {
     static_assert(RESID || !GRAD, "the adjoint keeps the box-matrix residual");
     static_assert(GRAD || !FORCES, "forces come with the adjoint");
+    static_assert(!COMP || (!FORCES && NS > 1), "the centre-image path has no forces and several sites");
     constexpr bool COLS = GRAD && !FORCES;
     const int tid = threadIdx.x;
     const bool valid = io.valid;
@@ -776,11 +834,12 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
     uint32_t ux[NS], uy[NS], uz[NS];
 #pragma unroll
     for (int k = 0; k < NS; ++k) ux[k] = uy[k] = uz[k] = 0u;
+    uint32_t cfix[3] = {0u, 0u, 0u};  // the pose centre (COMP)
     bool blocked = false;  // inaccessible pocket: U = +Inf without its pair terms mattering
     if (valid) {
         if (io.pose_mode == POSE_PHILOX) {
             float com[3];
-            pose_sites<NS>(S, io.seed, static_cast<unsigned long long>(item), ux, uy, uz, com);
+            pose_sites<NS>(S, io.seed, static_cast<unsigned long long>(item), ux, uy, uz, com, cfix);
             if (S.acc) blocked = !accessible_com(S, com);
         } else if (io.pose_mode == POSE_SITES) {
             const uint32_t* p = io.site_fix + static_cast<size_t>(item) * S.n_sites * 3;
@@ -842,6 +901,37 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
     int cb = 0;  // running sub-chunk index: the order of S.cbox
     const bool box_cull = io.cull && S.cbox != nullptr;
 
+    // ---- centre-image path (COMP) -----------------------------------------------
+    // Every image of a record within the cutoff of a site has all its fractional displacements
+    // inside (-1/2, 1/2) (the cutoff is below half of every perpendicular width W_d), so it is the
+    // site's wrapped image, the only one that can contribute.  Where every W_d >= 2 (cutoff +
+    // com_reach) (S.com_axis == -1), that image's displacement from the pose centre lies within
+    // cutoff + com_reach < W_d / 2 along every face normal, so it is the centre's wrapped image;
+    // and a site whose wrapped image differs lies at least W_d / 2 - com_reach >= cutoff away in
+    // both, where every term is an exact zero.  So the records' displacements from the centre are
+    // converted once per record and each site subtracts its Cartesian offset: the site registers
+    // hold the negated offsets (FP32 bits) from here on, after the reciprocal space has used them
+    // as fixed points.
+    float plc_hi = 0.0f, plc_lo = 0.0f;
+    if constexpr (COMP) {
+        if (CHARGED && valid) kspace_fwd<NS, false>(S, ux, uy, uz, plc_hi, plc_lo);
+#pragma unroll
+        for (int k = 0; k < NS; ++k) {
+            float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+            if (valid && k < S.n_sites) {
+                const float fx = __int2float_rn(static_cast<int>(ux[k] - cfix[0]));
+                const float fy = __int2float_rn(static_cast<int>(uy[k] - cfix[1]));
+                const float fz = __int2float_rn(static_cast<int>(uz[k] - cfix[2]));
+                nx = -(fmaf(g.h00, fx, fmaf(g.h01, fy, g.h02 * fz)) + fmaf(g.p00, fx, fmaf(g.p01, fy, g.p02 * fz)));
+                ny = -(fmaf(g.h11, fy, g.h12 * fz) + fmaf(g.p11, fy, g.p12 * fz));
+                nz = -fmaf(g.h22, fz, g.p22 * fz);
+            }
+            ux[k] = __float_as_uint(nx);
+            uy[k] = __float_as_uint(ny);
+            uz[k] = __float_as_uint(nz);
+        }
+    }
+
     for (int t = 0; t < n_tiles; ++t) {
         const int slot = t % PMGB_NSTAGE;
         const uint32_t parity = (fills[slot] + static_cast<uint32_t>(t / PMGB_NSTAGE)) & 1u;
@@ -879,9 +969,14 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                 // the others are skipped whole, distances included (warp-uniform)
                 unsigned near_sub = (1u << n_sub) - 1u;
                 if (box_cull) {
-                    for (int sb = 0; sb < n_sub; ++sb)
-                        if (!chunk_near<NS>(S, S.cbox + cb + sb, ux, uy, uz, valid && !blocked, g2.rcmax2))
-                            near_sub &= ~(1u << sb);
+                    if constexpr (COMP) {
+                        for (int sb = 0; sb < n_sub; ++sb)
+                            if (!chunk_near_com(S, S.cbox + cb + sb, cfix, valid && !blocked)) near_sub &= ~(1u << sb);
+                    } else {
+                        for (int sb = 0; sb < n_sub; ++sb)
+                            if (!chunk_near<NS>(S, S.cbox + cb + sb, ux, uy, uz, valid && !blocked, g2.rcmax2))
+                                near_sub &= ~(1u << sb);
+                    }
                     cb += n_sub;
                     if (near_sub == 0u) continue;
                 }
@@ -889,7 +984,81 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
 #pragma unroll
                 for (int k = 0; k < NS; ++k) ljp2[k] = php2[k] = f2(0.0f);
                 float ljp[NS], php[NS];
-                if (FORCES) {
+                // terms of four records for site k from their squared distances; the warp's items
+                // are usually spatially close, so the terms are skipped when no lane has the site
+                // inside the cutoff (those terms are exact zeros, so the sums are unchanged)
+                auto terms4 = [&](int k, float2 d01, float2 d23, const int4& r0, const int4& r1, const int4& r2,
+                                  const int4& r3) {
+                    const float dmin = fminf(fminf(d01.x, d01.y), fminf(d23.x, d23.y));
+                    segmin[k] = fminf(segmin[k], dmin);
+                    if (__any_sync(0xffffffffu, valid && !blocked && dmin < g2.rcmax2)) {
+                        const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
+                        pair2_energy<CHARGED, COLS>(d01, __int_as_float(r0.w), __int_as_float(r1.w), g2, a12, a6,
+                                                    ljp2[k], php2[k], &i12[k], &i6[k]);
+                        pair2_energy<CHARGED, COLS>(d23, __int_as_float(r2.w), __int_as_float(r3.w), g2, a12, a6,
+                                                    ljp2[k], php2[k], &i12[k], &i6[k]);
+                    }
+                };
+                // groups of four over the near sub-chunks, in the order of one sweep over [j0, j1);
+                // a skipped last sub-chunk takes the remainder with it.  Returns the first record
+                // left (fewer than four).
+                auto sweep = [&](auto&& group) {
+                    int j = j0;
+                    if (near_sub == (1u << n_sub) - 1u) {
+                        for (; j + 4 <= j1; j += 4) group(j);
+                    } else {
+                        for (int sb = 0; sb < n_sub; ++sb) {
+                            const int s_end = min(j0 + (sb + 1) * kSub, j1);
+                            if (!(near_sub >> sb & 1u)) {
+                                j = (sb == n_sub - 1) ? j1 : s_end;
+                                continue;
+                            }
+                            for (; j + 4 <= s_end; j += 4) group(j);
+                        }
+                    }
+                    return j;
+                };
+                if constexpr (COMP) {
+                    // centre images (culled or not: the same arithmetic and order, so culling
+                    // changes no sum).  The records' displacements keep the box-matrix residual
+                    // in every variant: one conversion per record serves all sites, and that form
+                    // gives the single-system and the batch kernels the same roundings.
+                    auto group4c = [&](int j) {
+                        const int4 r0 = T[j - t0], r1 = T[j + 1 - t0], r2 = T[j + 2 - t0], r3 = T[j + 3 - t0];
+                        float2 X01, Y01, Z01, X23, Y23, Z23;
+                        com_disp2<true>(r0, r1, cfix[0], cfix[1], cfix[2], g2, X01, Y01, Z01);
+                        com_disp2<true>(r2, r3, cfix[0], cfix[1], cfix[2], g2, X23, Y23, Z23);
+#pragma unroll
+                        for (int k = 0; k < NS; ++k) {
+                            const float nx = __uint_as_float(ux[k]), ny = __uint_as_float(uy[k]),
+                                        nz = __uint_as_float(uz[k]);
+                            terms4(k, site_r2(X01, Y01, Z01, nx, ny, nz), site_r2(X23, Y23, Z23, nx, ny, nz), r0, r1,
+                                   r2, r3);
+                        }
+                    };
+                    int j = sweep(group4c);
+                    for (; j < j1; ++j) {
+                        // one record: the second lane of the packed terms is far beyond every
+                        // cutoff with no charge, so its terms are exact zeros
+                        const int4 r = T[j - t0];
+                        float2 X, Y, Z;
+                        com_disp2<true>(r, r, cfix[0], cfix[1], cfix[2], g2, X, Y, Z);
+#pragma unroll
+                        for (int k = 0; k < NS; ++k) {
+                            float2 dd = site_r2(X, Y, Z, __uint_as_float(ux[k]), __uint_as_float(uy[k]),
+                                                __uint_as_float(uz[k]));
+                            dd.y = 1e30f;
+                            segmin[k] = fminf(segmin[k], dd.x);
+                            pair2_energy<CHARGED, COLS>(dd, __int_as_float(r.w), 0.0f, g2, f2(lj12[k]), f2(lj6[k]),
+                                                        ljp2[k], php2[k], &i12[k], &i6[k]);
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < NS; ++k) {
+                        ljp[k] = ljp2[k].x + ljp2[k].y;
+                        php[k] = php2[k].x + php2[k].y;
+                    }
+                } else if (FORCES) {
                     for (int sb = 0; sb < n_sub; ++sb) {
                     if (!(near_sub >> sb & 1u)) continue;
                     const int s_end = min(j0 + (sb + 1) * kSub, j1);
@@ -1045,7 +1214,12 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
     float gu[NS][3];
 #pragma unroll
     for (int k = 0; k < NS; ++k) gu[k][0] = gu[k][1] = gu[k][2] = 0.0f;
-    if (CHARGED && valid) kspace_fwd<NS, FORCES>(S, ux, uy, uz, pl_hi, pl_lo, gu);
+    if constexpr (COMP) {
+        pl_hi = plc_hi;
+        pl_lo = plc_lo;
+    } else if (CHARGED && valid) {
+        kspace_fwd<NS, FORCES>(S, ux, uy, uz, pl_hi, pl_lo, gu);
+    }
 
     // ---- per-item energies (FP64) ----------------------------------------------
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
@@ -1056,7 +1230,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
         if (k < S.n_sites) {
             uv += static_cast<double>(lj_hi[k]) + static_cast<double>(lj_lo[k]);
             if (CHARGED && S.q[k] != 0.0f)
-                usr += static_cast<double>(S.q[k]) * (static_cast<double>(ph_hi[k]) + static_cast<double>(ph_lo[k]));
+                usr = fma(static_cast<double>(S.q[k]), static_cast<double>(ph_hi[k]) + static_cast<double>(ph_lo[k]), usr);
             if (FORCES) {
                 // real space: dU/dx_site = -2 sum c dU/dr^2; reciprocal space: G^T dU/du
                 gcx += -2.0f * (gx[k].x + gx[k].y) + S.g00 * gu[k][0];

@@ -84,6 +84,11 @@ struct SysDev {
     int n_sites;
     float body[PMGB_MAX_SITES][3];
     float q[PMGB_MAX_SITES];
+    float com_reach;               // largest distance of a guest site from the pose centre (A)
+    // centre-image geometry (set with the cutoffs): com_axis -1 = the pose centre's minimum image
+    // serves every guest site, -2 = per-site images only; com_reach2 = (larger cutoff + com_reach)^2
+    int com_axis;
+    float com_reach2;
     // Ewald reciprocal space
     int n_krow, n_k;
     const KRow* krow;

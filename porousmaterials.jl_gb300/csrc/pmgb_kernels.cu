@@ -6,7 +6,7 @@
 namespace {
 
 // Single-system launch: CTA b runs unit b.
-template <int NS, bool CHARGED, bool GRAD, bool RESID = true, bool FORCES = GRAD>
+template <int NS, bool CHARGED, bool GRAD, bool RESID = true, bool FORCES = GRAD, bool COMP = false>
 __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_constant__ LaunchArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     int4* stage = reinterpret_cast<int4*>(smem_raw);
@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
     io.partial = (a.partials && !a.perm) ? a.partials + blockIdx.x : nullptr;
     ring_init(bars);
     uint32_t fills[PMGB_NSTAGE] = {};
-    (void)run_unit<NS, CHARGED, GRAD, RESID, FORCES>(a.sys, io, stage, bars, red, fills, a.status);
+    (void)run_unit<NS, CHARGED, GRAD, RESID, FORCES, COMP>(a.sys, io, stage, bars, red, fills, a.status);
 }
 
 // ---- latency path: few configurations, one CTA each -----------------------------------
@@ -474,14 +474,28 @@ __global__ void __launch_bounds__(256) fp32_peak_kernel(float* sink, int iters) 
     if (r == 12345.678f) sink[blockIdx.x] = r;
 }
 
-template <int NS, bool CH, bool RESID>
-cudaError_t launch_one_r(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
+// the centre-image variant serves Widom poses of guests with several sites where the system's
+// geometry allows it (SysDev::com_axis)
+__host__ __forceinline__ bool centre_image(const LaunchArgs& a) {
+    return a.pose_mode == POSE_PHILOX && a.sys.com_axis >= -1 && a.sys.n_sites > 1;
+}
+
+template <int NS, bool CH, bool RESID, bool COMP>
+cudaError_t launch_one_rc(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
     const size_t smem = pmgb_pairs_smem_bytes();
-    cudaError_t e = cudaFuncSetAttribute(pairs_kernel<NS, CH, false, RESID>,
+    cudaError_t e = cudaFuncSetAttribute(pairs_kernel<NS, CH, false, RESID, false, COMP>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    pairs_kernel<NS, CH, false, RESID><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
+    pairs_kernel<NS, CH, false, RESID, false, COMP><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
     return cudaGetLastError();
+}
+
+// (the centre-image variant keeps the box-matrix residual whether or not refinement follows)
+template <int NS, bool CH, bool RESID>
+cudaError_t launch_one_r(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
+    if constexpr (NS > 1)
+        if (centre_image(a)) return launch_one_rc<NS, CH, true, true>(a, n_ctas, st);
+    return launch_one_rc<NS, CH, RESID, false>(a, n_ctas, st);
 }
 
 template <int NS, bool CH>
@@ -489,20 +503,23 @@ cudaError_t launch_one(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
     return a.no_resid ? launch_one_r<NS, CH, false>(a, n_ctas, st) : launch_one_r<NS, CH, true>(a, n_ctas, st);
 }
 
-template <int NS, bool CH, bool FORCES>
+template <int NS, bool CH, bool FORCES, bool COMP>
 cudaError_t launch_grad_one_f(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
     const size_t smem = pmgb_pairs_smem_bytes();
-    cudaError_t e = cudaFuncSetAttribute(pairs_kernel<NS, CH, true, true, FORCES>,
+    cudaError_t e = cudaFuncSetAttribute(pairs_kernel<NS, CH, true, true, FORCES, COMP>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    pairs_kernel<NS, CH, true, true, FORCES><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
+    pairs_kernel<NS, CH, true, true, FORCES, COMP><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
     return cudaGetLastError();
 }
 
 // forces (dU/dx) only when the caller asked for them; the columns alone take the forward loops
 template <int NS, bool CH>
 cudaError_t launch_grad_one(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
-    return a.grad_u ? launch_grad_one_f<NS, CH, true>(a, n_ctas, st) : launch_grad_one_f<NS, CH, false>(a, n_ctas, st);
+    if (a.grad_u) return launch_grad_one_f<NS, CH, true, false>(a, n_ctas, st);
+    if constexpr (NS > 1)
+        if (centre_image(a)) return launch_grad_one_f<NS, CH, false, true>(a, n_ctas, st);
+    return launch_grad_one_f<NS, CH, false, false>(a, n_ctas, st);
 }
 
 template <bool CH>

@@ -395,12 +395,12 @@ __device__ __forceinline__ void warp_site_setup(const SysDev& S, unsigned long l
     make_pose(seed, item, xf, R);
     const int k = min(lane / 3, S.n_sites - 1), d = lane % 3;
     const double bx = S.body64[k][0], by = S.body64[k][1], bz = S.body64[k][2];
-    const double ox = static_cast<double>(R[0]) * bx + static_cast<double>(R[3]) * by + static_cast<double>(R[6]) * bz;
-    const double oy = static_cast<double>(R[1]) * bx + static_cast<double>(R[4]) * by + static_cast<double>(R[7]) * bz;
-    const double oz = static_cast<double>(R[2]) * bx + static_cast<double>(R[5]) * by + static_cast<double>(R[8]) * bz;
+    const double ox = fma(static_cast<double>(R[0]), bx, fma(static_cast<double>(R[3]), by, static_cast<double>(R[6]) * bz));
+    const double oy = fma(static_cast<double>(R[1]), bx, fma(static_cast<double>(R[4]), by, static_cast<double>(R[7]) * bz));
+    const double oz = fma(static_cast<double>(R[2]), bx, fma(static_cast<double>(R[5]), by, static_cast<double>(R[8]) * bz));
     double x;
-    if (d == 0) x = static_cast<double>(xf[0]) + (S.g64[0] * ox + S.g64[1] * oy + S.g64[2] * oz);
-    else if (d == 1) x = static_cast<double>(xf[1]) + (S.g64[3] * oy + S.g64[4] * oz);
+    if (d == 0) x = static_cast<double>(xf[0]) + fma(S.g64[0], ox, fma(S.g64[1], oy, S.g64[2] * oz));
+    else if (d == 1) x = static_cast<double>(xf[1]) + fma(S.g64[3], oy, S.g64[4] * oz);
     else x = static_cast<double>(xf[2]) + S.g64[5] * oz;
     const double ux = x * 4294967296.0;
     const long long fx = __double2ll_rn(ux);
@@ -665,11 +665,11 @@ __device__ __forceinline__ void refined_entry(const RefineArgs& a, long long e, 
     make_pose(seed, static_cast<unsigned long long>(item), xf, R);
     for (int k = 0; k < S->n_sites; ++k) {
         const double bx = S->body64[k][0], by = S->body64[k][1], bz = S->body64[k][2];
-        const double ox = static_cast<double>(R[0]) * bx + static_cast<double>(R[3]) * by + static_cast<double>(R[6]) * bz;
-        const double oy = static_cast<double>(R[1]) * bx + static_cast<double>(R[4]) * by + static_cast<double>(R[7]) * bz;
-        const double oz = static_cast<double>(R[2]) * bx + static_cast<double>(R[5]) * by + static_cast<double>(R[8]) * bz;
-        xs[k][0] = static_cast<double>(xf[0]) + (S->g64[0] * ox + S->g64[1] * oy + S->g64[2] * oz);
-        xs[k][1] = static_cast<double>(xf[1]) + (S->g64[3] * oy + S->g64[4] * oz);
+        const double ox = fma(static_cast<double>(R[0]), bx, fma(static_cast<double>(R[3]), by, static_cast<double>(R[6]) * bz));
+        const double oy = fma(static_cast<double>(R[1]), bx, fma(static_cast<double>(R[4]), by, static_cast<double>(R[7]) * bz));
+        const double oz = fma(static_cast<double>(R[2]), bx, fma(static_cast<double>(R[5]), by, static_cast<double>(R[8]) * bz));
+        xs[k][0] = static_cast<double>(xf[0]) + fma(S->g64[0], ox, fma(S->g64[1], oy, S->g64[2] * oz));
+        xs[k][1] = static_cast<double>(xf[1]) + fma(S->g64[3], oy, S->g64[4] * oz);
         xs[k][2] = static_cast<double>(xf[2]) + S->g64[5] * oz;
     }
 }

@@ -48,6 +48,7 @@ SIGNATURES = [
     ("pmgb_structure_factor", C.c_int, [_vp, _dp]),
     ("pmgb_energies", C.c_int, [_vp, C.c_int64, _dp, _dp]),
     ("pmgb_system_set_cull", C.c_int, [_vp, C.c_int32]),
+    ("pmgb_system_set_centre_image", C.c_int, [_vp, C.c_int32]),
     ("pmgb_system_set_accessibility", C.c_int, [_vp, _ip, _ip, C.POINTER(C.c_uint8)]),
     ("pmgb_system_set_refine", C.c_int, [_vp, C.c_double]),
     ("pmgb_system_refined_count", C.c_int, [_vp, C.POINTER(C.c_int64)]),
@@ -70,6 +71,7 @@ SIGNATURES = [
     ("pmgb_batch_tune", C.c_int, [_vp, C.c_uint64, C.c_double, C.c_int32, _dp]),
     ("pmgb_batch_set_refine", C.c_int, [_vp, C.c_double]),
     ("pmgb_batch_set_cull", C.c_int, [_vp, C.c_int32]),
+    ("pmgb_batch_energies", C.c_int, [_vp, _dp]),
     ("pmgb_set_kernel_timing", C.c_int, [_vp, C.c_int32]),
     ("pmgb_kernel_timing", C.c_int, [_vp, _dp, C.POINTER(C.c_int64)]),
     ("pmgb_batch_refined_counts", C.c_int, [_vp, C.POINTER(C.c_int64)]),

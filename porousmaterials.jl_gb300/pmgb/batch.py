@@ -100,6 +100,20 @@ class BatchScreen:
         self.ctx.check(self.ctx._lib.pmgb_batch_refined_counts(self.handle, out.ctypes.data_as(C.POINTER(C.c_int64))))
         return out
 
+    def energies(self) -> list[np.ndarray]:
+        """Per-insertion (U_vdw, U_es) of the last run, one [n_blocks * n_per_block, 2] array per
+        system in index order, refined insertions with their FP64 energies (pmgb_batch_energies:
+        needs culling or refinement on)."""
+        total = int(self.info()["insertions_per_run"])
+        u = np.zeros((total, 2))
+        self.ctx.check(self.ctx._lib.pmgb_batch_energies(self.handle, ptr(u, C.c_double)))
+        out, o = [], 0
+        for npb in self.n_per_block:
+            n = int(npb) * self.n_blocks
+            out.append(u[o:o + n].copy())
+            o += n
+        return out
+
     def launch(self, seed: int, temperature: float):
         """Enqueue one run on the context stream (asynchronous)."""
         self.ctx.check(self.ctx._lib.pmgb_batch_launch(self.handle, int(seed) % (1 << 64), float(temperature)))

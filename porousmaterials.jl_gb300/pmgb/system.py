@@ -144,6 +144,11 @@ class GPUSystem:
         """Spatially ordered evaluation with cutoff culling (pmgb_system_set_cull; default on)."""
         self.ctx.check(self.ctx._lib.pmgb_system_set_cull(self.handle, int(bool(on))))
 
+    def set_centre_image(self, on: bool) -> None:
+        """Centre-image distances for multi-site guests where the cell allows them
+        (pmgb_system_set_centre_image; default on)."""
+        self.ctx.check(self.ctx._lib.pmgb_system_set_centre_image(self.handle, int(bool(on))))
+
     def refined_count(self) -> int:
         """Insertions the last refined Widom run re-evaluated in FP64."""
         out = C.c_int64()
