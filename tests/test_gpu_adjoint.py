@@ -111,19 +111,24 @@ def test_adjoint_without_forces(mol):
     ep = pmgb.setup_Ewald_sum(sc.box, ff.r_cutoff, eps=1e-6) if charged else None
     gs = pmgb.GPUSystem(sc, pmgb.Frac(getattr(synthetic, mol)(), sc.box), ff, ep)
     npb, seed = 3000, 12
-    fwd, u_fwd = gs.widom(npb, 5, seed, T, want_energies=True)
-    b0, a0 = gs.widom_adjoint(npb, 5, seed, T, want_energies=True)                  # columns only
     b1, a1 = gs.widom_adjoint(npb, 5, seed, T, want_energies=True, want_grad=True)  # with forces
-    np.testing.assert_array_equal(a0["u"], u_fwd)
-    np.testing.assert_array_equal(b0, fwd)
-    g0 = henry_gradients(gs, b0, a0, T, npb)
     g1 = henry_gradients(gs, b1, a1, T, npb)
-    for x, y in zip(g0[:2], g1[:2]):
-        scale = max(abs(v) for v in y.values())
-        for sp in y:
-            assert x[sp] == pytest.approx(y[sp], rel=1e-5, abs=1e-7 * scale), sp
-    if charged:
-        assert g0[2] == pytest.approx(g1[2], rel=1e-5)
+    # per-site images: the same pair arithmetic as the forces pass, so FP32 rounding of the columns;
+    # centre images (CO2, the default): to the gradient tolerance
+    for centre, rel in ((False, 1e-5), (True, 1e-4)):
+        gs.set_centre_image(centre)
+        fwd, u_fwd = gs.widom(npb, 5, seed, T, want_energies=True)
+        b0, a0 = gs.widom_adjoint(npb, 5, seed, T, want_energies=True)  # columns only
+        np.testing.assert_array_equal(a0["u"], u_fwd)
+        np.testing.assert_array_equal(b0, fwd)
+        g0 = henry_gradients(gs, b0, a0, T, npb)
+        for x, y in zip(g0[:2], g1[:2]):
+            scale = max(abs(v) for v in y.values())
+            for sp in y:
+                assert x[sp] == pytest.approx(y[sp], rel=rel, abs=1e-7 * scale), (centre, sp)
+        if charged:
+            assert g0[2] == pytest.approx(g1[2], rel=rel), centre
+    gs.set_centre_image(True)
 
 
 def test_dkh_lj():
