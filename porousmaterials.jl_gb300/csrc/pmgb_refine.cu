@@ -9,9 +9,12 @@
 //      gap L_b - x_i, in integer fixed point (order-independent, so deterministic);
 //   2. per block, the smallest gap cut that leaves at most `tail` of the weight above it;
 //   3. stable compaction of the selected insertions (count, scan, scatter in index order);
-//   4. FP64 energies of each selected insertion, one warp each: LJ with the reference's strict
-//      cutoff and overlap rule, real-space q erfc(alpha r)/r, and the reciprocal-space sum
-//      against the FP64 S(k) with exact fixed-point phases;
+//   4. high-precision energies of each selected insertion from its exact pose: LJ with the
+//      reference's strict cutoff and overlap rule, real-space q erfc(alpha r)/r, and the
+//      reciprocal-space sum against S(k) with exact fixed-point phases.  Tiny systems take one
+//      thread per insertion in FP64; the others are cut into chunks of records and k-space rows,
+//      one warp each, computing in double-float (hi + lo FP32 pairs, ~48 bits) on the FP32 pipes
+//      after an FP32 screen queues the pairs near the insertion;
 //   5. per block, the FP64 minus FP32 differences of e^{x}, U_vdw e^{x} and U_es e^{x}, added
 //      in index order to the block results; refined energies replace the FP32 ones in u.
 // The unrefined remainder then contributes at most tail x (its largest FP32 error)/T to
