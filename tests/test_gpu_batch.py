@@ -135,6 +135,30 @@ def test_batch_lj_members_match_oracle(mixed_systems):
             assert abs(refined[s, b, 0] - ref[b, 0]) <= 1e-6, (s, b)  # K_H within 1e-6 relative
 
 
+def test_batch_energies_match_single_system(mixed_systems):
+    """pmgb_batch_energies: every system's per-insertion energies, refined ones in FP64, equal
+    pmgb_widom's with the system's own seed; without culling and refinement there are none."""
+    npb, nb, seed = 300, 5, 71
+    screen = BatchScreen(mixed_systems, npb, nb, refine_tail=1e-3)
+    try:
+        screen.run(seed, T)
+        energies = screen.energies()
+        assert len(energies) == len(mixed_systems)
+        for s, gs in enumerate(mixed_systems):
+            gs.set_refine(1e-3)
+            _, u = gs.widom(npb, nb, system_seed(seed, s), T, want_energies=True)
+            gs.set_refine(0.0)
+            assert energies[s].shape == (npb * nb, 2)
+            np.testing.assert_array_equal(energies[s], u)
+        screen.set_refine(0.0)
+        screen.set_cull(False)
+        screen.run(seed, T)
+        with pytest.raises(pmgb.PMGBError):
+            screen.energies()
+    finally:
+        screen.close()
+
+
 def test_batch_refine_matches_single_system(mixed_systems):
     npb, nb, seed = 500, 5, 66
     screen = BatchScreen(mixed_systems, npb, nb, refine_tail=1e-3)
