@@ -302,7 +302,7 @@ extern "C" int pmgb_create(int device, pmgb_ctx** out) {
     cudaDeviceProp prop{};
     cudaGetDeviceProperties(&prop, device);
     if (prop.major < 10)
-        return fail(nullptr, PMGB_ERR_UNSUPPORTED, "pmgb_create: device %d is sm_%d%d; this build targets sm_103a",
+        return fail(nullptr, PMGB_ERR_UNSUPPORTED, "pmgb_create: device %d is sm_%d%d; libpmgb targets sm_103a",
                     device, prop.major, prop.minor);
     pmgb_ctx* c = new pmgb_ctx();
     c->device = device;

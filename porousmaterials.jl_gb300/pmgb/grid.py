@@ -103,7 +103,7 @@ def energy_grid(crystal: Crystal, molecule: Molecule, ljforcefield: LJForceField
         if math.isnan(temperature):
             raise ValueError("Must pass temperature (K) for Boltzmann weighted rotations.")
         raise NotImplementedError("energy grids of multi-site probes (rotational Boltzmann averages) are not "
-                                  "supported by this build")
+                                  "supported by pmgb")
     origin = crystal.box.f_to_c @ np.array([-0.5, -0.5, -0.5]) if center else np.zeros(3)
     if verbose:
         print(f"Computing energy grid of {molecule.species} in {crystal.name}")
