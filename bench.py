@@ -408,9 +408,10 @@ def other_configs(args, ctx, stream):
                 "energy terms of most remaining groups, so that figure exceeds the FP32 peak; "
                 "fp32_only_tflops_inside_cutoff counts distances of all pairs and energy terms inside the cutoff, "
                 "so it too credits the skipped distances",
-        "distances": "centre images: every width of this cell exceeds 2 (cutoff + 1.16 A), so each record's "
-                     "minimum image is taken from the pose centre once and the three sites subtract their offsets "
-                     "(pmgb_system_set_centre_image; the per-site form differs by FP32 rounding only)"}
+        "centre_image": gs.info()["centre_image"],
+        "distances": "with centre_image, each record's minimum image is taken from the pose centre once and the "
+                     "three sites subtract their offsets (every width of this cell exceeds 2 (cutoff + 1.16 A); "
+                     "pmgb_system_set_centre_image; the per-site form differs by FP32 rounding only)"}
     del gs
 
     # Monte Carlo move latency: one configuration per call through the captured graph

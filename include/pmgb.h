@@ -172,6 +172,10 @@ int pmgb_system_set_cull(pmgb_system* sys, int32_t on);
  * when it is created. */
 int pmgb_system_set_centre_image(pmgb_system* sys, int32_t on);
 
+/* *on_out = 1 when Widom insertions of this system take the centre-image form (switched on, a
+ * guest with several sites, and every width wide enough for the current cutoffs), else 0. */
+int pmgb_system_centre_image(const pmgb_system* sys, int32_t* on_out);
+
 /* Number of insertions the last refined Widom run re-evaluated in FP64 (synchronises). */
 int pmgb_system_refined_count(pmgb_system* sys, int64_t* count_out);
 

@@ -1408,6 +1408,12 @@ extern "C" int pmgb_system_set_cull(pmgb_system* s, int32_t on) {
     return PMGB_OK;
 }
 
+extern "C" int pmgb_system_centre_image(const pmgb_system* s, int32_t* on_out) {
+    if (!s || !on_out) return PMGB_ERR_INVALID_ARGUMENT;
+    *on_out = (s->dev.com_axis >= -1 && s->dev.n_sites > 1) ? 1 : 0;
+    return PMGB_OK;
+}
+
 extern "C" int pmgb_system_set_centre_image(pmgb_system* s, int32_t on) {
     if (!s) return PMGB_ERR_INVALID_ARGUMENT;
     s->centre_image = on != 0;

@@ -49,6 +49,7 @@ SIGNATURES = [
     ("pmgb_energies", C.c_int, [_vp, C.c_int64, _dp, _dp]),
     ("pmgb_system_set_cull", C.c_int, [_vp, C.c_int32]),
     ("pmgb_system_set_centre_image", C.c_int, [_vp, C.c_int32]),
+    ("pmgb_system_centre_image", C.c_int, [_vp, C.POINTER(C.c_int32)]),
     ("pmgb_system_set_accessibility", C.c_int, [_vp, _ip, _ip, C.POINTER(C.c_uint8)]),
     ("pmgb_system_set_refine", C.c_int, [_vp, C.c_double]),
     ("pmgb_system_refined_count", C.c_int, [_vp, C.POINTER(C.c_int64)]),

@@ -92,7 +92,11 @@ class GPUSystem:
         out = np.zeros(6, dtype=np.int64)
         self.ctx.check(self.ctx._lib.pmgb_system_info(self.handle, ptr(out, C.c_int64)))
         keys = ("n_records", "n_segments", "n_kvecs", "n_kvecs_evaluated", "n_sites", "h2d_bytes")
-        return {k: int(v) for k, v in zip(keys, out)}
+        info = {k: int(v) for k, v in zip(keys, out)}
+        on = C.c_int32()
+        self.ctx.check(self.ctx._lib.pmgb_system_centre_image(self.handle, C.byref(on)))
+        info["centre_image"] = bool(on.value)  # Widom distances from the pose centre (set_centre_image)
+        return info
 
     # -- evaluation ----------------------------------------------------------------------
     def site_coords(self, atom_xf: np.ndarray, charge_xf: np.ndarray | None) -> np.ndarray:

@@ -56,6 +56,20 @@ def _oracle_energies(gs, n_per_block, seed, n_blocks=5):
     return v, sr + lr, sv, ss + sl
 
 
+def test_centre_image_applies_where_the_cell_is_wide(wide):
+    assert wide.info()["centre_image"]
+    narrow = _system(synthetic.config1())  # 2x2x3 of a 13.2 x 18.9 x 9.8 A cell: 25.8 A across a
+    assert not narrow.info()["centre_image"]
+    try:
+        wide.set_centre_image(False)
+        assert not wide.info()["centre_image"]
+    finally:
+        wide.set_centre_image(True)
+    assert wide.info()["centre_image"]
+    ch4 = pmgb.GPUSystem(wide.crystal, pmgb.Frac(synthetic.ch4(), wide.crystal.box), synthetic.forcefield())
+    assert not ch4.info()["centre_image"]  # one site: it is the centre
+
+
 def test_centre_image_energies_match_oracle(wide):
     npb, seed = 200, 5
     v, es, sv, se = _oracle_energies(wide, npb, seed)
