@@ -453,8 +453,8 @@ __device__ __forceinline__ float2 pair2_r2(const int4 ra, const int4 rb, const u
 }
 
 // Cartesian minimum-image displacements of two records from the guest's pose centre (fixed
-// point cx, cy, cz), converted once per record for all guest sites (the centre-image path).
-template <bool RESID = true>
+// point cx, cy, cz), converted once per record for all guest sites (the centre-image path),
+// with the box-matrix residual.
 __device__ __forceinline__ void com_disp2(const int4 ra, const int4 rb, const uint32_t cx, const uint32_t cy,
                                           const uint32_t cz, const Geo2& g, float2& X, float2& Y, float2& Z) {
     const float2 dx = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.x) - cx)),
@@ -463,12 +463,6 @@ __device__ __forceinline__ void com_disp2(const int4 ra, const int4 rb, const ui
                                   __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.y) - cy)));
     const float2 dz = make_float2(__int2float_rn(static_cast<int>(static_cast<uint32_t>(ra.z) - cz)),
                                   __int2float_rn(static_cast<int>(static_cast<uint32_t>(rb.z) - cz)));
-    if (!RESID) {
-        X = fma2(g.h00, dx, fma2(g.h01, dy, mul2(g.h02, dz)));
-        Y = fma2(g.h11, dy, mul2(g.h12, dz));
-        Z = mul2(g.h22, dz);
-        return;
-    }
     const float2 rx = fma2(g.p00, dx, fma2(g.p01, dy, mul2(g.p02, dz)));
     const float2 ry = fma2(g.p11, dy, mul2(g.p12, dz));
     const float2 rz = mul2(g.p22, dz);
@@ -1026,8 +1020,8 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                     auto group4c = [&](int j) {
                         const int4 r0 = T[j - t0], r1 = T[j + 1 - t0], r2 = T[j + 2 - t0], r3 = T[j + 3 - t0];
                         float2 X01, Y01, Z01, X23, Y23, Z23;
-                        com_disp2<true>(r0, r1, cfix[0], cfix[1], cfix[2], g2, X01, Y01, Z01);
-                        com_disp2<true>(r2, r3, cfix[0], cfix[1], cfix[2], g2, X23, Y23, Z23);
+                        com_disp2(r0, r1, cfix[0], cfix[1], cfix[2], g2, X01, Y01, Z01);
+                        com_disp2(r2, r3, cfix[0], cfix[1], cfix[2], g2, X23, Y23, Z23);
 #pragma unroll
                         for (int k = 0; k < NS; ++k) {
                             const float nx = __uint_as_float(ux[k]), ny = __uint_as_float(uy[k]),
@@ -1042,7 +1036,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                         // cutoff with no charge, so its terms are exact zeros
                         const int4 r = T[j - t0];
                         float2 X, Y, Z;
-                        com_disp2<true>(r, r, cfix[0], cfix[1], cfix[2], g2, X, Y, Z);
+                        com_disp2(r, r, cfix[0], cfix[1], cfix[2], g2, X, Y, Z);
 #pragma unroll
                         for (int k = 0; k < NS; ++k) {
                             float2 dd = site_r2(X, Y, Z, __uint_as_float(ux[k]), __uint_as_float(uy[k]),
