@@ -142,6 +142,22 @@ function widom_adjoint(sys::GPUSystem, nb_per_block::Integer, temperature::Float
     return blocks, dθ
 end
 
+"""
+    set_centre_image!(sys, on); centre_image(sys) -> Bool
+
+pmgb_system_set_centre_image / pmgb_system_centre_image: Widom distances from the pose centre
+for guests with several sites, where every width of the supercell is at least
+2 (cutoff + guest reach) + 0.1 Å (on by default; the per-site form differs by FP32 rounding only).
+"""
+set_centre_image!(sys::GPUSystem, on::Bool) =
+    check(sys.ctx, ccall((:pmgb_system_set_centre_image, LIB), Cint, (Ptr{Cvoid}, Int32), sys.ptr, Int32(on)))
+
+function centre_image(sys::GPUSystem)
+    on = Ref{Int32}(0)
+    check(sys.ctx, ccall((:pmgb_system_centre_image, LIB), Cint, (Ptr{Cvoid}, Ptr{Int32}), sys.ptr, on))
+    return on[] != 0
+end
+
 # ---------------------------------------------------------------------------- drop-in bodies
 """
 Drop-in for `henry_coefficient` (src/henry.jl:34-181): the same set-up, statistics, result
@@ -153,7 +169,7 @@ function henry_coefficient(crystal::Crystal, molecule::Molecule, temperature::Fl
                            ljforcefield::LJForceField; insertions_per_volume::Union{Int, Float64}=200,
                            verbose::Bool=true, ewald_precision::Float64=1e-6, autosave::Bool=true,
                            filename_comment::AbstractString="", seed::UInt64=rand(UInt64),
-                           ctx::Context=default_context(), refine_tail::Float64=1e-3)
+                           ctx::Context=default_context(), refine_tail::Float64=1e-3, return_energies::Bool=false)
     assert_P1_symmetry(crystal)
     time_start = time()
     nb_insertions = max(N_BLOCKS, ceil(Int, insertions_per_volume * crystal.box.Ω))
@@ -297,10 +313,13 @@ end
 
 # ---------------------------------------------------------------------------- batched screening
 """
-    henry_screen(crystals, molecule, temperature, ljff; insertions=20_000, seed=0, tune=true)
+    henry_screen(crystals, molecule, temperature, ljff; insertions=20_000, seed=0, tune=true,
+                 return_energies=false)
 
 K_H (mol/(m³ bar)) of every crystal from one persistent, graph-captured launch
-(pmgb_batch_*).  System s uses the Philox key seed + s * 0x9E3779B97F4A7C15.
+(pmgb_batch_*).  System s uses the Philox key seed + s * 0x9E3779B97F4A7C15.  With
+`return_energies`, also each crystal's per-insertion energies as a 2 x n matrix
+(U_vdw, U_es in K; pmgb_batch_energies).
 """
 function henry_screen(crystals::Vector{Crystal}, molecule::Molecule, temperature::Float64, ljff::LJForceField;
                       insertions::Int=20_000, seed::Integer=0, tune::Bool=true, ewald_precision=1e-6,
@@ -330,7 +349,12 @@ function henry_screen(crystals::Vector{Crystal}, molecule::Molecule, temperature
         check(ctx, ccall((:pmgb_batch_results, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}),
                          handle[], blocks, C_NULL))
         R = PorousMaterials.UNIV_GAS_CONST
-        return [mean(exp.(blocks[1, :, s] .- log(R * temperature * nb))) for s in 1:length(systems)]
+        kh = [mean(exp.(blocks[1, :, s] .- log(R * temperature * nb))) for s in 1:length(systems)]
+        return_energies || return kh
+        n = nb * N_BLOCKS
+        u = zeros(2, n * length(systems))  # (U_vdw, U_es) per insertion, system after system
+        check(ctx, ccall((:pmgb_batch_energies, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), handle[], u))
+        return kh, [u[:, (s - 1) * n + 1:s * n] for s in 1:length(systems)]
     finally
         ccall((:pmgb_batch_destroy, LIB), Cvoid, (Ptr{Cvoid},), handle[])
     end
