@@ -5,8 +5,8 @@
  * The reference (PorousMaterials.jl v0.4.2, pure Julia) has no FFI for this path; its
  * boundary is the exported Julia functions.  Each entry point below names the reference
  * function it replaces (file:line inside the PorousMaterials.jl source tree).  A Julia
- * package binds these with `ccall`; Python binds them with ctypes
- * (porousmaterials.jl_gb300/pmgb/_lib.py).
+ * package binds these with `ccall` (porousmaterials.jl_gb300/julia/PorousMaterialsGB300.jl);
+ * Python binds them with ctypes (porousmaterials.jl_gb300/pmgb/_lib.py).
  *
  * Conventions
  *   - Every function returns PMGB_OK (0) or a negative PMGB_ERR_* code; the message of the
@@ -184,16 +184,24 @@ int pmgb_system_refined_count(pmgb_system* sys, int64_t* count_out);
 int pmgb_widom_device(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
                       double temperature, double* block_out_dev, double* u_out_dev);
 
-/* The computation of pmgb_widom_device for callers that cannot let the library allocate:
- * the call makes no cudaMalloc / cudaFree (which synchronise the whole device and may find
- * no memory left when another allocator's pool holds it) and uses a fixed per-device scratch
- * array instead, sized for at most 65,536 CTAs: n_blocks * ceil(n_per_block / 256) <= 65536,
- * i.e. up to 16.7M insertions per call; larger requests fail with PMGB_ERR_INVALID_ARGUMENT.
+/* Widom insertions for callers that cannot let the library allocate.  Some hosts cannot have
+ * cudaMalloc / cudaFree called under them during a run: cudaFree synchronises the whole
+ * device (a stall for a host that keeps other work in flight on the GPU), and a process whose
+ * device memory is held by another framework's caching allocator may find none left.  This
+ * call makes no allocation and no free: its per-CTA partial sums live in a fixed per-device
+ * array (3 MiB, held by every GPU that loads the library until the process exits), sized for
+ * at most 65,536 CTAs: n_blocks * ceil(n_per_block / 256) <= 65536, i.e. up to 16.7M
+ * insertions per call; larger requests fail with PMGB_ERR_INVALID_ARGUMENT.
+ * What it computes: the FP32 pass of pmgb_widom_device with the same poses, energies and block
+ * results.  Spatial ordering (pmgb_system_set_cull) is not applied; it changes no result bit.
+ * FP64 tail refinement needs per-run scratch, so a system with pmgb_system_set_refine(> 0) is
+ * refused with PMGB_ERR_INVALID_ARGUMENT rather than given an unrefined K_H.
  * The caller passes device-resident outputs (block_out_dev: 4*n_blocks doubles, u_out_dev
- * optional).  The first call on a device looks up the scratch address (once per device);
- * make that first call before any stream capture.  All calls on a device share the one
- * array: calls that overlap on the GPU (other streams or threads) race and must be
- * serialised by the caller.  No counterpart in the reference. */
+ * optional).  The first call on a device looks up the array's device address (once per
+ * device, cached; host threads may race on that first lookup harmlessly, all storing the same
+ * address); make that first call before any stream capture.  All calls on a device share the
+ * one array and overwrite it: calls that overlap on the GPU (other streams or threads) race
+ * and must be serialised by the caller.  No counterpart in the reference. */
 int pmgb_widom_noalloc(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
                        double temperature, double* block_out_dev, double* u_out_dev);
 
@@ -325,6 +333,13 @@ int pmgb_fp32_peak(pmgb_ctx* ctx, int n_ctas, int iters, double* tflops_out);
 
 /* Read and clear the device status word (0 = no kernel-side failure). */
 int pmgb_device_status(pmgb_ctx* ctx, uint32_t* status_out);
+
+/* Self-test of the failure path of the kernels' bounded waits (no reference counterpart): one
+ * thread waits at most limit_ns (1 .. 1e8) on a shared-memory mbarrier.  arm = 1 announces a
+ * transfer that nothing delivers (no copy is issued, so none is in flight when the wait gives
+ * up): the kernel records the staging-timeout bit in the status word and returns, and the call
+ * returns PMGB_ERR_DEVICE_STATUS with the status cleared.  arm = 0 completes the phase: PMGB_OK. */
+int pmgb_test_bounded_wait(pmgb_ctx* ctx, int64_t limit_ns, int32_t arm);
 
 /* Kernel timing (no reference counterpart; measurement): while on, every Widom pass records a
  * CUDA event before and after its pair-kernel launch on the launching stream (at most 4096

@@ -400,6 +400,16 @@ extern "C" int pmgb_synchronize(pmgb_ctx* ctx) {
     return PMGB_OK;
 }
 
+extern "C" int pmgb_test_bounded_wait(pmgb_ctx* ctx, int64_t limit_ns, int32_t arm) {
+    if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
+    if (limit_ns < 1 || limit_ns > 100000000)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_test_bounded_wait: limit_ns in [1, 1e8]");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, pmgb_launch_bounded_wait_test(ctx->d_status, static_cast<unsigned long long>(limit_ns), arm ? 1 : 0,
+                                               ctx->stream));
+    return check_status(ctx);
+}
+
 extern "C" int pmgb_device_status(pmgb_ctx* ctx, uint32_t* status_out) {
     if (!ctx || !status_out) return PMGB_ERR_INVALID_ARGUMENT;
     PMGB_CK(ctx, cudaSetDevice(ctx->device));
@@ -1438,8 +1448,11 @@ extern "C" int pmgb_widom_device(pmgb_system* s, int64_t n_per_block, int32_t n_
     if (!(temperature > 0.0) || !std::isfinite(temperature))
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom: temperature must be positive (got %g)", temperature);
     if (int rc = ready_for_charges(s)) return rc;
+    // compare before multiplying: n_per_block near INT64_MAX must not wrap the CTA count
+    if (n_per_block > static_cast<int64_t>(INT32_MAX) * PMGB_THREADS)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom: too many insertions per block for one launch");
     const int64_t cpb = (n_per_block + PMGB_THREADS - 1) / PMGB_THREADS;
-    if (cpb * n_blocks > INT32_MAX)
+    if (cpb > INT32_MAX / n_blocks)
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom: too many insertions for one launch");
     PMGB_CK(ctx, cudaSetDevice(ctx->device));
     const int n_ctas = static_cast<int>(cpb * n_blocks);
@@ -1482,8 +1495,10 @@ extern "C" int pmgb_widom_device(pmgb_system* s, int64_t n_per_block, int32_t n_
     return PMGB_OK;
 }
 
-// Same launches as pmgb_widom_device, with the per-CTA partials in the library's fixed
-// device array instead of memory the system allocates; nothing is allocated or freed.
+// The unordered FP32 Widom pass of pmgb_widom_device, with the per-CTA partials in the
+// library's fixed device array instead of memory the system allocates; nothing is allocated
+// or freed.  Spatial ordering is not applied: it changes no result bit (the ordered pass forms
+// the same sums), only the time.  A system with FP64 tail refinement is refused.
 extern "C" int pmgb_widom_noalloc(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
                                   double temperature, double* block_out_dev, double* u_out_dev) {
     if (!s) return PMGB_ERR_INVALID_ARGUMENT;
@@ -1495,14 +1510,20 @@ extern "C" int pmgb_widom_noalloc(pmgb_system* s, int64_t n_per_block, int32_t n
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_noalloc: temperature must be positive (got %g)",
                     temperature);
     if (int rc = ready_for_charges(s)) return rc;
-    const int64_t cpb = (n_per_block + PMGB_THREADS - 1) / PMGB_THREADS;
-    if (cpb * n_blocks > PMGB_NOALLOC_MAX_CTAS)
+    if (s->refine_tail > 0.0)
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT,
-                    "pmgb_widom_noalloc: %lld blocks of %lld insertions need %lld CTAs of %d insertions; the fixed "
-                    "scratch holds %d (at most %lld insertions per call)",
-                    static_cast<long long>(n_blocks), static_cast<long long>(n_per_block),
-                    static_cast<long long>(cpb * n_blocks), PMGB_THREADS, PMGB_NOALLOC_MAX_CTAS,
-                    static_cast<long long>(PMGB_NOALLOC_MAX_CTAS) * PMGB_THREADS);
+                    "pmgb_widom_noalloc: this system refines its Boltzmann tail in FP64 (pmgb_system_set_refine), "
+                    "which needs per-run scratch the fixed array does not hold; switch refinement off for this "
+                    "call or use pmgb_widom_device");
+    // compare before multiplying: the CTA count must not wrap for huge n_per_block
+    const int64_t cpb = (n_per_block + PMGB_THREADS - 1) / PMGB_THREADS;
+    if (n_per_block > static_cast<int64_t>(PMGB_NOALLOC_MAX_CTAS) * PMGB_THREADS ||
+        cpb > PMGB_NOALLOC_MAX_CTAS / n_blocks)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT,
+                    "pmgb_widom_noalloc: %lld blocks of %lld insertions need more than the fixed scratch's %d CTAs "
+                    "of %d insertions (at most %lld insertions per call)",
+                    static_cast<long long>(n_blocks), static_cast<long long>(n_per_block), PMGB_NOALLOC_MAX_CTAS,
+                    PMGB_THREADS, static_cast<long long>(PMGB_NOALLOC_MAX_CTAS) * PMGB_THREADS);
     PMGB_CK(ctx, cudaSetDevice(ctx->device));
     LsePartial* scratch = nullptr;
     PMGB_CK(ctx, pmgb_noalloc_scratch(ctx->device, &scratch));

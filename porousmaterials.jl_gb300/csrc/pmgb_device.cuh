@@ -80,12 +80,13 @@ __device__ __forceinline__ unsigned long long global_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
-// Spin on an mbarrier phase for at most kWaitLimitNs (and a hard iteration cap).
-__device__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+// Spin on an mbarrier phase for at most limit_ns (and a hard iteration cap).
+__device__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                  unsigned long long limit_ns = kWaitLimitNs) {
     unsigned long long t0 = global_ns();
     for (uint32_t it = 0; it < (1u << 28); ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 63u) == 63u && global_ns() - t0 > kWaitLimitNs) return false;
+        if ((it & 63u) == 63u && global_ns() - t0 > limit_ns) return false;
     }
     return false;
 }

@@ -321,6 +321,8 @@ cudaError_t pmgb_launch_sample_poses(unsigned long long seed, long long start, l
 cudaError_t pmgb_launch_philox(const unsigned int* ctr, const unsigned int* key, long long n,
                                unsigned int* out, cudaStream_t st);
 cudaError_t pmgb_launch_fp32_peak(float* sink, int n_ctas, int iters, cudaStream_t st);
+cudaError_t pmgb_launch_bounded_wait_test(unsigned int* status, unsigned long long limit_ns, int arm,
+                                          cudaStream_t st);
 size_t pmgb_pairs_smem_bytes();
 
 // fixed per-device scratch of pmgb_widom_noalloc (defined in pmgb_kernels.cu)

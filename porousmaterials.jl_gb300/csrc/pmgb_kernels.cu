@@ -3,6 +3,8 @@
 // exported launchers.  The per-unit device body lives in pmgb_device.cuh.
 #include "pmgb_device.cuh"
 
+#include <atomic>
+
 namespace {
 
 // Single-system launch: CTA b runs unit b.
@@ -648,6 +650,31 @@ cudaError_t pmgb_launch_philox(const unsigned int* ctr, const unsigned int* key,
     return cudaGetLastError();
 }
 
+// Self-test of the bounded mbarrier wait the staging ring uses.  One thread initialises an
+// mbarrier for one arrival; with `arm` it arrives announcing 16 bytes of transaction that no
+// copy will ever deliver (no bulk copy is issued, so nothing is in flight), otherwise it
+// arrives plainly and the phase completes.  The wait, limited to limit_ns, then either gives up
+// -- the kernel records PMGB_DEVERR_TMA_TIMEOUT in the status word, as the ring's failure path
+// does, and returns -- or succeeds.
+__global__ void bounded_wait_test_kernel(unsigned int* status, unsigned long long limit_ns, int arm) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    if (arm) {
+        mbar_expect_tx(&bar, 16u);
+    } else {
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&bar)) : "memory");
+    }
+    if (!mbar_wait_bounded(&bar, 0u, limit_ns)) atomicOr(status, PMGB_DEVERR_TMA_TIMEOUT);
+}
+
+cudaError_t pmgb_launch_bounded_wait_test(unsigned int* status, unsigned long long limit_ns, int arm,
+                                          cudaStream_t st) {
+    bounded_wait_test_kernel<<<1, 32, 0, st>>>(status, limit_ns, arm);
+    return cudaGetLastError();
+}
+
 cudaError_t pmgb_launch_fp32_peak(float* sink, int n_ctas, int iters, cudaStream_t st) {
     fp32_peak_kernel<<<n_ctas, 256, 0, st>>>(sink, iters);
     return cudaGetLastError();
@@ -669,16 +696,18 @@ __device__ __align__(256) LsePartial g_noalloc_partials[PMGB_NOALLOC_MAX_CTAS];
 
 // Device address of g_noalloc_partials on `device` (which must be current).  Host code must
 // not use the symbol itself: on the host it names a stand-in, not device memory.  The
-// lookup runs once per device and is cached; it allocates nothing.
+// lookup runs once per device and is cached in an atomic slot, so host threads with their
+// own contexts may make their first calls concurrently (each may look the address up; all
+// store the same value).  It allocates nothing.
 cudaError_t pmgb_noalloc_scratch(int device, LsePartial** ptr) {
-    static void* cached[PMGB_NOALLOC_MAX_DEVICES] = {};
+    static std::atomic<void*> cached[PMGB_NOALLOC_MAX_DEVICES] = {};
     if (device < 0 || device >= PMGB_NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
-    if (!cached[device]) {
-        void* p = nullptr;
+    void* p = cached[device].load(std::memory_order_acquire);
+    if (!p) {
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
         if (e != cudaSuccess) return e;
-        cached[device] = p;
+        cached[device].store(p, std::memory_order_release);
     }
-    *ptr = static_cast<LsePartial*>(cached[device]);
+    *ptr = static_cast<LsePartial*>(p);
     return cudaSuccess;
 }

@@ -82,6 +82,7 @@ SIGNATURES = [
     ("pmgb_philox4x32_10", C.c_int, [_vp, C.c_int64, _up, _up, _up]),
     ("pmgb_fp32_peak", C.c_int, [_vp, C.c_int, C.c_int, _dp]),
     ("pmgb_device_status", C.c_int, [_vp, _up]),
+    ("pmgb_test_bounded_wait", C.c_int, [_vp, C.c_int64, C.c_int32]),
 ]
 
 
@@ -167,6 +168,11 @@ class Context:
         st = C.c_uint32(0)
         self.check(self._lib.pmgb_device_status(self.handle, C.byref(st)))
         return int(st.value)
+
+    def test_bounded_wait(self, limit_ns: int, arm: bool) -> None:
+        """Run the self-test of the kernels' bounded mbarrier wait (pmgb_test_bounded_wait);
+        raises PMGBError (kernel-side failure) when the wait gave up."""
+        self.check(self._lib.pmgb_test_bounded_wait(self.handle, int(limit_ns), int(bool(arm))))
 
     def philox4x32_10(self, ctr: np.ndarray, key: np.ndarray) -> np.ndarray:
         ctr = np.ascontiguousarray(ctr, dtype=np.uint32).reshape(-1, 4)

@@ -26,12 +26,14 @@ def golden():
 
 
 @pytest.fixture(scope="session", autouse=True)
-def _data_paths():
+def _data_paths(tmp_path_factory):
     import pmgb
 
     pmgb.set_paths(DATA)
-    pmgb.rc["paths"]["simulations"] = str(ROOT / "_work" / "simulations")
-    pmgb.rc["paths"]["grids"] = str(ROOT / "_work" / "grids")
+    # results the drop-ins save (autosave, .cube files) go to the session's temporary folder
+    out = tmp_path_factory.mktemp("pm_output")
+    pmgb.rc["paths"]["simulations"] = str(out / "simulations")
+    pmgb.rc["paths"]["grids"] = str(out / "grids")
     yield
 
 

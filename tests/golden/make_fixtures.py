@@ -4,14 +4,16 @@ The reference (PorousMaterials.jl, pure Julia) cannot run here, so its pins are 
 test inputs and known answers: this script copies the input files its tests read
 (crystals, force fields, molecules, NIST configurations) into data/ and writes
 golden.json with the expected values those tests assert, each with the test file:line.
-Run:  python tests/golden/make_fixtures.py [path/to/PorousMaterials.jl]
+Run:  python tests/golden/make_fixtures.py path/to/PorousMaterials.jl
 """
 import json
 import shutil
 import sys
 from pathlib import Path
 
-REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_fixtures.py path/to/PorousMaterials.jl")
+REF = Path(sys.argv[1])
 OUT = Path(__file__).resolve().parent / "data"
 
 FILES = {

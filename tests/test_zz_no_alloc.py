@@ -53,8 +53,20 @@ def test_noalloc_matches_allocating_entry_point():
     again_b, _ = run(lib.pmgb_widom_noalloc, first[0])
     np.testing.assert_allclose(again_b, first[1], rtol=1e-12, atol=1e-9)
 
-    # a request larger than the fixed scratch is refused with a clear message
+    # a request larger than the fixed scratch is refused with a clear message, also where the
+    # CTA count would wrap a 64-bit product
     out = torch.empty(4 * n_blocks, dtype=torch.float64, device=dev)
-    with pytest.raises(pmgb.PMGBError, match="fixed scratch"):
-        ctx.check(lib.pmgb_widom_noalloc(system.handle, 65536 * 256, n_blocks, 1, 298.0, out.data_ptr(), None))
+    for npb in (65536 * 256, 2 ** 62):
+        with pytest.raises(pmgb.PMGBError, match="fixed scratch"):
+            ctx.check(lib.pmgb_widom_noalloc(system.handle, npb, n_blocks, 1, 298.0, out.data_ptr(), None))
+
+    # a system that refines its Boltzmann tail in FP64 needs per-run scratch: the call refuses it
+    # instead of returning the unrefined K_H, and works again once refinement is off
+    system.set_refine(1e-3)
+    with pytest.raises(pmgb.PMGBError, match="refines its Boltzmann tail"):
+        ctx.check(lib.pmgb_widom_noalloc(system.handle, n_per_block, n_blocks, 17, 298.0, out.data_ptr(), None))
+    system.set_refine(0.0)
+    got_b, _ = run(lib.pmgb_widom_noalloc, 17)
+    ref_b, _ = run(lib.pmgb_widom_device, 17)
+    np.testing.assert_allclose(got_b, ref_b, rtol=1e-12, atol=1e-9)
     assert ctx.device_status() == 0
