@@ -43,6 +43,10 @@ F_LJ, F_COUL, F_K = 28, 40, 17
 # cutoff the LJ terms 11 and the real-space terms 30 more
 F_DIST, F_LJ_IN, F_ES_IN = 26, 11, 30
 REFINE_TAIL = 1e-3
+# DRAM traffic of the config1 pair kernel, from ncu (dram__bytes_read.sum + dram__bytes_write.sum of
+# one launch over 1e5 insertions: 0.59 MB read, 0 written; profiles/pairs_kernel_config1.md),
+# per insertion; a full launch scales with the insertions it processes
+PAIR_DRAM_BYTES_PER_INSERTION = 0.59e6 / 1e5
 # kernels per Widom step: spatial order (count, scan, scatter), pairs, insertion-order partials,
 # block reduction, and the refinement's hist, cut, count, scan, scatter, FP64 energies (thread
 # and warp passes), correction
@@ -169,22 +173,32 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU legs
-def cpu_rate(sc, mol, ep, budget_s: float, seed: int = 99, poses=None, nthreads: int = 0):
-    """Insertions/s of the FP64 oracle (direct e^{ik.r} form, all host threads, or nthreads) on a
-    bounded sample of the workload's insertions."""
+def oracle_system(sc, mol, ff, ep):
+    """The FP64 oracle (the reference's algorithm restated in C) holding a workload's inputs."""
     sys.path.insert(0, str(ROOT / "oracle"))
-    import numpy as np
-
     import oracle
-    from pmgb.molecule import body_offsets
 
     species = list(dict.fromkeys(list(sc.atoms.species) + list(mol.atom_species)))
     sid = {s: i for i, s in enumerate(species)}
-    ff_eps, ff_sig2 = _tables
+    eps, sig2 = ff.tables(species)
     o = oracle.OracleSystem(sc.box.f_to_c, sc.atoms.xf, [sid[s] for s in sc.atoms.species], sc.charges.xf,
-                            sc.charges.q, ff_eps, ff_sig2, 12.5 ** 2, [sid[s] for s in mol.atom_species],
-                            mol.charge_q)
-    o.set_ewald(ep.alpha, ep.sr_cutoff_r, ep.kreps, ep.kvec_abc, ep.kvec_wt)
+                            sc.charges.q, eps, sig2, ff.r2_cutoff, [sid[s] for s in mol.atom_species], mol.charge_q)
+    if ep is not None:
+        o.set_ewald(ep.alpha, ep.sr_cutoff_r, ep.kreps, ep.kvec_abc, ep.kvec_wt)
+    return o
+
+
+def cpu_rate(sc, mol, ep, budget_s: float, seed: int = 99, nthreads: int = 0, use_sk: bool = False, ff=None):
+    """Insertions/s of the FP64 oracle (direct e^{ik.r} form unless use_sk, all host threads or
+    nthreads) on a bounded sample of the workload's insertions (random poses)."""
+    import numpy as np
+
+    import oracle
+    from pmgb import synthetic
+    from pmgb.molecule import body_offsets
+
+    o = oracle_system(sc, mol, ff or synthetic.forcefield(12.5), ep)
+    charged = ep is not None and mol.n_charges > 0
     cores = nthreads if nthreads > 0 else oracle.num_threads()
     rng = np.random.default_rng(seed)
     ax, qx = body_offsets(mol, sc.box)
@@ -193,9 +207,9 @@ def cpu_rate(sc, mol, ep, budget_s: float, seed: int = 99, poses=None, nthreads:
         xf = rng.random((n, 3))
         R = np.stack([_rot(rng) for _ in range(n)])
         lj = xf[:, None, :] + np.einsum("ij,njk,lk->nli", sc.box.c_to_f, R, ax)
-        q = xf[:, None, :] + np.einsum("ij,njk,lk->nli", sc.box.c_to_f, R, qx)
+        q = xf[:, None, :] + np.einsum("ij,njk,lk->nli", sc.box.c_to_f, R, qx) if charged else None
         t0 = time.perf_counter()
-        o.energies(lj, q, charged=True, use_sk=False, nthreads=nthreads)
+        o.energies(lj, q, charged=charged, use_sk=use_sk, nthreads=nthreads)
         return time.perf_counter() - t0
 
     # calibrate on a few insertions per thread, then sample until the time budget is spent
@@ -210,22 +224,71 @@ def cpu_rate(sc, mol, ep, budget_s: float, seed: int = 99, poses=None, nthreads:
     return total_n / total_t, cores, total_n, total_t
 
 
+def cpu_legs(sc, mol, ep, ff):
+    """The reference's algorithm on the host cores (the FP64 oracle port), beside the GPU:
+    config1 (the workload) with the direct e^{ik.r} Ewald form on all threads and on one, and with
+    the structure-factor form (the same algorithm the GPU runs, so the two config1 rates split the
+    speed-up into algorithm and hardware); config0 in full (1e5 CH4 insertions), config2 in full
+    (the 96^3 Xe grid) and a bounded sample of config4 (direct form)."""
+    import numpy as np
+
+    import oracle
+    import pmgb
+    from pmgb import synthetic
+
+    r, cores, n, dt = cpu_rate(sc, mol, ep, budget_s=15.0)
+    r1, _, n1, dt1 = cpu_rate(sc, mol, ep, budget_s=4.0, seed=98, nthreads=1)
+    rsk, _, nsk, dtsk = cpu_rate(sc, mol, ep, budget_s=5.0, seed=97, use_sk=True)
+    out = {"value": r, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"{n} insertions of the workload (random poses), FP64 direct e^(ik.r) Ewald sum + LJ "
+                     f"(the reference's algorithm), OpenMP over insertions, {dt:.1f} s",
+           "single_core": {"value": r1, "unit": UNIT, "cores": 1,
+                           "sample": f"{n1} insertions on one thread, {dt1:.1f} s"},
+           "sk_form": {"value": rsk, "unit": UNIT, "cores": cores,
+                       "sample": f"{nsk} insertions, FP64 structure-factor form of the reciprocal space (every "
+                                 f"k-vector, S(k) precomputed) + LJ + real space, {dtsk:.1f} s"}}
+    # config0 in full: CH4 (one LJ bead) in the 424-atom cubic cell, 1e5 insertions
+    c0 = synthetic.config0()
+    rep0 = pmgb.replication_factors(c0.box, ff)
+    sc0 = pmgb.replicate(c0, rep0)
+    ch4 = synthetic.ch4()
+    o0 = oracle_system(sc0, ch4, ff, None)
+    rng = np.random.default_rng(11)
+    xf = rng.random((100_000, 1, 3))
+    t0 = time.perf_counter()
+    o0.energies(xf)
+    t_c0 = time.perf_counter() - t0
+    out["config0_full"] = {"value": 1e5 / t_c0, "unit": UNIT, "cores": cores,
+                           "sample": f"all 1e5 insertions of config0 (CH4, 424 atoms, LJ), FP64, {t_c0:.2f} s"}
+    # config2 in full: Xe over the 96^3 grid of config0
+    ox = oracle_system(sc0, synthetic.xe(), ff, None)
+    t0 = time.perf_counter()
+    ox.energy_grid((96, 96, 96), rep0)
+    t_c2 = time.perf_counter() - t0
+    out["config2_full"] = {"value": 96 ** 3 / t_c2, "unit": "grid points/s", "cores": cores,
+                           "sample": f"the full 96^3 grid of config2 (Xe in config0), FP64, {t_c2:.2f} s"}
+    # config4: a bounded sample with the direct form
+    c4 = synthetic.config4()
+    sc4 = pmgb.replicate(c4, pmgb.replication_factors(c4.box, ff))
+    ep4 = pmgb.setup_Ewald_sum(sc4.box, ff.r_cutoff, eps=1e-6)
+    r4, _, n4, dt4 = cpu_rate(sc4, mol, ep4, budget_s=10.0, seed=96, ff=ff)
+    out["config4_sample"] = {"value": r4, "unit": UNIT, "cores": cores,
+                             "sample": f"{n4} insertions of config4 (CO2, 20,000 atoms, 6,974 k-vectors), FP64 direct "
+                                       f"e^(ik.r) form, {dt4:.1f} s"}
+    del oracle
+    return out
+
+
 def _rot(rng):
     import pmgb
 
     return pmgb.random_rotation_matrix(rng)
 
 
-_tables = None
-
-
 def reference_arm(args, rank, world):
-    global _tables
     if rank != 0:
         return
     cr, sc, ff, ep, mol, rep = workload()
-    species = list(dict.fromkeys(list(sc.atoms.species) + list(mol.atom_species)))
-    _tables = ff.tables(species)
     for _ in range(args.warmup):
         cpu_rate(sc, mol, ep, budget_s=1.0)
     rates, times, ns = [], [], []
@@ -351,8 +414,129 @@ def batched_leg(args, ctx, stream):
     return out
 
 
+# ------------------------------------------------------------------ error against the FP64 oracle
+def widom_error(gs, ff, n_per_block: int, seed: int):
+    """A Widom run of gs (its refinement setting) against the FP64 oracle (structure-factor form)
+    on the exact device poses: the largest relative error of a block's K_H (sum of e^{-U/T}) and of
+    its <U>, and the fraction of insertions whose energy is within 1e-5 relative or 1e-4 K."""
+    import numpy as np
+
+    from pmgb.molecule import body_offsets
+
+    blocks, u = gs.widom(n_per_block, N_BLOCKS, seed, T, want_energies=True)
+    xf, rot = gs.ctx.sample_poses(seed, 0, N_BLOCKS * n_per_block)
+    body = np.zeros((gs.n_sites, 3))
+    ax, qx = body_offsets(gs.molecule, gs.crystal.box)
+    for k in range(gs.n_sites):
+        body[k] = ax[gs.site_atom[k]] if gs.site_atom[k] >= 0 else qx[gs.site_charge[k]]
+    o = oracle_system(gs.crystal, gs.molecule, ff, gs.eparams)
+    sites = o.sites_from_poses(xf.astype(np.float64), rot.astype(np.float64), body)
+    n = sites.shape[0]
+    lj = np.zeros((n, gs.molecule.n_atoms, 3))
+    q = np.zeros((n, gs.molecule.n_charges, 3))
+    for k in range(gs.n_sites):
+        if gs.site_atom[k] >= 0:
+            lj[:, gs.site_atom[k]] = sites[:, k]
+        if gs.site_charge[k] >= 0:
+            q[:, gs.site_charge[k]] = sites[:, k]
+    v, sr, lr = o.energies(lj, q, charged=gs.charged, use_sk=True)
+    u_ref = v + sr + lr
+    ug = u.sum(axis=1)
+    both_inf = np.isinf(ug) & np.isinf(u_ref)
+    ok = both_inf | (np.abs(ug - u_ref) <= np.maximum(1e-5 * np.abs(u_ref), 1e-4))
+    x = np.where(np.isfinite(u_ref), -u_ref / T, -np.inf).reshape(N_BLOCKS, n_per_block)
+    m = x.max(axis=1, keepdims=True)
+    w = np.exp(x - m)
+    log_ref = m[:, 0] + np.log(w.sum(axis=1))
+    u_mean = (np.where(np.isfinite(u_ref), u_ref, 0.0).reshape(N_BLOCKS, -1) * w).sum(axis=1) / w.sum(axis=1)
+    kh_rel = np.abs(np.expm1(blocks[:, 0] - log_ref))
+    u_rel = np.abs(blocks[:, 1] + blocks[:, 2] - u_mean) / np.abs(u_mean)
+    return {"insertions": n, "kh_max_rel_error": float(kh_rel.max()), "u_mean_max_rel_error": float(u_rel.max()),
+            "insertion_energies_within_tolerance": float(ok.mean()),
+            "oracle": "FP64 structure-factor form of the reference's algorithm on the device's own poses"}
+
+
+def grid_error(gs, ff, n_pts, rep, grid, n_sample: int = 20000, seed: int = 3):
+    """Grid values (K) at a random sample of points against the FP64 oracle: the largest relative
+    error and the fraction within 1e-5 relative or 1e-4 K."""
+    import numpy as np
+
+    o = oracle_system(gs.crystal, gs.molecule, ff, None)
+    rng = np.random.default_rng(seed)
+    idx = rng.integers(0, int(np.prod(n_pts)), n_sample)
+    i, j, k = idx % n_pts[0], (idx // n_pts[0]) % n_pts[1], idx // (n_pts[0] * n_pts[1])
+    f = [np.where(a / (n - 1) >= 1.0, 0.0, a / (n - 1)) / r for a, n, r in zip((i, j, k), n_pts, rep)]
+    pts = np.stack(f, axis=1)[:, None, :]
+    ref = o.energies(pts)[0]
+    got = grid[i, j, k].astype(np.float64)
+    fin = np.isfinite(ref)
+    ok = (np.isinf(got) & ~fin) | (np.abs(got - ref) <= np.maximum(1e-5 * np.abs(ref), 1e-4))
+    rel = np.abs(got[fin] - ref[fin]) / np.maximum(np.abs(ref[fin]), 1e-300)
+    return {"points_checked": n_sample, "within_tolerance": float(ok.mean()), "max_rel_error": float(rel.max())}
+
+
+# ------------------------------------------------------------------ porous cell
+def porous_leg(args, ctx, stream, flush):
+    """The bench workload's guest and Ewald set-up in a porous variant of the config1 cell (the
+    same lattice and species mix at a quarter of the atoms; synthetic.config1_porous), where the
+    Boltzmann weight spreads over many insertions: the refined pass with its refined count and the
+    refinement's share of the step, and the FP32 pass alone.  CUDA events on the launching stream,
+    L2 flushed before every timed step."""
+    import torch
+
+    import pmgb
+    from pmgb import synthetic
+
+    cr = synthetic.config1_porous()
+    ff = synthetic.forcefield(12.5)
+    sc = pmgb.replicate(cr, pmgb.replication_factors(cr.box, ff))
+    ep = pmgb.setup_Ewald_sum(sc.box, ff.r_cutoff, eps=1e-6)
+    gs = pmgb.GPUSystem(sc, pmgb.Frac(synthetic.co2(), sc.box), ff, ep, ctx=ctx, refine_tail=REFINE_TAIL)
+    npb = args.insertions // N_BLOCKS
+    n = npb * N_BLOCKS
+    dev = torch.device("cuda", torch.cuda.current_device())
+    block_out = torch.zeros(N_BLOCKS * 4, dtype=torch.float64, device=dev)
+    lib = ctx._lib
+
+    def run(seed0, k):
+        for w in range(2):
+            ctx.check(lib.pmgb_widom_device(gs.handle, npb, N_BLOCKS, seed0 + 100 + w, T, block_out.data_ptr(), None))
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+        refined = []
+        ctx.set_kernel_timing(True)
+        for i in range(k):
+            flush.zero_()
+            ev[i][0].record(stream)
+            ctx.check(lib.pmgb_widom_device(gs.handle, npb, N_BLOCKS, seed0 + i, T, block_out.data_ptr(), None))
+            ev[i][1].record(stream)
+            refined.append(gs.refined_count())
+        torch.cuda.synchronize()
+        k_ms, k_n = ctx.kernel_timing()
+        ctx.set_kernel_timing(False)
+        return sum(a.elapsed_time(b) for a, b in ev) / k, k_ms / max(k_n, 1), refined
+
+    k = max(3, min(args.steps, 10))
+    ms_ref, kern_ref, refined = run(5000, k)
+    err = widom_error(gs, ff, 20000, 5099)
+    gs.set_refine(0.0)
+    ms32, kern32, _ = run(6000, k)
+    assert ctx.device_status() == 0
+    return {"workload": "CO2 + Ewald 1e-6 in the porous config1 cell (150 atoms per 13.2 x 18.9 x 9.8 A cell, "
+                        "replicated 2x2x3), 1e6 insertions in 5 blocks, 298 K",
+            "framework_sites": sc.atoms.n, "insertions": n,
+            "insertions_per_s": n / (ms_ref * 1e-3), "ms_per_step": ms_ref,
+            "refined_per_step": {"mean": sum(refined) / len(refined), "max": max(refined)},
+            "pair_kernel_ms": kern_ref, "refinement_share_of_step": 1.0 - kern_ref / ms_ref,
+            "fp32_only_insertions_per_s": n / (ms32 * 1e-3), "fp32_only_ms_per_step": ms32,
+            "error_vs_fp64_oracle": err,
+            "note": "refined steps: the pair kernel without the box-matrix residual, then the FP64 re-evaluation "
+                    "of the insertions that carry all but 1e-3 of each block's Boltzmann weight (K_H within 1e-6); "
+                    "refinement_share_of_step = 1 - pair-kernel time / step time (the spatial order, partials and "
+                    "block reduction, ~2% of a step, count with the refinement)"}
+
+
 # ------------------------------------------------------------------ the other configurations
-def other_configs(args, ctx, stream):
+def other_configs(args, ctx, stream, peak=None):
     """The large Ewald cell (config4) and the energy grid (config2), one timed pass each after a
     warm-up, CUDA events on the launching stream.
 
@@ -361,6 +545,8 @@ def other_configs(args, ctx, stream):
       refinement, forward FP32 only, and forward + adjoint.
     config2: Xe over a 96^3 fractional grid of config0's framework (FP32 output), and the grid
       adjoint (dU/dr per point and dK_H/d(eps, sigma^2)) at 298 K."""
+    import ctypes as C
+
     import torch
 
     import pmgb
@@ -393,6 +579,8 @@ def other_configs(args, ctx, stream):
     gs.set_refine(0.0)
     ms32 = timed(lambda: gs.widom(npb, N_BLOCKS, 42, T))
     ms_adj = timed(lambda: gs.widom_adjoint(npb, N_BLOCKS, 43, T))
+    gs.set_refine(REFINE_TAIL)
+    err4 = widom_error(gs, ff, 4000, 44)
     fpi = flops_per_insertion(sc, mol, ep)
     out["config4_large_ewald"] = {
         "workload": "CO2 in a 20,000-atom 52x52x52 A cell, Ewald 1e-6", "framework_sites": sc.atoms.n,
@@ -408,6 +596,7 @@ def other_configs(args, ctx, stream):
                 "energy terms of most remaining groups, so that figure exceeds the FP32 peak; "
                 "fp32_only_tflops_inside_cutoff counts distances of all pairs and energy terms inside the cutoff, "
                 "so it too credits the skipped distances",
+        "error_vs_fp64_oracle": err4,
         "centre_image": gs.info()["centre_image"],
         "distances": "with centre_image, each record's minimum image is taken from the pose centre once and the "
                      "three sites subtract their offsets (every width of this cell exceeds 2 (cutoff + 1.16 A); "
@@ -443,12 +632,46 @@ def other_configs(args, ctx, stream):
     gx = pmgb.GPUSystem(sc0, pmgb.Frac(synthetic.xe(), sc0.box), ff, ctx=ctx)
     pts = (96, 96, 96)
     n_pts = 96 ** 3
-    ms_g = timed(lambda: gx.energy_grid(pts, rep, 1.0), reps=20, warm=3)  # sub-millisecond calls
+    dev = torch.device("cuda", torch.cuda.current_device())
+    grid_dev = torch.empty(n_pts, dtype=torch.float32, device=dev)
+    n3 = (C.c_int32 * 3)(*pts)
+    r3 = (C.c_int32 * 3)(*rep)
+
+    def grid_device():
+        ctx.check(ctx._lib.pmgb_energy_grid_device(gx.handle, n3, r3, 1.0, grid_dev.data_ptr()))
+
+    ms_exact = timed(grid_device, reps=20, warm=3)      # FP32 pass with error estimates + re-evaluation
+    refined = gx.refined_count()
+    grid_exact = gx.energy_grid(pts, rep, 1.0)
+    ms_g = timed(lambda: gx.energy_grid(pts, rep, 1.0), reps=20, warm=3)
     ms_ga = timed(lambda: gx.energy_grid_adjoint(pts, rep, 1.0, T), reps=10, warm=3)
+    gx.set_exact(False)
+    ms_fp32 = timed(grid_device, reps=20, warm=3)       # the FP32 grid kernel alone
+    grid_fp32 = gx.energy_grid(pts, rep, 1.0)
+    gx.set_exact(True)
+    # counted work of the FP32 grid kernel: the distance of every (record, probe) pair and the LJ terms
+    # of the pairs inside the cutoff (n 4/3 pi rc^3 / V per point); no sub-chunk of this cell is skipped
+    fpp = F_DIST * sc0.atoms.n + F_LJ_IN * sc0.atoms.n * (4.0 / 3.0 * math.pi * ff.r_cutoff ** 3 / sc0.box.Omega)
+    tf = fpp * n_pts / (ms_fp32 * 1e-3) / 1e12
     out["config2_energy_grid"] = {
         "workload": "Xe over a 96^3 grid of config0 (424 atoms, 25.832 A cubic)", "points": n_pts,
-        "points_per_s": n_pts / (ms_g * 1e-3), "adjoint_points_per_s": n_pts / (ms_ga * 1e-3),
-        "timing": "host call including the device-to-host copy of the grid (and gradients)"}
+        "points_per_s": n_pts / (ms_exact * 1e-3),
+        "exact": "every point within 1e-5 relative or 1e-4 K of FP64: the FP32 pass with a per-point error "
+                 "estimate, then the points it cannot clear re-evaluated in double-float",
+        "refined_points": refined, "refined_fraction": refined / n_pts,
+        "fp32_only_points_per_s": n_pts / (ms_fp32 * 1e-3),
+        "host_call_points_per_s": n_pts / (ms_g * 1e-3), "adjoint_points_per_s": n_pts / (ms_ga * 1e-3),
+        "roofline": {"bound": "fp32", "flops_per_point": fpp, "achieved": tf, "unit": "TFLOP/s",
+                     "frac": tf / peak if peak else None,
+                     "kernel": "pairs_kernel<1,false,...> (FP32 grid, exact energies off), CUDA events around "
+                               "pmgb_energy_grid_device",
+                     "counting": "distance of every (record, probe) pair 26 flops, LJ 11 more per pair inside the "
+                                 "cutoff (FMA = 2, MUFU = 1)"},
+        "error_vs_fp64_oracle": {"exact": grid_error(gx, ff, pts, rep, grid_exact),
+                                 "fp32_only": grid_error(gx, ff, pts, rep, grid_fp32)},
+        "timing": "points_per_s and fp32_only: CUDA events around the device call (grid left on the device); "
+                  "host_call and adjoint: the host call including the device-to-host copy of the grid (and "
+                  "gradients)"}
     assert ctx.device_status() == 0
     return out
 
@@ -468,7 +691,6 @@ def job_rate(ms_total: float, n_per_rank_step: int, steps: int, world: int, devi
 
 # ------------------------------------------------------------------ GPU arm
 def ours(args, rank, world, local_rank):
-    global _tables
     import numpy as np
     import torch
 
@@ -477,8 +699,6 @@ def ours(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     cr, sc, ff, ep, mol, rep = workload()
-    species = list(dict.fromkeys(list(sc.atoms.species) + list(mol.atom_species)))
-    _tables = ff.tables(species)
     ctx = pmgb.Context(local_rank)
     stream = torch.cuda.Stream(dev)          # a real (non-legacy) stream shared with the library
     torch.cuda.set_stream(stream)
@@ -495,7 +715,12 @@ def ours(args, rank, world, local_rank):
     def step(seed):
         ctx.check(lib.pmgb_widom_device(system.handle, npb, N_BLOCKS, seed, T, block_out.data_ptr(), None))
 
-    fp32_peak = ctx.fp32_peak_tflops() if rank == 0 else None
+    fp32_peak, peak_clocks = None, None
+    if rank == 0:
+        # the roofline denominator: the FFMA probe, best of three, with the SM clock it ran at
+        with ClockSampler(local_rank) as pclk:
+            fp32_peak = max(ctx.fp32_peak_tflops() for _ in range(3))
+        peak_clocks = pclk.summary()
     for w in range(args.warmup):
         step(10_000 + w)
     torch.cuda.synchronize()
@@ -538,6 +763,7 @@ def ours(args, rank, world, local_rank):
     torch.cuda.synchronize()
     ms32 = sum(a.elapsed_time(b) for a, b in ev32) / args.steps
     system.set_refine(REFINE_TAIL)
+    err1 = widom_error(system, ff, 4000, 77) if rank == 0 else None
 
     # forward + adjoint in one pass (pmgb_widom_adjoint: energies, dK_H/d(eps, sigma, lambda))
     adj = None
@@ -583,25 +809,42 @@ def ours(args, rank, world, local_rank):
         batched = batched_leg(args, ctx, stream)
     others = None
     if not args.skip_configs and rank == 0:
-        others = other_configs(args, ctx, stream)
+        others = other_configs(args, ctx, stream, fp32_peak)
+
+    porous = None
+    if not args.skip_configs and rank == 0:
+        porous = porous_leg(args, ctx, stream, flush)
 
     if rank != 0:
         return
     fpi = flops_per_insertion(sc, mol, ep)
-    achieved = fpi * n_ins / (kernel_ms * 1e-3) / 1e12
+    achieved_every = fpi * n_ins / (kernel_ms * 1e-3) / 1e12
     fpi_in = flops_inside_cutoff(sc, mol, ff, ep, system.info()["n_kvecs_evaluated"])
+    achieved = fpi_in * n_ins / (kernel_ms * 1e-3) / 1e12
     cpu = None
     if not args.skip_cpu:
-        r, cores, n, dt = cpu_rate(sc, mol, ep, budget_s=15.0)
-        r1, _, n1, dt1 = cpu_rate(sc, mol, ep, budget_s=4.0, seed=98, nthreads=1)
-        cpu = {"value": r, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{n} insertions of the workload (random poses), FP64 direct e^(ik.r) Ewald sum + LJ "
-                         f"(the reference's algorithm), OpenMP over insertions, {dt:.1f} s",
-               "single_core": {"value": r1, "unit": UNIT, "cores": 1,
-                               "sample": f"{n1} insertions on one thread, {dt1:.1f} s"}}
+        cpu = cpu_legs(sc, mol, ep, ff)
+    summary = {"kh_max_rel_error": err1["kh_max_rel_error"] if err1 else None,
+               "pair_kernel_frac_of_fp32_peak": achieved / fp32_peak if fp32_peak else None,
+               "e2e_insertions_per_s": e2e["value"] if e2e else None,
+               "cpu_direct_insertions_per_s": cpu["value"] if cpu else None,
+               "cpu_sk_form_insertions_per_s": cpu["sk_form"]["value"] if cpu else None}
+    if porous:
+        summary.update({"porous_insertions_per_s": porous["insertions_per_s"],
+                        "porous_refinement_share": porous["refinement_share_of_step"],
+                        "porous_kh_max_rel_error": porous["error_vs_fp64_oracle"]["kh_max_rel_error"]})
+    if batched:
+        fa = batched["forward_plus_adjoint"]
+        summary.update({"batched_fwd_adj_insertions_per_s": fa["batched_insertions_per_s"],
+                        "batched_vs_plain_prebuilt": fa["speedup_vs_plain"],
+                        "batched_vs_plain_with_setup": fa.get("speedup_with_setup_both_sides"),
+                        "batched_refined_fraction": batched.get("refined_fraction")})
+    if others:
+        summary.update({"config4_insertions_per_s": others["config4_large_ewald"]["insertions_per_s"],
+                        "config2_points_per_s": others["config2_energy_grid"]["points_per_s"]})
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic", "summary": summary,
            "config": {"workload": "widom_co2_ewald_600atom_triclinic_2x2x3_1e6",
                       "insertions_per_step": n_ins, "framework_sites": sc.atoms.n, "kvectors": ep.n_kvecs,
                       "guest": "CO2 (3 LJ sites, 3 charges)", "temperature_K": T, "blocks": N_BLOCKS,
@@ -612,33 +855,40 @@ def ours(args, rank, world, local_rank):
                          "refine_tail": REFINE_TAIL,
                          "kh_error": "insertions carrying all but 1e-3 of each block's Boltzmann weight "
                                      "re-evaluated in FP64 from exact positions: K_H within 1e-6 relative of "
-                                     "the FP64 oracle (tests/test_gpu_refine.py, this framework: ~5e-10)",
+                                     "the FP64 oracle",
+                         "error_vs_fp64_oracle": err1,
                          "fp32_only_insertions_per_s": n_ins / (ms32 * 1e-3),
                          "fp32_only_ms_per_step": ms32,
                          "fp32_only": "refinement off: the pair kernel keeps the box-matrix residual (the "
                                       "refined steps drop it, their FP64 pass re-evaluates the insertions "
                                       "that matter)"},
            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                        "frac": achieved / fp32_peak if fp32_peak else None, "traffic": None,
-                        "peak_source": "in-run FFMA probe (pmgb_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
-                        "flops_per_insertion": fpi,
-                        "convention": "every pair counted: LJ 28, real-space 40, k-term 17 flops (FMA=2, MUFU=1, "
-                                      "erfc=10); with cutoff culling the kernel skips the energy terms of records "
-                                      "outside every lane's cutoff, and it skips the k-vectors whose S(k) vanishes "
-                                      "on the replicated cell, so this credits skipped work",
-                        "inside_cutoff": {"flops_per_insertion": fpi_in,
-                                          "achieved": fpi_in * n_ins / (kernel_ms * 1e-3) / 1e12,
-                                          "frac": (fpi_in * n_ins / (kernel_ms * 1e-3) / 1e12) / fp32_peak
-                                          if fp32_peak else None,
-                                          "counting": "distance of every pair 26, LJ 11 and real-space 30 "
-                                                      "more per pair inside the cutoff (n 4/3 pi rc^3 / V per "
-                                                      "insertion), k-term 17 per evaluated k-vector",
-                                          "kvectors_evaluated": system.info()["n_kvecs_evaluated"]},
+                        "frac": achieved / fp32_peak if fp32_peak else None,
+                        "traffic": PAIR_DRAM_BYTES_PER_INSERTION * n_ins,
+                        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one pair-kernel "
+                                          "launch over 1e5 insertions (0.59 MB), scaled to this launch's insertions "
+                                          "(profiles/pairs_kernel_config1.md); the framework lives in shared "
+                                          "memory and L2, so the kernel is compute-bound",
+                        "peak_source": "in-run FFMA probe (pmgb_fp32_peak, best of 3); MEASURED_PEAKS.json has no "
+                                       "FP32 figure",
+                        "peak_clocks": peak_clocks,
+                        "flops_per_insertion": fpi_in,
+                        "counting": "the work the kernel does: the minimum-image distance of every (record, guest "
+                                    "site) pair 26 flops (no sub-chunk of this cell is skipped), LJ 11 and "
+                                    "real-space 30 more per pair inside the cutoff (n 4/3 pi rc^3 / V per "
+                                    "insertion), 17 per (evaluated k-vector, guest charge); FMA = 2, MUFU = 1",
+                        "kvectors_evaluated": system.info()["n_kvecs_evaluated"],
+                        "every_pair": {"flops_per_insertion": fpi, "achieved": achieved_every,
+                                       "frac": achieved_every / fp32_peak if fp32_peak else None,
+                                       "convention": "every pair and every k-vector counted: LJ 28, real-space 40, "
+                                                     "k-term 17 flops; credits the energy terms culling skips and "
+                                                     "the k-vectors whose S(k) vanishes"},
                         "kernel": "pairs_kernel<3,true,false,false> (CO2, Ewald, forward, no box residual): "
                                   "CUDA events around each of its launches inside the timed refined steps, "
                                   "on the launching stream",
                         "kernel_ms_per_launch": kernel_ms, "kernel_share_of_step": kernel_ms * args.steps / ms_total},
            "forward_plus_adjoint": adj,
+           "porous_cell": porous,
            "batched": batched,
            "other_configs": others,
            "clocks": clk.summary(),

@@ -123,8 +123,20 @@ int pmgb_structure_factor(pmgb_system* sys, double* sk_out);
  * (n_conf x n_sites x 3), out[3*i..3*i+2] = (U_vdw, U_es short-range, U_es long-range) in K.
  * Replaces vdw_energy(crystal, molecule, ljff) (src/vdw_energetics.jl:62-64 -> 25-47;
  * +Inf on overlap) and electrostatic_potential_energy(crystal, molecule, eparams, eikr)
- * (src/electrostatics.jl:331-342 -> _ϕ :347-388; the EwaldSum sr and lr parts). */
+ * (src/electrostatics.jl:331-342 -> _ϕ :347-388; the EwaldSum sr and lr parts).
+ * With exact energies (pmgb_system_set_exact, the default) every configuration is evaluated in
+ * double-float (~48-bit) arithmetic from its FP64 coordinates: within ~1e-10 relative of the
+ * FP64 reference.  Off: the FP32 pair pass, within ~4e-6 of the sum of the terms' magnitudes. */
 int pmgb_energies(pmgb_system* sys, int64_t n_conf, const double* site_xf, double* out);
+
+/* Exact single-configuration energies for this system (default on): pmgb_energies,
+ * pmgb_energies_grad (energies; gradients stay FP32), pmgb_move_* (handles created while on)
+ * and the energy grids meet the reference's FP64 values to 1e-5 relative or 1e-4 K for every
+ * configuration and grid point.  Grids run the FP32 pass with a per-point estimate of its
+ * rounding error and re-evaluate in double-float the points whose estimate exceeds that
+ * tolerance (or that have a pair within rounding of the cutoff or the overlap distance).
+ * 0 switches it off (FP32 only).  No reference counterpart: the reference is FP64 throughout. */
+int pmgb_system_set_exact(pmgb_system* sys, int32_t on);
 
 /* ---- Widom insertions ----------------------------------------------------------------
  * Replaces the pmap over N_BLOCKS blocks of _conduct_Widom_insertions
@@ -176,7 +188,9 @@ int pmgb_system_set_centre_image(pmgb_system* sys, int32_t on);
  * guest with several sites, and every width wide enough for the current cutoffs), else 0. */
 int pmgb_system_centre_image(const pmgb_system* sys, int32_t* on_out);
 
-/* Number of insertions the last refined Widom run re-evaluated in FP64 (synchronises). */
+/* Number of items the system's last double-float pass re-evaluated (synchronises): insertions of
+ * the last refined Widom run, configurations of the last exact pmgb_energies call, or points of
+ * the last exact energy grid. */
 int pmgb_system_refined_count(pmgb_system* sys, int64_t* count_out);
 
 /* Same computation on device-resident outputs, enqueued on the context stream without
@@ -230,16 +244,17 @@ int pmgb_widom_adjoint(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, 
  * The guest-host part of the energy a GCMC move needs (src/gcmc.jl:111-124 -> vdw_energy,
  * src/vdw_energetics.jl:62-64; plus the Ewald terms when the system is charged), as
  * pmgb_energies computes it, through a CUDA graph captured once: pinned staging, copy in,
- * one CTA per configuration with the framework split over its threads, copy out.  A handle
- * serves 1..max_conf configurations per call; calls are synchronous.  pmgb_energies itself
- * switches to the same kernel for up to 64 configurations. */
+ * one CTA per configuration with the framework split over its threads (FP32), or the
+ * double-float pass when the system had exact energies on at creation, copy out.  A handle
+ * serves 1..max_conf configurations per call; calls are synchronous. */
 typedef struct pmgb_move pmgb_move;
 int pmgb_move_create(pmgb_system* sys, int32_t max_conf, pmgb_move** out);
 int pmgb_move_energies(pmgb_move* move, int32_t n_conf, const double* site_xf, double* out);
 void pmgb_move_destroy(pmgb_move* move);
 
 /* pmgb_energies plus dU/dx of the configuration's reference point (all sites moved rigidly;
- * grad_out: n_conf x 3 floats, K/Å). */
+ * grad_out: n_conf x 3 floats, K/Å).  The energies follow pmgb_system_set_exact; the
+ * gradients come from the FP32 pass. */
 int pmgb_energies_grad(pmgb_system* sys, int64_t n_conf, const double* site_xf, double* out,
                        float* grad_out);
 
@@ -247,16 +262,33 @@ int pmgb_energies_grad(pmgb_system* sys, int64_t n_conf, const double* site_xf, 
  * Replaces energy_grid(crystal, molecule, ljff; resolution=(n1,n2,n3)) for single-site
  * probes (src/grid.jl:291-362): point (i,j,k) sits at (i/(n1-1), j/(n2-1), k/(n3-1)) of
  * the unit cell, i.e. that divided by repfactors in the supercell this system holds;
- * out[i + n1*(j + n2*k)] = U_vdw * unit_factor (1 for K, 8.314/1000 for kJ/mol). */
+ * out[i + n1*(j + n2*k)] = U_vdw * unit_factor (1 for K, 8.314/1000 for kJ/mol), rounded to
+ * FP32; with exact energies (pmgb_system_set_exact) every value meets the FP64 reference to
+ * 1e-5 relative or 1e-4 K before that rounding. */
 int pmgb_energy_grid(pmgb_system* sys, const int32_t n_pts[3], const int32_t repfactors[3],
                      double unit_factor, float* out);
 int pmgb_energy_grid_device(pmgb_system* sys, const int32_t n_pts[3], const int32_t repfactors[3],
                             double unit_factor, float* out_dev);
 
+/* Rotational energy grid: energy_grid's branch for probes that need rotations (several sites
+ * or charges; src/grid.jl:338-351).  At each point (placed as in pmgb_energy_grid) the probe's
+ * centre of mass takes n_rotations uniform random orientations -- orientation r of point p
+ * from Philox4x32-10 keyed by seed at counter p * n_rotations + r, as pmgb_sample_poses draws
+ * them -- and out[p] = -T log(Σ_r e^{-U_r/T} / n_rotations) * unit_factor, with U = U_vdw plus
+ * the Ewald energy when crystal and probe are charged (+Inf where every orientation overlaps).
+ * With exact energies (pmgb_system_set_exact) or tail refinement on, the orientations that carry
+ * all but 1e-3 (or the system's refinement fraction) of each point's Boltzmann weight are
+ * re-evaluated in FP64.  The reference's own branch passes a Frac molecule to the one-argument
+ * random_rotation!, which its v0.4.2 does not define (src/molecule.jl:269 takes a box). */
+int pmgb_energy_grid_rotational(pmgb_system* sys, const int32_t n_pts[3], const int32_t repfactors[3],
+                                int32_t n_rotations, double temperature, uint64_t seed, double unit_factor,
+                                float* out);
+
 /* Energy grid plus its adjoint: grad_out (optional, 3 floats per point) = dU/dr at each point
  * (K/Å, Cartesian), and dtheta as for pmgb_widom_adjoint with the grid points as the samples
  * (w_p = exp(-U_p/T - M), M = max_p -U_p/T): the grid estimate
- * K_H,grid = Σ_p e^{-U_p/T} / (R T n_points) has dK/dθ = -e^M Σ_p w_p ∂U_p/∂θ / (T R T n_points). */
+ * K_H,grid = Σ_p e^{-U_p/T} / (R T n_points) has dK/dθ = -e^M Σ_p w_p ∂U_p/∂θ / (T R T n_points).
+ * The grid values follow pmgb_system_set_exact; the weights and gradients use the FP32 pass. */
 int pmgb_energy_grid_adjoint(pmgb_system* sys, const int32_t n_pts[3], const int32_t repfactors[3],
                              double unit_factor, double temperature, float* out, float* grad_out,
                              double* dtheta);

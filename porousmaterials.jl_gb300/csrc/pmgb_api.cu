@@ -98,13 +98,16 @@ struct pmgb_system {
     double refine_tail = 0.0;       // FP64 refinement of the Boltzmann tail (0: off)
     bool cull = true;               // spatially ordered processing with cutoff culling
     bool centre_image = true;       // centre-image distances where the geometry allows them
+    bool exact = true;              // single-configuration energies and grids to the FP64 tolerance
+    double bound_kappa = 1.0;       // rounding condition of the box (scales the FP32 error estimate)
     DevBuf o_counts, o_perm;        // Widom processing order scratch
     DevBuf acc;                     // accessibility grid (uint8, i fastest)
-    int last_refine_ctas = 0;       // chunks of the last refined run (its refined count sits after them)
+    int last_refined_slot = -1;     // r_offsets entry holding the last double-float pass's count (-1: none)
     // grow-only scratch used by launches
     DevBuf r_hist, r_cut, r_counts, r_offsets, r_list, r_ref, r_plan, r_done, r_part;  // refinement scratch
     DevBuf partials, block_out, in_buf, out_buf, axes;
     DevBuf g_u, g_dsum, g_grad, g_part, g_cols;  // adjoint scratch
+    DevBuf x64, e_bound;            // exact energies: FP64 site coordinates, grid error estimates
 };
 
 namespace {
@@ -431,7 +434,7 @@ static void free_system_device(pmgb_system* s) {
                     s->g_part.p,   s->g_cols.p,   s->r_hist.p,  s->r_cut.p,  s->r_counts.p, s->r_offsets.p,
                     s->r_list.p,   s->r_ref.p,    s->o_counts.p, s->o_perm.p,  s->r_plan.p,  s->r_done.p,
                     s->r_part.p,   s->acc.p,      s->d_cbox,    s->d_es,     s->d_es_df,  s->d_rec_rq,
-                    s->d_rec_qlo,  s->d_segpar_df, s->d_tk_df};
+                    s->d_rec_qlo,  s->d_segpar_df, s->d_tk_df, s->x64.p,  s->e_bound.p};
     for (void* p : ptrs) dev_free(s->ctx, p);
 }
 
@@ -829,6 +832,15 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
         D.g64[i] = G[up[i]];
         D.h_df[i] = to_df(R[up[i]] * fix_unit);
     }
+    // rounding condition of the box, || |R| |R^-1| ||_inf (1 for an orthorhombic cell): how much
+    // the FP32 Cartesian conversion of a fractional displacement can amplify its roundings
+    s->bound_kappa = 1.0;
+    for (int i = 0; i < 3; ++i) {
+        double row = 0.0;
+        for (int j = 0; j < 3; ++j)
+            for (int m = 0; m < 3; ++m) row += std::fabs(R[i + 3 * m]) * std::fabs(G[m + 3 * j]);
+        s->bound_kappa = std::max(s->bound_kappa, row);
+    }
     D.rec_rq = s->d_rec_rq;
     D.rec_qlo = s->d_rec_qlo;
     D.segpar_df = s->d_segpar_df;
@@ -1184,6 +1196,75 @@ static LaunchArgs base_args(pmgb_system* s) {
     return a;
 }
 
+static int sm_count(pmgb_ctx* ctx) {
+    int n_sm = 0;
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device);
+    return std::max(1, n_sm);
+}
+
+// Chunk-items the double-float pass may need for n entries of this system: at most 4096 while
+// the entries are cut finely, else n times the coarse chunk count (the refinement's rule).
+static long long exact_items(const pmgb_system* s, int64_t n) {
+    const long long work = static_cast<long long>(s->n_sites) * (s->dev.n_rec + (s->dev.charged ? s->dev.n_k : 0));
+    const long long coarse = std::max(1ll, std::min(64ll, (work + 16383) / 16384));
+    return std::max<long long>(4096, static_cast<long long>(n) * coarse);
+}
+
+// Refinement arguments and scratch for a double-float pass over up to n entries with n_screen
+// screen chunks (0: every entry): entry list, screen counts and offsets (then the work counter),
+// plan, per-entry chunk counts and chunk partials, from the system's grow-only buffers.
+static int exact_args(pmgb_system* s, int64_t n, int n_screen, RefineArgs& r) {
+    pmgb_ctx* ctx = s->ctx;
+    const long long items = exact_items(s, n);
+    int rc;
+    if ((rc = ensure(ctx, s->r_list, sizeof(long long) * n)) ||
+        (rc = ensure(ctx, s->r_counts, sizeof(int) * std::max(1, n_screen))) ||
+        (rc = ensure(ctx, s->r_offsets, sizeof(int) * (n_screen + 2))) || (rc = ensure(ctx, s->r_plan, sizeof(int) * 4)) ||
+        (rc = ensure(ctx, s->r_done, sizeof(int) * n)) || (rc = ensure(ctx, s->r_part, sizeof(double) * 4 * items)))
+        return rc;
+    r = RefineArgs{};
+    r.sys = s->dev;
+    r.n_systems = 1;
+    r.n_blocks = 1;
+    r.counts = static_cast<int*>(s->r_counts.p);
+    r.offsets = static_cast<int*>(s->r_offsets.p);
+    r.list = static_cast<long long*>(s->r_list.p);
+    r.counter = r.offsets + n_screen + 1;
+    r.plan = static_cast<int*>(s->r_plan.p);
+    r.one_chunk = r.plan + 2;
+    r.done = static_cast<int*>(s->r_done.p);
+    r.part = static_cast<double*>(s->r_part.p);
+    r.cap_items = items;
+    r.cap_entries = n;
+    s->last_refined_slot = n_screen;
+    return PMGB_OK;
+}
+
+// Upload explicit site coordinates in FP64, each wrapped into [0, 1) (a whole-cell shift: the
+// same minimum images), for the double-float pass.
+static int upload_sites64(pmgb_system* s, size_t n_coord, const double* site_xf) {
+    pmgb_ctx* ctx = s->ctx;
+    std::vector<double> x(n_coord);
+    for (size_t i = 0; i < n_coord; ++i) x[i] = wrap01(site_xf[i]);
+    if (int rc = ensure(ctx, s->x64, sizeof(double) * n_coord)) return rc;
+    PMGB_CK(ctx, cudaMemcpyAsync(s->x64.p, x.data(), sizeof(double) * n_coord, cudaMemcpyHostToDevice, ctx->stream));
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // the staging vector is released on return
+    return PMGB_OK;
+}
+
+// Enqueue double-float energies of n_conf configurations (coordinates in s->x64) into e_out_dev
+// as (U_vdw, U_es short-range, U_es long-range).
+static int exact_energies(pmgb_system* s, int64_t n_conf, double* e_out_dev) {
+    pmgb_ctx* ctx = s->ctx;
+    RefineArgs r;
+    if (int rc = exact_args(s, n_conf, 0, r)) return rc;
+    r.pose_src = REFINE_POSE_SITES;
+    r.site_xf = static_cast<const double*>(s->x64.p);
+    r.ref_u = e_out_dev;
+    PMGB_CK(ctx, pmgb_launch_exact(r, n_conf, nullptr, sm_count(ctx), ctx->stream));
+    return PMGB_OK;
+}
+
 extern "C" int pmgb_energies(pmgb_system* s, int64_t n_conf, const double* site_xf, double* out) {
     if (!s) return PMGB_ERR_INVALID_ARGUMENT;
     pmgb_ctx* ctx = s->ctx;
@@ -1191,13 +1272,24 @@ extern "C" int pmgb_energies(pmgb_system* s, int64_t n_conf, const double* site_
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energies: bad arguments");
     if (int rc = ready_for_charges(s)) return rc;
     if (n_conf == 0) return PMGB_OK;
-    if (n_conf > (int64_t(1) << 31) * PMGB_THREADS / 2)
+    if (n_conf > INT32_MAX)
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energies: n_conf too large");
     PMGB_CK(ctx, cudaSetDevice(ctx->device));
     const size_t n_coord = 3 * static_cast<size_t>(s->n_sites) * static_cast<size_t>(n_conf);
     for (size_t i = 0; i < n_coord; ++i)
         if (!std::isfinite(site_xf[i]))
             return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energies: non-finite site coordinate at %zu", i);
+    if (s->exact) {
+        // every configuration in double-float from its FP64 coordinates
+        int rc;
+        if ((rc = upload_sites64(s, n_coord, site_xf)) ||
+            (rc = ensure(ctx, s->out_buf, sizeof(double) * 3 * static_cast<size_t>(n_conf))) ||
+            (rc = exact_energies(s, n_conf, static_cast<double*>(s->out_buf.p))))
+            return rc;
+        PMGB_CK(ctx, cudaMemcpyAsync(out, s->out_buf.p, sizeof(double) * 3 * static_cast<size_t>(n_conf),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+        return check_status(ctx);
+    }
     std::vector<uint32_t> fix(n_coord);
     for (size_t i = 0; i < n_coord; ++i) fix[i] = to_fix(site_xf[i]);
     const size_t in_bytes = sizeof(uint32_t) * n_coord;
@@ -1226,10 +1318,19 @@ extern "C" int pmgb_energies(pmgb_system* s, int64_t n_conf, const double* site_
 struct pmgb_move {
     pmgb_system* sys = nullptr;
     int max_conf = 0;
-    uint32_t* h_stage = nullptr;  // pinned: [0] = n_conf, then fixed-point site coordinates
+    bool exact = false;           // the system's exact setting when the handle was created
+    // pinned staging: [0] = n_conf, then the site coordinates: 32-bit fixed point (FP32 pass)
+    // or FP64 words (exact: the count in the first word's low 32 bits)
+    void* h_stage = nullptr;
     double* h_out = nullptr;      // pinned: 3 per configuration
-    uint32_t* d_stage = nullptr;
+    void* d_stage = nullptr;
     double* d_out = nullptr;
+    // the double-float pass's own scratch (the graph must not follow the system's buffers)
+    long long* d_list = nullptr;
+    int* d_offsets = nullptr;     // [0] entry count, [1] work counter
+    int* d_plan = nullptr;
+    int* d_done = nullptr;
+    double* d_part = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
 
@@ -1237,8 +1338,9 @@ static void move_free(pmgb_move* m) {
     if (m->exec) cudaGraphExecDestroy(m->exec);
     if (m->h_stage) cudaFreeHost(m->h_stage);
     if (m->h_out) cudaFreeHost(m->h_out);
-    if (m->d_stage) cudaFree(m->d_stage);
-    if (m->d_out) cudaFree(m->d_out);
+    void* dev[] = {m->d_stage, m->d_out, m->d_list, m->d_offsets, m->d_plan, m->d_done, m->d_part};
+    for (void* p : dev)
+        if (p) cudaFree(p);
 }
 
 extern "C" int pmgb_move_create(pmgb_system* s, int32_t max_conf, pmgb_move** out) {
@@ -1252,26 +1354,55 @@ extern "C" int pmgb_move_create(pmgb_system* s, int32_t max_conf, pmgb_move** ou
     auto* m = new pmgb_move();
     m->sys = s;
     m->max_conf = max_conf;
+    m->exact = s->exact;
     const size_t words = 1 + static_cast<size_t>(max_conf) * s->n_sites * 3;
-    cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&m->h_stage), sizeof(uint32_t) * words, cudaHostAllocDefault);
+    const size_t stage_bytes = words * (m->exact ? sizeof(double) : sizeof(uint32_t));
+    const long long items = exact_items(s, max_conf);
+    cudaError_t e = cudaHostAlloc(&m->h_stage, stage_bytes, cudaHostAllocDefault);
     if (e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void**>(&m->h_out), sizeof(double) * 3 * max_conf,
                                             cudaHostAllocDefault);
-    if (e == cudaSuccess) e = cudaMalloc(&m->d_stage, sizeof(uint32_t) * words);
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_stage, stage_bytes);
     if (e == cudaSuccess) e = cudaMalloc(&m->d_out, sizeof(double) * 3 * max_conf);
+    if (m->exact) {
+        if (e == cudaSuccess) e = cudaMalloc(&m->d_list, sizeof(long long) * max_conf);
+        if (e == cudaSuccess) e = cudaMalloc(&m->d_offsets, sizeof(int) * 2);
+        if (e == cudaSuccess) e = cudaMalloc(&m->d_plan, sizeof(int) * 4);
+        if (e == cudaSuccess) e = cudaMalloc(&m->d_done, sizeof(int) * max_conf);
+        if (e == cudaSuccess) e = cudaMalloc(&m->d_part, sizeof(double) * 4 * items);
+    }
     if (e == cudaSuccess) {
         // one graph: copy in (count + coordinates), evaluate, copy out
         LaunchArgs a = base_args(s);
         a.pose_mode = POSE_SITES;
         a.out_mode = OUT_ENERGY;
-        a.site_fix = m->d_stage + 1;
+        a.site_fix = static_cast<const uint32_t*>(m->d_stage) + 1;
         a.n_conf = max_conf;
-        a.n_conf_dev = reinterpret_cast<const int*>(m->d_stage);
+        a.n_conf_dev = static_cast<const int*>(m->d_stage);
         a.e_out = m->d_out;
+        RefineArgs r{};
+        r.sys = s->dev;
+        r.n_systems = 1;
+        r.n_blocks = 1;
+        r.offsets = m->d_offsets;
+        r.counter = m->d_offsets + 1;
+        r.list = m->d_list;
+        r.plan = m->d_plan;
+        r.one_chunk = m->d_plan + 2;
+        r.done = m->d_done;
+        r.part = m->d_part;
+        r.cap_items = items;
+        r.cap_entries = max_conf;
+        r.pose_src = REFINE_POSE_SITES;
+        r.site_xf = static_cast<const double*>(m->d_stage) + 1;
+        r.ref_u = m->d_out;
+        const int n_sm = sm_count(ctx);
         cudaStream_t st = ctx->stream;
         e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            cudaError_t e2 = cudaMemcpyAsync(m->d_stage, m->h_stage, sizeof(uint32_t) * words, cudaMemcpyHostToDevice, st);
-            if (e2 == cudaSuccess) e2 = pmgb_launch_energies_latency(a, max_conf, st);
+            cudaError_t e2 = cudaMemcpyAsync(m->d_stage, m->h_stage, stage_bytes, cudaMemcpyHostToDevice, st);
+            if (e2 == cudaSuccess)
+                e2 = m->exact ? pmgb_launch_exact(r, max_conf, a.n_conf_dev, n_sm, st)
+                              : pmgb_launch_energies_latency(a, max_conf, st);
             if (e2 == cudaSuccess)
                 e2 = cudaMemcpyAsync(m->h_out, m->d_out, sizeof(double) * 3 * max_conf, cudaMemcpyDeviceToHost, st);
             cudaGraph_t g = nullptr;
@@ -1298,12 +1429,19 @@ extern "C" int pmgb_move_energies(pmgb_move* m, int32_t n_conf, const double* si
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_move_energies: 0 <= n_conf <= %d", m->max_conf);
     if (n_conf == 0) return PMGB_OK;
     const size_t n_coord = 3 * static_cast<size_t>(m->sys->n_sites) * n_conf;
-    for (size_t i = 0; i < n_coord; ++i) {
+    for (size_t i = 0; i < n_coord; ++i)
         if (!std::isfinite(site_xf[i]))
             return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_move_energies: non-finite site coordinate at %zu", i);
-        m->h_stage[1 + i] = to_fix(site_xf[i]);
+    if (m->exact) {
+        double* st = static_cast<double*>(m->h_stage);
+        for (size_t i = 0; i < n_coord; ++i) st[1 + i] = wrap01(site_xf[i]);
+        const int32_t cnt[2] = {n_conf, 0};
+        std::memcpy(st, cnt, sizeof(cnt));
+    } else {
+        uint32_t* st = static_cast<uint32_t*>(m->h_stage);
+        for (size_t i = 0; i < n_coord; ++i) st[1 + i] = to_fix(site_xf[i]);
+        st[0] = static_cast<uint32_t>(n_conf);
     }
-    m->h_stage[0] = static_cast<uint32_t>(n_conf);
     PMGB_CK(ctx, cudaSetDevice(ctx->device));
     PMGB_CK(ctx, cudaGraphLaunch(m->exec, ctx->stream));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1322,9 +1460,10 @@ extern "C" void pmgb_move_destroy(pmgb_move* m) {
 }
 
 // Enqueue the FP64 refinement of the Boltzmann tail of a Widom run whose block results are
-// in block_out_dev and per-insertion energies in u_dev (both corrected in place).
+// in block_out_dev and per-insertion energies in u_dev (both corrected in place).  at_point
+// (rotational energy grids): the run's poses sit at grid points (its pose fields are used).
 static int run_refine(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uint64_t seed, double temperature,
-                      double* block_out_dev, double* u_dev) {
+                      double* block_out_dev, double* u_dev, double tail, const RefineArgs* at_point = nullptr) {
     pmgb_ctx* ctx = s->ctx;
     const int64_t cpb = (n_per_block + PMGB_THREADS - 1) / PMGB_THREADS;
     const int n_ctas = static_cast<int>(cpb * n_blocks);
@@ -1345,7 +1484,16 @@ static int run_refine(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uin
     r.ctas_per_block = static_cast<int>(cpb);
     r.seed = seed;
     r.inv_temperature = 1.0 / temperature;
-    r.tail = s->refine_tail;
+    r.tail = tail;
+    if (at_point) {
+        r.pose_src = REFINE_POSE_ROTGRID;
+        for (int d = 0; d < 3; ++d) {
+            r.grid_n[d] = at_point->grid_n[d];
+            r.grid_rep[d] = at_point->grid_rep[d];
+        }
+        r.point_base = at_point->point_base;
+        r.item_base = at_point->item_base;
+    }
     r.block_out = block_out_dev;
     r.u = u_dev;
     r.hist = static_cast<unsigned long long*>(s->r_hist.p);
@@ -1364,7 +1512,7 @@ static int run_refine(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uin
     int n_sm = 0;
     cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device);
     PMGB_CK(ctx, pmgb_launch_refine(r, n_ctas, std::max(1, n_sm), ctx->stream));
-    s->last_refine_ctas = n_ctas;
+    s->last_refined_slot = n_ctas;
     return PMGB_OK;
 }
 
@@ -1372,10 +1520,10 @@ extern "C" int pmgb_system_refined_count(pmgb_system* s, int64_t* count_out) {
     if (!s || !count_out) return PMGB_ERR_INVALID_ARGUMENT;
     pmgb_ctx* ctx = s->ctx;
     *count_out = 0;
-    if (s->last_refine_ctas <= 0) return PMGB_OK;
+    if (s->last_refined_slot < 0) return PMGB_OK;
     PMGB_CK(ctx, cudaSetDevice(ctx->device));
     int n = 0;
-    PMGB_CK(ctx, cudaMemcpyAsync(&n, static_cast<int*>(s->r_offsets.p) + s->last_refine_ctas, sizeof(int),
+    PMGB_CK(ctx, cudaMemcpyAsync(&n, static_cast<int*>(s->r_offsets.p) + s->last_refined_slot, sizeof(int),
                                  cudaMemcpyDeviceToHost, ctx->stream));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
     *count_out = n;
@@ -1428,6 +1576,12 @@ extern "C" int pmgb_system_set_centre_image(pmgb_system* s, int32_t on) {
     if (!s) return PMGB_ERR_INVALID_ARGUMENT;
     s->centre_image = on != 0;
     update_centre_image(s);
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_system_set_exact(pmgb_system* s, int32_t on) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    s->exact = on != 0;
     return PMGB_OK;
 }
 
@@ -1491,7 +1645,7 @@ extern "C" int pmgb_widom_device(pmgb_system* s, int64_t n_per_block, int32_t n_
         PMGB_CK(ctx, launch_pairs_timed(ctx, a, n_ctas));
     }
     PMGB_CK(ctx, pmgb_launch_reduce_blocks(a.partials, n_blocks, a.ctas_per_block, block_out_dev, ctx->stream));
-    if (refine) return run_refine(s, n_per_block, n_blocks, seed, temperature, block_out_dev, a.u_out);
+    if (refine) return run_refine(s, n_per_block, n_blocks, seed, temperature, block_out_dev, a.u_out, s->refine_tail);
     return PMGB_OK;
 }
 
@@ -1565,6 +1719,8 @@ extern "C" int pmgb_widom(pmgb_system* s, int64_t n_per_block, int32_t n_blocks,
 
 // ---------------------------------------------------------------------------- adjoint
 static int grid_axes(pmgb_system* s, const int32_t n_pts[3], const int32_t rep[3]);
+static int exact_grid(pmgb_system* s, const int32_t n_pts[3], const int32_t repfactors[3], double unit_factor,
+                      float* out_dev);
 static int template_sites(int n) { return n <= 1 ? 1 : n <= 2 ? 2 : n <= 3 ? 3 : n <= 4 ? 4 : n <= 6 ? 6 : 8; }
 
 // Assemble Σ w ∂U/∂ε_ab and Σ w ∂U/∂σ²_ab (a: guest species, b: framework species) from the
@@ -1650,7 +1806,7 @@ extern "C" int pmgb_widom_adjoint(pmgb_system* s, int64_t n_per_block, int32_t n
     PMGB_CK(ctx, cudaMemcpyAsync(fp32_blocks.data(), d_block, sizeof(double) * 4 * n_blocks, cudaMemcpyDeviceToHost,
                                  ctx->stream));
     if (s->refine_tail > 0.0)
-        if ((rc = run_refine(s, n_per_block, n_blocks, seed, temperature, d_block, a.u_out))) return rc;
+        if ((rc = run_refine(s, n_per_block, n_blocks, seed, temperature, d_block, a.u_out, s->refine_tail))) return rc;
     PMGB_CK(ctx, cudaMemcpyAsync(block_out, d_block, sizeof(double) * 4 * n_blocks, cudaMemcpyDeviceToHost, ctx->stream));
     PMGB_CK(ctx, cudaMemcpyAsync(cols.data(), s->g_cols.p, sizeof(double) * (n_cols + 2), cudaMemcpyDeviceToHost,
                                  ctx->stream));
@@ -1674,6 +1830,7 @@ extern "C" int pmgb_energies_grad(pmgb_system* s, int64_t n_conf, const double* 
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energies_grad: bad arguments");
     if (int rc = ready_for_charges(s)) return rc;
     if (n_conf == 0) return PMGB_OK;
+    if (n_conf > INT32_MAX) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energies_grad: n_conf too large");
     PMGB_CK(ctx, cudaSetDevice(ctx->device));
     const size_t n_coord = 3 * static_cast<size_t>(s->n_sites) * static_cast<size_t>(n_conf);
     std::vector<uint32_t> fix(n_coord);
@@ -1699,6 +1856,9 @@ extern "C" int pmgb_energies_grad(pmgb_system* s, int64_t n_conf, const double* 
     a.dsum_stride = n_conf;
     a.grad_u = static_cast<float*>(s->g_grad.p);
     PMGB_CK(ctx, pmgb_launch_pairs_grad(a, static_cast<int>((n_conf + PMGB_THREADS - 1) / PMGB_THREADS), ctx->stream));
+    // the energies to the FP64 tolerance (the gradients stay FP32)
+    if (s->exact && ((rc = upload_sites64(s, n_coord, site_xf)) || (rc = exact_energies(s, n_conf, a.e_out))))
+        return rc;
     PMGB_CK(ctx, cudaMemcpyAsync(out, s->out_buf.p, sizeof(double) * 3 * n_conf, cudaMemcpyDeviceToHost, ctx->stream));
     PMGB_CK(ctx, cudaMemcpyAsync(grad_out, s->g_grad.p, sizeof(float) * 3 * n_conf, cudaMemcpyDeviceToHost, ctx->stream));
     return check_status(ctx);
@@ -1754,6 +1914,8 @@ extern "C" int pmgb_energy_grid_adjoint(pmgb_system* s, const int32_t n_pts[3], 
     PMGB_CK(ctx, pmgb_launch_weighted_columns(a.u_out, 1, total, inv_t, d_scale, 1, a.dsum, n_cols, total,
                                               static_cast<double*>(s->g_part.p), n_chunks,
                                               static_cast<double*>(s->g_cols.p), ctx->stream));
+    // the grid values to the FP64 tolerance (the weights above keep the FP32 energies)
+    if (s->exact && (rc = exact_grid(s, n_pts, repfactors, unit_factor, a.grid_out))) return rc;
     std::vector<double> cols(n_cols + 2);
     double M = 0.0;
     PMGB_CK(ctx, cudaMemcpyAsync(out, a.grid_out, sizeof(float) * total, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1807,6 +1969,48 @@ static int grid_axes(pmgb_system* s, const int32_t n_pts[3], const int32_t rep[3
     return PMGB_OK;
 }
 
+// The exact energy grid (grid_axes uploaded): the FP32 pass with each point's rounding-error
+// estimate, then the points whose estimate exceeds max(1e-5 |U|, 1e-4 K) re-evaluated in
+// double-float (their FP64 energies, rounded to FP32, replace the grid values).
+static int exact_grid(pmgb_system* s, const int32_t n_pts[3], const int32_t repfactors[3], double unit_factor,
+                      float* out_dev) {
+    pmgb_ctx* ctx = s->ctx;
+    const int64_t total = int64_t(n_pts[0]) * n_pts[1] * n_pts[2];
+    const int n_screen = pmgb_grid_screen_ctas(total);
+    int rc;
+    if ((rc = ensure(ctx, s->e_bound, sizeof(float) * total)) || (rc = ensure(ctx, s->r_ref, sizeof(double) * 3 * total)))
+        return rc;
+    LaunchArgs a = base_args(s);
+    a.sys.charged = 0;  // grid.jl:337-338: single-site probes get the vdW energy only
+    a.pose_mode = POSE_GRID;
+    a.out_mode = OUT_GRID;
+    for (int d = 0; d < 3; ++d) a.n_pts[d] = n_pts[d];
+    const uint32_t* ax = static_cast<const uint32_t*>(s->axes.p);
+    a.grid_x = ax;
+    a.grid_y = ax + n_pts[0];
+    a.grid_z = ax + n_pts[0] + n_pts[1];
+    a.unit_factor = static_cast<float>(unit_factor);
+    a.grid_out = out_dev;
+    a.grid_bricks = 1;
+    a.bound_out = static_cast<float*>(s->e_bound.p);
+    // worst-case per-term rounding of the FP32 pair terms, and 8 times the rms of independent
+    // per-term roundings, both scaled by the box's rounding condition
+    a.bound_rho = static_cast<float>(4.0e-6 * s->bound_kappa);
+    a.bound_stat = static_cast<float>(4.5e-6 * s->bound_kappa);
+    PMGB_CK(ctx, pmgb_launch_grid_bound(a, pmgb_grid_brick_ctas(n_pts), ctx->stream));
+    RefineArgs r;
+    if ((rc = exact_args(s, total, n_screen, r))) return rc;
+    r.sys.charged = 0;
+    r.pose_src = REFINE_POSE_GRID;
+    for (int d = 0; d < 3; ++d) {
+        r.grid_n[d] = n_pts[d];
+        r.grid_rep[d] = repfactors[d];
+    }
+    r.ref_u = static_cast<double*>(s->r_ref.p);
+    PMGB_CK(ctx, pmgb_launch_grid_exact(r, a.bound_out, out_dev, total, unit_factor, sm_count(ctx), ctx->stream));
+    return PMGB_OK;
+}
+
 extern "C" int pmgb_energy_grid_device(pmgb_system* s, const int32_t n_pts[3], const int32_t repfactors[3],
                                        double unit_factor, float* out_dev) {
     if (!s) return PMGB_ERR_INVALID_ARGUMENT;
@@ -1824,8 +2028,12 @@ extern "C" int pmgb_energy_grid_device(pmgb_system* s, const int32_t n_pts[3], c
     const int64_t total = int64_t(n_pts[0]) * n_pts[1] * n_pts[2];
     if (total > int64_t(INT32_MAX) * PMGB_THREADS / 2)
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid: grid too large");
+    if (!(unit_factor > 0.0) || !std::isfinite(unit_factor))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid: unit_factor must be positive (got %g)",
+                    unit_factor);
     PMGB_CK(ctx, cudaSetDevice(ctx->device));
     if (int rc = grid_axes(s, n_pts, repfactors)) return rc;
+    if (s->exact) return exact_grid(s, n_pts, repfactors, unit_factor, out_dev);
     LaunchArgs a = base_args(s);
     a.sys.charged = 0;  // grid.jl:337-338: single-site probes get the vdW energy only
     a.pose_mode = POSE_GRID;
@@ -1841,6 +2049,82 @@ extern "C" int pmgb_energy_grid_device(pmgb_system* s, const int32_t n_pts[3], c
     const int n_ctas = s->cull ? pmgb_grid_brick_ctas(n_pts) : static_cast<int>((total + PMGB_THREADS - 1) / PMGB_THREADS);
     PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
     return PMGB_OK;
+}
+
+extern "C" int pmgb_energy_grid_rotational(pmgb_system* s, const int32_t n_pts[3], const int32_t repfactors[3],
+                                           int32_t n_rotations, double temperature, uint64_t seed, double unit_factor,
+                                           float* out) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (!n_pts || !repfactors || !out)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid_rotational: NULL argument");
+    for (int d = 0; d < 3; ++d)
+        if (n_pts[d] < 1 || repfactors[d] < 1)
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT,
+                        "pmgb_energy_grid_rotational: n_pts and repfactors must be >= 1");
+    if (n_rotations < 1)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid_rotational: n_rotations must be >= 1");
+    if (!(temperature > 0.0) || !std::isfinite(temperature))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT,
+                    "pmgb_energy_grid_rotational: Must pass temperature (K) for Boltzmann weighted rotations "
+                    "(got %g)", temperature);
+    if (!(unit_factor > 0.0) || !std::isfinite(unit_factor))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid_rotational: unit_factor must be positive");
+    if (int rc = ready_for_charges(s)) return rc;
+    const int64_t total = int64_t(n_pts[0]) * n_pts[1] * n_pts[2];
+    if (total > INT32_MAX) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid_rotational: grid too large");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    if (int rc = grid_axes(s, n_pts, repfactors)) return rc;
+    // the points in slices of at most ~8M insertions, bounding the per-insertion scratch
+    const int64_t cpb = (int64_t(n_rotations) + PMGB_THREADS - 1) / PMGB_THREADS;
+    const int64_t slice = std::max<int64_t>(1, std::min<int64_t>(total, (int64_t(1) << 23) / n_rotations));
+    const bool refine = s->exact || s->refine_tail > 0.0;
+    const double tail = s->refine_tail > 0.0 ? s->refine_tail : 1e-3;
+    int rc;
+    if ((rc = ensure(ctx, s->out_buf, sizeof(float) * total)) ||
+        (rc = ensure(ctx, s->partials, sizeof(LsePartial) * slice * cpb)) ||
+        (rc = ensure(ctx, s->block_out, sizeof(double) * 4 * slice)) ||
+        (refine && (rc = ensure(ctx, s->g_u, sizeof(double) * 2 * slice * n_rotations))))
+        return rc;
+    const uint32_t* ax = static_cast<const uint32_t*>(s->axes.p);
+    for (int64_t p0 = 0; p0 < total; p0 += slice) {
+        const int nb = static_cast<int>(std::min(slice, total - p0));
+        LaunchArgs a = base_args(s);
+        a.pose_mode = POSE_PHILOX;
+        a.out_mode = OUT_WIDOM;
+        a.seed = seed;
+        a.n_per_block = n_rotations;
+        a.n_blocks = nb;
+        a.ctas_per_block = static_cast<int>(cpb);
+        a.inv_temperature = 1.0 / temperature;
+        a.partials = static_cast<LsePartial*>(s->partials.p);
+        a.u_out = refine ? static_cast<double*>(s->g_u.p) : nullptr;
+        a.no_resid = refine ? 1 : 0;
+        a.rot_grid = 1;
+        a.point_base = p0;
+        a.item_base = p0 * n_rotations;
+        for (int d = 0; d < 3; ++d) a.n_pts[d] = n_pts[d];
+        a.grid_x = ax;
+        a.grid_y = ax + n_pts[0];
+        a.grid_z = ax + n_pts[0] + n_pts[1];
+        double* bo = static_cast<double*>(s->block_out.p);
+        PMGB_CK(ctx, pmgb_launch_pairs(a, static_cast<int>(nb * cpb), ctx->stream));
+        PMGB_CK(ctx, pmgb_launch_reduce_blocks(a.partials, nb, a.ctas_per_block, bo, ctx->stream));
+        if (refine) {
+            RefineArgs where{};
+            for (int d = 0; d < 3; ++d) {
+                where.grid_n[d] = n_pts[d];
+                where.grid_rep[d] = repfactors[d];
+            }
+            where.point_base = p0;
+            where.item_base = a.item_base;
+            if ((rc = run_refine(s, n_rotations, nb, seed, temperature, bo, a.u_out, tail, &where))) return rc;
+        }
+        PMGB_CK(ctx, pmgb_launch_rot_grid_out(bo, nb, temperature, std::log(static_cast<double>(n_rotations)),
+                                              unit_factor, static_cast<float*>(s->out_buf.p) + p0, ctx->stream));
+    }
+    PMGB_CK(ctx, cudaMemcpyAsync(out, s->out_buf.p, sizeof(float) * total, cudaMemcpyDeviceToHost, ctx->stream));
+    return check_status(ctx);
 }
 
 extern "C" int pmgb_energy_grid(pmgb_system* s, const int32_t n_pts[3], const int32_t repfactors[3],

@@ -163,10 +163,12 @@ __device__ __forceinline__ uint32_t frac2fix64(double x) {
 // Guest sites of Widom insertion `item` as fixed-point fractions: the FP32 pose (make_pose;
 // its centre of mass is an exact 24-bit fraction) applied to the FP64 site offsets in FP64,
 // as the oracle composes them from the same pose.
+// com_at (optional): a fixed centre of mass (fixed point) instead of the drawn one; the
+// rotation is still the pose's.
 template <int NS>
 __device__ __forceinline__ void pose_sites(const SysDev& S, unsigned long long seed, unsigned long long item,
                                            uint32_t* ux, uint32_t* uy, uint32_t* uz, float* com = nullptr,
-                                           uint32_t* cfix = nullptr) {
+                                           uint32_t* cfix = nullptr, const uint32_t* com_at = nullptr) {
     float xf[3], R[9];
     make_pose(seed, item, xf, R);
     if (com) {
@@ -174,7 +176,9 @@ __device__ __forceinline__ void pose_sites(const SysDev& S, unsigned long long s
         com[1] = xf[1];
         com[2] = xf[2];
     }
-    const uint32_t cx = frac2fix(xf[0]), cy = frac2fix(xf[1]), cz = frac2fix(xf[2]);
+    const uint32_t cx = com_at ? com_at[0] : frac2fix(xf[0]);
+    const uint32_t cy = com_at ? com_at[1] : frac2fix(xf[1]);
+    const uint32_t cz = com_at ? com_at[2] : frac2fix(xf[2]);
     if (cfix) {
         cfix[0] = cx;
         cfix[1] = cy;
@@ -269,9 +273,11 @@ __device__ __forceinline__ float dist2(const int4 r, const uint32_t ux, const ui
 template <bool CHARGED, bool COLS = false>
 __device__ __forceinline__ void pair_fwd(const int4 r, const uint32_t ux, const uint32_t uy, const uint32_t uz,
                                          const Geo& g, const float sig2, const float eps4, float& segmin,
-                                         float& ljp, float& php, float* c12 = nullptr, float* c6 = nullptr) {
+                                         float& ljp, float& php, float* c12 = nullptr, float* c6 = nullptr,
+                                         float* c24 = nullptr, float* cgap = nullptr) {
     const float r2 = dist2(r, ux, uy, uz, g);
     segmin = fminf(segmin, r2);
+    if (cgap) *cgap = fminf(*cgap, fabsf(r2 - g.rc2));  // error bound: distance to the LJ cutoff
     const bool in = r2 < g.rc2;
     float ir2, y = 0.0f;
     if (CHARGED) {
@@ -289,8 +295,10 @@ __device__ __forceinline__ void pair_fwd(const int4 r, const uint32_t ux, const 
     ljp = fmaf(eps4, in ? t : 0.0f, ljp);
     if (COLS) {
         const float ir6 = in ? ir2 * ir2 * ir2 : 0.0f;
-        *c12 = fmaf(ir6, ir6, *c12);
+        const float ir12 = ir6 * ir6;
+        *c12 += ir12;
         *c6 += ir6;
+        if (c24) *c24 = fmaf(ir12, ir12, *c24);
     }
     if (CHARGED) {
         const float e = erfc_fit(g.alpha * (r2 * y)) * y;
@@ -485,7 +493,7 @@ __device__ __forceinline__ float2 site_r2(const float2 X, const float2 Y, const 
 template <bool CHARGED, bool COLS = false>
 __device__ __forceinline__ void pair2_energy(const float2 r2, const float qa, const float qb, const Geo2& g,
                                              const float2 lj12, const float2 lj6, float2& ljp, float2& php,
-                                             float2* c12 = nullptr, float2* c6 = nullptr) {
+                                             float2* c12 = nullptr, float2* c6 = nullptr, float2* c24 = nullptr) {
     float2 ir2, y = f2(0.0f);
     if (CHARGED) {
         y = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
@@ -501,8 +509,10 @@ __device__ __forceinline__ void pair2_energy(const float2 r2, const float qa, co
     const float2 ir6c = make_float2(r2.x < g.rc2 ? ir6.x : 0.0f, r2.y < g.rc2 ? ir6.y : 0.0f);
     ljp = fma2(ir6c, fma2(lj12, ir6c, lj6), ljp);
     if (COLS) {
-        *c12 = __fadd2_rn(*c12, mul2(ir6c, ir6c));
+        const float2 ir12c = mul2(ir6c, ir6c);
+        *c12 = __fadd2_rn(*c12, ir12c);
         *c6 = __fadd2_rn(*c6, ir6c);
+        if (c24) *c24 = fma2(ir12c, ir12c, *c24);
     }
     if (CHARGED) {
         const float2 rr = mul2(r2, y);
@@ -738,6 +748,11 @@ struct UnitIO {
     int pose_mode, out_mode;
     long long item;              // this thread's item index within its system
     bool valid;
+    // POSE_PHILOX on a grid (rotational energy grids): the centre of mass is the grid point of
+    // the item's block, com_at (fixed point); the rotation comes from Philox counter item + item_base
+    bool at_point;
+    uint32_t com_at[3];
+    long long item_base;
     unsigned long long seed;     // POSE_PHILOX
     double inv_temperature;
     const uint32_t* site_fix;    // POSE_SITES
@@ -750,6 +765,8 @@ struct UnitIO {
     float* dsum;                 // GRAD columns: dsum[c * dsum_stride + col_item]
     long long dsum_stride, col_item;
     float* grad_u;               // GRAD, optional
+    float* bound_out;            // OUT_GRID with BOUND: per-item FP32 error estimate (+Inf: must be refined)
+    float bound_rho, bound_stat; // BOUND: worst-case per-term factor, statistical factor (see run_unit)
     LsePartial* partial;         // OUT_WIDOM: this unit's partial
     double* x_out;               // OUT_WIDOM, optional: this thread's -U/T (-inf if none)
     double* m_out;               // OUT_WIDOM, optional (shared): the unit's max of -U/T
@@ -814,13 +831,24 @@ __device__ __forceinline__ bool chunk_near_com(const SysDev& S, const ChunkBox* 
 // dU/dx per item.  Without FORCES the adjoint runs the forward loops with the columns added, so
 // its energies are the forward kernel's.  COMP: the centre-image path (Widom poses of a guest
 // with several sites where S.com_axis >= -1; the caller checks both).
-template <int NS, bool CHARGED, bool GRAD, bool RESID = true, bool FORCES = GRAD, bool COMP = false>
+// BOUND (energy grids of uncharged probes): also an estimate of the item's FP32 rounding error,
+// written to io.bound_out for the screen that picks the items to re-evaluate in double-float.
+// With rep, att the r^-12 and r^-6 magnitudes of each LJ term inside the cutoff,
+// B = sum (rep + att) and Q = sum (rep^2 + att^2):
+//   E = min(bound_rho B, bound_stat sqrt(Q)) + 2e-8 B,
+// the first a worst-case bound of the per-term rounding, the second a multiple of the rms of
+// independent per-term roundings, the last the 2^-32 quantisation of the item's position; +Inf
+// when some pair sits within FP32 rounding of the cutoff or of the overlap distance (the two
+// sides of either give different energies).  Runs the spatially culled loop.
+template <int NS, bool CHARGED, bool GRAD, bool RESID = true, bool FORCES = GRAD, bool COMP = false,
+          bool BOUND = false>
 __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4* stage, uint64_t* bars,
                                          LsePartial* red, uint32_t (&fills)[PMGB_NSTAGE], unsigned int* status) {
     static_assert(RESID || !GRAD, "the adjoint keeps the box-matrix residual");
     static_assert(GRAD || !FORCES, "forces come with the adjoint");
     static_assert(!COMP || (!FORCES && NS > 1), "the centre-image path has no forces and several sites");
-    constexpr bool COLS = GRAD && !FORCES;
+    static_assert(!BOUND || (!GRAD && !COMP && !CHARGED), "the error scale is for uncharged forward grids");
+    constexpr bool COLS = (GRAD && !FORCES) || BOUND;
     const int tid = threadIdx.x;
     const bool valid = io.valid;
     const long long item = io.item;
@@ -832,7 +860,10 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
     uint32_t cfix[3] = {0u, 0u, 0u};  // the pose centre (COMP)
     bool blocked = false;  // inaccessible pocket: U = +Inf without its pair terms mattering
     if (valid) {
-        if (io.pose_mode == POSE_PHILOX) {
+        if (io.pose_mode == POSE_PHILOX && io.at_point) {
+            pose_sites<NS>(S, io.seed, static_cast<unsigned long long>(item + io.item_base), ux, uy, uz, nullptr, cfix,
+                           io.com_at);
+        } else if (io.pose_mode == POSE_PHILOX) {
             float com[3];
             pose_sites<NS>(S, io.seed, static_cast<unsigned long long>(item), ux, uy, uz, com, cfix);
             if (S.acc) blocked = !accessible_com(S, com);
@@ -893,6 +924,10 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
     }
     bool ovl = false, abort = false;
     int fail_tile = 0;
+    // BOUND: smallest |r^2 - rc^2| seen, an overlap distance within rounding, sum of squared terms
+    float cgap = __int_as_float(0x7f800000);
+    bool thr_near = false;
+    double bsq = 0.0, bsum = 0.0;
     int cb = 0;  // running sub-chunk index: the order of S.cbox
     const bool box_cull = io.cull && S.cbox != nullptr;
 
@@ -954,9 +989,9 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                 lj6[k] = p.lj6;
                 segmin[k] = __int_as_float(0x7f800000);
             }
-            float2 i12[NS], i6[NS];
+            float2 i12[NS], i6[NS], i24[NS];
 #pragma unroll
-            for (int k = 0; k < NS; ++k) i12[k] = i6[k] = f2(0.0f);
+            for (int k = 0; k < NS; ++k) i12[k] = i6[k] = i24[k] = f2(0.0f);
             for (int j0 = lo; j0 < hi; j0 += kChunk) {
                 const int j1 = min(j0 + kChunk, hi);
                 const int n_sub = (j1 - j0 + kSub - 1) / kSub;
@@ -1086,7 +1121,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                         ljp[k] = ljp2[k].x + ljp2[k].y;
                         php[k] = php2[k].x + php2[k].y;
                     }
-                } else if (io.cull) {
+                } else if (io.cull || BOUND) {
                     // the warp's insertions are spatially close: after the distances, skip the
                     // pair terms of four records when no lane has the site inside the cutoff
                     // (those terms are exact zeros, so the sums are unchanged)
@@ -1098,12 +1133,17 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                             const float2 d23 = pair2_r2<RESID>(r2, r3, ux[k], uy[k], uz[k], g2);
                             const float dmin = fminf(fminf(d01.x, d01.y), fminf(d23.x, d23.y));
                             segmin[k] = fminf(segmin[k], dmin);
+                            if (BOUND)
+                                cgap = fminf(cgap, fminf(fminf(fabsf(d01.x - g2.rc2), fabsf(d01.y - g2.rc2)),
+                                                         fminf(fabsf(d23.x - g2.rc2), fabsf(d23.y - g2.rc2))));
                             if (__any_sync(0xffffffffu, valid && !blocked && dmin < g2.rcmax2)) {
                                 const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
                                 pair2_energy<CHARGED, COLS>(d01, __int_as_float(r0.w), __int_as_float(r1.w), g2,
-                                                            a12, a6, ljp2[k], php2[k], &i12[k], &i6[k]);
+                                                            a12, a6, ljp2[k], php2[k], &i12[k], &i6[k],
+                                                            BOUND ? &i24[k] : nullptr);
                                 pair2_energy<CHARGED, COLS>(d23, __int_as_float(r2.w), __int_as_float(r3.w), g2,
-                                                            a12, a6, ljp2[k], php2[k], &i12[k], &i6[k]);
+                                                            a12, a6, ljp2[k], php2[k], &i12[k], &i6[k],
+                                                            BOUND ? &i24[k] : nullptr);
                             }
                         }
                     };
@@ -1132,7 +1172,8 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
 #pragma unroll
                         for (int k = 0; k < NS; ++k)
                             pair_fwd<CHARGED, COLS>(r, ux[k], uy[k], uz[k], g, sig2[k], eps4[k], segmin[k], ljp[k],
-                                                    php[k], &i12[k].x, &i6[k].x);
+                                                    php[k], &i12[k].x, &i6[k].x, BOUND ? &i24[k].x : nullptr,
+                                                    BOUND ? &cgap : nullptr);
                     }
                 } else {
                     int j = j0;
@@ -1168,6 +1209,18 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
             }
 #pragma unroll
             for (int k = 0; k < NS; ++k) ovl = ovl || (segmin[k] < r2o[k]);
+            if (BOUND) {
+                // rep = lj12 r^-12 and att = |lj6| r^-6 per pair inside the cutoff: sum rep^2 + att^2
+#pragma unroll
+                for (int k = 0; k < NS; ++k) {
+                    const double a12 = lj12[k], a6 = lj6[k];
+                    const double s12 = static_cast<double>(i12[k].x) + static_cast<double>(i12[k].y);
+                    const double s6 = static_cast<double>(i6[k].x) + static_cast<double>(i6[k].y);
+                    bsq += a12 * a12 * (static_cast<double>(i24[k].x) + static_cast<double>(i24[k].y)) + a6 * a6 * s12;
+                    bsum += a12 * s12 - a6 * s6;  // lj6 < 0: the attraction's magnitude
+                    thr_near = thr_near || fabsf(segmin[k] - r2o[k]) <= 4e-6f * r2o[k];
+                }
+            }
             if (GRAD && valid) {
                 // this thread owns its item's columns: write on the segment's first tile, add after
                 const bool first = (lo == d.lo);
@@ -1260,6 +1313,11 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
         if (valid) {
             io.grid_out[item] = static_cast<float>(uv * static_cast<double>(io.unit_factor));
             if (GRAD && io.u_out) io.u_out[item] = uv;
+            if (BOUND) {
+                const bool edge = thr_near || cgap <= 4e-6f * g.rc2;
+                const double e = fmin(io.bound_rho * bsum, io.bound_stat * sqrt(bsq)) + 2e-8 * bsum;
+                io.bound_out[item] = edge ? __int_as_float(0x7f800000) : static_cast<float>(e);
+            }
         }
         return true;
     }

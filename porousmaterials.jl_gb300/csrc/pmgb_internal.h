@@ -178,6 +178,11 @@ struct LaunchArgs {
     float unit_factor;
     float* grid_out;
     int grid_bricks;             // warps take 4 x 4 x 2 bricks of points (spatially compact)
+    // rotational energy grid (POSE_PHILOX): block b's insertions sit at grid point point_base + b
+    // (planes grid_x/y/z, n_pts) with rotations from Philox counters item_base + item; warps skip
+    // out-of-cutoff terms (their lanes share the centre) without a processing order
+    int rot_grid;
+    long long point_base, item_base;
     // forward Widom whose Boltzmann tail is refined in FP64: distances from the FP32 box matrix
     // alone (no residual), ~13% less work; the refinement re-evaluates the insertions that matter
     int no_resid;
@@ -185,6 +190,9 @@ struct LaunchArgs {
     float* dsum;                 // [(seg * NS + site) * 2 + {0: sum r^-12, 1: sum r^-6}][item], within cutoff
     long long dsum_stride;       // items per column
     float* grad_u;               // optional: [item * 3] dU/dx of the centre of mass (K/A)
+    // energy grid with error scale (pmgb_launch_grid_bound)
+    float* bound_out;            // [item] FP32 rounding-error estimate (K), +Inf where a pair sits at a threshold
+    float bound_rho, bound_stat; // factors of the estimate (run_unit, BOUND)
     // status
     unsigned int* status;
 };
@@ -281,8 +289,30 @@ struct RefineArgs {
     int* done;                      // [cap_entries] chunks finished per refined insertion
     double* part;                   // [4 cap_items] chunk partials (U_vdw, U_sr / coul, U_lr, overlap)
     long long cap_items, cap_entries;
+    // where the entries' guest sites come from (REFINE_POSE_*): Widom poses, the caller's
+    // explicit FP64 site coordinates, or energy-grid points of a single-site probe
+    int pose_src;
+    const double* site_xf;          // REFINE_POSE_SITES: [n x n_sites x 3] supercell fractions
+    int grid_n[3], grid_rep[3];     // REFINE_POSE_GRID / _ROTGRID: points per axis, replication factors
+    long long point_base, item_base;  // REFINE_POSE_ROTGRID: block b at point point_base + b; rotation
+                                      //   of insertion i from Philox counter item_base + i
 };
+// REFINE_POSE_ROTGRID: Widom insertions of a rotational energy grid (centre of mass at the block's
+// grid point, Philox rotation)
+enum RefinePose : int { REFINE_POSE_PHILOX = 0, REFINE_POSE_SITES = 1, REFINE_POSE_GRID = 2, REFINE_POSE_ROTGRID = 3 };
 cudaError_t pmgb_launch_refine(const RefineArgs& a, int n_ctas, int n_sm, cudaStream_t st);
+// Double-float energies of every explicit configuration 0..n-1 (n from *n_dev when n_dev is set,
+// else n), written to a.ref_u as (U_vdw, U_es short-range, U_es long-range): pose_src
+// REFINE_POSE_SITES; a.list, a.offsets (>= 1 entry), a.plan, a.done, a.part, a.counter scratch.
+cudaError_t pmgb_launch_exact(const RefineArgs& a, long long n, const int* n_dev, int n_sm, cudaStream_t st);
+// Re-evaluate in double-float every point of an FP32 energy grid whose error estimate (bound,
+// from pmgb_launch_grid_bound) exceeds max(1e-5 |U|, 1e-4 K), and overwrite its value in grid
+// (U * unit_factor): pose_src REFINE_POSE_GRID; a.counts / a.offsets hold one entry per 256
+// points.  n_points = the grid's points.
+cudaError_t pmgb_launch_grid_exact(const RefineArgs& a, const float* bound, float* grid, long long n_points,
+                                   double unit_factor, int n_sm, cudaStream_t st);
+// CTAs of the grid screen (one per PMGB_THREADS points)
+int pmgb_grid_screen_ctas(long long n_points);
 size_t pmgb_refine_hist_words();
 
 // Index of the compiled template variant for n_sites guest sites with or without charges;
@@ -292,6 +322,9 @@ int pmgb_batch_variant(int n_sites, bool charged);
 // kernels (defined in pmgb_kernels.cu); return cudaError_t of the launch
 cudaError_t pmgb_launch_pairs(const LaunchArgs& a, int n_ctas, cudaStream_t st);
 cudaError_t pmgb_launch_pairs_grad(const LaunchArgs& a, int n_ctas, cudaStream_t st);
+// Energy grid of a single-site uncharged probe (POSE_GRID, OUT_GRID) plus each point's FP32
+// error scale in a.bound_out (run_unit's BOUND form)
+cudaError_t pmgb_launch_grid_bound(const LaunchArgs& a, int n_ctas, cudaStream_t st);
 // persistent batch (defined in pmgb_batch.cu)
 cudaError_t pmgb_batch_prepare(bool grad);  // function attributes, before any stream capture
 cudaError_t pmgb_launch_batch(const BatchArgs& b, bool grad, int n_ctas, cudaStream_t st);
@@ -321,6 +354,8 @@ cudaError_t pmgb_launch_sample_poses(unsigned long long seed, long long start, l
 cudaError_t pmgb_launch_philox(const unsigned int* ctr, const unsigned int* key, long long n,
                                unsigned int* out, cudaStream_t st);
 cudaError_t pmgb_launch_fp32_peak(float* sink, int n_ctas, int iters, cudaStream_t st);
+cudaError_t pmgb_launch_rot_grid_out(const double* block_out, int n, double temperature, double log_n, double unit,
+                                     float* out, cudaStream_t st);
 cudaError_t pmgb_launch_bounded_wait_test(unsigned int* status, unsigned long long limit_ns, int arm,
                                           cudaStream_t st);
 size_t pmgb_pairs_smem_bytes();

@@ -8,7 +8,8 @@
 namespace {
 
 // Single-system launch: CTA b runs unit b.
-template <int NS, bool CHARGED, bool GRAD, bool RESID = true, bool FORCES = GRAD, bool COMP = false>
+template <int NS, bool CHARGED, bool GRAD, bool RESID = true, bool FORCES = GRAD, bool COMP = false,
+          bool BOUND = false>
 __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_constant__ LaunchArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     int4* stage = reinterpret_cast<int4*>(smem_raw);
@@ -26,6 +27,16 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
         if (a.perm && io.valid) within = a.perm[static_cast<size_t>(b) * a.n_per_block + slot];
         io.item = static_cast<long long>(b) * a.n_per_block + within;
         io.cull = a.perm != nullptr;
+        if (a.rot_grid) {
+            const long long p = a.point_base + b;
+            const long long n1 = a.n_pts[0], n2 = a.n_pts[1];
+            io.at_point = true;
+            io.com_at[0] = a.grid_x[static_cast<int>(p % n1)];
+            io.com_at[1] = a.grid_y[static_cast<int>((p / n1) % n2)];
+            io.com_at[2] = a.grid_z[static_cast<int>(p / (n1 * n2))];
+            io.item_base = a.item_base;
+            io.cull = true;  // every lane of the CTA sits at the same point: skip what none reaches
+        }
     } else if (a.pose_mode == POSE_SITES) {
         io.item = static_cast<long long>(blockIdx.x) * PMGB_THREADS + tid;
         io.valid = io.item < a.n_conf;
@@ -61,10 +72,13 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
     io.dsum_stride = a.dsum_stride;
     io.col_item = io.item;
     io.grad_u = a.grad_u;
+    io.bound_out = a.bound_out;
+    io.bound_rho = a.bound_rho;
+    io.bound_stat = a.bound_stat;
     io.partial = (a.partials && !a.perm) ? a.partials + blockIdx.x : nullptr;
     ring_init(bars);
     uint32_t fills[PMGB_NSTAGE] = {};
-    (void)run_unit<NS, CHARGED, GRAD, RESID, FORCES, COMP>(a.sys, io, stage, bars, red, fills, a.status);
+    (void)run_unit<NS, CHARGED, GRAD, RESID, FORCES, COMP, BOUND>(a.sys, io, stage, bars, red, fills, a.status);
 }
 
 // ---- latency path: few configurations, one CTA each -----------------------------------
@@ -557,6 +571,17 @@ cudaError_t pmgb_launch_pairs(const LaunchArgs& a, int n_ctas, cudaStream_t st) 
     return a.sys.charged ? launch_ns<true>(a, n_ctas, st) : launch_ns<false>(a, n_ctas, st);
 }
 
+cudaError_t pmgb_launch_grid_bound(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
+    if (n_ctas <= 0) return cudaSuccess;
+    if (a.sys.charged || a.sys.n_sites != 1 || a.pose_mode != POSE_GRID || !a.bound_out) return cudaErrorInvalidValue;
+    const size_t smem = pmgb_pairs_smem_bytes();
+    cudaError_t e = cudaFuncSetAttribute(pairs_kernel<1, false, false, true, false, false, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    pairs_kernel<1, false, false, true, false, false, true><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t pmgb_launch_pairs_grad(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
     if (n_ctas <= 0) return cudaSuccess;
     return a.sys.charged ? launch_grad_ns<true>(a, n_ctas, st) : launch_grad_ns<false>(a, n_ctas, st);
@@ -672,6 +697,23 @@ __global__ void bounded_wait_test_kernel(unsigned int* status, unsigned long lon
 cudaError_t pmgb_launch_bounded_wait_test(unsigned int* status, unsigned long long limit_ns, int arm,
                                           cudaStream_t st) {
     bounded_wait_test_kernel<<<1, 32, 0, st>>>(status, limit_ns, arm);
+    return cudaGetLastError();
+}
+
+// Rotational energy grid values from the block results of its points: -T log(Σ e^{-U/T} / n)
+// times the unit factor (+Inf where every orientation overlaps), src/grid.jl:338-351.
+__global__ void rot_grid_out_kernel(const double* block_out, int n, double temperature, double log_n, double unit,
+                                    float* out) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    const double L = block_out[4 * b];
+    out[b] = isfinite(L) ? static_cast<float>(-temperature * (L - log_n) * unit) : __int_as_float(0x7f800000);
+}
+
+cudaError_t pmgb_launch_rot_grid_out(const double* block_out, int n, double temperature, double log_n, double unit,
+                                     float* out, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    rot_grid_out_kernel<<<(n + 255) / 256, 256, 0, st>>>(block_out, n, temperature, log_n, unit, out);
     return cudaGetLastError();
 }
 

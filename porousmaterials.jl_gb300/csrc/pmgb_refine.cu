@@ -21,6 +21,8 @@
 // log K_H.
 #include "pmgb_device.cuh"
 
+#include <algorithm>
+
 namespace {
 
 constexpr int kBins = 256;             // histogram bins of the gap L - x
@@ -384,27 +386,51 @@ struct SiteScreen {
     float r2max;
 };
 
-// The guest sites of insertion `item`, set up once per warp: the pose is drawn as in make_pose,
-// and lane 3k + d (k < n_sites, d < 3) composes coordinate d of site k in FP64 from it -- the
-// same products as refined_entry -- then takes it to the 32-bit fixed point with its FP32
-// remainder and to the 64-bit fixed-point phase; lane 3k also splits the charge of site k into
-// a double-float.  The lanes then exchange the values, so the FP64 set-up costs a warp one pass
-// instead of one per site and coordinate.
-__device__ __forceinline__ void warp_site_setup(const SysDev& S, unsigned long long seed, unsigned long long item,
-                                                SiteScreen& sc) {
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
+// FP64 fractional coordinate d of guest site k of entry `item` (supercell fractions):
+//  - a Widom insertion: its pose (make_pose) applied to the FP64 site offsets in FP64 (the
+//    same products as the FP32 pass's pose_sites, without the rounding to fixed point);
+//  - explicit configurations: the caller's FP64 coordinates;
+//  - an energy-grid point (single site): (i/(n-1)) / rep per axis, the end plane folded onto
+//    the first (its periodic image, as the FP32 grid pass evaluates it).
+__device__ __forceinline__ double grid_coord(const RefineArgs& a, unsigned long long point, int d) {
+    const unsigned long long n1 = a.grid_n[0], n2 = a.grid_n[1];
+    const unsigned long long i = d == 0 ? point % n1 : d == 1 ? (point / n1) % n2 : point / (n1 * n2);
+    const int n = a.grid_n[d];
+    double f = n > 1 ? static_cast<double>(i) / static_cast<double>(n - 1) : 0.0;
+    if (f >= 1.0) f -= 1.0;
+    return f / static_cast<double>(a.grid_rep[d]);
+}
+
+__device__ __forceinline__ double site_coord(const RefineArgs& a, const SysDev& S, unsigned long long seed,
+                                             unsigned long long item, int k, int d) {
+    if (a.pose_src == REFINE_POSE_SITES) return a.site_xf[(item * S.n_sites + k) * 3 + d];
+    if (a.pose_src == REFINE_POSE_GRID) return grid_coord(a, item, d);
+    // a Widom pose: its rotation applied to the FP64 site offsets; the centre of mass drawn with
+    // it, or (rotational grids) the block's grid point
+    const bool at_point = a.pose_src == REFINE_POSE_ROTGRID;
     float xf[3], R[9];
-    make_pose(seed, item, xf, R);
-    const int k = min(lane / 3, S.n_sites - 1), d = lane % 3;
+    make_pose(seed, at_point ? item + a.item_base : item, xf, R);
+    const double c = at_point ? grid_coord(a, a.point_base + item / a.n_per_block, d) : static_cast<double>(xf[d]);
     const double bx = S.body64[k][0], by = S.body64[k][1], bz = S.body64[k][2];
     const double ox = fma(static_cast<double>(R[0]), bx, fma(static_cast<double>(R[3]), by, static_cast<double>(R[6]) * bz));
     const double oy = fma(static_cast<double>(R[1]), bx, fma(static_cast<double>(R[4]), by, static_cast<double>(R[7]) * bz));
     const double oz = fma(static_cast<double>(R[2]), bx, fma(static_cast<double>(R[5]), by, static_cast<double>(R[8]) * bz));
-    double x;
-    if (d == 0) x = static_cast<double>(xf[0]) + fma(S.g64[0], ox, fma(S.g64[1], oy, S.g64[2] * oz));
-    else if (d == 1) x = static_cast<double>(xf[1]) + fma(S.g64[3], oy, S.g64[4] * oz);
-    else x = static_cast<double>(xf[2]) + S.g64[5] * oz;
+    if (d == 0) return c + fma(S.g64[0], ox, fma(S.g64[1], oy, S.g64[2] * oz));
+    if (d == 1) return c + fma(S.g64[3], oy, S.g64[4] * oz);
+    return c + S.g64[5] * oz;
+}
+
+// The guest sites of entry `item`, set up once per warp: lane 3k + d (k < n_sites, d < 3) takes
+// coordinate d of site k in FP64 (site_coord), then to the 32-bit fixed point with its FP32
+// remainder and to the 64-bit fixed-point phase; lane 3k also splits the charge of site k into
+// a double-float.  The lanes then exchange the values, so the FP64 set-up costs a warp one pass
+// instead of one per site and coordinate.
+__device__ __forceinline__ void warp_site_setup(const RefineArgs& a, const SysDev& S, unsigned long long seed,
+                                                unsigned long long item, SiteScreen& sc) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int k = min(lane / 3, S.n_sites - 1), d = lane % 3;
+    const double x = site_coord(a, S, seed, item, k, d);
     const double ux = x * 4294967296.0;
     const long long fx = __double2ll_rn(ux);
     const uint32_t fix = static_cast<uint32_t>(fx);  // as frac2fix64
@@ -570,15 +596,16 @@ __device__ __forceinline__ void queued_pair(const SysDev& S, int sg, int e, cons
 // insertion however they are spread over its lanes.  k-space half-rows: lanes stride over them.
 // The lane sums are added across the warp in double-float.
 // out4 = (U_vdw part, U_sr part / coul, U_lr part, overlap).
-__device__ void energy_fp64_warp_part(const SysDev& S, unsigned long long seed, unsigned long long item, int j0, int j1,
-                                      int k0, int k1, double* out4, int* queue, const float4* phase_tab) {
+__device__ void energy_fp64_warp_part(const RefineArgs& a, const SysDev& S, unsigned long long seed,
+                                      unsigned long long item, int j0, int j1, int k0, int k1, double* out4,
+                                      int* queue, const float4* phase_tab) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int ns = S.n_sites;
     dfl vd{0.0f, 0.0f}, srd{0.0f, 0.0f}, lrd{0.0f, 0.0f};  // this lane's sums (double-float)
     bool ovl = false;
     SiteScreen sc;
-    warp_site_setup(S, seed, item, sc);
+    warp_site_setup(a, S, seed, item, sc);
     for (int sg = 0; sg < S.n_seg; ++sg) {
         const SegDesc d = S.seg[sg];
         const int lo = max(d.lo, j0), hi = min(d.hi, j1);
@@ -663,7 +690,13 @@ __device__ __forceinline__ void refined_entry(const RefineArgs& a, long long e, 
     S = a.systems ? &a.systems[sys].sys : &a.sys;
     unsigned long long seed, item;
     entry_pose(a, e, seed, item);
-    // the insertion's pose applied to the FP64 site offsets, kept in FP64 (no fixed point)
+    if (a.pose_src != REFINE_POSE_PHILOX) {
+        for (int k = 0; k < S->n_sites; ++k)
+            for (int d = 0; d < 3; ++d) xs[k][d] = site_coord(a, *S, seed, item, k, d);
+        return;
+    }
+    // the insertion's pose applied to the FP64 site offsets, kept in FP64 (no fixed point): the
+    // products of site_coord with one pose draw for all sites
     float xf[3], R[9];
     make_pose(seed, static_cast<unsigned long long>(item), xf, R);
     for (int k = 0; k < S->n_sites; ++k) {
@@ -788,7 +821,7 @@ __global__ void __launch_bounds__(PMGB_THREADS) refine_large_kernel(const __grid
         const int k0 = static_cast<int>(static_cast<long long>(S.n_krow) * c / C);
         const int k1 = static_cast<int>(static_cast<long long>(S.n_krow) * (c + 1) / C);
         double* p = a.part + 4 * static_cast<size_t>(i);
-        energy_fp64_warp_part(S, seed, item, j0, j1, k0, k1, p, s_queue[threadIdx.x >> 5], s_phase);
+        energy_fp64_warp_part(a, S, seed, item, j0, j1, k0, k1, p, s_queue[threadIdx.x >> 5], s_phase);
         if (lane == 0 && C == 1) {  // the whole insertion in one chunk
             double* out = a.ref_u + 3 * static_cast<size_t>(r);
             out[0] = p[3] > 0.0 ? __longlong_as_double(0x7ff0000000000000ll) : p[0];
@@ -885,7 +918,99 @@ __global__ void tail_correct_kernel(const __grid_constant__ RefineArgs a) {
     }
 }
 
+// ---- exact energies of explicit configurations and of energy-grid points --------------------
+// The entry list of the double-float pass when every configuration is evaluated: list[i] = i and
+// the entry count in offsets[0] (the refinement kernels then run with zero screen chunks).
+__global__ void exact_list_kernel(const __grid_constant__ RefineArgs a, long long n, const int* n_dev) {
+    const long long cnt = n_dev ? static_cast<long long>(*n_dev) : n;
+    for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < cnt;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        a.list[i] = i;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.offsets[0] = static_cast<int>(cnt);
+}
+
+// A grid point goes to the double-float pass when its FP32 error estimate could exceed its
+// tolerance max(1e-5 |U|, 1e-4 K), or is +Inf (a pair at the cutoff or overlap distance).  A point
+// that overlaps (U = +Inf) away from the threshold is +Inf whatever the rounding of its terms.
+__device__ __forceinline__ bool grid_selected(const float* grid, const float* bound, long long p, long long n,
+                                              double inv_unit) {
+    if (p >= n) return false;
+    const float b = bound[p];
+    if (isinf(b)) return true;
+    const double u = static_cast<double>(grid[p]) * inv_unit;
+    if (!isfinite(u)) return false;
+    return static_cast<double>(b) > fmax(1e-5 * fabs(u), 1e-4);
+}
+
+__global__ void grid_count_kernel(const __grid_constant__ RefineArgs a, const float* grid, const float* bound,
+                                  long long n, double inv_unit) {
+    const long long p = static_cast<long long>(blockIdx.x) * PMGB_THREADS + threadIdx.x;
+    const int c = __syncthreads_count(grid_selected(grid, bound, p, n, inv_unit) ? 1 : 0);
+    if (threadIdx.x == 0) a.counts[blockIdx.x] = c;
+}
+
+// stable compaction of the selected points (index order), as tail_scatter_kernel
+__global__ void grid_scatter_kernel(const __grid_constant__ RefineArgs a, const float* grid, const float* bound,
+                                    long long n, double inv_unit) {
+    __shared__ int warp_base[PMGB_THREADS / 32];
+    const long long p = static_cast<long long>(blockIdx.x) * PMGB_THREADS + threadIdx.x;
+    const bool sel = grid_selected(grid, bound, p, n, inv_unit);
+    const unsigned ballot = __ballot_sync(0xffffffffu, sel);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) warp_base[warp] = __popc(ballot);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = a.offsets[blockIdx.x];
+        for (int w = 0; w < PMGB_THREADS / 32; ++w) {
+            const int c = warp_base[w];
+            warp_base[w] = acc;
+            acc += c;
+        }
+    }
+    __syncthreads();
+    if (sel) a.list[warp_base[warp] + __popc(ballot & ((1u << lane) - 1u))] = p;
+}
+
+// the re-evaluated points' van der Waals energies (+Inf on overlap) into the grid
+__global__ void grid_write_kernel(const __grid_constant__ RefineArgs a, float* grid, int n_ctas, double unit) {
+    const int n_ref = a.offsets[n_ctas];
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_ref; r += gridDim.x * blockDim.x)
+        grid[a.list[r]] = static_cast<float>(a.ref_u[3 * static_cast<size_t>(r)] * unit);
+}
+
 }  // namespace
+
+int pmgb_grid_screen_ctas(long long n_points) { return static_cast<int>((n_points + PMGB_THREADS - 1) / PMGB_THREADS); }
+
+cudaError_t pmgb_launch_exact(const RefineArgs& a, long long n, const int* n_dev, int n_sm, cudaStream_t st) {
+    if (!n_dev && n <= 0) return cudaSuccess;
+    const long long cap = n_dev ? a.cap_entries : n;
+    const int blocks = static_cast<int>(std::max(1ll, std::min((cap + 255) / 256, 4ll * n_sm)));
+    exact_list_kernel<<<blocks, 256, 0, st>>>(a, n, n_dev);
+    cudaError_t e = cudaMemsetAsync(a.done, 0, sizeof(int) * static_cast<size_t>(cap), st);
+    if (e != cudaSuccess) return e;
+    refine_small_kernel<<<4 * n_sm, PMGB_THREADS, 0, st>>>(a, 0);
+    refine_plan_kernel<<<1, 1024, 0, st>>>(a, 0);
+    refine_large_kernel<<<4 * n_sm, PMGB_THREADS, 0, st>>>(a, 0);
+    return cudaGetLastError();
+}
+
+cudaError_t pmgb_launch_grid_exact(const RefineArgs& a, const float* bound, float* grid, long long n_points,
+                                   double unit_factor, int n_sm, cudaStream_t st) {
+    if (n_points <= 0) return cudaSuccess;
+    const int n_ctas = pmgb_grid_screen_ctas(n_points);
+    const double inv_unit = 1.0 / unit_factor;
+    grid_count_kernel<<<n_ctas, PMGB_THREADS, 0, st>>>(a, grid, bound, n_points, inv_unit);
+    tail_scan_kernel<<<1, 1024, 0, st>>>(a, n_ctas);
+    grid_scatter_kernel<<<n_ctas, PMGB_THREADS, 0, st>>>(a, grid, bound, n_points, inv_unit);
+    cudaError_t e = cudaMemsetAsync(a.done, 0, sizeof(int) * static_cast<size_t>(n_points), st);
+    if (e != cudaSuccess) return e;
+    refine_small_kernel<<<4 * n_sm, PMGB_THREADS, 0, st>>>(a, n_ctas);
+    refine_plan_kernel<<<1, 1024, 0, st>>>(a, n_ctas);
+    refine_large_kernel<<<4 * n_sm, PMGB_THREADS, 0, st>>>(a, n_ctas);
+    grid_write_kernel<<<4 * n_sm, 256, 0, st>>>(a, grid, n_ctas, unit_factor);
+    return cudaGetLastError();
+}
 
 cudaError_t pmgb_launch_refine(const RefineArgs& a, int n_ctas, int n_sm, cudaStream_t st) {
     if (n_ctas <= 0) return cudaSuccess;

@@ -5,9 +5,10 @@
 include/pmgb.h) for PorousMaterials.jl v0.4.  It provides drop-in bodies for
 
   * `henry_coefficient(crystal, molecule, temperature, ljff; insertions_per_volume,
-     verbose, ewald_precision, autosave, filename_comment)`      (src/henry.jl:34-181)
-  * `energy_grid(crystal, molecule, ljff; resolution, units, center, verbose)` for
-     single-site probes                                          (src/grid.jl:291-362)
+     verbose, ewald_precision, autosave, filename_comment, accessibility_grid)`
+                                                                 (src/henry.jl:34-181)
+  * `energy_grid(crystal, molecule, ljff; resolution, n_rotations, temperature, units,
+     center, verbose)`                                           (src/grid.jl:291-362)
 
 plus the derivative of K_H with respect to the pure-species LJ parameters and the framework
 charge scale (a ChainRulesCore `rrule`), and batched screening of many frameworks in one
@@ -160,90 +161,140 @@ end
 
 # ---------------------------------------------------------------------------- drop-in bodies
 """
-Drop-in for `henry_coefficient` (src/henry.jl:34-181): the same set-up, statistics, result
-keys, units and autosave; the insertions run on the GPU.  `seed` makes a run reproducible;
-`refine_tail` (default 1e-3) re-evaluates in high precision the insertions that carry all but that
-fraction of each block's Boltzmann weight, which keeps K_H within 1e-6 of an FP64 evaluation.
+Drop-in for `henry_coefficient` (src/henry.jl:34-181): the same arguments and keywords, the same
+block statistics, result keys, units and autosave file; the insertions run on the GPU.
+`accessibility_grid` (a `Grid{Bool}` over the unit cell) gates the insertions as in the reference:
+an insertion whose nearest grid node and its 26 neighbours are all inaccessible gets U = Inf.
+`seed` makes a run reproducible; `refine_tail` (default 1e-3) re-evaluates in high precision the
+insertions that carry all but that fraction of each block's Boltzmann weight, which keeps K_H
+within 1e-6 of an FP64 evaluation.
 """
 function henry_coefficient(crystal::Crystal, molecule::Molecule, temperature::Float64,
                            ljforcefield::LJForceField; insertions_per_volume::Union{Int, Float64}=200,
                            verbose::Bool=true, ewald_precision::Float64=1e-6, autosave::Bool=true,
-                           filename_comment::AbstractString="", seed::UInt64=rand(UInt64),
-                           ctx::Context=default_context(), refine_tail::Float64=1e-3, return_energies::Bool=false)
+                           filename_comment::AbstractString="",
+                           accessibility_grid::Union{Nothing, Grid{Bool}}=nothing,
+                           seed::UInt64=rand(UInt64), ctx::Context=default_context(), refine_tail::Float64=1e-3)
     assert_P1_symmetry(crystal)
-    time_start = time()
-    nb_insertions = max(N_BLOCKS, ceil(Int, insertions_per_volume * crystal.box.Ω))
-    nb_insertions_per_block = ceil(Int, nb_insertions / N_BLOCKS)
+    # the grid must describe this crystal's unit cell (the reference checks this under `verbose`;
+    # a mismatched grid would gate the wrong pockets, so it is checked on every call here)
+    if !isnothing(accessibility_grid) && !isapprox(accessibility_grid.box, crystal.box)
+        error(@sprintf("accessibility grid box does not match box of %s.\n", crystal.name))
+    end
+    t0 = time()
+    n_total = max(N_BLOCKS, ceil(Int, insertions_per_volume * crystal.box.Ω))   # before replication
+    n_per_block = ceil(Int, n_total / N_BLOCKS)
     repfactors = replication_factors(crystal.box, ljforcefield)
-    crystal = replicate(crystal, repfactors)
-    molecule = Frac(molecule, crystal.box)
-    charged_system = has_charges(crystal) && has_charges(molecule)
-    ρ = crystal_density(crystal)
-    eparams = charged_system ? setup_Ewald_sum(crystal.box, sqrt(ljforcefield.r²_cutoff);
-                                               ϵ=ewald_precision, verbose=verbose) : nothing
-    sys = GPUSystem(ctx, crystal, molecule, ljforcefield; eparams=eparams, refine_tail=refine_tail)
-    blocks = widom_blocks(sys, nb_insertions_per_block, temperature; seed=seed)
+    supercell = replicate(crystal, repfactors)
+    guest = Frac(molecule, supercell.box)
+    charged = has_charges(supercell) && has_charges(guest)
+    ρ = crystal_density(supercell)
+    ep = charged ? setup_Ewald_sum(supercell.box, sqrt(ljforcefield.r²_cutoff); ϵ=ewald_precision,
+                                   verbose=verbose) : nothing
+    sys = GPUSystem(ctx, supercell, guest, ljforcefield; eparams=ep, refine_tail=refine_tail)
+    if !isnothing(accessibility_grid)
+        verbose && println("Using provided accessibility grid to block inaccessible pockets")
+        set_accessibility!(sys, accessibility_grid, repfactors)
+    end
+    blocks = widom_blocks(sys, n_per_block, temperature; seed=seed)
 
-    henry_coefficients = exp.(blocks[1, :] .- log(PorousMaterials.UNIV_GAS_CONST * temperature *
-                                                    nb_insertions_per_block))
-    avg_vdw = blocks[2, :]
-    avg_es = charged_system ? blocks[3, :] : zeros(N_BLOCKS)
-    err_kh = 2.0 * std(henry_coefficients) / sqrt(N_BLOCKS)
-    err_vdw = 2.0 * std(avg_vdw) / sqrt(N_BLOCKS)
-    err_es = 2.0 * std(avg_es) / sqrt(N_BLOCKS)
-    K_TO_KJ = PorousMaterials.K_TO_KJ_PER_MOL
-
-    results = Dict{String, Any}()
-    results["henry coefficient [mol/(m³-bar)]"] = mean(henry_coefficients)
-    results["xtal"] = crystal.name
-    results["henry coefficient [mmol/(g-bar)]"] = results["henry coefficient [mol/(m³-bar)]"] / ρ
-    results["err henry coefficient [mmol/(g-bar)]"] = err_kh / ρ
-    results["henry coefficient [mol/(kg-Pa)]"] = results["henry coefficient [mmol/(g-bar)]"] / 100000.0
-    results["⟨U, vdw⟩ (K)"] = mean(avg_vdw)
-    results["⟨U, es⟩ (K)"] = mean(avg_es)
-    results["⟨U⟩ (K)"] = results["⟨U, vdw⟩ (K)"] + results["⟨U, es⟩ (K)"]
-    results["⟨U⟩ (kJ/mol)"] = results["⟨U⟩ (K)"] * K_TO_KJ
-    results["⟨U, vdw⟩ (kJ/mol)"] = results["⟨U, vdw⟩ (K)"] * K_TO_KJ
-    results["err ⟨U, vdw⟩ (kJ/mol)"] = err_vdw * K_TO_KJ
-    results["⟨U, es⟩ (kJ/mol)"] = results["⟨U, es⟩ (K)"] * K_TO_KJ
-    results["err ⟨U, es⟩ (kJ/mol)"] = err_es * K_TO_KJ
-    results["Qst (kJ/mol)"] = -results["⟨U⟩ (kJ/mol)"] + temperature * K_TO_KJ
-    results["err Qst (kJ/mol)"] = (err_vdw + err_es) * K_TO_KJ
-    results["elapsed time (min)"] = (time() - time_start) / 60
+    # per block: K_H = Σ e^{-U/T} / (R T n), ⟨U⟩ weighted by e^{-U/T}; errors 2σ/√N_BLOCKS
+    R = PorousMaterials.UNIV_GAS_CONST
+    kh = exp.(blocks[1, :] .- log(R * temperature * n_per_block))
+    u_vdw = blocks[2, :]
+    u_es = charged ? blocks[3, :] : zeros(N_BLOCKS)
+    two_se(v) = 2.0 * std(v) / sqrt(N_BLOCKS)
+    kj = PorousMaterials.K_TO_KJ_PER_MOL
+    kh_molar = mean(kh)
+    kh_mass = kh_molar / ρ
+    uv, ue = mean(u_vdw), mean(u_es)
+    results = Dict{String, Any}(
+        "xtal" => supercell.name,
+        "henry coefficient [mol/(m³-bar)]" => kh_molar,
+        "henry coefficient [mmol/(g-bar)]" => kh_mass,
+        "err henry coefficient [mmol/(g-bar)]" => two_se(kh) / ρ,
+        "henry coefficient [mol/(kg-Pa)]" => kh_mass / 100000.0,
+        "⟨U, vdw⟩ (K)" => uv,
+        "⟨U, es⟩ (K)" => ue,
+        "⟨U⟩ (K)" => uv + ue,
+        "⟨U⟩ (kJ/mol)" => (uv + ue) * kj,
+        "⟨U, vdw⟩ (kJ/mol)" => uv * kj,
+        "err ⟨U, vdw⟩ (kJ/mol)" => two_se(u_vdw) * kj,
+        "⟨U, es⟩ (kJ/mol)" => ue * kj,
+        "err ⟨U, es⟩ (kJ/mol)" => two_se(u_es) * kj,
+        "Qst (kJ/mol)" => -(uv + ue) * kj + temperature * kj,
+        "err Qst (kJ/mol)" => (two_se(u_vdw) + two_se(u_es)) * kj,
+        "elapsed time (min)" => (time() - t0) / 60)
     if autosave
-        isdir(rc[:paths][:simulations]) || mkdir(rc[:paths][:simulations])
-        savename = joinpath(rc[:paths][:simulations],
-                            henry_result_savename(crystal, molecule, temperature, ljforcefield,
-                                                  insertions_per_volume, comment=filename_comment))
-        @save savename results
-        verbose && println("\tResults saved in: ", savename)
+        dir = rc[:paths][:simulations]
+        isdir(dir) || mkdir(dir)
+        file = joinpath(dir, henry_result_savename(supercell, molecule, temperature, ljforcefield,
+                                                   insertions_per_volume, comment=filename_comment))
+        @save file results
+        verbose && println("\tResults saved in: ", file)
     end
     if verbose
-        for key in ["henry coefficient [mmol/(g-bar)]", "⟨U, vdw⟩ (kJ/mol)", "⟨U, es⟩ (kJ/mol)", "Qst (kJ/mol)"]
-            @printf("\t%s = %f +/- %f\n", key, results[key], results["err " * key])
+        for (name, v, err) in (("henry coefficient [mmol/(g-bar)]", kh_mass, two_se(kh) / ρ),
+                               ("⟨U, vdw⟩ (kJ/mol)", uv * kj, two_se(u_vdw) * kj),
+                               ("⟨U, es⟩ (kJ/mol)", ue * kj, two_se(u_es) * kj),
+                               ("Qst (kJ/mol)", results["Qst (kJ/mol)"], results["err Qst (kJ/mol)"]))
+            @printf("\t%s = %f +/- %f\n", name, v, err)
         end
     end
     return results
 end
 
 """
-Drop-in for `energy_grid` (src/grid.jl:291-362) with a single-site probe (no rotations).
+    set_accessibility!(sys, grid, repfactors)
+
+pmgb_system_set_accessibility: gate this system's Widom insertions by a `Grid{Bool}` over the unit
+cell (src/henry.jl:225 -> accessible, src/grid.jl:778-836); `repfactors` is the replication of the
+system's supercell.
+"""
+function set_accessibility!(sys::GPUSystem, grid::Grid{Bool}, repfactors)
+    data = UInt8.(grid.data)        # column-major, i fastest: the ABI's layout
+    check(sys.ctx, ccall((:pmgb_system_set_accessibility, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{Int32}, Ptr{Int32}, Ptr{UInt8}),
+        sys.ptr, Int32[size(data)...], Int32[repfactors...], data))
+end
+
+"""
+Drop-in for `energy_grid` (src/grid.jl:291-362): the same arguments and keywords.  A single-site
+probe gets its van der Waals energy at every point (pmgb_energy_grid, exact to the FP64 tolerance).
+A probe with several sites (or charges) gets the Boltzmann-weighted rotational average
+-T log(⟨e^{-U/T}⟩) over `n_rotations` uniform random orientations at `temperature`
+(pmgb_energy_grid_rotational), with the electrostatic energy included where both the crystal and the
+probe are charged, as the reference's rotational branch defines it.
 """
 function energy_grid(crystal::Crystal, molecule::Molecule{Cart}, ljforcefield::LJForceField;
-                     resolution::Union{Float64, Tuple{Int, Int, Int}}=1.0, units::Symbol=:kJ_mol,
-                     center::Bool=false, verbose::Bool=true, ctx::Context=default_context())
+                     resolution::Union{Float64, Tuple{Int, Int, Int}}=1.0, n_rotations::Int=1000,
+                     temperature::Float64=NaN, units::Symbol=:kJ_mol, center::Bool=false,
+                     verbose::Bool=true, seed::UInt64=rand(UInt64), ctx::Context=default_context())
     assert_P1_symmetry(crystal)
     units in (:kJ_mol, :K) || error("Pass :kJ_mol or :K for units of kJ/mol or K, respectively.")
-    needs_rotations(molecule) && error("the GPU energy grid takes single-site probes")
+    rotations = needs_rotations(molecule)
+    if rotations && isnan(temperature)
+        error("Must pass temperature (K) for Boltzmann weighted rotations.\n")
+    end
     n_pts = isa(resolution, Tuple{Int, Int, Int}) ? resolution : required_n_pts(crystal.box, resolution)
     repfactors = replication_factors(crystal.box, ljforcefield)
-    sc = replicate(crystal, repfactors)
-    sys = GPUSystem(ctx, sc, Frac(molecule, sc.box), ljforcefield)
-    factor = units == :kJ_mol ? PorousMaterials.K_TO_KJ_PER_MOL : 1.0
-    data = Array{Float32}(undef, n_pts...)     # column-major: i fastest, as the ABI writes
-    check(ctx, ccall((:pmgb_energy_grid, LIB), Cint,
-        (Ptr{Cvoid}, Ptr{Int32}, Ptr{Int32}, Float64, Ptr{Float32}),
-        sys.ptr, Int32[n_pts...], Int32[repfactors...], factor, data))
+    supercell = replicate(crystal, repfactors)
+    guest = Frac(molecule, supercell.box)
+    factor = units == :kJ_mol ? 8.314 / 1000.0 : 1.0     # the factor src/grid.jl:357-359 applies
+    data = Array{Float32}(undef, n_pts...)                # column-major: i fastest, as the ABI writes
+    if rotations
+        charged = has_charges(supercell) && has_charges(guest)
+        ep = charged ? setup_Ewald_sum(supercell.box, sqrt(ljforcefield.r²_cutoff); verbose=verbose) : nothing
+        sys = GPUSystem(ctx, supercell, guest, ljforcefield; eparams=ep)
+        check(ctx, ccall((:pmgb_energy_grid_rotational, LIB), Cint,
+            (Ptr{Cvoid}, Ptr{Int32}, Ptr{Int32}, Int32, Float64, UInt64, Float64, Ptr{Float32}),
+            sys.ptr, Int32[n_pts...], Int32[repfactors...], n_rotations, temperature, seed, factor, data))
+    else
+        sys = GPUSystem(ctx, supercell, guest, ljforcefield)
+        check(ctx, ccall((:pmgb_energy_grid, LIB), Cint,
+            (Ptr{Cvoid}, Ptr{Int32}, Ptr{Int32}, Float64, Ptr{Float32}),
+            sys.ptr, Int32[n_pts...], Int32[repfactors...], factor, data))
+    end
     return Grid(crystal.box, n_pts, Float64.(data), units,
                 center ? crystal.box.f_to_c * [-0.5, -0.5, -0.5] : [0.0, 0.0, 0.0])
 end
@@ -323,7 +374,7 @@ K_H (mol/(m³ bar)) of every crystal from one persistent, graph-captured launch
 """
 function henry_screen(crystals::Vector{Crystal}, molecule::Molecule, temperature::Float64, ljff::LJForceField;
                       insertions::Int=20_000, seed::Integer=0, tune::Bool=true, ewald_precision=1e-6,
-                      ctx::Context=default_context(), refine_tail::Float64=1e-3)
+                      ctx::Context=default_context(), refine_tail::Float64=1e-3, return_energies::Bool=false)
     nb = cld(insertions, N_BLOCKS)
     systems = GPUSystem[]
     for cr in crystals

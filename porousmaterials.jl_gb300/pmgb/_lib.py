@@ -52,6 +52,7 @@ SIGNATURES = [
     ("pmgb_system_centre_image", C.c_int, [_vp, C.POINTER(C.c_int32)]),
     ("pmgb_system_set_accessibility", C.c_int, [_vp, _ip, _ip, C.POINTER(C.c_uint8)]),
     ("pmgb_system_set_refine", C.c_int, [_vp, C.c_double]),
+    ("pmgb_system_set_exact", C.c_int, [_vp, C.c_int32]),
     ("pmgb_system_refined_count", C.c_int, [_vp, C.POINTER(C.c_int64)]),
     ("pmgb_widom", C.c_int, [_vp, C.c_int64, C.c_int32, C.c_uint64, C.c_double, _dp, _dp]),
     ("pmgb_widom_device", C.c_int, [_vp, C.c_int64, C.c_int32, C.c_uint64, C.c_double, _vp, _vp]),
@@ -65,6 +66,7 @@ SIGNATURES = [
     ("pmgb_sample_poses", C.c_int, [_vp, C.c_uint64, C.c_int64, C.c_int64, _fp, _fp]),
     ("pmgb_energy_grid", C.c_int, [_vp, _ip, _ip, C.c_double, _fp]),
     ("pmgb_energy_grid_device", C.c_int, [_vp, _ip, _ip, C.c_double, _vp]),
+    ("pmgb_energy_grid_rotational", C.c_int, [_vp, _ip, _ip, C.c_int32, C.c_double, C.c_uint64, C.c_double, _fp]),
     ("pmgb_batch_create", C.c_int, [_vp, C.c_int32, C.POINTER(_vp), C.POINTER(C.c_int64), C.c_int32, C.c_int32,
                                      C.POINTER(_vp)]),
     ("pmgb_batch_destroy", None, [_vp]),

@@ -7,6 +7,7 @@ accessibility lookup (:778-836).
 from __future__ import annotations
 
 import math
+import secrets
 from dataclasses import dataclass
 from pathlib import Path
 
@@ -92,30 +93,43 @@ def _units(units) -> str:
 
 def energy_grid(crystal: Crystal, molecule: Molecule, ljforcefield: LJForceField, *, resolution=1.0,
                 n_rotations: int = 1000, temperature: float = float("nan"), units="kJ_mol", center: bool = False,
-                verbose: bool = True) -> Grid:
-    """Potential energy of a single-site probe on a regular fractional grid of the unit
-    cell (endpoints included), in kJ/mol (×8.314/1000) or K; FP32 data."""
+                verbose: bool = True, seed: int | None = None) -> Grid:
+    """Potential energy of a probe on a regular fractional grid of the unit cell (endpoints
+    included), in kJ/mol (×8.314/1000) or K; FP32 data (src/grid.jl:291-362).  A single-site
+    probe gets its van der Waals energy; a probe that needs rotations gets -T log⟨e^{-U/T}⟩ over
+    n_rotations random orientations at `temperature`, with the Ewald energy included when crystal
+    and probe are charged (pmgb_energy_grid_rotational; `seed` fixes the orientations)."""
     assert_P1_symmetry(crystal)
     units = _units(units)
     n_pts = tuple(int(v) for v in resolution) if isinstance(resolution, (tuple, list)) else \
         required_n_pts(crystal.box, float(resolution))
-    if needs_rotations(molecule):
-        if math.isnan(temperature):
-            raise ValueError("Must pass temperature (K) for Boltzmann weighted rotations.")
-        raise NotImplementedError("energy grids of multi-site probes (rotational Boltzmann averages) are not "
-                                  "supported by pmgb")
+    rotations = needs_rotations(molecule)
+    if rotations and math.isnan(temperature):
+        raise ValueError("Must pass temperature (K) for Boltzmann weighted rotations.")
     origin = crystal.box.f_to_c @ np.array([-0.5, -0.5, -0.5]) if center else np.zeros(3)
     if verbose:
         print(f"Computing energy grid of {molecule.species} in {crystal.name}")
         print(f"\tRegular grid (in fractional space) of {n_pts[0]} by {n_pts[1]} by {n_pts[2]} points "
               f"superimposed over the unit cell.")
+        if rotations:
+            print(f"\t{n_rotations} molecule rotations per grid point with temperature {temperature:f} K.")
     box = crystal.box
-    fmol = Frac(molecule, box)
     repfactors = replication_factors(box, ljforcefield)
     sc = replicate(crystal, repfactors)
-    system = GPUSystem(sc, Frac(molecule, sc.box), ljforcefield, None)
-    data = system.energy_grid(n_pts, repfactors, KJ_PER_MOL_FACTOR if units == "kJ_mol" else 1.0)
-    del fmol
+    factor = KJ_PER_MOL_FACTOR if units == "kJ_mol" else 1.0
+    if rotations:
+        from .crystal import has_charges
+        from .ewald import setup_Ewald_sum
+
+        charged = has_charges(sc) and molecule.n_charges > 0
+        ep = setup_Ewald_sum(sc.box, ljforcefield.r_cutoff, verbose=verbose and charged) if charged else None
+        system = GPUSystem(sc, Frac(molecule, sc.box), ljforcefield, ep)
+        if seed is None:
+            seed = secrets.randbits(63)
+        data = system.energy_grid_rotational(n_pts, repfactors, n_rotations, temperature, seed, factor)
+    else:
+        system = GPUSystem(sc, Frac(molecule, sc.box), ljforcefield, None)
+        data = system.energy_grid(n_pts, repfactors, factor)
     return Grid(box, n_pts, np.ascontiguousarray(data), units, origin)
 
 

@@ -144,6 +144,11 @@ class GPUSystem:
         self.ctx.check(self.ctx._lib.pmgb_system_set_accessibility(self.handle, ptr(n, C.c_int32), ptr(r, C.c_int32),
                                                                    ptr(flat, C.c_uint8)))
 
+    def set_exact(self, on: bool) -> None:
+        """Exact single-configuration energies and grids (pmgb_system_set_exact; default on):
+        every energy within 1e-5 relative or 1e-4 K of the FP64 reference.  Off: FP32 only."""
+        self.ctx.check(self.ctx._lib.pmgb_system_set_exact(self.handle, int(bool(on))))
+
     def set_cull(self, on: bool) -> None:
         """Spatially ordered evaluation with cutoff culling (pmgb_system_set_cull; default on)."""
         self.ctx.check(self.ctx._lib.pmgb_system_set_cull(self.handle, int(bool(on))))
@@ -225,6 +230,17 @@ class GPUSystem:
         self.ctx.check(self.ctx._lib.pmgb_energy_grid(self.handle, ptr(n, C.c_int32), ptr(r, C.c_int32),
                                                       float(unit_factor), ptr(out, C.c_float)))
         return out.reshape(tuple(int(v) for v in n[::-1])).transpose(2, 1, 0)  # data[i, j, k], i fastest
+
+    def energy_grid_rotational(self, n_pts, repfactors, n_rotations: int, temperature: float, seed: int,
+                               unit_factor: float) -> np.ndarray:
+        """-T log⟨e^{-U/T}⟩ over n_rotations orientations at each grid point (pmgb_energy_grid_rotational)."""
+        n = np.ascontiguousarray(n_pts, dtype=np.int32)
+        r = np.ascontiguousarray(repfactors, dtype=np.int32)
+        out = np.zeros(int(np.prod(n)), dtype=np.float32)
+        self.ctx.check(self.ctx._lib.pmgb_energy_grid_rotational(
+            self.handle, ptr(n, C.c_int32), ptr(r, C.c_int32), int(n_rotations), float(temperature), int(seed),
+            float(unit_factor), ptr(out, C.c_float)))
+        return out.reshape(tuple(int(v) for v in n[::-1])).transpose(2, 1, 0)
 
     def close(self) -> None:
         if getattr(self, "handle", None):

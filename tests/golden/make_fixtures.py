@@ -59,8 +59,55 @@ GOLDEN = {
 }
 
 
+# the drop-in functions whose signatures the bindings mirror: (name, reference source file)
+DROP_INS = [("henry_coefficient", "src/henry.jl"), ("energy_grid", "src/grid.jl")]
+
+
+def _signature(path: Path, name: str) -> dict:
+    """Positional argument and keyword names of `function name(...)` in a reference source file,
+    with the file:line range of the signature."""
+    import re
+
+    lines = path.read_text().splitlines()
+    start = next(i for i, ln in enumerate(lines) if re.match(rf"\s*function {name}\(", ln))
+    text, depth, end = "", 0, start
+    for end in range(start, len(lines)):
+        for ch in lines[end]:
+            if ch == "(":
+                depth += 1
+            elif ch == ")":
+                depth -= 1
+            text += ch
+            if depth == 0 and text.count("(") > 0:
+                break
+        if depth == 0 and "(" in text:
+            break
+        text += " "
+    inner = text[text.index("(") + 1:text.rindex(")")]
+    pos, _, kw = inner.partition(";")
+
+    def names(part):
+        out, depth, cur = [], 0, ""
+        for ch in part + ",":
+            if ch in "({[":
+                depth += 1
+            elif ch in ")}]":
+                depth -= 1
+            if ch == "," and depth == 0:
+                if cur.strip():
+                    out.append(re.match(r"\s*([A-Za-z_][A-Za-z_0-9!²]*)", cur).group(1))
+                cur = ""
+            else:
+                cur += ch
+        return out
+
+    rel = path.relative_to(REF)
+    return {"cite": f"{rel}:{start + 1}-{end + 1}", "positional": names(pos), "keywords": names(kw)}
+
+
 def main():
     OUT.mkdir(parents=True, exist_ok=True)
+    GOLDEN["drop_in_signatures"] = {name: _signature(REF / src, name) for name, src in DROP_INS}
     td = REF / "test" / "data"
     for sub, names in FILES.items():
         (OUT / sub).mkdir(exist_ok=True)

@@ -57,6 +57,7 @@ def test_culled_grid_is_bit_identical(n_pts):
     rep = pmgb.replication_factors(cr.box, ff)
     sc = pmgb.replicate(cr, rep)
     gs = pmgb.GPUSystem(sc, pmgb.Frac(synthetic.xe(), sc.box), ff)
+    gs.set_exact(False)  # the FP32 grid kernels themselves, ordered and unordered
     gs.set_cull(False)
     g0 = gs.energy_grid(n_pts, rep, 1.0)
     gs.set_cull(True)
@@ -83,12 +84,14 @@ def test_culled_adjoint_is_bit_identical(case, want_grad):
         np.testing.assert_array_equal(a1[key], a0[key])
 
 
-def test_culled_grid_adjoint_is_bit_identical():
+@pytest.mark.parametrize("exact", [True, False])
+def test_culled_grid_adjoint_is_bit_identical(exact):
     cr = synthetic.config0()
     ff = synthetic.forcefield()
     rep = pmgb.replication_factors(cr.box, ff)
     sc = pmgb.replicate(cr, rep)
     gs = pmgb.GPUSystem(sc, pmgb.Frac(synthetic.xe(), sc.box), ff)
+    gs.set_exact(exact)
     res = []
     for cull in (False, True):
         gs.set_cull(cull)

@@ -1,6 +1,8 @@
-"""Latency path for Monte Carlo moves: pmgb_energies with up to 64 configurations (one CTA
-each) and the graph-captured pmgb_move_* evaluator, against the FP64 oracle with the FP32
-error model of the parity tests (per-term 4e-6 x the sum of term magnitudes + 1e-4 K), and
+"""Latency path for Monte Carlo moves: pmgb_energies with up to 64 configurations and the
+graph-captured pmgb_move_* evaluator, against the FP64 oracle.  With exact energies (the
+default) every configuration is evaluated in double-float and must meet 1e-5 relative or
+1e-4 K; the FP32 latency kernel (one CTA per configuration, exact energies off) is checked with
+the FP32 error model of the parity tests (4e-6 x the sum of term magnitudes + 1e-4 K) and
 against the many-configuration kernel."""
 from __future__ import annotations
 
@@ -10,7 +12,7 @@ import numpy as np
 import pytest
 
 import pmgb
-from pm_helpers import oracle_for, random_configs
+from pm_helpers import oracle_for, random_configs, within
 from pmgb import synthetic
 
 pytestmark = pytest.mark.gpu
@@ -24,38 +26,47 @@ def _system(cr, mol, charged):
     return pmgb.GPUSystem(sc, pmgb.Frac(mol, sc.box), ff, ep)
 
 
+@pytest.mark.parametrize("exact", [True, False])
 @pytest.mark.parametrize("case", ["co2_ewald", "ch4"])
-def test_latency_path_matches_oracle(case):
+def test_latency_path_matches_oracle(case, exact):
     gs = _system(synthetic.config1(), synthetic.co2(), True) if case == "co2_ewald" else \
         _system(synthetic.config0(), synthetic.ch4(), False)
+    gs.set_exact(exact)
     sites, lj, q = random_configs(gs, 64, seed=71)
-    small = gs.energies(sites)                       # 64 configurations: latency kernel
+    small = gs.energies(sites)                       # 64 configurations: latency kernel (FP32 pass)
     big = gs.energies(np.concatenate([sites, sites[:1]]))[:64]  # 65: the many-configuration kernel
     o = oracle_for(gs)
     if gs.charged:
         v, sr, lr, sv, ss = o.energies(lj, q, charged=True, use_sk=True, scales=True)
     else:
         v, sr, lr, sv, ss = o.energies(lj, scales=True)
+        lr = np.zeros_like(v)
     for gpu in (small, big):
         assert np.array_equal(np.isinf(gpu[:, 0]), np.isinf(v))
         fin = np.isfinite(v)
+        if exact:
+            assert within(gpu[fin].sum(axis=1), (v + sr + lr)[fin], 1e-5, ATOL).all()
+            assert within(gpu[fin, 0], v[fin], 1e-5, ATOL).all()
+            continue
         assert np.all(np.abs(gpu[fin, 0] - v[fin]) <= TOL * sv[fin] + ATOL)
         if gs.charged:
             assert np.all(np.abs(gpu[:, 1] - sr) <= TOL * ss + ATOL)
-    if gs.charged:
+    if gs.charged and not exact:
         # reciprocal space: the same FP32 recurrence, rows split over threads instead of one thread
         # per configuration (checked against the oracle with its own error scale in the parity tests)
         assert np.all(np.abs(small[:, 2] - big[:, 2]) <= 2e-3 + 1e-6 * np.abs(big[:, 2]))
 
 
-def test_move_evaluator_matches_energies():
+@pytest.mark.parametrize("exact", [True, False])
+def test_move_evaluator_matches_energies(exact):
     gs = _system(synthetic.config1(), synthetic.co2(), True)
+    gs.set_exact(exact)
     sites, _, _ = random_configs(gs, 40, seed=72)
     ev = gs.move_evaluator(max_conf=8)
     ref = gs.energies(sites)
     for k in range(0, 40, 8):
         got = ev.energies(sites[k:k + 8])
-        np.testing.assert_array_equal(got, ref[k:k + 8])  # same kernel, same inputs
+        np.testing.assert_array_equal(got, ref[k:k + 8])  # same kernels, same inputs
     one = ev.energies(sites[3])
     np.testing.assert_array_equal(one[0], ref[3])
     with pytest.raises(pmgb.PMGBError, match="n_conf"):
@@ -69,5 +80,6 @@ def test_move_evaluator_matches_energies():
     for i in range(n):
         ev1.energies(sites[i % 40])
     dt = (time.perf_counter() - t) / n
-    print(f"[move] CO2 + Ewald in 7,200 sites: {dt * 1e6:.1f} us per single-configuration call")
+    print(f"[move] CO2 + Ewald in 7,200 sites ({'exact' if exact else 'FP32'}): {dt * 1e6:.1f} us per "
+          f"single-configuration call")
     assert gs.ctx.device_status() == 0
