@@ -49,8 +49,11 @@ REFINE_TAIL = 1e-3
 PAIR_DRAM_BYTES_PER_INSERTION = 0.59e6 / 1e5
 # kernels per Widom step: spatial order (count, scan, scatter), pairs, insertion-order partials,
 # block reduction, and the refinement's hist, cut, count, scan, scatter, FP64 energies (thread
-# and warp passes), correction
-LAUNCHES_PER_STEP = 14
+# pass, plan, warp pass), and the store, chunk re-form and block recombination of the results
+LAUNCHES_PER_STEP = 17
+
+
+ALL_LEGS = ("adjoint", "e2e", "porous", "batched", "config4", "moves", "config2", "cpu")
 
 
 def parse():
@@ -67,7 +70,24 @@ def parse():
     p.add_argument("--batch-insertions", type=int, default=20000, help="insertions per (framework, guest)")
     p.add_argument("--c4-insertions", type=int, default=10_000_000, help="insertions of the large-cell leg")
     p.add_argument("--skip-configs", action="store_true", help="omit the large-cell and energy-grid legs")
-    return p.parse_args()
+    p.add_argument("--legs", default="all",
+                   help="comma list of the legs beside the config1 workload to run: " + ",".join(ALL_LEGS) +
+                        " (default all; the skip flags remove legs from it)")
+    args = p.parse_args()
+    legs = set(ALL_LEGS) if args.legs == "all" else {x.strip() for x in args.legs.split(",") if x.strip()}
+    unknown = legs - set(ALL_LEGS)
+    if unknown:
+        p.error(f"unknown legs {sorted(unknown)}")
+    if args.skip_cpu:
+        legs.discard("cpu")
+    if args.skip_e2e:
+        legs -= {"e2e", "adjoint"}
+    if args.skip_configs:
+        legs -= {"porous", "config4", "config2", "moves"}
+    if args.batch_frameworks <= 0:
+        legs.discard("batched")
+    args.legs = legs
+    return args
 
 
 def workload():
@@ -331,10 +351,14 @@ def batched_leg(args, ctx, stream):
 
     t0 = time.perf_counter()
     fws = synthetic.batch_frameworks(args.batch_frameworks)
+    t_gen = time.perf_counter() - t0
     ff = synthetic.forcefield(12.5)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
     systems = build_systems(fws, synthetic.ch4(), ff, ctx=ctx) + build_systems(fws, synthetic.co2(), ff, ctx=ctx)
     for gs in systems:
         gs.set_refine(REFINE_TAIL)  # as the drop-in calls: K_H within 1e-6 of FP64
+    torch.cuda.synchronize()
     t_setup = time.perf_counter() - t0
     npb = max(1, args.batch_insertions // N_BLOCKS)
     n_ins = npb * N_BLOCKS * len(systems)
@@ -374,7 +398,11 @@ def batched_leg(args, ctx, stream):
         t_dropin = dropin(adjoint)
         plain(adjoint)  # warm-up: per-system scratch allocations
         t_plain = min(plain(adjoint) for _ in range(2))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         screen = BatchScreen(systems, npb, N_BLOCKS, with_adjoint=adjoint, ctx=ctx, refine_tail=REFINE_TAIL)
+        torch.cuda.synchronize()
+        t_create = time.perf_counter() - t0
         tuned_ms = screen.tune(1, T, repeats=2)
         info = screen.info()
         for w in range(args.warmup):
@@ -390,6 +418,7 @@ def batched_leg(args, ctx, stream):
             screen.results()
         t_batched = (time.perf_counter() - t) / k
         ms_dev = sum(a.elapsed_time(b) for a, b in ev) / k
+        refined = int(screen.refined_counts().sum())
         screen.close()
         key = "forward_plus_adjoint" if adjoint else "forward"
         out[key] = {"plain_dropin_insertions_per_s": n_ins / t_dropin, "plain_dropin_s": t_dropin,
@@ -397,20 +426,29 @@ def batched_leg(args, ctx, stream):
                     "plain_insertions_per_s": n_ins / t_plain, "plain_s": t_plain,
                     "batched_insertions_per_s": n_ins / t_batched, "batched_s": t_batched,
                     "batched_device_ms": ms_dev, "batched_device_insertions_per_s": n_ins / (ms_dev * 1e-3),
-                    "speedup_vs_plain": t_plain / t_batched, "tuned": {"n_ctas": info["n_ctas"],
+                    "speedup_vs_plain": t_plain / t_batched,
+                    "batch_create_s": t_create,
+                    "speedup_with_setup_both_sides": t_dropin / (t_setup + t_create + t_batched),
+                    "refined_insertions_per_run": refined, "refined_fraction": refined / n_ins,
+                    "tuned": {"n_ctas": info["n_ctas"],
                     "order": ["cost-descending", "by-system"][info["order"]], "ms": tuned_ms},
-                    "work_units": info["n_units"], "gpu_launches_per_run": 10}  # batch kernel, per-system reduction, 8 refinement kernels
+                    "work_units": info["n_units"], "gpu_launches_per_run": 17}
+        # spatial order (3), batch kernel, insertion-order partials, per-system reduction, 11 refinement kernels
     assert ctx.device_status() == 0
+    out["refined_fraction"] = out["forward_plus_adjoint"]["refined_fraction"]
     out.update({"systems": len(systems), "frameworks": len(fws), "guests": ["CH4", "CO2"],
                 "insertions_per_system": npb * N_BLOCKS, "insertions_per_run": n_ins,
                 "framework_sites": {"min": int(sizes.min()), "median": float(np.median(sizes)),
                                     "max": int(sizes.max()), "total": int(sizes.sum())},
-                "setup_s": t_setup,
+                "setup_s": t_setup, "framework_generation_s": t_gen,
                 "timing": "plain_dropin: wall clock of henry_coefficient(_gradient) per (framework, guest), "
                           "set-up included (one pass); plain: wall clock of the per-system loop over pre-built "
                           "systems (best of 2); batched: wall clock of launch + results per run over the same "
                           "pre-built systems, and CUDA events around the graph replay; setup_s: building the "
-                          "batch's systems once"})
+                          "batch's systems once (replication, Ewald parameters, pmgb_system_create, S(k)); "
+                          "speedup_with_setup_both_sides: the drop-in loop (which builds every system) over "
+                          "setup_s + batch_create_s + one batched run; framework_generation_s (the synthetic "
+                          "crystals themselves) is charged to neither side"})
     return out
 
 
@@ -567,10 +605,25 @@ def other_configs(args, ctx, stream, peak=None):
         return e0.elapsed_time(e1) / reps
 
     ff = synthetic.forcefield(12.5)
+    mol = synthetic.co2()
+    if "config4" in args.legs:
+        out["config4_large_ewald"] = config4_leg(args, ctx, ff, mol, timed, peak)
+    if "moves" in args.legs:
+        out["monte_carlo_move"] = moves_leg(ctx, ff, mol)
+    if "config2" in args.legs:
+        out["config2_energy_grid"] = config2_leg(ctx, ff, timed, peak)
+    assert ctx.device_status() == 0
+    return out
+
+
+def config4_leg(args, ctx, ff, mol, timed, peak):
+    """config4: refined, FP32-only and forward + adjoint Widom runs and the error against the oracle."""
+    import pmgb
+    from pmgb import synthetic
+
     cr = synthetic.config4()
     sc = pmgb.replicate(cr, pmgb.replication_factors(cr.box, ff))
     ep = pmgb.setup_Ewald_sum(sc.box, ff.r_cutoff, eps=1e-6)
-    mol = synthetic.co2()
     gs = pmgb.GPUSystem(sc, pmgb.Frac(mol, sc.box), ff, ep, ctx=ctx, refine_tail=REFINE_TAIL)
     npb = args.c4_insertions // N_BLOCKS
     n = npb * N_BLOCKS
@@ -582,7 +635,7 @@ def other_configs(args, ctx, stream, peak=None):
     gs.set_refine(REFINE_TAIL)
     err4 = widom_error(gs, ff, 4000, 44)
     fpi = flops_per_insertion(sc, mol, ep)
-    out["config4_large_ewald"] = {
+    return {
         "workload": "CO2 in a 20,000-atom 52x52x52 A cell, Ewald 1e-6", "framework_sites": sc.atoms.n,
         "kvectors": ep.n_kvecs, "insertions": n,
         "insertions_per_s": n / (ms_ref * 1e-3), "refined_insertions": refined,
@@ -601,30 +654,53 @@ def other_configs(args, ctx, stream, peak=None):
         "distances": "with centre_image, each record's minimum image is taken from the pose centre once and the "
                      "three sites subtract their offsets (every width of this cell exceeds 2 (cutoff + 1.16 A); "
                      "pmgb_system_set_centre_image; the per-site form differs by FP32 rounding only)"}
-    del gs
 
-    # Monte Carlo move latency: one configuration per call through the captured graph
+
+def moves_leg(ctx, ff, mol):
+    """Monte Carlo move latency: one configuration per call through the captured graph, with exact
+    energies (the default) and with the FP32 latency kernel."""
     import numpy as np
+
+    import pmgb
+    from pmgb import synthetic
 
     c1 = synthetic.config1()
     sc1 = pmgb.replicate(c1, pmgb.replication_factors(c1.box, ff))
     g1 = pmgb.GPUSystem(sc1, pmgb.Frac(mol, sc1.box), ff, pmgb.setup_Ewald_sum(sc1.box, ff.r_cutoff, eps=1e-6),
                         ctx=ctx)
-    ev = g1.move_evaluator(1)
     rng = np.random.default_rng(5)
     confs = rng.random((64, 1, 3)) + np.zeros((64, g1.n_sites, 3))  # rigid shifts of all sites
-    for c in confs[:16]:
-        ev.energies(c)
-    t0 = time.perf_counter()
-    for i in range(500):
-        ev.energies(confs[i % 64])
-    move_us = (time.perf_counter() - t0) / 500 * 1e6
-    ev.close()
-    out["monte_carlo_move"] = {
+
+    def latency():
+        ev = g1.move_evaluator(1)
+        for c in confs[:16]:
+            ev.energies(c)
+        t0 = time.perf_counter()
+        for i in range(500):
+            ev.energies(confs[i % 64])
+        dt = (time.perf_counter() - t0) / 500 * 1e6
+        ev.close()
+        return dt
+
+    exact_us = latency()
+    g1.set_exact(False)
+    fp32_us = latency()
+    return {
         "workload": "guest-host energy of one CO2 configuration in the config1 supercell (7,200 sites, Ewald)",
-        "us_per_call": move_us,
+        "us_per_call": exact_us, "fp32_us_per_call": fp32_us,
         "call": "GPUSystem.move_evaluator(1).energies (pmgb_move_energies: pinned staging, one graph replay, "
-                "synchronous)"}
+                "synchronous); us_per_call: exact energies (double-float, the default), fp32: the FP32 latency "
+                "kernel"}
+
+
+def config2_leg(ctx, ff, timed, peak):
+    """config2: the 96^3 Xe grid, exact and FP32-only, its counted-work roofline and its error."""
+    import ctypes as C
+
+    import torch
+
+    import pmgb
+    from pmgb import synthetic
 
     c0 = synthetic.config0()
     rep = pmgb.replication_factors(c0.box, ff)
@@ -653,7 +729,7 @@ def other_configs(args, ctx, stream, peak=None):
     # of the pairs inside the cutoff (n 4/3 pi rc^3 / V per point); no sub-chunk of this cell is skipped
     fpp = F_DIST * sc0.atoms.n + F_LJ_IN * sc0.atoms.n * (4.0 / 3.0 * math.pi * ff.r_cutoff ** 3 / sc0.box.Omega)
     tf = fpp * n_pts / (ms_fp32 * 1e-3) / 1e12
-    out["config2_energy_grid"] = {
+    return {
         "workload": "Xe over a 96^3 grid of config0 (424 atoms, 25.832 A cubic)", "points": n_pts,
         "points_per_s": n_pts / (ms_exact * 1e-3),
         "exact": "every point within 1e-5 relative or 1e-4 K of FP64: the FP32 pass with a per-point error "
@@ -672,8 +748,6 @@ def other_configs(args, ctx, stream, peak=None):
         "timing": "points_per_s and fp32_only: CUDA events around the device call (grid left on the device); "
                   "host_call and adjoint: the host call including the device-to-host copy of the grid (and "
                   "gradients)"}
-    assert ctx.device_status() == 0
-    return out
 
 
 def job_rate(ms_total: float, n_per_rank_step: int, steps: int, world: int, device="cpu"):
@@ -718,8 +792,8 @@ def ours(args, rank, world, local_rank):
     fp32_peak, peak_clocks = None, None
     if rank == 0:
         # the roofline denominator: the FFMA probe, best of three, with the SM clock it ran at
-        with ClockSampler(local_rank) as pclk:
-            fp32_peak = max(ctx.fp32_peak_tflops() for _ in range(3))
+        with ClockSampler(local_rank) as pclk:  # ~0.5 s of probes, so the sampler sees their clock
+            fp32_peak = max(ctx.fp32_peak_tflops(iters=65536) for _ in range(3))
         peak_clocks = pclk.summary()
     for w in range(args.warmup):
         step(10_000 + w)
@@ -767,8 +841,7 @@ def ours(args, rank, world, local_rank):
 
     # forward + adjoint in one pass (pmgb_widom_adjoint: energies, dK_H/d(eps, sigma, lambda))
     adj = None
-    if not args.skip_e2e:
-        import numpy as _np
+    if "adjoint" in args.legs:
         system.widom_adjoint(npb, N_BLOCKS, 7, T)  # warm-up (allocates its scratch)
         a_times = []
         for s in range(max(3, args.steps // 2)):
@@ -783,7 +856,7 @@ def ours(args, rank, world, local_rank):
 
     # end to end through the reference-facing call (host buffers, copies inside)
     e2e = None
-    if not args.skip_e2e:
+    if "e2e" in args.legs:
         ipv = n_ins / cr.box.Omega
         e_times = []
         ctx_default = pmgb.Context.default(local_rank)
@@ -805,14 +878,14 @@ def ours(args, rank, world, local_rank):
                "pmgb_system_create + pmgb_system_set_ewald + pmgb_widom)"}
 
     batched = None
-    if args.batch_frameworks > 0 and rank == 0:
+    if "batched" in args.legs and rank == 0:
         batched = batched_leg(args, ctx, stream)
     others = None
-    if not args.skip_configs and rank == 0:
+    if args.legs & {"config4", "moves", "config2"} and rank == 0:
         others = other_configs(args, ctx, stream, fp32_peak)
 
     porous = None
-    if not args.skip_configs and rank == 0:
+    if "porous" in args.legs and rank == 0:
         porous = porous_leg(args, ctx, stream, flush)
 
     if rank != 0:
@@ -822,7 +895,7 @@ def ours(args, rank, world, local_rank):
     fpi_in = flops_inside_cutoff(sc, mol, ff, ep, system.info()["n_kvecs_evaluated"])
     achieved = fpi_in * n_ins / (kernel_ms * 1e-3) / 1e12
     cpu = None
-    if not args.skip_cpu:
+    if "cpu" in args.legs:
         cpu = cpu_legs(sc, mol, ep, ff)
     summary = {"kh_max_rel_error": err1["kh_max_rel_error"] if err1 else None,
                "pair_kernel_frac_of_fp32_peak": achieved / fp32_peak if fp32_peak else None,
@@ -839,9 +912,10 @@ def ours(args, rank, world, local_rank):
                         "batched_vs_plain_prebuilt": fa["speedup_vs_plain"],
                         "batched_vs_plain_with_setup": fa.get("speedup_with_setup_both_sides"),
                         "batched_refined_fraction": batched.get("refined_fraction")})
-    if others:
-        summary.update({"config4_insertions_per_s": others["config4_large_ewald"]["insertions_per_s"],
-                        "config2_points_per_s": others["config2_energy_grid"]["points_per_s"]})
+    if others and "config4_large_ewald" in others:
+        summary["config4_insertions_per_s"] = others["config4_large_ewald"]["insertions_per_s"]
+    if others and "config2_energy_grid" in others:
+        summary["config2_points_per_s"] = others["config2_energy_grid"]["points_per_s"]
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "summary": summary,

@@ -92,6 +92,39 @@ int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9],
                        const double* guest_charge_q,
                        pmgb_system** out);
 
+/* ---- host-side set-up from a unit cell (no device work) ----------------------------------
+ * replication_factors(box, r_cutoff) (src/forcefield.jl:120-158): the smallest supercell whose
+ * perpendicular half-widths reach r_cutoff.  f_to_c is the unit cell (column-major). */
+int pmgb_replication_factors(const double f_to_c[9], double r_cutoff, int32_t rep_out[3]);
+
+/* setup_Ewald_sum(box, sr_cutoff; ϵ=precision) (src/electrostatics.jl:256-272 with
+ * determine_ewald_params :123-141, required_kreps :157-175, precompute_kvec_wts :198-232) for the
+ * supercell box f_to_c: α, |k|²_max, kreps and the k-vectors (ka, kb, kc) with their weights, in
+ * the reference's order.  The two precision conditions are solved by bisection on the reference's
+ * brackets.  *n_kvecs_out always receives the number of k-vectors; they are written when capacity
+ * holds them all (capacity 0: query the count only). */
+int pmgb_ewald_setup(const double f_to_c[9], double sr_cutoff, double precision, int64_t capacity,
+                     double* alpha_out, double* max_k2_out, int32_t kreps_out[3], int64_t* n_kvecs_out,
+                     int32_t* kvec_abc, double* kvec_wt);
+
+/* pmgb_system_create from the UNIT cell, with the rest of henry_coefficient's set-up done
+ * natively (src/henry.jl:78-97): the replication factors for r_cutoff, the replicated supercell
+ * (Xtals.replicate: images (i, j, k) with k fastest, coordinates (x + shift) / rep), and, when the
+ * framework and the guest are both charged, the Ewald parameters at ewald_precision
+ * (pmgb_ewald_setup) and pmgb_system_set_ewald.  The LJ cutoff is r_cutoff² and the short-range
+ * Ewald cutoff r_cutoff, as the reference sets both from the force field.  repfactors_out
+ * (optional) receives the replication.  Other arguments as pmgb_system_create. */
+int pmgb_system_create_unitcell(pmgb_ctx* ctx, const double f_to_c[9],
+                                int32_t n_atoms, const double* atom_xf, const int32_t* atom_species,
+                                int32_t n_charges, const double* charge_xf, const double* charge_q,
+                                int32_t n_species, const double* epsilon, const double* sigma2,
+                                double r_cutoff,
+                                int32_t n_guest_atoms, const double* guest_atom_x,
+                                const int32_t* guest_atom_species,
+                                int32_t n_guest_charges, const double* guest_charge_x,
+                                const double* guest_charge_q, double ewald_precision,
+                                int32_t repfactors_out[3], pmgb_system** out);
+
 /* Ewald parameters: EwaldParams (src/electrostatics.jl:54-63) as produced by
  * setup_Ewald_sum (src/electrostatics.jl:256-272): α, the short-range cutoff, and the
  * k-vectors (ka, kb, kc) with weights wt (precompute_kvec_wts, :198-232).  The

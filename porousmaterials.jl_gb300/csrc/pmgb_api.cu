@@ -289,6 +289,9 @@ inline uint32_t spread10(uint32_t v) {
 // ============================================================================
 // library / context
 // ============================================================================
+// the failure message of a context, for entry points defined in other translation units
+int pmgb_fail_message(pmgb_ctx* ctx, int code, const char* message) { return fail(ctx, code, "%s", message); }
+
 extern "C" int pmgb_abi_version(void) { return PMGB_ABI_VERSION; }
 
 extern "C" int pmgb_create(int device, pmgb_ctx** out) {
@@ -1495,6 +1498,7 @@ static int run_refine(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uin
         r.item_base = at_point->item_base;
     }
     r.block_out = block_out_dev;
+    r.partials = static_cast<LsePartial*>(s->partials.p);
     r.u = u_dev;
     r.hist = static_cast<unsigned long long*>(s->r_hist.p);
     r.cut = static_cast<int*>(s->r_cut.p);
@@ -2286,6 +2290,7 @@ int batch_capture(pmgb_batch* b) {
         r.n_blocks = b->n_blocks;
         r.tail = b->refine_tail;
         r.block_out = b->d_block_out;
+        r.partials = b->d_partials;
         r.u = b->d_u;
         r.hist = b->d_hist;
         r.cut = b->d_cut;

@@ -288,6 +288,7 @@ struct RefineArgs {
     int* one_chunk;                 // [1] set when the chunk-items would exceed cap_items
     int* done;                      // [cap_entries] chunks finished per refined insertion
     double* part;                   // [4 cap_items] chunk partials (U_vdw, U_sr / coul, U_lr, overlap)
+    LsePartial* partials;           // [chunks] the Widom pass's Boltzmann partials (re-formed where refined)
     long long cap_items, cap_entries;
     // where the entries' guest sites come from (REFINE_POSE_*): Widom poses, the caller's
     // explicit FP64 site coordinates, or energy-grid points of a single-site probe
@@ -359,6 +360,10 @@ cudaError_t pmgb_launch_rot_grid_out(const double* block_out, int n, double temp
 cudaError_t pmgb_launch_bounded_wait_test(unsigned int* status, unsigned long long limit_ns, int arm,
                                           cudaStream_t st);
 size_t pmgb_pairs_smem_bytes();
+
+// record a failure message on ctx and return code (defined in pmgb_api.cu)
+struct pmgb_ctx;
+int pmgb_fail_message(pmgb_ctx* ctx, int code, const char* message);
 
 // fixed per-device scratch of pmgb_widom_noalloc (defined in pmgb_kernels.cu)
 #define PMGB_NOALLOC_MAX_CTAS 65536   // LsePartial entries: 3 MiB, up to 16.7M insertions per call

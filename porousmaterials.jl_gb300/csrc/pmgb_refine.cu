@@ -15,10 +15,12 @@
 //      thread per insertion in FP64; the others are cut into chunks of records and k-space rows,
 //      one warp each, computing in double-float (hi + lo FP32 pairs, ~48 bits) on the FP32 pipes
 //      after an FP32 screen queues the pairs near the insertion;
-//   5. per block, the FP64 minus FP32 differences of e^{x}, U_vdw e^{x} and U_es e^{x}, added
-//      in index order to the block results; refined energies replace the FP32 ones in u.
+//   5. the refined insertions' FP64 energies replace the FP32 ones in u; the Boltzmann partials of
+//      the chunks holding them are formed again from u and their blocks' results recombined.
 // The unrefined remainder then contributes at most tail x (its largest FP32 error)/T to
 // log K_H.
+// The same double-float pass also serves the exact single-configuration energies: entries from
+// explicit FP64 coordinates (every configuration) or from screened energy-grid points.
 #include "pmgb_device.cuh"
 
 #include <algorithm>
@@ -848,73 +850,91 @@ __global__ void __launch_bounds__(PMGB_THREADS) refine_large_kernel(const __grid
     }
 }
 
-// Per (system, block): add the FP64 - FP32 differences of the refined insertions (index order)
-// to the block results and store the refined energies in u.
-__global__ void tail_correct_kernel(const __grid_constant__ RefineArgs a) {
+// The refined insertions' FP64 energies replace the FP32 ones in u (every block, grid-stride).
+__global__ void tail_store_kernel(const __grid_constant__ RefineArgs a, int n_ctas) {
+    const int n_ref = a.offsets[n_ctas];
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_ref; r += gridDim.x * blockDim.x) {
+        const long long e = a.list[r];
+        const long long base = a.systems ? a.systems[static_cast<int>(e >> 40)].u_base : 0;
+        const long long ui = base + (e & ((1ll << 40) - 1));
+        const double* f = a.ref_u + 3 * static_cast<size_t>(r);
+        a.u[2 * ui] = f[0];
+        a.u[2 * ui + 1] = f[1] + f[2];
+    }
+}
+
+// The Boltzmann partial of every chunk that holds refined insertions, formed again from u by the
+// FP32 pass's own CTA reduction (lse_cta); the other chunks keep theirs.  Forming the sums from
+// the energies, rather than adding FP64 - FP32 differences to them, stays exact where the FP32
+// pass erred by many kT (energies of ~1e11 K, where 1e-7 relative is hundreds of kT): there the
+// differences would cancel the whole sum.
+__global__ void __launch_bounds__(PMGB_THREADS) tail_rechunk_kernel(const __grid_constant__ RefineArgs a) {
+    __shared__ LsePartial red[PMGB_THREADS / 32];
+    if (a.counts[blockIdx.x] == 0) return;  // uniform over the CTA
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    const TailRef t = tail_locate(a, blockIdx.x, threadIdx.x);
+    double x = -inf, ev = 0.0, ee = 0.0;
+    long long ninf = 0;
+    if (t.valid) {
+        const double uv = a.u[2 * t.ui], ue = a.u[2 * t.ui + 1];
+        const double u = uv + ue;
+        if (isfinite(u)) {
+            x = -u * inv_temp(a);
+            ev = uv;
+            ee = ue;
+        } else {
+            ninf = 1;
+        }
+    }
+    lse_cta(x, ev, ee, ninf, red, a.partials + blockIdx.x, nullptr);
+}
+
+// Per (system, block) with refined insertions: its chunk partials combined in a fixed order, as
+// the FP32 pass's block reduction combines them (one warp per block).
+__global__ void tail_reblock_kernel(const __grid_constant__ RefineArgs a) {
     const int g = blockIdx.x;
     const int lane = threadIdx.x;
     const double inf = __longlong_as_double(0x7ff0000000000000ll);
-    const double inv_t = inv_temp(a);
+    const unsigned full = 0xffffffffu;
     int c0, cpb;
-    long long u_base = 0;
     if (a.systems) {
         const BatchSystem& bs = a.systems[g / a.n_blocks];
         cpb = bs.ctas_per_block;
         c0 = bs.chunk_first + (g % a.n_blocks) * cpb;
-        u_base = bs.u_base;
     } else {
         cpb = a.ctas_per_block;
         c0 = g * cpb;
     }
-    const int r0 = a.offsets[c0], r1 = a.offsets[c0 + cpb];
-    double* bo = a.block_out + 4 * g;
-    const double L = bo[0];
-    double ds = 0.0, dv = 0.0, de = 0.0;
-    long long dn = 0;
-    for (int r = r0 + lane; r < r1; r += 32) {
-        const long long ui = u_base + (a.list[r] & ((1ll << 40) - 1));
-        const double uv32 = a.u[2 * ui], ue32 = a.u[2 * ui + 1];
-        const double* f = a.ref_u + 3 * static_cast<size_t>(r);
-        const double uv64 = f[0], ue64 = f[1] + f[2];
-        const double x32 = -(uv32 + ue32) * inv_t;
-        const double x64 = -(uv64 + ue64) * inv_t;
-        const double w32 = exp(x32 - L);
-        if (isfinite(x64)) {
-            const double w64 = w32 * exp(x64 - x32);
-            ds += w32 * expm1(x64 - x32);
-            dv += uv64 * w64 - uv32 * w32;
-            de += ue64 * w64 - ue32 * w32;
-        } else {
-            ds -= w32;
-            dv -= uv32 * w32;
-            de -= ue32 * w32;
-            dn += 1;
-        }
-        a.u[2 * ui] = uv64;
-        a.u[2 * ui + 1] = ue64;
+    if (a.offsets[c0 + cpb] == a.offsets[c0]) return;  // no refined insertion: the FP32-pass results stand
+    const LsePartial* p = a.partials + c0;
+    double m = -inf;
+    for (int c = lane; c < cpb; c += 32) m = fmax(m, p[c].m);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(full, m, o));
+    double s = 0.0, tv = 0.0, te = 0.0;
+    long long n = 0;
+    for (int c = lane; c < cpb; c += 32) {
+        const LsePartial q = p[c];
+        const double f = (m == -inf || q.m == -inf) ? 0.0 : exp(q.m - m);
+        s += q.s * f;
+        tv += q.tv * f;
+        te += q.te * f;
+        n += q.n_inf;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        ds += __shfl_xor_sync(0xffffffffu, ds, o);
-        dv += __shfl_xor_sync(0xffffffffu, dv, o);
-        de += __shfl_xor_sync(0xffffffffu, de, o);
-        dn += __shfl_xor_sync(0xffffffffu, dn, o);
+        s += __shfl_xor_sync(full, s, o);
+        tv += __shfl_xor_sync(full, tv, o);
+        te += __shfl_xor_sync(full, te, o);
+        n += __shfl_xor_sync(full, n, o);
     }
-    if (lane == 0 && r1 > r0) {
-        // block_out = (L, <U_vdw>, <U_es>, n_inf) with sums relative to e^L equal to (1, <U_vdw>, <U_es>)
-        const double s = 1.0 + ds;
-        if (s > 0.0) {
-            bo[0] = L + log1p(ds);
-            bo[1] = (bo[1] + dv) / s;
-            bo[2] = (bo[2] + de) / s;
-        } else {
-            // every insertion of the block overlaps: the weighted means are 0/0, as the reference's
-            const double nan = __longlong_as_double(0x7ff8000000000000ll);
-            bo[0] = -inf;
-            bo[1] = nan;
-            bo[2] = nan;
-        }
-        bo[3] += static_cast<double>(dn);
+    if (lane == 0) {
+        // every insertion of the block overlapping gives -inf and 0/0 means, as the reference's
+        double* bo = a.block_out + 4 * g;
+        bo[0] = (s > 0.0) ? m + log(s) : -inf;
+        bo[1] = tv / s;
+        bo[2] = te / s;
+        bo[3] = static_cast<double>(n);
     }
 }
 
@@ -1027,7 +1047,9 @@ cudaError_t pmgb_launch_refine(const RefineArgs& a, int n_ctas, int n_sm, cudaSt
     refine_small_kernel<<<4 * n_sm, PMGB_THREADS, 0, st>>>(a, n_ctas);
     refine_plan_kernel<<<1, 1024, 0, st>>>(a, n_ctas);
     refine_large_kernel<<<4 * n_sm, PMGB_THREADS, 0, st>>>(a, n_ctas);
-    tail_correct_kernel<<<n_g, 32, 0, st>>>(a);
+    tail_store_kernel<<<4 * n_sm, 256, 0, st>>>(a, n_ctas);
+    tail_rechunk_kernel<<<n_ctas, PMGB_THREADS, 0, st>>>(a);
+    tail_reblock_kernel<<<n_g, 32, 0, st>>>(a);
     return cudaGetLastError();
 }
 

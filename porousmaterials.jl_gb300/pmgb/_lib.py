@@ -41,6 +41,12 @@ SIGNATURES = [
      [_vp, _dp, C.c_int32, _dp, _ip, C.c_int32, _dp, _dp, C.c_int32, _dp, _dp, C.c_double,
       C.c_int32, _dp, _ip, C.c_int32, _dp, _dp, C.POINTER(_vp)]),
     ("pmgb_system_set_ewald", C.c_int, [_vp, C.c_double, C.c_double, C.c_int32, _ip, _dp]),
+    ("pmgb_replication_factors", C.c_int, [_dp, C.c_double, _ip]),
+    ("pmgb_ewald_setup", C.c_int, [_dp, C.c_double, C.c_double, C.c_int64, _dp, _dp, _ip, C.POINTER(C.c_int64),
+                                   _ip, _dp]),
+    ("pmgb_system_create_unitcell", C.c_int,
+     [_vp, _dp, C.c_int32, _dp, _ip, C.c_int32, _dp, _dp, C.c_int32, _dp, _dp, C.c_double,
+      C.c_int32, _dp, _ip, C.c_int32, _dp, _dp, C.c_double, _ip, C.POINTER(_vp)]),
     ("pmgb_system_destroy", None, [_vp]),
     ("pmgb_system_info", C.c_int, [_vp, C.POINTER(C.c_int64)]),
     ("pmgb_system_n_sites", C.c_int, [_vp]),

@@ -145,13 +145,9 @@ def build_systems(crystals: list[Crystal], molecule: Molecule | list[Molecule], 
     """One GPUSystem per crystal (replicated for the cutoff, Ewald set up when both are charged)."""
     ctx = ctx or Context.default()
     mols = molecule if isinstance(molecule, (list, tuple)) else [molecule] * len(crystals)
-    out = []
-    for cr, mol in zip(crystals, mols):
-        sc = replicate(cr, replication_factors(cr.box, ljff))
-        charged = has_charges(sc) and mol.n_charges > 0
-        ep = setup_Ewald_sum(sc.box, ljff.r_cutoff, eps=ewald_precision) if charged else None
-        out.append(GPUSystem(sc, Frac(mol, sc.box), ljff, ep, ctx=ctx))
-    return out
+    # replication, supercell and Ewald set-up natively per framework (pmgb_system_create_unitcell)
+    return [GPUSystem.from_unit_cell(cr, mol, ljff, ewald_precision=ewald_precision, ctx=ctx)
+            for cr, mol in zip(crystals, mols)]
 
 
 def henry_coefficient_screen(crystals: list[Crystal], molecule: Molecule | list[Molecule], temperature: float,

@@ -21,19 +21,35 @@ from .system import GPUSystem
 K_TO_KJ = 8.314 / 1000.0  # energy_min.jl:49 (the grid factor, not R)
 
 
+N_CANDIDATES = 16  # lowest grid points re-evaluated at full precision before the argmin
+
+
 def find_energy_minimum_gridsearch(crystal: Crystal, molecule: Molecule, ljforcefield: LJForceField, *,
                                    resolution=1.0, n_pts=None):
     """(molecule at the lowest grid point (fractional), that energy in kJ/mol).  n_pts is the
-    keyword the reference's test passes (test/energy_min.jl:20); resolution is the function's."""
+    keyword the reference's test passes (test/energy_min.jl:20); resolution is the function's.
+
+    The grid holds FP32 values; the lowest N_CANDIDATES points are re-evaluated in double-float
+    (pmgb_energies, FP64-grade) and the minimum is taken over those values, the first in
+    column-major order on a tie, as Julia's findmin over an FP64 grid."""
     res = n_pts if n_pts is not None else resolution
     grid = energy_grid(crystal, molecule, ljforcefield, resolution=res, verbose=False, units="kJ_mol")
     data = np.asarray(grid.data)
-    # first minimum in column-major order, as Julia's findmin over the grid
-    idx = np.unravel_index(int(np.argmin(data.ravel(order="F"))), data.shape, order="F")
-    xf = id_to_xf(tuple(int(i) + 1 for i in idx), grid.n_pts)
+    flat = data.ravel(order="F")
+    k = min(N_CANDIDATES, flat.size)
+    cand = np.sort(np.argpartition(flat, k - 1)[:k])           # column-major order
+    ids = [np.unravel_index(int(c), data.shape, order="F") for c in cand]
+    xfs = np.array([id_to_xf(tuple(int(i) + 1 for i in idx), grid.n_pts) for idx in ids])
+    rep = replication_factors(crystal.box, ljforcefield)
+    sc = replicate(crystal, rep)
+    system = GPUSystem(sc, Frac(molecule, sc.box), ljforcefield, None)
+    ax, _ = _offsets(system)
+    sites = (np.mod(xfs, 1.0) / np.asarray(rep))[:, None, :] + ax[None, :, :]
+    e = system.energies(sites)[:, 0] * K_TO_KJ
+    best = int(np.argmin(np.where(np.isfinite(e), e, np.inf)))
     mol = Frac(molecule, crystal.box)
-    translate_to(mol, xf)
-    return mol, float(data[idx])
+    translate_to(mol, xfs[best])
+    return mol, float(e[best])
 
 
 def find_energy_minimum(crystal: Crystal, molecule: Molecule, ljforcefield: LJForceField, *, gtol: float = 1e-9,

@@ -92,14 +92,35 @@ def precompute_kvec_wts(kreps, box: Box, alpha: float, max_mag_k_sqrd: float = m
 
 
 def setup_Ewald_sum(box: Box, sr_cutoff_r: float, eps: float = 1e-6, verbose: bool = False) -> EwaldParams:
-    alpha, max_k2 = determine_ewald_params(sr_cutoff_r, eps)
-    kreps = required_kreps(box, max_k2)
-    abc, wt = precompute_kvec_wts(kreps, box, alpha, max_k2)
-    ep = EwaldParams(kreps, alpha, float(sr_cutoff_r), abc, wt)
+    """setup_Ewald_sum (src/electrostatics.jl:256-272) through the library's native set-up
+    (pmgb_ewald_setup): the steps of determine_ewald_params, required_kreps and
+    precompute_kvec_wts above, in C++, so that a screening loop does not pay interpreter time per
+    framework.  The library is loaded for this host-only call; no device work is done."""
+    import ctypes as C
+
+    from ._lib import PMGBError, lib
+
+    L = lib()
+    f = np.ascontiguousarray(box.f_to_c.T.reshape(-1))  # column-major
+    fp = f.ctypes.data_as(C.POINTER(C.c_double))
+    n = C.c_int64(0)
+    rc = L.pmgb_ewald_setup(fp, float(sr_cutoff_r), float(eps), 0, None, None, None, C.byref(n), None, None)
+    if rc != 0:
+        raise PMGBError(rc, "pmgb_ewald_setup: the box must be non-singular, the cutoff positive and the precision "
+                            "in (0, 1)")
+    abc = np.zeros((n.value, 3), dtype=np.int32)
+    wt = np.zeros(n.value, dtype=np.float64)
+    alpha, kr = C.c_double(0.0), (C.c_int32 * 3)()
+    rc = L.pmgb_ewald_setup(fp, float(sr_cutoff_r), float(eps), n.value, C.byref(alpha), None, kr, C.byref(n),
+                            abc.ctypes.data_as(C.POINTER(C.c_int32)), wt.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc != 0:
+        raise PMGBError(rc, "pmgb_ewald_setup failed")
+    kreps = (int(kr[0]), int(kr[1]), int(kr[2]))
+    ep = EwaldParams(kreps, float(alpha.value), float(sr_cutoff_r), abc, wt)
     if verbose:
         print("\tEwald summation parameters:")
         print(f"\t\tk-replication factors: {kreps[0]} {kreps[1]} {kreps[2]}")
-        print(f"\t\tEwald convergence param. α = {alpha:f}")
+        print(f"\t\tEwald convergence param. α = {ep.alpha:f}")
         print(f"\t\tshort-range cutoff radius (Å): {sr_cutoff_r:f}")
         print(f"\t\t{ep.n_kvecs} kvectors")
         print(f"\t\t(calculated with specified precision {eps:e})")

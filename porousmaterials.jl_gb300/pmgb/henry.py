@@ -86,15 +86,16 @@ def henry_coefficient(crystal: Crystal, molecule: Molecule, temperature: float, 
     if verbose:
         print(f"\tReplicating crystal {repfactors[0]} by {repfactors[1]} by {repfactors[2]} for short-range "
               f"cutoff {ljforcefield.r_cutoff:.2f}")
-    crystal = replicate(crystal, repfactors)
-    fmol = Frac(molecule, crystal.box)
     charged = has_charges(crystal) and molecule.n_charges > 0
-    rho = crystal_density(crystal, masses)
-    eparams = setup_Ewald_sum(crystal.box, ljforcefield.r_cutoff, eps=ewald_precision,
-                              verbose=verbose and charged) if charged else None
+    rho = crystal_density(crystal, masses)  # the supercell's density is the unit cell's
     if seed is None:
         seed = secrets.randbits(63)
-    system = GPUSystem(crystal, fmol, ljforcefield, eparams, refine_tail=refine_tail)
+    # replication, the supercell and the Ewald set-up natively (pmgb_system_create_unitcell)
+    system = GPUSystem.from_unit_cell(crystal, molecule, ljforcefield, ewald_precision=ewald_precision,
+                                      refine_tail=refine_tail)
+    assert system.repfactors == tuple(repfactors)
+    if verbose and charged:
+        setup_Ewald_sum(system.crystal.box, ljforcefield.r_cutoff, eps=ewald_precision, verbose=True)
     if accessibility_grid is not None:
         system.set_accessibility(accessibility_grid, repfactors)
     if system_out is not None:
@@ -175,13 +176,11 @@ def henry_coefficient_gradient(crystal: Crystal, molecule: Molecule, temperature
     temperature = float(temperature)
     nb_insertions = max(N_BLOCKS, math.ceil(insertions_per_volume * crystal.box.Omega))
     nb_per_block = math.ceil(nb_insertions / N_BLOCKS)
-    repfactors = replication_factors(crystal.box, ljforcefield)
-    sc = replicate(crystal, repfactors)
-    charged = has_charges(sc) and molecule.n_charges > 0
-    eparams = setup_Ewald_sum(sc.box, ljforcefield.r_cutoff, eps=ewald_precision) if charged else None
+    charged = has_charges(crystal) and molecule.n_charges > 0
     if seed is None:
         seed = secrets.randbits(63)
-    system = GPUSystem(sc, Frac(molecule, sc.box), ljforcefield, eparams, refine_tail=refine_tail)
+    system = GPUSystem.from_unit_cell(crystal, molecule, ljforcefield, ewald_precision=ewald_precision,
+                                      refine_tail=refine_tail)
     if system_out is not None:
         system_out.append(system)
     blocks, adj = system.widom_adjoint(nb_per_block, N_BLOCKS, seed, temperature, want_grad=want_forces)

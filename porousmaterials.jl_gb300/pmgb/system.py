@@ -75,6 +75,77 @@ class GPUSystem:
         if refine_tail:
             self.set_refine(refine_tail)
 
+    @classmethod
+    def from_unit_cell(cls, crystal: Crystal, molecule: Molecule, ljff: LJForceField, *,
+                       ewald_precision: float = 1e-6, ctx: Context | None = None,
+                       refine_tail: float = 0.0) -> "GPUSystem":
+        """The system henry_coefficient sets up from a UNIT cell (src/henry.jl:78-97), built natively
+        by pmgb_system_create_unitcell: replication for the cutoff, the replicated supercell and, when
+        framework and guest are charged, the Ewald parameters at ewald_precision.  The supercell
+        `crystal`, the guest in its fractions `molecule` and the `eparams` are built on the host only
+        if a caller reads them."""
+        self = cls.__new__(cls)
+        self.ctx = ctx or Context.default()
+        self.ljff = ljff
+        self._unit = crystal
+        self._ewald_precision = float(ewald_precision)
+        self._guest = molecule
+        species = list(dict.fromkeys([*dict.fromkeys(crystal.atoms.species), *molecule.atom_species]))
+        self.species = species
+        sid = {s_: i for i, s_ in enumerate(species)}
+        eps, sig2 = ljff.tables(species)
+        self._eps = np.ascontiguousarray(eps)
+        self._sig2 = np.ascontiguousarray(sig2)
+        atom_xf = np.ascontiguousarray(crystal.atoms.xf, dtype=np.float64)
+        atom_sp = np.fromiter(map(sid.__getitem__, crystal.atoms.species), dtype=np.int32,
+                              count=len(crystal.atoms.species))
+        q_xf = np.ascontiguousarray(crystal.charges.xf, dtype=np.float64)
+        q = np.ascontiguousarray(crystal.charges.q, dtype=np.float64)
+        f_to_c = np.ascontiguousarray(crystal.box.f_to_c.T.reshape(-1))  # column-major
+        ax, qx = body_offsets(molecule, crystal.box)
+        self._gax = np.ascontiguousarray(ax, dtype=np.float64)
+        self._gsp = np.ascontiguousarray([sid[s_] for s_ in molecule.atom_species], dtype=np.int32)
+        self._gqx = np.ascontiguousarray(qx, dtype=np.float64)
+        self._gq = np.ascontiguousarray(molecule.charge_q, dtype=np.float64)
+        h = C.c_void_p()
+        rep_ = (C.c_int32 * 3)()
+        lib = self.ctx._lib
+        self.ctx.check(lib.pmgb_system_create_unitcell(
+            self.ctx.handle, ptr(f_to_c, C.c_double),
+            len(atom_sp), ptr(atom_xf, C.c_double), ptr(atom_sp, C.c_int32),
+            q.shape[0], ptr(q_xf, C.c_double), ptr(q, C.c_double),
+            len(species), ptr(self._eps, C.c_double), ptr(self._sig2, C.c_double), float(ljff.r_cutoff),
+            len(self._gsp), ptr(self._gax, C.c_double), ptr(self._gsp, C.c_int32),
+            self._gq.shape[0], ptr(self._gqx, C.c_double), ptr(self._gq, C.c_double),
+            float(ewald_precision), rep_, C.byref(h)))
+        self.handle = h
+        self.repfactors = tuple(int(r) for r in rep_)
+        self.charged = has_charges(crystal) and molecule.n_charges > 0
+        self.n_sites = int(lib.pmgb_system_n_sites(h))
+        sa = np.zeros(self.n_sites, dtype=np.int32)
+        sc = np.zeros(self.n_sites, dtype=np.int32)
+        self.ctx.check(lib.pmgb_system_sites(h, ptr(sa, C.c_int32), ptr(sc, C.c_int32)))
+        self.site_atom, self.site_charge = sa, sc
+        self.refine_tail = 0.0
+        if refine_tail:
+            self.set_refine(refine_tail)
+        return self
+
+    def __getattr__(self, name):
+        # the host-side objects of a system built from its unit cell, made on first use
+        if name in ("crystal", "molecule", "eparams") and "_unit" in self.__dict__:
+            from .crystal import replicate
+            from .ewald import setup_Ewald_sum
+            from .molecule import Frac
+
+            sc = replicate(self._unit, self.repfactors)
+            self.crystal = sc
+            self.molecule = Frac(self._guest, sc.box)
+            self.eparams = setup_Ewald_sum(sc.box, self.ljff.r_cutoff, eps=self._ewald_precision) \
+                if self.charged else None
+            return self.__dict__[name]
+        raise AttributeError(name)
+
     # -- set-up ------------------------------------------------------------------------
     def set_ewald(self, ep: EwaldParams) -> None:
         abc = np.ascontiguousarray(ep.kvec_abc, dtype=np.int32)
