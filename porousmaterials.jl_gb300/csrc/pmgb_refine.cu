@@ -663,8 +663,9 @@ __device__ void energy_fp64_warp_part(const RefineArgs& a, const SysDev& S, unsi
 // Work units of one insertion (pair terms + reciprocal-space terms).  Tiny insertions are
 // evaluated by one thread each; the others are cut into chunks (records and k-space half-rows in
 // proportion), one warp per chunk, so that one large insertion spreads over many SMs instead of
-// waiting on one warp.  The chunk size adapts to the system's number of refined insertions: ~1024
-// units while its chunk-items stay within 4096 (a few insertions: the pass is latency-bound, finer
+// waiting on one warp.  The chunk size adapts to the system's number of refined insertions: ~256
+// units while its chunk-items stay within 256 (one or a few configurations, a Monte Carlo move:
+// the pass is pure latency), ~1024 units while they stay within 4096 (a few insertions: finer
 // chunks fill more SMs), else ~16384 units (many insertions: fewer repetitions of the per-chunk
 // set-up).  The count is the same for a system alone or in a batch, so the two evaluate identical
 // chunks.
@@ -674,6 +675,8 @@ __device__ __forceinline__ long long fp64_work(const SysDev& S) {
 __device__ __forceinline__ bool small_system(const SysDev& S) { return fp64_work(S) <= 64; }
 __device__ __forceinline__ int fp64_chunks(const SysDev& S, long long count) {
     if (small_system(S)) return 0;
+    const long long finest = min(64ll, (fp64_work(S) + 255) / 256);
+    if (count * finest <= 256) return static_cast<int>(finest);
     const long long fine = min(64ll, (fp64_work(S) + 1023) / 1024);
     if (count * fine <= 4096) return static_cast<int>(fine);
     return static_cast<int>(min(64ll, (fp64_work(S) + 16383) / 16384));
@@ -1007,9 +1010,15 @@ cudaError_t pmgb_launch_exact(const RefineArgs& a, long long n, const int* n_dev
     const long long cap = n_dev ? a.cap_entries : n;
     const int blocks = static_cast<int>(std::max(1ll, std::min((cap + 255) / 256, 4ll * n_sm)));
     exact_list_kernel<<<blocks, 256, 0, st>>>(a, n, n_dev);
+    // one system: only the thread pass (tiny systems) or only the warp pass runs
+    const long long work = static_cast<long long>(a.sys.n_sites) * (a.sys.n_rec + (a.sys.charged ? a.sys.n_k : 0));
+    if (work <= 64) {
+        const int tb = static_cast<int>(std::max(1ll, std::min((cap + PMGB_THREADS - 1) / PMGB_THREADS, 4ll * n_sm)));
+        refine_small_kernel<<<tb, PMGB_THREADS, 0, st>>>(a, 0);
+        return cudaGetLastError();
+    }
     cudaError_t e = cudaMemsetAsync(a.done, 0, sizeof(int) * static_cast<size_t>(cap), st);
     if (e != cudaSuccess) return e;
-    refine_small_kernel<<<4 * n_sm, PMGB_THREADS, 0, st>>>(a, 0);
     refine_plan_kernel<<<1, 1024, 0, st>>>(a, 0);
     refine_large_kernel<<<4 * n_sm, PMGB_THREADS, 0, st>>>(a, 0);
     return cudaGetLastError();

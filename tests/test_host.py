@@ -174,3 +174,65 @@ def test_pocket_classification_on_built_grids():
     a, b = seg[4, 0, 2] - 1, seg[0, 3, 2] - 1
     cls = _classify_segments(n, _segment_connections(seg))
     assert cls[a] == 0 and cls[b] == 1
+
+
+def _native():
+    lib_path = ROOT / "porousmaterials.jl_gb300" / "pmgb" / "libpmgb.so"
+    if not lib_path.exists():
+        pytest.skip("libpmgb.so not built")
+    return pmgb._lib.lib()
+
+
+def test_native_replication_factors_match_the_host_mirror(golden):
+    """pmgb_replication_factors (host-only, no device work) against the Python restatement of
+    src/forcefield.jl:120-158 over the synthetic frameworks, the reference's crystals and skewed
+    random cells."""
+    L = _native()
+    from pmgb import synthetic
+
+    boxes = [cr.box for cr in synthetic.batch_frameworks(24)] + [synthetic.config0().box, synthetic.config1().box]
+    boxes += [pmgb.read_cif(DATA / "crystals" / n).box for n in ("SBMOF-1.cif", "NU-1000_Greg.cif", "CAXVII_clean.cif")]
+    rng = np.random.default_rng(4)
+    for _ in range(40):
+        boxes.append(pmgb.Box(*rng.uniform(3.0, 30.0, 3), *np.radians(rng.uniform(65.0, 115.0, 3))))
+    for box in boxes:
+        for rc in (8.0, 12.5, 14.0):
+            f = np.ascontiguousarray(box.f_to_c.T.reshape(-1))
+            out = (ctypes.c_int32 * 3)()
+            assert L.pmgb_replication_factors(f.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), rc, out) == 0
+            assert tuple(out) == pmgb.replication_factors(box, rc)
+    # the reference's own case (test/forcefield.jl:27-30: Dreiding at its 12.5 A cutoff)
+    cr = pmgb.read_cif(DATA / "crystals" / "test_structure.cif")
+    out = (ctypes.c_int32 * 3)()
+    f = np.ascontiguousarray(cr.box.f_to_c.T.reshape(-1))
+    L.pmgb_replication_factors(f.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 12.5, out)
+    assert list(out) == golden["forcefield_dreiding"]["rep_test_structure"]
+    # degenerate input is refused, not looped on
+    assert L.pmgb_replication_factors(np.zeros(9).ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 12.5, out) == -1
+
+
+def test_native_ewald_setup_matches_the_restated_steps():
+    """setup_Ewald_sum (through pmgb_ewald_setup) against the Python restatements of its steps
+    (determine_ewald_params, required_kreps, precompute_kvec_wts): the same alpha, kreps and
+    k-vectors, weights within rounding; the count query and the capacity check."""
+    L = _native()
+    from pmgb import synthetic
+
+    for cr in [synthetic.config1(), synthetic.config4()] + synthetic.batch_frameworks(8):
+        sc = pmgb.replicate(cr, pmgb.replication_factors(cr.box, 12.5))
+        ep = pmgb.setup_Ewald_sum(sc.box, 12.5, eps=1e-6)
+        alpha, k2 = pmgb.determine_ewald_params(12.5, 1e-6)
+        kreps = pmgb.required_kreps(sc.box, k2)
+        abc, wt = pmgb.precompute_kvec_wts(kreps, sc.box, alpha, k2)
+        assert ep.alpha == alpha and tuple(ep.kreps) == tuple(kreps)
+        np.testing.assert_array_equal(ep.kvec_abc, abc)
+        np.testing.assert_allclose(ep.kvec_wt, wt, rtol=1e-13)
+    f = np.ascontiguousarray(sc.box.f_to_c.T.reshape(-1))
+    fp = f.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    n = ctypes.c_int64()
+    small = np.zeros(3, dtype=np.int32)
+    w = np.zeros(1)
+    rc = L.pmgb_ewald_setup(fp, 12.5, 1e-6, 1, None, None, None, ctypes.byref(n),
+                            small.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), w.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    assert rc == -1 and n.value == ep.n_kvecs    # too small a capacity: refused, count still given
+    assert L.pmgb_ewald_setup(fp, 12.5, 0.0, 0, None, None, None, ctypes.byref(n), None, None) == -1
