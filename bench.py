@@ -113,6 +113,14 @@ def flops_per_insertion(sc, mol, ep):
     return f
 
 
+def counted_flops(counts: dict, n_items: int, n_q_sites: int = 0, n_kvecs: int = 0) -> float:
+    """Algorithmic FP32 flops per item of the work a pass did (pmgb_*_work_counts): 26 per
+    (guest site, record) distance evaluated, 11 more per LJ term and 30 per real-space term inside
+    their cutoffs, 17 per (evaluated k-vector, guest charge)."""
+    return (F_DIST * counts["distances"] + F_LJ_IN * counts["lj_terms"] + F_ES_IN * counts["es_terms"]) / n_items + \
+        F_K * n_q_sites * n_kvecs
+
+
 def flops_inside_cutoff(sc, mol, ff, ep, n_kvecs=None):
     """Algorithmic FP32 flops of one insertion (FMA = 2, MUFU = 1): the minimum-image distance
     of every (framework record, guest site) pair; the LJ and real-space terms of the pairs inside
@@ -635,20 +643,26 @@ def config4_leg(args, ctx, ff, mol, timed, peak):
     gs.set_refine(REFINE_TAIL)
     err4 = widom_error(gs, ff, 4000, 44)
     fpi = flops_per_insertion(sc, mol, ep)
+    work4 = gs.widom_work_counts(npb, N_BLOCKS, 42)   # the FP32-only run's insertions
+    fpc = counted_flops(work4, n, mol.n_charges, gs.info()["n_kvecs_evaluated"])
+    tf4 = fpc * n / (ms32 * 1e-3) / 1e12
     return {
         "workload": "CO2 in a 20,000-atom 52x52x52 A cell, Ewald 1e-6", "framework_sites": sc.atoms.n,
         "kvectors": ep.n_kvecs, "insertions": n,
         "insertions_per_s": n / (ms_ref * 1e-3), "refined_insertions": refined,
         "fp32_only_insertions_per_s": n / (ms32 * 1e-3),
         "forward_plus_adjoint_insertions_per_s": n / (ms_adj * 1e-3),
-        "flops_per_insertion": fpi, "fp32_only_tflops": fpi * n / (ms32 * 1e-3) / 1e12,
-        "fp32_only_tflops_inside_cutoff": flops_inside_cutoff(sc, mol, ff, ep, gs.info()["n_kvecs_evaluated"])
-        * n / (ms32 * 1e-3) / 1e12,
-        "note": "fp32_only_tflops follows the every-pair convention; in this 52 A cell the kernel skips whole "
-                "chunks of records beyond every lane's cutoff (their distances too, by bounding boxes) and the "
-                "energy terms of most remaining groups, so that figure exceeds the FP32 peak; "
-                "fp32_only_tflops_inside_cutoff counts distances of all pairs and energy terms inside the cutoff, "
-                "so it too credits the skipped distances",
+        "roofline": {"bound": "fp32", "flops_per_insertion": fpc, "achieved": tf4, "unit": "TFLOP/s",
+                     "frac": tf4 / peak if peak else None, "work_counts": work4,
+                     "kernel": "the FP32-only Widom pass (centre-image pair kernel + partials), CUDA events",
+                     "counting": "counted by pmgb_widom_work_counts over the same insertions: distances "
+                                 "evaluated (sub-chunks skipped whole are not), LJ and real-space terms inside "
+                                 "their cutoffs, k-terms of the evaluated k-vectors (26 / 11 / 30 / 17 flops)"},
+        "every_pair_flops_per_insertion": fpi,
+        "every_pair_tflops": fpi * n / (ms32 * 1e-3) / 1e12,
+        "note": "every_pair_tflops counts every pair and k-vector; in this 52 A cell the kernel skips whole "
+                "sub-chunks of records beyond every lane's cutoff, distances included, and the energy terms of "
+                "most remaining groups, so that figure exceeds the FP32 peak; the roofline counts the work done",
         "error_vs_fp64_oracle": err4,
         "centre_image": gs.info()["centre_image"],
         "distances": "with centre_image, each record's minimum image is taken from the pose centre once and the "
@@ -725,9 +739,10 @@ def config2_leg(ctx, ff, timed, peak):
     ms_fp32 = timed(grid_device, reps=20, warm=3)       # the FP32 grid kernel alone
     grid_fp32 = gx.energy_grid(pts, rep, 1.0)
     gx.set_exact(True)
-    # counted work of the FP32 grid kernel: the distance of every (record, probe) pair and the LJ terms
-    # of the pairs inside the cutoff (n 4/3 pi rc^3 / V per point); no sub-chunk of this cell is skipped
-    fpp = F_DIST * sc0.atoms.n + F_LJ_IN * sc0.atoms.n * (4.0 / 3.0 * math.pi * ff.r_cutoff ** 3 / sc0.box.Omega)
+    # counted work of the FP32 grid kernel (pmgb_energy_grid_work_counts): the distances it evaluates
+    # and the LJ terms inside the cutoff
+    gwork = gx.energy_grid_work_counts(pts, rep)
+    fpp = counted_flops(gwork, n_pts)
     tf = fpp * n_pts / (ms_fp32 * 1e-3) / 1e12
     return {
         "workload": "Xe over a 96^3 grid of config0 (424 atoms, 25.832 A cubic)", "points": n_pts,
@@ -738,11 +753,11 @@ def config2_leg(ctx, ff, timed, peak):
         "fp32_only_points_per_s": n_pts / (ms_fp32 * 1e-3),
         "host_call_points_per_s": n_pts / (ms_g * 1e-3), "adjoint_points_per_s": n_pts / (ms_ga * 1e-3),
         "roofline": {"bound": "fp32", "flops_per_point": fpp, "achieved": tf, "unit": "TFLOP/s",
-                     "frac": tf / peak if peak else None,
+                     "frac": tf / peak if peak else None, "work_counts": gwork,
                      "kernel": "pairs_kernel<1,false,...> (FP32 grid, exact energies off), CUDA events around "
                                "pmgb_energy_grid_device",
-                     "counting": "distance of every (record, probe) pair 26 flops, LJ 11 more per pair inside the "
-                                 "cutoff (FMA = 2, MUFU = 1)"},
+                     "counting": "counted by pmgb_energy_grid_work_counts: 26 flops per (record, probe) distance "
+                                 "evaluated, 11 more per LJ term inside the cutoff (FMA = 2, MUFU = 1)"},
         "error_vs_fp64_oracle": {"exact": grid_error(gx, ff, pts, rep, grid_exact),
                                  "fp32_only": grid_error(gx, ff, pts, rep, grid_fp32)},
         "timing": "points_per_s and fp32_only: CUDA events around the device call (grid left on the device); "
@@ -892,7 +907,10 @@ def ours(args, rank, world, local_rank):
         return
     fpi = flops_per_insertion(sc, mol, ep)
     achieved_every = fpi * n_ins / (kernel_ms * 1e-3) / 1e12
-    fpi_in = flops_inside_cutoff(sc, mol, ff, ep, system.info()["n_kvecs_evaluated"])
+    n_kev = system.info()["n_kvecs_evaluated"]
+    work = system.widom_work_counts(npb, N_BLOCKS, 1)   # the insertions of the first timed step
+    fpi_in = counted_flops(work, n_ins, mol.n_charges, n_kev)
+    fpi_est = flops_inside_cutoff(sc, mol, ff, ep, n_kev)
     achieved = fpi_in * n_ins / (kernel_ms * 1e-3) / 1e12
     cpu = None
     if "cpu" in args.legs:
@@ -947,10 +965,13 @@ def ours(args, rank, world, local_rank):
                                        "FP32 figure",
                         "peak_clocks": peak_clocks,
                         "flops_per_insertion": fpi_in,
-                        "counting": "the work the kernel does: the minimum-image distance of every (record, guest "
-                                    "site) pair 26 flops (no sub-chunk of this cell is skipped), LJ 11 and "
-                                    "real-space 30 more per pair inside the cutoff (n 4/3 pi rc^3 / V per "
-                                    "insertion), 17 per (evaluated k-vector, guest charge); FMA = 2, MUFU = 1",
+                        "work_counts": work,
+                        "counting": "the work the kernel does, counted by its work-counting pass "
+                                    "(pmgb_widom_work_counts) over the first timed step's insertions: 26 flops per "
+                                    "(guest site, record) distance evaluated (no sub-chunk of this cell is skipped), "
+                                    "11 more per LJ and 30 per real-space term inside their cutoffs, 17 per "
+                                    "(evaluated k-vector, guest charge); FMA = 2, MUFU = 1",
+                        "flops_per_insertion_uniform_estimate": fpi_est,
                         "kvectors_evaluated": system.info()["n_kvecs_evaluated"],
                         "every_pair": {"flops_per_insertion": fpi, "achieved": achieved_every,
                                        "frac": achieved_every / fp32_peak if fp32_peak else None,

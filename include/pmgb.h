@@ -406,6 +406,17 @@ int pmgb_device_status(pmgb_ctx* ctx, uint32_t* status_out);
  * returns PMGB_ERR_DEVICE_STATUS with the status cleared.  arm = 0 completes the phase: PMGB_OK. */
 int pmgb_test_bounded_wait(pmgb_ctx* ctx, int64_t limit_ns, int32_t arm);
 
+/* Work counts (no reference counterpart; measurement of the counted-work roofline): the forward
+ * pass of pmgb_widom_device (spatially ordered, with its cutoff culling; the FP32 pass, no
+ * refinement) or of pmgb_energy_grid (its FP32 pass), run with counters:
+ * counts_out = (guest-site-to-record distances evaluated -- the records of sub-chunks skipped whole
+ * are not -- , LJ pair terms inside the LJ cutoff, real-space pair terms inside the short-range
+ * cutoff).  Results are not returned.  Guests of one or three sites. */
+int pmgb_widom_work_counts(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
+                           int64_t counts_out[3]);
+int pmgb_energy_grid_work_counts(pmgb_system* sys, const int32_t n_pts[3], const int32_t repfactors[3],
+                                 int64_t counts_out[3]);
+
 /* Kernel timing (no reference counterpart; measurement): while on, every Widom pass records a
  * CUDA event before and after its pair-kernel launch on the launching stream (at most 4096
  * launches between two reads).  pmgb_kernel_timing synchronises on the recorded events and

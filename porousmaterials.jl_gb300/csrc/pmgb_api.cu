@@ -108,6 +108,7 @@ struct pmgb_system {
     DevBuf partials, block_out, in_buf, out_buf, axes;
     DevBuf g_u, g_dsum, g_grad, g_part, g_cols;  // adjoint scratch
     DevBuf x64, e_bound;            // exact energies: FP64 site coordinates, grid error estimates
+    DevBuf stats;                   // work counts of the diagnostic passes
 };
 
 namespace {
@@ -437,7 +438,7 @@ static void free_system_device(pmgb_system* s) {
                     s->g_part.p,   s->g_cols.p,   s->r_hist.p,  s->r_cut.p,  s->r_counts.p, s->r_offsets.p,
                     s->r_list.p,   s->r_ref.p,    s->o_counts.p, s->o_perm.p,  s->r_plan.p,  s->r_done.p,
                     s->r_part.p,   s->acc.p,      s->d_cbox,    s->d_es,     s->d_es_df,  s->d_rec_rq,
-                    s->d_rec_qlo,  s->d_segpar_df, s->d_tk_df, s->x64.p,  s->e_bound.p};
+                    s->d_rec_qlo,  s->d_segpar_df, s->d_tk_df, s->x64.p,  s->e_bound.p, s->stats.p};
     for (void* p : ptrs) dev_free(s->ctx, p);
 }
 
@@ -2053,6 +2054,88 @@ extern "C" int pmgb_energy_grid_device(pmgb_system* s, const int32_t n_pts[3], c
     const int n_ctas = s->cull ? pmgb_grid_brick_ctas(n_pts) : static_cast<int>((total + PMGB_THREADS - 1) / PMGB_THREADS);
     PMGB_CK(ctx, pmgb_launch_pairs(a, n_ctas, ctx->stream));
     return PMGB_OK;
+}
+
+// The work-counting pass (pmgb_launch_pairs_stats) on prepared arguments; counts_out receives the
+// three counters.
+static int run_work_counts(pmgb_system* s, LaunchArgs& a, int n_ctas, int64_t counts_out[3]) {
+    pmgb_ctx* ctx = s->ctx;
+    if (int rc = ensure(ctx, s->stats, sizeof(unsigned long long) * 3)) return rc;
+    a.stats = static_cast<unsigned long long*>(s->stats.p);
+    PMGB_CK(ctx, cudaMemsetAsync(a.stats, 0, sizeof(unsigned long long) * 3, ctx->stream));
+    const cudaError_t e = pmgb_launch_pairs_stats(a, n_ctas, ctx->stream);
+    if (e == cudaErrorNotSupported)
+        return fail(ctx, PMGB_ERR_UNSUPPORTED, "work counts: guests of one or three sites only (got %d)", s->n_sites);
+    PMGB_CK(ctx, e);
+    unsigned long long c[3] = {0, 0, 0};
+    PMGB_CK(ctx, cudaMemcpyAsync(c, a.stats, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
+    if (int rc = check_status(ctx)) return rc;
+    for (int i = 0; i < 3; ++i) counts_out[i] = static_cast<int64_t>(c[i]);
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_widom_work_counts(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
+                                      int64_t counts_out[3]) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (n_per_block < 1 || n_blocks < 1 || !counts_out)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_work_counts: bad arguments");
+    if (int rc = ready_for_charges(s)) return rc;
+    if (n_per_block > static_cast<int64_t>(INT32_MAX) * PMGB_THREADS)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_work_counts: too many insertions per block");
+    const int64_t cpb = (n_per_block + PMGB_THREADS - 1) / PMGB_THREADS;
+    if (cpb > INT32_MAX / n_blocks) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_work_counts: too many");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    const size_t n_ins = static_cast<size_t>(n_per_block) * n_blocks;
+    int rc;
+    if ((rc = ensure(ctx, s->o_counts, sizeof(int) * pmgb_widom_order_cells() * n_blocks)) ||
+        (rc = ensure(ctx, s->o_perm, sizeof(int) * n_ins)))
+        return rc;
+    LaunchArgs a = base_args(s);
+    a.pose_mode = POSE_PHILOX;
+    a.out_mode = OUT_WIDOM;
+    a.seed = seed;
+    a.n_per_block = n_per_block;
+    a.n_blocks = n_blocks;
+    a.ctas_per_block = static_cast<int>(cpb);
+    a.inv_temperature = 1.0;
+    a.perm = static_cast<const int*>(s->o_perm.p);  // the spatially ordered pass of pmgb_widom_device
+    PMGB_CK(ctx, pmgb_launch_widom_order(seed, n_per_block, n_blocks, static_cast<int*>(s->o_counts.p),
+                                         static_cast<int*>(s->o_perm.p), ctx->stream));
+    return run_work_counts(s, a, static_cast<int>(cpb * n_blocks), counts_out);
+}
+
+extern "C" int pmgb_energy_grid_work_counts(pmgb_system* s, const int32_t n_pts[3], const int32_t repfactors[3],
+                                            int64_t counts_out[3]) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    if (!n_pts || !repfactors || !counts_out)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid_work_counts: NULL argument");
+    for (int d = 0; d < 3; ++d)
+        if (n_pts[d] < 1 || repfactors[d] < 1)
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT,
+                        "pmgb_energy_grid_work_counts: n_pts and repfactors must be >= 1");
+    if (s->n_sites != 1)
+        return fail(ctx, PMGB_ERR_UNSUPPORTED, "pmgb_energy_grid_work_counts: the probe must be a single site");
+    const int64_t total = int64_t(n_pts[0]) * n_pts[1] * n_pts[2];
+    if (total > int64_t(INT32_MAX) * PMGB_THREADS / 2)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid_work_counts: grid too large");
+    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    if (int rc = grid_axes(s, n_pts, repfactors)) return rc;
+    if (int rc = ensure(ctx, s->out_buf, sizeof(float) * total)) return rc;
+    LaunchArgs a = base_args(s);
+    a.sys.charged = 0;  // grid.jl:337-338: single-site probes get the vdW energy only
+    a.pose_mode = POSE_GRID;
+    a.out_mode = OUT_GRID;
+    for (int d = 0; d < 3; ++d) a.n_pts[d] = n_pts[d];
+    const uint32_t* ax = static_cast<const uint32_t*>(s->axes.p);
+    a.grid_x = ax;
+    a.grid_y = ax + n_pts[0];
+    a.grid_z = ax + n_pts[0] + n_pts[1];
+    a.unit_factor = 1.0f;
+    a.grid_out = static_cast<float*>(s->out_buf.p);
+    a.grid_bricks = 1;  // the brick order of the grid pass
+    return run_work_counts(s, a, pmgb_grid_brick_ctas(n_pts), counts_out);
 }
 
 extern "C" int pmgb_energy_grid_rotational(pmgb_system* s, const int32_t n_pts[3], const int32_t repfactors[3],

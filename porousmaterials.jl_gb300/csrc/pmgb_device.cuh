@@ -767,6 +767,7 @@ struct UnitIO {
     float* grad_u;               // GRAD, optional
     float* bound_out;            // OUT_GRID with BOUND: per-item FP32 error estimate (+Inf: must be refined)
     float bound_rho, bound_stat; // BOUND: worst-case per-term factor, statistical factor (see run_unit)
+    unsigned long long* stats;   // STATS: [3] distances evaluated, LJ and real-space terms inside their cutoffs
     LsePartial* partial;         // OUT_WIDOM: this unit's partial
     double* x_out;               // OUT_WIDOM, optional: this thread's -U/T (-inf if none)
     double* m_out;               // OUT_WIDOM, optional (shared): the unit's max of -U/T
@@ -840,14 +841,18 @@ __device__ __forceinline__ bool chunk_near_com(const SysDev& S, const ChunkBox* 
 // independent per-term roundings, the last the 2^-32 quantisation of the item's position; +Inf
 // when some pair sits within FP32 rounding of the cutoff or of the overlap distance (the two
 // sides of either give different energies).  Runs the spatially culled loop.
+// STATS (a diagnostic of the work done, for the counted-work roofline): the loops also count, per
+// valid item, the (record, site) distances evaluated -- records of skipped sub-chunks are not --
+// and the pairs inside the LJ and real-space cutoffs, added into io.stats[0..2].
 template <int NS, bool CHARGED, bool GRAD, bool RESID = true, bool FORCES = GRAD, bool COMP = false,
-          bool BOUND = false>
+          bool BOUND = false, bool STATS = false>
 __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4* stage, uint64_t* bars,
                                          LsePartial* red, uint32_t (&fills)[PMGB_NSTAGE], unsigned int* status) {
     static_assert(RESID || !GRAD, "the adjoint keeps the box-matrix residual");
     static_assert(GRAD || !FORCES, "forces come with the adjoint");
     static_assert(!COMP || (!FORCES && NS > 1), "the centre-image path has no forces and several sites");
     static_assert(!BOUND || (!GRAD && !COMP && !CHARGED), "the error scale is for uncharged forward grids");
+    static_assert(!STATS || (!GRAD && !BOUND), "the work counts are for forward passes");
     constexpr bool COLS = (GRAD && !FORCES) || BOUND;
     const int tid = threadIdx.x;
     const bool valid = io.valid;
@@ -924,6 +929,16 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
     }
     bool ovl = false, abort = false;
     int fail_tile = 0;
+    unsigned long long st_dist = 0, st_lj = 0, st_es = 0;  // STATS: this item's counts
+    // STATS: count the distances of n records to one site and the pairs inside each cutoff
+    auto count_pairs = [&](int n, float a, float b, float c, float d) {
+        if (STATS && valid && !blocked) {
+            st_dist += n;
+            st_lj += (a < g2.rc2) + (n > 1 && b < g2.rc2) + (n > 2 && c < g2.rc2) + (n > 3 && d < g2.rc2);
+            if (CHARGED)
+                st_es += (a < g2.rc2e) + (n > 1 && b < g2.rc2e) + (n > 2 && c < g2.rc2e) + (n > 3 && d < g2.rc2e);
+        }
+    };
     // BOUND: smallest |r^2 - rc^2| seen, an overlap distance within rounding, sum of squared terms
     float cgap = __int_as_float(0x7f800000);
     bool thr_near = false;
@@ -1021,6 +1036,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                                   const int4& r3) {
                     const float dmin = fminf(fminf(d01.x, d01.y), fminf(d23.x, d23.y));
                     segmin[k] = fminf(segmin[k], dmin);
+                    count_pairs(4, d01.x, d01.y, d23.x, d23.y);
                     if (__any_sync(0xffffffffu, valid && !blocked && dmin < g2.rcmax2)) {
                         const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
                         pair2_energy<CHARGED, COLS>(d01, __int_as_float(r0.w), __int_as_float(r1.w), g2, a12, a6,
@@ -1079,6 +1095,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                                                 __uint_as_float(uz[k]));
                             dd.y = 1e30f;
                             segmin[k] = fminf(segmin[k], dd.x);
+                            count_pairs(1, dd.x, 0.0f, 0.0f, 0.0f);
                             pair2_energy<CHARGED, COLS>(dd, __int_as_float(r.w), 0.0f, g2, f2(lj12[k]), f2(lj6[k]),
                                                         ljp2[k], php2[k], &i12[k], &i6[k]);
                         }
@@ -1133,6 +1150,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                             const float2 d23 = pair2_r2<RESID>(r2, r3, ux[k], uy[k], uz[k], g2);
                             const float dmin = fminf(fminf(d01.x, d01.y), fminf(d23.x, d23.y));
                             segmin[k] = fminf(segmin[k], dmin);
+                            count_pairs(4, d01.x, d01.y, d23.x, d23.y);
                             if (BOUND)
                                 cgap = fminf(cgap, fminf(fminf(fabsf(d01.x - g2.rc2), fabsf(d01.y - g2.rc2)),
                                                          fminf(fabsf(d23.x - g2.rc2), fabsf(d23.y - g2.rc2))));
@@ -1170,10 +1188,12 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                     for (; j < j1; ++j) {
                         const int4 r = T[j - t0];
 #pragma unroll
-                        for (int k = 0; k < NS; ++k)
+                        for (int k = 0; k < NS; ++k) {
+                            if (STATS) count_pairs(1, dist2(r, ux[k], uy[k], uz[k], g), 0.0f, 0.0f, 0.0f);
                             pair_fwd<CHARGED, COLS>(r, ux[k], uy[k], uz[k], g, sig2[k], eps4[k], segmin[k], ljp[k],
                                                     php[k], &i12[k].x, &i6[k].x, BOUND ? &i24[k].x : nullptr,
                                                     BOUND ? &cgap : nullptr);
+                        }
                     }
                 } else {
                     int j = j0;
@@ -1249,6 +1269,15 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                                         (fills[t % PMGB_NSTAGE] + static_cast<uint32_t>(t / PMGB_NSTAGE)) & 1u);
         }
         return false;
+    }
+    if (STATS) {  // warp sums, one atomic per counter and warp
+        unsigned long long c[3] = {st_dist, st_lj, st_es};
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) c[i] += __shfl_xor_sync(0xffffffffu, c[i], o);
+            if ((tid & 31) == 0 && c[i]) atomicAdd(io.stats + i, c[i]);
+        }
     }
     // every tile t completed one phase of slot t % NSTAGE (none was refilled if resident)
     if (!io.resident) {

@@ -193,6 +193,8 @@ struct LaunchArgs {
     // energy grid with error scale (pmgb_launch_grid_bound)
     float* bound_out;            // [item] FP32 rounding-error estimate (K), +Inf where a pair sits at a threshold
     float bound_rho, bound_stat; // factors of the estimate (run_unit, BOUND)
+    // work counts (pmgb_launch_pairs_stats)
+    unsigned long long* stats;   // [3] distances evaluated, LJ and real-space terms inside their cutoffs
     // status
     unsigned int* status;
 };
@@ -326,6 +328,9 @@ cudaError_t pmgb_launch_pairs_grad(const LaunchArgs& a, int n_ctas, cudaStream_t
 // Energy grid of a single-site uncharged probe (POSE_GRID, OUT_GRID) plus each point's FP32
 // error scale in a.bound_out (run_unit's BOUND form)
 cudaError_t pmgb_launch_grid_bound(const LaunchArgs& a, int n_ctas, cudaStream_t st);
+// The forward pass with the work it does counted into a.stats (run_unit's STATS form): guests of
+// one or three sites; Widom poses take the centre-image form where the system does
+cudaError_t pmgb_launch_pairs_stats(const LaunchArgs& a, int n_ctas, cudaStream_t st);
 // persistent batch (defined in pmgb_batch.cu)
 cudaError_t pmgb_batch_prepare(bool grad);  // function attributes, before any stream capture
 cudaError_t pmgb_launch_batch(const BatchArgs& b, bool grad, int n_ctas, cudaStream_t st);

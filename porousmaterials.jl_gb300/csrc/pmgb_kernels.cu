@@ -9,7 +9,7 @@ namespace {
 
 // Single-system launch: CTA b runs unit b.
 template <int NS, bool CHARGED, bool GRAD, bool RESID = true, bool FORCES = GRAD, bool COMP = false,
-          bool BOUND = false>
+          bool BOUND = false, bool STATS = false>
 __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_constant__ LaunchArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     int4* stage = reinterpret_cast<int4*>(smem_raw);
@@ -75,10 +75,12 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_kernel(const __grid_con
     io.bound_out = a.bound_out;
     io.bound_rho = a.bound_rho;
     io.bound_stat = a.bound_stat;
+    io.stats = a.stats;
     io.partial = (a.partials && !a.perm) ? a.partials + blockIdx.x : nullptr;
     ring_init(bars);
     uint32_t fills[PMGB_NSTAGE] = {};
-    (void)run_unit<NS, CHARGED, GRAD, RESID, FORCES, COMP, BOUND>(a.sys, io, stage, bars, red, fills, a.status);
+    (void)run_unit<NS, CHARGED, GRAD, RESID, FORCES, COMP, BOUND, STATS>(a.sys, io, stage, bars, red, fills,
+                                                                          a.status);
 }
 
 // ---- latency path: few configurations, one CTA each -----------------------------------
@@ -580,6 +582,30 @@ cudaError_t pmgb_launch_grid_bound(const LaunchArgs& a, int n_ctas, cudaStream_t
     if (e != cudaSuccess) return e;
     pairs_kernel<1, false, false, true, false, false, true><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
     return cudaGetLastError();
+}
+
+template <int NS, bool CH, bool COMP>
+cudaError_t launch_stats_one(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
+    const size_t smem = pmgb_pairs_smem_bytes();
+    cudaError_t e = cudaFuncSetAttribute(pairs_kernel<NS, CH, false, true, false, COMP, false, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    pairs_kernel<NS, CH, false, true, false, COMP, false, true><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t pmgb_launch_pairs_stats(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
+    if (n_ctas <= 0) return cudaSuccess;
+    if (!a.stats) return cudaErrorInvalidValue;
+    const bool comp = centre_image(a);
+    if (a.sys.n_sites == 1)
+        return a.sys.charged ? launch_stats_one<1, true, false>(a, n_ctas, st) : launch_stats_one<1, false, false>(a, n_ctas, st);
+    if (a.sys.n_sites == 3) {
+        if (a.sys.charged)
+            return comp ? launch_stats_one<3, true, true>(a, n_ctas, st) : launch_stats_one<3, true, false>(a, n_ctas, st);
+        return comp ? launch_stats_one<3, false, true>(a, n_ctas, st) : launch_stats_one<3, false, false>(a, n_ctas, st);
+    }
+    return cudaErrorNotSupported;
 }
 
 cudaError_t pmgb_launch_pairs_grad(const LaunchArgs& a, int n_ctas, cudaStream_t st) {

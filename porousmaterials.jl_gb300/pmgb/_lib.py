@@ -81,6 +81,8 @@ SIGNATURES = [
     ("pmgb_batch_set_refine", C.c_int, [_vp, C.c_double]),
     ("pmgb_batch_set_cull", C.c_int, [_vp, C.c_int32]),
     ("pmgb_batch_energies", C.c_int, [_vp, _dp]),
+    ("pmgb_widom_work_counts", C.c_int, [_vp, C.c_int64, C.c_int32, C.c_uint64, C.POINTER(C.c_int64)]),
+    ("pmgb_energy_grid_work_counts", C.c_int, [_vp, _ip, _ip, C.POINTER(C.c_int64)]),
     ("pmgb_set_kernel_timing", C.c_int, [_vp, C.c_int32]),
     ("pmgb_kernel_timing", C.c_int, [_vp, _dp, C.POINTER(C.c_int64)]),
     ("pmgb_batch_refined_counts", C.c_int, [_vp, C.POINTER(C.c_int64)]),

@@ -229,6 +229,23 @@ class GPUSystem:
         (pmgb_system_set_centre_image; default on)."""
         self.ctx.check(self.ctx._lib.pmgb_system_set_centre_image(self.handle, int(bool(on))))
 
+    def widom_work_counts(self, n_per_block: int, n_blocks: int, seed: int) -> dict:
+        """The work the ordered forward Widom pass does (pmgb_widom_work_counts): distances evaluated,
+        LJ and real-space pair terms inside their cutoffs."""
+        out = np.zeros(3, dtype=np.int64)
+        self.ctx.check(self.ctx._lib.pmgb_widom_work_counts(self.handle, int(n_per_block), int(n_blocks), int(seed),
+                                                            ptr(out, C.c_int64)))
+        return {"distances": int(out[0]), "lj_terms": int(out[1]), "es_terms": int(out[2])}
+
+    def energy_grid_work_counts(self, n_pts, repfactors) -> dict:
+        """The work the FP32 energy-grid pass does (pmgb_energy_grid_work_counts)."""
+        n = np.ascontiguousarray(n_pts, dtype=np.int32)
+        r = np.ascontiguousarray(repfactors, dtype=np.int32)
+        out = np.zeros(3, dtype=np.int64)
+        self.ctx.check(self.ctx._lib.pmgb_energy_grid_work_counts(self.handle, ptr(n, C.c_int32), ptr(r, C.c_int32),
+                                                                  ptr(out, C.c_int64)))
+        return {"distances": int(out[0]), "lj_terms": int(out[1]), "es_terms": int(out[2])}
+
     def refined_count(self) -> int:
         """Insertions the last refined Widom run re-evaluated in FP64."""
         out = C.c_int64()
