@@ -489,7 +489,8 @@ def widom_error(gs, ff, n_per_block: int, seed: int):
     u_ref = v + sr + lr
     ug = u.sum(axis=1)
     both_inf = np.isinf(ug) & np.isinf(u_ref)
-    ok = both_inf | (np.abs(ug - u_ref) <= np.maximum(1e-5 * np.abs(u_ref), 1e-4))
+    with np.errstate(invalid="ignore"):  # inf - inf where both are infinite
+        ok = both_inf | (np.abs(ug - u_ref) <= np.maximum(1e-5 * np.abs(u_ref), 1e-4))
     x = np.where(np.isfinite(u_ref), -u_ref / T, -np.inf).reshape(N_BLOCKS, n_per_block)
     m = x.max(axis=1, keepdims=True)
     w = np.exp(x - m)
@@ -516,7 +517,8 @@ def grid_error(gs, ff, n_pts, rep, grid, n_sample: int = 20000, seed: int = 3):
     ref = o.energies(pts)[0]
     got = grid[i, j, k].astype(np.float64)
     fin = np.isfinite(ref)
-    ok = (np.isinf(got) & ~fin) | (np.abs(got - ref) <= np.maximum(1e-5 * np.abs(ref), 1e-4))
+    with np.errstate(invalid="ignore"):  # inf - inf where both are infinite
+        ok = (np.isinf(got) & ~fin) | (np.abs(got - ref) <= np.maximum(1e-5 * np.abs(ref), 1e-4))
     rel = np.abs(got[fin] - ref[fin]) / np.maximum(np.abs(ref[fin]), 1e-300)
     return {"points_checked": n_sample, "within_tolerance": float(ok.mean()), "max_rel_error": float(rel.max())}
 

@@ -49,7 +49,8 @@ int pmgb_abi_version(void);
 
 /* Create a context on CUDA device `device` with its own stream.  No reference
  * counterpart: the reference runs in Julia worker processes (src/henry.jl:109).
- * Systems and batches keep their context alive: handles may be destroyed in any order. */
+ * Systems, move handles and batches keep what they use alive (a system its context, a move
+ * handle its system, a batch its systems and context): handles may be destroyed in any order. */
 int pmgb_create(int device, pmgb_ctx** out);
 void pmgb_destroy(pmgb_ctx* ctx);
 
@@ -334,7 +335,7 @@ int pmgb_energy_grid_adjoint(pmgb_system* sys, const int32_t n_pts[3], const int
  * (mod 2^64): the insertions, energies and block results of pmgb_widom with that seed.
  * with_adjoint adds the Boltzmann-weighted parameter sums of pmgb_widom_adjoint (dtheta),
  * accumulated inside the launch with weights relative to M = max_i -U_i/T of each system.
- * All systems must belong to ctx and stay alive while the batch exists. */
+ * All systems must belong to ctx; the batch holds them (destroying a system handle first is fine). */
 typedef struct pmgb_batch pmgb_batch;
 int pmgb_batch_create(pmgb_ctx* ctx, int32_t n_systems, pmgb_system* const* systems,
                       const int64_t* n_per_block, int32_t n_blocks, int32_t with_adjoint,

@@ -59,6 +59,7 @@ struct pmgb_ctx {
 
 struct pmgb_system {
     pmgb_ctx* ctx = nullptr;
+    int refs = 1;                   // the handle itself + one per move handle or batch holding it
     SysDev dev{};
     // device allocations
     int4* d_rec = nullptr;
@@ -134,6 +135,16 @@ int cuda_fail(pmgb_ctx* ctx, cudaError_t e, const char* what) {
         cudaError_t e_ = (call);                                  \
         if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call); \
     } while (0)
+
+// Entry of every call that works on the device: select the context's device and discard an error
+// left in the thread's CUDA error state by earlier, unrelated runtime calls (another library's, or
+// a teardown's), so that the launch checks below report only this call's own errors.  A sticky
+// error of a broken context is not hidden by this: every later call on the device returns it.
+static cudaError_t enter_device(int device) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) (void)cudaGetLastError();
+    return e;
+}
 
 // Device memory from the context's pool, ordered on its current stream (all of a context's
 // work runs on that stream; pmgb_set_stream waits for the previous one).
@@ -361,6 +372,7 @@ extern "C" void pmgb_destroy(pmgb_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     ctx->stream = ctx->own_stream;  // a caller's stream may not outlive this handle
     ctx_release(ctx);
+    (void)cudaGetLastError();
 }
 
 extern "C" const char* pmgb_last_error(const pmgb_ctx* ctx) {
@@ -369,7 +381,7 @@ extern "C" const char* pmgb_last_error(const pmgb_ctx* ctx) {
 
 extern "C" int pmgb_set_stream(pmgb_ctx* ctx, void* stream) {
     if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // pool memory is ordered on one stream
     ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
     return PMGB_OK;
@@ -377,7 +389,7 @@ extern "C" int pmgb_set_stream(pmgb_ctx* ctx, void* stream) {
 
 extern "C" int pmgb_set_kernel_timing(pmgb_ctx* ctx, int32_t on) {
     if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->timing = on != 0;
     ctx->timing_used = 0;
@@ -386,7 +398,7 @@ extern "C" int pmgb_set_kernel_timing(pmgb_ctx* ctx, int32_t on) {
 
 extern "C" int pmgb_kernel_timing(pmgb_ctx* ctx, double* total_ms, int64_t* launches) {
     if (!ctx || !total_ms || !launches) return PMGB_ERR_INVALID_ARGUMENT;
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     double sum = 0.0;
     for (size_t i = 0; i < ctx->timing_used; ++i) {
         PMGB_CK(ctx, cudaEventSynchronize(ctx->timing_events[i].second));
@@ -402,7 +414,7 @@ extern "C" int pmgb_kernel_timing(pmgb_ctx* ctx, double* total_ms, int64_t* laun
 
 extern "C" int pmgb_synchronize(pmgb_ctx* ctx) {
     if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
     return PMGB_OK;
 }
@@ -411,7 +423,7 @@ extern "C" int pmgb_test_bounded_wait(pmgb_ctx* ctx, int64_t limit_ns, int32_t a
     if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
     if (limit_ns < 1 || limit_ns > 100000000)
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_test_bounded_wait: limit_ns in [1, 1e8]");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     PMGB_CK(ctx, pmgb_launch_bounded_wait_test(ctx->d_status, static_cast<unsigned long long>(limit_ns), arm ? 1 : 0,
                                                ctx->stream));
     return check_status(ctx);
@@ -419,7 +431,7 @@ extern "C" int pmgb_test_bounded_wait(pmgb_ctx* ctx, int64_t limit_ns, int32_t a
 
 extern "C" int pmgb_device_status(pmgb_ctx* ctx, uint32_t* status_out) {
     if (!ctx || !status_out) return PMGB_ERR_INVALID_ARGUMENT;
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     unsigned int st = 0;
     PMGB_CK(ctx, cudaMemcpyAsync(&st, ctx->d_status, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream));
     PMGB_CK(ctx, cudaMemsetAsync(ctx->d_status, 0, sizeof(unsigned int), ctx->stream));
@@ -513,7 +525,7 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     for (int k = 0; k < n_species * n_species; ++k)
         if (!std::isfinite(epsilon[k]) || !std::isfinite(sigma2[k]))
             return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "force-field table entry %d is not finite", k);
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
 
     // ---- box: upper-triangular factor --------------------------------------------
     double R[9], Q[9], G[9];
@@ -961,7 +973,7 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "Ewald alpha and sr_cutoff must be positive and finite");
     if (n_kvecs < 0 || (n_kvecs > 0 && (!kvec_abc || !kvec_wt)))
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "bad k-vector arrays");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     for (int k = 0; k < n_kvecs; ++k)
         if (!std::isfinite(kvec_wt[k])) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "k-vector %d weight not finite", k);
     // group runs of constant (ka, kb) and consecutive kc, then split each run at kc = 0 into
@@ -1143,14 +1155,24 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
     return PMGB_OK;
 }
 
-extern "C" void pmgb_system_destroy(pmgb_system* s) {
-    if (!s) return;
+// Drop one reference to a system; the last one frees it (and releases its context).  Move handles
+// and batches hold references, so a garbage-collected host may destroy the handles in any order.
+// Errors of the teardown calls are cleared from the thread's CUDA error state, so that they are not
+// reported later by an unrelated launch.
+static void system_release(pmgb_system* s) {
+    if (--s->refs > 0) return;
     pmgb_ctx* ctx = s->ctx;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     free_system_device(s);
     delete s;
     ctx_release(ctx);
+    (void)cudaGetLastError();
+}
+
+extern "C" void pmgb_system_destroy(pmgb_system* s) {
+    if (!s) return;
+    system_release(s);
 }
 
 extern "C" int pmgb_system_info(const pmgb_system* s, int64_t* out6) {
@@ -1278,7 +1300,7 @@ extern "C" int pmgb_energies(pmgb_system* s, int64_t n_conf, const double* site_
     if (n_conf == 0) return PMGB_OK;
     if (n_conf > INT32_MAX)
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energies: n_conf too large");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     const size_t n_coord = 3 * static_cast<size_t>(s->n_sites) * static_cast<size_t>(n_conf);
     for (size_t i = 0; i < n_coord; ++i)
         if (!std::isfinite(site_xf[i]))
@@ -1354,7 +1376,7 @@ extern "C" int pmgb_move_create(pmgb_system* s, int32_t max_conf, pmgb_move** ou
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_move_create: max_conf in [1, 65535]");
     if (int rc = ready_for_charges(s)) return rc;
     *out = nullptr;
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     auto* m = new pmgb_move();
     m->sys = s;
     m->max_conf = max_conf;
@@ -1421,7 +1443,7 @@ extern "C" int pmgb_move_create(pmgb_system* s, int32_t max_conf, pmgb_move** ou
         delete m;
         return cuda_fail(ctx, e, "pmgb_move_create");
     }
-    ++ctx->refs;
+    ++s->refs;  // the graph reads the system's device data: keep it alive with the handle
     *out = m;
     return PMGB_OK;
 }
@@ -1446,7 +1468,7 @@ extern "C" int pmgb_move_energies(pmgb_move* m, int32_t n_conf, const double* si
         for (size_t i = 0; i < n_coord; ++i) st[1 + i] = to_fix(site_xf[i]);
         st[0] = static_cast<uint32_t>(n_conf);
     }
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     PMGB_CK(ctx, cudaGraphLaunch(m->exec, ctx->stream));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
     std::memcpy(out, m->h_out, sizeof(double) * 3 * n_conf);
@@ -1455,12 +1477,13 @@ extern "C" int pmgb_move_energies(pmgb_move* m, int32_t n_conf, const double* si
 
 extern "C" void pmgb_move_destroy(pmgb_move* m) {
     if (!m) return;
-    pmgb_ctx* ctx = m->sys->ctx;
-    cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
+    pmgb_system* s = m->sys;
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
     move_free(m);
     delete m;
-    ctx_release(ctx);
+    system_release(s);
+    (void)cudaGetLastError();
 }
 
 // Enqueue the FP64 refinement of the Boltzmann tail of a Widom run whose block results are
@@ -1526,7 +1549,7 @@ extern "C" int pmgb_system_refined_count(pmgb_system* s, int64_t* count_out) {
     pmgb_ctx* ctx = s->ctx;
     *count_out = 0;
     if (s->last_refined_slot < 0) return PMGB_OK;
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     int n = 0;
     PMGB_CK(ctx, cudaMemcpyAsync(&n, static_cast<int*>(s->r_offsets.p) + s->last_refined_slot, sizeof(int),
                                  cudaMemcpyDeviceToHost, ctx->stream));
@@ -1550,7 +1573,7 @@ extern "C" int pmgb_system_set_accessibility(pmgb_system* s, const int32_t n_pts
             return fail(ctx, PMGB_ERR_INVALID_ARGUMENT,
                         "pmgb_system_set_accessibility: n_pts and repfactors must be >= 1");
     const size_t n = static_cast<size_t>(n_pts[0]) * n_pts[1] * n_pts[2];
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // no run may still read the old grid
     if (int rc = ensure(ctx, s->acc, n)) return rc;
     std::vector<uint8_t> h(data, data + n);
@@ -1613,7 +1636,7 @@ extern "C" int pmgb_widom_device(pmgb_system* s, int64_t n_per_block, int32_t n_
     const int64_t cpb = (n_per_block + PMGB_THREADS - 1) / PMGB_THREADS;
     if (cpb > INT32_MAX / n_blocks)
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom: too many insertions for one launch");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     const int n_ctas = static_cast<int>(cpb * n_blocks);
     if (int rc = ensure(ctx, s->partials, sizeof(LsePartial) * n_ctas)) return rc;
     LaunchArgs a = base_args(s);
@@ -1683,7 +1706,7 @@ extern "C" int pmgb_widom_noalloc(pmgb_system* s, int64_t n_per_block, int32_t n
                     "of %d insertions (at most %lld insertions per call)",
                     static_cast<long long>(n_blocks), static_cast<long long>(n_per_block), PMGB_NOALLOC_MAX_CTAS,
                     PMGB_THREADS, static_cast<long long>(PMGB_NOALLOC_MAX_CTAS) * PMGB_THREADS);
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     LsePartial* scratch = nullptr;
     PMGB_CK(ctx, pmgb_noalloc_scratch(ctx->device, &scratch));
     LaunchArgs a = base_args(s);
@@ -1708,7 +1731,7 @@ extern "C" int pmgb_widom(pmgb_system* s, int64_t n_per_block, int32_t n_blocks,
     if (!block_out) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom: block_out is NULL");
     if (n_per_block < 1 || n_blocks < 1)
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom: need n_per_block >= 1 and n_blocks >= 1");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     int rc;
     if ((rc = ensure(ctx, s->block_out, sizeof(double) * 4 * n_blocks))) return rc;
     const size_t u_bytes = u_out ? sizeof(double) * 2 * static_cast<size_t>(n_per_block) * n_blocks : 0;
@@ -1763,7 +1786,7 @@ extern "C" int pmgb_widom_adjoint(pmgb_system* s, int64_t n_per_block, int32_t n
     const int nst = template_sites(s->n_sites);
     const int n_cols = static_cast<int>(s->seg_species.size()) * nst * 2;
     const int64_t n = n_per_block * n_blocks;
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     const int n_ctas = static_cast<int>(cpb * n_blocks);
     const int n_chunks = static_cast<int>(std::min<int64_t>(1024, (n + 4095) / 4096));
     int rc;
@@ -1836,7 +1859,7 @@ extern "C" int pmgb_energies_grad(pmgb_system* s, int64_t n_conf, const double* 
     if (int rc = ready_for_charges(s)) return rc;
     if (n_conf == 0) return PMGB_OK;
     if (n_conf > INT32_MAX) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energies_grad: n_conf too large");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     const size_t n_coord = 3 * static_cast<size_t>(s->n_sites) * static_cast<size_t>(n_conf);
     std::vector<uint32_t> fix(n_coord);
     for (size_t i = 0; i < n_coord; ++i) {
@@ -1882,7 +1905,7 @@ extern "C" int pmgb_energy_grid_adjoint(pmgb_system* s, const int32_t n_pts[3], 
     if (s->n_sites != 1)
         return fail(ctx, PMGB_ERR_UNSUPPORTED, "pmgb_energy_grid_adjoint: the probe must be a single site");
     const int64_t total = int64_t(n_pts[0]) * n_pts[1] * n_pts[2];
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     if (int rc = grid_axes(s, n_pts, repfactors)) return rc;
     const int n_cols = static_cast<int>(s->seg_species.size()) * 1 * 2;
     const int n_chunks = static_cast<int>(std::min<int64_t>(1024, (total + 4095) / 4096));
@@ -1941,7 +1964,7 @@ extern "C" int pmgb_sample_poses(pmgb_ctx* ctx, uint64_t seed, int64_t start, in
     if (n < 0 || start < 0 || (n > 0 && (!xf_out || !rot_out)))
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_sample_poses: bad arguments");
     if (n == 0) return PMGB_OK;
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     float *dx = nullptr, *dr = nullptr;
     PMGB_CK(ctx, cudaMalloc(&dx, sizeof(float) * 3 * n));
     cudaError_t e = cudaMalloc(&dr, sizeof(float) * 9 * n);
@@ -2036,7 +2059,7 @@ extern "C" int pmgb_energy_grid_device(pmgb_system* s, const int32_t n_pts[3], c
     if (!(unit_factor > 0.0) || !std::isfinite(unit_factor))
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid: unit_factor must be positive (got %g)",
                     unit_factor);
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     if (int rc = grid_axes(s, n_pts, repfactors)) return rc;
     if (s->exact) return exact_grid(s, n_pts, repfactors, unit_factor, out_dev);
     LaunchArgs a = base_args(s);
@@ -2085,7 +2108,7 @@ extern "C" int pmgb_widom_work_counts(pmgb_system* s, int64_t n_per_block, int32
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_work_counts: too many insertions per block");
     const int64_t cpb = (n_per_block + PMGB_THREADS - 1) / PMGB_THREADS;
     if (cpb > INT32_MAX / n_blocks) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_work_counts: too many");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     const size_t n_ins = static_cast<size_t>(n_per_block) * n_blocks;
     int rc;
     if ((rc = ensure(ctx, s->o_counts, sizeof(int) * pmgb_widom_order_cells() * n_blocks)) ||
@@ -2120,7 +2143,7 @@ extern "C" int pmgb_energy_grid_work_counts(pmgb_system* s, const int32_t n_pts[
     const int64_t total = int64_t(n_pts[0]) * n_pts[1] * n_pts[2];
     if (total > int64_t(INT32_MAX) * PMGB_THREADS / 2)
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid_work_counts: grid too large");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     if (int rc = grid_axes(s, n_pts, repfactors)) return rc;
     if (int rc = ensure(ctx, s->out_buf, sizeof(float) * total)) return rc;
     LaunchArgs a = base_args(s);
@@ -2160,7 +2183,7 @@ extern "C" int pmgb_energy_grid_rotational(pmgb_system* s, const int32_t n_pts[3
     if (int rc = ready_for_charges(s)) return rc;
     const int64_t total = int64_t(n_pts[0]) * n_pts[1] * n_pts[2];
     if (total > INT32_MAX) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid_rotational: grid too large");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     if (int rc = grid_axes(s, n_pts, repfactors)) return rc;
     // the points in slices of at most ~8M insertions, bounding the per-insertion scratch
     const int64_t cpb = (int64_t(n_rotations) + PMGB_THREADS - 1) / PMGB_THREADS;
@@ -2219,7 +2242,7 @@ extern "C" int pmgb_energy_grid(pmgb_system* s, const int32_t n_pts[3], const in
     if (!s) return PMGB_ERR_INVALID_ARGUMENT;
     pmgb_ctx* ctx = s->ctx;
     if (!out || !n_pts) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_energy_grid: NULL argument");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     const int64_t total = int64_t(std::max(n_pts[0], 0)) * std::max(n_pts[1], 0) * std::max(n_pts[2], 0);
     if (int rc = ensure(ctx, s->out_buf, sizeof(float) * std::max<int64_t>(total, 1))) return rc;
     if (int rc = pmgb_energy_grid_device(s, n_pts, repfactors, unit_factor, static_cast<float*>(s->out_buf.p)))
@@ -2234,7 +2257,7 @@ extern "C" int pmgb_philox4x32_10(pmgb_ctx* ctx, int64_t n, const uint32_t* ctr,
     if (n < 0 || (n > 0 && (!ctr || !key || !out)))
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_philox4x32_10: bad arguments");
     if (n == 0) return PMGB_OK;
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     unsigned int *dc = nullptr, *dk = nullptr, *dout = nullptr;
     cudaError_t e = cudaMalloc(&dc, 16 * n);
     if (e == cudaSuccess) e = cudaMalloc(&dk, 8 * n);
@@ -2253,7 +2276,7 @@ extern "C" int pmgb_philox4x32_10(pmgb_ctx* ctx, int64_t n, const uint32_t* ctr,
 
 extern "C" int pmgb_fp32_peak(pmgb_ctx* ctx, int n_ctas, int iters, double* tflops_out) {
     if (!ctx || !tflops_out || n_ctas < 1 || iters < 1) return PMGB_ERR_INVALID_ARGUMENT;
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     float* sink = nullptr;
     PMGB_CK(ctx, cudaMalloc(&sink, sizeof(float) * n_ctas));
     cudaEvent_t e0, e1;
@@ -2487,7 +2510,7 @@ extern "C" int pmgb_batch_create(pmgb_ctx* ctx, int32_t n_systems, pmgb_system* 
     if (!out || n_systems < 1 || !systems || !n_per_block || n_blocks < 1)
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_batch_create: bad arguments");
     *out = nullptr;
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     auto* b = new pmgb_batch();
     b->ctx = ctx;
     b->n_blocks = n_blocks;
@@ -2569,6 +2592,7 @@ extern "C" int pmgb_batch_create(pmgb_ctx* ctx, int32_t n_systems, pmgb_system* 
         return rc;
     }
     ++ctx->refs;
+    for (pmgb_system* sy : b->systems) ++sy->refs;  // the batch reads them: keep them alive with it
     *out = b;
     return PMGB_OK;
 }
@@ -2579,8 +2603,10 @@ extern "C" void pmgb_batch_destroy(pmgb_batch* b) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     batch_free(b);
+    for (pmgb_system* sy : b->systems) system_release(sy);
     delete b;
     ctx_release(ctx);
+    (void)cudaGetLastError();
 }
 
 extern "C" int pmgb_batch_configure(pmgb_batch* b, int32_t n_ctas, int32_t order, double unit_mflop) {
@@ -2589,7 +2615,7 @@ extern "C" int pmgb_batch_configure(pmgb_batch* b, int32_t n_ctas, int32_t order
     if (n_ctas < 0 || n_ctas > b->max_ctas || (order != 0 && order != 1) || !(unit_mflop >= 0.0))
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT,
                     "pmgb_batch_configure: n_ctas in [0, %d], order 0 or 1, unit_mflop >= 0", b->max_ctas);
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
     b->n_ctas = n_ctas == 0 ? b->max_ctas : n_ctas;
     if (int rc = batch_build_units(b, unit_mflop, order)) return rc;
@@ -2602,7 +2628,7 @@ extern "C" int pmgb_batch_set_refine(pmgb_batch* b, double tail_fraction) {
     pmgb_ctx* ctx = b->ctx;
     if (!(tail_fraction >= 0.0 && tail_fraction < 1.0))
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_batch_set_refine: tail fraction in [0, 1)");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
     if (tail_fraction > 0.0 && !b->d_hist) {
         // scratch sized for the worst case: every insertion refined
@@ -2624,7 +2650,7 @@ extern "C" int pmgb_batch_set_refine(pmgb_batch* b, double tail_fraction) {
 extern "C" int pmgb_batch_set_cull(pmgb_batch* b, int32_t on) {
     if (!b) return PMGB_ERR_INVALID_ARGUMENT;
     pmgb_ctx* ctx = b->ctx;
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
     if (on && !b->d_perm) {
         const size_t cells = b->systems.size() * b->n_blocks * pmgb_batch_order_cells();
@@ -2643,7 +2669,7 @@ extern "C" int pmgb_batch_launch(pmgb_batch* b, uint64_t seed, double temperatur
     if (!b) return PMGB_ERR_INVALID_ARGUMENT;
     if (!(temperature > 0.0) || !std::isfinite(temperature))
         return fail(b->ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_batch_launch: temperature must be positive");
-    PMGB_CK(b->ctx, cudaSetDevice(b->ctx->device));
+    PMGB_CK(b->ctx, enter_device(b->ctx->device));
     return batch_enqueue(b, seed, temperature);
 }
 
@@ -2653,7 +2679,7 @@ extern "C" int pmgb_batch_tune(pmgb_batch* b, uint64_t seed, double temperature,
     pmgb_ctx* ctx = b->ctx;
     if (repeats < 1 || !(temperature > 0.0))
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_batch_tune: repeats >= 1 and a positive temperature");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     cudaEvent_t e0, e1;
     PMGB_CK(ctx, cudaEventCreate(&e0));
     PMGB_CK(ctx, cudaEventCreate(&e1));
@@ -2702,7 +2728,7 @@ extern "C" int pmgb_batch_results(pmgb_batch* b, double* block_out, double* dthe
     if (!block_out || (b->grad && !dtheta))
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_batch_results: block_out (and dtheta with the adjoint)");
     if (!b->launched) return fail(ctx, PMGB_ERR_NOT_READY, "pmgb_batch_results: no run since the batch was configured");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     const size_t nb = b->host_sys.size() * 4 * static_cast<size_t>(b->n_blocks);
     PMGB_CK(ctx, cudaMemcpyAsync(block_out, b->d_block_out, sizeof(double) * nb, cudaMemcpyDeviceToHost, ctx->stream));
     std::vector<double> cols(b->grad ? b->n_out_cols : 0);
@@ -2729,7 +2755,7 @@ extern "C" int pmgb_batch_refined_counts(pmgb_batch* b, int64_t* per_system) {
     pmgb_ctx* ctx = b->ctx;
     for (size_t i = 0; i < b->systems.size(); ++i) per_system[i] = 0;
     if (!(b->refine_tail > 0.0) || !b->launched) return PMGB_OK;
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     std::vector<int> off(static_cast<size_t>(b->n_chunks) + 1);
     PMGB_CK(ctx, cudaMemcpyAsync(off.data(), b->d_offsets, sizeof(int) * off.size(), cudaMemcpyDeviceToHost,
                                  ctx->stream));
@@ -2747,7 +2773,7 @@ extern "C" int pmgb_batch_energies(pmgb_batch* b, double* u_out) {
     pmgb_ctx* ctx = b->ctx;
     if (!b->launched || !(b->refine_tail > 0.0 || b->cull) || !b->d_u)
         return fail(ctx, PMGB_ERR_NOT_READY, "pmgb_batch_energies: needs a run with culling or refinement on");
-    PMGB_CK(ctx, cudaSetDevice(ctx->device));
+    PMGB_CK(ctx, enter_device(ctx->device));
     PMGB_CK(ctx, cudaMemcpyAsync(u_out, b->d_u, sizeof(double) * 2 * static_cast<size_t>(b->n_insertions),
                                  cudaMemcpyDeviceToHost, ctx->stream));
     PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
