@@ -126,6 +126,25 @@ int pmgb_system_create_unitcell(pmgb_ctx* ctx, const double f_to_c[9],
                                 const double* guest_charge_q, double ewald_precision,
                                 int32_t repfactors_out[3], pmgb_system** out);
 
+/* Many systems from their unit cells in one call: the set-up of a screen over frameworks (the
+ * loop of src/henry.jl:78-97 over them).  System i is exactly what pmgb_system_create_unitcell
+ * makes from entry i of every array argument (one count or pointer per system; species tables
+ * n_species[i]^2 each).  The host work -- replication, records, Ewald parameters and k-vectors,
+ * the choice of k-vectors once S(k) is known -- runs on n_threads host threads (0: one per
+ * hardware thread, at most 64), and the device work is enqueued back to back through pinned
+ * staging, with two stream synchronisations in all.  repfactors_out (optional) receives 3 per
+ * system.  All or nothing: on failure no handle is created and the message names the system. */
+int pmgb_systems_create_unitcell(pmgb_ctx* ctx, int32_t n_systems, const double* const* f_to_c,
+                                 const int32_t* n_atoms, const double* const* atom_xf,
+                                 const int32_t* const* atom_species, const int32_t* n_charges,
+                                 const double* const* charge_xf, const double* const* charge_q,
+                                 const int32_t* n_species, const double* const* epsilon,
+                                 const double* const* sigma2, double r_cutoff, const int32_t* n_guest_atoms,
+                                 const double* const* guest_atom_x, const int32_t* const* guest_atom_species,
+                                 const int32_t* n_guest_charges, const double* const* guest_charge_x,
+                                 const double* const* guest_charge_q, double ewald_precision, int32_t n_threads,
+                                 int32_t* repfactors_out, pmgb_system** out);
+
 /* Ewald parameters: EwaldParams (src/electrostatics.jl:54-63) as produced by
  * setup_Ewald_sum (src/electrostatics.jl:256-272): α, the short-range cutoff, and the
  * k-vectors (ka, kb, kc) with weights wt (precompute_kvec_wts, :198-232).  The

@@ -13,7 +13,10 @@
 #include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <atomic>
+#include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -50,6 +53,19 @@ struct pmgb_ctx {
     // cutoff reuses it)
     double es_alpha = 0.0, es_smax = 0.0;
     std::vector<double> es_table;
+    // device copies of the erfc(alpha r)/r tables built (FP64 and double-float), one per
+    // (alpha, cutoff); shared by the context's systems and freed with the context
+    struct EsTable {
+        double alpha, smax;
+        double* d_es;
+        float2* d_es_df;
+        int n;
+    };
+    std::vector<EsTable> es_tables;
+    // pinned staging of host-to-device uploads: a bump region, reused from its start once the
+    // stream has drained
+    char* stage = nullptr;
+    size_t stage_cap = 0, stage_used = 0;
     // optional CUDA events around the Widom passes' pair-kernel launches (pmgb_set_kernel_timing)
     bool timing = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timing_events;
@@ -77,8 +93,6 @@ struct pmgb_system {
     double* d_sk = nullptr;
     int* d_kabc = nullptr;          // k-vectors in half-row traversal order
     double* d_wt = nullptr;
-    double* d_es = nullptr;         // erfc(alpha r)/r table of the FP64 refinement
-    float2* d_es_df = nullptr;      // the same as double-float
     float4* d_rec_rq = nullptr;     // double-float record data of the refinement
     float* d_rec_qlo = nullptr;
     float4* d_segpar_df = nullptr;
@@ -187,15 +201,46 @@ int ensure(pmgb_ctx* ctx, DevBuf& b, size_t bytes) {
     return PMGB_OK;
 }
 
+// Host-to-device copy through the context's pinned staging region: the bytes are copied there on
+// the host and the transfer is enqueued without waiting for the stream (a copy from pageable
+// memory would first wait for all earlier work on it), so `src` may be released on return.  When
+// the region is full the stream is drained and the region reused from its start; arrays larger
+// than its largest size go as plain copies.
+int staged_h2d(pmgb_ctx* ctx, void* dst, const void* src, size_t bytes) {
+    if (bytes == 0) return PMGB_OK;
+    constexpr size_t kMin = size_t{4} << 20, kMax = size_t{64} << 20;
+    if (bytes > kMax) {
+        PMGB_CK(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        return PMGB_OK;
+    }
+    const size_t need = (bytes + 255) & ~size_t{255};
+    if (ctx->stage_used + need > ctx->stage_cap) {
+        PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // every staged copy has landed
+        ctx->stage_used = 0;
+        if (need > ctx->stage_cap) {
+            if (ctx->stage) cudaFreeHost(ctx->stage);
+            ctx->stage = nullptr;
+            ctx->stage_cap = 0;
+            size_t cap = kMin;
+            while (cap < need) cap <<= 1;
+            PMGB_CK(ctx, cudaMallocHost(reinterpret_cast<void**>(&ctx->stage), cap));
+            ctx->stage_cap = cap;
+        }
+    }
+    char* at = ctx->stage + ctx->stage_used;
+    std::memcpy(at, src, bytes);
+    PMGB_CK(ctx, cudaMemcpyAsync(dst, at, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    ctx->stage_used += need;
+    return PMGB_OK;
+}
+
 template <class T>
 int upload(pmgb_ctx* ctx, T** dst, const std::vector<T>& v, int64_t* counter = nullptr) {
     *dst = nullptr;
     if (counter) *counter += static_cast<int64_t>(v.size() * sizeof(T));
     const size_t bytes = std::max<size_t>(v.size() * sizeof(T), 16);
     PMGB_CK(ctx, dev_malloc(ctx, reinterpret_cast<void**>(dst), bytes));
-    if (!v.empty())
-        PMGB_CK(ctx, cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
-    return PMGB_OK;
+    return staged_h2d(ctx, *dst, v.data(), v.size() * sizeof(T));
 }
 
 // fractional coordinate -> 32-bit fixed point (x * 2^32 mod 2^32), exact rounding in FP64
@@ -360,6 +405,12 @@ static void ctx_release(pmgb_ctx* ctx) {
         cudaEventDestroy(ev.first);
         cudaEventDestroy(ev.second);
     }
+    for (const auto& t : ctx->es_tables) {
+        cudaFreeAsync(t.d_es, ctx->stream);
+        cudaFreeAsync(t.d_es_df, ctx->stream);
+    }
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->stage) cudaFreeHost(ctx->stage);
     if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -449,7 +500,7 @@ static void free_system_device(pmgb_system* s) {
                     s->in_buf.p,   s->out_buf.p,   s->axes.p,    s->g_u.p,    s->g_dsum.p, s->g_grad.p,
                     s->g_part.p,   s->g_cols.p,   s->r_hist.p,  s->r_cut.p,  s->r_counts.p, s->r_offsets.p,
                     s->r_list.p,   s->r_ref.p,    s->o_counts.p, s->o_perm.p,  s->r_plan.p,  s->r_done.p,
-                    s->r_part.p,   s->acc.p,      s->d_cbox,    s->d_es,     s->d_es_df,  s->d_rec_rq,
+                    s->r_part.p,   s->acc.p,      s->d_cbox,    s->d_rec_rq,
                     s->d_rec_qlo,  s->d_segpar_df, s->d_tk_df, s->x64.p,  s->e_bound.p, s->stats.p};
     for (void* p : ptrs) dev_free(s->ctx, p);
 }
@@ -478,54 +529,115 @@ static void update_centre_image(pmgb_system* s) {
     if (!s->centre_image) s->dev.com_axis = -2;
 }
 
-extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t n_atoms, const double* atom_xf,
-                                  const int32_t* atom_species, int32_t n_charges, const double* charge_xf,
-                                  const double* charge_q, int32_t n_species, const double* epsilon,
-                                  const double* sigma2, double r2_cutoff, int32_t n_guest_atoms,
-                                  const double* guest_atom_x, const int32_t* guest_atom_species,
-                                  int32_t n_guest_charges, const double* guest_charge_x,
-                                  const double* guest_charge_q, pmgb_system** out) {
-    if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
-    if (!out) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_system_create: out is NULL");
-    *out = nullptr;
-    if (!f_to_c) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_system_create: f_to_c is NULL");
+namespace {
+
+// Error of a step that may run off the calling thread: the code and message are kept here and
+// reported through the context afterwards.
+struct Err {
+    int code = PMGB_OK;
+    std::string msg;
+    int set(int c, const char* fmt, ...) {
+        char buf[1024];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        code = c;
+        msg = buf;
+        return c;
+    }
+};
+
+// The arrays of pmgb_system_create.
+struct CreateIn {
+    const double* f_to_c;
+    int32_t n_atoms;
+    const double* atom_xf;
+    const int32_t* atom_species;
+    int32_t n_charges;
+    const double* charge_xf;
+    const double* charge_q;
+    int32_t n_species;
+    const double* epsilon;
+    const double* sigma2;
+    double r2_cutoff;
+    int32_t n_guest_atoms;
+    const double* guest_atom_x;
+    const int32_t* guest_atom_species;
+    int32_t n_guest_charges;
+    const double* guest_charge_x;
+    const double* guest_charge_q;
+};
+
+// What a system's device arrays are built from, computed on the host.
+struct SysHost {
+    std::vector<int4> rec;
+    std::vector<double> rec_q, rec_xf;
+    std::vector<float4> rec_rq;
+    std::vector<float> rec_qlo;
+    std::vector<SegDesc> seg;
+    std::vector<SitePar> par;
+    std::vector<double2> par64;
+    std::vector<float4> par_df;
+    std::vector<ChunkBox> cbox;
+    std::vector<double> qxf, q;
+    bool keep_cbox = false;  // the sub-chunk boxes are worth testing (see the estimate below)
+};
+
+}  // namespace
+
+// Host half of pmgb_system_create: validates the arrays and fills every host-side field of s and
+// the arrays of h; touches neither the device nor the context, so systems can be built on several
+// threads at once.
+static int system_build_host(const CreateIn& in, pmgb_system* s, SysHost& h, Err& er) {
+    const double* f_to_c = in.f_to_c;
+    const int32_t n_atoms = in.n_atoms, n_charges = in.n_charges, n_species = in.n_species;
+    const double *atom_xf = in.atom_xf, *charge_xf = in.charge_xf, *charge_q = in.charge_q;
+    const int32_t* atom_species = in.atom_species;
+    const double *epsilon = in.epsilon, *sigma2 = in.sigma2;
+    const double r2_cutoff = in.r2_cutoff;
+    const int32_t n_guest_atoms = in.n_guest_atoms, n_guest_charges = in.n_guest_charges;
+    const double *guest_atom_x = in.guest_atom_x, *guest_charge_x = in.guest_charge_x,
+                 *guest_charge_q = in.guest_charge_q;
+    const int32_t* guest_atom_species = in.guest_atom_species;
+
+    if (!f_to_c) return er.set(PMGB_ERR_INVALID_ARGUMENT, "pmgb_system_create: f_to_c is NULL");
     for (int k = 0; k < 9; ++k)
-        if (!std::isfinite(f_to_c[k])) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "f_to_c has a non-finite entry");
+        if (!std::isfinite(f_to_c[k])) return er.set(PMGB_ERR_INVALID_ARGUMENT, "f_to_c has a non-finite entry");
     if (n_atoms < 0 || n_charges < 0 || n_guest_atoms < 0 || n_guest_charges < 0 || n_species < 0)
-        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "negative count");
+        return er.set(PMGB_ERR_INVALID_ARGUMENT, "negative count");
     if ((n_atoms > 0 && (!atom_xf || !atom_species)) || (n_charges > 0 && (!charge_xf || !charge_q)) ||
         (n_guest_atoms > 0 && (!guest_atom_x || !guest_atom_species)) ||
         (n_guest_charges > 0 && (!guest_charge_x || !guest_charge_q)) ||
         (n_species > 0 && (!epsilon || !sigma2)))
-        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "NULL array with a nonzero count");
+        return er.set(PMGB_ERR_INVALID_ARGUMENT, "NULL array with a nonzero count");
     if (!(r2_cutoff > 0.0) || !std::isfinite(r2_cutoff))
-        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "r2_cutoff must be positive and finite (got %g)", r2_cutoff);
+        return er.set(PMGB_ERR_INVALID_ARGUMENT, "r2_cutoff must be positive and finite (got %g)", r2_cutoff);
     if (n_guest_atoms + n_guest_charges == 0)
-        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "guest has no atoms and no charges");
+        return er.set(PMGB_ERR_INVALID_ARGUMENT, "guest has no atoms and no charges");
     for (int i = 0; i < n_atoms; ++i) {
         if (atom_species[i] < 0 || atom_species[i] >= n_species)
-            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "framework atom %d: species id %d not in [0, %d)", i,
+            return er.set(PMGB_ERR_INVALID_ARGUMENT, "framework atom %d: species id %d not in [0, %d)", i,
                         atom_species[i], n_species);
         if (!finite3(atom_xf + 3 * i))
-            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "framework atom %d has a non-finite coordinate", i);
+            return er.set(PMGB_ERR_INVALID_ARGUMENT, "framework atom %d has a non-finite coordinate", i);
     }
     for (int i = 0; i < n_charges; ++i)
         if (!finite3(charge_xf + 3 * i) || !std::isfinite(charge_q[i]))
-            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "framework charge %d is not finite", i);
+            return er.set(PMGB_ERR_INVALID_ARGUMENT, "framework charge %d is not finite", i);
     for (int i = 0; i < n_guest_atoms; ++i) {
         if (guest_atom_species[i] < 0 || guest_atom_species[i] >= n_species)
-            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "guest atom %d: species id %d not in [0, %d)", i,
+            return er.set(PMGB_ERR_INVALID_ARGUMENT, "guest atom %d: species id %d not in [0, %d)", i,
                         guest_atom_species[i], n_species);
         if (!finite3(guest_atom_x + 3 * i))
-            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "guest atom %d has a non-finite coordinate", i);
+            return er.set(PMGB_ERR_INVALID_ARGUMENT, "guest atom %d has a non-finite coordinate", i);
     }
     for (int i = 0; i < n_guest_charges; ++i)
         if (!finite3(guest_charge_x + 3 * i) || !std::isfinite(guest_charge_q[i]))
-            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "guest charge %d is not finite", i);
+            return er.set(PMGB_ERR_INVALID_ARGUMENT, "guest charge %d is not finite", i);
     for (int k = 0; k < n_species * n_species; ++k)
         if (!std::isfinite(epsilon[k]) || !std::isfinite(sigma2[k]))
-            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "force-field table entry %d is not finite", k);
-    PMGB_CK(ctx, enter_device(ctx->device));
+            return er.set(PMGB_ERR_INVALID_ARGUMENT, "force-field table entry %d is not finite", k);
 
     // ---- box: upper-triangular factor --------------------------------------------
     double R[9], Q[9], G[9];
@@ -537,7 +649,7 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
         R[1] = R[2] = R[5] = 0.0;
         for (int k = 0; k < 9; ++k) Q[k] = (k % 4 == 0) ? 1.0 : 0.0;
     } else if (!upper_factor(f_to_c, R, Q)) {
-        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "f_to_c is singular");
+        return er.set(PMGB_ERR_INVALID_ARGUMENT, "f_to_c is singular");
     }
     inv_upper(R, G);
 
@@ -546,7 +658,7 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
         double x, y, z, q;
         int species;  // -1: charge-only
     };
-    std::vector<Rec> recs;
+    std::vector<Rec> recs;  // (the local layout of a record while the segments are built)
     recs.reserve(n_atoms + n_charges);
     for (int i = 0; i < n_atoms; ++i)
         recs.push_back(Rec{wrap01(atom_xf[3 * i]), wrap01(atom_xf[3 * i + 1]), wrap01(atom_xf[3 * i + 2]), 0.0,
@@ -585,7 +697,7 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     // groups of them that lie beyond the cutoff.  Sort keys (species, Z code, index) packed in 64
     // bits: 7 + 30 + 27 (index last, so equal codes keep their input order).
     if (recs.size() >= (size_t{1} << 27))
-        return fail(ctx, PMGB_ERR_UNSUPPORTED, "framework has %zu records (max 2^27)", recs.size());
+        return er.set(PMGB_ERR_UNSUPPORTED, "framework has %zu records (max 2^27)", recs.size());
     std::vector<uint64_t> skey(recs.size());
     for (size_t i = 0; i < recs.size(); ++i) {
         const uint32_t zc = spread10(to_fix(recs[i].x) >> 22) | spread10(to_fix(recs[i].y) >> 22) << 1 |
@@ -596,12 +708,12 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     std::sort(skey.begin(), skey.end());
     std::vector<int> order(recs.size());
     for (size_t i = 0; i < recs.size(); ++i) order[i] = static_cast<int>(skey[i] & ((uint64_t{1} << 27) - 1));
-    std::vector<int4> h_rec;
-    std::vector<double> h_rec_q;   // FP64 charge of each record
-    std::vector<double> h_rec_xf;  // its exact fractional coordinates
-    std::vector<float4> h_rec_rq;  // position beyond the fixed point (units of 2^-32), q hi
-    std::vector<float> h_rec_qlo;  // q lo
-    std::vector<SegDesc> h_seg;
+    std::vector<int4>& h_rec = h.rec;
+    std::vector<double>& h_rec_q = h.rec_q;      // FP64 charge of each record
+    std::vector<double>& h_rec_xf = h.rec_xf;    // its exact fractional coordinates
+    std::vector<float4>& h_rec_rq = h.rec_rq;    // position beyond the fixed point (units of 2^-32), q hi
+    std::vector<float>& h_rec_qlo = h.rec_qlo;   // q lo
+    std::vector<SegDesc>& h_seg = h.seg;
     for (size_t p = 0; p < order.size();) {
         const int sp = recs[order[p]].species;
         size_t e = p;
@@ -634,20 +746,15 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
         p = e;
     }
     if (h_seg.size() > PMGB_MAX_SEG)
-        return fail(ctx, PMGB_ERR_UNSUPPORTED, "framework has %zu species segments (max %d)", h_seg.size(),
+        return er.set(PMGB_ERR_UNSUPPORTED, "framework has %zu species segments (max %d)", h_seg.size(),
                     PMGB_MAX_SEG);
 
     // ---- guest sites: merge LJ atoms and charges sharing an offset -------------------
-    pmgb_system* s = new pmgb_system();
-    s->ctx = ctx;
     double body[PMGB_MAX_SITES][3];
     double sq[PMGB_MAX_SITES];
     int ns = 0;
     for (int i = 0; i < n_guest_atoms; ++i) {
-        if (ns >= PMGB_MAX_SITES) {
-            delete s;
-            return fail(ctx, PMGB_ERR_UNSUPPORTED, "guest has more than %d sites", PMGB_MAX_SITES);
-        }
+        if (ns >= PMGB_MAX_SITES) return er.set(PMGB_ERR_UNSUPPORTED, "guest has more than %d sites", PMGB_MAX_SITES);
         for (int d = 0; d < 3; ++d) body[ns][d] = guest_atom_x[3 * i + d];
         s->site_atom[ns] = i;
         s->site_charge[ns] = -1;
@@ -667,10 +774,8 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
             }
         }
         if (hit < 0) {
-            if (ns >= PMGB_MAX_SITES) {
-                delete s;
-                return fail(ctx, PMGB_ERR_UNSUPPORTED, "guest has more than %d sites", PMGB_MAX_SITES);
-            }
+            if (ns >= PMGB_MAX_SITES)
+                return er.set(PMGB_ERR_UNSUPPORTED, "guest has more than %d sites", PMGB_MAX_SITES);
             hit = ns++;
             for (int d = 0; d < 3; ++d) body[hit][d] = guest_charge_x[3 * c + d];
             s->site_atom[hit] = -1;
@@ -686,9 +791,12 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     for (int k = 0; k < ns; ++k) s->site_species.push_back(s->site_atom[k] >= 0 ? guest_atom_species[s->site_atom[k]] : -1);
 
     // per (segment, site) LJ parameters
-    std::vector<SitePar> h_par(h_seg.size() * PMGB_MAX_SITES, SitePar{1.0f, 0.0f, -1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f});
-    std::vector<double2> h_par64(h_seg.size() * PMGB_MAX_SITES, make_double2(-1.0, 0.0));  // -1: no LJ
-    std::vector<float4> h_par_df(h_seg.size() * PMGB_MAX_SITES, make_float4(-1.0f, 0.0f, 0.0f, 0.0f));
+    std::vector<SitePar>& h_par = h.par;
+    std::vector<double2>& h_par64 = h.par64;
+    std::vector<float4>& h_par_df = h.par_df;
+    h_par.assign(h_seg.size() * PMGB_MAX_SITES, SitePar{1.0f, 0.0f, -1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f});
+    h_par64.assign(h_seg.size() * PMGB_MAX_SITES, make_double2(-1.0, 0.0));  // -1: no LJ
+    h_par_df.assign(h_seg.size() * PMGB_MAX_SITES, make_float4(-1.0f, 0.0f, 0.0f, 0.0f));
     for (size_t g = 0; g < h_seg.size(); ++g)
         for (int k = 0; k < ns; ++k) {
             const int a = s->site_atom[k];
@@ -708,7 +816,7 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
         }
 
     // bounding box of every sub-chunk of records, in the kernels' traversal order
-    std::vector<ChunkBox> h_cbox;
+    std::vector<ChunkBox>& h_cbox = h.cbox;
     {
         const int n_rec = static_cast<int>(h_rec.size());
         for (int t0 = 0; t0 < n_rec; t0 += PMGB_TILE) {
@@ -742,37 +850,15 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     }
 
     // charge fractional coordinates for S(k), FP64
-    std::vector<double> h_qxf;
-    std::vector<double> h_q;
+    std::vector<double>& h_qxf = h.qxf;
+    std::vector<double>& h_q = h.q;
     for (int c = 0; c < n_charges; ++c) {
         for (int d = 0; d < 3; ++d) h_qxf.push_back(wrap01(charge_xf[3 * c + d]));
         h_q.push_back(charge_q[c]);
     }
     s->n_q = n_charges;
 
-    int rc = PMGB_OK;
-    int64_t* nb = &s->h2d_bytes;
-    if ((rc = upload(ctx, &s->d_rec, h_rec, nb)) || (rc = upload(ctx, &s->d_cbox, h_cbox, nb)) ||
-        (rc = upload(ctx, &s->d_rec_q, h_rec_q, nb)) ||
-        (rc = upload(ctx, &s->d_segpar64, h_par64, nb)) || (rc = upload(ctx, &s->d_seg, h_seg, nb)) ||
-        (rc = upload(ctx, &s->d_segpar, h_par, nb)) || (rc = upload(ctx, &s->d_qxf, h_qxf, nb)) ||
-        (rc = upload(ctx, &s->d_rec_xf, h_rec_xf, nb)) || (rc = upload(ctx, &s->d_rec_rq, h_rec_rq, nb)) ||
-        (rc = upload(ctx, &s->d_rec_qlo, h_rec_qlo, nb)) || (rc = upload(ctx, &s->d_segpar_df, h_par_df, nb)) ||
-        (rc = upload(ctx, &s->d_q, h_q, nb))) {
-        free_system_device(s);
-        delete s;
-        return rc;
-    }
-    cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) {
-        free_system_device(s);
-        delete s;
-        return cuda_fail(ctx, e, "pmgb_system_create upload");
-    }
-
     SysDev& D = s->dev;
-    D.rec = s->d_rec;
-    D.cbox = s->d_cbox;
     {
         // skipping pays only where sub-chunks often lie beyond the cutoff of a compact group of
         // sites: estimate the skipped fraction 1 - (4/3) pi (rc + rho)^3 / V per sub-chunk (rho:
@@ -796,7 +882,7 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
             const double r = rc + std::sqrt(rho2);
             skip += std::max(0.0, 1.0 - 4.0 / 3.0 * M_PI * r * r * r / vol);
         }
-        if (h_cbox.empty() || skip < 0.1 * static_cast<double>(h_cbox.size())) D.cbox = nullptr;
+        h.keep_cbox = !h_cbox.empty() && skip >= 0.1 * static_cast<double>(h_cbox.size());
     }
     {
         // perpendicular width W_d = 1 / |row d of c_to_f|; unit face normals n_d = row / |row|
@@ -821,8 +907,6 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     D.n_rec = static_cast<int>(h_rec.size());
     D.n_tiles = (D.n_rec + PMGB_TILE - 1) / PMGB_TILE;
     D.n_seg = static_cast<int>(h_seg.size());
-    D.seg = s->d_seg;
-    D.segpar = s->d_segpar;
     const double fix_unit = 1.0 / 4294967296.0;  // one fixed-point step of a fractional coordinate
     D.h00 = static_cast<float>(R[0] * fix_unit);
     D.h01 = static_cast<float>(R[3] * fix_unit);
@@ -857,9 +941,6 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
             for (int m = 0; m < 3; ++m) row += std::fabs(R[i + 3 * m]) * std::fabs(G[m + 3 * j]);
         s->bound_kappa = std::max(s->bound_kappa, row);
     }
-    D.rec_rq = s->d_rec_rq;
-    D.rec_qlo = s->d_rec_qlo;
-    D.segpar_df = s->d_segpar_df;
     D.rc2_df = to_df(r2_cutoff);
     D.rc2e_df = D.rc2_df;
     D.es_tab_df = nullptr;
@@ -870,9 +951,6 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     D.rc2_64 = r2_cutoff;
     D.rc2e_64 = r2_cutoff;
     D.alpha64 = 0.0;
-    D.rec_q = s->d_rec_q;
-    D.rec_xf = s->d_rec_xf;
-    D.segpar64 = s->d_segpar64;
     D.sk64 = nullptr;
     D.wt64 = nullptr;
     D.kabc = nullptr;
@@ -904,6 +982,69 @@ extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t
     D.krow = nullptr;
     D.skw = nullptr;
     D.ks[0] = D.ks[1] = D.ks[2] = 1;
+    return PMGB_OK;
+}
+
+// Device half: allocate and fill the system's arrays from h (ordered on the context's stream;
+// the copies are staged through pinned memory, so h may be released when this returns) and set
+// the device pointers of s->dev.
+static int system_upload(pmgb_ctx* ctx, pmgb_system* s, const SysHost& h) {
+    int rc = PMGB_OK;
+    int64_t* nb = &s->h2d_bytes;
+    if ((rc = upload(ctx, &s->d_rec, h.rec, nb)) || (rc = upload(ctx, &s->d_cbox, h.cbox, nb)) ||
+        (rc = upload(ctx, &s->d_rec_q, h.rec_q, nb)) || (rc = upload(ctx, &s->d_segpar64, h.par64, nb)) ||
+        (rc = upload(ctx, &s->d_seg, h.seg, nb)) || (rc = upload(ctx, &s->d_segpar, h.par, nb)) ||
+        (rc = upload(ctx, &s->d_qxf, h.qxf, nb)) || (rc = upload(ctx, &s->d_rec_xf, h.rec_xf, nb)) ||
+        (rc = upload(ctx, &s->d_rec_rq, h.rec_rq, nb)) || (rc = upload(ctx, &s->d_rec_qlo, h.rec_qlo, nb)) ||
+        (rc = upload(ctx, &s->d_segpar_df, h.par_df, nb)) || (rc = upload(ctx, &s->d_q, h.q, nb)))
+        return rc;
+    SysDev& D = s->dev;
+    D.rec = s->d_rec;
+    D.cbox = h.keep_cbox ? s->d_cbox : nullptr;
+    D.seg = s->d_seg;
+    D.segpar = s->d_segpar;
+    D.rec_rq = s->d_rec_rq;
+    D.rec_qlo = s->d_rec_qlo;
+    D.segpar_df = s->d_segpar_df;
+    D.rec_q = s->d_rec_q;
+    D.rec_xf = s->d_rec_xf;
+    D.segpar64 = s->d_segpar64;
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_system_create(pmgb_ctx* ctx, const double f_to_c[9], int32_t n_atoms, const double* atom_xf,
+                                  const int32_t* atom_species, int32_t n_charges, const double* charge_xf,
+                                  const double* charge_q, int32_t n_species, const double* epsilon,
+                                  const double* sigma2, double r2_cutoff, int32_t n_guest_atoms,
+                                  const double* guest_atom_x, const int32_t* guest_atom_species,
+                                  int32_t n_guest_charges, const double* guest_charge_x,
+                                  const double* guest_charge_q, pmgb_system** out) {
+    if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
+    if (!out) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_system_create: out is NULL");
+    *out = nullptr;
+    const CreateIn in{f_to_c,       n_atoms,      atom_xf,       atom_species,       n_charges,
+                      charge_xf,    charge_q,     n_species,     epsilon,            sigma2,
+                      r2_cutoff,    n_guest_atoms, guest_atom_x, guest_atom_species, n_guest_charges,
+                      guest_charge_x, guest_charge_q};
+    pmgb_system* s = new pmgb_system();
+    s->ctx = ctx;
+    SysHost h;
+    Err er;
+    if (system_build_host(in, s, h, er) != PMGB_OK) {
+        delete s;
+        return fail(ctx, er.code, "%s", er.msg.c_str());
+    }
+    const cudaError_t e0 = enter_device(ctx->device);
+    int rc = e0 != cudaSuccess ? cuda_fail(ctx, e0, "cudaSetDevice") : system_upload(ctx, s, h);
+    if (rc == PMGB_OK) {
+        const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = cuda_fail(ctx, e, "pmgb_system_create upload");
+    }
+    if (rc != PMGB_OK) {
+        free_system_device(s);
+        delete s;
+        return rc;
+    }
     ++ctx->refs;
     *out = s;
     return PMGB_OK;
@@ -965,23 +1106,75 @@ std::vector<double> erfc_over_r_table(double alpha, double s_max) {
 
 }  // namespace
 
-extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cutoff, int32_t n_kvecs,
-                                     const int32_t* kvec_abc, const double* kvec_wt) {
-    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
-    pmgb_ctx* ctx = s->ctx;
-    if (!(alpha > 0.0) || !std::isfinite(alpha) || !(sr_cutoff > 0.0) || !std::isfinite(sr_cutoff))
-        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "Ewald alpha and sr_cutoff must be positive and finite");
-    if (n_kvecs < 0 || (n_kvecs > 0 && (!kvec_abc || !kvec_wt)))
-        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "bad k-vector arrays");
-    PMGB_CK(ctx, enter_device(ctx->device));
-    for (int k = 0; k < n_kvecs; ++k)
-        if (!std::isfinite(kvec_wt[k])) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "k-vector %d weight not finite", k);
-    // group runs of constant (ka, kb) and consecutive kc, then split each run at kc = 0 into
-    // half-rows that start at the kc nearest 0 and step outward
+// The device erfc(alpha r)/r tables (FP64 and double-float) for (alpha, s_max = cutoff^2): built
+// and uploaded on first use, then shared by every system of the context with that Ewald set-up.
+static int es_table_for(pmgb_ctx* ctx, double alpha, double smax, const pmgb_ctx::EsTable** out) {
+    for (const auto& t : ctx->es_tables)
+        if (t.alpha == alpha && t.smax == smax) {
+            *out = &t;
+            return PMGB_OK;
+        }
+    if (ctx->es_table.empty() || ctx->es_alpha != alpha || ctx->es_smax != smax) {
+        ctx->es_table = erfc_over_r_table(alpha, smax);
+        ctx->es_alpha = alpha;
+        ctx->es_smax = smax;
+    }
+    const std::vector<double>& es = ctx->es_table;
+    std::vector<float2> es_df(es.size());
+    for (size_t i = 0; i < es.size(); ++i) es_df[i] = to_df(es[i]);
+    pmgb_ctx::EsTable t{alpha, smax, nullptr, nullptr, static_cast<int>(es.size())};
+    int rc = upload(ctx, &t.d_es, es);
+    if (rc == PMGB_OK) rc = upload(ctx, &t.d_es_df, es_df);
+    if (rc != PMGB_OK) {
+        dev_free(ctx, t.d_es);
+        dev_free(ctx, t.d_es_df);
+        return rc;
+    }
+    ctx->es_tables.push_back(t);
+    *out = &ctx->es_tables.back();
+    return PMGB_OK;
+}
+
+namespace {
+
+// Ewald state of a system computed on the host before S(k) is known: the caller's k-vectors
+// grouped into half-rows.
+struct EwaldHost {
+    double alpha = 0.0, sr_cutoff = 0.0;
+    int n_kvecs = 0;
     std::vector<KRow> rows;
-    std::vector<int> order;
-    std::vector<int> kabc;
+    std::vector<int> order;  // traversal position -> caller's k index
+    std::vector<int> kabc;   // k-vectors in traversal order
     std::vector<double> wt;
+    int kmax[3] = {0, 0, 0};
+};
+
+// ... and after S(k): the k-vectors kept (every one, or the multiples of the replica strides).
+struct EwaldFinal {
+    int ks[3] = {1, 1, 1};
+    bool pruned = false;
+    std::vector<KRow> rows;
+    std::vector<int> kabc;
+    std::vector<double> wt, sk;
+    std::vector<float2> skw;
+    std::vector<float4> tk;   // wt S(k) as double-float, the kept k-vectors
+    std::vector<double> h_sk; // S(k) of every caller k-vector (re, im), caller order
+};
+
+// Validate the Ewald arguments and group the k-vectors: runs of constant (ka, kb) and consecutive
+// kc, each split at kc = 0 into half-rows that start at the kc nearest 0 and step outward.
+// Host only (thread-safe).
+int ewald_build_host(double alpha, double sr_cutoff, int32_t n_kvecs, const int32_t* kvec_abc, const double* kvec_wt,
+                     EwaldHost& eh, Err& er) {
+    if (!(alpha > 0.0) || !std::isfinite(alpha) || !(sr_cutoff > 0.0) || !std::isfinite(sr_cutoff))
+        return er.set(PMGB_ERR_INVALID_ARGUMENT, "Ewald alpha and sr_cutoff must be positive and finite");
+    if (n_kvecs < 0 || (n_kvecs > 0 && (!kvec_abc || !kvec_wt)))
+        return er.set(PMGB_ERR_INVALID_ARGUMENT, "bad k-vector arrays");
+    for (int k = 0; k < n_kvecs; ++k)
+        if (!std::isfinite(kvec_wt[k])) return er.set(PMGB_ERR_INVALID_ARGUMENT, "k-vector %d weight not finite", k);
+    eh.alpha = alpha;
+    eh.sr_cutoff = sr_cutoff;
+    eh.n_kvecs = n_kvecs;
     for (int k = 0; k < n_kvecs;) {
         const int ka = kvec_abc[3 * k], kb = kvec_abc[3 * k + 1], lo = kvec_abc[3 * k + 2];
         int e = k + 1;
@@ -990,18 +1183,18 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
             ++e;
         const int hi = lo + (e - k) - 1;
         auto add_row = [&](int kc_start, int kc_end, int dir) {
-            KRow r{ka, kb, kc_start, 0, static_cast<int>(order.size()), dir, 0, 0};
+            KRow r{ka, kb, kc_start, 0, static_cast<int>(eh.order.size()), dir, 0, 0};
             for (int kc = kc_start;; kc += dir) {
                 const int idx = k + (kc - lo);
-                order.push_back(idx);
-                kabc.push_back(ka);
-                kabc.push_back(kb);
-                kabc.push_back(kc);
-                wt.push_back(kvec_wt[idx]);
+                eh.order.push_back(idx);
+                eh.kabc.push_back(ka);
+                eh.kabc.push_back(kb);
+                eh.kabc.push_back(kc);
+                eh.wt.push_back(kvec_wt[idx]);
                 ++r.n;
                 if (kc == kc_end) break;
             }
-            rows.push_back(r);
+            eh.rows.push_back(r);
         };
         if (lo >= 0) {
             add_row(lo, hi, +1);
@@ -1013,50 +1206,62 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
         }
         k = e;
     }
-    // drop previous Ewald state
-    void* old[] = {s->d_krow, s->d_skw, s->d_sk, s->d_kabc, s->d_wt, s->d_es, s->d_es_df, s->d_tk_df};
+    for (int i = 0; i < n_kvecs; ++i)
+        for (int d = 0; d < 3; ++d) eh.kmax[d] = std::max(eh.kmax[d], std::abs(eh.kabc[3 * i + d]));
+    return PMGB_OK;
+}
+
+}  // namespace
+
+// Drop the system's previous Ewald state, upload the k-vectors and enqueue S(k) of the framework
+// charges (FP64, on the device) and its copy into sk_host (2 n_kvecs doubles, traversal order).
+// Asynchronous when sk_host is pinned; the caller synchronises before reading it.
+static int ewald_launch_sk(pmgb_ctx* ctx, pmgb_system* s, const EwaldHost& eh, double* sk_host) {
+    void* old[] = {s->d_krow, s->d_skw, s->d_sk, s->d_kabc, s->d_wt, s->d_tk_df};
     for (void* p : old) dev_free(ctx, p);
     s->d_krow = nullptr;
     s->d_skw = nullptr;
     s->d_sk = nullptr;
     s->d_kabc = nullptr;
     s->d_wt = nullptr;
-    s->d_es = nullptr;
-    s->d_es_df = nullptr;
     s->d_tk_df = nullptr;
     s->ewald_set = false;
+    const int n_kvecs = eh.n_kvecs;
     int rc;
-    if ((rc = upload(ctx, &s->d_kabc, kabc, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_wt, wt, &s->h2d_bytes)))
+    if ((rc = upload(ctx, &s->d_kabc, eh.kabc, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_wt, eh.wt, &s->h2d_bytes)))
         return rc;
     PMGB_CK(ctx, dev_malloc(ctx, reinterpret_cast<void**>(&s->d_skw), std::max<size_t>(sizeof(float2) * n_kvecs, 16)));
     PMGB_CK(ctx, dev_malloc(ctx, reinterpret_cast<void**>(&s->d_sk), std::max<size_t>(2 * sizeof(double) * n_kvecs, 16)));
-    int kmax[3] = {0, 0, 0};
-    for (int i = 0; i < n_kvecs; ++i)
-        for (int d = 0; d < 3; ++d) kmax[d] = std::max(kmax[d], std::abs(kabc[3 * i + d]));
     double2* d_table = nullptr;  // per-axis phasors of every charge, freed once S(k) is built
-    const size_t table_len = pmgb_structure_factor_table_len(s->n_q, kmax);
+    const size_t table_len = pmgb_structure_factor_table_len(s->n_q, eh.kmax);
     PMGB_CK(ctx, dev_malloc(ctx, reinterpret_cast<void**>(&d_table), std::max<size_t>(sizeof(double2) * table_len, 16)));
-    const cudaError_t e_sk = pmgb_launch_structure_factor(s->d_qxf, s->d_q, s->n_q, s->d_kabc, s->d_wt, n_kvecs, kmax,
-                                                          d_table, s->d_sk, s->d_skw, ctx->stream);
+    const cudaError_t e_sk = pmgb_launch_structure_factor(s->d_qxf, s->d_q, s->n_q, s->d_kabc, s->d_wt, n_kvecs,
+                                                          eh.kmax, d_table, s->d_sk, s->d_skw, ctx->stream);
     dev_free(ctx, d_table);
     PMGB_CK(ctx, e_sk);
-    std::vector<double> sk(2 * static_cast<size_t>(n_kvecs));
     if (n_kvecs > 0)
-        PMGB_CK(ctx, cudaMemcpyAsync(sk.data(), s->d_sk, sizeof(double) * sk.size(), cudaMemcpyDeviceToHost,
+        PMGB_CK(ctx, cudaMemcpyAsync(sk_host, s->d_sk, 2 * sizeof(double) * n_kvecs, cudaMemcpyDeviceToHost,
                                      ctx->stream));
-    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
-    s->h_sk.assign(sk.size(), 0.0);
+    return PMGB_OK;
+}
+
+// With S(k) known (sk: traversal order): the caller-order copy, and for replicated frameworks
+// the k-vectors that can contribute.  S(k) of n_a x n_b x n_c copies of a cell vanishes unless
+// n_d | k_d for every d (the sum over copies of e^{2 pi i k_d j / n_d} is zero otherwise), so
+// those k-vectors add nothing.  The strides ks_d = gcd of k_d over the k-vectors whose |S(k)|
+// exceeds 1e-10 max |S| (the others are FP64 rounding of an exact zero); the k-vectors that are
+// not multiples are dropped if the most they could add, sum wt |S(k)| sum_g |q_g|, stays under
+// 1e-9 K.  A framework that is not a replica keeps every k-vector (ks = 1).  Host only.
+static void ewald_finish_host(const pmgb_system* s, const EwaldHost& eh, const double* sk, EwaldFinal& ef) {
+    const int n_kvecs = eh.n_kvecs;
+    const std::vector<int>& kabc = eh.kabc;
+    const std::vector<double>& wt = eh.wt;
+    ef.h_sk.assign(2 * static_cast<size_t>(n_kvecs), 0.0);
     for (int i = 0; i < n_kvecs; ++i) {
-        s->h_sk[2 * order[i]] = sk[2 * i];
-        s->h_sk[2 * order[i] + 1] = sk[2 * i + 1];
+        ef.h_sk[2 * eh.order[i]] = sk[2 * i];
+        ef.h_sk[2 * eh.order[i] + 1] = sk[2 * i + 1];
     }
-    // Replicated frameworks: S(k) of n_a x n_b x n_c copies of a cell vanishes unless n_d | k_d
-    // for every d (the sum over copies of e^{2 pi i k_d j / n_d} is zero otherwise), so those
-    // k-vectors add nothing.  The strides ks_d = gcd of k_d over the k-vectors whose |S(k)|
-    // exceeds 1e-10 max |S| (the others are FP64 rounding of an exact zero); the k-vectors that
-    // are not multiples are dropped if the most they could add, sum wt |S(k)| sum_g |q_g|, stays
-    // under 1e-9 K.  A framework that is not a replica keeps every k-vector (ks = 1).
-    int ks[3] = {1, 1, 1};
+    int* ks = ef.ks;
     {
         double smax = 0.0;
         for (int i = 0; i < n_kvecs; ++i) smax = std::max(smax, std::hypot(sk[2 * i], sk[2 * i + 1]));
@@ -1073,85 +1278,277 @@ extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cut
                 dropped += std::fabs(wt[i]) * std::hypot(sk[2 * i], sk[2 * i + 1]) * qg;
         if (dropped > 1e-9) ks[0] = ks[1] = ks[2] = 1;
     }
-    int n_eval = n_kvecs;
-    if (ks[0] * ks[1] * ks[2] > 1) {
+    ef.pruned = ks[0] * ks[1] * ks[2] > 1;
+    if (ef.pruned) {
         // kept k-vectors: the multiples, each half-row thinned to every ks2-th kc, rows in k / ks
-        std::vector<KRow> rows_p;
-        std::vector<int> kabc_p;
-        std::vector<double> wt_p, sk_p;
-        std::vector<float2> skw_p;
-        for (const KRow& r : rows) {
+        for (const KRow& r : eh.rows) {
             if (r.ka % ks[0] || r.kb % ks[1]) continue;
-            KRow q{r.ka / ks[0], r.kb / ks[1], 0, 0, static_cast<int>(wt_p.size()), r.dir, 0, 0};
+            KRow q{r.ka / ks[0], r.kb / ks[1], 0, 0, static_cast<int>(ef.wt.size()), r.dir, 0, 0};
             for (int m = 0; m < r.n; ++m) {
                 const int kc = r.kc0 + r.dir * m;
                 if (kc % ks[2]) continue;
                 const int i = r.off + m;
                 if (q.n == 0) q.kc0 = kc / ks[2];
                 ++q.n;
-                kabc_p.insert(kabc_p.end(), {r.ka, r.kb, kc});
-                wt_p.push_back(wt[i]);
-                sk_p.push_back(sk[2 * i]);
-                sk_p.push_back(sk[2 * i + 1]);
-                skw_p.push_back(make_float2(static_cast<float>(wt[i] * sk[2 * i]),
-                                            static_cast<float>(wt[i] * sk[2 * i + 1])));
+                ef.kabc.insert(ef.kabc.end(), {r.ka, r.kb, kc});
+                ef.wt.push_back(wt[i]);
+                ef.sk.push_back(sk[2 * i]);
+                ef.sk.push_back(sk[2 * i + 1]);
+                ef.skw.push_back(make_float2(static_cast<float>(wt[i] * sk[2 * i]),
+                                             static_cast<float>(wt[i] * sk[2 * i + 1])));
             }
-            if (q.n > 0) rows_p.push_back(q);
+            if (q.n > 0) ef.rows.push_back(q);
         }
+    } else {
+        ef.rows = eh.rows;
+        ef.wt = wt;
+        ef.sk.assign(sk, sk + 2 * static_cast<size_t>(n_kvecs));
+    }
+    const size_t n_eval = ef.wt.size();
+    ef.tk.resize(n_eval);
+    for (size_t i = 0; i < n_eval; ++i) {
+        const float2 re = to_df(ef.wt[i] * ef.sk[2 * i]), im = to_df(ef.wt[i] * ef.sk[2 * i + 1]);
+        ef.tk[i] = make_float4(re.x, re.y, im.x, im.y);
+    }
+}
+
+// Device half after S(k): the kept k-vector arrays, the double-float weights, the rows and the
+// shared erfc table; then every Ewald field of s->dev (asynchronous; no synchronisation).
+static int ewald_upload_finish(pmgb_ctx* ctx, pmgb_system* s, EwaldHost& eh, EwaldFinal& ef) {
+    int rc;
+    if (ef.pruned) {
         void* full[] = {s->d_skw, s->d_sk, s->d_kabc, s->d_wt};
         for (void* p : full) dev_free(ctx, p);
         s->d_skw = nullptr;
         s->d_sk = nullptr;
         s->d_kabc = nullptr;
         s->d_wt = nullptr;
-        if ((rc = upload(ctx, &s->d_kabc, kabc_p, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_wt, wt_p, &s->h2d_bytes)) ||
-            (rc = upload(ctx, &s->d_sk, sk_p, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_skw, skw_p, &s->h2d_bytes)))
+        if ((rc = upload(ctx, &s->d_kabc, ef.kabc, &s->h2d_bytes)) ||
+            (rc = upload(ctx, &s->d_wt, ef.wt, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_sk, ef.sk, &s->h2d_bytes)) ||
+            (rc = upload(ctx, &s->d_skw, ef.skw, &s->h2d_bytes)))
             return rc;
-        rows.swap(rows_p);
-        n_eval = static_cast<int>(wt_p.size());
-        wt.swap(wt_p);
-        sk.swap(sk_p);
     }
-    std::vector<float4> tk(static_cast<size_t>(n_eval));  // wt S(k) as double-float, the kept k-vectors
-    for (int i = 0; i < n_eval; ++i) {
-        const float2 re = to_df(wt[i] * sk[2 * i]), im = to_df(wt[i] * sk[2 * i + 1]);
-        tk[i] = make_float4(re.x, re.y, im.x, im.y);
-    }
-    if ((rc = upload(ctx, &s->d_tk_df, tk, &s->h2d_bytes))) return rc;
-    if ((rc = upload(ctx, &s->d_krow, rows, &s->h2d_bytes))) return rc;
-    if (ctx->es_table.empty() || ctx->es_alpha != alpha || ctx->es_smax != sr_cutoff * sr_cutoff) {
-        ctx->es_table = erfc_over_r_table(alpha, sr_cutoff * sr_cutoff);
-        ctx->es_alpha = alpha;
-        ctx->es_smax = sr_cutoff * sr_cutoff;
-    }
-    const std::vector<double>& es = ctx->es_table;
-    std::vector<float2> es_df(es.size());
-    for (size_t i = 0; i < es.size(); ++i) es_df[i] = to_df(es[i]);
-    if ((rc = upload(ctx, &s->d_es, es, &s->h2d_bytes)) || (rc = upload(ctx, &s->d_es_df, es_df, &s->h2d_bytes)))
-        return rc;
-    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // the uploads read host vectors
-    s->n_k = n_kvecs;
-    s->k_order = order;
+    if ((rc = upload(ctx, &s->d_tk_df, ef.tk, &s->h2d_bytes))) return rc;
+    if ((rc = upload(ctx, &s->d_krow, ef.rows, &s->h2d_bytes))) return rc;
+    const pmgb_ctx::EsTable* es = nullptr;
+    if ((rc = es_table_for(ctx, eh.alpha, eh.sr_cutoff * eh.sr_cutoff, &es))) return rc;
+    const double alpha = eh.alpha, sr_cutoff = eh.sr_cutoff;
+    s->n_k = eh.n_kvecs;
+    s->k_order.swap(eh.order);
+    s->h_sk.swap(ef.h_sk);
     s->ewald_set = true;
-    for (int d = 0; d < 3; ++d) s->dev.ks[d] = ks[d];
+    for (int d = 0; d < 3; ++d) s->dev.ks[d] = ef.ks[d];
     s->dev.alpha = static_cast<float>(alpha);
     s->dev.rc2e = static_cast<float>(sr_cutoff * sr_cutoff);
     s->dev.alpha64 = alpha;
     s->dev.rc2e_64 = sr_cutoff * sr_cutoff;
     update_centre_image(s);
-    s->dev.es_tab = s->d_es;
+    s->dev.es_tab = es->d_es;
     s->dev.es_e_lo = PMGB_ES_E_LO;
-    s->dev.es_n_oct = static_cast<int>(es.size() / (PMGB_ES_COEF * PMGB_ES_SUB));
-    s->dev.es_tab_df = s->d_es_df;
+    s->dev.es_n_oct = es->n / (PMGB_ES_COEF * PMGB_ES_SUB);
+    s->dev.es_tab_df = es->d_es_df;
     s->dev.tk_df = s->d_tk_df;
     s->dev.rc2e_df = to_df(sr_cutoff * sr_cutoff);
     s->dev.sk64 = s->d_sk;
     s->dev.wt64 = s->d_wt;
     s->dev.kabc = s->d_kabc;
-    s->dev.n_krow = static_cast<int>(rows.size());
-    s->dev.n_k = n_eval;
+    s->dev.n_krow = static_cast<int>(ef.rows.size());
+    s->dev.n_k = static_cast<int>(ef.wt.size());
     s->dev.krow = s->d_krow;
     s->dev.skw = s->d_skw;
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_system_set_ewald(pmgb_system* s, double alpha, double sr_cutoff, int32_t n_kvecs,
+                                     const int32_t* kvec_abc, const double* kvec_wt) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    pmgb_ctx* ctx = s->ctx;
+    EwaldHost eh;
+    Err er;
+    if (ewald_build_host(alpha, sr_cutoff, n_kvecs, kvec_abc, kvec_wt, eh, er) != PMGB_OK)
+        return fail(ctx, er.code, "%s", er.msg.c_str());
+    PMGB_CK(ctx, enter_device(ctx->device));
+    std::vector<double> sk(2 * static_cast<size_t>(n_kvecs));
+    if (int rc = ewald_launch_sk(ctx, s, eh, sk.data())) return rc;
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    EwaldFinal ef;
+    ewald_finish_host(s, eh, sk.data(), ef);
+    if (int rc = ewald_upload_finish(ctx, s, eh, ef)) return rc;
+    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return PMGB_OK;
+}
+
+// Run body(i) for i in [0, n) on up to n_threads host threads (0: one per hardware thread).
+template <class F>
+static void run_parallel(int n, int n_threads, F body) {
+    int t = n_threads > 0 ? n_threads : static_cast<int>(std::thread::hardware_concurrency());
+    t = std::max(1, std::min({t, 64, n}));
+    if (t == 1) {
+        for (int i = 0; i < n; ++i) body(i);
+        return;
+    }
+    std::atomic<int> next{0};
+    std::vector<std::thread> pool;
+    pool.reserve(t);
+    for (int k = 0; k < t; ++k)
+        pool.emplace_back([&] {
+            for (int i = next++; i < n; i = next++) body(i);
+        });
+    for (auto& th : pool) th.join();
+}
+
+extern "C" int pmgb_systems_create_unitcell(pmgb_ctx* ctx, int32_t n_systems, const double* const* f_to_c,
+                                            const int32_t* n_atoms, const double* const* atom_xf,
+                                            const int32_t* const* atom_species, const int32_t* n_charges,
+                                            const double* const* charge_xf, const double* const* charge_q,
+                                            const int32_t* n_species, const double* const* epsilon,
+                                            const double* const* sigma2, double r_cutoff, const int32_t* n_guest_atoms,
+                                            const double* const* guest_atom_x, const int32_t* const* guest_atom_species,
+                                            const int32_t* n_guest_charges, const double* const* guest_charge_x,
+                                            const double* const* guest_charge_q, double ewald_precision,
+                                            int32_t n_threads, int32_t* repfactors_out, pmgb_system** out) {
+    if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
+    const char* self = n_systems == 1 ? "pmgb_system_create_unitcell" : "pmgb_systems_create_unitcell";
+    if (n_systems < 0 || !out ||
+        (n_systems > 0 && (!f_to_c || !n_atoms || !atom_xf || !atom_species || !n_charges || !charge_xf ||
+                           !charge_q || !n_species || !epsilon || !sigma2 || !n_guest_atoms || !guest_atom_x ||
+                           !guest_atom_species || !n_guest_charges || !guest_charge_x || !guest_charge_q)))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "%s: bad arguments", self);
+    for (int i = 0; i < n_systems; ++i) out[i] = nullptr;
+    if (n_systems == 0) return PMGB_OK;
+    struct Item {
+        pmgb_system* s = nullptr;
+        SysHost h;
+        bool charged = false;
+        EwaldHost eh;
+        EwaldFinal ef;
+        size_t sk_off = 0;
+        int32_t rep[3] = {1, 1, 1};
+        Err er;
+    };
+    std::vector<Item> items(static_cast<size_t>(n_systems));
+    for (Item& it : items) {
+        it.s = new pmgb_system();
+        it.s->ctx = ctx;
+    }
+    auto give_up = [&](int rc) {
+        for (Item& it : items) {
+            free_system_device(it.s);
+            delete it.s;
+        }
+        return rc;
+    };
+    // host: supercell, records and, for charged pairs, the Ewald parameters and k-vector rows
+    run_parallel(n_systems, n_threads, [&](int i) {
+        Item& it = items[i];
+        try {
+            PmgbSupercell sc;
+            const char* why = nullptr;
+            if (pmgb_make_supercell(f_to_c[i], r_cutoff, n_atoms[i], atom_xf[i], atom_species[i], n_charges[i],
+                                    charge_xf[i], charge_q[i], sc, &why) != PMGB_OK) {
+                it.er.set(PMGB_ERR_INVALID_ARGUMENT, "%s", why);
+                return;
+            }
+            for (int d = 0; d < 3; ++d) it.rep[d] = sc.rep[d];
+            const CreateIn in{sc.f_to_c,
+                              static_cast<int32_t>(sc.atom_species.size()),
+                              sc.atom_xf.data(),
+                              sc.atom_species.data(),
+                              static_cast<int32_t>(sc.charge_q.size()),
+                              sc.charge_xf.data(),
+                              sc.charge_q.data(),
+                              n_species[i],
+                              epsilon[i],
+                              sigma2[i],
+                              r_cutoff * r_cutoff,
+                              n_guest_atoms[i],
+                              guest_atom_x[i],
+                              guest_atom_species[i],
+                              n_guest_charges[i],
+                              guest_charge_x[i],
+                              guest_charge_q[i]};
+            if (system_build_host(in, it.s, it.h, it.er) != PMGB_OK) return;
+            it.charged = n_charges[i] > 0 && n_guest_charges[i] > 0;  // src/henry.jl:93-97
+            if (it.charged) {
+                double alpha = 0.0;
+                int64_t n_k = 0;
+                std::vector<int32_t> abc;
+                std::vector<double> wt;
+                if (pmgb_ewald_kvectors(sc.f_to_c, r_cutoff, ewald_precision, &alpha, nullptr, nullptr, &abc, &wt,
+                                        &n_k) != PMGB_OK ||
+                    n_k > INT32_MAX) {
+                    it.er.set(PMGB_ERR_INVALID_ARGUMENT, "Ewald set-up failed (precision must lie in (0, 1))");
+                    return;
+                }
+                ewald_build_host(alpha, r_cutoff, static_cast<int32_t>(n_k), abc.data(), wt.data(), it.eh, it.er);
+            }
+        } catch (const std::bad_alloc&) {
+            it.er.set(PMGB_ERR_OUT_OF_MEMORY, "host memory exhausted");
+        }
+    });
+    for (int i = 0; i < n_systems; ++i)
+        if (items[i].er.code != PMGB_OK) {
+            const int code = items[i].er.code;
+            if (n_systems == 1) fail(ctx, code, "%s: %s", self, items[i].er.msg.c_str());
+            else fail(ctx, code, "%s: system %d: %s", self, i, items[i].er.msg.c_str());
+            return give_up(code);
+        }
+    // device: every system's arrays, then S(k) of the charged ones, back to back
+    cudaError_t e = enter_device(ctx->device);
+    if (e != cudaSuccess) return give_up(cuda_fail(ctx, e, "cudaSetDevice"));
+    size_t sk_total = 0;
+    for (Item& it : items)
+        if (it.charged) {
+            it.sk_off = sk_total;
+            sk_total += 2 * static_cast<size_t>(it.eh.n_kvecs);
+        }
+    double* sk = nullptr;  // pinned: the S(k) copies do not wait on one another
+    if (sk_total > 0) {
+        e = cudaMallocHost(reinterpret_cast<void**>(&sk), sizeof(double) * sk_total);
+        if (e != cudaSuccess) return give_up(cuda_fail(ctx, e, "cudaMallocHost"));
+    }
+    auto finish = [&](int rc) {
+        if (sk) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFreeHost(sk);
+        }
+        return rc == PMGB_OK ? rc : give_up(rc);
+    };
+    for (Item& it : items) {
+        int rc = system_upload(ctx, it.s, it.h);
+        if (rc == PMGB_OK && it.charged) rc = ewald_launch_sk(ctx, it.s, it.eh, sk + it.sk_off);
+        if (rc != PMGB_OK) return finish(rc);
+        it.h = SysHost{};  // staged: the host arrays are no longer needed
+    }
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return finish(cuda_fail(ctx, e, self));
+    // host: the k-vectors kept once S(k) is known
+    run_parallel(n_systems, n_threads, [&](int i) {
+        Item& it = items[i];
+        if (!it.charged) return;
+        try {
+            ewald_finish_host(it.s, it.eh, sk + it.sk_off, it.ef);
+        } catch (const std::bad_alloc&) {
+            it.er.set(PMGB_ERR_OUT_OF_MEMORY, "host memory exhausted");
+        }
+    });
+    for (int i = 0; i < n_systems; ++i)
+        if (items[i].er.code != PMGB_OK) {
+            fail(ctx, items[i].er.code, "%s: system %d: %s", self, i, items[i].er.msg.c_str());
+            return finish(items[i].er.code);
+        }
+    for (Item& it : items)
+        if (it.charged)
+            if (int rc = ewald_upload_finish(ctx, it.s, it.eh, it.ef)) return finish(rc);
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return finish(cuda_fail(ctx, e, self));
+    finish(PMGB_OK);
+    for (int i = 0; i < n_systems; ++i) {
+        ++ctx->refs;
+        out[i] = items[i].s;
+        if (repfactors_out)
+            for (int d = 0; d < 3; ++d) repfactors_out[3 * i + d] = items[i].rep[d];
+    }
     return PMGB_OK;
 }
 

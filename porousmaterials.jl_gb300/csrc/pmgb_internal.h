@@ -15,6 +15,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <vector>
 
 #define PMGB_MAX_SITES 8      // guest sites (merged LJ atoms + point charges)
 #define PMGB_MAX_SEG 64       // framework species segments
@@ -369,6 +370,20 @@ size_t pmgb_pairs_smem_bytes();
 // record a failure message on ctx and return code (defined in pmgb_api.cu)
 struct pmgb_ctx;
 int pmgb_fail_message(pmgb_ctx* ctx, int code, const char* message);
+
+// host set-up helpers (defined in pmgb_setup.cu)
+struct PmgbSupercell {
+    int32_t rep[3];
+    double f_to_c[9];
+    std::vector<double> atom_xf, charge_xf, charge_q;
+    std::vector<int32_t> atom_species;
+};
+int pmgb_make_supercell(const double f_to_c[9], double r_cutoff, int32_t n_atoms, const double* atom_xf,
+                        const int32_t* atom_species, int32_t n_charges, const double* charge_xf,
+                        const double* charge_q, PmgbSupercell& sc, const char** why);
+int pmgb_ewald_kvectors(const double f_to_c[9], double sr_cutoff, double precision, double* alpha_out,
+                        double* max_k2_out, int32_t kreps_out[3], std::vector<int32_t>* abc, std::vector<double>* wt,
+                        int64_t* n_k_out);
 
 // fixed per-device scratch of pmgb_widom_noalloc (defined in pmgb_kernels.cu)
 #define PMGB_NOALLOC_MAX_CTAS 65536   // LsePartial entries: 3 MiB, up to 16.7M insertions per call

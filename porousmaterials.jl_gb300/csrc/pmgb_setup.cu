@@ -109,11 +109,12 @@ extern "C" int pmgb_replication_factors(const double f_to_c[9], double r_cutoff,
     return PMGB_OK;
 }
 
-extern "C" int pmgb_ewald_setup(const double f_to_c[9], double sr_cutoff, double precision, int64_t capacity,
-                                double* alpha_out, double* max_k2_out, int32_t kreps_out[3], int64_t* n_kvecs_out,
-                                int32_t* kvec_abc, double* kvec_wt) {
-    if (!f_to_c || !n_kvecs_out || !(sr_cutoff > 0.0) || !std::isfinite(sr_cutoff) || !(precision > 0.0) ||
-        !(precision < 1.0) || capacity < 0 || (capacity > 0 && (!kvec_abc || !kvec_wt)))
+// setup_Ewald_sum for the box f_to_c: alpha, |k|^2_max, kreps and, when abc/wt are given, the
+// k-vectors with their weights appended in the reference's order; n_k receives their count.
+int pmgb_ewald_kvectors(const double f_to_c[9], double sr_cutoff, double precision, double* alpha_out,
+                        double* max_k2_out, int32_t kreps_out[3], std::vector<int32_t>* abc, std::vector<double>* wt,
+                        int64_t* n_k_out) {
+    if (!f_to_c || !(sr_cutoff > 0.0) || !std::isfinite(sr_cutoff) || !(precision > 0.0) || !(precision < 1.0))
         return PMGB_ERR_INVALID_ARGUMENT;
     double rec[3][3];
     if (!reciprocal(f_to_c, rec)) return PMGB_ERR_INVALID_ARGUMENT;
@@ -152,44 +153,58 @@ extern "C" int pmgb_ewald_setup(const double f_to_c[9], double sr_cutoff, double
                 for (int d = 0; d < 3; ++d) k[d] = ka * rec[0][d] + kb * rec[1][d] + kc * rec[2][d];
                 const double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
                 if (!(k2 < max_k2)) continue;
-                if (n_k < capacity) {
-                    kvec_abc[3 * n_k + 0] = ka;
-                    kvec_abc[3 * n_k + 1] = kb;
-                    kvec_abc[3 * n_k + 2] = kc;
-                    kvec_wt[n_k] = 2.0 * std::exp(-k2 / (4.0 * alpha * alpha)) / k2 / e0 / omega;
-                }
+                if (abc) abc->insert(abc->end(), {ka, kb, kc});
+                if (wt) wt->push_back(2.0 * std::exp(-k2 / (4.0 * alpha * alpha)) / k2 / e0 / omega);
                 ++n_k;
             }
     if (alpha_out) *alpha_out = alpha;
     if (max_k2_out) *max_k2_out = max_k2;
     if (kreps_out)
         for (int d = 0; d < 3; ++d) kreps_out[d] = kreps[d];
-    *n_kvecs_out = n_k;
-    return (capacity > 0 && n_k > capacity) ? PMGB_ERR_INVALID_ARGUMENT : PMGB_OK;
+    if (n_k_out) *n_k_out = n_k;
+    return PMGB_OK;
 }
 
-extern "C" int pmgb_system_create_unitcell(pmgb_ctx* ctx, const double f_to_c[9], int32_t n_atoms,
-                                           const double* atom_xf, const int32_t* atom_species, int32_t n_charges,
-                                           const double* charge_xf, const double* charge_q, int32_t n_species,
-                                           const double* epsilon, const double* sigma2, double r_cutoff,
-                                           int32_t n_guest_atoms, const double* guest_atom_x,
-                                           const int32_t* guest_atom_species, int32_t n_guest_charges,
-                                           const double* guest_charge_x, const double* guest_charge_q,
-                                           double ewald_precision, int32_t repfactors_out[3], pmgb_system** out) {
-    if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
-    if (!out || !f_to_c || n_atoms < 0 || n_charges < 0 || (n_atoms > 0 && (!atom_xf || !atom_species)) ||
+extern "C" int pmgb_ewald_setup(const double f_to_c[9], double sr_cutoff, double precision, int64_t capacity,
+                                double* alpha_out, double* max_k2_out, int32_t kreps_out[3], int64_t* n_kvecs_out,
+                                int32_t* kvec_abc, double* kvec_wt) {
+    if (!n_kvecs_out || capacity < 0 || (capacity > 0 && (!kvec_abc || !kvec_wt))) return PMGB_ERR_INVALID_ARGUMENT;
+    std::vector<int32_t> abc;
+    std::vector<double> wt;
+    int64_t n_k = 0;
+    const int rc = pmgb_ewald_kvectors(f_to_c, sr_cutoff, precision, alpha_out, max_k2_out, kreps_out,
+                                       capacity > 0 ? &abc : nullptr, capacity > 0 ? &wt : nullptr, &n_k);
+    if (rc != PMGB_OK) return rc;
+    *n_kvecs_out = n_k;
+    if (capacity > 0 && n_k > capacity) return PMGB_ERR_INVALID_ARGUMENT;
+    if (capacity > 0) {
+        std::copy(abc.begin(), abc.end(), kvec_abc);
+        std::copy(wt.begin(), wt.end(), kvec_wt);
+    }
+    return PMGB_OK;
+}
+
+// The supercell of henry_coefficient's set-up (src/henry.jl:78-86): replication factors for
+// r_cutoff and the replicated arrays -- images (i, j, k) with k fastest, each holding every atom
+// in order, fractional coordinates rescaled into the supercell, (x + shift) / rep
+// (Xtals.replicate).  why names a failure.
+int pmgb_make_supercell(const double f_to_c[9], double r_cutoff, int32_t n_atoms, const double* atom_xf,
+                        const int32_t* atom_species, int32_t n_charges, const double* charge_xf,
+                        const double* charge_q, PmgbSupercell& sc, const char** why) {
+    *why = "bad arguments";
+    if (!f_to_c || n_atoms < 0 || n_charges < 0 || (n_atoms > 0 && (!atom_xf || !atom_species)) ||
         (n_charges > 0 && (!charge_xf || !charge_q)))
-        return pmgb_fail_message(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_system_create_unitcell: bad arguments");
-    int32_t rep[3];
-    if (pmgb_replication_factors(f_to_c, r_cutoff, rep) != PMGB_OK)
-        return pmgb_fail_message(ctx, PMGB_ERR_INVALID_ARGUMENT,
-                                 "pmgb_system_create_unitcell: the box must be finite and non-singular and the cutoff "
-                                 "positive");
+        return PMGB_ERR_INVALID_ARGUMENT;
+    int32_t* rep = sc.rep;
+    if (pmgb_replication_factors(f_to_c, r_cutoff, rep) != PMGB_OK) {
+        *why = "the box must be finite and non-singular and the cutoff positive";
+        return PMGB_ERR_INVALID_ARGUMENT;
+    }
     const int64_t n_img = int64_t(rep[0]) * rep[1] * rep[2];
-    if (n_img * std::max(n_atoms, n_charges) > INT32_MAX)
-        return pmgb_fail_message(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_system_create_unitcell: supercell too large");
-    // the supercell: images (i, j, k) with k fastest, each holding every atom in order; fractional
-    // coordinates rescaled into the supercell, (x + shift) / rep (Xtals.replicate)
+    if (n_img * std::max(n_atoms, n_charges) > INT32_MAX) {
+        *why = "supercell too large";
+        return PMGB_ERR_INVALID_ARGUMENT;
+    }
     auto replicate = [&](int32_t n, const double* xf, std::vector<double>& out_xf) {
         out_xf.resize(static_cast<size_t>(3 * n * n_img));
         size_t w = 0;
@@ -202,47 +217,36 @@ extern "C" int pmgb_system_create_unitcell(pmgb_ctx* ctx, const double f_to_c[9]
                         out_xf[w++] = (xf[3 * a + 2] + k) / rep[2];
                     }
     };
-    std::vector<double> sxf, sqxf, sq;
-    std::vector<int32_t> ssp;
-    replicate(n_atoms, atom_xf, sxf);
-    replicate(n_charges, charge_xf, sqxf);
-    ssp.reserve(static_cast<size_t>(n_atoms * n_img));
-    sq.reserve(static_cast<size_t>(n_charges * n_img));
+    replicate(n_atoms, atom_xf, sc.atom_xf);
+    replicate(n_charges, charge_xf, sc.charge_xf);
+    sc.atom_species.clear();
+    sc.charge_q.clear();
+    sc.atom_species.reserve(static_cast<size_t>(n_atoms * n_img));
+    sc.charge_q.reserve(static_cast<size_t>(n_charges * n_img));
     for (int64_t m = 0; m < n_img; ++m) {
-        ssp.insert(ssp.end(), atom_species, atom_species + n_atoms);
-        sq.insert(sq.end(), charge_q, charge_q + n_charges);
+        sc.atom_species.insert(sc.atom_species.end(), atom_species, atom_species + n_atoms);
+        sc.charge_q.insert(sc.charge_q.end(), charge_q, charge_q + n_charges);
     }
-    double sf[9];
     for (int j = 0; j < 3; ++j)
-        for (int i = 0; i < 3; ++i) sf[i + 3 * j] = f_to_c[i + 3 * j] * rep[j];
-    pmgb_system* s = nullptr;
-    const int32_t n_sa = static_cast<int32_t>(n_atoms * n_img), n_sq = static_cast<int32_t>(n_charges * n_img);
-    if (int rc = pmgb_system_create(ctx, sf, n_sa, sxf.data(), ssp.data(), n_sq, sqxf.data(), sq.data(), n_species,
-                                    epsilon, sigma2, r_cutoff * r_cutoff, n_guest_atoms, guest_atom_x,
-                                    guest_atom_species, n_guest_charges, guest_charge_x, guest_charge_q, &s))
-        return rc;
-    if (n_charges > 0 && n_guest_charges > 0) {  // src/henry.jl:93-97
-        double alpha = 0.0;
-        int64_t n_k = 0;
-        int rc = pmgb_ewald_setup(sf, r_cutoff, ewald_precision, 0, nullptr, nullptr, nullptr, &n_k, nullptr, nullptr);
-        std::vector<int32_t> abc(static_cast<size_t>(3 * n_k));
-        std::vector<double> wt(static_cast<size_t>(n_k));
-        if (rc == PMGB_OK)
-            rc = pmgb_ewald_setup(sf, r_cutoff, ewald_precision, n_k, &alpha, nullptr, nullptr, &n_k, abc.data(),
-                                  wt.data());
-        if (rc == PMGB_OK && n_k > INT32_MAX) rc = PMGB_ERR_INVALID_ARGUMENT;
-        if (rc == PMGB_OK)
-            rc = pmgb_system_set_ewald(s, alpha, r_cutoff, static_cast<int32_t>(n_k), abc.data(), wt.data());
-        if (rc != PMGB_OK) {
-            pmgb_system_destroy(s);
-            return rc == PMGB_ERR_INVALID_ARGUMENT
-                       ? pmgb_fail_message(ctx, rc, "pmgb_system_create_unitcell: Ewald set-up failed (precision "
-                                                    "must lie in (0, 1))")
-                       : rc;
-        }
-    }
-    if (repfactors_out)
-        for (int d = 0; d < 3; ++d) repfactors_out[d] = rep[d];
-    *out = s;
+        for (int i = 0; i < 3; ++i) sc.f_to_c[i + 3 * j] = f_to_c[i + 3 * j] * rep[j];
     return PMGB_OK;
+}
+
+extern "C" int pmgb_system_create_unitcell(pmgb_ctx* ctx, const double f_to_c[9], int32_t n_atoms,
+                                           const double* atom_xf, const int32_t* atom_species, int32_t n_charges,
+                                           const double* charge_xf, const double* charge_q, int32_t n_species,
+                                           const double* epsilon, const double* sigma2, double r_cutoff,
+                                           int32_t n_guest_atoms, const double* guest_atom_x,
+                                           const int32_t* guest_atom_species, int32_t n_guest_charges,
+                                           const double* guest_charge_x, const double* guest_charge_q,
+                                           double ewald_precision, int32_t repfactors_out[3], pmgb_system** out) {
+    if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
+    int32_t rep[3] = {1, 1, 1};
+    const int rc = pmgb_systems_create_unitcell(ctx, 1, &f_to_c, &n_atoms, &atom_xf, &atom_species, &n_charges,
+                                                &charge_xf, &charge_q, &n_species, &epsilon, &sigma2, r_cutoff,
+                                                &n_guest_atoms, &guest_atom_x, &guest_atom_species, &n_guest_charges,
+                                                &guest_charge_x, &guest_charge_q, ewald_precision, 1, rep, out);
+    if (rc == PMGB_OK && repfactors_out)
+        for (int d = 0; d < 3; ++d) repfactors_out[d] = rep[d];
+    return rc;
 }

@@ -47,6 +47,10 @@ SIGNATURES = [
     ("pmgb_system_create_unitcell", C.c_int,
      [_vp, _dp, C.c_int32, _dp, _ip, C.c_int32, _dp, _dp, C.c_int32, _dp, _dp, C.c_double,
       C.c_int32, _dp, _ip, C.c_int32, _dp, _dp, C.c_double, _ip, C.POINTER(_vp)]),
+    ("pmgb_systems_create_unitcell", C.c_int,
+     [_vp, C.c_int32, C.POINTER(_dp), _ip, C.POINTER(_dp), C.POINTER(_ip), _ip, C.POINTER(_dp), C.POINTER(_dp), _ip,
+      C.POINTER(_dp), C.POINTER(_dp), C.c_double, _ip, C.POINTER(_dp), C.POINTER(_ip), _ip, C.POINTER(_dp),
+      C.POINTER(_dp), C.c_double, C.c_int32, _ip, C.POINTER(_vp)]),
     ("pmgb_system_destroy", None, [_vp]),
     ("pmgb_system_info", C.c_int, [_vp, C.POINTER(C.c_int64)]),
     ("pmgb_system_n_sites", C.c_int, [_vp]),

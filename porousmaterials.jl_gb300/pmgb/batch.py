@@ -141,13 +141,14 @@ class BatchScreen:
 
 
 def build_systems(crystals: list[Crystal], molecule: Molecule | list[Molecule], ljff: LJForceField, *,
-                  ewald_precision: float = 1e-6, ctx: Context | None = None) -> list[GPUSystem]:
-    """One GPUSystem per crystal (replicated for the cutoff, Ewald set up when both are charged)."""
+                  ewald_precision: float = 1e-6, ctx: Context | None = None, n_threads: int = 0) -> list[GPUSystem]:
+    """One GPUSystem per crystal (replicated for the cutoff, Ewald set up when both are charged),
+    all built in one native call (pmgb_systems_create_unitcell: host set-up on n_threads threads,
+    0 = all; device set-up back to back)."""
     ctx = ctx or Context.default()
-    mols = molecule if isinstance(molecule, (list, tuple)) else [molecule] * len(crystals)
-    # replication, supercell and Ewald set-up natively per framework (pmgb_system_create_unitcell)
-    return [GPUSystem.from_unit_cell(cr, mol, ljff, ewald_precision=ewald_precision, ctx=ctx)
-            for cr, mol in zip(crystals, mols)]
+    mols = list(molecule) if isinstance(molecule, (list, tuple)) else [molecule] * len(crystals)
+    return GPUSystem.many_from_unit_cells(list(crystals), mols, ljff, ewald_precision=ewald_precision, ctx=ctx,
+                                          n_threads=n_threads)
 
 
 def henry_coefficient_screen(crystals: list[Crystal], molecule: Molecule | list[Molecule], temperature: float,

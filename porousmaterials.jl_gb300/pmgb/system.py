@@ -76,16 +76,11 @@ class GPUSystem:
             self.set_refine(refine_tail)
 
     @classmethod
-    def from_unit_cell(cls, crystal: Crystal, molecule: Molecule, ljff: LJForceField, *,
-                       ewald_precision: float = 1e-6, ctx: Context | None = None,
-                       refine_tail: float = 0.0) -> "GPUSystem":
-        """The system henry_coefficient sets up from a UNIT cell (src/henry.jl:78-97), built natively
-        by pmgb_system_create_unitcell: replication for the cutoff, the replicated supercell and, when
-        framework and guest are charged, the Ewald parameters at ewald_precision.  The supercell
-        `crystal`, the guest in its fractions `molecule` and the `eparams` are built on the host only
-        if a caller reads them."""
+    def _unit_cell_prep(cls, crystal: Crystal, molecule: Molecule, ljff: LJForceField, ewald_precision: float,
+                        ctx: Context) -> "GPUSystem":
+        """A GPUSystem shell holding the host arrays of pmgb_system_create_unitcell (no handle yet)."""
         self = cls.__new__(cls)
-        self.ctx = ctx or Context.default()
+        self.ctx = ctx
         self.ljff = ljff
         self._unit = crystal
         self._ewald_precision = float(ewald_precision)
@@ -96,40 +91,96 @@ class GPUSystem:
         eps, sig2 = ljff.tables(species)
         self._eps = np.ascontiguousarray(eps)
         self._sig2 = np.ascontiguousarray(sig2)
-        atom_xf = np.ascontiguousarray(crystal.atoms.xf, dtype=np.float64)
-        atom_sp = np.fromiter(map(sid.__getitem__, crystal.atoms.species), dtype=np.int32,
-                              count=len(crystal.atoms.species))
-        q_xf = np.ascontiguousarray(crystal.charges.xf, dtype=np.float64)
-        q = np.ascontiguousarray(crystal.charges.q, dtype=np.float64)
-        f_to_c = np.ascontiguousarray(crystal.box.f_to_c.T.reshape(-1))  # column-major
+        self._atom_xf = np.ascontiguousarray(crystal.atoms.xf, dtype=np.float64)
+        self._atom_sp = np.fromiter(map(sid.__getitem__, crystal.atoms.species), dtype=np.int32,
+                                    count=len(crystal.atoms.species))
+        self._q_xf = np.ascontiguousarray(crystal.charges.xf, dtype=np.float64)
+        self._q = np.ascontiguousarray(crystal.charges.q, dtype=np.float64)
+        self._f_to_c = np.ascontiguousarray(crystal.box.f_to_c.T.reshape(-1))  # column-major
         ax, qx = body_offsets(molecule, crystal.box)
         self._gax = np.ascontiguousarray(ax, dtype=np.float64)
         self._gsp = np.ascontiguousarray([sid[s_] for s_ in molecule.atom_species], dtype=np.int32)
         self._gqx = np.ascontiguousarray(qx, dtype=np.float64)
         self._gq = np.ascontiguousarray(molecule.charge_q, dtype=np.float64)
+        self.charged = has_charges(crystal) and molecule.n_charges > 0
+        self.refine_tail = 0.0
+        return self
+
+    def _unit_cell_done(self, handle, rep) -> None:
+        """Take the handle made from the arrays of _unit_cell_prep (which are then released)."""
+        lib = self.ctx._lib
+        self.handle = handle
+        self.repfactors = tuple(int(r) for r in rep)
+        for k in ("_atom_xf", "_atom_sp", "_q_xf", "_q", "_f_to_c"):
+            del self.__dict__[k]
+        self.n_sites = int(lib.pmgb_system_n_sites(handle))
+        sa = np.zeros(self.n_sites, dtype=np.int32)
+        sc = np.zeros(self.n_sites, dtype=np.int32)
+        self.ctx.check(lib.pmgb_system_sites(handle, ptr(sa, C.c_int32), ptr(sc, C.c_int32)))
+        self.site_atom, self.site_charge = sa, sc
+
+    @classmethod
+    def from_unit_cell(cls, crystal: Crystal, molecule: Molecule, ljff: LJForceField, *,
+                       ewald_precision: float = 1e-6, ctx: Context | None = None,
+                       refine_tail: float = 0.0) -> "GPUSystem":
+        """The system henry_coefficient sets up from a UNIT cell (src/henry.jl:78-97), built natively
+        by pmgb_system_create_unitcell: replication for the cutoff, the replicated supercell and, when
+        framework and guest are charged, the Ewald parameters at ewald_precision.  The supercell
+        `crystal`, the guest in its fractions `molecule` and the `eparams` are built on the host only
+        if a caller reads them."""
+        self = cls._unit_cell_prep(crystal, molecule, ljff, ewald_precision, ctx or Context.default())
         h = C.c_void_p()
         rep_ = (C.c_int32 * 3)()
         lib = self.ctx._lib
         self.ctx.check(lib.pmgb_system_create_unitcell(
-            self.ctx.handle, ptr(f_to_c, C.c_double),
-            len(atom_sp), ptr(atom_xf, C.c_double), ptr(atom_sp, C.c_int32),
-            q.shape[0], ptr(q_xf, C.c_double), ptr(q, C.c_double),
-            len(species), ptr(self._eps, C.c_double), ptr(self._sig2, C.c_double), float(ljff.r_cutoff),
+            self.ctx.handle, ptr(self._f_to_c, C.c_double),
+            len(self._atom_sp), ptr(self._atom_xf, C.c_double), ptr(self._atom_sp, C.c_int32),
+            self._q.shape[0], ptr(self._q_xf, C.c_double), ptr(self._q, C.c_double),
+            len(self.species), ptr(self._eps, C.c_double), ptr(self._sig2, C.c_double), float(ljff.r_cutoff),
             len(self._gsp), ptr(self._gax, C.c_double), ptr(self._gsp, C.c_int32),
             self._gq.shape[0], ptr(self._gqx, C.c_double), ptr(self._gq, C.c_double),
             float(ewald_precision), rep_, C.byref(h)))
-        self.handle = h
-        self.repfactors = tuple(int(r) for r in rep_)
-        self.charged = has_charges(crystal) and molecule.n_charges > 0
-        self.n_sites = int(lib.pmgb_system_n_sites(h))
-        sa = np.zeros(self.n_sites, dtype=np.int32)
-        sc = np.zeros(self.n_sites, dtype=np.int32)
-        self.ctx.check(lib.pmgb_system_sites(h, ptr(sa, C.c_int32), ptr(sc, C.c_int32)))
-        self.site_atom, self.site_charge = sa, sc
-        self.refine_tail = 0.0
+        self._unit_cell_done(h.value, rep_)
         if refine_tail:
             self.set_refine(refine_tail)
         return self
+
+    @classmethod
+    def many_from_unit_cells(cls, crystals: list[Crystal], molecules: list[Molecule], ljff: LJForceField, *,
+                             ewald_precision: float = 1e-6, ctx: Context | None = None,
+                             n_threads: int = 0) -> list["GPUSystem"]:
+        """from_unit_cell for every (crystal, molecule) pair in one native call
+        (pmgb_systems_create_unitcell): the host set-up of the systems runs on n_threads host threads
+        (0: all) and their device set-up back to back, with two synchronisations in all."""
+        ctx = ctx or Context.default()
+        shells = [cls._unit_cell_prep(cr, mol, ljff, ewald_precision, ctx) for cr, mol in zip(crystals, molecules)]
+        n = len(shells)
+        if n == 0:
+            return []
+
+        def ptrs(attr, ctype):
+            return (C.POINTER(ctype) * n)(*[ptr(getattr(g, attr), ctype) for g in shells])
+
+        def counts(fn):
+            return np.ascontiguousarray([fn(g) for g in shells], dtype=np.int32)
+
+        n_atoms = counts(lambda g: len(g._atom_sp))
+        n_q = counts(lambda g: g._q.shape[0])
+        n_sp = counts(lambda g: len(g.species))
+        n_ga = counts(lambda g: len(g._gsp))
+        n_gq = counts(lambda g: g._gq.shape[0])
+        rep = np.zeros((n, 3), dtype=np.int32)
+        handles = (C.c_void_p * n)()
+        ctx.check(ctx._lib.pmgb_systems_create_unitcell(
+            ctx.handle, n, ptrs("_f_to_c", C.c_double), ptr(n_atoms, C.c_int32), ptrs("_atom_xf", C.c_double),
+            ptrs("_atom_sp", C.c_int32), ptr(n_q, C.c_int32), ptrs("_q_xf", C.c_double), ptrs("_q", C.c_double),
+            ptr(n_sp, C.c_int32), ptrs("_eps", C.c_double), ptrs("_sig2", C.c_double), float(ljff.r_cutoff),
+            ptr(n_ga, C.c_int32), ptrs("_gax", C.c_double), ptrs("_gsp", C.c_int32), ptr(n_gq, C.c_int32),
+            ptrs("_gqx", C.c_double), ptrs("_gq", C.c_double), float(ewald_precision), int(n_threads),
+            ptr(rep, C.c_int32), handles))
+        for g, h, r in zip(shells, handles, rep):
+            g._unit_cell_done(h, r)
+        return shells
 
     def __getattr__(self, name):
         # the host-side objects of a system built from its unit cell, made on first use

@@ -246,3 +246,44 @@ def test_batch_errors(mixed_systems):
     with pytest.raises(pmgb.PMGBError, match="unit_mflop"):
         screen.configure(0, 0, -1.0)
     assert ctx.device_status() == 0
+
+
+def test_many_systems_in_one_call_match_single_set_up():
+    """pmgb_systems_create_unitcell (host set-up on several threads, device set-up back to back)
+    builds exactly the systems pmgb_system_create_unitcell builds one at a time: the same records,
+    k-vectors kept, S(k) and Widom results to the last bit, whatever the number of threads."""
+    ff = synthetic.forcefield()
+    fws = synthetic.batch_frameworks(10, seed=5)
+    mols = [synthetic.co2() if i % 2 else synthetic.ch4() for i in range(len(fws))]
+    ctx = pmgb.Context.default()
+    one_by_one = [pmgb.GPUSystem.from_unit_cell(cr, m, ff, ctx=ctx) for cr, m in zip(fws, mols)]
+    for threads in (1, 4, 0):
+        many = pmgb.GPUSystem.many_from_unit_cells(fws, mols, ff, ctx=ctx, n_threads=threads)
+        for a, b in zip(one_by_one, many):
+            assert a.repfactors == b.repfactors and a.charged == b.charged
+            assert a.info() == b.info()
+            if a.charged:
+                ep = a.eparams
+                assert ep is not None and b.eparams.n_kvecs == ep.n_kvecs
+                np.testing.assert_array_equal(a.structure_factor(), b.structure_factor())
+            ra, _ = a.widom(400, 5, 17, T)
+            rb, _ = b.widom(400, 5, 17, T)
+            np.testing.assert_array_equal(ra, rb)
+        for g in many:
+            g.close()
+    assert any(g.charged for g in one_by_one) and not all(g.charged for g in one_by_one)
+
+
+def test_many_systems_all_or_nothing():
+    """A framework that cannot be set up fails the whole call, naming the system; none is created
+    and the context stays usable."""
+    ff = synthetic.forcefield()
+    fws = synthetic.batch_frameworks(4, seed=8)
+    bad = fws[2]
+    bad.box.f_to_c[:, 1] = bad.box.f_to_c[:, 0]   # singular box
+    ctx = pmgb.Context.default()
+    with pytest.raises(pmgb.PMGBError, match="system 2"):
+        pmgb.GPUSystem.many_from_unit_cells(fws, [synthetic.co2()] * 4, ff, ctx=ctx, n_threads=2)
+    good = pmgb.GPUSystem.many_from_unit_cells(fws[:2], [synthetic.co2()] * 2, ff, ctx=ctx)
+    assert len(good) == 2 and all(g.info()["n_records"] > 0 for g in good)
+    assert pmgb.GPUSystem.many_from_unit_cells([], [], ff, ctx=ctx) == []
