@@ -120,7 +120,7 @@ struct pmgb_system {
     int last_refined_slot = -1;     // r_offsets entry holding the last double-float pass's count (-1: none)
     // grow-only scratch used by launches
     DevBuf r_hist, r_cut, r_counts, r_offsets, r_list, r_ref, r_plan, r_done, r_part;  // refinement scratch
-    DevBuf partials, block_out, in_buf, out_buf, axes;
+    DevBuf partials, block_out, in_buf, out_buf, axes, axes64;
     DevBuf g_u, g_dsum, g_grad, g_part, g_cols;  // adjoint scratch
     DevBuf x64, e_bound;            // exact energies: FP64 site coordinates, grid error estimates
     DevBuf stats;                   // work counts of the diagnostic passes
@@ -497,7 +497,7 @@ extern "C" int pmgb_device_status(pmgb_ctx* ctx, uint32_t* status_out) {
 static void free_system_device(pmgb_system* s) {
     void* ptrs[] = {s->d_rec,      s->d_rec_q,     s->d_segpar64, s->d_seg,   s->d_segpar,  s->d_qxf,    s->d_rec_xf, s->d_q,     s->d_krow,
                     s->d_skw,      s->d_sk,        s->d_kabc,    s->d_wt,     s->partials.p, s->block_out.p,
-                    s->in_buf.p,   s->out_buf.p,   s->axes.p,    s->g_u.p,    s->g_dsum.p, s->g_grad.p,
+                    s->in_buf.p,   s->out_buf.p,   s->axes.p,    s->axes64.p,    s->g_u.p,    s->g_dsum.p, s->g_grad.p,
                     s->g_part.p,   s->g_cols.p,   s->r_hist.p,  s->r_cut.p,  s->r_counts.p, s->r_offsets.p,
                     s->r_list.p,   s->r_ref.p,    s->o_counts.p, s->o_perm.p,  s->r_plan.p,  s->r_done.p,
                     s->r_part.p,   s->acc.p,      s->d_cbox,    s->d_rec_rq,
@@ -1245,6 +1245,68 @@ static int ewald_launch_sk(pmgb_ctx* ctx, pmgb_system* s, const EwaldHost& eh, d
     return PMGB_OK;
 }
 
+// S(k) of a supercell of rep[0] x rep[1] x rep[2] exact copies of a unit cell, from the unit cell:
+// S(k) vanishes unless rep_d | k_d for every d, and then equals n_img S_cell(k / rep) (the copies'
+// phases are all 1), so only those k-vectors are evaluated, over the unit cell's charges (unit_q_xf:
+// its fractional coordinates), n_img^2 times less work than the supercell sum.  Drops the system's
+// previous Ewald state and enqueues the evaluation and its copy into sk_host (2 per index of
+// unit_idx, the traversal positions of the multiples, which this fills).  The device arrays of the
+// k-vectors are made afterwards by ewald_upload_finish.
+static int ewald_launch_sk_unit(pmgb_ctx* ctx, pmgb_system* s, const EwaldHost& eh, const int32_t rep[3], int n_uq,
+                                const double* unit_q_xf, const double* unit_q, std::vector<int>& unit_idx,
+                                double* sk_host) {
+    void* old[] = {s->d_krow, s->d_skw, s->d_sk, s->d_kabc, s->d_wt, s->d_tk_df};
+    for (void* p : old) dev_free(ctx, p);
+    s->d_krow = nullptr;
+    s->d_skw = nullptr;
+    s->d_sk = nullptr;
+    s->d_kabc = nullptr;
+    s->d_wt = nullptr;
+    s->d_tk_df = nullptr;
+    s->ewald_set = false;
+    std::vector<int> kr;
+    std::vector<double> wr;
+    int kmax[3] = {0, 0, 0};
+    unit_idx.clear();
+    for (int i = 0; i < eh.n_kvecs; ++i) {
+        const int* k = &eh.kabc[3 * i];
+        if (k[0] % rep[0] || k[1] % rep[1] || k[2] % rep[2]) continue;
+        unit_idx.push_back(i);
+        for (int d = 0; d < 3; ++d) {
+            kr.push_back(k[d] / rep[d]);
+            kmax[d] = std::max(kmax[d], std::abs(k[d] / rep[d]));
+        }
+        wr.push_back(eh.wt[i]);
+    }
+    const int n_r = static_cast<int>(unit_idx.size());
+    if (n_r == 0) return PMGB_OK;
+    std::vector<double> qxf(3 * static_cast<size_t>(n_uq)), q(unit_q, unit_q + n_uq);
+    for (size_t i = 0; i < qxf.size(); ++i) qxf[i] = wrap01(unit_q_xf[i]);
+    int *d_k = nullptr;
+    double *d_w = nullptr, *d_qxf = nullptr, *d_q = nullptr, *d_sk = nullptr;
+    float2* d_skw = nullptr;
+    double2* d_table = nullptr;
+    const size_t table_len = pmgb_structure_factor_table_len(n_uq, kmax);
+    int rc = upload(ctx, &d_k, kr);
+    if (rc == PMGB_OK) rc = upload(ctx, &d_w, wr);
+    if (rc == PMGB_OK) rc = upload(ctx, &d_qxf, qxf);
+    if (rc == PMGB_OK) rc = upload(ctx, &d_q, q);
+    cudaError_t e = cudaSuccess;
+    if (rc == PMGB_OK) e = dev_malloc(ctx, reinterpret_cast<void**>(&d_sk), 2 * sizeof(double) * n_r);
+    if (rc == PMGB_OK && e == cudaSuccess) e = dev_malloc(ctx, reinterpret_cast<void**>(&d_skw), sizeof(float2) * n_r);
+    if (rc == PMGB_OK && e == cudaSuccess)
+        e = dev_malloc(ctx, reinterpret_cast<void**>(&d_table), std::max<size_t>(sizeof(double2) * table_len, 16));
+    if (rc == PMGB_OK && e == cudaSuccess)
+        e = pmgb_launch_structure_factor(d_qxf, d_q, n_uq, d_k, d_w, n_r, kmax, d_table, d_sk, d_skw, ctx->stream);
+    if (rc == PMGB_OK && e == cudaSuccess)
+        e = cudaMemcpyAsync(sk_host, d_sk, 2 * sizeof(double) * n_r, cudaMemcpyDeviceToHost, ctx->stream);
+    void* tmp[] = {d_k, d_w, d_qxf, d_q, d_sk, d_skw, d_table};
+    for (void* p : tmp) dev_free(ctx, p);
+    if (rc != PMGB_OK) return rc;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "structure factor");
+    return PMGB_OK;
+}
+
 // With S(k) known (sk: traversal order): the caller-order copy, and for replicated frameworks
 // the k-vectors that can contribute.  S(k) of n_a x n_b x n_c copies of a cell vanishes unless
 // n_d | k_d for every d (the sum over copies of e^{2 pi i k_d j / n_d} is zero otherwise), so
@@ -1301,8 +1363,11 @@ static void ewald_finish_host(const pmgb_system* s, const EwaldHost& eh, const d
         }
     } else {
         ef.rows = eh.rows;
+        ef.kabc = kabc;
         ef.wt = wt;
         ef.sk.assign(sk, sk + 2 * static_cast<size_t>(n_kvecs));
+        for (int i = 0; i < n_kvecs; ++i)
+            ef.skw.push_back(make_float2(static_cast<float>(wt[i] * sk[2 * i]), static_cast<float>(wt[i] * sk[2 * i + 1])));
     }
     const size_t n_eval = ef.wt.size();
     ef.tk.resize(n_eval);
@@ -1316,7 +1381,7 @@ static void ewald_finish_host(const pmgb_system* s, const EwaldHost& eh, const d
 // shared erfc table; then every Ewald field of s->dev (asynchronous; no synchronisation).
 static int ewald_upload_finish(pmgb_ctx* ctx, pmgb_system* s, EwaldHost& eh, EwaldFinal& ef) {
     int rc;
-    if (ef.pruned) {
+    if (ef.pruned || !s->d_sk) {  // (no device S(k) yet: it was evaluated from the unit cell)
         void* full[] = {s->d_skw, s->d_sk, s->d_kabc, s->d_wt};
         for (void* p : full) dev_free(ctx, p);
         s->d_skw = nullptr;
@@ -1424,6 +1489,7 @@ extern "C" int pmgb_systems_create_unitcell(pmgb_ctx* ctx, int32_t n_systems, co
         EwaldFinal ef;
         size_t sk_off = 0;
         int32_t rep[3] = {1, 1, 1};
+        std::vector<int> unit_idx;  // S(k) from the unit cell: the k-vectors evaluated (traversal positions)
         Err er;
     };
     std::vector<Item> items(static_cast<size_t>(n_systems));
@@ -1514,9 +1580,17 @@ extern "C" int pmgb_systems_create_unitcell(pmgb_ctx* ctx, int32_t n_systems, co
         }
         return rc == PMGB_OK ? rc : give_up(rc);
     };
-    for (Item& it : items) {
+    for (int i = 0; i < n_systems; ++i) {
+        Item& it = items[i];
         int rc = system_upload(ctx, it.s, it.h);
-        if (rc == PMGB_OK && it.charged) rc = ewald_launch_sk(ctx, it.s, it.eh, sk + it.sk_off);
+        if (rc == PMGB_OK && it.charged) {
+            // the supercell is an exact replica: its S(k) from the unit cell's charges
+            if (it.rep[0] * it.rep[1] * it.rep[2] > 1)
+                rc = ewald_launch_sk_unit(ctx, it.s, it.eh, it.rep, n_charges[i], charge_xf[i], charge_q[i],
+                                          it.unit_idx, sk + it.sk_off);
+            else
+                rc = ewald_launch_sk(ctx, it.s, it.eh, sk + it.sk_off);
+        }
         if (rc != PMGB_OK) return finish(rc);
         it.h = SysHost{};  // staged: the host arrays are no longer needed
     }
@@ -1527,7 +1601,18 @@ extern "C" int pmgb_systems_create_unitcell(pmgb_ctx* ctx, int32_t n_systems, co
         Item& it = items[i];
         if (!it.charged) return;
         try {
-            ewald_finish_host(it.s, it.eh, sk + it.sk_off, it.ef);
+            const double* skv = sk + it.sk_off;
+            std::vector<double> full;
+            const int n_img = it.rep[0] * it.rep[1] * it.rep[2];
+            if (n_img > 1) {  // S(k) of every k-vector: n_img S_cell(k / rep) on the multiples, 0 elsewhere
+                full.assign(2 * static_cast<size_t>(it.eh.n_kvecs), 0.0);
+                for (size_t m = 0; m < it.unit_idx.size(); ++m) {
+                    full[2 * it.unit_idx[m]] = n_img * skv[2 * m];
+                    full[2 * it.unit_idx[m] + 1] = n_img * skv[2 * m + 1];
+                }
+                skv = full.data();
+            }
+            ewald_finish_host(it.s, it.eh, skv, it.ef);
         } catch (const std::bad_alloc&) {
             it.er.set(PMGB_ERR_OUT_OF_MEMORY, "host memory exhausted");
         }
@@ -1915,6 +2000,7 @@ static int run_refine(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uin
             r.grid_n[d] = at_point->grid_n[d];
             r.grid_rep[d] = at_point->grid_rep[d];
         }
+        r.grid_ax64 = at_point->grid_ax64;
         r.point_base = at_point->point_base;
         r.item_base = at_point->item_base;
     }
@@ -2378,6 +2464,7 @@ extern "C" int pmgb_sample_poses(pmgb_ctx* ctx, uint64_t seed, int64_t start, in
 static int grid_axes(pmgb_system* s, const int32_t n_pts[3], const int32_t rep[3]) {
     pmgb_ctx* ctx = s->ctx;
     std::vector<uint32_t> ax;
+    std::vector<double> ax64;  // the FP64 fractions, for the double-float re-evaluation
     for (int d = 0; d < 3; ++d)
         for (int i = 0; i < n_pts[d]; ++i) {
             double f = (n_pts[d] > 1) ? static_cast<double>(i) / static_cast<double>(n_pts[d] - 1) : 0.0;
@@ -2385,12 +2472,14 @@ static int grid_axes(pmgb_system* s, const int32_t n_pts[3], const int32_t rep[3
             // identical position so both planes hold bit-identical energies
             if (f >= 1.0) f -= 1.0;
             ax.push_back(to_fix(f / rep[d]));
+            ax64.push_back(f / rep[d]);
         }
-    if (int rc = ensure(ctx, s->axes, sizeof(uint32_t) * ax.size())) return rc;
-    PMGB_CK(ctx, cudaMemcpyAsync(s->axes.p, ax.data(), sizeof(uint32_t) * ax.size(), cudaMemcpyHostToDevice,
-                                 ctx->stream));
-    // the staging vector is released on return: make the copy complete first
-    PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    int rc;
+    if ((rc = ensure(ctx, s->axes, sizeof(uint32_t) * ax.size())) || (rc = ensure(ctx, s->axes64, sizeof(double) * ax64.size())))
+        return rc;
+    if ((rc = staged_h2d(ctx, s->axes.p, ax.data(), sizeof(uint32_t) * ax.size())) ||
+        (rc = staged_h2d(ctx, s->axes64.p, ax64.data(), sizeof(double) * ax64.size())))
+        return rc;
     return PMGB_OK;
 }
 
@@ -2431,6 +2520,7 @@ static int exact_grid(pmgb_system* s, const int32_t n_pts[3], const int32_t repf
         r.grid_n[d] = n_pts[d];
         r.grid_rep[d] = repfactors[d];
     }
+    r.grid_ax64 = static_cast<const double*>(s->axes64.p);
     r.ref_u = static_cast<double*>(s->r_ref.p);
     PMGB_CK(ctx, pmgb_launch_grid_exact(r, a.bound_out, out_dev, total, unit_factor, sm_count(ctx), ctx->stream));
     return PMGB_OK;
@@ -2623,6 +2713,7 @@ extern "C" int pmgb_energy_grid_rotational(pmgb_system* s, const int32_t n_pts[3
                 where.grid_n[d] = n_pts[d];
                 where.grid_rep[d] = repfactors[d];
             }
+            where.grid_ax64 = static_cast<const double*>(s->axes64.p);
             where.point_base = p0;
             where.item_base = a.item_base;
             if ((rc = run_refine(s, n_rotations, nb, seed, temperature, bo, a.u_out, tail, &where))) return rc;

@@ -942,7 +942,7 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
     // BOUND: smallest |r^2 - rc^2| seen, an overlap distance within rounding, sum of squared terms
     float cgap = __int_as_float(0x7f800000);
     bool thr_near = false;
-    double bsq = 0.0, bsum = 0.0;
+    float bsq = 0.0f, bsum = 0.0f;  // FP32: an estimate (an overflow to +Inf only asks for re-evaluation)
     int cb = 0;  // running sub-chunk index: the order of S.cbox
     const bool box_cull = io.cull && S.cbox != nullptr;
 
@@ -1233,11 +1233,10 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                 // rep = lj12 r^-12 and att = |lj6| r^-6 per pair inside the cutoff: sum rep^2 + att^2
 #pragma unroll
                 for (int k = 0; k < NS; ++k) {
-                    const double a12 = lj12[k], a6 = lj6[k];
-                    const double s12 = static_cast<double>(i12[k].x) + static_cast<double>(i12[k].y);
-                    const double s6 = static_cast<double>(i6[k].x) + static_cast<double>(i6[k].y);
-                    bsq += a12 * a12 * (static_cast<double>(i24[k].x) + static_cast<double>(i24[k].y)) + a6 * a6 * s12;
-                    bsum += a12 * s12 - a6 * s6;  // lj6 < 0: the attraction's magnitude
+                    const float a12 = lj12[k], a6 = lj6[k];
+                    const float s12 = i12[k].x + i12[k].y, s6 = i6[k].x + i6[k].y;
+                    bsq = fmaf(a12 * a12, i24[k].x + i24[k].y, fmaf(a6 * a6, s12, bsq));
+                    bsum = fmaf(a12, s12, fmaf(-a6, s6, bsum));  // lj6 < 0: the attraction's magnitude
                     thr_near = thr_near || fabsf(segmin[k] - r2o[k]) <= 4e-6f * r2o[k];
                 }
             }
@@ -1344,8 +1343,8 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
             if (GRAD && io.u_out) io.u_out[item] = uv;
             if (BOUND) {
                 const bool edge = thr_near || cgap <= 4e-6f * g.rc2;
-                const double e = fmin(io.bound_rho * bsum, io.bound_stat * sqrt(bsq)) + 2e-8 * bsum;
-                io.bound_out[item] = edge ? __int_as_float(0x7f800000) : static_cast<float>(e);
+                const float e = fmaf(2e-8f, bsum, fminf(io.bound_rho * bsum, io.bound_stat * sqrtf(bsq)));
+                io.bound_out[item] = (edge || !(e < __int_as_float(0x7f800000))) ? __int_as_float(0x7f800000) : e;
             }
         }
         return true;

@@ -298,6 +298,7 @@ struct RefineArgs {
     int pose_src;
     const double* site_xf;          // REFINE_POSE_SITES: [n x n_sites x 3] supercell fractions
     int grid_n[3], grid_rep[3];     // REFINE_POSE_GRID / _ROTGRID: points per axis, replication factors
+    const double* grid_ax64;        // ... and the FP64 supercell fractions of the points along x, y, z (concatenated)
     long long point_base, item_base;  // REFINE_POSE_ROTGRID: block b at point point_base + b; rotation
                                       //   of insertion i from Philox counter item_base + i
 };

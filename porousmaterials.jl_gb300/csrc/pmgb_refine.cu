@@ -395,8 +395,16 @@ struct SiteScreen {
 //  - an energy-grid point (single site): (i/(n-1)) / rep per axis, the end plane folded onto
 //    the first (its periodic image, as the FP32 grid pass evaluates it).
 __device__ __forceinline__ double grid_coord(const RefineArgs& a, unsigned long long point, int d) {
-    const unsigned long long n1 = a.grid_n[0], n2 = a.grid_n[1];
-    const unsigned long long i = d == 0 ? point % n1 : d == 1 ? (point / n1) % n2 : point / (n1 * n2);
+    unsigned long long i;
+    if (point < (1ull << 32)) {  // 32-bit division where it suffices
+        const unsigned p = static_cast<unsigned>(point), n1 = a.grid_n[0], n2 = a.grid_n[1];
+        i = d == 0 ? p % n1 : d == 1 ? (p / n1) % n2 : p / (n1 * n2);
+    } else {
+        const unsigned long long n1 = a.grid_n[0], n2 = a.grid_n[1];
+        i = d == 0 ? point % n1 : d == 1 ? (point / n1) % n2 : point / (n1 * n2);
+    }
+    // the host's table holds these very FP64 values, (i / (n - 1), minus 1 on the end plane) / rep
+    if (a.grid_ax64) return a.grid_ax64[(d > 0 ? a.grid_n[0] : 0) + (d > 1 ? a.grid_n[1] : 0) + i];
     const int n = a.grid_n[d];
     double f = n > 1 ? static_cast<double>(i) / static_cast<double>(n - 1) : 0.0;
     if (f >= 1.0) f -= 1.0;

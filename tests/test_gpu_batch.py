@@ -266,6 +266,16 @@ def test_many_systems_in_one_call_match_single_set_up():
                 ep = a.eparams
                 assert ep is not None and b.eparams.n_kvecs == ep.n_kvecs
                 np.testing.assert_array_equal(a.structure_factor(), b.structure_factor())
+                if threads == 1:
+                    # a replica's S(k) is evaluated from its unit cell; the supercell sum agrees
+                    sup = pmgb.GPUSystem(a.crystal, a.molecule, ff, ep, ctx=ctx)
+                    sk_a, sk_s = a.structure_factor(), sup.structure_factor()
+                    scale = np.abs(sk_s).max()
+                    np.testing.assert_allclose(sk_a, sk_s, rtol=0, atol=1e-12 * scale)
+                    assert sup.info()["n_kvecs_evaluated"] == a.info()["n_kvecs_evaluated"]
+                    np.testing.assert_allclose(a.widom(400, 5, 17, T)[0], sup.widom(400, 5, 17, T)[0],
+                                               rtol=1e-7, atol=1e-9)
+                    sup.close()
             ra, _ = a.widom(400, 5, 17, T)
             rb, _ = b.widom(400, 5, 17, T)
             np.testing.assert_array_equal(ra, rb)
