@@ -381,6 +381,8 @@ extern "C" int pmgb_create(int device, pmgb_ctx** out) {
         uint64_t keep = UINT64_MAX;  // never trim: freed blocks stay cached until the context goes
         if (e == cudaSuccess) e = cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
+    if (e == cudaSuccess) e = pmgb_launch_phase_table(c->own_stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->own_stream);
     if (e != cudaSuccess) {
         if (c->pool) cudaMemPoolDestroy(c->pool);
         if (c->d_status) cudaFree(c->d_status);

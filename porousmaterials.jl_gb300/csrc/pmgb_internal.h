@@ -368,6 +368,10 @@ cudaError_t pmgb_launch_bounded_wait_test(unsigned int* status, unsigned long lo
                                           cudaStream_t st);
 size_t pmgb_pairs_smem_bytes();
 
+// the double-float phase table of the refinement's reciprocal space, built once per device
+// (synchronously at context creation, before any launch or capture reads it)
+cudaError_t pmgb_launch_phase_table(cudaStream_t st);
+
 // record a failure message on ctx and return code (defined in pmgb_api.cu)
 struct pmgb_ctx;
 int pmgb_fail_message(pmgb_ctx* ctx, int code, const char* message);

@@ -311,15 +311,23 @@ __device__ __forceinline__ dfc dfc_mul(dfc a, dfc b) {
     return {df_add(df_mul(a.re, b.re), df_neg(df_mul(a.im, b.im))), df_add(df_mul(a.re, b.im), df_mul(a.im, b.re))};
 }
 
-// e^{-2 pi i j / 256}, j < 256, as double-float (re hi, re lo, im hi, im lo): one per CTA in shared memory
+// e^{-2 pi i j / 256}, j < 256, as double-float (re hi, re lo, im hi, im lo): built once per device
+// (pmgb_launch_phase_table, at context creation) and copied into each CTA's shared memory, so a
+// refinement launch pays no FP64 sincos per CTA.
+__device__ float4 g_phase_tab[256];
+
+__global__ void phase_table_kernel() {
+    const int j = threadIdx.x;
+    if (j >= 256) return;
+    double sn, cs;
+    sincospi(-static_cast<double>(j) / 128.0, &sn, &cs);
+    const float ch = static_cast<float>(cs), sh = static_cast<float>(sn);
+    g_phase_tab[j] = make_float4(ch, static_cast<float>(cs - static_cast<double>(ch)), sh,
+                                 static_cast<float>(sn - static_cast<double>(sh)));
+}
+
 __device__ __forceinline__ void phase_table_init(float4* tab) {
-    for (int j = threadIdx.x; j < 256; j += blockDim.x) {
-        double sn, cs;
-        sincospi(-static_cast<double>(j) / 128.0, &sn, &cs);
-        const float ch = static_cast<float>(cs), sh = static_cast<float>(sn);
-        tab[j] = make_float4(ch, static_cast<float>(cs - static_cast<double>(ch)), sh,
-                             static_cast<float>(sn - static_cast<double>(sh)));
-    }
+    for (int j = threadIdx.x; j < 256; j += blockDim.x) tab[j] = g_phase_tab[j];
 }
 
 // e^{-2 pi i P / 2^64} for a 64-bit fixed-point phase P (exact modulo one turn): the table entry of
@@ -1012,6 +1020,11 @@ __global__ void grid_write_kernel(const __grid_constant__ RefineArgs a, float* g
 }  // namespace
 
 int pmgb_grid_screen_ctas(long long n_points) { return static_cast<int>((n_points + PMGB_THREADS - 1) / PMGB_THREADS); }
+
+cudaError_t pmgb_launch_phase_table(cudaStream_t st) {
+    phase_table_kernel<<<1, 256, 0, st>>>();
+    return cudaGetLastError();
+}
 
 cudaError_t pmgb_launch_exact(const RefineArgs& a, long long n, const int* n_dev, int n_sm, cudaStream_t st) {
     if (!n_dev && n <= 0) return cudaSuccess;
