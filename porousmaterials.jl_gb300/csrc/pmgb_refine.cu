@@ -448,14 +448,20 @@ __device__ __forceinline__ void warp_site_setup(const RefineArgs& a, const SysDe
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int k = min(lane / 3, S.n_sites - 1), d = lane % 3;
-    const double x = site_coord(a, S, seed, item, k, d);
-    const double ux = x * 4294967296.0;
-    const long long fx = __double2ll_rn(ux);
-    const uint32_t fix = static_cast<uint32_t>(fx);  // as frac2fix64
-    const float rem = static_cast<float>(ux - static_cast<double>(fx));
-    const uint64_t U = S.charged ? static_cast<uint64_t>(S.ks[d]) * frac2fix128(x) : 0ull;
-    const float qh = static_cast<float>(S.q64[k]);
-    const float ql = static_cast<float>(S.q64[k] - static_cast<double>(qh));
+    // only the lanes whose values are read below do the FP64 work
+    uint32_t fix = 0;
+    float rem = 0.0f, qh = 0.0f, ql = 0.0f;
+    uint64_t U = 0;
+    if (lane < 3 * S.n_sites) {
+        const double x = site_coord(a, S, seed, item, k, d);
+        const double ux = x * 4294967296.0;
+        const long long fx = __double2ll_rn(ux);
+        fix = static_cast<uint32_t>(fx);  // as frac2fix64
+        rem = static_cast<float>(ux - static_cast<double>(fx));
+        U = S.charged ? static_cast<uint64_t>(S.ks[d]) * frac2fix128(x) : 0ull;
+        qh = static_cast<float>(S.q64[k]);
+        ql = static_cast<float>(S.q64[k] - static_cast<double>(qh));
+    }
     for (int kk = 0; kk < S.n_sites; ++kk) {
         const int l = 3 * kk;
         sc.x[kk] = __shfl_sync(full, fix, l);
@@ -679,9 +685,10 @@ __device__ void energy_fp64_warp_part(const RefineArgs& a, const SysDev& S, unsi
 // Work units of one insertion (pair terms + reciprocal-space terms).  Tiny insertions are
 // evaluated by one thread each; the others are cut into chunks (records and k-space half-rows in
 // proportion), one warp per chunk, so that one large insertion spreads over many SMs instead of
-// waiting on one warp.  The chunk size adapts to the system's number of refined insertions: ~256
-// units while its chunk-items stay within 256 (one or a few configurations, a Monte Carlo move:
-// the pass is pure latency), ~1024 units while they stay within 4096 (a few insertions: finer
+// waiting on one warp.  The chunk size adapts to the system's number of refined insertions: ~128
+// units (at most 256 chunks) for a single one (a Monte Carlo move: the pass is pure latency, and
+// shorter chunks mean shorter chains of dependent loads), ~256 units while its chunk-items stay
+// within 256 (a few configurations), ~1024 units while they stay within 4096 (a few insertions: finer
 // chunks fill more SMs), else ~16384 units (many insertions: fewer repetitions of the per-chunk
 // set-up).  The count is the same for a system alone or in a batch, so the two evaluate identical
 // chunks.
@@ -691,6 +698,7 @@ __device__ __forceinline__ long long fp64_work(const SysDev& S) {
 __device__ __forceinline__ bool small_system(const SysDev& S) { return fp64_work(S) <= 64; }
 __device__ __forceinline__ int fp64_chunks(const SysDev& S, long long count) {
     if (small_system(S)) return 0;
+    if (count == 1) return static_cast<int>(min(256ll, (fp64_work(S) + 127) / 128));
     const long long finest = min(64ll, (fp64_work(S) + 255) / 256);
     if (count * finest <= 256) return static_cast<int>(finest);
     const long long fine = min(64ll, (fp64_work(S) + 1023) / 1024);
