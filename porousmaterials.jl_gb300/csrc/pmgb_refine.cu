@@ -816,7 +816,7 @@ __global__ void __launch_bounds__(1024) refine_plan_kernel(const __grid_constant
 }
 
 // Chunk-items of the large insertions: one warp each, from a work counter.  The warp that
-// completes an insertion's last chunk adds the chunk partials in chunk order (the same sum
+// completes an insertion's last chunk adds the chunk partials in a fixed order (the same sum
 // whatever the scheduling) and stores the insertion's FP64 energies.
 __global__ void __launch_bounds__(PMGB_THREADS) refine_large_kernel(const __grid_constant__ RefineArgs a, int n_ctas) {
     __shared__ int s_queue[PMGB_THREADS / 32][kQueueLen];
@@ -856,22 +856,38 @@ __global__ void __launch_bounds__(PMGB_THREADS) refine_large_kernel(const __grid
             out[0] = p[3] > 0.0 ? __longlong_as_double(0x7ff0000000000000ll) : p[0];
             out[1] = p[1] * S.coul;
             out[2] = p[2];
-        } else if (lane == 0) {
-            __threadfence();  // this chunk's partial before the count
-            if (atomicAdd(&a.done[r], 1) == C - 1) {
+        } else if (C > 1) {
+            int last = 0;
+            if (lane == 0) {
+                __threadfence();  // this chunk's partial before the count
+                last = atomicAdd(&a.done[r], 1) == C - 1;
+            }
+            if (__shfl_sync(0xffffffffu, last, 0)) {
+                // the warp that completes the entry adds the chunk partials: lane l takes chunks
+                // l, l + 32, ... in order, then a fixed butterfly over the lanes -- the same sum
+                // whatever the scheduling, with loads in flight on every lane instead of a chain
                 __threadfence();  // every other chunk's partial is visible
-                const volatile double* q = a.part + 4 * static_cast<size_t>(i - c);
+                const double* q = a.part + 4 * static_cast<size_t>(i - c);
                 double v = 0.0, sr = 0.0, lr = 0.0, ov = 0.0;
-                for (int cc = 0; cc < C; ++cc) {
-                    v += q[4 * cc];
-                    sr += q[4 * cc + 1];
-                    lr += q[4 * cc + 2];
-                    ov += q[4 * cc + 3];
+                for (int cc = lane; cc < C; cc += 32) {
+                    v += __ldcg(q + 4 * cc);
+                    sr += __ldcg(q + 4 * cc + 1);
+                    lr += __ldcg(q + 4 * cc + 2);
+                    ov += __ldcg(q + 4 * cc + 3);
                 }
-                double* out = a.ref_u + 3 * static_cast<size_t>(r);
-                out[0] = ov > 0.0 ? __longlong_as_double(0x7ff0000000000000ll) : v;
-                out[1] = sr * S.coul;
-                out[2] = lr;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    v += __shfl_xor_sync(0xffffffffu, v, o);
+                    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+                    lr += __shfl_xor_sync(0xffffffffu, lr, o);
+                    ov += __shfl_xor_sync(0xffffffffu, ov, o);
+                }
+                if (lane == 0) {
+                    double* out = a.ref_u + 3 * static_cast<size_t>(r);
+                    out[0] = ov > 0.0 ? __longlong_as_double(0x7ff0000000000000ll) : v;
+                    out[1] = sr * S.coul;
+                    out[2] = lr;
+                }
             }
         }
     }
