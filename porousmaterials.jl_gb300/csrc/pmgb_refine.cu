@@ -692,18 +692,27 @@ __device__ void energy_fp64_warp_part(const RefineArgs& a, const SysDev& S, unsi
 // chunks fill more SMs), else ~16384 units (many insertions: fewer repetitions of the per-chunk
 // set-up).  The count is the same for a system alone or in a batch, so the two evaluate identical
 // chunks.
-__device__ __forceinline__ long long fp64_work(const SysDev& S) {
+__host__ __device__ __forceinline__ long long fp64_work(const SysDev& S) {
     return static_cast<long long>(S.n_sites) * (S.n_rec + (S.charged ? S.n_k : 0));
 }
-__device__ __forceinline__ bool small_system(const SysDev& S) { return fp64_work(S) <= 64; }
-__device__ __forceinline__ int fp64_chunks(const SysDev& S, long long count) {
+__host__ __device__ __forceinline__ bool small_system(const SysDev& S) { return fp64_work(S) <= 64; }
+__host__ __device__ __forceinline__ long long min_ll(long long x, long long y) { return x < y ? x : y; }
+__host__ __device__ __forceinline__ int fp64_chunks(const SysDev& S, long long count) {
     if (small_system(S)) return 0;
-    if (count == 1) return static_cast<int>(min(256ll, (fp64_work(S) + 127) / 128));
-    const long long finest = min(64ll, (fp64_work(S) + 255) / 256);
+    if (count == 1) return static_cast<int>(min_ll(256, (fp64_work(S) + 127) / 128));
+    const long long finest = min_ll(64, (fp64_work(S) + 255) / 256);
     if (count * finest <= 256) return static_cast<int>(finest);
-    const long long fine = min(64ll, (fp64_work(S) + 1023) / 1024);
+    const long long fine = min_ll(64, (fp64_work(S) + 1023) / 1024);
     if (count * fine <= 4096) return static_cast<int>(fine);
-    return static_cast<int>(min(64ll, (fp64_work(S) + 16383) / 16384));
+    return static_cast<int>(min_ll(64, (fp64_work(S) + 16383) / 16384));
+}
+
+// The chunk-items of a single-system pass over cnt entries: cnt x fp64_chunks, or one chunk per
+// entry when that exceeds the partials' capacity (refine_plan_kernel's rule for one system).
+__host__ __device__ __forceinline__ long long single_items(const RefineArgs& a, long long cnt, int* one_chunk) {
+    const long long items = cnt * fp64_chunks(a.sys, cnt);
+    *one_chunk = items > a.cap_items ? 1 : 0;
+    return *one_chunk ? cnt : items;
 }
 
 // Pose stream of refined entry e (system << 40 | insertion): its system's seed and insertion index.
@@ -984,12 +993,26 @@ __global__ void tail_reblock_kernel(const __grid_constant__ RefineArgs a) {
 // ---- exact energies of explicit configurations and of energy-grid points --------------------
 // The entry list of the double-float pass when every configuration is evaluated: list[i] = i and
 // the entry count in offsets[0] (the refinement kernels then run with zero screen chunks).
-__global__ void exact_list_kernel(const __grid_constant__ RefineArgs a, long long n, const int* n_dev) {
+// The entry list of an exact pass (every entry, in order) and its count; with `plan` also the
+// chunk-item plan of the warp pass and the zeroed chunk counts (what refine_plan_kernel and a
+// memset would do, folded into this launch for the single-system pass).
+__global__ void exact_list_kernel(const __grid_constant__ RefineArgs a, long long n, const int* n_dev, int plan) {
     const long long cnt = n_dev ? static_cast<long long>(*n_dev) : n;
     for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < cnt;
-         i += static_cast<long long>(gridDim.x) * blockDim.x)
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
         a.list[i] = i;
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.offsets[0] = static_cast<int>(cnt);
+        if (plan) a.done[i] = 0;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.offsets[0] = static_cast<int>(cnt);
+        if (plan) {
+            int one = 0;
+            const long long items = single_items(a, cnt, &one);
+            a.plan[0] = 0;
+            a.plan[1] = static_cast<int>(min_ll(items, 0x7fffffffll));
+            a.one_chunk[0] = one;
+        }
+    }
 }
 
 // A grid point goes to the double-float pass when its FP32 error estimate could exceed its
@@ -1054,18 +1077,22 @@ cudaError_t pmgb_launch_exact(const RefineArgs& a, long long n, const int* n_dev
     if (!n_dev && n <= 0) return cudaSuccess;
     const long long cap = n_dev ? a.cap_entries : n;
     const int blocks = static_cast<int>(std::max(1ll, std::min((cap + 255) / 256, 4ll * n_sm)));
-    exact_list_kernel<<<blocks, 256, 0, st>>>(a, n, n_dev);
     // one system: only the thread pass (tiny systems) or only the warp pass runs
-    const long long work = static_cast<long long>(a.sys.n_sites) * (a.sys.n_rec + (a.sys.charged ? a.sys.n_k : 0));
-    if (work <= 64) {
+    const bool small = small_system(a.sys);
+    exact_list_kernel<<<blocks, 256, 0, st>>>(a, n, n_dev, small ? 0 : 1);
+    if (small) {
         const int tb = static_cast<int>(std::max(1ll, std::min((cap + PMGB_THREADS - 1) / PMGB_THREADS, 4ll * n_sm)));
         refine_small_kernel<<<tb, PMGB_THREADS, 0, st>>>(a, 0);
         return cudaGetLastError();
     }
-    cudaError_t e = cudaMemsetAsync(a.done, 0, sizeof(int) * static_cast<size_t>(cap), st);
-    if (e != cudaSuccess) return e;
-    refine_plan_kernel<<<1, 1024, 0, st>>>(a, 0);
-    refine_large_kernel<<<4 * n_sm, PMGB_THREADS, 0, st>>>(a, 0);
+    // warps for the chunk-items (8 per CTA), when the count is known here; the work counter
+    // spreads them whatever the number of CTAs
+    long long ctas = 4ll * n_sm;
+    if (!n_dev) {
+        int one = 0;
+        ctas = std::max(1ll, std::min(ctas, (single_items(a, n, &one) + 7) / 8));
+    }
+    refine_large_kernel<<<static_cast<int>(ctas), PMGB_THREADS, 0, st>>>(a, 0);
     return cudaGetLastError();
 }
 
