@@ -838,7 +838,7 @@ __global__ void __launch_bounds__(PMGB_THREADS) refine_large_kernel(const __grid
         int i = 0;
         if (lane == 0) i = atomicAdd(a.counter, 1);
         i = __shfl_sync(0xffffffffu, i, 0);
-        if (i >= total) break;
+        if (i >= total || i < 0) break;
         // the system of item i: the last s with plan[s] <= i
         int lo = 0, hi = a.n_systems - 1;
         while (lo < hi) {
@@ -994,8 +994,8 @@ __global__ void tail_reblock_kernel(const __grid_constant__ RefineArgs a) {
 // The entry list of the double-float pass when every configuration is evaluated: list[i] = i and
 // the entry count in offsets[0] (the refinement kernels then run with zero screen chunks).
 // The entry list of an exact pass (every entry, in order) and its count; with `plan` also the
-// chunk-item plan of the warp pass and the zeroed chunk counts (what refine_plan_kernel and a
-// memset would do, folded into this launch for the single-system pass).
+// chunk-item plan of the warp pass, its zeroed work counter and the zeroed chunk counts (what
+// refine_plan_kernel and a memset would do, folded into this launch for the single-system pass).
 __global__ void exact_list_kernel(const __grid_constant__ RefineArgs a, long long n, const int* n_dev, int plan) {
     const long long cnt = n_dev ? static_cast<long long>(*n_dev) : n;
     for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < cnt;
@@ -1008,6 +1008,7 @@ __global__ void exact_list_kernel(const __grid_constant__ RefineArgs a, long lon
         if (plan) {
             int one = 0;
             const long long items = single_items(a, cnt, &one);
+            a.counter[0] = 0;  // the warp pass's work counter starts from the first chunk-item
             a.plan[0] = 0;
             a.plan[1] = static_cast<int>(min_ll(items, 0x7fffffffll));
             a.one_chunk[0] = one;
