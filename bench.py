@@ -340,7 +340,7 @@ def reference_arm(args, rank, world):
 
 
 # ------------------------------------------------------------------ batched screening leg
-def batched_leg(args, ctx, stream):
+def batched_leg(args, ctx, stream, peak=None):
     """Batched vs plain forward + adjoint Widom over uneven synthetic frameworks.
 
     Frameworks: atoms log-uniform 50-5000, cell lengths U(8, 40) Å, angles U(80, 110)°,
@@ -355,7 +355,7 @@ def batched_leg(args, ctx, stream):
     import torch
 
     from pmgb import synthetic
-    from pmgb.batch import BatchScreen, build_systems
+    from pmgb.batch import BatchScreen, build_systems, system_seed
 
     t0 = time.perf_counter()
     fws = synthetic.batch_frameworks(args.batch_frameworks)
@@ -442,6 +442,36 @@ def batched_leg(args, ctx, stream):
                     "order": ["cost-descending", "by-system"][info["order"]], "ms": tuned_ms},
                     "work_units": info["n_units"], "gpu_launches_per_run": 17}
         # spatial order (3), batch kernel, insertion-order partials, per-system reduction, 11 refinement kernels
+    # counted-work roofline of the batch kernel: its FP32 pass (refinement off) over insertions of
+    # the same kind, against the work the counting pass reports for each system
+    screen = BatchScreen(systems, npb, N_BLOCKS, with_adjoint=False, ctx=ctx, refine_tail=0.0)
+    screen.tune(1, T, repeats=2)
+    for w in range(args.warmup):
+        screen.run(2 + w, T)
+    k = max(3, args.steps // 2)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+    torch.cuda.synchronize()
+    for i in range(k):
+        ev[i][0].record(stream)
+        screen.launch(100 + i, T)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ms_fp32 = sum(a.elapsed_time(b) for a, b in ev) / k
+    screen.close()
+    flops = 0.0
+    for s_, gs in enumerate(systems):
+        c = gs.widom_work_counts(npb, N_BLOCKS, system_seed(100, s_))
+        nq = int((gs.site_charge >= 0).sum()) if gs.charged else 0
+        nk = gs.info()["n_kvecs_evaluated"] if gs.charged else 0
+        flops += counted_flops(c, npb * N_BLOCKS, nq, nk) * npb * N_BLOCKS
+    tf = flops / (ms_fp32 * 1e-3) / 1e12
+    out["roofline"] = {"bound": "fp32", "achieved": tf, "unit": "TFLOP/s", "frac": tf / peak if peak else None,
+                       "flops_per_run": flops, "fp32_pass_ms": ms_fp32,
+                       "kernel": "the batch's forward FP32 pass (refinement off: the spatial order, the persistent "
+                                 "batch kernel, partials and per-system reduction), CUDA events around the graph "
+                                 "replay",
+                       "counting": "pmgb_widom_work_counts of each system over its insertions of one run (26 / 11 / "
+                                   "30 / 17 flops per distance, LJ term, real-space term, k-term)"}
     assert ctx.device_status() == 0
     out["refined_fraction"] = out["forward_plus_adjoint"]["refined_fraction"]
     out.update({"systems": len(systems), "frameworks": len(fws), "guests": ["CH4", "CO2"],
@@ -896,7 +926,7 @@ def ours(args, rank, world, local_rank):
 
     batched = None
     if "batched" in args.legs and rank == 0:
-        batched = batched_leg(args, ctx, stream)
+        batched = batched_leg(args, ctx, stream, fp32_peak)
     others = None
     if args.legs & {"config4", "moves", "config2"} and rank == 0:
         others = other_configs(args, ctx, stream, fp32_peak)
@@ -931,7 +961,8 @@ def ours(args, rank, world, local_rank):
         summary.update({"batched_fwd_adj_insertions_per_s": fa["batched_insertions_per_s"],
                         "batched_vs_plain_prebuilt": fa["speedup_vs_plain"],
                         "batched_vs_plain_with_setup": fa.get("speedup_with_setup_both_sides"),
-                        "batched_refined_fraction": batched.get("refined_fraction")})
+                        "batched_refined_fraction": batched.get("refined_fraction"),
+                        "batched_fp32_pass_frac_of_fp32_peak": batched["roofline"]["frac"]})
     if others and "config4_large_ewald" in others:
         summary["config4_insertions_per_s"] = others["config4_large_ewald"]["insertions_per_s"]
     if others and "config2_energy_grid" in others:
