@@ -412,6 +412,24 @@ int pmgb_batch_info(const pmgb_batch* batch, int64_t* out8);
 int pmgb_philox4x32_10(pmgb_ctx* ctx, int64_t n, const uint32_t* ctr, const uint32_t* key,
                        uint32_t* out);
 
+/* Guest-host van der Waals energies in FP64 in the reference's own operation order:
+ * vdw_energy(atoms_i, atoms_j, box, ljff) (src/vdw_energetics.jl:25-47), with Xtals'
+ * nearest_image! (d -= sign(d) where |d| > 1/2) and the f_to_c product summed left to right,
+ * every operation rounded separately (no fused multiply-adds), the atoms summed in the order
+ * given.  Configurations whose energies are equal in exact arithmetic (inversion images on a
+ * grid) then compare as the reference's FP64 arithmetic compares them; find_energy_minimum_gridsearch
+ * (src/energy_min.jl:75-85) takes its argmin over these values.  One thread per configuration,
+ * serial in the atoms: meant for a few configurations.
+ *   f_to_c:   the (replicated) box, column-major as everywhere in this header
+ *   atom_xf:  n_atoms x 3 fractional coordinates, in the crystal's atom order
+ *   eps, sigma2: n_species x n_species, row = guest site species, column = atom species
+ *   site_xf:  n_conf x n_sites x 3 fractional guest site coordinates
+ *   out:      n_conf energies in K (+Inf where a pair is closer than r^2 = 0.1 A^2) */
+int pmgb_vdw_energy_ordered(pmgb_ctx* ctx, const double f_to_c[9], int32_t n_atoms, const double* atom_xf,
+                            const int32_t* atom_species, int32_t n_species, const double* eps,
+                            const double* sigma2, double r2_cutoff, int64_t n_conf, int32_t n_sites,
+                            const int32_t* site_species, const double* site_xf, double* out);
+
 /* FP32 FMA throughput probe: runs n_ctas x 256 threads x iters x 128 FMAs and returns the
  * measured TFLOP/s (the roofline denominator of the pair kernels). */
 int pmgb_fp32_peak(pmgb_ctx* ctx, int n_ctas, int iters, double* tflops_out);

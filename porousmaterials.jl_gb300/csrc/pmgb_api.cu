@@ -2764,6 +2764,57 @@ extern "C" int pmgb_philox4x32_10(pmgb_ctx* ctx, int64_t n, const uint32_t* ctr,
     return PMGB_OK;
 }
 
+extern "C" int pmgb_vdw_energy_ordered(pmgb_ctx* ctx, const double f_to_c[9], int32_t n_atoms, const double* atom_xf,
+                                       const int32_t* atom_species, int32_t n_species, const double* eps,
+                                       const double* sigma2, double r2_cutoff, int64_t n_conf, int32_t n_sites,
+                                       const int32_t* site_species, const double* site_xf, double* out) {
+    if (!ctx) return PMGB_ERR_INVALID_ARGUMENT;
+    if (!f_to_c || n_atoms < 0 || (n_atoms > 0 && (!atom_xf || !atom_species)) || n_species < 1 || !eps ||
+        !sigma2 || n_conf < 0 || n_sites < 1 || !site_species || (n_conf > 0 && (!site_xf || !out)) ||
+        n_conf > (int64_t{1} << 40) / n_sites)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_vdw_energy_ordered: bad arguments");
+    for (int32_t j = 0; j < n_atoms; ++j)
+        if (atom_species[j] < 0 || atom_species[j] >= n_species)
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_vdw_energy_ordered: atom species out of range");
+    for (int32_t i = 0; i < n_sites; ++i)
+        if (site_species[i] < 0 || site_species[i] >= n_species)
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_vdw_energy_ordered: site species out of range");
+    if (n_conf == 0) return PMGB_OK;
+    PMGB_CK(ctx, enter_device(ctx->device));
+    const size_t nt = static_cast<size_t>(n_species) * n_species;
+    const size_t b_f = 9 * sizeof(double), b_ax = 3 * sizeof(double) * n_atoms, b_as = sizeof(int) * n_atoms,
+                 b_t = sizeof(double) * nt, b_ss = sizeof(int) * n_sites,
+                 b_sx = 3 * sizeof(double) * static_cast<size_t>(n_conf) * n_sites, b_o = sizeof(double) * n_conf;
+    // one allocation, each part on a 256-byte boundary
+    auto up = [](size_t b) { return (b + 255) & ~size_t{255}; };
+    const size_t o_ax = up(b_f), o_as = o_ax + up(b_ax), o_e = o_as + up(b_as), o_s = o_e + up(b_t),
+                 o_ss = o_s + up(b_t), o_sx = o_ss + up(b_ss), o_o = o_sx + up(b_sx), total = o_o + up(b_o);
+    char* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, total);
+    auto h2d = [&](size_t off, const void* src, size_t b) {
+        if (e == cudaSuccess && b) e = cudaMemcpyAsync(d + off, src, b, cudaMemcpyHostToDevice, ctx->stream);
+    };
+    h2d(0, f_to_c, b_f);
+    h2d(o_ax, atom_xf, b_ax);
+    h2d(o_as, atom_species, b_as);
+    h2d(o_e, eps, b_t);
+    h2d(o_s, sigma2, b_t);
+    h2d(o_ss, site_species, b_ss);
+    h2d(o_sx, site_xf, b_sx);
+    if (e == cudaSuccess)
+        e = pmgb_launch_vdw_ordered(reinterpret_cast<const double*>(d), n_atoms,
+                                    reinterpret_cast<const double*>(d + o_ax), reinterpret_cast<const int*>(d + o_as),
+                                    n_species, reinterpret_cast<const double*>(d + o_e),
+                                    reinterpret_cast<const double*>(d + o_s), r2_cutoff, n_conf, n_sites,
+                                    reinterpret_cast<const int*>(d + o_ss), reinterpret_cast<const double*>(d + o_sx),
+                                    reinterpret_cast<double*>(d + o_o), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d + o_o, b_o, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "pmgb_vdw_energy_ordered");
+    return PMGB_OK;
+}
+
 extern "C" int pmgb_fp32_peak(pmgb_ctx* ctx, int n_ctas, int iters, double* tflops_out) {
     if (!ctx || !tflops_out || n_ctas < 1 || iters < 1) return PMGB_ERR_INVALID_ARGUMENT;
     PMGB_CK(ctx, enter_device(ctx->device));

@@ -362,6 +362,10 @@ cudaError_t pmgb_launch_sample_poses(unsigned long long seed, long long start, l
 cudaError_t pmgb_launch_philox(const unsigned int* ctr, const unsigned int* key, long long n,
                                unsigned int* out, cudaStream_t st);
 cudaError_t pmgb_launch_fp32_peak(float* sink, int n_ctas, int iters, cudaStream_t st);
+cudaError_t pmgb_launch_vdw_ordered(const double* f2c, int n_atoms, const double* atom_xf, const int* atom_sp,
+                                    int n_sp, const double* eps, const double* sig2, double r2_cut, long long n_conf,
+                                    int n_sites, const int* site_sp, const double* site_xf, double* out,
+                                    cudaStream_t st);
 cudaError_t pmgb_launch_rot_grid_out(const double* block_out, int n, double temperature, double log_n, double unit,
                                      float* out, cudaStream_t st);
 cudaError_t pmgb_launch_bounded_wait_test(unsigned int* status, unsigned long long limit_ns, int arm,

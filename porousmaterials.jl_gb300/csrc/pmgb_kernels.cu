@@ -476,6 +476,57 @@ __global__ void philox_kernel(const unsigned int* ctr, const unsigned int* key, 
     out[4 * i + 3] = r.w;
 }
 
+// Guest-host van der Waals energy in FP64 in the reference's own operation order, one
+// configuration per thread (src/vdw_energetics.jl:25-47): for each guest site i (outer) the
+// displacements x_j - x_i of the atoms in their given order, Xtals' nearest_image! (d -= sign(d)
+// where |d| > 1/2), Cartesian = f_to_c d summed left to right, r^2 = (dx^2 + dy^2) + dz^2, and for
+// r^2 < rc^2: +Inf if r^2 < 0.1, else E += ((4 eps) t) (t - 1) with t = (s2 / r^2)^3 = (u u) u.
+// Every operation is an explicit round-to-nearest FP64 operation (no contraction into FMAs),
+// so configurations whose energies are equal in exact arithmetic compare as the reference's
+// FP64 arithmetic compares them.  Serial in the atoms: meant for a handful of configurations.
+__global__ void vdw_ordered_kernel(const double* __restrict__ f2c, int n_atoms, const double* __restrict__ atom_xf,
+                                   const int* __restrict__ atom_sp, int n_sp, const double* __restrict__ eps,
+                                   const double* __restrict__ sig2, double r2_cut, long long n_conf, int n_sites,
+                                   const int* __restrict__ site_sp, const double* __restrict__ site_xf,
+                                   double* __restrict__ out) {
+    const long long c = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= n_conf) return;
+    double f[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) f[k] = f2c[k];  // column-major f_to_c: f[i + 3 j] = M[i][j]
+    double energy = 0.0;
+    for (int i = 0; i < n_sites; ++i) {
+        const double* xi = site_xf + (c * n_sites + i) * 3;
+        const double x0 = xi[0], x1 = xi[1], x2 = xi[2];
+        const int si = site_sp[i];
+        for (int j = 0; j < n_atoms; ++j) {
+            double d[3] = {__dsub_rn(atom_xf[3 * j], x0), __dsub_rn(atom_xf[3 * j + 1], x1),
+                           __dsub_rn(atom_xf[3 * j + 2], x2)};
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                if (fabs(d[k]) > 0.5) d[k] = __dsub_rn(d[k], d[k] > 0.0 ? 1.0 : -1.0);
+            double r[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                r[k] = __dadd_rn(__dadd_rn(__dmul_rn(f[k], d[0]), __dmul_rn(f[k + 3], d[1])), __dmul_rn(f[k + 6], d[2]));
+            const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(r[0], r[0]), __dmul_rn(r[1], r[1])), __dmul_rn(r[2], r[2]));
+            if (r2 < r2_cut) {
+                if (r2 < 0.1) {
+                    energy = __longlong_as_double(0x7ff0000000000000LL);  // +Inf, as the reference returns
+                    i = n_sites;
+                    break;
+                }
+                const int sj = atom_sp[j];
+                const double u = __ddiv_rn(sig2[si * n_sp + sj], r2);
+                const double t = __dmul_rn(__dmul_rn(u, u), u);
+                energy = __dadd_rn(energy, __dmul_rn(__dmul_rn(__dmul_rn(4.0, eps[si * n_sp + sj]), t),
+                                                     __dsub_rn(t, 1.0)));
+            }
+        }
+    }
+    out[c] = energy;
+}
+
 // FP32 FMA throughput probe: 8 independent dependency chains per thread.
 __global__ void __launch_bounds__(256) fp32_peak_kernel(float* sink, int iters) {
     float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1e-7f, a2 = a0 + 2e-7f, a3 = a0 + 3e-7f;
@@ -698,6 +749,16 @@ cudaError_t pmgb_launch_philox(const unsigned int* ctr, const unsigned int* key,
                                cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     philox_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(ctr, key, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t pmgb_launch_vdw_ordered(const double* f2c, int n_atoms, const double* atom_xf, const int* atom_sp,
+                                    int n_sp, const double* eps, const double* sig2, double r2_cut, long long n_conf,
+                                    int n_sites, const int* site_sp, const double* site_xf, double* out,
+                                    cudaStream_t st) {
+    if (n_conf <= 0) return cudaSuccess;
+    vdw_ordered_kernel<<<static_cast<unsigned>((n_conf + 63) / 64), 64, 0, st>>>(
+        f2c, n_atoms, atom_xf, atom_sp, n_sp, eps, sig2, r2_cut, n_conf, n_sites, site_sp, site_xf, out);
     return cudaGetLastError();
 }
 

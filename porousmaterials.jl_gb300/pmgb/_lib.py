@@ -94,6 +94,8 @@ SIGNATURES = [
     ("pmgb_batch_results", C.c_int, [_vp, _dp, _dp]),
     ("pmgb_batch_info", C.c_int, [_vp, C.POINTER(C.c_int64)]),
     ("pmgb_philox4x32_10", C.c_int, [_vp, C.c_int64, _up, _up, _up]),
+    ("pmgb_vdw_energy_ordered", C.c_int, [_vp, _dp, C.c_int32, _dp, _ip, C.c_int32, _dp, _dp, C.c_double,
+                                          C.c_int64, C.c_int32, _ip, _dp, _dp]),
     ("pmgb_fp32_peak", C.c_int, [_vp, C.c_int, C.c_int, _dp]),
     ("pmgb_device_status", C.c_int, [_vp, _up]),
     ("pmgb_test_bounded_wait", C.c_int, [_vp, C.c_int64, C.c_int32]),
@@ -195,6 +197,27 @@ class Context:
         out = np.zeros_like(ctr)
         self.check(self._lib.pmgb_philox4x32_10(self.handle, ctr.shape[0], ptr(ctr, C.c_uint32),
                                                 ptr(key, C.c_uint32), ptr(out, C.c_uint32)))
+        return out
+
+    def vdw_energy_ordered(self, f_to_c, atom_xf, atom_species, eps, sigma2, r2_cutoff: float, site_species,
+                           site_xf) -> np.ndarray:
+        """FP64 guest-host van der Waals energies (K) in the reference's operation order
+        (pmgb_vdw_energy_ordered).  atom_xf (n_atoms, 3) in the crystal's atom order; eps and
+        sigma2 (n_species, n_species) indexed [guest species, atom species]; site_xf
+        (n_conf, n_sites, 3)."""
+        f2c = np.ascontiguousarray(np.asarray(f_to_c, dtype=np.float64).reshape(3, 3).T)  # column-major
+        axf = np.ascontiguousarray(atom_xf, dtype=np.float64).reshape(-1, 3)
+        asp = np.ascontiguousarray(atom_species, dtype=np.int32)
+        e = np.ascontiguousarray(eps, dtype=np.float64)
+        s2 = np.ascontiguousarray(sigma2, dtype=np.float64)
+        ssp = np.ascontiguousarray(site_species, dtype=np.int32)
+        sxf = np.ascontiguousarray(site_xf, dtype=np.float64).reshape(-1, ssp.shape[0], 3)
+        assert asp.shape[0] == axf.shape[0] and e.shape == s2.shape and e.shape[0] == e.shape[1]
+        out = np.zeros(sxf.shape[0], dtype=np.float64)
+        self.check(self._lib.pmgb_vdw_energy_ordered(
+            self.handle, ptr(f2c, C.c_double), axf.shape[0], ptr(axf, C.c_double), ptr(asp, C.c_int32),
+            e.shape[0], ptr(e, C.c_double), ptr(s2, C.c_double), float(r2_cutoff), sxf.shape[0], ssp.shape[0],
+            ptr(ssp, C.c_int32), ptr(sxf, C.c_double), ptr(out, C.c_double)))
         return out
 
     def sample_poses(self, seed: int, start: int, n: int):

@@ -236,3 +236,28 @@ def test_native_ewald_setup_matches_the_restated_steps():
                             small.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), w.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     assert rc == -1 and n.value == ep.n_kvecs    # too small a capacity: refused, count still given
     assert L.pmgb_ewald_setup(fp, 12.5, 0.0, 0, None, None, None, ctypes.byref(n), None, None) == -1
+
+
+def test_reference_grid_positions_replay_the_grid_loop():
+    """reference_grid_positions equals a literal replay of energy_grid's loop (src/grid.jl:331-333)
+    with translate_to!'s FP64 steps (src/molecule.jl:147-151,176-179), bit for bit."""
+    from pmgb.energy_min import reference_grid_positions
+
+    for n_pts, rep, atom0, com0 in (((4, 3, 5), (2, 1, 3), [0.1234567, 0.7, 0.33], [0.1234567, 0.7, 0.33]),
+                                    ((15, 15, 15), (2, 2, 2), [0.0, 0.0, 0.0], [0.0, 0.0, 0.0]),
+                                    ((3, 6, 7), (3, 2, 1), [0.31, 0.29, 0.71], [0.3100000000000001, 0.29, 0.7])):
+        pts = [[(m / (n - 1.0)) for m in range(n)] for n in n_pts]
+        atom, com = np.array(atom0, dtype=float), np.array(com0, dtype=float)
+        seen = {}
+        for i in range(n_pts[0]):
+            for j in range(n_pts[1]):
+                for k in range(n_pts[2]):
+                    target = np.array([pts[0][i], pts[1][j], pts[2][k]]) / np.array(rep, dtype=float)
+                    d = target - com
+                    atom = atom + d
+                    com = com + d
+                    seen[(i, j, k)] = atom.copy()
+        ids = list(seen)
+        got = reference_grid_positions(n_pts, rep, atom0, com0, ids)
+        want = np.array([seen[t] for t in ids])
+        assert np.array_equal(got, want)
