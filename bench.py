@@ -42,6 +42,9 @@ F_LJ, F_COUL, F_K = 28, 40, 17
 # the same work counted by what the cutoff keeps: the distance of every pair 26; inside the
 # cutoff the LJ terms 11 and the real-space terms 30 more
 F_DIST, F_LJ_IN, F_ES_IN = 26, 11, 30
+# with image lists a distance is an offset from the warp's list: 3 subtractions and r^2 (5); the
+# list building (once per warp and image) and the close-pair residual terms are not counted
+F_DIST_IMG = 8
 REFINE_TAIL = 1e-3
 # DRAM traffic of the config1 pair kernel, from ncu (dram__bytes_read.sum + dram__bytes_write.sum of
 # one launch over 1e5 insertions: 0.59 MB read, 0 written; profiles/pairs_kernel_config1.md),
@@ -113,11 +116,13 @@ def flops_per_insertion(sc, mol, ep):
     return f
 
 
-def counted_flops(counts: dict, n_items: int, n_q_sites: int = 0, n_kvecs: int = 0) -> float:
+def counted_flops(counts: dict, n_items: int, n_q_sites: int = 0, n_kvecs: int = 0, image_lists: bool = False) -> float:
     """Algorithmic FP32 flops per item of the work a pass did (pmgb_*_work_counts): 26 per
-    (guest site, record) distance evaluated, 11 more per LJ term and 30 per real-space term inside
-    their cutoffs, 17 per (evaluated k-vector, guest charge)."""
-    return (F_DIST * counts["distances"] + F_LJ_IN * counts["lj_terms"] + F_ES_IN * counts["es_terms"]) / n_items + \
+    (guest site, record) distance evaluated (8 per (guest site, list image) distance with image
+    lists), 11 more per LJ term and 30 per real-space term inside their cutoffs, 17 per (evaluated
+    k-vector, guest charge)."""
+    fd = F_DIST_IMG if image_lists else F_DIST
+    return (fd * counts["distances"] + F_LJ_IN * counts["lj_terms"] + F_ES_IN * counts["es_terms"]) / n_items + \
         F_K * n_q_sites * n_kvecs
 
 
@@ -463,7 +468,7 @@ def batched_leg(args, ctx, stream, peak=None):
         c = gs.widom_work_counts(npb, N_BLOCKS, system_seed(100, s_))
         nq = int((gs.site_charge >= 0).sum()) if gs.charged else 0
         nk = gs.info()["n_kvecs_evaluated"] if gs.charged else 0
-        flops += counted_flops(c, npb * N_BLOCKS, nq, nk) * npb * N_BLOCKS
+        flops += counted_flops(c, npb * N_BLOCKS, nq, nk, gs.image_lists(npb * N_BLOCKS)) * npb * N_BLOCKS
     tf = flops / (ms_fp32 * 1e-3) / 1e12
     out["roofline"] = {"bound": "fp32", "achieved": tf, "unit": "TFLOP/s", "frac": tf / peak if peak else None,
                        "flops_per_run": flops, "fp32_pass_ms": ms_fp32,
@@ -471,7 +476,8 @@ def batched_leg(args, ctx, stream, peak=None):
                                  "batch kernel, partials and per-system reduction), CUDA events around the graph "
                                  "replay",
                        "counting": "pmgb_widom_work_counts of each system over its insertions of one run (26 / 11 / "
-                                   "30 / 17 flops per distance, LJ term, real-space term, k-term)"}
+                                   "30 / 17 flops per distance, LJ term, real-space term, k-term; 8 per distance "
+                                   "from an image list, the lists' building not counted)"}
     assert ctx.device_status() == 0
     out["refined_fraction"] = out["forward_plus_adjoint"]["refined_fraction"]
     out.update({"systems": len(systems), "frameworks": len(fws), "guests": ["CH4", "CO2"],
@@ -676,7 +682,7 @@ def config4_leg(args, ctx, ff, mol, timed, peak):
     err4 = widom_error(gs, ff, 4000, 44)
     fpi = flops_per_insertion(sc, mol, ep)
     work4 = gs.widom_work_counts(npb, N_BLOCKS, 42)   # the FP32-only run's insertions
-    fpc = counted_flops(work4, n, mol.n_charges, gs.info()["n_kvecs_evaluated"])
+    fpc = counted_flops(work4, n, mol.n_charges, gs.info()["n_kvecs_evaluated"], gs.image_lists(n))
     tf4 = fpc * n / (ms32 * 1e-3) / 1e12
     return {
         "workload": "CO2 in a 20,000-atom 52x52x52 A cell, Ewald 1e-6", "framework_sites": sc.atoms.n,
@@ -686,10 +692,11 @@ def config4_leg(args, ctx, ff, mol, timed, peak):
         "forward_plus_adjoint_insertions_per_s": n / (ms_adj * 1e-3),
         "roofline": {"bound": "fp32", "flops_per_insertion": fpc, "achieved": tf4, "unit": "TFLOP/s",
                      "frac": tf4 / peak if peak else None, "work_counts": work4,
-                     "kernel": "the FP32-only Widom pass (centre-image pair kernel + partials), CUDA events",
+                     "kernel": "the FP32-only Widom pass (image-list pair kernel + partials), CUDA events",
                      "counting": "counted by pmgb_widom_work_counts over the same insertions: distances "
-                                 "evaluated (sub-chunks skipped whole are not), LJ and real-space terms inside "
-                                 "their cutoffs, k-terms of the evaluated k-vectors (26 / 11 / 30 / 17 flops)"},
+                                 "evaluated (8 flops each from an image list, the lists' building not counted), "
+                                 "LJ and real-space terms inside their cutoffs, k-terms of the evaluated "
+                                 "k-vectors (11 / 30 / 17 flops)"},
         "every_pair_flops_per_insertion": fpi,
         "every_pair_tflops": fpi * n / (ms32 * 1e-3) / 1e12,
         "note": "every_pair_tflops counts every pair and k-vector; in this 52 A cell the kernel skips whole "
@@ -941,7 +948,7 @@ def ours(args, rank, world, local_rank):
     achieved_every = fpi * n_ins / (kernel_ms * 1e-3) / 1e12
     n_kev = system.info()["n_kvecs_evaluated"]
     work = system.widom_work_counts(npb, N_BLOCKS, 1)   # the insertions of the first timed step
-    fpi_in = counted_flops(work, n_ins, mol.n_charges, n_kev)
+    fpi_in = counted_flops(work, n_ins, mol.n_charges, n_kev, system.image_lists(n_ins))
     fpi_est = flops_inside_cutoff(sc, mol, ff, ep, n_kev)
     achieved = fpi_in * n_ins / (kernel_ms * 1e-3) / 1e12
     cpu = None
@@ -1000,10 +1007,11 @@ def ours(args, rank, world, local_rank):
                         "flops_per_insertion": fpi_in,
                         "work_counts": work,
                         "counting": "the work the kernel does, counted by its work-counting pass "
-                                    "(pmgb_widom_work_counts) over the first timed step's insertions: 26 flops per "
-                                    "(guest site, record) distance evaluated (no sub-chunk of this cell is skipped), "
-                                    "11 more per LJ and 30 per real-space term inside their cutoffs, 17 per "
-                                    "(evaluated k-vector, guest charge); FMA = 2, MUFU = 1",
+                                    "(pmgb_widom_work_counts) over the first timed step's insertions: 8 flops per "
+                                    "(guest site, list image) distance (3 subtractions and r^2 from the warp's image "
+                                    "list; building the lists, ~60 flops per image and warp, is not counted), 11 "
+                                    "more per LJ and 30 per real-space term inside their cutoffs, 17 per (evaluated "
+                                    "k-vector, guest charge); FMA = 2, MUFU = 1",
                         "flops_per_insertion_uniform_estimate": fpi_est,
                         "kvectors_evaluated": system.info()["n_kvecs_evaluated"],
                         "every_pair": {"flops_per_insertion": fpi, "achieved": achieved_every,

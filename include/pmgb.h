@@ -237,6 +237,23 @@ int pmgb_system_set_cull(pmgb_system* sys, int32_t on);
  * when it is created. */
 int pmgb_system_set_centre_image(pmgb_system* sys, int32_t on);
 
+/* Image lists for the spatially ordered Widom pass (no reference counterpart).  mode 0: off;
+ * 1 (the default): where the run's insertions are dense enough that a CTA's list is expected to
+ * hold under 60% of the records; 2: always where they apply.  They apply where culling is on, the
+ * guest has one or three sites and every perpendicular width exceeds twice the larger cutoff.  The
+ * insertions of a run are sorted once by position; each CTA (256 insertions) gathers the periodic
+ * images of the framework records within (cutoff + the spread of its guest sites) of its sites'
+ * centre, as double-float Cartesian offsets, into a shared-memory list, and its lanes take
+ * distances from that list (pairs closer than 4 A with the offsets' residuals).  The energies are
+ * the per-site form's to FP32 rounding, with the same error bound against FP64.  A batch takes
+ * image lists for its systems that qualify, over the same insertion order, so its results equal
+ * the single-system runs'. */
+int pmgb_system_set_image_lists(pmgb_system* sys, int32_t mode);
+
+/* *on_out = 1 when a forward Widom run of n_insertions insertions of this system takes image
+ * lists (the mode, culling, the guest, the widths and the density all allow it), else 0. */
+int pmgb_system_image_lists(const pmgb_system* sys, int64_t n_insertions, int32_t* on_out);
+
 /* *on_out = 1 when Widom insertions of this system take the centre-image form (switched on, a
  * guest with several sites, and every width wide enough for the current cutoffs), else 0. */
 int pmgb_system_centre_image(const pmgb_system* sys, int32_t* on_out);
@@ -259,8 +276,11 @@ int pmgb_widom_device(pmgb_system* sys, int64_t n_per_block, int32_t n_blocks, u
  * array (3 MiB, held by every GPU that loads the library until the process exits), sized for
  * at most 65,536 CTAs: n_blocks * ceil(n_per_block / 256) <= 65536, i.e. up to 16.7M
  * insertions per call; larger requests fail with PMGB_ERR_INVALID_ARGUMENT.
- * What it computes: the FP32 pass of pmgb_widom_device with the same poses, energies and block
- * results.  Spatial ordering (pmgb_system_set_cull) is not applied; it changes no result bit.
+ * What it computes: the unordered FP32 pass (per-site distances) with the poses of
+ * pmgb_widom_device.  Its energies and block results equal pmgb_widom_device's bit for bit where
+ * that call takes per-site distances too (culling alone changes no result bit); where
+ * pmgb_widom_device takes image lists (pmgb_system_set_image_lists) the two differ by FP32
+ * rounding.
  * FP64 tail refinement needs per-run scratch, so a system with pmgb_system_set_refine(> 0) is
  * refused with PMGB_ERR_INVALID_ARGUMENT rather than given an unrefined K_H.
  * The caller passes device-resident outputs (block_out_dev: 4*n_blocks doubles, u_out_dev

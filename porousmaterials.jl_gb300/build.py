@@ -20,7 +20,7 @@ OUT_DIR = HERE / "pmgb"
 LIB = OUT_DIR / "libpmgb.so"
 OBJ_DIR = HERE / "_build"
 
-SOURCES = ["pmgb_kernels.cu", "pmgb_batch.cu", "pmgb_refine.cu", "pmgb_api.cu", "pmgb_setup.cu"]
+SOURCES = ["pmgb_kernels.cu", "pmgb_img.cu", "pmgb_batch.cu", "pmgb_refine.cu", "pmgb_api.cu", "pmgb_setup.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no floating-point contraction, so x86 and Arm builds give the same host results
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-ftz=true", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off", f"-I{INCLUDE}",

@@ -113,6 +113,7 @@ struct pmgb_system {
     double refine_tail = 0.0;       // FP64 refinement of the Boltzmann tail (0: off)
     bool cull = true;               // spatially ordered processing with cutoff culling
     bool centre_image = true;       // centre-image distances where the geometry allows them
+    int image_lists = 1;            // ordered Widom passes: image lists (csrc/pmgb_img.cu): 0 off, 1 auto, 2 on
     bool exact = true;              // single-configuration energies and grids to the FP64 tolerance
     double bound_kappa = 1.0;       // rounding condition of the box (scales the FP32 error estimate)
     DevBuf o_counts, o_perm;        // Widom processing order scratch
@@ -171,8 +172,11 @@ void dev_free(pmgb_ctx* ctx, void* p) {
 
 // The Widom passes' pair-kernel launch, between two CUDA events on the launching stream when
 // kernel timing is on (at most 4096 launches are timed between two reads).
-cudaError_t launch_pairs_timed(pmgb_ctx* ctx, const LaunchArgs& a, int n_ctas) {
-    if (!ctx->timing || ctx->timing_used >= 4096) return pmgb_launch_pairs(a, n_ctas, ctx->stream);
+cudaError_t launch_pairs_timed(pmgb_ctx* ctx, const LaunchArgs& a, int n_ctas, bool img = false) {
+    auto launch = [&]() {
+        return img ? pmgb_launch_pairs_img(a, n_ctas, ctx->stream) : pmgb_launch_pairs(a, n_ctas, ctx->stream);
+    };
+    if (!ctx->timing || ctx->timing_used >= 4096) return launch();
     if (ctx->timing_used == ctx->timing_events.size()) {
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         cudaError_t e = cudaEventCreate(&e0);
@@ -185,7 +189,7 @@ cudaError_t launch_pairs_timed(pmgb_ctx* ctx, const LaunchArgs& a, int n_ctas) {
     }
     const auto& ev = ctx->timing_events[ctx->timing_used++];
     cudaError_t e = cudaEventRecord(ev.first, ctx->stream);
-    if (e == cudaSuccess) e = pmgb_launch_pairs(a, n_ctas, ctx->stream);
+    if (e == cudaSuccess) e = launch();
     if (e == cudaSuccess) e = cudaEventRecord(ev.second, ctx->stream);
     return e;
 }
@@ -2079,6 +2083,53 @@ extern "C" int pmgb_system_set_cull(pmgb_system* s, int32_t on) {
     return PMGB_OK;
 }
 
+extern "C" int pmgb_system_set_image_lists(pmgb_system* s, int32_t mode) {
+    if (!s) return PMGB_ERR_INVALID_ARGUMENT;
+    if (mode < 0 || mode > 2)
+        return fail(s->ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_system_set_image_lists: mode 0 (off), 1 (auto) or 2 (on)");
+    s->image_lists = mode;
+    return PMGB_OK;
+}
+
+// Whether the spatially ordered forward Widom pass of a run of n insertions takes image lists: a
+// guest form the kernels instantiate, every perpendicular width above twice the larger cutoff (at
+// most one image of a record within the cutoff of a site; the replication factors guarantee it for
+// the LJ cutoff), and (auto) a CTA's list expected to hold under 60% of the records.  The CTA's
+// 256 insertions, in the run's Z order, occupy about 256 V / n of the cell: a region of radius
+// ~1.6 (3 256 V / (4 pi n))^(1/3) (the factor for the order's elongated chunks, from simulated
+// orders of the config1, config3 and config4 shapes); its list holds the images within
+// cutoff + guest reach + that radius of the centre.
+static bool image_lists_fit(const pmgb_system* s, int mode) {
+    if (mode == 0 || !pmgb_img_supported(s->dev.n_sites)) return false;
+    const double rc2 = std::max<double>(s->dev.rc2, s->dev.charged ? s->dev.rc2e : 0.0);
+    for (int a = 0; a < 3; ++a) {
+        const double w = static_cast<double>(s->dev.cw[a]) * 4294967296.0;
+        if (!(4.0 * rc2 < w * w * (1.0 - 1e-6))) return false;
+    }
+    return true;
+}
+
+static bool image_lists_for(const pmgb_system* s, int64_t n_insertions) {
+    if (!image_lists_fit(s, s->image_lists)) return false;
+    if (s->image_lists == 2) return true;
+    const double pi = 3.14159265358979323846;
+    const double vol = std::fabs(s->dev.f2c64[0] * s->dev.f2c64[3] * s->dev.f2c64[5]);
+    const double r_cta = 1.6 * std::cbrt(3.0 * PMGB_THREADS * vol / (4.0 * pi * std::max<int64_t>(n_insertions, 1)));
+    const double rc = std::sqrt(std::max<double>(s->dev.rc2, s->dev.charged ? s->dev.rc2e : 0.0));
+    const double reach = rc + s->dev.com_reach + r_cta;
+    return 4.0 / 3.0 * pi * reach * reach * reach < 0.6 * vol;
+}
+
+static bool uses_image_lists(const pmgb_system* s, int64_t n_insertions) {
+    return s->cull && image_lists_for(s, n_insertions);
+}
+
+extern "C" int pmgb_system_image_lists(const pmgb_system* s, int64_t n_insertions, int32_t* on_out) {
+    if (!s || !on_out || n_insertions < 1) return PMGB_ERR_INVALID_ARGUMENT;
+    *on_out = uses_image_lists(s, n_insertions) ? 1 : 0;
+    return PMGB_OK;
+}
+
 extern "C" int pmgb_system_centre_image(const pmgb_system* s, int32_t* on_out) {
     if (!s || !on_out) return PMGB_ERR_INVALID_ARGUMENT;
     *on_out = (s->dev.com_axis >= -1 && s->dev.n_sites > 1) ? 1 : 0;
@@ -2141,7 +2192,22 @@ extern "C" int pmgb_widom_device(pmgb_system* s, int64_t n_per_block, int32_t n_
         if (int rc = ensure(ctx, s->g_u, sizeof(double) * 2 * n_ins)) return rc;
         a.u_out = static_cast<double*>(s->g_u.p);
     }
-    if (s->cull) {
+    if (uses_image_lists(s, static_cast<int64_t>(n_ins))) {
+        // one spatial order over the whole run; warps gather their image lists (csrc/pmgb_img.cu);
+        // the block sums are formed from the energies in insertion order
+        if (n_ins > static_cast<size_t>(INT32_MAX))
+            return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom: too many insertions for one run");
+        const long long n_cells = 1ll << (3 * pmgb_run_order_bits(static_cast<long long>(n_ins)));
+        int rc;
+        if ((rc = ensure(ctx, s->o_counts, sizeof(int) * n_cells)) || (rc = ensure(ctx, s->o_perm, sizeof(int) * n_ins)))
+            return rc;
+        a.perm = static_cast<const int*>(s->o_perm.p);
+        PMGB_CK(ctx, pmgb_launch_run_order(seed, static_cast<long long>(n_ins), static_cast<int*>(s->o_counts.p),
+                                           static_cast<int*>(s->o_perm.p), ctx->stream));
+        PMGB_CK(ctx, launch_pairs_timed(ctx, a, n_ctas, true));
+        PMGB_CK(ctx, pmgb_launch_lse_from_u(a.u_out, n_per_block, n_blocks, a.ctas_per_block, a.inv_temperature,
+                                            a.partials, ctx->stream));
+    } else if (s->cull) {
         // spatially sorted processing order, so that warps can skip out-of-cutoff records; the
         // block sums are then formed from the energies in insertion order
         int rc;
@@ -2162,10 +2228,11 @@ extern "C" int pmgb_widom_device(pmgb_system* s, int64_t n_per_block, int32_t n_
     return PMGB_OK;
 }
 
-// The unordered FP32 Widom pass of pmgb_widom_device, with the per-CTA partials in the
+// The unordered FP32 Widom pass (per-site distances), with the per-CTA partials in the
 // library's fixed device array instead of memory the system allocates; nothing is allocated
-// or freed.  Spatial ordering is not applied: it changes no result bit (the ordered pass forms
-// the same sums), only the time.  A system with FP64 tail refinement is refused.
+// or freed.  Spatial ordering with per-site distances changes no result bit (the ordered pass
+// forms the same sums); image lists change FP32 roundings.  A system with FP64 tail refinement
+// is refused.
 extern "C" int pmgb_widom_noalloc(pmgb_system* s, int64_t n_per_block, int32_t n_blocks, uint64_t seed,
                                   double temperature, double* block_out_dev, double* u_out_dev) {
     if (!s) return PMGB_ERR_INVALID_ARGUMENT;
@@ -2570,12 +2637,12 @@ extern "C" int pmgb_energy_grid_device(pmgb_system* s, const int32_t n_pts[3], c
 
 // The work-counting pass (pmgb_launch_pairs_stats) on prepared arguments; counts_out receives the
 // three counters.
-static int run_work_counts(pmgb_system* s, LaunchArgs& a, int n_ctas, int64_t counts_out[3]) {
+static int run_work_counts(pmgb_system* s, LaunchArgs& a, int n_ctas, int64_t counts_out[3], bool img = false) {
     pmgb_ctx* ctx = s->ctx;
     if (int rc = ensure(ctx, s->stats, sizeof(unsigned long long) * 3)) return rc;
     a.stats = static_cast<unsigned long long*>(s->stats.p);
     PMGB_CK(ctx, cudaMemsetAsync(a.stats, 0, sizeof(unsigned long long) * 3, ctx->stream));
-    const cudaError_t e = pmgb_launch_pairs_stats(a, n_ctas, ctx->stream);
+    const cudaError_t e = img ? pmgb_launch_pairs_img(a, n_ctas, ctx->stream) : pmgb_launch_pairs_stats(a, n_ctas, ctx->stream);
     if (e == cudaErrorNotSupported)
         return fail(ctx, PMGB_ERR_UNSUPPORTED, "work counts: guests of one or three sites only (got %d)", s->n_sites);
     PMGB_CK(ctx, e);
@@ -2599,9 +2666,13 @@ extern "C" int pmgb_widom_work_counts(pmgb_system* s, int64_t n_per_block, int32
     if (cpb > INT32_MAX / n_blocks) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_work_counts: too many");
     PMGB_CK(ctx, enter_device(ctx->device));
     const size_t n_ins = static_cast<size_t>(n_per_block) * n_blocks;
+    const bool img = uses_image_lists(s, static_cast<int64_t>(n_ins));
+    if (img && n_ins > static_cast<size_t>(INT32_MAX))
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_work_counts: too many insertions for one run");
+    const size_t n_cells = img ? size_t{1} << (3 * pmgb_run_order_bits(static_cast<long long>(n_ins)))
+                               : pmgb_widom_order_cells() * n_blocks;
     int rc;
-    if ((rc = ensure(ctx, s->o_counts, sizeof(int) * pmgb_widom_order_cells() * n_blocks)) ||
-        (rc = ensure(ctx, s->o_perm, sizeof(int) * n_ins)))
+    if ((rc = ensure(ctx, s->o_counts, sizeof(int) * n_cells)) || (rc = ensure(ctx, s->o_perm, sizeof(int) * n_ins)))
         return rc;
     LaunchArgs a = base_args(s);
     a.pose_mode = POSE_PHILOX;
@@ -2612,6 +2683,13 @@ extern "C" int pmgb_widom_work_counts(pmgb_system* s, int64_t n_per_block, int32
     a.ctas_per_block = static_cast<int>(cpb);
     a.inv_temperature = 1.0;
     a.perm = static_cast<const int*>(s->o_perm.p);  // the spatially ordered pass of pmgb_widom_device
+    if (img) {
+        if ((rc = ensure(ctx, s->g_u, sizeof(double) * 2 * n_ins))) return rc;
+        a.u_out = static_cast<double*>(s->g_u.p);
+        PMGB_CK(ctx, pmgb_launch_run_order(seed, static_cast<long long>(n_ins), static_cast<int*>(s->o_counts.p),
+                                           static_cast<int*>(s->o_perm.p), ctx->stream));
+        return run_work_counts(s, a, static_cast<int>(cpb * n_blocks), counts_out, true);
+    }
     PMGB_CK(ctx, pmgb_launch_widom_order(seed, n_per_block, n_blocks, static_cast<int*>(s->o_counts.p),
                                          static_cast<int*>(s->o_perm.p), ctx->stream));
     return run_work_counts(s, a, static_cast<int>(cpb * n_blocks), counts_out);
@@ -2880,6 +2958,9 @@ struct pmgb_batch {
     int* d_perm = nullptr;
     int* d_cells = nullptr;
     double* d_unit_m = nullptr;
+    // image-list systems (forward runs with refinement): one order over each system's run
+    int64_t img_cells = 0;             // sum over systems of 2^(3 order_bits)
+    int* d_img_cells = nullptr;
     cudaGraphExec_t exec = nullptr;
     bool launched = false;
 };
@@ -2892,7 +2973,7 @@ void batch_free(pmgb_batch* b) {
     void* ptrs[] = {b->d_sys, b->d_units, b->d_order, b->d_counter, b->d_run, b->d_partials,
                     b->d_dsum, b->d_unit_cols, b->d_block_out, b->d_out_cols, b->d_chunk_sys, b->d_u,
                     b->d_hist, b->d_cut, b->d_counts, b->d_offsets, b->d_list, b->d_ref_u,
-                    b->d_plan, b->d_done, b->d_part, b->d_perm, b->d_cells, b->d_unit_m};
+                    b->d_plan, b->d_done, b->d_part, b->d_perm, b->d_cells, b->d_unit_m, b->d_img_cells};
     for (void* p : ptrs) dev_free(b->ctx, p);
 }
 
@@ -2911,6 +2992,22 @@ int batch_capture(pmgb_batch* b) {
         PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));
         cudaGraphExecDestroy(b->exec);
         b->exec = nullptr;
+    }
+    // image lists for the systems that allow them, in forward runs with spatial order
+    bool any_img = false, changed = false;
+    for (size_t i = 0; i < b->systems.size(); ++i) {
+        const int img = (!b->grad && b->cull &&
+                         image_lists_for(b->systems[i], b->host_sys[i].n_per_block * b->n_blocks)) ? 1 : 0;
+        changed = changed || b->host_sys[i].img != img;
+        b->host_sys[i].img = img;
+        any_img = any_img || img;
+    }
+    if (any_img && !b->d_img_cells)
+        if (int rc = batch_alloc(b, &b->d_img_cells, static_cast<size_t>(b->img_cells))) return rc;
+    if (changed) {
+        PMGB_CK(ctx, cudaMemcpyAsync(b->d_sys, b->host_sys.data(), sizeof(BatchSystem) * b->host_sys.size(),
+                                     cudaMemcpyHostToDevice, ctx->stream));
+        PMGB_CK(ctx, cudaStreamSynchronize(ctx->stream));  // host_sys may change again before the next upload
     }
     BatchArgs a{};
     a.systems = b->d_sys;
@@ -2960,6 +3057,9 @@ int batch_capture(pmgb_batch* b) {
     if (e == cudaSuccess && b->cull)
         e = pmgb_launch_batch_order(b->d_sys, b->d_chunk_sys, n_chunks, n_sys, b->n_blocks, b->d_run, b->d_cells,
                                     b->d_perm, st);
+    if (e == cudaSuccess && any_img)
+        e = pmgb_launch_batch_run_order(b->d_sys, b->d_chunk_sys, n_chunks, n_sys, b->d_run, b->d_img_cells,
+                                        b->img_cells, b->d_perm, st);
     if (e == cudaSuccess) e = pmgb_launch_batch(a, b->grad, b->n_ctas, st);
     if (e == cudaSuccess && b->cull)
         e = pmgb_launch_batch_lse(b->d_sys, b->d_chunk_sys, n_chunks, b->d_run, b->d_u, b->d_partials, st);
@@ -3085,6 +3185,10 @@ extern "C" int pmgb_batch_create(pmgb_ctx* ctx, int32_t n_systems, pmgb_system* 
         bs.col_base = col_base;
         bs.out_base = out_base;
         bs.u_base = b->n_insertions;
+        bs.img = 0;  // set with the run's settings (batch_capture)
+        bs.order_bits = pmgb_run_order_bits(n_per_block[i] * n_blocks);
+        bs.cell_base = b->img_cells;
+        b->img_cells += int64_t{1} << (3 * bs.order_bits);
         // cost model of one chunk: algorithmic flops of its pair and reciprocal-space terms
         const double pair = s->dev.charged ? 68.0 : 28.0;
         b->chunk_flops.push_back(PMGB_THREADS * nst *

@@ -9,7 +9,7 @@
 // its Boltzmann-weighted r^-12 / r^-6 columns inside the unit (weights relative to the
 // unit's own maximum of -U/T), so no per-insertion columns reach HBM; a per-system
 // reduction combines units in a fixed order.
-#include "pmgb_device.cuh"
+#include "pmgb_img.cuh"
 
 namespace {
 
@@ -65,7 +65,27 @@ __device__ __forceinline__ bool run_variant(int variant, bool no_resid, bool com
     return run_variant_r<GRAD, true>(variant, comp, S, io, stage, bars, red, fills, status);
 }
 
+// image-list units of a forward run with refinement (csrc/pmgb_img.cuh), one function per variant
+template <int NS, bool CHARGED>
+__device__ __noinline__ void img_unit_fn(const SysDev& S, const UnitIO& io, unsigned char* smem) {
+    img_unit<NS, CHARGED, false>(S, io, smem);
+}
+
+// the list takes the TMA ring's shared memory (idle here: every copy a unit issues is consumed
+// inside that unit)
+__device__ __forceinline__ void run_img(const SysDev& S, const UnitIO& io, unsigned char* smem) {
+    if (S.n_sites == 1) {
+        if (S.charged) img_unit_fn<1, true>(S, io, smem);
+        else img_unit_fn<1, false>(S, io, smem);
+    } else {
+        if (S.charged) img_unit_fn<3, true>(S, io, smem);
+        else img_unit_fn<3, false>(S, io, smem);
+    }
+}
+
 static_assert(sizeof(BatchSystem) % 4 == 0, "BatchSystem is copied to shared memory as 32-bit words");
+static_assert(kImgSmemBytes <= size_t(PMGB_NSTAGE) * PMGB_TILE * sizeof(int4),
+              "the image list fits in the TMA ring's shared memory");
 
 template <bool GRAD>
 __global__ void __launch_bounds__(PMGB_THREADS, 2) batch_kernel(const __grid_constant__ BatchArgs b) {
@@ -110,6 +130,14 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) batch_kernel(const __grid_con
             long long within = slot_in_block;
             if (b.perm && io.valid)
                 within = b.perm[s_bs.u_base + static_cast<long long>(unit.block) * npb + slot_in_block];
+            if (!GRAD && s_bs.img) {
+                // one order over the system's whole run: perm holds the system's insertion index
+                io.item = io.valid ? within : 0;
+                io.seed = run.seed + static_cast<unsigned long long>(unit.system) * 0x9E3779B97F4A7C15ull;
+                io.u_out = b.u + 2 * s_bs.u_base;
+                run_img(s_bs.sys, io, smem_raw);
+                continue;
+            }
             io.item = static_cast<long long>(unit.block) * npb + within;
             io.cull = b.perm != nullptr;
             io.seed = run.seed + static_cast<unsigned long long>(unit.system) * 0x9E3779B97F4A7C15ull;
@@ -286,7 +314,7 @@ __device__ __forceinline__ ChunkRef chunk_ref(const BatchSystem* systems, const 
 __global__ void batch_order_count_kernel(const BatchSystem* systems, const int* chunk_sys, int n_blocks,
                                          const BatchRun* run, int* counts) {
     const ChunkRef r = chunk_ref(systems, chunk_sys, blockIdx.x, threadIdx.x);
-    if (!r.valid) return;
+    if (!r.valid || systems[r.sys].img) return;
     const unsigned long long seed = run->seed + static_cast<unsigned long long>(r.sys) * 0x9E3779B97F4A7C15ull;
     const int cell = batch_cell(seed, static_cast<unsigned long long>(r.blk * r.npb + r.within));
     atomicAdd(&counts[(static_cast<size_t>(r.sys) * n_blocks + r.blk) * kBatchOrderCells + cell], 1);
@@ -323,11 +351,63 @@ __global__ void __launch_bounds__(1024) batch_order_scan_kernel(int* counts) {
 __global__ void batch_order_scatter_kernel(const BatchSystem* systems, const int* chunk_sys, int n_blocks,
                                            const BatchRun* run, int* offsets, int* perm) {
     const ChunkRef r = chunk_ref(systems, chunk_sys, blockIdx.x, threadIdx.x);
-    if (!r.valid) return;
+    if (!r.valid || systems[r.sys].img) return;
     const unsigned long long seed = run->seed + static_cast<unsigned long long>(r.sys) * 0x9E3779B97F4A7C15ull;
     const int cell = batch_cell(seed, static_cast<unsigned long long>(r.blk * r.npb + r.within));
     const int pos = atomicAdd(&offsets[(static_cast<size_t>(r.sys) * n_blocks + r.blk) * kBatchOrderCells + cell], 1);
     perm[systems[r.sys].u_base + r.blk * r.npb + pos] = static_cast<int>(r.within);
+}
+
+// ---- one order over each image-list system's run (the single-system order, csrc/pmgb_img.cu) ----
+__global__ void batch_run_count_kernel(const BatchSystem* systems, const int* chunk_sys, const BatchRun* run,
+                                       int* cells) {
+    const ChunkRef r = chunk_ref(systems, chunk_sys, blockIdx.x, threadIdx.x);
+    if (!r.valid) return;
+    const BatchSystem& bs = systems[r.sys];
+    if (!bs.img) return;
+    const unsigned long long seed = run->seed + static_cast<unsigned long long>(r.sys) * 0x9E3779B97F4A7C15ull;
+    atomicAdd(&cells[bs.cell_base + run_cell(seed, static_cast<unsigned long long>(r.blk * r.npb + r.within),
+                                             bs.order_bits)], 1);
+}
+
+// exclusive scan of one image-list system's cells (CTA s: system s)
+__global__ void __launch_bounds__(1024) batch_run_scan_kernel(const BatchSystem* systems, int* cells) {
+    const BatchSystem& bs = systems[blockIdx.x];
+    if (!bs.img) return;  // uniform over the CTA
+    scan_cells(cells + bs.cell_base, 1 << (3 * bs.order_bits));
+}
+
+__global__ void batch_run_scatter_kernel(const BatchSystem* systems, const int* chunk_sys, const BatchRun* run,
+                                         int* cells, int* perm) {
+    const ChunkRef r = chunk_ref(systems, chunk_sys, blockIdx.x, threadIdx.x);
+    if (!r.valid) return;
+    const BatchSystem& bs = systems[r.sys];
+    if (!bs.img) return;
+    const unsigned long long seed = run->seed + static_cast<unsigned long long>(r.sys) * 0x9E3779B97F4A7C15ull;
+    const long long idx = r.blk * r.npb + r.within;
+    const int pos = atomicAdd(&cells[bs.cell_base + run_cell(seed, static_cast<unsigned long long>(idx), bs.order_bits)], 1);
+    perm[bs.u_base + pos] = static_cast<int>(idx);
+}
+
+// each cell's insertions by index (CTA s: system s; cells[c] is the end of cell c after the scatter)
+__global__ void batch_run_sort_kernel(const BatchSystem* systems, const int* cells, int* perm) {
+    const BatchSystem& bs = systems[blockIdx.x];
+    if (!bs.img) return;
+    const int n_cells = 1 << (3 * bs.order_bits);
+    const int* end = cells + bs.cell_base;
+    int* p = perm + bs.u_base;
+    for (int c = threadIdx.x; c < n_cells; c += blockDim.x) {
+        const int lo = c == 0 ? 0 : end[c - 1], hi = end[c];
+        for (int i = lo + 1; i < hi; ++i) {
+            const int v = p[i];
+            int j = i - 1;
+            while (j >= lo && p[j] > v) {
+                p[j + 1] = p[j];
+                --j;
+            }
+            p[j + 1] = v;
+        }
+    }
 }
 
 // per-chunk log-sum-exp partials in insertion order (what the kernel forms without a spatial order)
@@ -366,6 +446,17 @@ cudaError_t pmgb_launch_batch_order(const BatchSystem* systems, const int* chunk
     batch_order_count_kernel<<<n_chunks, PMGB_THREADS, 0, st>>>(systems, chunk_sys, n_blocks, run, counts);
     batch_order_scan_kernel<<<n_systems * n_blocks, 1024, 0, st>>>(counts);
     batch_order_scatter_kernel<<<n_chunks, PMGB_THREADS, 0, st>>>(systems, chunk_sys, n_blocks, run, counts, perm);
+    return cudaGetLastError();
+}
+
+cudaError_t pmgb_launch_batch_run_order(const BatchSystem* systems, const int* chunk_sys, int n_chunks, int n_systems,
+                                        const BatchRun* run, int* cells, long long n_cells, int* perm, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(cells, 0, sizeof(int) * static_cast<size_t>(n_cells), st);
+    if (e != cudaSuccess) return e;
+    batch_run_count_kernel<<<n_chunks, PMGB_THREADS, 0, st>>>(systems, chunk_sys, run, cells);
+    batch_run_scan_kernel<<<n_systems, 1024, 0, st>>>(systems, cells);
+    batch_run_scatter_kernel<<<n_chunks, PMGB_THREADS, 0, st>>>(systems, chunk_sys, run, cells, perm);
+    batch_run_sort_kernel<<<n_systems, 256, 0, st>>>(systems, cells, perm);
     return cudaGetLastError();
 }
 

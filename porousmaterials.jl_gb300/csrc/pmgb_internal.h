@@ -210,6 +210,15 @@ cudaError_t pmgb_launch_energies_latency(const LaunchArgs& a, int n_ctas, cudaSt
 cudaError_t pmgb_launch_widom_order(unsigned long long seed, long long n_per_block, int n_blocks, int* counts,
                                     int* perm, cudaStream_t st);
 size_t pmgb_widom_order_cells();
+// Image-list Widom pass (csrc/pmgb_img.cu): one spatial order over a whole run (counts: scratch of
+// 2^(3 bits) cells, bits = pmgb_run_order_bits(n); perm: [n] insertion indices in processing
+// order, each cell's insertions by index), and the pass itself (a.perm, a.u_out required; one
+// CTA per PMGB_THREADS slots of perm; a.stats set: the work-counting variant).
+int pmgb_run_order_bits(long long n);
+cudaError_t pmgb_launch_run_order(unsigned long long seed, long long n, int* counts, int* perm, cudaStream_t st);
+bool pmgb_img_supported(int n_sites);
+size_t pmgb_img_smem_bytes();
+cudaError_t pmgb_launch_pairs_img(const LaunchArgs& a, int n_ctas, cudaStream_t st);
 // Per-CTA log-sum-exp partials of a Widom run from its per-insertion energies, in insertion
 // order (the partials the pair kernel forms itself when it runs without a permutation).
 cudaError_t pmgb_launch_lse_from_u(const double* u, long long n_per_block, int n_blocks, int ctas_per_block,
@@ -237,6 +246,9 @@ struct BatchSystem {
     long long col_base;   // adjoint: first of this system's chunk column partials (n_cols per chunk)
     long long out_base;   // adjoint: first of this system's 3 + n_cols combined outputs
     long long u_base;     // first of this system's insertions in the batch's per-insertion energies
+    int img;              // forward run in spatial order: image lists over one order of the system's run
+    int order_bits;       // image lists: Z-order cells per axis 2^order_bits (pmgb_run_order_bits)
+    long long cell_base;  // image lists: first of this system's cells in the batch's order counts
 };
 struct BatchUnit {
     int system, block, chunk0, n_chunks;
@@ -346,6 +358,10 @@ cudaError_t pmgb_launch_batch_reduce(const BatchSystem* systems, int n_systems, 
 size_t pmgb_batch_order_cells();
 cudaError_t pmgb_launch_batch_order(const BatchSystem* systems, const int* chunk_sys, int n_chunks, int n_systems,
                                     int n_blocks, const BatchRun* run, int* counts, int* perm, cudaStream_t st);
+// Image-list systems of a batch: one order over each such system's run (cells: the batch's
+// counts, system s at cell_base), perm[u_base + slot] = the system's insertion index.
+cudaError_t pmgb_launch_batch_run_order(const BatchSystem* systems, const int* chunk_sys, int n_chunks, int n_systems,
+                                        const BatchRun* run, int* cells, long long n_cells, int* perm, cudaStream_t st);
 cudaError_t pmgb_launch_batch_lse(const BatchSystem* systems, const int* chunk_sys, int n_chunks, const BatchRun* run,
                                   const double* u, LsePartial* partials, cudaStream_t st);
 cudaError_t pmgb_launch_reduce_blocks(const LsePartial* partials, int n_blocks, int ctas_per_block,

@@ -58,6 +58,8 @@ SIGNATURES = [
     ("pmgb_structure_factor", C.c_int, [_vp, _dp]),
     ("pmgb_energies", C.c_int, [_vp, C.c_int64, _dp, _dp]),
     ("pmgb_system_set_cull", C.c_int, [_vp, C.c_int32]),
+    ("pmgb_system_set_image_lists", C.c_int, [_vp, C.c_int32]),
+    ("pmgb_system_image_lists", C.c_int, [_vp, C.c_int64, _ip]),
     ("pmgb_system_set_centre_image", C.c_int, [_vp, C.c_int32]),
     ("pmgb_system_centre_image", C.c_int, [_vp, C.POINTER(C.c_int32)]),
     ("pmgb_system_set_accessibility", C.c_int, [_vp, _ip, _ip, C.POINTER(C.c_uint8)]),

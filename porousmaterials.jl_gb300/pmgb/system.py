@@ -275,6 +275,19 @@ class GPUSystem:
         """Spatially ordered evaluation with cutoff culling (pmgb_system_set_cull; default on)."""
         self.ctx.check(self.ctx._lib.pmgb_system_set_cull(self.handle, int(bool(on))))
 
+    def set_image_lists(self, on) -> None:
+        """Image lists in the ordered Widom pass (pmgb_system_set_image_lists): False off, "auto"
+        (the default: where the run's insertions are dense enough to pay), True wherever they apply."""
+        mode = 1 if on == "auto" else (2 if on else 0)
+        self.ctx.check(self.ctx._lib.pmgb_system_set_image_lists(self.handle, mode))
+
+    def image_lists(self, n_insertions: int) -> bool:
+        """Whether a Widom run of n_insertions insertions of this system takes image lists
+        (pmgb_system_image_lists)."""
+        on = C.c_int32(0)
+        self.ctx.check(self.ctx._lib.pmgb_system_image_lists(self.handle, int(n_insertions), C.byref(on)))
+        return bool(on.value)
+
     def set_centre_image(self, on: bool) -> None:
         """Centre-image distances for multi-site guests where the cell allows them
         (pmgb_system_set_centre_image; default on)."""

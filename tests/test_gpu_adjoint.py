@@ -110,6 +110,7 @@ def test_adjoint_without_forces(mol):
     charged = mol == "co2"
     ep = pmgb.setup_Ewald_sum(sc.box, ff.r_cutoff, eps=1e-6) if charged else None
     gs = pmgb.GPUSystem(sc, pmgb.Frac(getattr(synthetic, mol)(), sc.box), ff, ep)
+    gs.set_image_lists(False)  # the forward pass in the adjoint's own distance forms
     npb, seed = 3000, 12
     b1, a1 = gs.widom_adjoint(npb, 5, seed, T, want_energies=True, want_grad=True)  # with forces
     g1 = henry_gradients(gs, b1, a1, T, npb)

@@ -176,23 +176,58 @@ def test_batch_refine_matches_single_system(mixed_systems):
 
 def test_batch_cull_matches_unordered(mixed_systems):
     """Spatial order + cutoff culling: block results equal the unordered run's bit for bit
-    (ragged counts, several unit shapes, with and without the FP64 refinement)."""
+    (ragged counts, several unit shapes, with and without the FP64 refinement).  Per-site
+    distances (image lists off: those change FP32 roundings; tests/test_gpu_image_lists.py)."""
     npb = [1 + 251 * i for i in range(len(mixed_systems))]
     seed = 31
-    plain = BatchScreen(mixed_systems, npb, 5, cull=False)
-    base, _ = plain.run(seed, T)
-    culled = BatchScreen(mixed_systems, npb, 5)
-    for n_ctas, order, mflop in ((0, 0, 0.0), (5, 1, 64.0), (0, 0, 1e6)):
-        culled.configure(n_ctas, order, mflop)
-        got, _ = culled.run(seed, T)
-        np.testing.assert_array_equal(got, base)
-    plain.set_refine(1e-3)
-    culled.set_refine(1e-3)
-    np.testing.assert_array_equal(culled.run(seed, T)[0], plain.run(seed, T)[0])
-    np.testing.assert_array_equal(culled.refined_counts(), plain.refined_counts())
-    culled.set_cull(False)
-    np.testing.assert_array_equal(culled.run(seed, T)[0], plain.run(seed, T)[0])
+    for gs in mixed_systems:
+        gs.set_image_lists(False)
+    try:
+        plain = BatchScreen(mixed_systems, npb, 5, cull=False)
+        base, _ = plain.run(seed, T)
+        culled = BatchScreen(mixed_systems, npb, 5)
+        for n_ctas, order, mflop in ((0, 0, 0.0), (5, 1, 64.0), (0, 0, 1e6)):
+            culled.configure(n_ctas, order, mflop)
+            got, _ = culled.run(seed, T)
+            np.testing.assert_array_equal(got, base)
+        plain.set_refine(1e-3)
+        culled.set_refine(1e-3)
+        np.testing.assert_array_equal(culled.run(seed, T)[0], plain.run(seed, T)[0])
+        np.testing.assert_array_equal(culled.refined_counts(), plain.refined_counts())
+        culled.set_cull(False)
+        np.testing.assert_array_equal(culled.run(seed, T)[0], plain.run(seed, T)[0])
+    finally:
+        for gs in mixed_systems:
+            gs.set_image_lists("auto")
     assert culled.ctx.device_status() == 0
+
+
+def test_batch_image_lists_match_single_system(mixed_systems):
+    """Image lists in the batch (the systems that qualify) over the same insertion order as the
+    single-system runs: equal block results and energies bit for bit, with and without the FP64
+    refinement, ragged counts and several unit shapes."""
+    npb = [1 + 173 * i for i in range(len(mixed_systems))]
+    seed = 57
+    for gs in mixed_systems:
+        gs.set_image_lists(True)  # wherever they apply: these runs are sparse
+    assert all(gs.image_lists(5 * n) for gs, n in zip(mixed_systems, npb))
+    screen = BatchScreen(mixed_systems, npb, 5)
+    try:
+        for tail in (0.0, 1e-3):
+            screen.set_refine(tail)
+            for n_ctas, order, mflop in ((0, 0, 0.0), (5, 1, 64.0)):
+                screen.configure(n_ctas, order, mflop)
+                got, _ = screen.run(seed, T)
+                for s, gs in enumerate(mixed_systems):
+                    gs.set_refine(tail)
+                    ref, _ = gs.widom(npb[s], 5, system_seed(seed, s), T)
+                    np.testing.assert_array_equal(got[s], ref)
+    finally:
+        for gs in mixed_systems:
+            gs.set_refine(0.0)
+            gs.set_image_lists("auto")
+        screen.close()
+    assert mixed_systems[0].ctx.device_status() == 0
 
 
 @pytest.mark.parametrize("unit_mflop", [0.0, 64.0])

@@ -36,6 +36,7 @@ def test_culled_widom_is_bit_identical(case, npb):
     if case == "co2_config4" and npb > 257:
         npb = 4000  # 20,000 framework atoms: keep the unordered reference run short
     gs = _system(make[0](), make[1](), make[2])
+    gs.set_image_lists(False)  # culling of the per-site pass (image lists: tests/test_gpu_image_lists.py)
     gs.set_cull(False)
     b0, u0 = gs.widom(npb, 5, 123, T, want_energies=True)
     gs.set_cull(True)

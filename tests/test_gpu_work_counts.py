@@ -51,6 +51,7 @@ def _pairs_inside(gs, seed, n, r_cut):
 @pytest.mark.parametrize("case", ["config1", "config4"])
 def test_widom_work_counts(case):
     gs = _system(synthetic.config1() if case == "config1" else synthetic.config4(), synthetic.co2())
+    gs.set_image_lists(False)  # the per-site pass (image lists: tests/test_gpu_image_lists.py)
     npb, nb, seed = 200, 5, 31
     n = npb * nb
     c = gs.widom_work_counts(npb, nb, seed)
