@@ -1029,22 +1029,6 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
 #pragma unroll
                 for (int k = 0; k < NS; ++k) ljp2[k] = php2[k] = f2(0.0f);
                 float ljp[NS], php[NS];
-                // terms of four records for site k from their squared distances; the warp's items
-                // are usually spatially close, so the terms are skipped when no lane has the site
-                // inside the cutoff (those terms are exact zeros, so the sums are unchanged)
-                auto terms4 = [&](int k, float2 d01, float2 d23, const int4& r0, const int4& r1, const int4& r2,
-                                  const int4& r3) {
-                    const float dmin = fminf(fminf(d01.x, d01.y), fminf(d23.x, d23.y));
-                    segmin[k] = fminf(segmin[k], dmin);
-                    count_pairs(4, d01.x, d01.y, d23.x, d23.y);
-                    if (__any_sync(0xffffffffu, valid && !blocked && dmin < g2.rcmax2)) {
-                        const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
-                        pair2_energy<CHARGED, COLS>(d01, __int_as_float(r0.w), __int_as_float(r1.w), g2, a12, a6,
-                                                    ljp2[k], php2[k], &i12[k], &i6[k]);
-                        pair2_energy<CHARGED, COLS>(d23, __int_as_float(r2.w), __int_as_float(r3.w), g2, a12, a6,
-                                                    ljp2[k], php2[k], &i12[k], &i6[k]);
-                    }
-                };
                 // groups of four over the near sub-chunks, in the order of one sweep over [j0, j1);
                 // a skipped last sub-chunk takes the remainder with it.  Returns the first record
                 // left (fewer than four).
@@ -1074,12 +1058,29 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                         float2 X01, Y01, Z01, X23, Y23, Z23;
                         com_disp2(r0, r1, cfix[0], cfix[1], cfix[2], g2, X01, Y01, Z01);
                         com_disp2(r2, r3, cfix[0], cfix[1], cfix[2], g2, X23, Y23, Z23);
+                        // every site's distances, one vote for the group, then every site's terms
+                        float2 d01[NS], d23[NS];
+                        float dall = __int_as_float(0x7f800000);
 #pragma unroll
                         for (int k = 0; k < NS; ++k) {
                             const float nx = __uint_as_float(ux[k]), ny = __uint_as_float(uy[k]),
                                         nz = __uint_as_float(uz[k]);
-                            terms4(k, site_r2(X01, Y01, Z01, nx, ny, nz), site_r2(X23, Y23, Z23, nx, ny, nz), r0, r1,
-                                   r2, r3);
+                            d01[k] = site_r2(X01, Y01, Z01, nx, ny, nz);
+                            d23[k] = site_r2(X23, Y23, Z23, nx, ny, nz);
+                            const float dmin = fminf(fminf(d01[k].x, d01[k].y), fminf(d23[k].x, d23[k].y));
+                            segmin[k] = fminf(segmin[k], dmin);
+                            if (k < S.n_sites) dall = fminf(dall, dmin);
+                            count_pairs(4, d01[k].x, d01[k].y, d23[k].x, d23[k].y);
+                        }
+                        if (__any_sync(0xffffffffu, valid && !blocked && dall < g2.rcmax2)) {
+#pragma unroll
+                            for (int k = 0; k < NS; ++k) {
+                                const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
+                                pair2_energy<CHARGED, COLS>(d01[k], __int_as_float(r0.w), __int_as_float(r1.w), g2, a12,
+                                                            a6, ljp2[k], php2[k], &i12[k], &i6[k]);
+                                pair2_energy<CHARGED, COLS>(d23[k], __int_as_float(r2.w), __int_as_float(r3.w), g2, a12,
+                                                            a6, ljp2[k], php2[k], &i12[k], &i6[k]);
+                            }
                         }
                     };
                     int j = sweep(group4c);
@@ -1144,22 +1145,31 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                     // (those terms are exact zeros, so the sums are unchanged)
                     auto group4 = [&](int j) {
                         const int4 r0 = T[j - t0], r1 = T[j + 1 - t0], r2 = T[j + 2 - t0], r3 = T[j + 3 - t0];
+                        // the distances of every site first, one vote for the group, then the terms of
+                        // every site: 2 NS independent chains for the schedulers (the sites of a guest
+                        // are near or far together; a far pair's terms are exact zeros either way)
+                        float2 d01[NS], d23[NS];
+                        float dall = __int_as_float(0x7f800000);
 #pragma unroll
                         for (int k = 0; k < NS; ++k) {
-                            const float2 d01 = pair2_r2<RESID>(r0, r1, ux[k], uy[k], uz[k], g2);
-                            const float2 d23 = pair2_r2<RESID>(r2, r3, ux[k], uy[k], uz[k], g2);
-                            const float dmin = fminf(fminf(d01.x, d01.y), fminf(d23.x, d23.y));
+                            d01[k] = pair2_r2<RESID>(r0, r1, ux[k], uy[k], uz[k], g2);
+                            d23[k] = pair2_r2<RESID>(r2, r3, ux[k], uy[k], uz[k], g2);
+                            const float dmin = fminf(fminf(d01[k].x, d01[k].y), fminf(d23[k].x, d23[k].y));
                             segmin[k] = fminf(segmin[k], dmin);
-                            count_pairs(4, d01.x, d01.y, d23.x, d23.y);
+                            if (k < S.n_sites) dall = fminf(dall, dmin);
+                            count_pairs(4, d01[k].x, d01[k].y, d23[k].x, d23[k].y);
                             if (BOUND)
-                                cgap = fminf(cgap, fminf(fminf(fabsf(d01.x - g2.rc2), fabsf(d01.y - g2.rc2)),
-                                                         fminf(fabsf(d23.x - g2.rc2), fabsf(d23.y - g2.rc2))));
-                            if (__any_sync(0xffffffffu, valid && !blocked && dmin < g2.rcmax2)) {
+                                cgap = fminf(cgap, fminf(fminf(fabsf(d01[k].x - g2.rc2), fabsf(d01[k].y - g2.rc2)),
+                                                         fminf(fabsf(d23[k].x - g2.rc2), fabsf(d23[k].y - g2.rc2))));
+                        }
+                        if (__any_sync(0xffffffffu, valid && !blocked && dall < g2.rcmax2)) {
+#pragma unroll
+                            for (int k = 0; k < NS; ++k) {
                                 const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
-                                pair2_energy<CHARGED, COLS>(d01, __int_as_float(r0.w), __int_as_float(r1.w), g2,
+                                pair2_energy<CHARGED, COLS>(d01[k], __int_as_float(r0.w), __int_as_float(r1.w), g2,
                                                             a12, a6, ljp2[k], php2[k], &i12[k], &i6[k],
                                                             BOUND ? &i24[k] : nullptr);
-                                pair2_energy<CHARGED, COLS>(d23, __int_as_float(r2.w), __int_as_float(r3.w), g2,
+                                pair2_energy<CHARGED, COLS>(d23[k], __int_as_float(r2.w), __int_as_float(r3.w), g2,
                                                             a12, a6, ljp2[k], php2[k], &i12[k], &i6[k],
                                                             BOUND ? &i24[k] : nullptr);
                             }

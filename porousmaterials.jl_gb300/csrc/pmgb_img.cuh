@@ -283,9 +283,12 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
                 for (int i = 0; i < n4; i += 4) {
                     const float4* P0 = list + (i >> 1) * 4;  // pair i/2: A, B, C, D; pair i/2 + 1 follows
                     const float4 A0 = P0[0], B0 = P0[1], A1 = P0[4], B1 = P0[5];
+                    // the distances of every site first, one vote for the group, then the terms of
+                    // every site: 2 NS independent chains (sites of a guest are near or far together)
+                    float2 d01[NS], d23[NS];
+                    float dmin = __int_as_float(0x7f800000);
 #pragma unroll
                     for (int k = 0; k < NS; ++k) {
-                        if (k >= S.n_sites) continue;
                         const float2 sx = f2(nx[k]), sy = f2(ny[k]), sz = f2(nz[k]);
                         const float2 ex0 = __fadd2_rn(make_float2(A0.x, A0.y), sx);
                         const float2 ey0 = __fadd2_rn(make_float2(A0.z, A0.w), sy);
@@ -293,34 +296,53 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
                         const float2 ex1 = __fadd2_rn(make_float2(A1.x, A1.y), sx);
                         const float2 ey1 = __fadd2_rn(make_float2(A1.z, A1.w), sy);
                         const float2 ez1 = __fadd2_rn(make_float2(B1.x, B1.y), sz);
-                        float2 d01 = fma2(ex0, ex0, fma2(ey0, ey0, mul2(ez0, ez0)));
-                        float2 d23 = fma2(ex1, ex1, fma2(ey1, ey1, mul2(ez1, ez1)));
-                        const float dmin = fminf(fminf(d01.x, d01.y), fminf(d23.x, d23.y));
-                        if (__any_sync(full, active && dmin < g2.rcmax2)) {
-                            if (__any_sync(full, active && dmin < kImgClose2)) {
-                                // close pairs: r^2 = |e + delta|^2 with delta = the offsets'
-                                // residuals (|delta| ~ 1e-6 A): add 2 e . delta
-                                const float4 C0 = P0[2], D0 = P0[3], C1 = P0[6], D1 = P0[7];
+                        d01[k] = fma2(ex0, ex0, fma2(ey0, ey0, mul2(ez0, ez0)));
+                        d23[k] = fma2(ex1, ex1, fma2(ey1, ey1, mul2(ez1, ez1)));
+                        if (k < S.n_sites) dmin = fminf(dmin, fminf(fminf(d01[k].x, d01[k].y), fminf(d23[k].x, d23[k].y)));
+                    }
+                    if (__any_sync(full, active && dmin < g2.rcmax2)) {
+                        if (__any_sync(full, active && dmin < kImgClose2)) {
+                            // close pairs: r^2 = |e + delta|^2 with delta = the offsets' residuals
+                            // (|delta| ~ 1e-6 A): add 2 e . delta
+                            const float4 C0 = P0[2], D0 = P0[3], C1 = P0[6], D1 = P0[7];
+#pragma unroll
+                            for (int k = 0; k < NS; ++k) {
+                                const float2 sx = f2(nx[k]), sy = f2(ny[k]), sz = f2(nz[k]);
                                 const float2 lx = f2(site_lo[3 * k + 0]), ly = f2(site_lo[3 * k + 1]),
                                              lz = f2(site_lo[3 * k + 2]);
+                                const float2 ex0 = __fadd2_rn(make_float2(A0.x, A0.y), sx);
+                                const float2 ey0 = __fadd2_rn(make_float2(A0.z, A0.w), sy);
+                                const float2 ez0 = __fadd2_rn(make_float2(B0.x, B0.y), sz);
+                                const float2 ex1 = __fadd2_rn(make_float2(A1.x, A1.y), sx);
+                                const float2 ey1 = __fadd2_rn(make_float2(A1.z, A1.w), sy);
+                                const float2 ez1 = __fadd2_rn(make_float2(B1.x, B1.y), sz);
                                 const float2 dx0 = __fadd2_rn(make_float2(C0.x, C0.y), lx);
                                 const float2 dy0 = __fadd2_rn(make_float2(C0.z, C0.w), ly);
                                 const float2 dz0 = __fadd2_rn(make_float2(D0.x, D0.y), lz);
                                 const float2 dx1 = __fadd2_rn(make_float2(C1.x, C1.y), lx);
                                 const float2 dy1 = __fadd2_rn(make_float2(C1.z, C1.w), ly);
                                 const float2 dz1 = __fadd2_rn(make_float2(D1.x, D1.y), lz);
-                                d01 = fma2(f2(2.0f), fma2(ex0, dx0, fma2(ey0, dy0, mul2(ez0, dz0))), d01);
-                                d23 = fma2(f2(2.0f), fma2(ex1, dx1, fma2(ey1, dy1, mul2(ez1, dz1))), d23);
+                                d01[k] = fma2(f2(2.0f), fma2(ex0, dx0, fma2(ey0, dy0, mul2(ez0, dz0))), d01[k]);
+                                d23[k] = fma2(f2(2.0f), fma2(ex1, dx1, fma2(ey1, dy1, mul2(ez1, dz1))), d23[k]);
                             }
-                            const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
-                            pair2_energy<CHARGED>(d01, B0.z, B0.w, g2, a12, a6, ljp2[k], php2[k]);
-                            pair2_energy<CHARGED>(d23, B1.z, B1.w, g2, a12, a6, ljp2[k], php2[k]);
                         }
-                        segmin[k] = fminf(segmin[k], fminf(fminf(d01.x, d01.y), fminf(d23.x, d23.y)));
+#pragma unroll
+                        for (int k = 0; k < NS; ++k) {
+                            if (k >= S.n_sites) continue;
+                            const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
+                            pair2_energy<CHARGED>(d01[k], B0.z, B0.w, g2, a12, a6, ljp2[k], php2[k]);
+                            pair2_energy<CHARGED>(d23[k], B1.z, B1.w, g2, a12, a6, ljp2[k], php2[k]);
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < NS; ++k) {
+                        if (k >= S.n_sites) continue;
+                        segmin[k] = fminf(segmin[k], fminf(fminf(d01[k].x, d01[k].y), fminf(d23[k].x, d23[k].y)));
                         if (STATS && active) {
-                            st_lj += (d01.x < g2.rc2) + (d01.y < g2.rc2) + (d23.x < g2.rc2) + (d23.y < g2.rc2);
+                            st_lj += (d01[k].x < g2.rc2) + (d01[k].y < g2.rc2) + (d23[k].x < g2.rc2) + (d23[k].y < g2.rc2);
                             if (CHARGED)
-                                st_es += (d01.x < g2.rc2e) + (d01.y < g2.rc2e) + (d23.x < g2.rc2e) + (d23.y < g2.rc2e);
+                                st_es += (d01[k].x < g2.rc2e) + (d01[k].y < g2.rc2e) + (d23[k].x < g2.rc2e) +
+                                         (d23[k].y < g2.rc2e);
                         }
                     }
                     if ((i & 63) == 60 || i + 4 >= n4) {  // compensated fold every 64 images
