@@ -206,10 +206,24 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU legs
+def oracle_module():
+    """The FP64 oracle's Python binding (oracle/oracle.py).  Its folder goes first on the path
+    before the first import: with the repository root alone on the path, `import oracle` would
+    find the oracle/ folder itself as an empty namespace package."""
+    p = str(ROOT / "oracle")
+    if p not in sys.path:
+        sys.path.insert(0, p)
+    mod = sys.modules.get("oracle")
+    if mod is not None and not hasattr(mod, "OracleSystem"):
+        del sys.modules["oracle"]
+    import importlib
+
+    return importlib.import_module("oracle")
+
+
 def oracle_system(sc, mol, ff, ep):
     """The FP64 oracle (the reference's algorithm restated in C) holding a workload's inputs."""
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
+    oracle = oracle_module()
 
     species = list(dict.fromkeys(list(sc.atoms.species) + list(mol.atom_species)))
     sid = {s: i for i, s in enumerate(species)}
@@ -226,7 +240,7 @@ def cpu_rate(sc, mol, ep, budget_s: float, seed: int = 99, nthreads: int = 0, us
     nthreads) on a bounded sample of the workload's insertions (random poses)."""
     import numpy as np
 
-    import oracle
+    oracle = oracle_module()
     from pmgb import synthetic
     from pmgb.molecule import body_offsets
 
@@ -265,7 +279,7 @@ def cpu_legs(sc, mol, ep, ff):
     (the 96^3 Xe grid) and a bounded sample of config4 (direct form)."""
     import numpy as np
 
-    import oracle
+    oracle = oracle_module()
     import pmgb
     from pmgb import synthetic
 

@@ -96,11 +96,12 @@ size_t pmgb_img_smem_bytes() { return kImgSmemBytes; }
 
 bool pmgb_img_supported(int n_sites) { return n_sites == 1 || n_sites == 3; }
 
-// Z-order cells per axis 2^bits: the fewest bits (3 to 6) that leave at most 8 insertions per cell
-// on average (6 bits, 262,144 cells, for runs above ~2.1e6 insertions keep more)
+// Z-order cells per axis 2^bits: the fewest bits (3 to 6) that leave at most 32 insertions per cell
+// on average (a cell of a 1e6-insertion run in a 28,700 A^3 cell is ~0.9 A across; the order within
+// a cell is by index)
 int pmgb_run_order_bits(long long n) {
     int bits = 3;
-    while (bits < 6 && (n >> (3 * bits)) > 8) ++bits;
+    while (bits < 6 && (n >> (3 * bits)) > 32) ++bits;
     return bits;
 }
 

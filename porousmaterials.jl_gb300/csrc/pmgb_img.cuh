@@ -21,16 +21,28 @@ __device__ __forceinline__ int run_cell(unsigned long long seed, unsigned long l
     return code;
 }
 
-// Exclusive scan of n_cells counts by one CTA of 1024 threads: chunks of 1024 consecutive cells
-// (coalesced), each scanned by the CTA and offset by the running total.
+// Exclusive scan of n_cells counts (a multiple of 512) by one CTA of 1024 threads: chunks of
+// 8192 consecutive cells, 8 per thread (two coalesced 16-byte loads), each chunk scanned by the
+// CTA and offset by the running total.
 __device__ __forceinline__ void scan_cells(int* counts, int n_cells) {
     __shared__ int wsum[32];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     int carry = 0;
-    for (int base = 0; base < n_cells; base += 1024) {
-        const int i = base + t;
-        const int v = i < n_cells ? counts[i] : 0;
-        int incl = v;
+    for (int base = 0; base < n_cells; base += 8192) {
+        const int i0 = base + 8 * t;
+        int v[8];
+        if (i0 < n_cells) {
+            const int4 a = *reinterpret_cast<const int4*>(counts + i0);
+            const int4 b = *reinterpret_cast<const int4*>(counts + i0 + 4);
+            v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        } else {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[q] = 0;
+        }
+        int own = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) own += v[q];
+        int incl = own;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const int u = __shfl_up_sync(0xffffffffu, incl, o);
@@ -39,17 +51,23 @@ __device__ __forceinline__ void scan_cells(int* counts, int n_cells) {
         if (lane == 31) wsum[w] = incl;
         __syncthreads();
         if (w == 0) {
-            int s = wsum[lane];
+            int sum = wsum[lane];
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                const int u = __shfl_up_sync(0xffffffffu, s, o);
-                if (lane >= o) s += u;
+                const int u = __shfl_up_sync(0xffffffffu, sum, o);
+                if (lane >= o) sum += u;
             }
-            wsum[lane] = s;  // inclusive over warps
+            wsum[lane] = sum;  // inclusive over warps
         }
         __syncthreads();
-        const int before = (w > 0 ? wsum[w - 1] : 0) + incl - v;
-        if (i < n_cells) counts[i] = carry + before;
+        int run = carry + (w > 0 ? wsum[w - 1] : 0) + incl - own;
+        if (i0 < n_cells) {
+            int4 a, b;
+            a.x = run; run += v[0]; a.y = run; run += v[1]; a.z = run; run += v[2]; a.w = run; run += v[3];
+            b.x = run; run += v[4]; b.y = run; run += v[5]; b.z = run; run += v[6]; b.w = run;
+            *reinterpret_cast<int4*>(counts + i0) = a;
+            *reinterpret_cast<int4*>(counts + i0 + 4) = b;
+        }
         carry += wsum[31];
         __syncthreads();  // wsum is rewritten by the next chunk
     }
