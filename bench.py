@@ -46,14 +46,15 @@ F_DIST, F_LJ_IN, F_ES_IN = 26, 11, 30
 # list building (once per warp and image) and the close-pair residual terms are not counted
 F_DIST_IMG = 8
 REFINE_TAIL = 1e-3
-# DRAM traffic of the config1 pair kernel, from ncu (dram__bytes_read.sum + dram__bytes_write.sum of
-# one launch over 1e5 insertions: 0.59 MB read, 0 written; profiles/pairs_kernel_config1.md),
-# per insertion; a full launch scales with the insertions it processes
-PAIR_DRAM_BYTES_PER_INSERTION = 0.59e6 / 1e5
-# kernels per Widom step: spatial order (count, scan, scatter), pairs, insertion-order partials,
-# block reduction, and the refinement's hist, cut, count, scan, scatter, FP64 energies (thread
-# pass, plan, warp pass), and the store, chunk re-form and block recombination of the results
-LAUNCHES_PER_STEP = 17
+# DRAM traffic of the config1 image-list pair kernel, from ncu (dram bytes of one launch over 5e5
+# insertions: 2.19 MB; profiles/pairs_img_kernel_config1.md), per insertion; a full launch scales
+# with the insertions it processes
+PAIR_DRAM_BYTES_PER_INSERTION = 2.19e6 / 5e5
+# kernels per Widom step: the run's spatial order (count, scan, scatter, per-cell sort), pairs,
+# insertion-order partials, block reduction, and the refinement's hist, cut, count, scan, scatter,
+# FP64 energies (thread pass, plan, warp pass), and the store, chunk re-form and block
+# recombination of the results
+LAUNCHES_PER_STEP = 18
 
 
 ALL_LEGS = ("adjoint", "e2e", "porous", "batched", "config4", "moves", "config2", "cpu")
@@ -73,6 +74,8 @@ def parse():
     p.add_argument("--batch-insertions", type=int, default=20000, help="insertions per (framework, guest)")
     p.add_argument("--c4-insertions", type=int, default=10_000_000, help="insertions of the large-cell leg")
     p.add_argument("--skip-configs", action="store_true", help="omit the large-cell and energy-grid legs")
+    p.add_argument("--image-lists", default="auto", choices=["auto", "on", "off"],
+                   help="image lists in the config1 workload's ordered Widom pass (pmgb_system_set_image_lists)")
     p.add_argument("--legs", default="all",
                    help="comma list of the legs beside the config1 workload to run: " + ",".join(ALL_LEGS) +
                         " (default all; the skip flags remove legs from it)")
@@ -847,6 +850,7 @@ def ours(args, rank, world, local_rank):
     ctx.set_stream(stream.cuda_stream)
     # FP32 pair pass + FP64 refinement of the Boltzmann tail: K_H within 1e-6 of FP64
     system = pmgb.GPUSystem(sc, pmgb.Frac(mol, sc.box), ff, ep, ctx=ctx, refine_tail=REFINE_TAIL)
+    system.set_image_lists({"auto": "auto", "on": True, "off": False}[args.image_lists])
     n_ins = args.insertions
     npb = n_ins // N_BLOCKS
     n_ins = npb * N_BLOCKS
@@ -962,7 +966,20 @@ def ours(args, rank, world, local_rank):
     achieved_every = fpi * n_ins / (kernel_ms * 1e-3) / 1e12
     n_kev = system.info()["n_kvecs_evaluated"]
     work = system.widom_work_counts(npb, N_BLOCKS, 1)   # the insertions of the first timed step
-    fpi_in = counted_flops(work, n_ins, mol.n_charges, n_kev, system.image_lists(n_ins))
+    img = system.image_lists(n_ins)
+    fpi_in = counted_flops(work, n_ins, mol.n_charges, n_kev, img)
+    per_site_eq = None
+    if img:  # the same insertions' counted work in the per-site form, completed in the lists' time
+        system.set_image_lists(False)
+        work_ps = system.widom_work_counts(npb, N_BLOCKS, 1)
+        system.set_image_lists({"auto": "auto", "on": True, "off": False}[args.image_lists])
+        fpi_ps = counted_flops(work_ps, n_ins, mol.n_charges, n_kev)
+        ach_ps = fpi_ps * n_ins / (kernel_ms * 1e-3) / 1e12
+        per_site_eq = {"flops_per_insertion": fpi_ps, "work_counts": work_ps, "achieved": ach_ps,
+                       "frac": ach_ps / fp32_peak if fp32_peak else None,
+                       "meaning": "the per-site pass's counted work for the same insertions (26 flops per "
+                                  "(site, record) distance) over the image-list kernel's time: the rate at which "
+                                  "the per-site form's work is completed, not a rate of executed flops"}
     fpi_est = flops_inside_cutoff(sc, mol, ff, ep, n_kev)
     achieved = fpi_in * n_ins / (kernel_ms * 1e-3) / 1e12
     cpu = None
@@ -1005,16 +1022,15 @@ def ours(args, rank, world, local_rank):
                          "error_vs_fp64_oracle": err1,
                          "fp32_only_insertions_per_s": n_ins / (ms32 * 1e-3),
                          "fp32_only_ms_per_step": ms32,
-                         "fp32_only": "refinement off: the pair kernel keeps the box-matrix residual (the "
-                                      "refined steps drop it, their FP64 pass re-evaluates the insertions "
-                                      "that matter)"},
+                         "fp32_only": "refinement off: the same pass without the FP64 re-evaluation of the "
+                                      "Boltzmann tail"},
            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                         "frac": achieved / fp32_peak if fp32_peak else None,
                         "traffic": PAIR_DRAM_BYTES_PER_INSERTION * n_ins,
-                        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one pair-kernel "
-                                          "launch over 1e5 insertions (0.59 MB), scaled to this launch's insertions "
-                                          "(profiles/pairs_kernel_config1.md); the framework lives in shared "
-                                          "memory and L2, so the kernel is compute-bound",
+                        "traffic_source": "ncu DRAM bytes of one image-list pair-kernel launch over 5e5 insertions "
+                                          "(2.19 MB), scaled to this launch's insertions "
+                                          "(profiles/pairs_img_kernel_config1.md); the framework lives in L2 and "
+                                          "the CTAs' shared-memory lists, so the kernel is compute-bound",
                         "peak_source": "in-run FFMA probe (pmgb_fp32_peak, best of 3); MEASURED_PEAKS.json has no "
                                        "FP32 figure",
                         "peak_clocks": peak_clocks,
@@ -1022,10 +1038,12 @@ def ours(args, rank, world, local_rank):
                         "work_counts": work,
                         "counting": "the work the kernel does, counted by its work-counting pass "
                                     "(pmgb_widom_work_counts) over the first timed step's insertions: 8 flops per "
-                                    "(guest site, list image) distance (3 subtractions and r^2 from the warp's image "
-                                    "list; building the lists, ~60 flops per image and warp, is not counted), 11 "
-                                    "more per LJ and 30 per real-space term inside their cutoffs, 17 per (evaluated "
-                                    "k-vector, guest charge); FMA = 2, MUFU = 1",
+                                    "(guest site, list image) distance (3 subtractions and r^2 from the CTA's image "
+                                    "list; building the lists, once per CTA and record, is not counted) or 26 per "
+                                    "(guest site, record) distance in the per-site form, 11 more per LJ and 30 per "
+                                    "real-space term inside their cutoffs, 17 per (evaluated k-vector, guest "
+                                    "charge); FMA = 2, MUFU = 1",
+                        "per_site_equivalent": per_site_eq,
                         "flops_per_insertion_uniform_estimate": fpi_est,
                         "kvectors_evaluated": system.info()["n_kvecs_evaluated"],
                         "every_pair": {"flops_per_insertion": fpi, "achieved": achieved_every,
@@ -1033,9 +1051,11 @@ def ours(args, rank, world, local_rank):
                                        "convention": "every pair and every k-vector counted: LJ 28, real-space 40, "
                                                      "k-term 17 flops; credits the energy terms culling skips and "
                                                      "the k-vectors whose S(k) vanishes"},
-                        "kernel": "pairs_kernel<3,true,false,false> (CO2, Ewald, forward, no box residual): "
-                                  "CUDA events around each of its launches inside the timed refined steps, "
-                                  "on the launching stream",
+                        "kernel": ("pairs_img_kernel<3,true> (CO2, Ewald, forward, image lists over the run's "
+                                   "order)" if system.image_lists(n_ins) else
+                                   "pairs_kernel<3,true,false,false> (CO2, Ewald, forward, per site, no box residual)")
+                                  + ": CUDA events around each of its launches inside the timed refined steps, on the "
+                                    "launching stream",
                         "kernel_ms_per_launch": kernel_ms, "kernel_share_of_step": kernel_ms * args.steps / ms_total},
            "forward_plus_adjoint": adj,
            "porous_cell": porous,
