@@ -304,7 +304,7 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
                     // the distances of every site first, one vote for the group, then the terms of
                     // every site: 2 NS independent chains (sites of a guest are near or far together)
                     float2 d01[NS], d23[NS];
-                    float dmin = __int_as_float(0x7f800000);
+                    float m01 = __int_as_float(0x7f800000), m23 = m01;
 #pragma unroll
                     for (int k = 0; k < NS; ++k) {
                         const float2 sx = f2(nx[k]), sy = f2(ny[k]), sz = f2(nz[k]);
@@ -316,10 +316,19 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
                         const float2 ez1 = __fadd2_rn(make_float2(B1.x, B1.y), sz);
                         d01[k] = fma2(ex0, ex0, fma2(ey0, ey0, mul2(ez0, ez0)));
                         d23[k] = fma2(ex1, ex1, fma2(ey1, ey1, mul2(ez1, ez1)));
-                        if (k < S.n_sites) dmin = fminf(dmin, fminf(fminf(d01[k].x, d01[k].y), fminf(d23[k].x, d23[k].y)));
+                        if (k < S.n_sites) {
+                            m01 = fminf(m01, fminf(d01[k].x, d01[k].y));
+                            m23 = fminf(m23, fminf(d23[k].x, d23[k].y));
+                        }
                     }
-                    if (__any_sync(full, active && dmin < g2.rcmax2)) {
-                        if (__any_sync(full, active && dmin < kImgClose2)) {
+                    // one vote per pair of images: bits 0, 1 some lane reaches images 0-1, 2-3;
+                    // bits 2, 3 some lane has a pair there within the residuals' radius
+                    const unsigned flags = __reduce_or_sync(
+                        full, active ? (unsigned(m01 < g2.rcmax2) | unsigned(m23 < g2.rcmax2) << 1 |
+                                        unsigned(m01 < kImgClose2) << 2 | unsigned(m23 < kImgClose2) << 3)
+                                     : 0u);
+                    if (flags & 3u) {
+                        if (flags & 12u) {
                             // close pairs: r^2 = |e + delta|^2 with delta = the offsets' residuals
                             // (|delta| ~ 1e-6 A): add 2 e . delta
                             const float4 C0 = P0[2], D0 = P0[3], C1 = P0[6], D1 = P0[7];
@@ -344,12 +353,25 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
                                 d23[k] = fma2(f2(2.0f), fma2(ex1, dx1, fma2(ey1, dy1, mul2(ez1, dz1))), d23[k]);
                             }
                         }
+                        // the terms of the reached pairs (those of the others are exact zeros); both
+                        // pairs together where both are reached, for 2 NS independent chains
+                        if ((flags & 3u) == 3u) {
 #pragma unroll
-                        for (int k = 0; k < NS; ++k) {
-                            if (k >= S.n_sites) continue;
-                            const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
-                            pair2_energy<CHARGED>(d01[k], B0.z, B0.w, g2, a12, a6, ljp2[k], php2[k]);
-                            pair2_energy<CHARGED>(d23[k], B1.z, B1.w, g2, a12, a6, ljp2[k], php2[k]);
+                            for (int k = 0; k < NS; ++k) {
+                                if (k >= S.n_sites) continue;
+                                const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
+                                pair2_energy<CHARGED>(d01[k], B0.z, B0.w, g2, a12, a6, ljp2[k], php2[k]);
+                                pair2_energy<CHARGED>(d23[k], B1.z, B1.w, g2, a12, a6, ljp2[k], php2[k]);
+                            }
+                        } else {
+                            const bool first = flags & 1u;
+                            const float qa = first ? B0.z : B1.z, qb = first ? B0.w : B1.w;
+#pragma unroll
+                            for (int k = 0; k < NS; ++k) {
+                                if (k >= S.n_sites) continue;
+                                const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
+                                pair2_energy<CHARGED>(first ? d01[k] : d23[k], qa, qb, g2, a12, a6, ljp2[k], php2[k]);
+                            }
                         }
                     }
 #pragma unroll
