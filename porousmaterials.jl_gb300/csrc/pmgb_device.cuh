@@ -1029,6 +1029,35 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
 #pragma unroll
                 for (int k = 0; k < NS; ++k) ljp2[k] = php2[k] = f2(0.0f);
                 float ljp[NS], php[NS];
+                // the terms of a group of four records after every site's distances: one vote per pair
+                // of records (bit 0: some lane reaches records 0-1, bit 1: records 2-3; the terms of a
+                // pair no lane reaches are exact zeros); both pairs together where both are reached,
+                // for 2 NS independent chains
+                auto terms_by_pair = [&](float m01, float m23, const float2 (&d01)[NS], const float2 (&d23)[NS],
+                                         const int4& r0, const int4& r1, const int4& r2, const int4& r3) {
+                    const bool act = valid && !blocked;
+                    const unsigned flags = __reduce_or_sync(
+                        0xffffffffu, act ? (unsigned(m01 < g2.rcmax2) | unsigned(m23 < g2.rcmax2) << 1) : 0u);
+                    if (flags == 3u) {
+#pragma unroll
+                        for (int k = 0; k < NS; ++k) {
+                            const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
+                            pair2_energy<CHARGED, COLS>(d01[k], __int_as_float(r0.w), __int_as_float(r1.w), g2, a12, a6,
+                                                        ljp2[k], php2[k], &i12[k], &i6[k], BOUND ? &i24[k] : nullptr);
+                            pair2_energy<CHARGED, COLS>(d23[k], __int_as_float(r2.w), __int_as_float(r3.w), g2, a12, a6,
+                                                        ljp2[k], php2[k], &i12[k], &i6[k], BOUND ? &i24[k] : nullptr);
+                        }
+                    } else if (flags != 0u) {
+                        const bool first = flags == 1u;
+                        const float qa = __int_as_float(first ? r0.w : r2.w), qb = __int_as_float(first ? r1.w : r3.w);
+#pragma unroll
+                        for (int k = 0; k < NS; ++k) {
+                            const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
+                            pair2_energy<CHARGED, COLS>(first ? d01[k] : d23[k], qa, qb, g2, a12, a6, ljp2[k], php2[k],
+                                                        &i12[k], &i6[k], BOUND ? &i24[k] : nullptr);
+                        }
+                    }
+                };
                 // groups of four over the near sub-chunks, in the order of one sweep over [j0, j1);
                 // a skipped last sub-chunk takes the remainder with it.  Returns the first record
                 // left (fewer than four).
@@ -1060,28 +1089,21 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                         com_disp2(r2, r3, cfix[0], cfix[1], cfix[2], g2, X23, Y23, Z23);
                         // every site's distances, one vote for the group, then every site's terms
                         float2 d01[NS], d23[NS];
-                        float dall = __int_as_float(0x7f800000);
+                        float m01 = __int_as_float(0x7f800000), m23 = m01;
 #pragma unroll
                         for (int k = 0; k < NS; ++k) {
                             const float nx = __uint_as_float(ux[k]), ny = __uint_as_float(uy[k]),
                                         nz = __uint_as_float(uz[k]);
                             d01[k] = site_r2(X01, Y01, Z01, nx, ny, nz);
                             d23[k] = site_r2(X23, Y23, Z23, nx, ny, nz);
-                            const float dmin = fminf(fminf(d01[k].x, d01[k].y), fminf(d23[k].x, d23[k].y));
-                            segmin[k] = fminf(segmin[k], dmin);
-                            if (k < S.n_sites) dall = fminf(dall, dmin);
+                            segmin[k] = fminf(segmin[k], fminf(fminf(d01[k].x, d01[k].y), fminf(d23[k].x, d23[k].y)));
+                            if (k < S.n_sites) {
+                                m01 = fminf(m01, fminf(d01[k].x, d01[k].y));
+                                m23 = fminf(m23, fminf(d23[k].x, d23[k].y));
+                            }
                             count_pairs(4, d01[k].x, d01[k].y, d23[k].x, d23[k].y);
                         }
-                        if (__any_sync(0xffffffffu, valid && !blocked && dall < g2.rcmax2)) {
-#pragma unroll
-                            for (int k = 0; k < NS; ++k) {
-                                const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
-                                pair2_energy<CHARGED, COLS>(d01[k], __int_as_float(r0.w), __int_as_float(r1.w), g2, a12,
-                                                            a6, ljp2[k], php2[k], &i12[k], &i6[k]);
-                                pair2_energy<CHARGED, COLS>(d23[k], __int_as_float(r2.w), __int_as_float(r3.w), g2, a12,
-                                                            a6, ljp2[k], php2[k], &i12[k], &i6[k]);
-                            }
-                        }
+                        terms_by_pair(m01, m23, d01, d23, r0, r1, r2, r3);
                     };
                     int j = sweep(group4c);
                     for (; j < j1; ++j) {
@@ -1149,31 +1171,22 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                         // every site: 2 NS independent chains for the schedulers (the sites of a guest
                         // are near or far together; a far pair's terms are exact zeros either way)
                         float2 d01[NS], d23[NS];
-                        float dall = __int_as_float(0x7f800000);
+                        float m01 = __int_as_float(0x7f800000), m23 = m01;
 #pragma unroll
                         for (int k = 0; k < NS; ++k) {
                             d01[k] = pair2_r2<RESID>(r0, r1, ux[k], uy[k], uz[k], g2);
                             d23[k] = pair2_r2<RESID>(r2, r3, ux[k], uy[k], uz[k], g2);
-                            const float dmin = fminf(fminf(d01[k].x, d01[k].y), fminf(d23[k].x, d23[k].y));
-                            segmin[k] = fminf(segmin[k], dmin);
-                            if (k < S.n_sites) dall = fminf(dall, dmin);
+                            segmin[k] = fminf(segmin[k], fminf(fminf(d01[k].x, d01[k].y), fminf(d23[k].x, d23[k].y)));
+                            if (k < S.n_sites) {
+                                m01 = fminf(m01, fminf(d01[k].x, d01[k].y));
+                                m23 = fminf(m23, fminf(d23[k].x, d23[k].y));
+                            }
                             count_pairs(4, d01[k].x, d01[k].y, d23[k].x, d23[k].y);
                             if (BOUND)
                                 cgap = fminf(cgap, fminf(fminf(fabsf(d01[k].x - g2.rc2), fabsf(d01[k].y - g2.rc2)),
                                                          fminf(fabsf(d23[k].x - g2.rc2), fabsf(d23[k].y - g2.rc2))));
                         }
-                        if (__any_sync(0xffffffffu, valid && !blocked && dall < g2.rcmax2)) {
-#pragma unroll
-                            for (int k = 0; k < NS; ++k) {
-                                const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
-                                pair2_energy<CHARGED, COLS>(d01[k], __int_as_float(r0.w), __int_as_float(r1.w), g2,
-                                                            a12, a6, ljp2[k], php2[k], &i12[k], &i6[k],
-                                                            BOUND ? &i24[k] : nullptr);
-                                pair2_energy<CHARGED, COLS>(d23[k], __int_as_float(r2.w), __int_as_float(r3.w), g2,
-                                                            a12, a6, ljp2[k], php2[k], &i12[k], &i6[k],
-                                                            BOUND ? &i24[k] : nullptr);
-                            }
-                        }
+                        terms_by_pair(m01, m23, d01, d23, r0, r1, r2, r3);
                     };
                     int j = j0;
                     if (near_sub == (1u << n_sub) - 1u) {
