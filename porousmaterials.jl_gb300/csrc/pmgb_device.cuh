@@ -1036,8 +1036,11 @@ __device__ __forceinline__ bool run_unit(const SysDev& S, const UnitIO& io, int4
                 auto terms_by_pair = [&](float m01, float m23, const float2 (&d01)[NS], const float2 (&d23)[NS],
                                          const int4& r0, const int4& r1, const int4& r2, const int4& r3) {
                     const bool act = valid && !blocked;
-                    const unsigned flags = __reduce_or_sync(
-                        0xffffffffu, act ? (unsigned(m01 < g2.rcmax2) | unsigned(m23 < g2.rcmax2) << 1) : 0u);
+                    // (uncharged: the LJ terms are cheap, one vote for the group costs less)
+                    const unsigned flags =
+                        CHARGED ? __reduce_or_sync(0xffffffffu,
+                                                   act ? (unsigned(m01 < g2.rcmax2) | unsigned(m23 < g2.rcmax2) << 1) : 0u)
+                                : (__any_sync(0xffffffffu, act && fminf(m01, m23) < g2.rcmax2) ? 3u : 0u);
                     if (flags == 3u) {
 #pragma unroll
                         for (int k = 0; k < NS; ++k) {

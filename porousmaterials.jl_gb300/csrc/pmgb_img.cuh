@@ -323,10 +323,13 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
                     }
                     // one vote per pair of images: bits 0, 1 some lane reaches images 0-1, 2-3;
                     // bits 2, 3 some lane has a pair there within the residuals' radius
+                    // (uncharged: the LJ terms are cheap, one vote for the group costs less)
+                    const float mg = fminf(m01, m23);
                     const unsigned flags = __reduce_or_sync(
-                        full, active ? (unsigned(m01 < g2.rcmax2) | unsigned(m23 < g2.rcmax2) << 1 |
-                                        unsigned(m01 < kImgClose2) << 2 | unsigned(m23 < kImgClose2) << 3)
-                                     : 0u);
+                        full, !active ? 0u
+                              : CHARGED ? (unsigned(m01 < g2.rcmax2) | unsigned(m23 < g2.rcmax2) << 1 |
+                                           unsigned(m01 < kImgClose2) << 2 | unsigned(m23 < kImgClose2) << 3)
+                                        : (unsigned(mg < g2.rcmax2) * 3u | unsigned(mg < kImgClose2) * 12u));
                     if (flags & 3u) {
                         if (flags & 12u) {
                             // close pairs: r^2 = |e + delta|^2 with delta = the offsets' residuals
