@@ -8,16 +8,38 @@ namespace {
 constexpr int kImgWarps = PMGB_THREADS / 32;
 constexpr float kFarAway = 1.0e15f;               // padding image: r^2 ~ 1e30, beyond every cutoff
 
-// Z-order cell (2^bits per axis) of Widom insertion idx: the top bits of its centre of mass (the
-// first Philox draw of make_pose), interleaved; the key of the spatial order over a whole run
+// Hilbert-curve cell (2^bits per axis) of Widom insertion idx: the key of the spatial order over a
+// whole run.  The cell holds the insertion's centre of mass (the top bits of the first Philox draw
+// of make_pose).  Consecutive cells along a Hilbert curve share a face, so a run of consecutive
+// insertions (a CTA's 256) stays compact everywhere; along a Z-order curve it can straddle a jump
+// across the cell, and the CTA's list then grows several-fold.  Index from J. Skilling,
+// "Programming the Hilbert curve", AIP Conf. Proc. 707 (2004): the axes are turned into the
+// transposed index (undo excess work, Gray encode), whose bits are then interleaved.
 __device__ __forceinline__ int run_cell(unsigned long long seed, unsigned long long idx, int bits) {
     const uint2 key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
     const uint4 a = philox4x32_10(make_uint4(static_cast<uint32_t>(idx), static_cast<uint32_t>(idx >> 32), 0u, 0u), key);
-    const uint32_t cx = a.x >> (32 - bits), cy = a.y >> (32 - bits), cz = a.z >> (32 - bits);
+    uint32_t x[3] = {a.x >> (32 - bits), a.y >> (32 - bits), a.z >> (32 - bits)};
+    for (uint32_t q = 1u << (bits - 1); q > 1u; q >>= 1) {
+        const uint32_t p = q - 1u;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (x[i] & q) {
+                x[0] ^= p;  // invert the low bits of axis 0
+            } else {
+                const uint32_t t = (x[0] ^ x[i]) & p;  // exchange the low bits of axes 0 and i
+                x[0] ^= t;
+                x[i] ^= t;
+            }
+        }
+    }
+    x[1] ^= x[0];
+    x[2] ^= x[1];
+    uint32_t t = 0;
+    for (uint32_t q = 1u << (bits - 1); q > 1u; q >>= 1)
+        if (x[2] & q) t ^= q - 1u;
     int code = 0;
-    for (int b = 0; b < bits; ++b)
-        code |= static_cast<int>(((cx >> b) & 1u) << (3 * b) | ((cy >> b) & 1u) << (3 * b + 1) |
-                                 ((cz >> b) & 1u) << (3 * b + 2));
+    for (int b = bits - 1; b >= 0; --b)
+        code = code << 3 | static_cast<int>(((x[0] ^ t) >> b & 1u) << 2 | ((x[1] ^ t) >> b & 1u) << 1 | ((x[2] ^ t) >> b & 1u));
     return code;
 }
 
@@ -354,6 +376,10 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
                                 const float2 dz1 = __fadd2_rn(make_float2(D1.x, D1.y), lz);
                                 d01[k] = fma2(f2(2.0f), fma2(ex0, dx0, fma2(ey0, dy0, mul2(ez0, dz0))), d01[k]);
                                 d23[k] = fma2(f2(2.0f), fma2(ex1, dx1, fma2(ey1, dy1, mul2(ez1, dz1))), d23[k]);
+                                // overlaps (r^2 < R^2_overlap = 0.1 A^2, far inside the close radius)
+                                // can only occur in a group that raised the close vote
+                                if (k < S.n_sites)
+                                    segmin[k] = fminf(segmin[k], fminf(fminf(d01[k].x, d01[k].y), fminf(d23[k].x, d23[k].y)));
                             }
                         }
                         // the terms of the reached pairs (those of the others are exact zeros); both
@@ -380,7 +406,6 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
 #pragma unroll
                     for (int k = 0; k < NS; ++k) {
                         if (k >= S.n_sites) continue;
-                        segmin[k] = fminf(segmin[k], fminf(fminf(d01[k].x, d01[k].y), fminf(d23[k].x, d23[k].y)));
                         if (STATS && active) {
                             st_lj += (d01[k].x < g2.rc2) + (d01[k].y < g2.rc2) + (d23[k].x < g2.rc2) + (d23[k].y < g2.rc2);
                             if (CHARGED)
