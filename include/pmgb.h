@@ -222,9 +222,9 @@ int pmgb_system_set_accessibility(pmgb_system* sys, const int32_t n_pts[3], cons
                                   const uint8_t* data);
 
 /* Spatially ordered evaluation (default on) for pmgb_widom / pmgb_widom_device and the energy
- * grid: insertions of each block are processed in Z-order of their centre of mass (grid points
- * in 4 x 4 x 2 bricks), and a warp skips the pair terms of framework records beyond the cutoff
- * of all its items.  The skipped terms are exact zeros and the block sums are formed in
+ * grid: insertions of each block are processed in Hilbert-curve order of their centre of mass
+ * (grid points in 4 x 4 x 2 bricks), and a warp skips the pair terms of framework records
+ * beyond the cutoff of all its items.  The skipped terms are exact zeros and the block sums are formed in
  * insertion order, so results are bit-identical with it on or off.  No reference counterpart. */
 int pmgb_system_set_cull(pmgb_system* sys, int32_t on);
 
@@ -399,8 +399,8 @@ int pmgb_batch_tune(pmgb_batch* batch, uint64_t seed, double temperature, int32_
 int pmgb_batch_set_refine(pmgb_batch* batch, double tail_fraction);
 
 /* Spatially ordered processing with cutoff culling, as pmgb_system_set_cull (on by default):
- * each (system, block)'s insertions are sorted into 16^3 Z-ordered cells of the unit cell, and
- * block results are formed from the per-insertion energies in insertion order, so they equal
+ * each (system, block)'s insertions are sorted into 16^3 cells of the unit cell, ordered along a
+ * Hilbert curve, and block results are formed from the per-insertion energies in insertion order, so they equal
  * those of an unordered run bit for bit.  Allocates scratch on first use and re-captures. */
 int pmgb_batch_set_cull(pmgb_batch* batch, int32_t on);
 

@@ -280,17 +280,12 @@ __global__ void batch_reduce_kernel(const BatchSystem* __restrict__ systems, int
 constexpr int kBatchOrderBits = 4;                           // 16 cells per axis
 constexpr int kBatchOrderCells = 1 << (3 * kBatchOrderBits);  // 4096
 
+// Hilbert-curve cell of insertion idx (the top 4 bits of each centre-of-mass coordinate)
 __device__ __forceinline__ int batch_cell(unsigned long long seed, unsigned long long idx) {
     const uint2 key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
     const uint4 a = philox4x32_10(make_uint4(static_cast<uint32_t>(idx), static_cast<uint32_t>(idx >> 32), 0u, 0u), key);
-    const uint32_t cx = a.x >> (32 - kBatchOrderBits), cy = a.y >> (32 - kBatchOrderBits),
-                   cz = a.z >> (32 - kBatchOrderBits);
-    int code = 0;
-#pragma unroll
-    for (int bit = 0; bit < kBatchOrderBits; ++bit)
-        code |= static_cast<int>(((cx >> bit) & 1u) << (3 * bit) | ((cy >> bit) & 1u) << (3 * bit + 1) |
-                                 ((cz >> bit) & 1u) << (3 * bit + 2));
-    return code;
+    return hilbert_cell(a.x >> (32 - kBatchOrderBits), a.y >> (32 - kBatchOrderBits), a.z >> (32 - kBatchOrderBits),
+                        kBatchOrderBits);
 }
 
 struct ChunkRef {

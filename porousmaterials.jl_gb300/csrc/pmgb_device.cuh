@@ -107,6 +107,38 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
 }
 __device__ __forceinline__ float u24(uint32_t x) { return static_cast<float>(x >> 8) * 5.9604644775390625e-08f; }
 
+// Index of cell (x, y, z) (2^bits per axis) along a Hilbert curve: the key of the spatial orders
+// of Widom runs.  Consecutive cells along the curve share a face, so a run of consecutive
+// insertions (a warp's 32, a CTA's 256) stays compact everywhere; along a Z-order curve it can
+// straddle a jump across the cell.  J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc.
+// 707 (2004): the axes are turned into the transposed index (undo excess work, Gray encode),
+// whose bits are then interleaved.
+__device__ __forceinline__ int hilbert_cell(uint32_t cx, uint32_t cy, uint32_t cz, int bits) {
+    uint32_t x[3] = {cx, cy, cz};
+    for (uint32_t q = 1u << (bits - 1); q > 1u; q >>= 1) {
+        const uint32_t p = q - 1u;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (x[i] & q) {
+                x[0] ^= p;  // invert the low bits of axis 0
+            } else {
+                const uint32_t t = (x[0] ^ x[i]) & p;  // exchange the low bits of axes 0 and i
+                x[0] ^= t;
+                x[i] ^= t;
+            }
+        }
+    }
+    x[1] ^= x[0];
+    x[2] ^= x[1];
+    uint32_t t = 0;
+    for (uint32_t q = 1u << (bits - 1); q > 1u; q >>= 1)
+        if (x[2] & q) t ^= q - 1u;
+    int code = 0;
+    for (int b = bits - 1; b >= 0; --b)
+        code = code << 3 | static_cast<int>(((x[0] ^ t) >> b & 1u) << 2 | ((x[1] ^ t) >> b & 1u) << 1 | ((x[2] ^ t) >> b & 1u));
+    return code;
+}
+
 // Pose of Widom insertion `idx`: centre of mass uniform in the supercell's
 // fractional cube (henry.jl:214) and a uniform rotation by Arvo's method
 // (molecule.jl:233-244): M = -(I - 2 v v^T) Rz(2 pi u1), v from (u2, u3).

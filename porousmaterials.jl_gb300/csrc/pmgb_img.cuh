@@ -10,37 +10,11 @@ constexpr float kFarAway = 1.0e15f;               // padding image: r^2 ~ 1e30, 
 
 // Hilbert-curve cell (2^bits per axis) of Widom insertion idx: the key of the spatial order over a
 // whole run.  The cell holds the insertion's centre of mass (the top bits of the first Philox draw
-// of make_pose).  Consecutive cells along a Hilbert curve share a face, so a run of consecutive
-// insertions (a CTA's 256) stays compact everywhere; along a Z-order curve it can straddle a jump
-// across the cell, and the CTA's list then grows several-fold.  Index from J. Skilling,
-// "Programming the Hilbert curve", AIP Conf. Proc. 707 (2004): the axes are turned into the
-// transposed index (undo excess work, Gray encode), whose bits are then interleaved.
+// of make_pose); along the curve a CTA's 256 insertions stay compact, and so does its list.
 __device__ __forceinline__ int run_cell(unsigned long long seed, unsigned long long idx, int bits) {
     const uint2 key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
     const uint4 a = philox4x32_10(make_uint4(static_cast<uint32_t>(idx), static_cast<uint32_t>(idx >> 32), 0u, 0u), key);
-    uint32_t x[3] = {a.x >> (32 - bits), a.y >> (32 - bits), a.z >> (32 - bits)};
-    for (uint32_t q = 1u << (bits - 1); q > 1u; q >>= 1) {
-        const uint32_t p = q - 1u;
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            if (x[i] & q) {
-                x[0] ^= p;  // invert the low bits of axis 0
-            } else {
-                const uint32_t t = (x[0] ^ x[i]) & p;  // exchange the low bits of axes 0 and i
-                x[0] ^= t;
-                x[i] ^= t;
-            }
-        }
-    }
-    x[1] ^= x[0];
-    x[2] ^= x[1];
-    uint32_t t = 0;
-    for (uint32_t q = 1u << (bits - 1); q > 1u; q >>= 1)
-        if (x[2] & q) t ^= q - 1u;
-    int code = 0;
-    for (int b = bits - 1; b >= 0; --b)
-        code = code << 3 | static_cast<int>(((x[0] ^ t) >> b & 1u) << 2 | ((x[1] ^ t) >> b & 1u) << 1 | ((x[2] ^ t) >> b & 1u));
-    return code;
+    return hilbert_cell(a.x >> (32 - bits), a.y >> (32 - bits), a.z >> (32 - bits), bits);
 }
 
 // Exclusive scan of n_cells counts (a multiple of 512) by one CTA of 1024 threads: chunks of

@@ -190,20 +190,14 @@ cudaError_t launch_latency_ns(const LaunchArgs& a, int n_ctas, cudaStream_t st) 
 
 // ---- spatial processing order of a Widom run ----------------------------------------
 constexpr int kOrderBits = 5;                       // 32 cells per axis
-constexpr int kOrderCells = 1 << (3 * kOrderBits);  // 32768 Z-order cells
+constexpr int kOrderCells = 1 << (3 * kOrderBits);  // 32768 cells
 
-// Z-order cell of insertion idx: the top 5 bits of each 24-bit centre-of-mass coordinate
-// (the first Philox draw of make_pose), bits interleaved
+// Hilbert-curve cell of insertion idx: the top 5 bits of each coordinate of its centre of mass
+// (the first Philox draw of make_pose)
 __device__ __forceinline__ int widom_cell(unsigned long long seed, unsigned long long idx) {
     const uint2 key = make_uint2(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
     const uint4 a = philox4x32_10(make_uint4(static_cast<uint32_t>(idx), static_cast<uint32_t>(idx >> 32), 0u, 0u), key);
-    const uint32_t cx = a.x >> (32 - kOrderBits), cy = a.y >> (32 - kOrderBits), cz = a.z >> (32 - kOrderBits);
-    int code = 0;
-#pragma unroll
-    for (int b = 0; b < kOrderBits; ++b)
-        code |= static_cast<int>(((cx >> b) & 1u) << (3 * b) | ((cy >> b) & 1u) << (3 * b + 1) |
-                                 ((cz >> b) & 1u) << (3 * b + 2));
-    return code;
+    return hilbert_cell(a.x >> (32 - kOrderBits), a.y >> (32 - kOrderBits), a.z >> (32 - kOrderBits), kOrderBits);
 }
 
 __global__ void order_count_kernel(unsigned long long seed, long long n_per_block, long long n, int* counts) {

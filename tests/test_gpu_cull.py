@@ -1,6 +1,6 @@
 """Spatially ordered evaluation with cutoff culling (pmgb_system_set_cull).
 
-The ordered path sorts each block's insertions by the Z-order cell of their centre of mass,
+The ordered path sorts each block's insertions by the Hilbert-curve cell of their centre of mass,
 lets a warp skip framework records beyond the cutoff of all its items (whole chunks of records
 by their bounding boxes in large cells, groups of four after their distances otherwise), and
 forms the block sums in insertion order.  Skipped terms are exact zeros, so every per-insertion energy and
