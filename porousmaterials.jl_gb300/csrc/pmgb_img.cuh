@@ -270,11 +270,10 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
 
         for (int sg = 0; sg < S.n_seg; ++sg) {
             const SegDesc dsc = S.seg[sg];
-            float r2o[NS], segmin[NS], lj12[NS], lj6[NS];
+            float segmin[NS], lj12[NS], lj6[NS];
 #pragma unroll
             for (int k = 0; k < NS; ++k) {
                 const SitePar p = S.segpar[sg * PMGB_MAX_SITES + k];
-                r2o[k] = p.r2ovl;
                 lj12[k] = p.lj12;
                 lj6[k] = p.lj6;
                 segmin[k] = __int_as_float(0x7f800000);
@@ -357,11 +356,12 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
                             }
                         }
                         // the terms of the reached pairs (those of the others are exact zeros); both
-                        // pairs together where both are reached, for 2 NS independent chains
+                        // pairs together where both are reached, for 2 NS independent chains.  Every
+                        // one of the NS sites, with no branch between them: the terms of a padding
+                        // site (k >= n_sites) go to sums that are never read
                         if ((flags & 3u) == 3u) {
 #pragma unroll
                             for (int k = 0; k < NS; ++k) {
-                                if (k >= S.n_sites) continue;
                                 const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
                                 pair2_energy<CHARGED>(d01[k], B0.z, B0.w, g2, a12, a6, ljp2[k], php2[k]);
                                 pair2_energy<CHARGED>(d23[k], B1.z, B1.w, g2, a12, a6, ljp2[k], php2[k]);
@@ -371,7 +371,6 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
                             const float qa = first ? B0.z : B1.z, qb = first ? B0.w : B1.w;
 #pragma unroll
                             for (int k = 0; k < NS; ++k) {
-                                if (k >= S.n_sites) continue;
                                 const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
                                 pair2_energy<CHARGED>(first ? d01[k] : d23[k], qa, qb, g2, a12, a6, ljp2[k], php2[k]);
                             }
@@ -470,7 +469,8 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
             }
             if (n > 0) flush();
 #pragma unroll
-            for (int k = 0; k < NS; ++k) ovl = ovl || (k < S.n_sites && segmin[k] < r2o[k]);
+            for (int k = 0; k < NS; ++k)  // the overlap radii read again: no registers held over the loop
+                ovl = ovl || (k < S.n_sites && segmin[k] < __ldg(&S.segpar[sg * PMGB_MAX_SITES + k].r2ovl));
         }
     }
     if (STATS) {
