@@ -45,6 +45,11 @@ F_DIST, F_LJ_IN, F_ES_IN = 26, 11, 30
 # with image lists a distance is an offset from the warp's list: 3 subtractions and r^2 (5); the
 # list building (once per warp and image) and the close-pair residual terms are not counted
 F_DIST_IMG = 8
+# the reciprocal-space loop as the kernels execute it, per evaluated k-vector and guest: 16 flops
+# (site 0's phase step and the structure-factor product) and 12 per further guest charge (its
+# phase-difference step and the charge sum); 21 in all for mirror-image sites (CO2,
+# pmgb_system_kspace_mirror), which step one phase difference and take a real charge sum
+F_KROW, F_KROW_SITE, F_KROW_MIRROR = 16, 12, 21
 REFINE_TAIL = 1e-3
 # DRAM traffic of the config1 image-list pair kernel, from ncu (dram bytes of one launch over 5e5
 # insertions: 2.19 MB; profiles/pairs_img_kernel_config1.md), per insertion; a full launch scales
@@ -119,14 +124,16 @@ def flops_per_insertion(sc, mol, ep):
     return f
 
 
-def counted_flops(counts: dict, n_items: int, n_q_sites: int = 0, n_kvecs: int = 0, image_lists: bool = False) -> float:
+def counted_flops(counts: dict, n_items: int, n_q_sites: int = 0, n_kvecs: int = 0, image_lists: bool = False,
+                  mirror: bool = False) -> float:
     """Algorithmic FP32 flops per item of the work a pass did (pmgb_*_work_counts): 26 per
     (guest site, record) distance evaluated (8 per (guest site, list image) distance with image
-    lists), 11 more per LJ term and 30 per real-space term inside their cutoffs, 17 per (evaluated
-    k-vector, guest charge)."""
+    lists), 11 more per LJ term and 30 per real-space term inside their cutoffs; per evaluated
+    k-vector 16 + 12 (n_q_sites - 1), or 21 with mirror-image sites."""
     fd = F_DIST_IMG if image_lists else F_DIST
+    fk = 0 if n_q_sites == 0 else (F_KROW_MIRROR if mirror else F_KROW + F_KROW_SITE * (n_q_sites - 1))
     return (fd * counts["distances"] + F_LJ_IN * counts["lj_terms"] + F_ES_IN * counts["es_terms"]) / n_items + \
-        F_K * n_q_sites * n_kvecs
+        fk * n_kvecs
 
 
 def flops_inside_cutoff(sc, mol, ff, ep, n_kvecs=None):
@@ -485,7 +492,8 @@ def batched_leg(args, ctx, stream, peak=None):
         c = gs.widom_work_counts(npb, N_BLOCKS, system_seed(100, s_))
         nq = int((gs.site_charge >= 0).sum()) if gs.charged else 0
         nk = gs.info()["n_kvecs_evaluated"] if gs.charged else 0
-        flops += counted_flops(c, npb * N_BLOCKS, nq, nk, gs.image_lists(npb * N_BLOCKS)) * npb * N_BLOCKS
+        flops += counted_flops(c, npb * N_BLOCKS, nq, nk, gs.image_lists(npb * N_BLOCKS),
+                               gs.info()["kspace_mirror"]) * npb * N_BLOCKS
     tf = flops / (ms_fp32 * 1e-3) / 1e12
     out["roofline"] = {"bound": "fp32", "achieved": tf, "unit": "TFLOP/s", "frac": tf / peak if peak else None,
                        "flops_per_run": flops, "fp32_pass_ms": ms_fp32,
@@ -493,8 +501,9 @@ def batched_leg(args, ctx, stream, peak=None):
                                  "batch kernel, partials and per-system reduction), CUDA events around the graph "
                                  "replay",
                        "counting": "pmgb_widom_work_counts of each system over its insertions of one run (26 / 11 / "
-                                   "30 / 17 flops per distance, LJ term, real-space term, k-term; 8 per distance "
-                                   "from an image list, the lists' building not counted)"}
+                                   "30 flops per distance, LJ term, real-space term; 8 per distance from an image "
+                                   "list, the lists' building not counted; per evaluated k-vector 16 + 12 per "
+                                   "further guest charge, 21 with mirror-image sites)"}
     assert ctx.device_status() == 0
     out["refined_fraction"] = out["forward_plus_adjoint"]["refined_fraction"]
     out.update({"systems": len(systems), "frameworks": len(fws), "guests": ["CH4", "CO2"],
@@ -699,7 +708,8 @@ def config4_leg(args, ctx, ff, mol, timed, peak):
     err4 = widom_error(gs, ff, 4000, 44)
     fpi = flops_per_insertion(sc, mol, ep)
     work4 = gs.widom_work_counts(npb, N_BLOCKS, 42)   # the FP32-only run's insertions
-    fpc = counted_flops(work4, n, mol.n_charges, gs.info()["n_kvecs_evaluated"], gs.image_lists(n))
+    fpc = counted_flops(work4, n, mol.n_charges, gs.info()["n_kvecs_evaluated"], gs.image_lists(n),
+                        gs.info()["kspace_mirror"])
     tf4 = fpc * n / (ms32 * 1e-3) / 1e12
     return {
         "workload": "CO2 in a 20,000-atom 52x52x52 A cell, Ewald 1e-6", "framework_sites": sc.atoms.n,
@@ -712,8 +722,8 @@ def config4_leg(args, ctx, ff, mol, timed, peak):
                      "kernel": "the FP32-only Widom pass (image-list pair kernel + partials), CUDA events",
                      "counting": "counted by pmgb_widom_work_counts over the same insertions: distances "
                                  "evaluated (8 flops each from an image list, the lists' building not counted), "
-                                 "LJ and real-space terms inside their cutoffs, k-terms of the evaluated "
-                                 "k-vectors (11 / 30 / 17 flops)"},
+                                 "LJ and real-space terms inside their cutoffs (11 / 30 flops), the evaluated "
+                                 "k-vectors (21 flops each: CO2's mirror-image sites)"},
         "every_pair_flops_per_insertion": fpi,
         "every_pair_tflops": fpi * n / (ms32 * 1e-3) / 1e12,
         "note": "every_pair_tflops counts every pair and k-vector; in this 52 A cell the kernel skips whole "
@@ -967,13 +977,14 @@ def ours(args, rank, world, local_rank):
     n_kev = system.info()["n_kvecs_evaluated"]
     work = system.widom_work_counts(npb, N_BLOCKS, 1)   # the insertions of the first timed step
     img = system.image_lists(n_ins)
-    fpi_in = counted_flops(work, n_ins, mol.n_charges, n_kev, img)
+    mirror = system.info()["kspace_mirror"]
+    fpi_in = counted_flops(work, n_ins, mol.n_charges, n_kev, img, mirror)
     per_site_eq = None
     if img:  # the same insertions' counted work in the per-site form, completed in the lists' time
         system.set_image_lists(False)
         work_ps = system.widom_work_counts(npb, N_BLOCKS, 1)
         system.set_image_lists({"auto": "auto", "on": True, "off": False}[args.image_lists])
-        fpi_ps = counted_flops(work_ps, n_ins, mol.n_charges, n_kev)
+        fpi_ps = counted_flops(work_ps, n_ins, mol.n_charges, n_kev, False, mirror)
         ach_ps = fpi_ps * n_ins / (kernel_ms * 1e-3) / 1e12
         per_site_eq = {"flops_per_insertion": fpi_ps, "work_counts": work_ps, "achieved": ach_ps,
                        "frac": ach_ps / fp32_peak if fp32_peak else None,
@@ -1041,8 +1052,9 @@ def ours(args, rank, world, local_rank):
                                     "(guest site, list image) distance (3 subtractions and r^2 from the CTA's image "
                                     "list; building the lists, once per CTA and record, is not counted) or 26 per "
                                     "(guest site, record) distance in the per-site form, 11 more per LJ and 30 per "
-                                    "real-space term inside their cutoffs, 17 per (evaluated k-vector, guest "
-                                    "charge); FMA = 2, MUFU = 1",
+                                    "real-space term inside their cutoffs; per evaluated k-vector the loop as "
+                                    "executed: 21 for CO2's mirror-image sites (16 + 12 per further guest charge "
+                                    "in the general loop); FMA = 2, MUFU = 1",
                         "per_site_equivalent": per_site_eq,
                         "flops_per_insertion_uniform_estimate": fpi_est,
                         "kvectors_evaluated": system.info()["n_kvecs_evaluated"],

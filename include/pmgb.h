@@ -258,6 +258,13 @@ int pmgb_system_image_lists(const pmgb_system* sys, int64_t n_insertions, int32_
  * guest with several sites, and every width wide enough for the current cutoffs), else 0. */
 int pmgb_system_centre_image(const pmgb_system* sys, int32_t* on_out);
 
+/* *on_out = 1 when the system's guest has three sites with site 0 at the centre of mass and
+ * sites 1 and 2 mirror images through it with equal charges (CO2 as the reference's data files
+ * give it): the reciprocal-space sums of its forward passes then carry the phase factors of
+ * site 1 alone, e^{-ik.d_2} = conj(e^{-ik.d_1}).  Else 0.  Results agree with the general form to
+ * FP32 rounding; the FP64 refinement does not use the shortcut. */
+int pmgb_system_kspace_mirror(const pmgb_system* sys, int32_t* on_out);
+
 /* Number of items the system's last double-float pass re-evaluated (synchronises): insertions of
  * the last refined Widom run, configurations of the last exact pmgb_energies call, or points of
  * the last exact energy grid. */

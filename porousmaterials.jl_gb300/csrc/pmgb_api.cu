@@ -982,6 +982,15 @@ static int system_build_host(const CreateIn& in, pmgb_system* s, SysHost& h, Err
                                               D.body64[k][2] * D.body64[k][2]));
         D.com_reach = reach > 0.0 ? static_cast<float>(reach * (1.0 + 1e-6) + 1e-4) : 0.0f;
     }
+    // mirror sites: the offsets are formed by sums of exactly negated products, and the poses
+    // round them to fixed point by an odd function, so site 2's offset from site 0 is exactly
+    // minus site 1's in every pose
+    D.k_mirror = 0;
+    if (ns == 3 && D.q[1] == D.q[2]) {
+        bool m = true;
+        for (int d = 0; d < 3; ++d) m = m && D.body64[0][d] == 0.0 && D.body64[1][d] == -D.body64[2][d];
+        D.k_mirror = m ? 1 : 0;
+    }
     update_centre_image(s);
     D.n_krow = 0;
     D.n_k = 0;
@@ -2133,6 +2142,12 @@ extern "C" int pmgb_system_image_lists(const pmgb_system* s, int64_t n_insertion
 extern "C" int pmgb_system_centre_image(const pmgb_system* s, int32_t* on_out) {
     if (!s || !on_out) return PMGB_ERR_INVALID_ARGUMENT;
     *on_out = (s->dev.com_axis >= -1 && s->dev.n_sites > 1) ? 1 : 0;
+    return PMGB_OK;
+}
+
+extern "C" int pmgb_system_kspace_mirror(const pmgb_system* s, int32_t* on_out) {
+    if (!s || !on_out) return PMGB_ERR_INVALID_ARGUMENT;
+    *on_out = s->dev.k_mirror;
     return PMGB_OK;
 }
 

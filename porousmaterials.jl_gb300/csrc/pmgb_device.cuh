@@ -632,6 +632,56 @@ __device__ __forceinline__ void kspace_fwd(const SysDev& S, const uint32_t Ua_in
         w0r = cs;
         w0i = -sn;
     }
+    if (NS == 3 && !GRAD && S.k_mirror) {
+        // sites 1 and 2 mirror each other through site 0 with equal charges: d_2 = -d_1 exactly,
+        // so D_2 = conj(D_1) and H = q_tot + 2 q_1 Re D_1 is real; part += Re[T] H.  Half the
+        // work per k-vector of the general loop below (which gives the same sum up to rounding)
+        const float q2 = 2.0f * qg[1];
+        float sn, cs;
+        sincospif(static_cast<float>(dc[1]) * (0.5f * kTurn), &sn, &cs);  // half angle
+        const float dwr = -2.0f * sn * sn, dwi = -2.0f * sn * cs;
+        const float wdr = __fadd_rn(1.0f, dwr);
+        for (int row = row0; row < S.n_krow; row += row_step) {
+            const KRow R = S.krow[row];
+            const float sgn = static_cast<float>(R.dir);
+            float er, ei;
+            {
+                const uint32_t P = static_cast<uint32_t>(R.ka) * Ua[0] + static_cast<uint32_t>(R.kb) * Ub[0] +
+                                   static_cast<uint32_t>(R.kc0) * Uc[0];
+                float s0, c0;
+                sincospif(static_cast<float>(static_cast<int32_t>(P)) * kTurn, &s0, &c0);
+                er = c0;
+                ei = -s0;
+            }
+            float Dr, Di;
+            {
+                const uint32_t p = static_cast<uint32_t>(R.ka) * static_cast<uint32_t>(da[1]) +
+                                   static_cast<uint32_t>(R.kb) * static_cast<uint32_t>(db[1]) +
+                                   static_cast<uint32_t>(R.kc0) * static_cast<uint32_t>(dc[1]);
+                float s1, c1;
+                sincospif(static_cast<float>(static_cast<int32_t>(p)) * (0.5f * kTurn), &s1, &c1);
+                Dr = -2.0f * s1 * s1;
+                Di = -2.0f * s1 * c1;
+            }
+            const float sw0i = sgn * w0i, swdi = sgn * dwi;
+            float part = 0.0f;
+            const float2* sw = S.skw + R.off;
+            for (int m = 0; m < R.n; ++m) {
+                const float2 w = __ldg(sw + m);
+                const float hr = fmaf(q2, Dr, qtot);
+                const float tr = fmaf(w.x, er, -w.y * ei);
+                part = fmaf(tr, hr, part);
+                const float nr = fmaf(er, w0r, -ei * sw0i);
+                ei = fmaf(er, sw0i, ei * w0r);
+                er = nr;
+                const float dr2 = fmaf(Dr, wdr, fmaf(-Di, swdi, dwr));
+                Di = fmaf(Dr, swdi, fmaf(Di, wdr, swdi));
+                Dr = dr2;
+            }
+            two_sum_acc(plr_hi, plr_lo, part);
+        }
+        return;
+    }
     float wdr[NS], wdi[NS], dwr[NS], dwi[NS];
 #pragma unroll
     for (int k = 1; k < NS; ++k) {

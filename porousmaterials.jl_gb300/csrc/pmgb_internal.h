@@ -98,6 +98,10 @@ struct SysDev {
     // k_d is a multiple of the replication factor n_d, and only those k-vectors are kept;
     // rows then hold k / ks and the kernels evaluate them at the coordinates ks_d u_d
     int ks[3];
+    // 1: three sites, site 0 at the centre of mass and sites 1 and 2 its mirror images through it
+    // with equal charges (CO2): their fixed-point offsets from site 0 are exact negatives, so the
+    // reciprocal-space sum needs the phase factor of site 1 only
+    int k_mirror;
     // FP64 copies: guest poses are composed in FP64, and the Boltzmann-tail refinement
     // re-evaluates selected insertions entirely in FP64
     double f2c64[6];                        // f_to_c, upper triangular (00 01 02 11 12 22)

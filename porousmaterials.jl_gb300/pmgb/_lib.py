@@ -62,6 +62,7 @@ SIGNATURES = [
     ("pmgb_system_image_lists", C.c_int, [_vp, C.c_int64, _ip]),
     ("pmgb_system_set_centre_image", C.c_int, [_vp, C.c_int32]),
     ("pmgb_system_centre_image", C.c_int, [_vp, C.POINTER(C.c_int32)]),
+    ("pmgb_system_kspace_mirror", C.c_int, [_vp, C.POINTER(C.c_int32)]),
     ("pmgb_system_set_accessibility", C.c_int, [_vp, _ip, _ip, C.POINTER(C.c_uint8)]),
     ("pmgb_system_set_refine", C.c_int, [_vp, C.c_double]),
     ("pmgb_system_set_exact", C.c_int, [_vp, C.c_int32]),

@@ -218,6 +218,8 @@ class GPUSystem:
         on = C.c_int32()
         self.ctx.check(self.ctx._lib.pmgb_system_centre_image(self.handle, C.byref(on)))
         info["centre_image"] = bool(on.value)  # Widom distances from the pose centre (set_centre_image)
+        self.ctx.check(self.ctx._lib.pmgb_system_kspace_mirror(self.handle, C.byref(on)))
+        info["kspace_mirror"] = bool(on.value)  # sites 1, 2 mirror images through site 0 (CO2)
         return info
 
     # -- evaluation ----------------------------------------------------------------------
