@@ -239,15 +239,17 @@ int pmgb_system_set_centre_image(pmgb_system* sys, int32_t on);
 
 /* Image lists for the spatially ordered Widom pass (no reference counterpart).  mode 0: off;
  * 1 (the default): where the run's insertions are dense enough that a CTA's list is expected to
- * hold under 60% of the records; 2: always where they apply.  They apply where culling is on, the
+ * hold under 90% of the records and the run fills the GPU (at least two CTAs of 256 insertions
+ * per SM), or, in a batch, under 140% of the records; 2: always where they apply.  They apply where culling is on, the
  * guest has one or three sites and every perpendicular width exceeds twice the larger cutoff.  The
  * insertions of a run are sorted once by position; each CTA (256 insertions) gathers the periodic
  * images of the framework records within (cutoff + the spread of its guest sites) of its sites'
  * centre, as double-float Cartesian offsets, into a shared-memory list, and its lanes take
  * distances from that list (pairs closer than 4 A with the offsets' residuals).  The energies are
- * the per-site form's to FP32 rounding, with the same error bound against FP64.  A batch takes
- * image lists for its systems that qualify, over the same insertion order, so its results equal
- * the single-system runs'. */
+ * the per-site form's to FP32 rounding, with the same error bound against FP64.  A batch runs
+ * its systems that take image lists over the same insertion order as a single-system run, so its
+ * results equal those of single-system runs that take the same form (mode 0 or 2 on both sides;
+ * in mode 1 the batch's bar is higher). */
 int pmgb_system_set_image_lists(pmgb_system* sys, int32_t mode);
 
 /* *on_out = 1 when a forward Widom run of n_insertions insertions of this system takes image

@@ -2103,11 +2103,13 @@ extern "C" int pmgb_system_set_image_lists(pmgb_system* s, int32_t mode) {
 // Whether the spatially ordered forward Widom pass of a run of n insertions takes image lists: a
 // guest form the kernels instantiate, every perpendicular width above twice the larger cutoff (at
 // most one image of a record within the cutoff of a site; the replication factors guarantee it for
-// the LJ cutoff), and (auto) a CTA's list expected to hold under 60% of the records.  The CTA's
-// 256 insertions, in the run's Z order, occupy about 256 V / n of the cell: a region of radius
-// ~1.6 (3 256 V / (4 pi n))^(1/3) (the factor for the order's elongated chunks, from simulated
-// orders of the config1, config3 and config4 shapes); its list holds the images within
-// cutoff + guest reach + that radius of the centre.
+// the LJ cutoff), and (auto) a CTA's list expected to be short enough to pay.  The CTA's 256
+// insertions, consecutive along the run's Hilbert order, occupy about 256 V / n of the cell: a
+// region of radius ~1.6 (3 256 V / (4 pi n))^(1/3) (from simulated orders of the config1, config3
+// and config4 shapes); its list holds the images within cutoff + guest reach + that radius of the
+// centre.  Measured on GB300: a run of one system gains below ~0.9 of the records when it fills
+// the GPU (two CTAs per SM; a smaller grid leaves the list building exposed), a batch, which fills
+// the GPU with many systems, below ~1.4.
 static bool image_lists_fit(const pmgb_system* s, int mode) {
     if (mode == 0 || !pmgb_img_supported(s->dev.n_sites)) return false;
     const double rc2 = std::max<double>(s->dev.rc2, s->dev.charged ? s->dev.rc2e : 0.0);
@@ -2118,7 +2120,7 @@ static bool image_lists_fit(const pmgb_system* s, int mode) {
     return true;
 }
 
-static bool image_lists_for(const pmgb_system* s, int64_t n_insertions) {
+static bool image_lists_for(const pmgb_system* s, int64_t n_insertions, bool in_batch) {
     if (!image_lists_fit(s, s->image_lists)) return false;
     if (s->image_lists == 2) return true;
     const double pi = 3.14159265358979323846;
@@ -2126,11 +2128,14 @@ static bool image_lists_for(const pmgb_system* s, int64_t n_insertions) {
     const double r_cta = 1.6 * std::cbrt(3.0 * PMGB_THREADS * vol / (4.0 * pi * std::max<int64_t>(n_insertions, 1)));
     const double rc = std::sqrt(std::max<double>(s->dev.rc2, s->dev.charged ? s->dev.rc2e : 0.0));
     const double reach = rc + s->dev.com_reach + r_cta;
-    return 4.0 / 3.0 * pi * reach * reach * reach < 0.6 * vol;
+    const double list = 4.0 / 3.0 * pi * reach * reach * reach / vol;  // expected list / records
+    if (in_batch) return list < 1.4;
+    const int64_t n_ctas = (n_insertions + PMGB_THREADS - 1) / PMGB_THREADS;
+    return list < 0.9 && n_ctas >= 2 * static_cast<int64_t>(sm_count(s->ctx));
 }
 
 static bool uses_image_lists(const pmgb_system* s, int64_t n_insertions) {
-    return s->cull && image_lists_for(s, n_insertions);
+    return s->cull && image_lists_for(s, n_insertions, false);
 }
 
 extern "C" int pmgb_system_image_lists(const pmgb_system* s, int64_t n_insertions, int32_t* on_out) {
@@ -3012,7 +3017,7 @@ int batch_capture(pmgb_batch* b) {
     bool any_img = false, changed = false;
     for (size_t i = 0; i < b->systems.size(); ++i) {
         const int img = (!b->grad && b->cull &&
-                         image_lists_for(b->systems[i], b->host_sys[i].n_per_block * b->n_blocks)) ? 1 : 0;
+                         image_lists_for(b->systems[i], b->host_sys[i].n_per_block * b->n_blocks, true)) ? 1 : 0;
         changed = changed || b->host_sys[i].img != img;
         b->host_sys[i].img = img;
         any_img = any_img || img;

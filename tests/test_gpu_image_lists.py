@@ -99,8 +99,8 @@ def test_image_list_energies_and_kh(case, npb):
 
 def test_image_lists_modes():
     """Off, on wherever they apply, and auto: by the run's insertion density (a CTA's list expected
-    under 60% of the records) -- the 1e6-insertion config1 run takes them, a 1e4-insertion run of
-    the same cell does not."""
+    under 90% of the records, in a run of at least two CTAs per SM) -- the 1e6-insertion config1
+    run takes them, a 1e4-insertion run of the same cell does not."""
     gs = _system("co2_dense")
     assert gs.image_lists(1000)          # on (set by _system)
     gs.set_cull(False)                   # no spatial order: the per-site pass
