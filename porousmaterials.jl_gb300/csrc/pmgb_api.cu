@@ -2384,7 +2384,20 @@ extern "C" int pmgb_widom_adjoint(pmgb_system* s, int64_t n_per_block, int32_t n
     a.dsum_stride = n;
     a.grad_u = grad_out ? static_cast<float*>(s->g_grad.p) : nullptr;
     double* d_block = static_cast<double*>(s->block_out.p);
-    if (s->cull) {  // spatially ordered, block sums from the energies in insertion order
+    if (!grad_out && uses_image_lists(s, n)) {
+        // the forward pass's image lists, with the columns (no forces requested): one spatial
+        // order over the whole run, block sums from the energies in insertion order
+        if (n > INT32_MAX) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_adjoint: too many insertions for one run");
+        const long long n_cells = 1ll << (3 * pmgb_run_order_bits(static_cast<long long>(n)));
+        if ((rc = ensure(ctx, s->o_counts, sizeof(int) * n_cells)) || (rc = ensure(ctx, s->o_perm, sizeof(int) * n)))
+            return rc;
+        a.perm = static_cast<const int*>(s->o_perm.p);
+        PMGB_CK(ctx, pmgb_launch_run_order(seed, static_cast<long long>(n), static_cast<int*>(s->o_counts.p),
+                                           static_cast<int*>(s->o_perm.p), ctx->stream));
+        PMGB_CK(ctx, pmgb_launch_pairs_img(a, n_ctas, ctx->stream));
+        PMGB_CK(ctx, pmgb_launch_lse_from_u(a.u_out, n_per_block, n_blocks, a.ctas_per_block, a.inv_temperature,
+                                            a.partials, ctx->stream));
+    } else if (s->cull) {  // spatially ordered, block sums from the energies in insertion order
         if ((rc = ensure(ctx, s->o_counts, sizeof(int) * pmgb_widom_order_cells() * n_blocks)) ||
             (rc = ensure(ctx, s->o_perm, sizeof(int) * n)))
             return rc;

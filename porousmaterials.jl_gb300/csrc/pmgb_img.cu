@@ -61,7 +61,7 @@ __global__ void run_order_sort_kernel(const int* offsets, int n_cells, int* perm
     }
 }
 
-template <int NS, bool CHARGED, bool STATS>
+template <int NS, bool CHARGED, bool STATS, bool COLS>
 __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_img_kernel(const __grid_constant__ LaunchArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
 
@@ -77,16 +77,21 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) pairs_img_kernel(const __grid
     io.seed = a.seed;
     io.u_out = a.u_out;
     io.stats = a.stats;
-    img_unit<NS, CHARGED, STATS>(a.sys, io, smem_raw);
+    if (COLS) {
+        io.dsum = a.dsum;
+        io.dsum_stride = a.dsum_stride;
+        io.col_item = io.item;
+    }
+    img_unit<NS, CHARGED, STATS, COLS>(a.sys, io, smem_raw);
 }
 
-template <int NS, bool CH, bool STATS>
+template <int NS, bool CH, bool STATS, bool COLS = false>
 cudaError_t launch_img(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
     const size_t smem = pmgb_img_smem_bytes();
-    cudaError_t e = cudaFuncSetAttribute(pairs_img_kernel<NS, CH, STATS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
+    cudaError_t e = cudaFuncSetAttribute(pairs_img_kernel<NS, CH, STATS, COLS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    pairs_img_kernel<NS, CH, STATS><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
+    pairs_img_kernel<NS, CH, STATS, COLS><<<n_ctas, PMGB_THREADS, smem, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -123,6 +128,14 @@ cudaError_t pmgb_launch_pairs_img(const LaunchArgs& a, int n_ctas, cudaStream_t 
     if (n_ctas <= 0) return cudaSuccess;
     if (!a.perm || !a.u_out || a.pose_mode != POSE_PHILOX) return cudaErrorInvalidValue;
     const bool stats = a.stats != nullptr;
+    if (a.dsum) {  // the adjoint's columns (no work counting)
+        if (stats) return cudaErrorInvalidValue;
+        if (a.sys.n_sites == 1)
+            return a.sys.charged ? launch_img<1, true, false, true>(a, n_ctas, st) : launch_img<1, false, false, true>(a, n_ctas, st);
+        if (a.sys.n_sites == 3)
+            return a.sys.charged ? launch_img<3, true, false, true>(a, n_ctas, st) : launch_img<3, false, false, true>(a, n_ctas, st);
+        return cudaErrorNotSupported;
+    }
     if (a.sys.n_sites == 1) {
         if (a.sys.charged) return stats ? launch_img<1, true, true>(a, n_ctas, st) : launch_img<1, true, false>(a, n_ctas, st);
         return stats ? launch_img<1, false, true>(a, n_ctas, st) : launch_img<1, false, false>(a, n_ctas, st);

@@ -141,7 +141,9 @@ __device__ __forceinline__ void cart_df(const SysDev& S, const int d[3], const i
 // One Widom insertion per thread; the CTA builds one list for its 256 insertions (the records
 // are read once per CTA, each thread taking one record per pass) and every warp evaluates its
 // lanes against it.  smem: kImgSmemBytes (list, the threads' site residuals, scratch).
-template <int NS, bool CHARGED, bool STATS>
+// COLS: also the adjoint's columns, per (species segment, site) the sums of r^-12 and r^-6 within
+// the LJ cutoff, into io.dsum[((sg NS + k) 2 + {0, 1}) io.dsum_stride + io.col_item].
+template <int NS, bool CHARGED, bool STATS, bool COLS = false>
 __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsigned char* smem) {
     static_assert(NS <= 3, "site residuals are kept for three sites");
     const unsigned full = 0xffffffffu;
@@ -271,12 +273,14 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
         for (int sg = 0; sg < S.n_seg; ++sg) {
             const SegDesc dsc = S.seg[sg];
             float segmin[NS], lj12[NS], lj6[NS];
+            float2 i12[NS], i6[NS];  // COLS: the segment's column sums
 #pragma unroll
             for (int k = 0; k < NS; ++k) {
                 const SitePar p = S.segpar[sg * PMGB_MAX_SITES + k];
                 lj12[k] = p.lj12;
                 lj6[k] = p.lj6;
                 segmin[k] = __int_as_float(0x7f800000);
+                i12[k] = i6[k] = f2(0.0f);
             }
             int n = 0;  // images in the list (the same in every thread)
             // evaluate the list (padded to whole groups of four) in every warp, and empty it
@@ -363,8 +367,8 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
 #pragma unroll
                             for (int k = 0; k < NS; ++k) {
                                 const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
-                                pair2_energy<CHARGED>(d01[k], B0.z, B0.w, g2, a12, a6, ljp2[k], php2[k]);
-                                pair2_energy<CHARGED>(d23[k], B1.z, B1.w, g2, a12, a6, ljp2[k], php2[k]);
+                                pair2_energy<CHARGED, COLS>(d01[k], B0.z, B0.w, g2, a12, a6, ljp2[k], php2[k], &i12[k], &i6[k]);
+                                pair2_energy<CHARGED, COLS>(d23[k], B1.z, B1.w, g2, a12, a6, ljp2[k], php2[k], &i12[k], &i6[k]);
                             }
                         } else {
                             const bool first = flags & 1u;
@@ -372,7 +376,8 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
 #pragma unroll
                             for (int k = 0; k < NS; ++k) {
                                 const float2 a12 = f2(lj12[k]), a6 = f2(lj6[k]);
-                                pair2_energy<CHARGED>(first ? d01[k] : d23[k], qa, qb, g2, a12, a6, ljp2[k], php2[k]);
+                                pair2_energy<CHARGED, COLS>(first ? d01[k] : d23[k], qa, qb, g2, a12, a6, ljp2[k], php2[k],
+                                                            &i12[k], &i6[k]);
                             }
                         }
                     }
@@ -468,6 +473,14 @@ __device__ __forceinline__ void img_unit(const SysDev& S, const UnitIO& io, unsi
                 __syncthreads();  // the pass's images are written; sc.wsum may be reused
             }
             if (n > 0) flush();
+            if (COLS && valid) {
+#pragma unroll
+                for (int k = 0; k < NS; ++k) {
+                    float* c12 = io.dsum + static_cast<size_t>((sg * NS + k) * 2) * io.dsum_stride + io.col_item;
+                    c12[0] = __fadd_rn(i12[k].x, i12[k].y);
+                    c12[io.dsum_stride] = __fadd_rn(i6[k].x, i6[k].y);
+                }
+            }
 #pragma unroll
             for (int k = 0; k < NS; ++k)  // the overlap radii read again: no registers held over the loop
                 ovl = ovl || (k < S.n_sites && segmin[k] < __ldg(&S.segpar[sg * PMGB_MAX_SITES + k].r2ovl));

@@ -132,6 +132,40 @@ def test_adjoint_without_forces(mol):
     gs.set_centre_image(True)
 
 
+@pytest.mark.parametrize("mol", ["co2", "ch4"])
+def test_adjoint_with_image_lists(mol):
+    """Without forces, a run that takes image lists forms the columns in the image-list pass: its
+    energies and block results are the forward image-list pass's bit for bit, and its dK_H/d(eps,
+    sigma, charge scale) agree with the per-site pass that also forms dU/dx to the gradient
+    tolerance (the two passes' FP32 energies and columns differ by rounding)."""
+    from pmgb.adjoint import henry_gradients
+
+    ff = synthetic.forcefield()
+    cr = synthetic.config1_porous()
+    sc = pmgb.replicate(cr, pmgb.replication_factors(cr.box, ff))
+    charged = mol == "co2"
+    ep = pmgb.setup_Ewald_sum(sc.box, ff.r_cutoff, eps=1e-6) if charged else None
+    gs = pmgb.GPUSystem(sc, pmgb.Frac(getattr(synthetic, mol)(), sc.box), ff, ep)
+    npb, seed = 3000, 14
+    gs.set_image_lists(False)
+    b1, a1 = gs.widom_adjoint(npb, 5, seed, T, want_energies=True, want_grad=True)  # per site, forces
+    g1 = henry_gradients(gs, b1, a1, T, npb)
+    gs.set_image_lists(True)
+    assert gs.image_lists(5 * npb)
+    fwd, u_fwd = gs.widom(npb, 5, seed, T, want_energies=True)
+    b0, a0 = gs.widom_adjoint(npb, 5, seed, T, want_energies=True)  # columns from the lists
+    np.testing.assert_array_equal(a0["u"], u_fwd)
+    np.testing.assert_array_equal(b0, fwd)
+    g0 = henry_gradients(gs, b0, a0, T, npb)
+    for x, y in zip(g0[:2], g1[:2]):
+        scale = max(abs(v) for v in y.values())
+        for sp in y:
+            assert x[sp] == pytest.approx(y[sp], rel=1e-4, abs=1e-7 * scale), sp
+    if charged:
+        assert g0[2] == pytest.approx(g1[2], rel=1e-4)
+    assert gs.ctx.device_status() == 0
+
+
 def test_dkh_lj():
     gs = _system(synthetic.config0(), synthetic.ch4(), synthetic.forcefield(), charged=False)
     _check_dkh(gs, 2000, seed=31, charged=False)
