@@ -66,6 +66,10 @@ struct pmgb_ctx {
     // stream has drained
     char* stage = nullptr;
     size_t stage_cap = 0, stage_used = 0;
+    // pinned landing buffer of the structure factors read back by the unit-cell set-up (grow-only;
+    // every call synchronises before it returns, so the next may reuse it)
+    double* sk_host = nullptr;
+    size_t sk_host_cap = 0;
     // optional CUDA events around the Widom passes' pair-kernel launches (pmgb_set_kernel_timing)
     bool timing = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timing_events;
@@ -417,6 +421,7 @@ static void ctx_release(pmgb_ctx* ctx) {
     }
     cudaStreamSynchronize(ctx->stream);
     if (ctx->stage) cudaFreeHost(ctx->stage);
+    if (ctx->sk_host) cudaFreeHost(ctx->sk_host);
     if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -1585,14 +1590,20 @@ extern "C" int pmgb_systems_create_unitcell(pmgb_ctx* ctx, int32_t n_systems, co
         }
     double* sk = nullptr;  // pinned: the S(k) copies do not wait on one another
     if (sk_total > 0) {
-        e = cudaMallocHost(reinterpret_cast<void**>(&sk), sizeof(double) * sk_total);
-        if (e != cudaSuccess) return give_up(cuda_fail(ctx, e, "cudaMallocHost"));
+        if (ctx->sk_host_cap < sk_total) {
+            if (ctx->sk_host) cudaFreeHost(ctx->sk_host);
+            ctx->sk_host = nullptr;
+            ctx->sk_host_cap = 0;
+            size_t cap = 4096;
+            while (cap < sk_total) cap <<= 1;
+            e = cudaMallocHost(reinterpret_cast<void**>(&ctx->sk_host), sizeof(double) * cap);
+            if (e != cudaSuccess) return give_up(cuda_fail(ctx, e, "cudaMallocHost"));
+            ctx->sk_host_cap = cap;
+        }
+        sk = ctx->sk_host;
     }
     auto finish = [&](int rc) {
-        if (sk) {
-            cudaStreamSynchronize(ctx->stream);
-            cudaFreeHost(sk);
-        }
+        if (sk) cudaStreamSynchronize(ctx->stream);  // the copies into the landing buffer are done
         return rc == PMGB_OK ? rc : give_up(rc);
     };
     for (int i = 0; i < n_systems; ++i) {
