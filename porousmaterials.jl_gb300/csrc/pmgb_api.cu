@@ -3037,10 +3037,11 @@ int batch_capture(pmgb_batch* b) {
         cudaGraphExecDestroy(b->exec);
         b->exec = nullptr;
     }
-    // image lists for the systems that allow them, in forward runs with spatial order
+    // image lists for the systems that allow them, in runs with spatial order (the adjoint's
+    // columns formed in the list loop)
     bool any_img = false, changed = false;
     for (size_t i = 0; i < b->systems.size(); ++i) {
-        const int img = (!b->grad && b->cull &&
+        const int img = (b->cull &&
                          image_lists_for(b->systems[i], b->host_sys[i].n_per_block * b->n_blocks, true)) ? 1 : 0;
         changed = changed || b->host_sys[i].img != img;
         b->host_sys[i].img = img;

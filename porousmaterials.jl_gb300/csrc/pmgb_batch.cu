@@ -65,21 +65,23 @@ __device__ __forceinline__ bool run_variant(int variant, bool no_resid, bool com
     return run_variant_r<GRAD, true>(variant, comp, S, io, stage, bars, red, fills, status);
 }
 
-// image-list units of a forward run with refinement (csrc/pmgb_img.cuh), one function per variant
-template <int NS, bool CHARGED>
+// image-list units (csrc/pmgb_img.cuh), one function per variant; COLS: with the adjoint's
+// columns (the forward runs have none)
+template <int NS, bool CHARGED, bool COLS>
 __device__ __noinline__ void img_unit_fn(const SysDev& S, const UnitIO& io, unsigned char* smem) {
-    img_unit<NS, CHARGED, false>(S, io, smem);
+    img_unit<NS, CHARGED, false, COLS>(S, io, smem);
 }
 
 // the list takes the TMA ring's shared memory (idle here: every copy a unit issues is consumed
 // inside that unit)
+template <bool COLS>
 __device__ __forceinline__ void run_img(const SysDev& S, const UnitIO& io, unsigned char* smem) {
     if (S.n_sites == 1) {
-        if (S.charged) img_unit_fn<1, true>(S, io, smem);
-        else img_unit_fn<1, false>(S, io, smem);
+        if (S.charged) img_unit_fn<1, true, COLS>(S, io, smem);
+        else img_unit_fn<1, false, COLS>(S, io, smem);
     } else {
-        if (S.charged) img_unit_fn<3, true>(S, io, smem);
-        else img_unit_fn<3, false>(S, io, smem);
+        if (S.charged) img_unit_fn<3, true, COLS>(S, io, smem);
+        else img_unit_fn<3, false, COLS>(S, io, smem);
     }
 }
 
@@ -130,31 +132,42 @@ __global__ void __launch_bounds__(PMGB_THREADS, 2) batch_kernel(const __grid_con
             long long within = slot_in_block;
             if (b.perm && io.valid)
                 within = b.perm[s_bs.u_base + static_cast<long long>(unit.block) * npb + slot_in_block];
-            if (!GRAD && s_bs.img) {
+            double x = -inf;  // GRAD: this thread's -U/T
+            if (s_bs.img) {
                 // one order over the system's whole run: perm holds the system's insertion index
                 io.item = io.valid ? within : 0;
                 io.seed = run.seed + static_cast<unsigned long long>(unit.system) * 0x9E3779B97F4A7C15ull;
                 io.u_out = b.u + 2 * s_bs.u_base;
-                run_img(s_bs.sys, io, smem_raw);
-                continue;
+                if (!GRAD) {
+                    run_img<false>(s_bs.sys, io, smem_raw);
+                    continue;
+                }
+                io.dsum = my_dsum;
+                io.dsum_stride = PMGB_THREADS;
+                io.col_item = tid;
+                run_img<true>(s_bs.sys, io, smem_raw);
+                if (io.valid) {  // the unit wrote this thread's energies; -U/T as run_unit forms it
+                    const double uu = io.u_out[2 * io.item] + io.u_out[2 * io.item + 1];
+                    if (isfinite(uu)) x = -uu * run.inv_temperature;
+                }
+            } else {
+                io.item = static_cast<long long>(unit.block) * npb + within;
+                io.cull = b.perm != nullptr;
+                io.seed = run.seed + static_cast<unsigned long long>(unit.system) * 0x9E3779B97F4A7C15ull;
+                io.inv_temperature = run.inv_temperature;
+                io.dsum = my_dsum;
+                io.dsum_stride = PMGB_THREADS;
+                io.col_item = tid;
+                io.partial = b.perm ? nullptr : b.partials + slot;
+                io.u_out = b.u ? b.u + 2 * s_bs.u_base : nullptr;
+                io.resident = fits && c > 0;
+                io.x_out = &x;
+                io.m_out = &s_m;
+                const bool comp = s_bs.sys.com_axis >= -1 && s_bs.sys.n_sites > 1;
+                if (!run_variant<GRAD>(s_bs.variant, b.no_resid != 0, comp, s_bs.sys, io, stage, bars, red, fills,
+                                       b.status))
+                    return;
             }
-            io.item = static_cast<long long>(unit.block) * npb + within;
-            io.cull = b.perm != nullptr;
-            io.seed = run.seed + static_cast<unsigned long long>(unit.system) * 0x9E3779B97F4A7C15ull;
-            io.inv_temperature = run.inv_temperature;
-            io.dsum = my_dsum;
-            io.dsum_stride = PMGB_THREADS;
-            io.col_item = tid;
-            io.partial = b.perm ? nullptr : b.partials + slot;
-            io.u_out = b.u ? b.u + 2 * s_bs.u_base : nullptr;
-            io.resident = fits && c > 0;
-            double x = -inf;
-            io.x_out = &x;
-            io.m_out = &s_m;
-            const bool comp = s_bs.sys.com_axis >= -1 && s_bs.sys.n_sites > 1;
-            if (!run_variant<GRAD>(s_bs.variant, b.no_resid != 0, comp, s_bs.sys, io, stage, bars, red, fills,
-                                   b.status))
-                return;
             if (GRAD) {
                 if (b.perm) {
                     // this processing chunk's own max of -U/T (the partials come from u later)

@@ -230,6 +230,35 @@ def test_batch_image_lists_match_single_system(mixed_systems):
     assert mixed_systems[0].ctx.device_status() == 0
 
 
+def test_batch_image_lists_adjoint_match_single_system(mixed_systems):
+    """The adjoint with image lists: the batch's units form the columns in the list loop and weigh
+    them per processing chunk; block results equal the single-system adjoint's (which takes the
+    lists too: no forces) bit for bit, gradients to 1e-9 relative (FP64 sums in another order)."""
+    npb, seed = [1 + 173 * i for i in range(len(mixed_systems))], 61
+    for gs in mixed_systems:
+        gs.set_image_lists(True)
+    screen = BatchScreen(mixed_systems, npb, 5, with_adjoint=True)
+    try:
+        for n_ctas, order, mflop in ((0, 0, 0.0), (5, 1, 64.0)):
+            screen.configure(n_ctas, order, mflop)
+            blocks, adj = screen.run(seed, T)
+            for s, gs in enumerate(mixed_systems):
+                ref_b, ref_a = gs.widom_adjoint(npb[s], 5, system_seed(seed, s), T)
+                np.testing.assert_array_equal(blocks[s], ref_b)
+                got = henry_gradients(gs, blocks[s], adj[s], T, npb[s])
+                want = henry_gradients(gs, ref_b, ref_a, T, npb[s])
+                for g, w in zip(got[:2], want[:2]):
+                    scale = max(abs(v) for v in w.values())
+                    for sp in w:
+                        assert g[sp] == pytest.approx(w[sp], rel=1e-9, abs=1e-12 * scale), (s, sp)
+                assert got[2] == pytest.approx(want[2], rel=1e-9, abs=1e-12 * abs(want[2]) + 1e-300)
+    finally:
+        for gs in mixed_systems:
+            gs.set_image_lists("auto")
+        screen.close()
+    assert mixed_systems[0].ctx.device_status() == 0
+
+
 @pytest.mark.parametrize("unit_mflop", [0.0, 64.0])
 def test_batch_cull_adjoint(mixed_systems, unit_mflop):
     """With culling, the adjoint's columns are weighted relative to each processing chunk's own
