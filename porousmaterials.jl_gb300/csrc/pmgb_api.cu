@@ -2364,8 +2364,11 @@ extern "C" int pmgb_widom_adjoint(pmgb_system* s, int64_t n_per_block, int32_t n
     if (!(temperature > 0.0) || !std::isfinite(temperature))
         return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_adjoint: temperature must be positive");
     if (int rc = ready_for_charges(s)) return rc;
+    // compare before multiplying: n_per_block near INT64_MAX must not wrap the CTA count
+    if (n_per_block > static_cast<int64_t>(INT32_MAX) * PMGB_THREADS)
+        return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_adjoint: too many insertions per block");
     const int64_t cpb = (n_per_block + PMGB_THREADS - 1) / PMGB_THREADS;
-    if (cpb * n_blocks > INT32_MAX) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_adjoint: too many insertions");
+    if (cpb > INT32_MAX / n_blocks) return fail(ctx, PMGB_ERR_INVALID_ARGUMENT, "pmgb_widom_adjoint: too many insertions");
     const int nst = template_sites(s->n_sites);
     const int n_cols = static_cast<int>(s->seg_species.size()) * nst * 2;
     const int64_t n = n_per_block * n_blocks;
