@@ -1,11 +1,12 @@
 // pmgb_img.cu -- the image-list form of the spatially ordered Widom pass (sm_103a).
 //
-// The insertions of a run are sorted once over the whole run (all statistics blocks) by the
-// Z-order cell of their centre of mass, so the 32 lanes of a warp hold insertions that sit close
-// together.  Each warp then takes the centre c of its guest sites' bounding box and the largest
-// distance rho of a site from c, and gathers from the framework records (read from global memory,
-// L2-resident) every periodic image within R = r_cut + rho of c, as a Cartesian offset from c,
-// into its own shared-memory list.  Every lane evaluates its guest sites against that list: a
+// The insertions of a run are sorted once over the whole run (all statistics blocks) by the cell
+// of their centre of mass along a Hilbert curve, so the 256 insertions of a CTA (and the 32 lanes
+// of each of its warps) sit close together.  Each CTA takes the centre c of its guest sites'
+// bounding box and the largest distance rho of a site from c, and gathers from the framework
+// records (read from global memory, L2-resident; each thread takes one record per pass) every
+// periodic image within R = r_cut + rho of c, as a double-float Cartesian offset from c, into a
+// shared-memory list.  Every lane of every warp evaluates its guest sites against that list: a
 // distance is three subtractions and a dot product, with no integer wrap or conversion per site,
 // and records beyond R of every lane are never looked at.
 //
@@ -18,10 +19,10 @@
 // species segment), so it and every sum over it are deterministic; the sort orders the insertions
 // of a cell by index, so the warps' compositions are deterministic too.
 //
-// Precision: list offsets are FP32 values up to R (~15 A) from c, each within half an FP32 ulp of
-// the minimum-image offset composed with the box-matrix residual; this pass is used where the FP64
-// tail refinement follows (the insertions carrying the Boltzmann weight are re-evaluated from
-// exact positions), as the residual-free per-site pass is.
+// Precision: the list holds each offset's FP32 value and its FP32 residual (value + residual is
+// the minimum-image offset to ~1e-13 A); distances take the values, and pairs closer than 4 A add
+// the residuals' first-order term, so the energies keep the per-site pass's FP32 error bound
+// against FP64, with or without the FP64 tail refinement.
 #include "pmgb_img.cuh"
 
 namespace {
@@ -101,7 +102,7 @@ size_t pmgb_img_smem_bytes() { return kImgSmemBytes; }
 
 bool pmgb_img_supported(int n_sites) { return n_sites == 1 || n_sites == 3; }
 
-// Z-order cells per axis 2^bits: the fewest bits (3 to 6) that leave at most 32 insertions per cell
+// Cells per axis 2^bits: the fewest bits (3 to 6) that leave at most 32 insertions per cell
 // on average (a cell of a 1e6-insertion run in a 28,700 A^3 cell is ~0.9 A across; the order within
 // a cell is by index)
 int pmgb_run_order_bits(long long n) {
