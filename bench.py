@@ -1000,7 +1000,8 @@ def ours(args, rank, world, local_rank):
                "pair_kernel_frac_of_fp32_peak": achieved / fp32_peak if fp32_peak else None,
                "e2e_insertions_per_s": e2e["value"] if e2e else None,
                "cpu_direct_insertions_per_s": cpu["value"] if cpu else None,
-               "cpu_sk_form_insertions_per_s": cpu["sk_form"]["value"] if cpu else None}
+               "cpu_sk_form_insertions_per_s": cpu["sk_form"]["value"] if cpu else None,
+               "fwd_adj_insertions_per_s": adj["value"] if adj else None}
     if porous:
         summary.update({"porous_insertions_per_s": porous["insertions_per_s"],
                         "porous_refinement_share": porous["refinement_share_of_step"],
