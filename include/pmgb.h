@@ -256,6 +256,12 @@ int pmgb_system_set_image_lists(pmgb_system* sys, int32_t mode);
  * lists (the mode, culling, the guest, the widths and the density all allow it), else 0. */
 int pmgb_system_image_lists(const pmgb_system* sys, int64_t n_insertions, int32_t* on_out);
 
+/* Index of cell (x, y, z) of a grid of 2^bits cells per axis along the Hilbert curve that orders
+ * the insertions of the spatially ordered Widom runs (J. Skilling's construction); -1 when bits is
+ * outside 1..10 or a coordinate outside the grid.  Host-side, no device work: the code the order
+ * kernels run, for checks of the order.  No reference counterpart. */
+int pmgb_hilbert_cell(uint32_t x, uint32_t y, uint32_t z, int32_t bits);
+
 /* *on_out = 1 when Widom insertions of this system take the centre-image form (switched on, a
  * guest with several sites, and every width wide enough for the current cutoffs), else 0. */
 int pmgb_system_centre_image(const pmgb_system* sys, int32_t* on_out);

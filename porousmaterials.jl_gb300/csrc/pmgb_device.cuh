@@ -113,7 +113,7 @@ __device__ __forceinline__ float u24(uint32_t x) { return static_cast<float>(x >
 // straddle a jump across the cell.  J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc.
 // 707 (2004): the axes are turned into the transposed index (undo excess work, Gray encode),
 // whose bits are then interleaved.
-__device__ __forceinline__ int hilbert_cell(uint32_t cx, uint32_t cy, uint32_t cz, int bits) {
+__host__ __device__ __forceinline__ int hilbert_cell(uint32_t cx, uint32_t cy, uint32_t cz, int bits) {
     uint32_t x[3] = {cx, cy, cz};
     for (uint32_t q = 1u << (bits - 1); q > 1u; q >>= 1) {
         const uint32_t p = q - 1u;

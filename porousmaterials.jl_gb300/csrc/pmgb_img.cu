@@ -100,6 +100,11 @@ cudaError_t launch_img(const LaunchArgs& a, int n_ctas, cudaStream_t st) {
 
 size_t pmgb_img_smem_bytes() { return kImgSmemBytes; }
 
+extern "C" int pmgb_hilbert_cell(uint32_t x, uint32_t y, uint32_t z, int32_t bits) {
+    if (bits < 1 || bits > 10 || (x >> bits) || (y >> bits) || (z >> bits)) return -1;
+    return hilbert_cell(x, y, z, bits);
+}
+
 bool pmgb_img_supported(int n_sites) { return n_sites == 1 || n_sites == 3; }
 
 // Cells per axis 2^bits: the fewest bits (3 to 6) that leave at most 32 insertions per cell

@@ -60,6 +60,7 @@ SIGNATURES = [
     ("pmgb_system_set_cull", C.c_int, [_vp, C.c_int32]),
     ("pmgb_system_set_image_lists", C.c_int, [_vp, C.c_int32]),
     ("pmgb_system_image_lists", C.c_int, [_vp, C.c_int64, _ip]),
+    ("pmgb_hilbert_cell", C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32]),
     ("pmgb_system_set_centre_image", C.c_int, [_vp, C.c_int32]),
     ("pmgb_system_centre_image", C.c_int, [_vp, C.POINTER(C.c_int32)]),
     ("pmgb_system_kspace_mirror", C.c_int, [_vp, C.POINTER(C.c_int32)]),

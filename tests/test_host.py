@@ -261,3 +261,22 @@ def test_reference_grid_positions_replay_the_grid_loop():
         got = reference_grid_positions(n_pts, rep, atom0, com0, ids)
         want = np.array([seen[t] for t in ids])
         assert np.array_equal(got, want)
+
+
+def test_hilbert_order_of_the_runs():
+    """pmgb_hilbert_cell (the host build of the order kernels' hilbert_cell): for 2^3 to 2^6
+    cells per axis a bijection onto [0, 8^bits) along which consecutive cells share a face, so
+    that runs of consecutive insertions stay compact; out-of-range arguments are refused."""
+    L = _native()
+    for bits in (3, 4, 5, 6):
+        n = 1 << bits
+        cells = np.array(np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")).reshape(3, -1).T
+        codes = np.array([L.pmgb_hilbert_cell(int(x), int(y), int(z), bits) for x, y, z in cells])
+        assert codes.min() == 0 and codes.max() == n ** 3 - 1
+        order = np.full(n ** 3, -1)
+        order[codes] = np.arange(n ** 3)
+        assert (order >= 0).all()  # every index taken once
+        steps = np.abs(np.diff(cells[order], axis=0)).sum(axis=1)
+        assert (steps == 1).all()
+    assert L.pmgb_hilbert_cell(8, 0, 0, 3) == -1
+    assert L.pmgb_hilbert_cell(0, 0, 0, 0) == -1 and L.pmgb_hilbert_cell(0, 0, 0, 11) == -1
